@@ -1,0 +1,370 @@
+"""ctypes wrappers for the CPU oracle (oracle/liboracle.so) and for the
+reference compiled from its own sources (oracle/_ref/libref.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
+bench.py's CPU-baseline leg as the checker; the GB300 library never uses it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import shutil
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(HERE)
+sys.path.insert(0, os.path.join(REPO, "moribs-pimc_gb300"))
+from pimc_types import PimcSystem, PimcTables, dptr, iptr, make_system, make_tables  # noqa: E402
+
+LIB = os.path.join(HERE, "liboracle.so")
+REFLIB = os.path.join(HERE, "_ref", "libref.so")
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+
+
+def build_oracle(force=False):
+    """Compile oracle/pimc_oracle.c into oracle/liboracle.so (C11 + OpenMP)."""
+    src = os.path.join(HERE, "pimc_oracle.c")
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(src):
+        return LIB
+    cmd = ["gcc", "-std=gnu11", "-O2", "-fopenmp", "-fPIC", "-shared", src, "-o", LIB, "-lm"]
+    subprocess.check_call(cmd)
+    return LIB
+
+
+class Stream(C.Structure):
+    _fields_ = [("v", _dp), ("n", C.c_long), ("pos", C.c_long)]
+
+
+class Replay(C.Structure):
+    _fields_ = [("u1", Stream), ("u2", Stream), ("u3", Stream), ("gauss", Stream), ("urot", Stream),
+                ("overrun", C.c_int)]
+
+
+def make_replay(u1=None, u2=None, u3=None, gauss=None, urot=None):
+    keep = []
+    rp = Replay()
+    for name, a in (("u1", u1), ("u2", u2), ("u3", u3), ("gauss", gauss), ("urot", urot)):
+        st = getattr(rp, name)
+        if a is not None:
+            a = np.ascontiguousarray(a, dtype=np.float64)
+            keep.append(a)
+            st.v, st.n, st.pos = dptr(a), len(a), 0
+    return rp, keep
+
+
+def _lib():
+    build_oracle()
+    lib = C.CDLL(LIB)
+    lib.orc_create.restype = C.c_void_p
+    lib.orc_create.argtypes = [C.POINTER(PimcSystem), C.POINTER(PimcTables), _ip]
+    lib.orc_destroy.argtypes = [C.c_void_p]
+    for name in ("orc_spot1d",):
+        getattr(lib, name).restype = C.c_double
+        getattr(lib, name).argtypes = [C.c_void_p, C.c_double]
+    lib.orc_lpot2d.restype = C.c_double
+    lib.orc_lpot2d.argtypes = [C.c_void_p, C.c_double, C.c_double]
+    lib.orc_srotdens.restype = C.c_double
+    lib.orc_srotdens.argtypes = [C.c_void_p, C.c_double, C.c_int]
+    lib.orc_vspher.restype = C.c_double
+    lib.orc_vspher.argtypes = [C.c_void_p, C.c_double]
+    lib.orc_matpre.argtypes = [_dp, _dp]
+    lib.orc_deleul.argtypes = [_dp, _dp, _dp]
+    lib.orc_rotden.restype = C.c_int
+    lib.orc_rotden.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp, _dp, _dp]
+    lib.orc_vcord.restype = C.c_double
+    lib.orc_vcord.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp, _dp, _dp]
+    lib.orc_rsrot.argtypes = [_dp, _dp, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int, C.c_double, _dp, _dp]
+    lib.orc_rsline.argtypes = [C.c_double, C.c_double, C.c_double, _dp, _dp]
+    lib.orc_caleng.restype = C.c_double
+    lib.orc_caleng.argtypes = [_dp, _dp, _dp, _dp]
+    lib.orc_set_state.argtypes = [C.c_void_p, _dp, _dp, _ip]
+    lib.orc_get_state.argtypes = [C.c_void_p, _dp, _dp, _dp, _ip]
+    for name in ("orc_pot_energy_slice",):
+        getattr(lib, name).restype = C.c_double
+        getattr(lib, name).argtypes = [C.c_void_p, C.c_int, _dp, C.c_int]
+    lib.orc_pot_energy_path.restype = C.c_double
+    lib.orc_pot_energy_path.argtypes = [C.c_void_p, C.c_int, _dp]
+    lib.orc_pot_rot_energy.restype = C.c_double
+    lib.orc_pot_rot_energy.argtypes = [C.c_void_p, C.c_int, _dp, C.c_int]
+    lib.orc_pot_rot_e3d.restype = C.c_double
+    lib.orc_pot_rot_e3d.argtypes = [C.c_void_p, C.c_int, _dp, C.c_int]
+    for name in ("orc_molecular_move", "orc_molecular_move_exchange"):
+        getattr(lib, name).argtypes = [C.c_void_p, C.c_int, C.POINTER(Replay), _dp, _ip]
+    for name in ("orc_bisection_move", "orc_bisection_move_exchange"):
+        getattr(lib, name).argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(Replay), _dp, _ip]
+    for name in ("orc_rotations_move", "orc_rotations_3d"):
+        getattr(lib, name).argtypes = [C.c_void_p, C.c_int, C.POINTER(Replay), _dp, _ip]
+    for name in ("orc_rot_lin_step", "orc_rot_3d_step"):
+        getattr(lib, name).argtypes = [C.c_void_p, C.c_int, C.c_int, _dp, _dp, _ip]
+    lib.orc_get_counters.argtypes = [C.c_void_p, _dp, _dp]
+    lib.orc_reset_counters.argtypes = [C.c_void_p]
+    for name in ("orc_kin_energy", "orc_pot_energy_est"):
+        getattr(lib, name).restype = C.c_double
+        getattr(lib, name).argtypes = [C.c_void_p]
+    for name in ("orc_rot_energy", "orc_rot_e3d"):
+        getattr(lib, name).restype = C.c_double
+        getattr(lib, name).argtypes = [C.c_void_p, _dp, _dp]
+    lib.orc_rcf.argtypes = [C.c_void_p, _dp]
+    lib.orc_run_steps.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_uint64, C.c_int, _dp]
+    return lib
+
+
+_LIB = None
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        _LIB = _lib()
+    return _LIB
+
+
+def _v3(x):
+    a = np.ascontiguousarray(np.asarray(x, dtype=np.float64).reshape(3))
+    return a
+
+
+class Oracle:
+    """One oracle context over a Workload (owns copies of tables and state)."""
+
+    def __init__(self, w):
+        self.w = w
+        self.L = lib()
+        self.sys = make_system(w)
+        tabs, keep = make_tables(w)
+        st = C.c_int(0)
+        self.h = self.L.orc_create(C.byref(self.sys), C.byref(tabs), C.byref(st))
+        if not self.h:
+            raise RuntimeError("orc_create failed: %d" % st.value)
+        self.na = w.natoms
+        self.P = w.nslices
+        if w.coords is not None:
+            self.set_state(w.coords, w.angles, w.pindex)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.L.orc_destroy(self.h)
+            self.h = None
+
+    # state
+    def set_state(self, coords, angles=None, pindex=None):
+        c = np.ascontiguousarray(coords, dtype=np.float64)
+        a = None if angles is None else np.ascontiguousarray(angles, dtype=np.float64)
+        p = None if pindex is None else np.ascontiguousarray(pindex, dtype=np.int32)
+        self.L.orc_set_state(self.h, dptr(c), dptr(a) if a is not None else None, iptr(p) if p is not None else None)
+
+    def get_state(self):
+        nb = self.na * self.P
+        c = np.zeros((3, nb)); a = np.zeros((3, nb)); co = np.zeros((3, nb)); p = np.zeros(self.na, np.int32)
+        self.L.orc_get_state(self.h, dptr(c), dptr(a), dptr(co), iptr(p))
+        return c, a, co, p
+
+    # leaves
+    def spot1d(self, r): return self.L.orc_spot1d(self.h, float(r))
+    def lpot2d(self, r, c): return self.L.orc_lpot2d(self.h, float(r), float(c))
+    def srotdens(self, g, which=0): return self.L.orc_srotdens(self.h, float(g), int(which))
+    def vspher(self, r): return self.L.orc_vspher(self.h, float(r))
+
+    def rotden(self, e1, e2):
+        e1, e2 = _v3(e1), _v3(e2)
+        rel, rho, er, es = np.zeros(3), C.c_double(), C.c_double(), C.c_double()
+        st = self.L.orc_rotden(self.h, dptr(e1), dptr(e2), dptr(rel), C.byref(rho), C.byref(er), C.byref(es))
+        return st, rel, rho.value, er.value, es.value
+
+    def vcord(self, eul, rcom, rpt):
+        e, a, b = _v3(eul), _v3(rcom), _v3(rpt)
+        r, t, c = C.c_double(), C.c_double(), C.c_double()
+        v = self.L.orc_vcord(self.h, dptr(e), dptr(a), dptr(b), C.byref(r), C.byref(t), C.byref(c))
+        return v, r.value, t.value, c.value
+
+    # energies
+    def pot_energy_slice(self, atom0, pos, it):
+        p = np.ascontiguousarray(pos, dtype=np.float64)
+        return self.L.orc_pot_energy_slice(self.h, int(atom0), dptr(p), int(it))
+
+    def pot_energy_path(self, atom0, pos):
+        p = np.ascontiguousarray(pos, dtype=np.float64)
+        return self.L.orc_pot_energy_path(self.h, int(atom0), dptr(p))
+
+    def pot_rot_energy(self, atom0, cosine, it):
+        p = np.ascontiguousarray(cosine, dtype=np.float64)
+        return self.L.orc_pot_rot_energy(self.h, int(atom0), dptr(p), int(it))
+
+    def pot_rot_e3d(self, atom0, eul, it):
+        e = _v3(eul)
+        return self.L.orc_pot_rot_e3d(self.h, int(atom0), dptr(e), int(it))
+
+    # moves
+    def molecular_move(self, type_, u1, u2, exchange=False):
+        rp, keep = make_replay(u1=u1, u2=u2)
+        n = self.w.types[type_]["numb"]
+        dv = np.zeros(n); acc = np.zeros(n, np.int32)
+        fn = self.L.orc_molecular_move_exchange if exchange else self.L.orc_molecular_move
+        st = fn(self.h, type_, C.byref(rp), dptr(dv), iptr(acc))
+        return st, dv, acc, (rp.u1.pos, rp.u2.pos)
+
+    def bisection_move(self, type_, time, gauss, u3, exchange=False):
+        rp, keep = make_replay(u3=u3, gauss=gauss)
+        t = self.w.types[type_]
+        ds = np.zeros(t["numb"] * t["levels"]); lv = np.zeros(t["numb"], np.int32)
+        fn = self.L.orc_bisection_move_exchange if exchange else self.L.orc_bisection_move
+        st = fn(self.h, type_, int(time), C.byref(rp), dptr(ds), iptr(lv))
+        return st, ds.reshape(t["numb"], t["levels"]), lv, (rp.gauss.pos, rp.u3.pos)
+
+    def rotations(self, type_, urot):
+        rp, keep = make_replay(urot=urot)
+        t = self.w.types[type_]
+        n = self.w.nrotslices * t["numb"]
+        rd = np.zeros(n); acc = np.zeros(n, np.int32)
+        fn = self.L.orc_rotations_move if t["molecule"] == 1 else self.L.orc_rotations_3d
+        st = fn(self.h, type_, C.byref(rp), dptr(rd), iptr(acc))
+        return st, rd, acc, rp.urot.pos
+
+    def counters(self):
+        tot = np.zeros(6); acc = np.zeros(6)
+        self.L.orc_get_counters(self.h, dptr(tot), dptr(acc))
+        return tot, acc
+
+    # estimators
+    def kin_energy(self): return self.L.orc_kin_energy(self.h)
+    def pot_energy_est(self): return self.L.orc_pot_energy_est(self.h)
+
+    def rot_energy(self, nonlinear):
+        a, b = C.c_double(), C.c_double()
+        fn = self.L.orc_rot_e3d if nonlinear else self.L.orc_rot_energy
+        s = fn(self.h, C.byref(a), C.byref(b))
+        return s, a.value, b.value
+
+    def rcf(self):
+        r = np.zeros(self.w.nrotslices)
+        self.L.orc_rcf(self.h, dptr(r))
+        return r
+
+    def run_steps(self, t_begin, t_count, seed, nthreads=1):
+        bm = C.c_double()
+        st = self.L.orc_run_steps(self.h, int(t_begin), int(t_count), C.c_uint64(seed), int(nthreads), C.byref(bm))
+        return st, bm.value
+
+
+def ref_available():
+    return os.path.exists(REFLIB)
+
+
+class Reference:
+    """The reference's own C++ (compiled here from its sources) over one
+    workload.  Each instance loads a private copy of libref.so so that the
+    reference's global state is per instance."""
+
+    def __init__(self, w, workdir=None):
+        sys.path.insert(0, os.path.join(REPO, "moribs-pimc_gb300"))
+        from workloads import write_reference_inputs
+        self.w = w
+        self.tmp = workdir or tempfile.mkdtemp(prefix="pimcref_")
+        write_reference_inputs(w, self.tmp)
+        libcopy = os.path.join(self.tmp, "libref_copy.so")
+        shutil.copy(REFLIB, libcopy)
+        L = C.CDLL(libcopy, mode=os.RTLD_LOCAL)
+        self.L = L
+        L.ref_setup.argtypes = [C.c_char_p]
+        L.ref_load_3d.argtypes = [_dp, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int]
+        L.ref_load_rho.argtypes = [_dp, _dp, _dp, C.c_int, C.c_int, C.c_int]
+        L.ref_load_sph.argtypes = [_dp, C.c_int, C.c_double, C.c_double, C.c_double]
+        L.ref_set_state.argtypes = [_dp, _dp, _ip]
+        L.ref_get_state.argtypes = [_dp, _dp, _dp]
+        L.ref_set_replay.argtypes = [_dp, C.c_long, _dp, C.c_long, _dp, C.c_long, _dp, C.c_long, _dp, C.c_long]
+        L.ref_replay_pos.argtypes = [C.POINTER(C.c_long)]
+        for n in ("ref_pot_energy_slice",):
+            getattr(L, n).restype = C.c_double
+            getattr(L, n).argtypes = [C.c_int, _dp, C.c_int]
+        L.ref_pot_energy_path.restype = C.c_double
+        L.ref_pot_energy_path.argtypes = [C.c_int, _dp]
+        L.ref_pot_rot_energy.restype = C.c_double
+        L.ref_pot_rot_energy.argtypes = [C.c_int, _dp, C.c_int]
+        L.ref_pot_rot_e3d.restype = C.c_double
+        L.ref_pot_rot_e3d.argtypes = [C.c_int, _dp, C.c_int]
+        L.ref_spot1d.restype = C.c_double
+        L.ref_spot1d.argtypes = [C.c_double, C.c_int]
+        L.ref_lpot2d.restype = C.c_double
+        L.ref_lpot2d.argtypes = [C.c_double, C.c_double, C.c_int]
+        L.ref_srotdens.restype = C.c_double
+        L.ref_srotdens.argtypes = [C.c_double, C.c_int, C.c_int]
+        for n in ("ref_molecular_move", "ref_molecular_move_exchange", "ref_rotations_move", "ref_rotations_3d"):
+            getattr(L, n).argtypes = [C.c_int]
+        for n in ("ref_bisection_move", "ref_bisection_move_exchange"):
+            getattr(L, n).argtypes = [C.c_int, C.c_int]
+        for n in ("ref_rot_lin_step", "ref_rot_3d_step"):
+            getattr(L, n).argtypes = [C.c_int, C.c_int, _dp, _dp, _dp]
+        L.ref_counters.argtypes = [_dp, _dp]
+        for n in ("ref_kin_energy", "ref_pot_energy_est"):
+            getattr(L, n).restype = C.c_double
+        for n in ("ref_rot_energy", "ref_rot_e3d"):
+            getattr(L, n).restype = C.c_double
+            getattr(L, n).argtypes = [_dp, _dp]
+        L.ref_tau.restype = C.c_double
+        L.ref_lambda.restype = C.c_double
+        L.ref_lambda.argtypes = [C.c_int]
+        cwd = os.getcwd()
+        try:
+            if L.ref_setup(self.tmp.encode()) != 0:
+                raise RuntimeError("ref_setup failed")
+        finally:
+            os.chdir(cwd)
+        tb = w.tables
+        self._keep = []
+        if "vtable" in tb:
+            vt = np.ascontiguousarray(tb["vtable"], dtype=np.float64).ravel()
+            self._keep.append(vt)
+            L.ref_load_3d(dptr(vt), tb["rgrd"], tb["thgrd"], tb["chgrd"], tb["rvmin"], tb["rvmax"],
+                          tb.get("chi_fold_deg", 0))
+        if "rhoprp" in tb:
+            arrs = [np.ascontiguousarray(tb[k], dtype=np.float64).ravel() for k in ("rhoprp", "erotpr", "erotsq")]
+            self._keep += arrs
+            L.ref_load_rho(dptr(arrs[0]), dptr(arrs[1]), dptr(arrs[2]), tb["nth"], tb["nph"], tb["nch"])
+        if "sph_table" in tb:
+            st = np.ascontiguousarray(tb["sph_table"], dtype=np.float64)
+            self._keep.append(st)
+            L.ref_load_sph(dptr(st), len(st), tb["sph_r0"], tb["sph_rmax"], tb["sph_rstep"])
+        self.na = w.natoms
+        self.P = w.nslices
+        if w.coords is not None:
+            self.set_state(w.coords, w.angles, w.pindex)
+
+    def set_state(self, coords, angles, pindex=None):
+        c = np.ascontiguousarray(coords, dtype=np.float64)
+        a = np.ascontiguousarray(angles, dtype=np.float64)
+        p = None if pindex is None else np.ascontiguousarray(pindex, dtype=np.int32)
+        self.L.ref_set_state(dptr(c), dptr(a), iptr(p) if p is not None else None)
+
+    def get_state(self):
+        nb = self.na * self.P
+        c = np.zeros((3, nb)); a = np.zeros((3, nb)); co = np.zeros((3, nb))
+        self.L.ref_get_state(dptr(c), dptr(a), dptr(co))
+        return c, a, co
+
+    def replay(self, u1=None, u2=None, u3=None, gauss=None, urot=None):
+        self._rp = []
+        args = []
+        for a in (u1, u2, u3, gauss, urot):
+            if a is None:
+                args += [None, 0]
+            else:
+                a = np.ascontiguousarray(a, dtype=np.float64)
+                self._rp.append(a)
+                args += [dptr(a), len(a)]
+        self.L.ref_set_replay(*args)
+
+    def replay_pos(self):
+        p = (C.c_long * 6)()
+        self.L.ref_replay_pos(p)
+        return list(p)
+
+    def counters(self):
+        tot = np.zeros(6); acc = np.zeros(6)
+        self.L.ref_counters(dptr(tot), dptr(acc))
+        return tot, acc

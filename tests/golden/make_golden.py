@@ -1,0 +1,166 @@
+"""Generate the golden fixtures in tests/golden/ from the reference itself.
+
+Runs the reference's own C++ (compiled from its sources into oracle/_ref by
+oracle/ref_build.sh, Fortran leaves bound to the oracle's C restatements)
+on small seeded systems of the three benchmark families, with replayed
+random numbers, and stores inputs and outputs:
+
+  * PotEnergy per slice / whole path (mc_piqmc.cc:1201-1383,1796-1965),
+    PotRotEnergy / PotRotE3D (mc_piqmc.cc:1967-2151) on given configurations;
+  * a sequence of MCBisectionMove, MCMolecularMove and MCRotationsMove /
+    MCRotations3D calls (mc_piqmc.cc:54-1199): the final path, the accept
+    counters and the number of random numbers each generator consumed;
+  * the estimators GetKinEnergy, GetPotEnergy_Densities, GetRotEnergy /
+    GetRotE3D (mc_estim.cc:500-1096) of the final path.
+
+The reference runs single-threaded: its whole-path PotEnergy shares one
+dr[3] array across OpenMP threads (mc_piqmc.cc:1210,1237) and is not
+reproducible with more than one thread.  Tables are regenerated from the
+seeds at test time (workloads.py), so only their checksums are stored.
+
+Usage (here, where the reference tree exists):
+    oracle/ref_build.sh && OMP_NUM_THREADS=1 python tests/golden/make_golden.py
+"""
+import os
+import sys
+
+os.environ["OMP_NUM_THREADS"] = "1"
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(REPO, "oracle"))
+sys.path.insert(0, os.path.join(REPO, "moribs-pimc_gb300"))
+
+import numpy as np  # noqa: E402
+
+import oracle as O  # noqa: E402
+import workloads as W  # noqa: E402
+
+CASES = {
+    "c0s": ("config0", dict(seed=11, nslices=32, nrotslices=8, n_he=4, r2d_step=0.05, c2d_step=0.04)),
+    "c1s": ("config1", dict(seed=12, nslices=32, nrotslices=8, n_h2=6, grid3d=(30, 37, 19), griddens=(19, 37, 37))),
+    "c3s": ("config3", dict(seed=13, nslices=64, nrotslices=16, griddens=(19, 37, 37))),
+}
+
+
+def make_workload(case):
+    fn, kw = CASES[case]
+    return getattr(W, fn)(**kw)
+
+
+def table_checksums(w):
+    out = {}
+    for k, v in sorted(w.tables.items()):
+        if isinstance(v, np.ndarray):
+            out["tab_" + k] = np.array([float(np.sum(v)), float(np.sum(np.abs(v))), float(v.ravel()[len(v.ravel()) // 3])])
+    return out
+
+
+def generate(case, nsteps=4, seed=2024):
+    w = make_workload(case)
+    rng = np.random.default_rng(seed)
+    ref = O.Reference(w)
+    nb = w.natoms * w.nslices
+    res = dict(case=np.array(case), coords0=w.coords.copy(), angles0=w.angles.copy())
+    res.update(table_checksums(w))
+    c0 = np.ascontiguousarray(w.coords)
+    # ---- energies on the initial path and on a displaced path
+    pos = np.ascontiguousarray(c0 + rng.normal(0.0, 0.05, c0.shape))
+    slices = np.array([0, 3, w.nslices // 2, w.nslices - 1], dtype=np.int32)
+    e_slice = np.zeros((w.natoms, len(slices), 2))
+    e_path = np.zeros((w.natoms, 2))
+    for a in range(w.natoms):
+        for j, it in enumerate(slices):
+            e_slice[a, j, 0] = ref.L.ref_pot_energy_slice(a, O.dptr(c0), int(it))
+            e_slice[a, j, 1] = ref.L.ref_pot_energy_slice(a, O.dptr(pos), int(it))
+        e_path[a, 0] = ref.L.ref_pot_energy_path(a, O.dptr(c0))
+        e_path[a, 1] = ref.L.ref_pot_energy_path(a, O.dptr(pos))
+    res.update(pos=pos, slices=slices, e_slice=e_slice, e_path=e_path)
+    # rotor energies: random orientation sets
+    rot_types = [i for i, t in enumerate(w.types) if t["molecule"] != 0]
+    rtype = rot_types[0]
+    roff = sum(t["numb"] for t in w.types[:rtype])
+    eul = np.column_stack([rng.uniform(0, 2 * np.pi, 6), np.arccos(rng.uniform(-1, 1, 6)), rng.uniform(0, 2 * np.pi, 6)])
+    e_rot = np.zeros((6, len(slices)))
+    cosine = None
+    if w.types[rtype]["molecule"] == 1:
+        cosine = np.zeros((3, nb))
+        for k in range(6):
+            cosine[:, :] = 0.0
+            th, ph = eul[k, 1], eul[k, 0]
+            cosine[0, :] = np.sin(th) * np.cos(ph)
+            cosine[1, :] = np.sin(th) * np.sin(ph)
+            cosine[2, :] = np.cos(th)
+            cz = np.ascontiguousarray(cosine)
+            for j, it in enumerate(slices):
+                e_rot[k, j] = ref.L.ref_pot_rot_energy(roff, O.dptr(cz), int(it))
+    else:
+        for k in range(6):
+            e = np.ascontiguousarray(eul[k])
+            for j, it in enumerate(slices):
+                e_rot[k, j] = ref.L.ref_pot_rot_e3d(roff, O.dptr(e), int(it))
+    res.update(eul=eul, e_rot=e_rot)
+    # ---- a move sequence with replayed randoms
+    seq = []
+    streams = dict(gauss=[], u1=[], u2=[], u3=[], urot=[])
+    consumed = []
+    times = rng.integers(0, w.nslices, size=nsteps * len(w.types))
+    k = 0
+    for step in range(nsteps):
+        for typ in range(len(w.types)):
+            g = rng.normal(size=3 * w.types[typ]["numb"] * (1 << w.types[typ]["levels"]))
+            u3 = rng.uniform(size=w.types[typ]["numb"] * w.types[typ]["levels"])
+            t = int(times[k]); k += 1
+            ref.replay(gauss=g, u3=u3)
+            ref.L.ref_bisection_move(typ, t)
+            consumed.append(ref.replay_pos())
+            seq.append((0, typ, t))
+            streams["gauss"].append(g); streams["u3"].append(u3)
+        for typ in range(len(w.types)):
+            n = w.types[typ]["numb"]
+            u1 = rng.uniform(size=3 * n); u2 = rng.uniform(size=n)
+            ref.replay(u1=u1, u2=u2)
+            ref.L.ref_molecular_move(typ)
+            consumed.append(ref.replay_pos())
+            seq.append((1, typ, 0))
+            streams["u1"].append(u1); streams["u2"].append(u2)
+        nr = w.types[rtype]["numb"]
+        ur = rng.uniform(size=4 * w.nrotslices * nr)
+        ref.replay(urot=ur)
+        if w.types[rtype]["molecule"] == 1:
+            ref.L.ref_rotations_move(rtype)
+        else:
+            ref.L.ref_rotations_3d(rtype)
+        consumed.append(ref.replay_pos())
+        seq.append((2, rtype, 0))
+        streams["urot"].append(ur)
+    c, a, co = ref.get_state()
+    tot, acc = ref.counters()
+    res.update(seq=np.array(seq, dtype=np.int32), consumed=np.array(consumed, dtype=np.int64),
+               coords1=c, angles1=a, cosine1=co, total=tot, accep=acc)
+    for name, lst in streams.items():
+        res["s_" + name] = np.concatenate(lst) if lst else np.zeros(0)
+        res["n_" + name] = np.array([len(x) for x in lst], dtype=np.int64)
+    # ---- estimators on the final path
+    kin = ref.L.ref_kin_energy()
+    esq, ets = np.zeros(1), np.zeros(1)
+    if w.types[rtype]["molecule"] == 1:
+        rot = ref.L.ref_rot_energy(O.dptr(esq), O.dptr(ets))
+    else:
+        rot = ref.L.ref_rot_e3d(O.dptr(esq), O.dptr(ets))
+    pot = ref.L.ref_pot_energy_est()
+    res.update(est=np.array([kin, pot, rot, esq[0], ets[0]]))
+    return res
+
+
+def main():
+    if not O.ref_available():
+        sys.exit("oracle/_ref/libref.so missing: run oracle/ref_build.sh first")
+    for case in CASES:
+        res = generate(case)
+        path = os.path.join(HERE, case + ".npz")
+        np.savez_compressed(path, **res)
+        print("wrote", path, os.path.getsize(path), "bytes")
+
+
+if __name__ == "__main__":
+    main()
