@@ -1,0 +1,114 @@
+/*
+ * pimc_gb300.h -- C ABI of the GB300 (sm_103a) MoRiBS-PIMC sampling path.
+ *
+ * Plain pointers and sizes only.  A handle owns its device buffers and one
+ * CUDA stream; calls on one handle are ordered on that stream and return a
+ * pimc_status.  Host buffers passed in are only read or written during the
+ * call.  Layouts and units are those of pimc_types.h (the reference's
+ * MCCoords / MCAngles / MCCosine arrays, Kelvin and Angstrom).
+ *
+ * Each entry point names the reference interface it replaces.  The replay
+ * entry points run exactly one reference call on the GPU with the random
+ * numbers supplied by the caller, consumed in the reference's order
+ * (conditional draws included), so that their results can be compared move
+ * by move with the reference.  pimc_run_passes is the production sampler.
+ */
+#ifndef PIMC_GB300_H
+#define PIMC_GB300_H
+
+#include <stdint.h>
+#include "pimc_types.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct pimc_handle pimc_handle;
+
+/* MCMemAlloc + MCInit (mc_setup.cc:135-163, 321-453): validate the system
+ * (segment 2^levels < P, P divisible by Q, <= 1024 particles, one molecule
+ * type with at most 16 rotors) and allocate the path on `device`. */
+pimc_status pimc_create(const pimc_system *sys, int device, pimc_handle **out);
+pimc_status pimc_destroy(pimc_handle *h);
+
+/* InitPotentials / InitRotDensity (mc_poten.cc:93-164, 254-546): upload the
+ * tables and derive the spline second derivatives and the 1D extrapolation
+ * constants exactly as init_pot1D / init_rotdens do. */
+pimc_status pimc_load_tables(pimc_handle *h, const pimc_tables *tab);
+
+/* The path: coords/angles in the reference's [3][natoms*P] layout
+ * (MCCoords, MCAngles; mc_main.cc:184-200 derives MCCosine from the
+ * angles), pindex = PIndex.  Any pointer may be NULL to keep that part. */
+pimc_status pimc_set_state(pimc_handle *h, const double *coords, const double *angles, const int *pindex);
+pimc_status pimc_get_state(pimc_handle *h, double *coords, double *angles, double *cosine, int *pindex);
+
+/* ---- replay entry points (one reference call each) ---------------------- */
+
+/* MCMolecularMove(type) (mc_piqmc.cc:54-102): u1 = rnd1() draws (3 per
+ * atom), u2 = rnd2() draws (one per atom whose dV >= 0).  consumed[0..1]
+ * returns the counts drawn; dv_out[atom], acc_out[atom] per atom. */
+pimc_status pimc_molecular_move(pimc_handle *h, int type, const double *u1, long n1, const double *u2, long n2,
+                                long *consumed, double *dv_out, int *acc_out);
+
+/* MCBisectionMove(type, time) (mc_piqmc.cc:194-294) and, with exchange = 1,
+ * MCBisectionMoveExchange(type, time) (mc_piqmc.cc:296-419): gauss holds the
+ * x1 = sqrt(-log r1) cos(2 pi r2) values of gauss() (mc_randg.cc:138-150),
+ * three per midpoint in level order; u3 the rnd3() draws.  ds_out[atom*levels
+ * + level] = level action difference, lvl_out[atom] = levels accepted. */
+pimc_status pimc_bisection_move(pimc_handle *h, int type, int time, int exchange, const double *gauss, long ng,
+                                const double *u3, long n3, long *consumed, double *ds_out, int *lvl_out);
+
+/* MCRotationsMove / MCRotations3D (mc_piqmc.cc:421-517, 692-779): one
+ * even/odd sweep of all rotational slices; urot = runif() draws, 3 (linear)
+ * or 4 (nonlinear) per (slice, rotor) in serial order: even slices, then odd,
+ * rotors in order inside a slice.  rd_out/acc_out[slice*nrotors + rotor]. */
+pimc_status pimc_rotations_move(pimc_handle *h, const double *urot, long nrot, double *rd_out, int *acc_out);
+
+/* ---- energies ----------------------------------------------------------- */
+
+/* PotEnergy(atom0, pos, it) (mc_piqmc.cc:1796-1965) for n queries: atom0 at
+ * xyz[3k..3k+2] against all other atoms' current beads at slice it[k]. */
+pimc_status pimc_pot_energy(pimc_handle *h, int n, const int *atom0, const int *it, const double *xyz, double *out);
+
+/* PotRotE3D(rotor, Eulang, it) (mc_piqmc.cc:2046-2151) with v3 = (phi,
+ * theta, chi) for a nonlinear rotor, or PotRotEnergy (mc_piqmc.cc:1967-2044)
+ * with v3 = the unit vector for the linear rotor; rotor = global atom index. */
+pimc_status pimc_pot_rot_energy(pimc_handle *h, int n, const int *rotor, const int *it, const double *v3, double *out);
+
+/* ---- estimators (one MCGetAverage sample, mc_main.cc:551-616) ---------- */
+
+/* out = {GetKinEnergy, GetPotEnergy_Densities, GetRotEnergy|GetRotE3D,
+ *        ErotSQ, Erot_termSQ} (mc_estim.cc:500-1096) */
+pimc_status pimc_estimators(pimc_handle *h, double *out);
+/* GetRCF row 0 of one sample (mc_estim.cc:1099-1139): rcf[Q] */
+pimc_status pimc_rcf(pimc_handle *h, double *rcf);
+
+/* ---- production sampler -------------------------------------------------- */
+
+/* npasses passes of the reference schedule's moves (mc_main.cc:348-381,
+ * PIMCPass mc_main.cc:510-522): per pass and type, one centroid move per
+ * atom, one bisection per (atom, start slice), and P sweeps of all
+ * rotational slices, executed as independent-set phases (disjoint bisection
+ * windows; even/odd rotational slices) with a counter-based generator keyed
+ * by seed.  Requires P divisible by every type's 2^levels.  Asynchronous on
+ * the handle's stream; errors are reported by the next synchronising call. */
+pimc_status pimc_run_passes(pimc_handle *h, int npasses, uint64_t seed);
+/* MCTotal / MCAccep (mc_piqmc.h:25-26): total[type*3+kind], kind = molecule,
+ * multilevel, rotation */
+pimc_status pimc_counters(pimc_handle *h, double *total, double *accep);
+pimc_status pimc_reset_counters(pimc_handle *h);
+pimc_status pimc_synchronize(pimc_handle *h);
+/* 1: table interpolation of the rotor-atom potential in FP32 with FP64 sums */
+pimc_status pimc_set_precision(pimc_handle *h, int mixed);
+/* scheduled bead-moves per pass: per type N*P*(2^L-1) + N*P, plus P*Q per rotor */
+double      pimc_bead_moves_per_pass(const pimc_handle *h);
+/* kernels launched on the handle's stream so far */
+long long   pimc_launch_count(const pimc_handle *h);
+/* the handle's cudaStream_t, for event timing by the caller */
+void       *pimc_stream(const pimc_handle *h);
+const char *pimc_status_string(pimc_status s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PIMC_GB300_H */

@@ -1,0 +1,841 @@
+// pimc_capi.cu -- the extern "C" entry points of include/pimc_gb300.h: handle
+// life cycle, table preparation, path transfers, replay moves, energy
+// queries, estimators and the graph-captured production pass.
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "../../include/pimc_gb300.h"
+#include "pimc_kernels.cuh"
+#include "pimc_launch.h"
+
+#define CK(x)                                                  \
+  do {                                                         \
+    cudaError_t e_ = (x);                                      \
+    if (e_ != cudaSuccess) {                                   \
+      h->last_cuda = e_;                                       \
+      return PIMC_ERR_CUDA;                                    \
+    }                                                          \
+  } while (0)
+
+struct pimc_handle {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  pimc_system sys;
+  Ctx ctx;
+  Frame *frames = nullptr;
+  unsigned long long *cnt = nullptr;   // [type][kind][total, accepted]
+  unsigned *pass = nullptr;
+  MolScratch *ms = nullptr;
+  long *cursors = nullptr;             // replay cursors: gauss, u, d
+  std::vector<void *> owned;           // table buffers
+  std::vector<double> angles_host;     // full MCAngles copy (non-rotor rows kept as given)
+  std::vector<int> pindex_host;
+  std::vector<double> cosine_host;
+  bool tables = false, state = false;
+  cudaGraphExec_t pass_exec = nullptr;
+  uint64_t pass_seed = 0;
+  long long nodes_per_pass = 0;
+  long long launches = 0;
+  cudaError_t last_cuda = cudaSuccess;
+  // growable scratch for queries
+  void *qbuf = nullptr;
+  size_t qbytes = 0;
+};
+
+extern "C" const char *pimc_status_string(pimc_status s)
+{
+  switch (s) {
+    case PIMC_OK: return "ok";
+    case PIMC_ERR_BAD_ARG: return "bad argument";
+    case PIMC_ERR_BAD_TABLE: return "bad or missing table";
+    case PIMC_ERR_GRID_RANGE: return "rotational density grid index out of range";
+    case PIMC_ERR_NEG_DENSITY: return "negative rotational density";
+    case PIMC_ERR_TIMEOUT: return "device wait timed out";
+    case PIMC_ERR_CUDA: return "CUDA error";
+    case PIMC_ERR_NO_DEVICE: return "no CUDA device";
+    case PIMC_ERR_SIZE: return "size beyond a compiled limit";
+    case PIMC_ERR_STATE: return "call out of order";
+  }
+  return "unknown";
+}
+
+// ------------------------------------------------------------ helpers
+
+template <class T>
+static pimc_status dalloc(pimc_handle *h, T **p, size_t n)
+{
+  void *v = nullptr;
+  CK(cudaMalloc(&v, n * sizeof(T) > 0 ? n * sizeof(T) : 1));
+  *p = (T *)v;
+  return PIMC_OK;
+}
+
+static pimc_status upload(pimc_handle *h, const double *src, size_t n, const double **dst)
+{
+  double *d = nullptr;
+  pimc_status st = dalloc(h, &d, n);
+  if (st) return st;
+  h->owned.push_back(d);
+  CK(cudaMemcpyAsync(d, src, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  *dst = d;
+  return PIMC_OK;
+}
+
+static pimc_status upload_f32(pimc_handle *h, const double *src, size_t n, const float **dst)
+{
+  std::vector<float> f(n);
+  for (size_t i = 0; i < n; i++) f[i] = (float)src[i];
+  float *d = nullptr;
+  pimc_status st = dalloc(h, &d, n);
+  if (st) return st;
+  h->owned.push_back(d);
+  CK(cudaMemcpy(d, f.data(), n * sizeof(float), cudaMemcpyHostToDevice));
+  *dst = d;
+  return PIMC_OK;
+}
+
+static pimc_status scratch(pimc_handle *h, size_t bytes, void **p)
+{
+  if (bytes > h->qbytes) {
+    if (h->qbuf) CK(cudaFree(h->qbuf));
+    h->qbuf = nullptr;
+    CK(cudaMalloc(&h->qbuf, bytes));
+    h->qbytes = bytes;
+  }
+  *p = h->qbuf;
+  return PIMC_OK;
+}
+
+static pimc_status check_err(pimc_handle *h)
+{
+  CK(cudaStreamSynchronize(h->stream));
+  unsigned e = 0;
+  CK(cudaMemcpy(&e, h->ctx.st.err, sizeof(unsigned), cudaMemcpyDeviceToHost));
+  if (e) {
+    unsigned z = 0;
+    CK(cudaMemcpy(h->ctx.st.err, &z, sizeof(unsigned), cudaMemcpyHostToDevice));
+    if (e & DERR_GRID_RANGE) return PIMC_ERR_GRID_RANGE;
+    if (e & DERR_NEG_DENSITY) return PIMC_ERR_NEG_DENSITY;
+    if (e & DERR_TIMEOUT) return PIMC_ERR_TIMEOUT;
+    if (e & DERR_STREAM) return PIMC_ERR_BAD_ARG;
+  }
+  return PIMC_OK;
+}
+
+// cubic spline second derivatives with end slopes from the first and last
+// intervals: init_spline + spline (mc_utils.cc:112-154, 188-201)
+static void spline_y2(const double *x, const double *y, int n, double *y2)
+{
+  double yp1 = (y[1] - y[0]) / (x[1] - x[0]);
+  double ypn = (y[n - 1] - y[n - 2]) / (x[n - 1] - x[n - 2]);
+  std::vector<double> u(n);
+  y2[0] = -.5;
+  u[0] = (3. / (x[1] - x[0])) * ((y[1] - y[0]) / (x[1] - x[0]) - yp1);
+  for (int i = 1; i < n - 1; i++) {
+    double sig = (x[i] - x[i - 1]) / (x[i + 1] - x[i - 1]);
+    double p = sig * y2[i - 1] + 2.;
+    y2[i] = (sig - 1.) / p;
+    u[i] = (y[i + 1] - y[i]) / (x[i + 1] - x[i]) - (y[i] - y[i - 1]) / (x[i] - x[i - 1]);
+    u[i] = (6. * u[i] / (x[i + 1] - x[i - 1]) - sig * u[i - 1]) / p;
+  }
+  double qn = .5;
+  double un = (3. / (x[n - 1] - x[n - 2])) * (ypn - (y[n - 1] - y[n - 2]) / (x[n - 1] - x[n - 2]));
+  y2[n - 1] = (un - qn * u[n - 2]) / (qn * y2[n - 2] + 1.);
+  for (int k = n - 2; k >= 0; k--) y2[k] = y2[k] * y2[k + 1] + u[k];
+}
+
+// ------------------------------------------------------------ life cycle
+
+extern "C" pimc_status pimc_create(const pimc_system *sys, int device, pimc_handle **out)
+{
+  if (!sys || !out) return PIMC_ERR_BAD_ARG;
+  *out = nullptr;
+  const pimc_system &s = *sys;
+  if (s.ntypes < 1 || s.ntypes > PIMC_MAX_TYPES || s.nslices < 2 || s.temperature <= 0.0) return PIMC_ERR_BAD_ARG;
+  int na = 0, imtype = -1, nmol = 0;
+  for (int t = 0; t < s.ntypes; t++) {
+    const pimc_type &ty = s.type[t];
+    if (ty.numb < 1 || ty.levels < 1 || ty.levels > 6 || ty.lambda <= 0.0) return PIMC_ERR_BAD_ARG;
+    if ((1 << ty.levels) >= s.nslices) return PIMC_ERR_BAD_ARG;       // mc_setup.cc:397-398
+    if (ty.molecule < 0 || ty.molecule > 2) return PIMC_ERR_BAD_ARG;
+    if (ty.molecule != PIMC_ATOM) { imtype = t; nmol++; }
+    else if (nmol > 0) return PIMC_ERR_BAD_ARG;                       // atoms first (mc_input.cc:194)
+    na += ty.numb;
+  }
+  if (nmol > 1 || na > PIMC_MAX_ATOMS) return PIMC_ERR_SIZE;
+  if (imtype >= 0 && s.type[imtype].molecule == PIMC_LINEAR && s.type[imtype].numb != 1) return PIMC_ERR_BAD_ARG;
+  if (imtype >= 0 && s.type[imtype].numb > PIMC_MAX_ROTORS) return PIMC_ERR_SIZE;
+  int Q = s.rotation ? s.nrotslices : 0;
+  if (s.rotation && (imtype < 0 || Q < 1 || s.nslices % Q)) return PIMC_ERR_BAD_ARG;   // mc_setup.cc:382-389
+  if (s.rotation && s.nslices / Q > 16) return PIMC_ERR_SIZE;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return PIMC_ERR_NO_DEVICE;
+  if (device < 0 || device >= ndev) return PIMC_ERR_BAD_ARG;
+
+  pimc_handle *h = new (std::nothrow) pimc_handle();
+  if (!h) return PIMC_ERR_SIZE;
+  h->device = device;
+  h->sys = s;
+  CK(cudaSetDevice(device));
+  CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+  DevSys &d = h->ctx.s;
+  memset(&d, 0, sizeof(d));
+  d.na = na;
+  d.nap = (na + 31) / 32 * 32;
+  d.P = s.nslices;
+  // without rotation the reference keeps one orientation per translational
+  // slice (RotRatio = 1, mc_setup.cc:379); store P orientations then
+  d.Q = Q > 0 ? Q : s.nslices;
+  d.R = Q > 0 ? s.nslices / Q : 1;
+  d.ntypes = s.ntypes;
+  d.imtype = imtype;
+  int g = 0;
+  for (int t = 0; t < s.ntypes; t++) {
+    d.numb[t] = s.type[t].numb;
+    d.molecule[t] = s.type[t].molecule;
+    d.stat[t] = s.type[t].stat;
+    d.levels[t] = s.type[t].levels;
+    d.first[t] = g;
+    d.lambda[t] = s.type[t].lambda;
+    d.mcstep[t] = s.type[t].mcstep;
+    g += s.type[t].numb;
+  }
+  d.nrotors = imtype >= 0 ? s.type[imtype].numb : 0;
+  d.rot_first = imtype >= 0 ? d.first[imtype] : 0;
+  d.beta = 1.0 / s.temperature;                       // mc_setup.cc:373-377
+  d.tau = d.beta / (double)s.nslices;
+  d.rot_tau = Q > 0 ? d.beta / (double)Q : 0.0;
+  d.temperature = s.temperature;
+  d.rtstep = s.rtstep;
+  d.ispher = s.ispher;
+  d.rot_den_type = s.rot_den_type;
+  d.rot_odevn = s.rot_odevn;
+  d.rn_ratio = s.rn_ratio > 0 ? s.rn_ratio : 1;
+  d.rot_eoff = s.rot_eoff;
+  for (int k = 0; k < 3; k++) { d.abc[k] = s.rot_abc[k]; d.box[k] = s.box[k]; }
+  d.minimage = s.minimage;
+
+  DevState &st = h->ctx.st;
+  size_t nb = (size_t)d.P * d.nap;
+  size_t nr = (size_t)(d.nrotors > 0 ? d.nrotors : 1) * d.Q;
+  pimc_status e;
+  if ((e = dalloc(h, &st.x, nb)) || (e = dalloc(h, &st.y, nb)) || (e = dalloc(h, &st.z, nb)) ||
+      (e = dalloc(h, &st.ang, 3 * nr)) || (e = dalloc(h, &st.cosv, 3 * nr)) || (e = dalloc(h, &st.pindex, na)) ||
+      (e = dalloc(h, &st.mctype, na)) || (e = dalloc(h, &st.err, 1)) || (e = dalloc(h, &h->frames, nr)) ||
+      (e = dalloc(h, &h->cnt, 12)) || (e = dalloc(h, &h->pass, 1)) || (e = dalloc(h, &h->cursors, 8))) {
+    pimc_destroy(h);
+    return e;
+  }
+  void *msv = nullptr;
+  if (cudaMalloc(&msv, mol_scratch_bytes()) != cudaSuccess) { pimc_destroy(h); return PIMC_ERR_CUDA; }
+  h->ms = (MolScratch *)msv;
+  CK(cudaMemset(st.x, 0, nb * sizeof(double)));
+  CK(cudaMemset(st.y, 0, nb * sizeof(double)));
+  CK(cudaMemset(st.z, 0, nb * sizeof(double)));
+  CK(cudaMemset(st.err, 0, sizeof(unsigned)));
+  CK(cudaMemset(h->cnt, 0, 12 * sizeof(unsigned long long)));
+  CK(cudaMemset(h->pass, 0, sizeof(unsigned)));
+  std::vector<int> mct(na), pidx(na);
+  g = 0;
+  for (int t = 0; t < s.ntypes; t++)
+    for (int a = 0; a < s.type[t].numb; a++) mct[g++] = t;        // mc_setup.cc:327-333
+  for (int a = 0; a < na; a++) pidx[a] = a;                       // mc_setup.cc:335-339
+  CK(cudaMemcpy(st.mctype, mct.data(), na * sizeof(int), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(st.pindex, pidx.data(), na * sizeof(int), cudaMemcpyHostToDevice));
+  h->pindex_host = pidx;
+  h->angles_host.assign(3 * (size_t)na * d.P, 0.0);
+  h->cosine_host.assign(3 * (size_t)na * d.P, 0.0);
+  *out = h;
+  return PIMC_OK;
+}
+
+extern "C" pimc_status pimc_destroy(pimc_handle *h)
+{
+  if (!h) return PIMC_ERR_BAD_ARG;
+  cudaSetDevice(h->device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  if (h->pass_exec) cudaGraphExecDestroy(h->pass_exec);
+  DevState &st = h->ctx.st;
+  void *bufs[] = {st.x, st.y, st.z, st.ang, st.cosv, st.pindex, st.mctype, st.err, h->frames, h->cnt, h->pass,
+                  h->cursors, h->ms, h->qbuf};
+  for (void *b : bufs)
+    if (b) cudaFree(b);
+  for (void *b : h->owned) cudaFree(b);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return PIMC_OK;
+}
+
+// ------------------------------------------------------------ tables
+
+extern "C" pimc_status pimc_load_tables(pimc_handle *h, const pimc_tables *tb)
+{
+  if (!h || !tb) return PIMC_ERR_BAD_ARG;
+  CK(cudaSetDevice(h->device));
+  DevTables &t = h->ctx.t;
+  const DevSys &d = h->ctx.s;
+  pimc_status e;
+  bool need1d = false, need2d = false, need3d = false, needrot = false, need3drho = false;
+  for (int k = 0; k < d.ntypes; k++) {
+    if (d.molecule[k] == PIMC_ATOM) need1d = true;
+    if (d.molecule[k] == PIMC_LINEAR) { need2d = true; if (h->sys.rotation && d.rot_den_type == 0) needrot = true; }
+    if (d.molecule[k] == PIMC_NONLINEAR) {
+      if (d.ntypes > 1 && !d.ispher) need3d = true;
+      if (d.ntypes > 1 && h->sys.rotation) need3d = true;          // PotRotE3D uses vcord regardless of ISPHER
+      if (h->sys.rotation && (d.rot_den_type == 0 || d.nrotors > 0)) need3drho = true;
+    }
+  }
+  if (need1d && d.numb[0] < 2) need1d = false;                     // a single atom has no atom partner
+  if (need1d) {
+    int n = tb->n1d;
+    if (n < 2 || !tb->grid1d || !tb->pot1d) return PIMC_ERR_BAD_TABLE;
+    std::vector<double> y2(n);
+    spline_y2(tb->grid1d, tb->pot1d, n, y2.data());
+    t.n1d = n;
+    if ((e = upload(h, tb->grid1d, n, &t.g1d)) || (e = upload(h, tb->pot1d, n, &t.p1d)) ||
+        (e = upload(h, y2.data(), n, &t.y21d)))
+      return e;
+    // short- and long-range extrapolation constants (mc_poten.cc:418-437)
+    double fr = tb->pot1d[0] / tb->pot1d[1];
+    double dr = tb->grid1d[1] - tb->grid1d[0];
+    t.alpha1d = log(fr) / dr;
+    t.unode1d = tb->pot1d[0] * exp(t.alpha1d * tb->grid1d[0]);
+    double r0 = pow(tb->grid1d[n - 2], 6.0), r1 = pow(tb->grid1d[n - 1], 6.0);
+    fr = tb->pot1d[n - 1] - tb->pot1d[n - 2];
+    t.c61d = fr / (1.0 / r0 - 1.0 / r1);
+  }
+  if (need2d) {
+    if (tb->nr2d < 2 || tb->nc2d < 2 || !tb->pot2d || !tb->rgrid2d || !tb->cgrid2d || tb->dr2d <= 0 || tb->dc2d <= 0)
+      return PIMC_ERR_BAD_TABLE;
+    t.nr2d = tb->nr2d; t.nc2d = tb->nc2d; t.dr2d = tb->dr2d; t.dc2d = tb->dc2d;
+    if ((e = upload(h, tb->rgrid2d, tb->nr2d, &t.rg2d)) || (e = upload(h, tb->cgrid2d, tb->nc2d, &t.cg2d)) ||
+        (e = upload(h, tb->pot2d, (size_t)tb->nr2d * tb->nc2d, &t.pot2d)))
+      return e;
+  }
+  if (need3d) {
+    if (tb->rgrd < 2 || tb->thgrd < 2 || tb->chgrd < 2 || !tb->vtable || tb->rvmax <= tb->rvmin) return PIMC_ERR_BAD_TABLE;
+    t.rgrd = tb->rgrd; t.thgrd = tb->thgrd; t.chgrd = tb->chgrd;
+    int fold = tb->chi_fold_deg;
+    if (fold == 0) fold = (t.chgrd == 181) ? 180 : (t.chgrd == 361 ? 360 : 90);    // vcord.f:78-85
+    if (fold != 90 && fold != 180 && fold != 360) return PIMC_ERR_BAD_TABLE;
+    t.chfold = fold;
+    t.rvmin = tb->rvmin; t.rvmax = tb->rvmax;
+    t.rvstep = (t.rvmax - t.rvmin) / (double)(t.rgrd - 1);      // mc_poten.cc:288
+    t.dth3 = 180.0 / (double)(t.thgrd - 1);
+    t.dch3 = (double)fold / (double)(t.chgrd - 1);
+    size_t n = (size_t)t.rgrd * t.thgrd * t.chgrd;
+    if ((e = upload(h, tb->vtable, n, &t.vtab)) || (e = upload_f32(h, tb->vtable, n, &t.vtab32))) return e;
+  }
+  if (d.ispher && d.ntypes > 1) {
+    if (tb->nsph < 2 || !tb->sph_table || tb->sph_rstep <= 0) return PIMC_ERR_BAD_TABLE;
+    t.nsph = tb->nsph; t.sph_r0 = tb->sph_r0; t.sph_rmax = tb->sph_rmax; t.sph_rstep = tb->sph_rstep;
+    if ((e = upload(h, tb->sph_table, tb->nsph, &t.sph))) return e;
+  }
+  if (needrot) {
+    int n = tb->nrot;
+    if (n < 2 || !tb->rotgrid || !tb->rotdens || !tb->rotderv || !tb->rotesqr) return PIMC_ERR_BAD_TABLE;
+    std::vector<double> a(n), b(n), c(n);
+    spline_y2(tb->rotgrid, tb->rotdens, n, a.data());              // init_rotdens mc_poten.cc:543-545
+    spline_y2(tb->rotgrid, tb->rotderv, n, b.data());
+    spline_y2(tb->rotgrid, tb->rotesqr, n, c.data());
+    t.nrot = n;
+    if ((e = upload(h, tb->rotgrid, n, &t.rg)) || (e = upload(h, tb->rotdens, n, &t.rd)) ||
+        (e = upload(h, tb->rotderv, n, &t.rdv)) || (e = upload(h, tb->rotesqr, n, &t.rde)) ||
+        (e = upload(h, a.data(), n, &t.rd_y2)) || (e = upload(h, b.data(), n, &t.rdv_y2)) ||
+        (e = upload(h, c.data(), n, &t.rde_y2)))
+      return e;
+  }
+  if (need3drho) {
+    if (tb->nth < 2 || tb->nph < 2 || tb->nch < 2 || !tb->rhoprp || !tb->erotpr || !tb->erotsq) {
+      if (d.rot_den_type == 0) return PIMC_ERR_BAD_TABLE;
+    } else {
+      t.nth = tb->nth; t.nph = tb->nph; t.nch = tb->nch;
+      t.dthd = 180.0 / (double)(t.nth - 1);
+      t.dphd = 360.0 / (double)(t.nph - 1);
+      t.dchd = 360.0 / (double)(t.nch - 1);
+      size_t n = (size_t)t.nth * t.nph * t.nch;
+      if ((e = upload(h, tb->rhoprp, n, &t.rho)) || (e = upload(h, tb->erotpr, n, &t.erot)) ||
+          (e = upload(h, tb->erotsq, n, &t.esq)))
+        return e;
+    }
+  }
+  CK(cudaStreamSynchronize(h->stream));
+  h->tables = true;
+  if (h->pass_exec) { cudaGraphExecDestroy(h->pass_exec); h->pass_exec = nullptr; }
+  return PIMC_OK;
+}
+
+// ------------------------------------------------------------ path
+
+extern "C" pimc_status pimc_set_state(pimc_handle *h, const double *coords, const double *angles, const int *pindex)
+{
+  if (!h) return PIMC_ERR_BAD_ARG;
+  CK(cudaSetDevice(h->device));
+  const DevSys &d = h->ctx.s;
+  size_t nbr = (size_t)d.na * d.P;      // reference layout length per row
+  if (coords) {
+    // [3][na*P] -> slice-major x/y/z[t*nap + a]
+    std::vector<double> buf((size_t)d.P * d.nap, 0.0);
+    double *dst[3] = {h->ctx.st.x, h->ctx.st.y, h->ctx.st.z};
+    for (int k = 0; k < 3; k++) {
+      for (int a = 0; a < d.na; a++)
+        for (int t = 0; t < d.P; t++) buf[(size_t)t * d.nap + a] = coords[k * nbr + (size_t)a * d.P + t];
+      CK(cudaMemcpy(dst[k], buf.data(), buf.size() * sizeof(double), cudaMemcpyHostToDevice));
+    }
+  }
+  if (angles) {
+    memcpy(h->angles_host.data(), angles, 3 * nbr * sizeof(double));
+    for (size_t i = 0; i < nbr; i++) {                      // mc_main.cc:193-199
+      double phi = angles[i], cost = angles[nbr + i];
+      double sint = sqrt(1.0 - cost * cost);
+      h->cosine_host[i] = sint * cos(phi);
+      h->cosine_host[nbr + i] = sint * sin(phi);
+      h->cosine_host[2 * nbr + i] = cost;
+    }
+    if (d.nrotors > 0) {
+      size_t n = (size_t)d.nrotors * d.Q;
+      std::vector<double> ang(3 * n), cs(3 * n);
+      for (int k = 0; k < 3; k++)
+        for (int r = 0; r < d.nrotors; r++)
+          for (int q = 0; q < d.Q; q++) {
+            size_t src = k * nbr + (size_t)(d.rot_first + r) * d.P + q;
+            ang[k * n + r * d.Q + q] = angles[src];
+            cs[k * n + r * d.Q + q] = h->cosine_host[src];
+          }
+      CK(cudaMemcpy(h->ctx.st.ang, ang.data(), 3 * n * sizeof(double), cudaMemcpyHostToDevice));
+      CK(cudaMemcpy(h->ctx.st.cosv, cs.data(), 3 * n * sizeof(double), cudaMemcpyHostToDevice));
+      launch_frames_init(h->ctx, h->frames, h->stream);
+      h->launches++;
+      CK(cudaGetLastError());
+    }
+  }
+  if (pindex) {
+    for (int a = 0; a < d.na; a++)
+      if (pindex[a] < 0 || pindex[a] >= d.na) return PIMC_ERR_BAD_ARG;
+    CK(cudaMemcpy(h->ctx.st.pindex, pindex, d.na * sizeof(int), cudaMemcpyHostToDevice));
+    h->pindex_host.assign(pindex, pindex + d.na);
+  }
+  CK(cudaStreamSynchronize(h->stream));
+  if (coords && angles) h->state = true;
+  return PIMC_OK;
+}
+
+extern "C" pimc_status pimc_get_state(pimc_handle *h, double *coords, double *angles, double *cosine, int *pindex)
+{
+  if (!h) return PIMC_ERR_BAD_ARG;
+  CK(cudaSetDevice(h->device));
+  CK(cudaStreamSynchronize(h->stream));
+  const DevSys &d = h->ctx.s;
+  size_t nbr = (size_t)d.na * d.P;
+  if (coords) {
+    std::vector<double> buf((size_t)d.P * d.nap);
+    double *src[3] = {h->ctx.st.x, h->ctx.st.y, h->ctx.st.z};
+    for (int k = 0; k < 3; k++) {
+      CK(cudaMemcpy(buf.data(), src[k], buf.size() * sizeof(double), cudaMemcpyDeviceToHost));
+      for (int a = 0; a < d.na; a++)
+        for (int t = 0; t < d.P; t++) coords[k * nbr + (size_t)a * d.P + t] = buf[(size_t)t * d.nap + a];
+    }
+  }
+  if (angles || cosine) {
+    if (d.nrotors > 0) {
+      size_t n = (size_t)d.nrotors * d.Q;
+      std::vector<double> ang(3 * n), cs(3 * n);
+      CK(cudaMemcpy(ang.data(), h->ctx.st.ang, 3 * n * sizeof(double), cudaMemcpyDeviceToHost));
+      CK(cudaMemcpy(cs.data(), h->ctx.st.cosv, 3 * n * sizeof(double), cudaMemcpyDeviceToHost));
+      for (int k = 0; k < 3; k++)
+        for (int r = 0; r < d.nrotors; r++)
+          for (int q = 0; q < d.Q; q++) {
+            size_t dst = k * nbr + (size_t)(d.rot_first + r) * d.P + q;
+            h->angles_host[dst] = ang[k * n + r * d.Q + q];
+            h->cosine_host[dst] = cs[k * n + r * d.Q + q];
+          }
+    }
+    if (angles) memcpy(angles, h->angles_host.data(), 3 * nbr * sizeof(double));
+    if (cosine) memcpy(cosine, h->cosine_host.data(), 3 * nbr * sizeof(double));
+  }
+  if (pindex) CK(cudaMemcpy(pindex, h->ctx.st.pindex, d.na * sizeof(int), cudaMemcpyDeviceToHost));
+  return PIMC_OK;
+}
+
+static pimc_status ready(pimc_handle *h)
+{
+  if (!h) return PIMC_ERR_BAD_ARG;
+  if (!h->tables || !h->state) return PIMC_ERR_STATE;
+  CK(cudaSetDevice(h->device));
+  return PIMC_OK;
+}
+
+// ------------------------------------------------------------ replay moves
+
+static pimc_status put_stream(pimc_handle *h, const double *v, long n, double **dv, char *&cursor)
+{
+  *dv = (double *)cursor;
+  if (n > 0) CK(cudaMemcpyAsync(*dv, v, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  cursor += ((size_t)(n > 0 ? n : 1) * sizeof(double) + 255) / 256 * 256;
+  return PIMC_OK;
+}
+
+extern "C" pimc_status pimc_bisection_move(pimc_handle *h, int type, int time, int exchange, const double *gauss,
+                                           long ng, const double *u3, long n3, long *consumed, double *ds_out,
+                                           int *lvl_out)
+{
+  pimc_status e = ready(h);
+  if (e) return e;
+  const DevSys &d = h->ctx.s;
+  if (type < 0 || type >= d.ntypes || time < 0 || time >= d.P || ng < 0 || n3 < 0 || (ng && !gauss) || (n3 && !u3))
+    return PIMC_ERR_BAD_ARG;
+  int numb = d.numb[type], L = d.levels[type];
+  if (exchange) {
+    // the permutation is sampled for the boson type only (mc_main.cc:366-367)
+    if (d.stat[type] != PIMC_BOSE) return PIMC_ERR_BAD_ARG;
+    for (int a = 0; a < numb; a++)
+      if (h->pindex_host[a] < 0 || h->pindex_host[a] >= numb) return PIMC_ERR_BAD_ARG;
+  }
+  size_t bytes = ((size_t)ng + n3 + 2 * (size_t)numb * L + numb + 16) * sizeof(double) + 4096;
+  void *buf;
+  if ((e = scratch(h, bytes, &buf))) return e;
+  char *cur = (char *)buf;
+  double *dg, *du, *dds;
+  if ((e = put_stream(h, gauss, ng, &dg, cur)) || (e = put_stream(h, u3, n3, &du, cur))) return e;
+  dds = (double *)cur;
+  cur += ((size_t)numb * L * sizeof(double) + 255) / 256 * 256;
+  int *dlv = (int *)cur;
+  CK(cudaMemsetAsync(h->cursors, 0, 8 * sizeof(long), h->stream));
+  CK(cudaMemsetAsync(dds, 0, (size_t)numb * L * sizeof(double), h->stream));
+  ReplaySrc src{dg, ng, h->cursors + 0, du, n3, h->cursors + 1, nullptr, 0, h->cursors + 2, h->ctx.st.err};
+  launch_bisect_replay(h->ctx, h->frames, type, time, exchange ? 1 : 0, src, dds, dlv, h->cnt, h->stream);
+  h->launches++;
+  CK(cudaGetLastError());
+  long cz[8];
+  CK(cudaMemcpyAsync(cz, h->cursors, 8 * sizeof(long), cudaMemcpyDeviceToHost, h->stream));
+  if (ds_out) CK(cudaMemcpyAsync(ds_out, dds, (size_t)numb * L * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  if (lvl_out) CK(cudaMemcpyAsync(lvl_out, dlv, numb * sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  e = check_err(h);
+  if (consumed) { consumed[0] = cz[0]; consumed[1] = cz[1]; }
+  return e;
+}
+
+extern "C" pimc_status pimc_molecular_move(pimc_handle *h, int type, const double *u1, long n1, const double *u2,
+                                           long n2, long *consumed, double *dv_out, int *acc_out)
+{
+  pimc_status e = ready(h);
+  if (e) return e;
+  const DevSys &d = h->ctx.s;
+  if (type < 0 || type >= d.ntypes || n1 < 0 || n2 < 0 || (n1 && !u1) || (n2 && !u2)) return PIMC_ERR_BAD_ARG;
+  int numb = d.numb[type];
+  size_t bytes = ((size_t)n1 + n2 + 2 * (size_t)numb + 16) * sizeof(double) + 4096;
+  void *buf;
+  if ((e = scratch(h, bytes, &buf))) return e;
+  char *cur = (char *)buf;
+  double *d1, *d2;
+  if ((e = put_stream(h, u1, n1, &d1, cur)) || (e = put_stream(h, u2, n2, &d2, cur))) return e;
+  double *ddv = (double *)cur;
+  cur += ((size_t)numb * sizeof(double) + 255) / 256 * 256;
+  int *dacc = (int *)cur;
+  CK(cudaMemsetAsync(h->cursors, 0, 8 * sizeof(long), h->stream));
+  ReplaySrc src{nullptr, 0, h->cursors + 0, d2, n2, h->cursors + 1, d1, n1, h->cursors + 2, h->ctx.st.err};
+  for (int a = 0; a < numb; a++) {
+    launch_mol(h->ctx, h->frames, type, a, true, src, 0, h->pass, 0, h->ms, ddv, dacc, h->cnt, h->stream);
+    h->launches += 3;
+  }
+  CK(cudaGetLastError());
+  long cz[8];
+  CK(cudaMemcpyAsync(cz, h->cursors, 8 * sizeof(long), cudaMemcpyDeviceToHost, h->stream));
+  if (dv_out) CK(cudaMemcpyAsync(dv_out, ddv, numb * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  if (acc_out) CK(cudaMemcpyAsync(acc_out, dacc, numb * sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  e = check_err(h);
+  if (consumed) { consumed[0] = cz[2]; consumed[1] = cz[1]; }
+  return e;
+}
+
+extern "C" pimc_status pimc_rotations_move(pimc_handle *h, const double *urot, long nrot, double *rd_out, int *acc_out)
+{
+  pimc_status e = ready(h);
+  if (e) return e;
+  const DevSys &d = h->ctx.s;
+  if (d.imtype < 0 || !h->sys.rotation || nrot < 0 || (nrot && !urot)) return PIMC_ERR_BAD_ARG;
+  size_t nk = (size_t)d.Q * d.nrotors;
+  size_t bytes = ((size_t)nrot + 2 * nk + 16) * sizeof(double) + 4096;
+  void *buf;
+  if ((e = scratch(h, bytes, &buf))) return e;
+  char *cur = (char *)buf;
+  double *du;
+  if ((e = put_stream(h, urot, nrot, &du, cur))) return e;
+  double *drd = (double *)cur;
+  cur += (nk * sizeof(double) + 255) / 256 * 256;
+  int *dacc = (int *)cur;
+  launch_rot_replay(h->ctx, h->frames, 0, du, nrot, drd, dacc, h->cnt, h->stream);
+  launch_rot_replay(h->ctx, h->frames, 1, du, nrot, drd, dacc, h->cnt, h->stream);
+  h->launches += 2;
+  CK(cudaGetLastError());
+  if (rd_out) CK(cudaMemcpyAsync(rd_out, drd, nk * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  if (acc_out) CK(cudaMemcpyAsync(acc_out, dacc, nk * sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  return check_err(h);
+}
+
+// ------------------------------------------------------------ energies
+
+extern "C" pimc_status pimc_pot_energy(pimc_handle *h, int n, const int *atom0, const int *it, const double *xyz,
+                                       double *out)
+{
+  pimc_status e = ready(h);
+  if (e) return e;
+  const DevSys &d = h->ctx.s;
+  if (n < 0 || (n && (!atom0 || !it || !xyz || !out))) return PIMC_ERR_BAD_ARG;
+  for (int k = 0; k < n; k++)
+    if (atom0[k] < 0 || atom0[k] >= d.na || it[k] < 0 || it[k] >= d.P) return PIMC_ERR_BAD_ARG;
+  size_t bytes = (size_t)n * (2 * sizeof(int) + 4 * sizeof(double)) + 4096;
+  void *buf;
+  if ((e = scratch(h, bytes, &buf))) return e;
+  char *cur = (char *)buf;
+  int *da = (int *)cur; cur += ((size_t)n * sizeof(int) + 255) / 256 * 256;
+  int *dt = (int *)cur; cur += ((size_t)n * sizeof(int) + 255) / 256 * 256;
+  double *dx = (double *)cur; cur += ((size_t)3 * n * sizeof(double) + 255) / 256 * 256;
+  double *dout = (double *)cur;
+  CK(cudaMemcpyAsync(da, atom0, n * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(dt, it, n * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(dx, xyz, 3 * n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  launch_q_slice(h->ctx, h->frames, n, da, dt, dx, dout, h->stream);
+  h->launches++;
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(out, dout, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  return check_err(h);
+}
+
+extern "C" pimc_status pimc_pot_rot_energy(pimc_handle *h, int n, const int *rotor, const int *it, const double *v3,
+                                           double *out)
+{
+  pimc_status e = ready(h);
+  if (e) return e;
+  const DevSys &d = h->ctx.s;
+  if (d.imtype < 0 || n < 0 || (n && (!rotor || !it || !v3 || !out))) return PIMC_ERR_BAD_ARG;
+  for (int k = 0; k < n; k++)
+    if (rotor[k] < d.rot_first || rotor[k] >= d.rot_first + d.nrotors || it[k] < 0 || it[k] >= d.P)
+      return PIMC_ERR_BAD_ARG;
+  size_t bytes = (size_t)n * (2 * sizeof(int) + 4 * sizeof(double)) + 4096;
+  void *buf;
+  if ((e = scratch(h, bytes, &buf))) return e;
+  char *cur = (char *)buf;
+  int *da = (int *)cur; cur += ((size_t)n * sizeof(int) + 255) / 256 * 256;
+  int *dt = (int *)cur; cur += ((size_t)n * sizeof(int) + 255) / 256 * 256;
+  double *dv = (double *)cur; cur += ((size_t)3 * n * sizeof(double) + 255) / 256 * 256;
+  double *dout = (double *)cur;
+  CK(cudaMemcpyAsync(da, rotor, n * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(dt, it, n * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(dv, v3, 3 * n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  launch_q_rot(h->ctx, h->frames, n, da, dt, dv, d.molecule[d.imtype] == PIMC_LINEAR, dout, h->stream);
+  h->launches++;
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(out, dout, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  return check_err(h);
+}
+
+// ------------------------------------------------------------ estimators
+
+extern "C" pimc_status pimc_estimators(pimc_handle *h, double *out)
+{
+  pimc_status e = ready(h);
+  if (e) return e;
+  if (!out) return PIMC_ERR_BAD_ARG;
+  const DevSys &d = h->ctx.s;
+  int npairs = d.na * (d.na - 1) / 2;
+  size_t nk = (size_t)d.nrotors * d.Q;
+  size_t nd = (size_t)d.na + npairs + 4 * nk + d.Q + 64;
+  void *buf;
+  if ((e = scratch(h, nd * sizeof(double) + 4096, &buf))) return e;
+  double *kin = (double *)buf, *pot = kin + d.na, *rot = pot + npairs, *rcf = rot + 4 * nk;
+  launch_est(h->ctx, h->frames, kin, pot, rot, rcf, h->stream);
+  h->launches += nk ? 4 : 2;
+  CK(cudaGetLastError());
+  std::vector<double> hv(nd);
+  CK(cudaMemcpyAsync(hv.data(), buf, nd * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  if ((e = check_err(h))) return e;
+  // GetKinEnergy: P*T*(0.5*3*N - sum_atoms r2 / (4 beta lambda)) (mc_estim.cc:923-934)
+  double r2avr = 0.0;
+  for (int a = 0; a < d.na; a++) r2avr += hv[a];
+  out[0] = (double)d.P * d.temperature * (0.5 * (double)(3 * d.na) - r2avr);
+  double spot = 0.0;
+  for (int p = 0; p < npairs; p++) spot += hv[d.na + p];
+  out[1] = spot / (double)d.P;
+  double erot = 0.0, esq = 0.0, ets = 0.0;
+  if (nk && h->sys.rotation) {
+    const double *r = hv.data() + d.na + npairs;
+    if (d.molecule[d.imtype] == PIMC_LINEAR) {          // GetRotEnergy mc_estim.cc:953-984
+      for (int q = 0; q < d.Q; q++) { erot += r[4 * q]; esq += r[4 * q + 1]; ets += r[4 * q + 2]; }
+      if (d.rot_den_type == 1) {
+        erot = erot / (double)d.Q;
+        erot = erot / d.rot_tau + 1.0 / d.rot_tau;
+      }
+    } else {                                              // GetRotE3D mc_estim.cc:1000-1092
+      int skip = d.rot_den_type == 0 ? 1 : d.rn_ratio;
+      double nq = (double)(d.Q / skip);
+      for (int rr = 0; rr < d.nrotors; rr++) {
+        double s = 0.0, q2 = 0.0, t2 = 0.0;
+        for (int q = 0; q < d.Q; q++) {
+          const double *v = r + 4 * ((size_t)rr * d.Q + q);
+          s += v[0]; q2 += v[1]; t2 += v[2];
+        }
+        erot += s / nq;
+        esq += q2 / (nq * nq);
+        ets += t2 / (nq * nq);
+        if (d.rot_den_type == 1 && d.rn_ratio == 1) {
+          erot = erot / (4.0 * (d.rot_tau / PIMC_WNO2K) * (d.rot_tau / PIMC_WNO2K));
+          erot += 0.25 * (d.abc[0] + d.abc[1] + d.abc[2]) + 1.5 / (d.rot_tau / PIMC_WNO2K);
+          erot = erot / PIMC_WNO2K;
+        }
+      }
+    }
+  }
+  out[2] = erot;
+  out[3] = esq;
+  out[4] = ets;
+  return PIMC_OK;
+}
+
+extern "C" pimc_status pimc_rcf(pimc_handle *h, double *rcf)
+{
+  pimc_status e = ready(h);
+  if (e) return e;
+  if (!rcf || h->ctx.s.nrotors == 0) return PIMC_ERR_BAD_ARG;
+  const DevSys &d = h->ctx.s;
+  int npairs = d.na * (d.na - 1) / 2;
+  size_t nk = (size_t)d.nrotors * d.Q;
+  size_t nd = (size_t)d.na + npairs + 4 * nk + d.Q + 64;
+  void *buf;
+  if ((e = scratch(h, nd * sizeof(double) + 4096, &buf))) return e;
+  double *kin = (double *)buf, *pot = kin + d.na, *rot = pot + npairs, *rc = rot + 4 * nk;
+  launch_est(h->ctx, h->frames, kin, pot, rot, rc, h->stream);
+  h->launches += 4;
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(rcf, rc, d.Q * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  return check_err(h);
+}
+
+// ------------------------------------------------------------ production
+
+// one pass of the independent-set schedule, recorded on h->stream
+static long long record_pass(pimc_handle *h, uint64_t seed)
+{
+  const DevSys &d = h->ctx.s;
+  long long n = 0;
+  launch_pass_begin(h->pass, h->stream);
+  n++;
+  // bisection phases: type, start offset s0 < M, atom rotation j < numb
+  struct Ph { int type, s0, j; };
+  std::vector<Ph> bis;
+  for (int t = 0; t < d.ntypes; t++) {
+    int M = 1 << d.levels[t];
+    for (int s0 = 0; s0 < M; s0++)
+      for (int j = 0; j < d.numb[t]; j++) bis.push_back({t, s0, j});
+  }
+  unsigned B = (unsigned)bis.size();
+  unsigned mol_phase = B + 2u * (unsigned)d.P;
+  // centroid moves at time 0 (PIMCPass, mc_main.cc:512-513)
+  for (int t = 0; t < d.ntypes; t++)
+    for (int a = 0; a < d.numb[t]; a++) {
+      ReplaySrc none{};
+      none.err = h->ctx.st.err;
+      launch_mol(h->ctx, h->frames, t, a, false, none, seed, h->pass, mol_phase + (unsigned)t, h->ms, nullptr, nullptr, h->cnt,
+                 h->stream);
+      n += 3;
+    }
+  // time iterations: the bisection phases spread evenly, then one sweep
+  size_t b = 0;
+  for (int it = 0; it < d.P; it++) {
+    size_t bend = (size_t)((unsigned long long)(it + 1) * B / d.P);
+    for (; b < bend; b++) {
+      launch_bisect_phase(h->ctx, h->frames, bis[b].type, bis[b].s0, bis[b].j, (unsigned)b, seed, h->pass, h->cnt,
+                          h->stream);
+      n++;
+    }
+    if (h->sys.rotation && d.nrotors > 0) {
+      launch_rot_phase(h->ctx, h->frames, 0, B + 2u * it, seed, h->pass, h->cnt, h->stream);
+      launch_rot_phase(h->ctx, h->frames, 1, B + 2u * it + 1, seed, h->pass, h->cnt, h->stream);
+      n += 2;
+    }
+  }
+  return n;
+}
+
+extern "C" pimc_status pimc_run_passes(pimc_handle *h, int npasses, uint64_t seed)
+{
+  pimc_status e = ready(h);
+  if (e) return e;
+  const DevSys &d = h->ctx.s;
+  if (npasses < 0) return PIMC_ERR_BAD_ARG;
+  for (int t = 0; t < d.ntypes; t++)
+    if (d.P % (1 << d.levels[t])) return PIMC_ERR_BAD_ARG;
+  if (!h->pass_exec || h->pass_seed != seed) {
+    if (h->pass_exec) { CK(cudaGraphExecDestroy(h->pass_exec)); h->pass_exec = nullptr; }
+    cudaGraph_t graph;
+    CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    long long n = record_pass(h, seed);
+    cudaError_t le = cudaGetLastError();
+    CK(cudaStreamEndCapture(h->stream, &graph));
+    if (le != cudaSuccess) { cudaGraphDestroy(graph); h->last_cuda = le; return PIMC_ERR_CUDA; }
+    cudaError_t ie = cudaGraphInstantiate(&h->pass_exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ie != cudaSuccess) { h->last_cuda = ie; return PIMC_ERR_CUDA; }
+    h->pass_seed = seed;
+    h->nodes_per_pass = n;
+  }
+  for (int p = 0; p < npasses; p++) {
+    CK(cudaGraphLaunch(h->pass_exec, h->stream));
+    h->launches += h->nodes_per_pass;
+  }
+  return PIMC_OK;
+}
+
+extern "C" pimc_status pimc_synchronize(pimc_handle *h)
+{
+  if (!h) return PIMC_ERR_BAD_ARG;
+  CK(cudaSetDevice(h->device));
+  return check_err(h);
+}
+
+extern "C" pimc_status pimc_counters(pimc_handle *h, double *total, double *accep)
+{
+  if (!h || !total || !accep) return PIMC_ERR_BAD_ARG;
+  CK(cudaSetDevice(h->device));
+  unsigned long long c[12];
+  CK(cudaMemcpyAsync(c, h->cnt, sizeof(c), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  for (int i = 0; i < 6; i++) { total[i] = (double)c[2 * i]; accep[i] = (double)c[2 * i + 1]; }
+  return PIMC_OK;
+}
+
+extern "C" pimc_status pimc_reset_counters(pimc_handle *h)
+{
+  if (!h) return PIMC_ERR_BAD_ARG;
+  CK(cudaSetDevice(h->device));
+  CK(cudaMemsetAsync(h->cnt, 0, 12 * sizeof(unsigned long long), h->stream));
+  return PIMC_OK;
+}
+
+extern "C" pimc_status pimc_set_precision(pimc_handle *h, int mixed)
+{
+  if (!h || mixed < 0 || mixed > 1) return PIMC_ERR_BAD_ARG;
+  h->ctx.s.mixed = mixed;
+  if (h->pass_exec) { cudaGraphExecDestroy(h->pass_exec); h->pass_exec = nullptr; }
+  return PIMC_OK;
+}
+
+extern "C" double pimc_bead_moves_per_pass(const pimc_handle *h)
+{
+  if (!h) return 0.0;
+  const DevSys &d = h->ctx.s;
+  double bm = 0.0;
+  for (int t = 0; t < d.ntypes; t++) {
+    bm += (double)d.numb[t] * d.P * ((1 << d.levels[t]) - 1) + (double)d.numb[t] * d.P;
+    if (t == d.imtype && h->sys.rotation) bm += (double)d.numb[t] * d.P * d.Q;
+  }
+  return bm;
+}
+
+extern "C" long long pimc_launch_count(const pimc_handle *h) { return h ? h->launches : 0; }
+
+extern "C" void *pimc_stream(const pimc_handle *h) { return h ? (void *)h->stream : nullptr; }

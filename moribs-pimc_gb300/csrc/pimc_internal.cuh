@@ -1,0 +1,493 @@
+// pimc_internal.cuh -- device-side data layout and leaf routines of the GB300
+// sampling path.  Each leaf names the reference routine whose arithmetic it
+// follows; the double-precision versions keep the reference's operation
+// order so that results agree with it to rounding.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#define PIMC_PI 3.14159265358979323846
+#define PIMC_WNO2K 0.6950356          /* mc_const.h:16 */
+#define PIMC_RZERO 1.0e-10            /* mc_confg.h:59 */
+#define PIMC_BLOCK 128                /* threads per move CTA */
+#define PIMC_MAX_SEG 64               /* largest bisection segment (levels <= 6) */
+#define PIMC_MAX_ROTORS 16            /* NumbRotLim (mc_setup.cc:63) */
+
+// error bits raised on the device and read back by the host
+enum { DERR_GRID_RANGE = 1, DERR_NEG_DENSITY = 2, DERR_STREAM = 4, DERR_TIMEOUT = 8 };
+
+struct DevTables {
+  // 1D spline, SPot1D (mc_poten.cc:379-438,624-639)
+  int n1d;
+  const double *g1d, *p1d, *y21d;
+  double alpha1d, unode1d, c61d;
+  // 2D bilinear, LPot2D (mc_poten.cc:688-729)
+  int nr2d, nc2d;
+  double dr2d, dc2d;
+  const double *rg2d, *cg2d, *pot2d;
+  // 3D, vcord/vcalc (vcord.f, vcalc.f) on a generalised angular grid
+  int rgrd, thgrd, chgrd, chfold;
+  double rvmin, rvmax, rvstep, dth3, dch3;
+  const double *vtab;
+  const float *vtab32;
+  // linear rotor density, SRotDens (mc_poten.cc:548-622)
+  int nrot;
+  const double *rg, *rd, *rdv, *rde, *rd_y2, *rdv_y2, *rde_y2;
+  // nonlinear rotor density, rotden/rotpro (rotden.f, rotpro_sub.f)
+  int nth, nph, nch;
+  double dthd, dphd, dchd;
+  const double *rho, *erot, *esq;
+  const float *rho32;
+  // spherical rotor-atom table, vspher (vspher.f)
+  int nsph;
+  double sph_r0, sph_rmax, sph_rstep;
+  const double *sph;
+};
+
+struct DevSys {
+  int na, nap;                 // atoms, padded row length of the slice-major arrays
+  int P, Q, R;                 // NumbTimes, NumbRotTimes, RotRatio
+  int ntypes, imtype, nrotors, rot_first;   // rotor type, its count, its first global atom
+  int numb[2], molecule[2], stat[2], levels[2], first[2];
+  double lambda[2], mcstep[2];
+  double tau, rot_tau, beta, temperature, rtstep;
+  int ispher, rot_den_type, rot_odevn, rn_ratio;
+  double rot_eoff, abc[3];
+  int minimage;
+  double box[3];
+  int mixed;                   // 1: FP32 table interpolation with FP64 sums
+};
+
+// path state on the device
+//   x/y/z[t*nap + a]: bead of global atom a at slice t (slice-major so a
+//   partner sweep at one slice is a unit-stride read);
+//   ang[k*nrotors*Q + r*Q + q], k = {phi, cos theta, chi}: rotor r at rotational slice q;
+//   cosv[k*nrotors*Q + r*Q + q]: its unit vector (MCCosine).
+struct DevState {
+  double *x, *y, *z;
+  double *ang, *cosv;
+  int *pindex;
+  int *mctype;
+  unsigned int *err;
+};
+
+struct Ctx {
+  DevSys s;
+  DevTables t;
+  DevState st;
+};
+
+// ------------------------------------------------------------------ frames
+// Body frame of a nonlinear rotor: the columns of matpre(phi, acos(cost), chi)
+// (rotden.f:136-163, vcord.f:31-36) plus |hatz| as dnorm computes it.
+struct Frame {
+  double e[3];          // phi, theta, chi
+  double m[9];          // rotmat(i,j) at m[i*3+j]
+  double hz_norm;
+};
+
+__device__ __forceinline__ void matpre(const double e[3], double m[9])
+{
+  double sp, cp, st, ct, sk, ck;
+  sincos(e[0], &sp, &cp);
+  sincos(e[1], &st, &ct);
+  sincos(e[2], &sk, &ck);
+  m[0] = cp * ct * ck - sp * sk;
+  m[1] = -cp * ct * sk - sp * ck;
+  m[2] = cp * st;
+  m[3] = sp * ct * ck + cp * sk;
+  m[4] = -sp * ct * sk + cp * ck;
+  m[5] = sp * st;
+  m[6] = -st * ck;
+  m[7] = st * sk;
+  m[8] = ct;
+}
+
+__device__ __forceinline__ void make_frame(double phi, double cost, double chi, Frame &f)
+{
+  f.e[0] = phi;
+  f.e[1] = acos(cost);
+  f.e[2] = chi;
+  matpre(f.e, f.m);
+  double s = 0.0;
+  s = s + f.m[2] * f.m[2];
+  s = s + f.m[5] * f.m[5];
+  s = s + f.m[8] * f.m[8];
+  f.hz_norm = sqrt(s);
+}
+
+// ------------------------------------------------------------------ leaves
+
+// splint (mc_utils.cc:156-186): bisection for klo, then the cubic
+__device__ __forceinline__ double splint(const double *__restrict__ xa, const double *__restrict__ ya,
+                                         const double *__restrict__ y2a, int n, double x)
+{
+  int klo = 0, khi = n - 1;
+  while (khi - klo > 1) {
+    int k = (khi + klo) >> 1;
+    if (__ldg(xa + k) > x) khi = k;
+    else klo = k;
+  }
+  double xk = __ldg(xa + khi), xl = __ldg(xa + klo);
+  double h = xk - xl;
+  double a = (xk - x) / h;
+  double b = (x - xl) / h;
+  return a * __ldg(ya + klo) + b * __ldg(ya + khi) +
+         ((a * a * a - a) * __ldg(y2a + klo) + (b * b * b - b) * __ldg(y2a + khi)) * (h * h) / 6.;
+}
+
+// SPot1D (mc_poten.cc:624-639)
+__device__ __forceinline__ double spot1d(const DevTables &t, double r)
+{
+  if (r >= __ldg(t.g1d + t.n1d - 1)) return -t.c61d / pow(r, 6.0);
+  if (r <= __ldg(t.g1d)) return t.unode1d * exp(-t.alpha1d * r);
+  return splint(t.g1d, t.p1d, t.y21d, t.n1d, r);
+}
+
+// LPot2D (mc_poten.cc:688-729): clamped index, unclamped fraction
+__device__ __forceinline__ double lpot2d(const DevTables &t, double r, double cost)
+{
+  double rmin = __ldg(t.rg2d), cmin = __ldg(t.cg2d);
+  int ir = (int)floor((r - rmin) / t.dr2d);
+  int ic = (int)floor((cost - cmin) / t.dc2d);
+  if (ir < 0) ir = 0;
+  else if (ir >= t.nr2d - 1) ir = t.nr2d - 2;
+  if (ic < 0) ic = 0;
+  else if (ic >= t.nc2d - 1) ic = t.nc2d - 2;
+  const double *p = t.pot2d + (size_t)ir * t.nc2d + ic;
+  double y1 = __ldg(p), y4 = __ldg(p + 1);
+  double y2 = __ldg(p + t.nc2d), y3 = __ldg(p + t.nc2d + 1);
+  double r1 = __ldg(t.rg2d + ir), r2 = __ldg(t.rg2d + ir + 1);
+  double c1 = __ldg(t.cg2d + ic), c2 = __ldg(t.cg2d + ic + 1);
+  double dr = (r - r1) / (r2 - r1);
+  double dc = (cost - c1) / (c2 - c1);
+  return (1.0 - dr) * (1.0 - dc) * y1 + dr * (1.0 - dc) * y2 + dr * dc * y3 + (1.0 - dr) * dc * y4;
+}
+
+// SRotDens / SRotDensDeriv / SRotDensEsqrt (mc_poten.cc:548-622)
+__device__ __forceinline__ double srotdens(const DevTables &t, double g, int which)
+{
+  const double *d = which == 0 ? t.rd : (which == 1 ? t.rdv : t.rde);
+  const double *y2 = which == 0 ? t.rd_y2 : (which == 1 ? t.rdv_y2 : t.rde_y2);
+  int n = t.nrot;
+  if (g > __ldg(t.rg + n - 1)) return which == 0 ? __ldg(d + n - 1) : 0.0;
+  if (g < __ldg(t.rg)) {
+    double rl = __ldg(t.rg), rr = __ldg(t.rg + 1);
+    double salpha = (__ldg(d + 1) - __ldg(d)) / (rr - rl);
+    double sbeta = (__ldg(d) * rr - __ldg(d + 1) * rl) / (rr - rl);
+    return salpha * g + sbeta;
+  }
+  return splint(t.rg, d, y2, n, g);
+}
+
+__device__ __forceinline__ double within1(double v)
+{
+  if (v > 1.0) v = 1.0;
+  if (v < -1.0) v = -1.0;
+  return v;
+}
+
+// deleul (rotden.f:32-134): Euler angles of rotma1^T rotmat
+__device__ __forceinline__ void deleul(const double m1[9], const double m2in[9], double rel[3])
+{
+  double m2[9];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) {
+      double s = 0.0;
+      for (int k = 0; k < 3; k++) s = s + m1[k * 3 + i] * m2in[k * 3 + j];
+      m2[i * 3 + j] = s;
+    }
+  const double small = 1.e-08, pi = PIMC_PI;
+  double cost = within1(m2[8]);
+  double theta2 = acos(cost);
+  double sint = sin(theta2);
+  double phi2, chi2, cchi, schi;
+  if (fabs(1.0 - cost) < small) {
+    phi2 = 0.0;
+    cchi = within1(m2[0]);
+    schi = within1(m2[3]);
+    chi2 = (schi > 0.0) ? acos(cchi) : 2.0 * pi - acos(cchi);
+  } else if (fabs(1.0 + cost) < small) {
+    phi2 = 0.0;
+    cchi = within1(m2[4]);
+    schi = within1(m2[1]);
+    chi2 = (schi > 0.0) ? acos(cchi) : 2.0 * pi - acos(cchi);
+  } else {
+    double cphi = within1(m2[2] / sint);
+    double sphi = within1(m2[5] / sint);
+    cchi = within1(-m2[6] / sint);
+    schi = within1(m2[7] / sint);
+    phi2 = (sphi > 0.0) ? acos(cphi) : 2.0 * pi - acos(cphi);
+    chi2 = (schi > 0.0) ? acos(cchi) : 2.0 * pi - acos(cchi);
+  }
+  rel[0] = phi2;
+  rel[1] = theta2;
+  rel[2] = chi2;
+}
+
+// rotden (rotden.f:1-31) -> rotpro (rotpro_sub.f:1-64) on the generalised
+// (theta, phi, chi) grid; returns the rho value, sets *bad on an index out
+// of range (the reference's istop).  which_mask bit0: rho, bit1: erot+esq.
+__device__ __forceinline__ double rotden_rho(const DevTables &t, const Frame &f1, const Frame &f2, int *bad,
+                                            double *erot_out, double *esq_out)
+{
+  double rel[3];
+  deleul(f1.m, f2.m, rel);
+  const double pi = PIMC_PI;
+  double phi = rel[0] * 180.0 / pi;
+  double theta = rel[1] * 180.0 / pi;
+  double chi = rel[2] * 180.0 / pi;
+  double xc = chi / t.dchd, xp = phi / t.dphd, xt = theta / t.dthd;
+  int ichi = (int)xc, iphi = (int)xp, ith = (int)xt;
+  if (ichi > t.nch - 1 || ichi < 0) { ichi = 0; *bad = 1; }
+  if (iphi > t.nph - 1 || iphi < 0) { iphi = 0; *bad = 1; }
+  if (ith > t.nth - 1 || ith < 0) { ith = 0; *bad = 1; }
+  size_t nph = t.nph, nch = t.nch;
+  size_t i0 = ((size_t)ith * nph + iphi) * nch + ichi;
+  double fc = xc - (double)ichi, fp = xp - (double)iphi, ft = xt - (double)ith;
+  double r0 = __ldg(t.rho + i0);
+  double dc = 0.0, dp = 0.0, dt = 0.0;
+  size_t ic = i0 + 1, ip = i0 + nch, itt = i0 + nph * nch;
+  if (ichi != t.nch - 1) dc = __ldg(t.rho + ic) - r0;
+  if (iphi != t.nph - 1) dp = __ldg(t.rho + ip) - r0;
+  if (ith != t.nth - 1) dt = __ldg(t.rho + itt) - r0;
+  double rho = r0 + dc * fc + dp * fp + dt * ft;
+  if (erot_out) {
+    double e0 = __ldg(t.erot + i0), s0 = __ldg(t.esq + i0);
+    double ec = 0, ep = 0, et = 0, sc = 0, sp = 0, st = 0;
+    if (ichi != t.nch - 1) { ec = __ldg(t.erot + ic) - e0; sc = __ldg(t.esq + ic) - s0; }
+    if (iphi != t.nph - 1) { ep = __ldg(t.erot + ip) - e0; sp = __ldg(t.esq + ip) - s0; }
+    if (ith != t.nth - 1) { et = __ldg(t.erot + itt) - e0; st = __ldg(t.esq + itt) - s0; }
+    *erot_out = (e0 + ec * fc + ep * fp + et * ft) / PIMC_WNO2K;
+    *esq_out = (s0 + sc * fc + sp * fp + st * ft) / (PIMC_WNO2K * PIMC_WNO2K);
+  }
+  return rho;
+}
+
+// rsrot (rotden.f:218-286): outputs written only for iodevn == -1
+__device__ __forceinline__ void rsrot(const Frame &f1, const Frame &f2, const double abc[3], double tauC, int iodevn,
+                                      double *rho, double *erot)
+{
+  double tau = tauC / PIMC_WNO2K;
+  double b0 = 1.0 / abc[0], b1 = 1.0 / abc[1], b2 = 1.0 / abc[2];
+  double dig[3];
+  for (int i = 0; i < 3; i++) {
+    double s = 0.0;
+    for (int j = 0; j < 3; j++) s = s + f1.m[j * 3 + i] * f2.m[j * 3 + i];
+    dig[i] = s;
+  }
+  double sumaxs = (b0 - b1 - b2) * (1.0 - dig[0]) + (b1 - b2 - b0) * (1.0 - dig[1]) + (b2 - b0 - b1) * (1.0 - dig[2]);
+  if (iodevn == -1) {
+    *rho = sumaxs;
+    double e = sumaxs / (4.0 * tau * tau);
+    e = e + 1.5 / tau + 0.25 * (abc[0] + abc[1] + abc[2]);
+    *erot = e / PIMC_WNO2K;
+  }
+}
+
+// rsline (rotden.f:356-375)
+__device__ __forceinline__ void rsline(double brot, double dprd, double tauC, double *rho, double *erot)
+{
+  double tau = tauC / PIMC_WNO2K;
+  double r = (1.0 - dprd) / (2.0 * brot * tau);
+  double e = (1.0 - r) / tau;
+  *rho = -r;
+  *erot = e / PIMC_WNO2K;
+}
+
+__device__ __forceinline__ double dot3(const double *a, const double *b)
+{
+  double d = 0.0;
+  d = d + a[0] * b[0];
+  d = d + a[1] * b[1];
+  d = d + a[2] * b[2];
+  return d;
+}
+
+// vcord (vcord.f:1-98) + vcalc (vcalc.f:1-65) for an atom at rpt around a
+// rotor at rcom with body frame f; optional (r, theta, chi) returns
+__device__ __forceinline__ double vcord(const DevTables &t, const Frame &f, double rcx, double rcy, double rcz,
+                                       double rpx, double rpy, double rpz, double *rr = nullptr,
+                                       double *th = nullptr, double *chr = nullptr)
+{
+  const double pi = PIMC_PI, small = 1.e-08, bo2ang = 0.529177249;
+  double R[3] = {rpx - rcx, rpy - rcy, rpz - rcz};
+  double hx[3] = {f.m[0], f.m[3], f.m[6]};
+  double hy[3] = {f.m[1], f.m[4], f.m[7]};
+  double hz[3] = {f.m[2], f.m[5], f.m[8]};
+  double rn = sqrt(dot3(R, R));
+  double da = dot3(hz, R) / (f.hz_norm * rn);
+  if (da > 1.0) da = 1.0;
+  if (da < -1.0) da = -1.0;
+  double thewff = acos(da);
+  double rdotx = dot3(R, hx), rdoty = dot3(R, hy);
+  double chiwff;
+  if (fabs(rdotx) < small) chiwff = pi / 2.0;
+  else chiwff = atan(fabs(rdoty / rdotx));
+  double chir;
+  if (rdotx >= 0.0 && rdoty >= 0.0) chir = chiwff;
+  else if (rdotx < 0.0 && rdoty >= 0.0) chir = pi - chiwff;
+  else if (rdotx < 0.0 && rdoty < 0.0) chir = pi + chiwff;
+  else chir = 2 * pi - chiwff;
+  if (t.chfold == 180) {
+    chiwff = chir;
+    if (chir > pi) chiwff = 2 * pi - chir;
+  } else if (t.chfold == 360) {
+    chiwff = chir;
+  }
+  if (rr) { *rr = rn; *th = thewff; *chr = chir; }
+  double r = rn / bo2ang;
+  double xth = (thewff * 180.0 / pi) / t.dth3;
+  double xch = (chiwff * 180.0 / pi) / t.dch3;
+  // vcalc
+  int maxrpt = t.rgrd - 1, mxthpt = t.thgrd - 1, mxchpt = t.chgrd - 1;
+  if (r < t.rvmin) r = t.rvmin;
+  if (r > t.rvmax) r = t.rvmax;
+  int ir = (int)((r - t.rvmin) / t.rvstep);
+  if (ir > maxrpt) ir = maxrpt;
+  int ith = (int)xth, ich = (int)xch;
+  if (ich > mxchpt) ich = mxchpt;
+  if (ich < 0) ich = 0;
+  if (ith > mxthpt) ith = mxthpt;
+  if (ith < 0) ith = 0;
+  size_t nth = t.thgrd, nch = t.chgrd;
+  size_t i0 = ((size_t)ir * nth + ith) * nch + ich;
+  double v0 = __ldg(t.vtab + i0);
+  double gradr = 0.0, delr = 0.0, gradth = 0.0, delth = 0.0, gradch = 0.0, delch = 0.0;
+  if (ir != maxrpt) {
+    gradr = (__ldg(t.vtab + i0 + nth * nch) - v0) / t.rvstep;
+    delr = r - (t.rvmin + ir * t.rvstep);
+  }
+  if (ith != mxthpt) {
+    gradth = (__ldg(t.vtab + i0 + nch) - v0);
+    delth = xth - (double)ith;
+  }
+  if (ich != mxchpt) {
+    gradch = (__ldg(t.vtab + i0 + 1) - v0);
+    delch = xch - (double)ich;
+  }
+  return v0 + gradr * delr + gradth * delth + gradch * delch;
+}
+
+// the FP32 form of vcord for the mixed-precision path: same grid logic in
+// float arithmetic on the float copy of the table
+__device__ __forceinline__ float vcord32(const DevTables &t, const float m[9], float hzn, float Rx, float Ry, float Rz)
+{
+  const float pi = 3.14159265358979f, small = 1.e-8f;
+  float rn = sqrtf(Rx * Rx + Ry * Ry + Rz * Rz);
+  float dz = m[2] * Rx + m[5] * Ry + m[8] * Rz;
+  float da = fminf(1.0f, fmaxf(-1.0f, dz / (hzn * rn)));
+  float thewff = acosf(da);
+  float rdotx = m[0] * Rx + m[3] * Ry + m[6] * Rz;
+  float rdoty = m[1] * Rx + m[4] * Ry + m[7] * Rz;
+  float chiwff = (fabsf(rdotx) < small) ? 0.5f * pi : atanf(fabsf(rdoty / rdotx));
+  float chir;
+  if (rdotx >= 0.0f && rdoty >= 0.0f) chir = chiwff;
+  else if (rdotx < 0.0f && rdoty >= 0.0f) chir = pi - chiwff;
+  else if (rdotx < 0.0f && rdoty < 0.0f) chir = pi + chiwff;
+  else chir = 2.0f * pi - chiwff;
+  if (t.chfold == 180) chiwff = (chir > pi) ? 2.0f * pi - chir : chir;
+  else if (t.chfold == 360) chiwff = chir;
+  float r = rn * (float)(1.0 / 0.529177249);
+  float xth = thewff * (float)(180.0 / PIMC_PI / t.dth3);
+  float xch = chiwff * (float)(180.0 / PIMC_PI / t.dch3);
+  float rvmin = (float)t.rvmin, rvmax = (float)t.rvmax, rstep = (float)t.rvstep;
+  r = fminf(fmaxf(r, rvmin), rvmax);
+  int maxrpt = t.rgrd - 1, mxthpt = t.thgrd - 1, mxchpt = t.chgrd - 1;
+  int ir = min((int)((r - rvmin) / rstep), maxrpt);
+  int ith = min(max((int)xth, 0), mxthpt), ich = min(max((int)xch, 0), mxchpt);
+  size_t nth = t.thgrd, nch = t.chgrd;
+  size_t i0 = ((size_t)ir * nth + ith) * nch + ich;
+  float v0 = __ldg(t.vtab32 + i0);
+  float v = v0;
+  if (ir != maxrpt) v += (__ldg(t.vtab32 + i0 + nth * nch) - v0) / rstep * (r - (rvmin + ir * rstep));
+  if (ith != mxthpt) v += (__ldg(t.vtab32 + i0 + nch) - v0) * (xth - (float)ith);
+  if (ich != mxchpt) v += (__ldg(t.vtab32 + i0 + 1) - v0) * (xch - (float)ich);
+  return v;
+}
+
+// caleng (caleng_tip4p_gg.f:2-186).  kcal2k is an INTEGER parameter in the
+// Fortran source (implicit typing), so the LJ term is scaled by 503.
+__device__ __forceinline__ double caleng(const Frame &f1, const Frame &f2, double c1x, double c1y, double c1z,
+                                         double c2x, double c2y, double c2z)
+{
+  const double qm = -1.04, qh = 0.520, br2ang = 0.52917721092, hr2k = 3.1577465e5, kcal2k = 503.0;
+  const double site[4][3] = {{0.0, 0.0, 0.06562}, {0.0, 0.0, -0.08438}, {0.7557, 0.0, -0.5223}, {-0.7557, 0.0, -0.5223}};
+  double a[4][3], b[4][3];   // O, M, H1, H2 in the space frame
+  const double c1[3] = {c1x, c1y, c1z}, c2[3] = {c2x, c2y, c2z};
+  for (int s = 0; s < 4; s++)
+    for (int i = 0; i < 3; i++) {
+      double u = c1[i], v = c2[i];
+      for (int j = 0; j < 3; j++) {
+        u = u + f1.m[i * 3 + j] * site[s][j];
+        v = v + f2.m[i * 3 + j] * site[s][j];
+      }
+      a[s][i] = u;
+      b[s][i] = v;
+    }
+  double roo = 0.0, rmm = 0.0;
+  for (int i = 0; i < 3; i++) {
+    roo = roo + (a[0][i] - b[0][i]) * (a[0][i] - b[0][i]);
+    rmm = rmm + (a[1][i] - b[1][i]) * (a[1][i] - b[1][i]);
+  }
+  rmm = sqrt(rmm);
+  double roo4 = roo * roo, roo6 = roo4 * roo, roo12 = roo6 * roo6;
+  double vlj = 6.e5 / roo12 - 610.0 / roo6;
+  auto d = [](const double *p, const double *q) {
+    double s = 0.0;
+    for (int i = 0; i < 3; i++) s = s + (p[i] - q[i]) * (p[i] - q[i]);
+    return sqrt(s);
+  };
+  double vmh = qm * qh * (1.0 / d(a[1], b[2]) + 1.0 / d(a[1], b[3]) + 1.0 / d(b[1], a[2]) + 1.0 / d(b[1], a[3]));
+  double vhh = qh * qh * (1.0 / d(a[2], b[2]) + 1.0 / d(a[2], b[3]) + 1.0 / d(a[3], b[2]) + 1.0 / d(a[3], b[3]));
+  double vmm = qm * qm * (1.0 / rmm);
+  return vlj * kcal2k + (vmh + vmm + vhh) * hr2k * br2ang;
+}
+
+// vspher (vspher.f:12-544) on the supplied table
+__device__ __forceinline__ double vspher(const DevTables &t, double r)
+{
+  const double ang2bo = (double)0.5291772f;
+  int maxrpt = t.nsph - 1;
+  r = r / ang2bo;
+  if (r < t.sph_r0) r = t.sph_r0;
+  if (r > t.sph_rmax) r = t.sph_rmax;
+  int ir = (int)((r - t.sph_r0) / t.sph_rstep);
+  if (ir > maxrpt) ir = maxrpt;
+  double v0 = __ldg(t.sph + ir);
+  if (ir == maxrpt) return v0;
+  return v0 + (__ldg(t.sph + ir + 1) - v0) / t.sph_rstep * (r - (t.sph_r0 + ir * t.sph_rstep));
+}
+
+// ---------------------------------------------------------- Philox 4x32-10
+// Counter-based generator of Salmon et al., "Parallel random numbers: as
+// easy as 1, 2, 3" (SC'11): ten rounds of two 32x32->64 multiplies with the
+// published multipliers and Weyl key increments.
+struct U4 { uint32_t x, y, z, w; };
+
+__device__ __forceinline__ U4 philox4x32(U4 c, uint32_t k0, uint32_t k1)
+{
+  const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u, W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#pragma unroll
+  for (int i = 0; i < 10; i++) {
+    uint32_t hi0 = __umulhi(M0, c.x), lo0 = M0 * c.x;
+    uint32_t hi1 = __umulhi(M1, c.z), lo1 = M1 * c.z;
+    U4 n = {hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0};
+    c = n;
+    k0 += W0;
+    k1 += W1;
+  }
+  return c;
+}
+
+// two uniforms in (0,1) with 53-bit resolution from one Philox block
+__device__ __forceinline__ void philox_u2(uint64_t seed, uint64_t a, uint32_t b, uint32_t c, double *u0, double *u1)
+{
+  U4 ctr = {(uint32_t)a, (uint32_t)(a >> 32), b, c};
+  U4 r = philox4x32(ctr, (uint32_t)seed, (uint32_t)(seed >> 32));
+  uint64_t v0 = ((uint64_t)r.x << 21) ^ (uint64_t)r.y;
+  uint64_t v1 = ((uint64_t)r.z << 21) ^ (uint64_t)r.w;
+  *u0 = ((double)(v0 & ((1ull << 53) - 1)) + 0.5) * (1.0 / 9007199254740992.0);
+  *u1 = ((double)(v1 & ((1ull << 53) - 1)) + 0.5) * (1.0 / 9007199254740992.0);
+}

@@ -1,0 +1,26 @@
+// pimc_launch.h -- host-callable launchers of the kernels in pimc_kernels.cu
+#pragma once
+#include "pimc_internal.cuh"
+
+struct ReplaySrc;
+struct MolScratch;
+
+void launch_frames_init(const Ctx &c, Frame *frames, cudaStream_t s);
+void launch_bisect_replay(const Ctx &c, Frame *f, int type, int time0, int exch, ReplaySrc src, double *ds, int *lvl,
+                          unsigned long long *cnt, cudaStream_t s);
+void launch_bisect_phase(const Ctx &c, Frame *f, int type, int s0, int j, unsigned phase, uint64_t seed,
+                         const unsigned *pass, unsigned long long *cnt, cudaStream_t s);
+void launch_rot_replay(const Ctx &c, Frame *f, int parity, const double *urot, long nurot, double *rd, int *acc,
+                       unsigned long long *cnt, cudaStream_t s);
+void launch_rot_phase(const Ctx &c, Frame *f, int parity, unsigned phase, uint64_t seed, const unsigned *pass,
+                      unsigned long long *cnt, cudaStream_t s);
+void launch_mol(const Ctx &c, Frame *f, int type, int atom, bool replay, ReplaySrc src, uint64_t seed,
+                const unsigned *pass, unsigned phase, MolScratch *ms, double *dv, int *acc, unsigned long long *cnt,
+                cudaStream_t s);
+void launch_q_slice(const Ctx &c, Frame *f, int n, const int *a0, const int *it, const double *xyz, double *out,
+                    cudaStream_t s);
+void launch_q_rot(const Ctx &c, Frame *f, int n, const int *rot, const int *it, const double *v3, int linear,
+                  double *out, cudaStream_t s);
+void launch_est(const Ctx &c, Frame *f, double *kin, double *pot, double *rot, double *rcf, cudaStream_t s);
+void launch_pass_begin(unsigned *pass, cudaStream_t s);
+size_t mol_scratch_bytes();

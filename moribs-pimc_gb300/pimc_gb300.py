@@ -1,0 +1,207 @@
+"""ctypes binding of libpimc_gb300.so (include/pimc_gb300.h).
+
+This module only marshals arrays; every computation runs in the CUDA
+library.  Loading fails loudly when the library has not been built: there is
+no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from pimc_types import PimcSystem, PimcTables, STATUS, dptr, iptr, make_system, make_tables
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIBPATH = os.path.join(HERE, "libpimc_gb300.so")
+REPO = os.path.dirname(HERE)
+HEADERS = [os.path.join(REPO, "include", "pimc_gb300.h")]
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+_lp = C.POINTER(C.c_long)
+_L = None
+
+
+class PimcError(RuntimeError):
+    def __init__(self, code, what):
+        super().__init__("%s failed: %s (%d)" % (what, STATUS.get(code, "?"), code))
+        self.code = code
+
+
+def load(path=LIBPATH):
+    """Load the CUDA library; raises if it is missing."""
+    global _L
+    if _L is not None:
+        return _L
+    if not os.path.exists(path):
+        raise RuntimeError("libpimc_gb300.so not built at %s: run __graft_entry__.build()" % path)
+    L = C.CDLL(path)
+    vp = C.c_void_p
+    L.pimc_create.argtypes = [C.POINTER(PimcSystem), C.c_int, C.POINTER(vp)]
+    L.pimc_destroy.argtypes = [vp]
+    L.pimc_load_tables.argtypes = [vp, C.POINTER(PimcTables)]
+    L.pimc_set_state.argtypes = [vp, _dp, _dp, _ip]
+    L.pimc_get_state.argtypes = [vp, _dp, _dp, _dp, _ip]
+    L.pimc_molecular_move.argtypes = [vp, C.c_int, _dp, C.c_long, _dp, C.c_long, _lp, _dp, _ip]
+    L.pimc_bisection_move.argtypes = [vp, C.c_int, C.c_int, C.c_int, _dp, C.c_long, _dp, C.c_long, _lp, _dp, _ip]
+    L.pimc_rotations_move.argtypes = [vp, _dp, C.c_long, _dp, _ip]
+    L.pimc_pot_energy.argtypes = [vp, C.c_int, _ip, _ip, _dp, _dp]
+    L.pimc_pot_rot_energy.argtypes = [vp, C.c_int, _ip, _ip, _dp, _dp]
+    L.pimc_estimators.argtypes = [vp, _dp]
+    L.pimc_rcf.argtypes = [vp, _dp]
+    L.pimc_run_passes.argtypes = [vp, C.c_int, C.c_uint64]
+    L.pimc_counters.argtypes = [vp, _dp, _dp]
+    L.pimc_reset_counters.argtypes = [vp]
+    L.pimc_synchronize.argtypes = [vp]
+    L.pimc_set_precision.argtypes = [vp, C.c_int]
+    L.pimc_bead_moves_per_pass.restype = C.c_double
+    L.pimc_bead_moves_per_pass.argtypes = [vp]
+    L.pimc_launch_count.restype = C.c_longlong
+    L.pimc_launch_count.argtypes = [vp]
+    L.pimc_stream.restype = vp
+    L.pimc_stream.argtypes = [vp]
+    L.pimc_status_string.restype = C.c_char_p
+    L.pimc_status_string.argtypes = [C.c_int]
+    _L = L
+    return L
+
+
+def declared_symbols():
+    """Names of the functions declared in include/pimc_gb300.h."""
+    import re
+    names = []
+    for h in HEADERS:
+        txt = open(h).read()
+        names += re.findall(r"^\s*(?:pimc_status|double|long long|void\s*\*|const char\s*\*)\s*(pimc_\w+)\s*\(", txt, re.M)
+    return names
+
+
+def _chk(code, what):
+    if code != 0:
+        raise PimcError(code, what)
+
+
+class Sampler:
+    """One pimc_handle: a system, its tables and its path on one GPU."""
+
+    def __init__(self, w, device=0, mixed=False):
+        self.L = load()
+        self.w = w
+        self.na = w.natoms
+        self.P = w.nslices
+        self.sys = make_system(w)
+        h = C.c_void_p()
+        _chk(self.L.pimc_create(C.byref(self.sys), device, C.byref(h)), "pimc_create")
+        self.h = h
+        tabs, keep = make_tables(w)
+        _chk(self.L.pimc_load_tables(self.h, C.byref(tabs)), "pimc_load_tables")
+        if mixed:
+            _chk(self.L.pimc_set_precision(self.h, 1), "pimc_set_precision")
+        if w.coords is not None:
+            self.set_state(w.coords, w.angles, w.pindex)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.pimc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # path
+    def set_state(self, coords=None, angles=None, pindex=None):
+        c = None if coords is None else np.ascontiguousarray(coords, dtype=np.float64)
+        a = None if angles is None else np.ascontiguousarray(angles, dtype=np.float64)
+        p = None if pindex is None else np.ascontiguousarray(pindex, dtype=np.int32)
+        _chk(self.L.pimc_set_state(self.h, dptr(c) if c is not None else None, dptr(a) if a is not None else None,
+                                   iptr(p) if p is not None else None), "pimc_set_state")
+
+    def get_state(self):
+        nb = self.na * self.P
+        c = np.zeros((3, nb)); a = np.zeros((3, nb)); co = np.zeros((3, nb)); p = np.zeros(self.na, np.int32)
+        _chk(self.L.pimc_get_state(self.h, dptr(c), dptr(a), dptr(co), iptr(p)), "pimc_get_state")
+        return c, a, co, p
+
+    # replay moves
+    def bisection_move(self, type_, time, gauss, u3, exchange=False):
+        g = np.ascontiguousarray(gauss, dtype=np.float64)
+        u = np.ascontiguousarray(u3, dtype=np.float64)
+        t = self.w.types[type_]
+        ds = np.zeros(t["numb"] * t["levels"]); lv = np.zeros(t["numb"], np.int32)
+        cons = (C.c_long * 2)()
+        st = self.L.pimc_bisection_move(self.h, type_, int(time), int(exchange), dptr(g), len(g), dptr(u), len(u),
+                                        cons, dptr(ds), iptr(lv))
+        return st, ds.reshape(t["numb"], t["levels"]), lv, (cons[0], cons[1])
+
+    def molecular_move(self, type_, u1, u2):
+        a = np.ascontiguousarray(u1, dtype=np.float64)
+        b = np.ascontiguousarray(u2, dtype=np.float64)
+        n = self.w.types[type_]["numb"]
+        dv = np.zeros(n); acc = np.zeros(n, np.int32)
+        cons = (C.c_long * 2)()
+        st = self.L.pimc_molecular_move(self.h, type_, dptr(a), len(a), dptr(b), len(b), cons, dptr(dv), iptr(acc))
+        return st, dv, acc, (cons[0], cons[1])
+
+    def rotations(self, urot):
+        u = np.ascontiguousarray(urot, dtype=np.float64)
+        rt = [t for t in self.w.types if t["molecule"] != 0][0]
+        n = self.w.nrotslices * rt["numb"]
+        rd = np.zeros(n); acc = np.zeros(n, np.int32)
+        st = self.L.pimc_rotations_move(self.h, dptr(u), len(u), dptr(rd), iptr(acc))
+        return st, rd, acc
+
+    # energies
+    def pot_energy(self, atom0, it, xyz):
+        a = np.ascontiguousarray(atom0, dtype=np.int32)
+        t = np.ascontiguousarray(it, dtype=np.int32)
+        x = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1)
+        out = np.zeros(len(a))
+        _chk(self.L.pimc_pot_energy(self.h, len(a), iptr(a), iptr(t), dptr(x), dptr(out)), "pimc_pot_energy")
+        return out
+
+    def pot_rot_energy(self, rotor, it, v3):
+        a = np.ascontiguousarray(rotor, dtype=np.int32)
+        t = np.ascontiguousarray(it, dtype=np.int32)
+        x = np.ascontiguousarray(v3, dtype=np.float64).reshape(-1)
+        out = np.zeros(len(a))
+        _chk(self.L.pimc_pot_rot_energy(self.h, len(a), iptr(a), iptr(t), dptr(x), dptr(out)), "pimc_pot_rot_energy")
+        return out
+
+    def estimators(self):
+        out = np.zeros(5)
+        _chk(self.L.pimc_estimators(self.h, dptr(out)), "pimc_estimators")
+        return out
+
+    def rcf(self):
+        out = np.zeros(self.w.nrotslices)
+        _chk(self.L.pimc_rcf(self.h, dptr(out)), "pimc_rcf")
+        return out
+
+    # production
+    def run_passes(self, n, seed):
+        _chk(self.L.pimc_run_passes(self.h, int(n), C.c_uint64(seed)), "pimc_run_passes")
+
+    def synchronize(self):
+        _chk(self.L.pimc_synchronize(self.h), "pimc_synchronize")
+
+    def counters(self):
+        tot = np.zeros(6); acc = np.zeros(6)
+        _chk(self.L.pimc_counters(self.h, dptr(tot), dptr(acc)), "pimc_counters")
+        return tot, acc
+
+    def reset_counters(self):
+        _chk(self.L.pimc_reset_counters(self.h), "pimc_reset_counters")
+
+    def bead_moves_per_pass(self):
+        return self.L.pimc_bead_moves_per_pass(self.h)
+
+    def launch_count(self):
+        return self.L.pimc_launch_count(self.h)
+
+    def stream(self):
+        return self.L.pimc_stream(self.h)
