@@ -1,0 +1,337 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 sampling path: bead-moves/s on the config-1 system
+(1 asymmetric-top SO2-like rotor + 64 para-H2, T = 0.37 K, P = 1024
+translational / Q = 256 rotational slices, 200x60x60 rotor-atom potential,
+61x121x121 rotational density), synthetic seeded tables.
+
+A step is one pass of the reference schedule (mc_main.cc:348-381): per type
+one centroid move per atom, N*P bisections of 2^L - 1 beads, and P sweeps of
+the Q rotational slices.  Bead-moves per pass are counted as the reference
+schedule counts them.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+--impl reference times the CPU restatement of the reference path (the oracle
+port, OpenMP over the host cores, the reference schedule) on a bounded sample
+of the same workload; the reference's compiled objects are x86 builds of
+this container and cannot run on the Arm GPU host.
+Under torchrun (N > 1) every rank runs an independent replica on its own GPU
+(the path does not shard); value is all ranks' bead-moves over the slowest
+rank's time.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(REPO, "moribs-pimc_gb300")
+for p in (PKG, os.path.join(REPO, "oracle")):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+METRIC = "bead-moves/s on 1 GB300: plain vs surrogate+batched, at matched <E> error"
+UNIT = "bead-moves/s"
+WORKLOAD = "config1: 1 asymmetric-top SO2 + 64 pH2, T=0.37 K, P=1024, Q=256, L=3, plain method"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
+
+
+def dist_init(world):
+    if world <= 1:
+        return None
+    import torch.distributed as dist
+    dist.init_process_group(backend="gloo")
+    return dist
+
+
+def reduce_max(dist, x):
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def workload(rank=0):
+    import workloads as W
+    return W.config1(seed=4321 + 17 * rank)
+
+
+def host_cpu():
+    try:
+        model = ""
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith(("model name", "cpu part")):
+                    model = line.split(":", 1)[1].strip()
+                    break
+        return model
+    except OSError:
+        return ""
+
+
+def cpu_baseline(w, seconds, nthreads):
+    """The oracle restatement of the reference schedule on the host cores:
+    time slices 0, 1, ... (centroid moves at slice 0) until `seconds` pass."""
+    import oracle as O
+    O.build_oracle()
+    o = O.Oracle(w)
+    done_t = 0
+    bm = 0.0
+    t0 = time.perf_counter()
+    chunk = 8
+    while True:
+        st, b = o.run_steps(done_t, chunk, seed=99, nthreads=nthreads)
+        if st != 0:
+            raise RuntimeError("oracle run_steps failed: %d" % st)
+        bm += b
+        done_t += chunk
+        el = time.perf_counter() - t0
+        if el >= seconds or done_t >= w.nslices:
+            break
+    rate = bm / el
+    sample = ("oracle port of the reference schedule, time slices 0..%d of one pass of %s "
+              "(%.3g bead-moves, %.1f s)" % (done_t - 1, WORKLOAD.split(":")[0], bm, el))
+    return rate, sample
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, dev):
+        self.dev = dev
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.dev),
+                 "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+                 "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.p.terminate()
+        try:
+            out, _ = self.p.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+            out, _ = self.p.communicate()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs"), "measured"
+    except (OSError, ValueError):
+        return 6800.0, "fallback"
+
+
+def rotation_phase_bytes(w):
+    """Compulsory bytes of one rotational phase launch (Q/2 slice moves):
+    per slice and rotor, 2*R*(N-1) rotor-atom pair evaluations each reading
+    the partner bead (24 B) and 4 table corners (32 B), plus 4 rotational
+    density lookups of 4 corners (32 B) and the 3 neighbouring orientations
+    (3 x 24 B), plus the rotor's R beads (24 B each)."""
+    P, Q = w.nslices, w.nrotslices
+    R = P // Q
+    na = w.natoms
+    nr = sum(t["numb"] for t in w.types if t["molecule"] != 0)
+    per_slice = nr * (2 * R * (na - 1) * (24 + 32) + 4 * 32 + 3 * 24 + R * 24)
+    return (Q // 2) * per_slice
+
+
+def bisection_phase_bytes(w, type_):
+    """Compulsory bytes of one bisection phase launch (P/M window moves, all
+    levels executed): each of the 2(M-1) slice energies reads N-1 partner beads
+    (24 B) and 4 spline words (32 B)."""
+    t = w.types[type_]
+    M = 1 << t["levels"]
+    na = w.natoms
+    return (w.nslices // M) * (2 * (M - 1) * (na - 1) * (24 + 32))
+
+
+def run_gb300(args, rank, local, world, dist):
+    import numpy as np
+    import torch
+    import pimc_gb300 as G
+
+    torch.cuda.set_device(local)
+    w = workload(rank)
+    s = G.Sampler(w, device=local, mixed=(args.precision == "mixed"))
+    bm_pass = s.bead_moves_per_pass()
+    seed = 1000 + rank
+    ext = torch.cuda.ExternalStream(s.stream(), device=torch.device("cuda", local))
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")   # 256 MiB > 129 MB L2
+    # warm-up: graph instantiation + W passes
+    s.run_passes(args.warmup, seed)
+    s.synchronize()
+    barrier(dist)
+    torch.cuda.synchronize()
+    clocks = Clocks(local)
+    clocks.start()
+    time.sleep(0.3)
+    l0 = s.launch_count()
+    evs = []
+    with torch.cuda.stream(ext):
+        for k in range(args.steps):
+            flush.zero_()                         # L2 flush outside the timed events
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(ext)
+            s.run_passes(1, seed)
+            e1.record(ext)
+            evs.append((e0, e1))
+    s.synchronize()
+    torch.cuda.synchronize()
+    l1 = s.launch_count()
+    ck = clocks.stop()
+    barrier(dist)
+    step_ms = [a.elapsed_time(b) for a, b in evs]
+    total_ms = reduce_max(dist, sum(step_ms))
+    value = bm_pass * args.steps * world / (total_ms / 1e3)
+    tot, acc = s.counters()
+
+    # ---- roofline of the dominant kernel from a live per-kind profile
+    ms, nl = s.profile_pass(seed + 7)
+    kinds = ["centroid", "bisection", "rotation"]
+    dom = int(np.argmax(ms))
+    if dom == 2:
+        bytes_launch = rotation_phase_bytes(w)
+        kname = "k_rot<false> (rotational even/odd phase)"
+    elif dom == 1:
+        bytes_launch = bisection_phase_bytes(w, 0)
+        kname = "k_bisect_phase (bisection independent-set phase)"
+    else:
+        bytes_launch = 2 * w.nslices * (w.natoms - 1) * 56
+        kname = "k_mol_pairs (centroid partner sums)"
+    per_launch_ms = ms[dom] / max(1, nl[dom])
+    achieved = bytes_launch / (per_launch_ms / 1e3) / 1e9
+    peak, peak_kind = measured_peaks()
+    roofline = {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 5), "traffic": None,
+                "kernel": kname, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
+                "per_launch_us": round(per_launch_ms * 1e3, 3), "algorithmic_bytes_per_launch": bytes_launch,
+                "pass_ms_by_kind": {k: round(v, 3) for k, v in zip(kinds, ms)},
+                "launches_by_kind": {k: int(v) for k, v in zip(kinds, nl)}}
+
+    # ---- end to end through the C ABI with host buffers
+    c, a, co, p = s.get_state()
+    pin_c = torch.from_numpy(c).pin_memory().numpy()
+    pin_a = torch.from_numpy(a).pin_memory().numpy()
+    out_c = torch.empty(c.shape, dtype=torch.float64).pin_memory().numpy()
+    out_a = torch.empty(a.shape, dtype=torch.float64).pin_memory().numpy()
+    out_co = torch.empty(c.shape, dtype=torch.float64).pin_memory().numpy()
+    out_p = np.zeros(w.natoms, np.int32)
+    est = np.zeros(5)
+    barrier(dist)
+    t0 = time.perf_counter()
+    for k in range(args.e2e_steps):
+        G._chk(s.L.pimc_set_state(s.h, G.dptr(pin_c), G.dptr(pin_a), G.iptr(p)), "set_state")
+        s.run_passes(1, seed + 11)
+        G._chk(s.L.pimc_get_state(s.h, G.dptr(out_c), G.dptr(out_a), G.dptr(out_co), G.iptr(out_p)), "get_state")
+        G._chk(s.L.pimc_estimators(s.h, G.dptr(est)), "estimators")
+        pin_c[...] = out_c
+        pin_a[...] = out_a
+    e2e_s = reduce_max(dist, time.perf_counter() - t0)
+    e2e = {"value": bm_pass * args.e2e_steps * world / e2e_s, "unit": UNIT,
+           "h2d_bytes_per_step": int(pin_c.nbytes + pin_a.nbytes + p.nbytes),
+           "d2h_bytes_per_step": int(out_c.nbytes + out_a.nbytes + out_co.nbytes + out_p.nbytes + est.nbytes),
+           "steps": args.e2e_steps, "path": "pimc_set_state + pimc_run_passes(1) + pimc_get_state + pimc_estimators"}
+    s.close()
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+            "data": "synthetic (seeded tables and paths of the config shapes; no dataset)",
+            "config": {"workload": WORKLOAD, "bead_moves_per_pass": bm_pass, "precision": args.precision,
+                       "replicas": world, "l2": "flushed between timed steps (256 MiB write)",
+                       "accept_ratios": {"pH2 centroid": acc[0] / max(1, tot[0]), "pH2 bisection": acc[1] / max(1, tot[1]),
+                                         "rotor bisection": acc[4] / max(1, tot[4]), "rotation": acc[5] / max(1, tot[5])}},
+            "roofline": roofline, "e2e": e2e, "gpu_launches": int(l1 - l0), "clocks": ck}
+    return line, w
+
+
+def main():
+    args = parse()
+    rank, local, world = dist_env()
+    dist = dist_init(world)
+    ncores = os.cpu_count() or 1
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        w = workload(0)
+        rate, sample = cpu_baseline(w, args.cpu_seconds, ncores)
+        line = {"impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": WORKLOAD, "host_cpu": host_cpu()},
+                "cpu_baseline": {"value": rate, "unit": UNIT, "cores": ncores, "kind": "port", "sample": sample},
+                "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return 0
+    line, w = run_gb300(args, rank, local, world, dist)
+    if rank == 0:
+        if not args.no_cpu:
+            rate, sample = cpu_baseline(w, args.cpu_seconds, ncores)
+            line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": ncores, "kind": "port", "sample": sample,
+                                    "host_cpu": host_cpu()}
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -93,6 +93,11 @@ pimc_status pimc_rcf(pimc_handle *h, double *rcf);
  * by seed.  Requires P divisible by every type's 2^levels.  Asynchronous on
  * the handle's stream; errors are reported by the next synchronising call. */
 pimc_status pimc_run_passes(pimc_handle *h, int npasses, uint64_t seed);
+/* Time one pass's launches grouped by move kind (0 centroid, 1 bisection,
+ * 2 rotation), outside the graph, with CUDA events on the handle's stream:
+ * ms[k] = device time of the group, launches[k] = its kernel launches.  The
+ * moves are real moves (the path advances one pass). */
+pimc_status pimc_profile_pass(pimc_handle *h, uint64_t seed, double *ms, long long *launches);
 /* MCTotal / MCAccep (mc_piqmc.h:25-26): total[type*3+kind], kind = molecule,
  * multilevel, rotation */
 pimc_status pimc_counters(pimc_handle *h, double *total, double *accep);

@@ -790,6 +790,62 @@ extern "C" pimc_status pimc_run_passes(pimc_handle *h, int npasses, uint64_t see
   return PIMC_OK;
 }
 
+extern "C" pimc_status pimc_profile_pass(pimc_handle *h, uint64_t seed, double *ms, long long *launches)
+{
+  pimc_status e = ready(h);
+  if (e) return e;
+  if (!ms || !launches) return PIMC_ERR_BAD_ARG;
+  const DevSys &d = h->ctx.s;
+  for (int t = 0; t < d.ntypes; t++)
+    if (d.P % (1 << d.levels[t])) return PIMC_ERR_BAD_ARG;
+  cudaEvent_t ev[6];
+  for (int k = 0; k < 6; k++) CK(cudaEventCreate(&ev[k]));
+  long long n[3] = {0, 0, 0};
+  launch_pass_begin(h->pass, h->stream);
+  std::vector<int> bt, bs, bj;
+  for (int t = 0; t < d.ntypes; t++) {
+    int M = 1 << d.levels[t];
+    for (int s0 = 0; s0 < M; s0++)
+      for (int j = 0; j < d.numb[t]; j++) { bt.push_back(t); bs.push_back(s0); bj.push_back(j); }
+  }
+  unsigned B = (unsigned)bt.size();
+  CK(cudaEventRecord(ev[0], h->stream));
+  for (int t = 0; t < d.ntypes; t++)
+    for (int a = 0; a < d.numb[t]; a++) {
+      ReplaySrc none{};
+      none.err = h->ctx.st.err;
+      launch_mol(h->ctx, h->frames, t, a, false, none, seed, h->pass, B + 2u * (unsigned)d.P + (unsigned)t, h->ms,
+                 nullptr, nullptr, h->cnt, h->stream);
+      n[0] += 3;
+    }
+  CK(cudaEventRecord(ev[1], h->stream));
+  CK(cudaEventRecord(ev[2], h->stream));
+  for (unsigned b = 0; b < B; b++) {
+    launch_bisect_phase(h->ctx, h->frames, bt[b], bs[b], bj[b], b, seed, h->pass, h->cnt, h->stream);
+    n[1]++;
+  }
+  CK(cudaEventRecord(ev[3], h->stream));
+  CK(cudaEventRecord(ev[4], h->stream));
+  if (h->sys.rotation && d.nrotors > 0)
+    for (int it = 0; it < d.P; it++) {
+      launch_rot_phase(h->ctx, h->frames, 0, B + 2u * it, seed, h->pass, h->cnt, h->stream);
+      launch_rot_phase(h->ctx, h->frames, 1, B + 2u * it + 1, seed, h->pass, h->cnt, h->stream);
+      n[2] += 2;
+    }
+  CK(cudaEventRecord(ev[5], h->stream));
+  CK(cudaGetLastError());
+  CK(cudaEventSynchronize(ev[5]));
+  for (int k = 0; k < 3; k++) {
+    float f = 0.f;
+    CK(cudaEventElapsedTime(&f, ev[2 * k], ev[2 * k + 1]));
+    ms[k] = f;
+    launches[k] = n[k];
+  }
+  for (int k = 0; k < 6; k++) cudaEventDestroy(ev[k]);
+  h->launches += 1 + n[0] + n[1] + n[2];
+  return check_err(h);
+}
+
 extern "C" pimc_status pimc_synchronize(pimc_handle *h)
 {
   if (!h) return PIMC_ERR_BAD_ARG;

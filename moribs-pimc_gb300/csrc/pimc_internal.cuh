@@ -226,6 +226,12 @@ __device__ __forceinline__ void deleul(const double m1[9], const double m2in[9],
   rel[2] = chi2;
 }
 
+// Note on the edge guards below (rotpro, vcalc, vspher): the reference tests
+// "index != last" after clamping the index to <= last.  Written that way,
+// ptxas 13.0 at its default optimisation level drops the guarded terms for
+// sm_103a (the same source is correct at -O0); "index < last" is the same
+// condition for a clamped index and compiles correctly.
+//
 // rotden (rotden.f:1-31) -> rotpro (rotpro_sub.f:1-64) on the generalised
 // (theta, phi, chi) grid; returns the rho value, sets *bad on an index out
 // of range (the reference's istop).  which_mask bit0: rho, bit1: erot+esq.
@@ -249,16 +255,16 @@ __device__ __forceinline__ double rotden_rho(const DevTables &t, const Frame &f1
   double r0 = __ldg(t.rho + i0);
   double dc = 0.0, dp = 0.0, dt = 0.0;
   size_t ic = i0 + 1, ip = i0 + nch, itt = i0 + nph * nch;
-  if (ichi != t.nch - 1) dc = __ldg(t.rho + ic) - r0;
-  if (iphi != t.nph - 1) dp = __ldg(t.rho + ip) - r0;
-  if (ith != t.nth - 1) dt = __ldg(t.rho + itt) - r0;
+  if (ichi < t.nch - 1) dc = __ldg(t.rho + ic) - r0;
+  if (iphi < t.nph - 1) dp = __ldg(t.rho + ip) - r0;
+  if (ith < t.nth - 1) dt = __ldg(t.rho + itt) - r0;
   double rho = r0 + dc * fc + dp * fp + dt * ft;
   if (erot_out) {
     double e0 = __ldg(t.erot + i0), s0 = __ldg(t.esq + i0);
     double ec = 0, ep = 0, et = 0, sc = 0, sp = 0, st = 0;
-    if (ichi != t.nch - 1) { ec = __ldg(t.erot + ic) - e0; sc = __ldg(t.esq + ic) - s0; }
-    if (iphi != t.nph - 1) { ep = __ldg(t.erot + ip) - e0; sp = __ldg(t.esq + ip) - s0; }
-    if (ith != t.nth - 1) { et = __ldg(t.erot + itt) - e0; st = __ldg(t.esq + itt) - s0; }
+    if (ichi < t.nch - 1) { ec = __ldg(t.erot + ic) - e0; sc = __ldg(t.esq + ic) - s0; }
+    if (iphi < t.nph - 1) { ep = __ldg(t.erot + ip) - e0; sp = __ldg(t.esq + ip) - s0; }
+    if (ith < t.nth - 1) { et = __ldg(t.erot + itt) - e0; st = __ldg(t.esq + itt) - s0; }
     *erot_out = (e0 + ec * fc + ep * fp + et * ft) / PIMC_WNO2K;
     *esq_out = (s0 + sc * fc + sp * fp + st * ft) / (PIMC_WNO2K * PIMC_WNO2K);
   }
@@ -355,15 +361,15 @@ __device__ __forceinline__ double vcord(const DevTables &t, const Frame &f, doub
   size_t i0 = ((size_t)ir * nth + ith) * nch + ich;
   double v0 = __ldg(t.vtab + i0);
   double gradr = 0.0, delr = 0.0, gradth = 0.0, delth = 0.0, gradch = 0.0, delch = 0.0;
-  if (ir != maxrpt) {
+  if (ir < maxrpt) {
     gradr = (__ldg(t.vtab + i0 + nth * nch) - v0) / t.rvstep;
     delr = r - (t.rvmin + ir * t.rvstep);
   }
-  if (ith != mxthpt) {
+  if (ith < mxthpt) {
     gradth = (__ldg(t.vtab + i0 + nch) - v0);
     delth = xth - (double)ith;
   }
-  if (ich != mxchpt) {
+  if (ich < mxchpt) {
     gradch = (__ldg(t.vtab + i0 + 1) - v0);
     delch = xch - (double)ich;
   }
@@ -401,9 +407,9 @@ __device__ __forceinline__ float vcord32(const DevTables &t, const float m[9], f
   size_t i0 = ((size_t)ir * nth + ith) * nch + ich;
   float v0 = __ldg(t.vtab32 + i0);
   float v = v0;
-  if (ir != maxrpt) v += (__ldg(t.vtab32 + i0 + nth * nch) - v0) / rstep * (r - (rvmin + ir * rstep));
-  if (ith != mxthpt) v += (__ldg(t.vtab32 + i0 + nch) - v0) * (xth - (float)ith);
-  if (ich != mxchpt) v += (__ldg(t.vtab32 + i0 + 1) - v0) * (xch - (float)ich);
+  if (ir < maxrpt) v += (__ldg(t.vtab32 + i0 + nth * nch) - v0) / rstep * (r - (rvmin + ir * rstep));
+  if (ith < mxthpt) v += (__ldg(t.vtab32 + i0 + nch) - v0) * (xth - (float)ith);
+  if (ich < mxchpt) v += (__ldg(t.vtab32 + i0 + 1) - v0) * (xch - (float)ich);
   return v;
 }
 
@@ -456,7 +462,7 @@ __device__ __forceinline__ double vspher(const DevTables &t, double r)
   int ir = (int)((r - t.sph_r0) / t.sph_rstep);
   if (ir > maxrpt) ir = maxrpt;
   double v0 = __ldg(t.sph + ir);
-  if (ir == maxrpt) return v0;
+  if (ir >= maxrpt) return v0;
   return v0 + (__ldg(t.sph + ir + 1) - v0) / t.sph_rstep * (r - (t.sph_r0 + ir * t.sph_rstep));
 }
 

@@ -53,6 +53,7 @@ def load(path=LIBPATH):
     L.pimc_rcf.argtypes = [vp, _dp]
     L.pimc_run_passes.argtypes = [vp, C.c_int, C.c_uint64]
     L.pimc_counters.argtypes = [vp, _dp, _dp]
+    L.pimc_profile_pass.argtypes = [vp, C.c_uint64, _dp, C.POINTER(C.c_longlong)]
     L.pimc_reset_counters.argtypes = [vp]
     L.pimc_synchronize.argtypes = [vp]
     L.pimc_set_precision.argtypes = [vp, C.c_int]
@@ -185,6 +186,12 @@ class Sampler:
     # production
     def run_passes(self, n, seed):
         _chk(self.L.pimc_run_passes(self.h, int(n), C.c_uint64(seed)), "pimc_run_passes")
+
+    def profile_pass(self, seed):
+        ms = np.zeros(3)
+        n = (C.c_longlong * 3)()
+        _chk(self.L.pimc_profile_pass(self.h, C.c_uint64(seed), dptr(ms), n), "pimc_profile_pass")
+        return ms, np.array(list(n))
 
     def synchronize(self):
         _chk(self.L.pimc_synchronize(self.h), "pimc_synchronize")
