@@ -70,6 +70,17 @@ pimc_status pimc_rotations_move(pimc_handle *h, const double *urot, long nrot, d
  * xyz[3k..3k+2] against all other atoms' current beads at slice it[k]. */
 pimc_status pimc_pot_energy(pimc_handle *h, int n, const int *atom0, const int *it, const double *xyz, double *out);
 
+/* No counterpart in the reference.  pimc_pot_energy for callers that must not
+ * have device memory allocated for them after set-up (an application that owns
+ * all device memory through its own pool, or runs under a fixed budget): the
+ * queries and results are staged in a fixed array inside the library, so the
+ * call makes no cudaMalloc/cudaFree.  n <= 4096 (PIMC_ERR_SIZE otherwise).
+ * All calls on a device share the array: calls that overlap on the GPU race
+ * and must be ordered by the caller.  The first call on each device looks up
+ * the array's address; make it before any stream capture. */
+pimc_status pimc_pot_energy_noalloc(pimc_handle *h, int n, const int *atom0, const int *it, const double *xyz,
+                                    double *out);
+
 /* PotRotE3D(rotor, Eulang, it) (mc_piqmc.cc:2046-2151) with v3 = (phi,
  * theta, chi) for a nonlinear rotor, or PotRotEnergy (mc_piqmc.cc:1967-2044)
  * with v3 = the unit vector for the linear rotor; rotor = global atom index. */

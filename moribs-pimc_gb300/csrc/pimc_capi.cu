@@ -895,3 +895,73 @@ extern "C" double pimc_bead_moves_per_pass(const pimc_handle *h)
 extern "C" long long pimc_launch_count(const pimc_handle *h) { return h ? h->launches : 0; }
 
 extern "C" void *pimc_stream(const pimc_handle *h) { return h ? (void *)h->stream : nullptr; }
+
+// ------------------------------------------------------------ allocation-free queries
+//
+// pimc_pot_energy_noalloc: the PotEnergy query of pimc_pot_energy for callers
+// that must not have device memory allocated on their behalf once their set-up
+// is done -- for example an application that reserves the device memory up
+// front for its own pool allocator, or runs under a fixed device-memory budget,
+// where a cudaMalloc at query time can fail (and would also synchronise the
+// device).  pimc_pot_energy stages its queries in the handle's scratch buffer,
+// which grows with cudaMalloc; this variant stages them in the fixed array
+// below instead and calls no cudaMalloc, cudaFree or other allocating routine.
+//
+// The array holds at most PIMC_NOALLOC_MAX_QUERIES queries; every GPU that
+// loads the library holds it (160 KiB) until the process exits.  All calls,
+// from every handle on a device, share it and it keeps the last call's
+// contents; nothing in it needs to start at zero because each call writes
+// every entry it later reads.  Calls that overlap on the GPU (two streams,
+// two host threads, two handles on one device) race on the array: callers
+// must order them.  Host code cannot use the array's name as an address, so
+// the first call on each device, with that device current, looks the address
+// up with cudaGetSymbolAddress; make that first call before any stream capture.
+#define PIMC_NOALLOC_MAX_QUERIES 4096
+#define PIMC_NOALLOC_BYTES (PIMC_NOALLOC_MAX_QUERIES * (4 * sizeof(double) + 2 * sizeof(int)))
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[PIMC_NOALLOC_BYTES];
+
+#include <mutex>
+static std::mutex g_noalloc_mu;
+static void *g_noalloc_ptr[256];     // per device: the array's device address
+
+static pimc_status noalloc_scratch(pimc_handle *h, unsigned char **p)
+{
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (h->device < 0 || h->device >= 256) return PIMC_ERR_BAD_ARG;
+  if (!g_noalloc_ptr[h->device]) {
+    void *ptr = nullptr;
+    CK(cudaSetDevice(h->device));
+    CK(cudaGetSymbolAddress(&ptr, g_noalloc_scratch));
+    g_noalloc_ptr[h->device] = ptr;
+  }
+  *p = (unsigned char *)g_noalloc_ptr[h->device];
+  return PIMC_OK;
+}
+
+extern "C" pimc_status pimc_pot_energy_noalloc(pimc_handle *h, int n, const int *atom0, const int *it,
+                                               const double *xyz, double *out)
+{
+  pimc_status e = ready(h);
+  if (e) return e;
+  const DevSys &d = h->ctx.s;
+  if (n < 0 || (n && (!atom0 || !it || !xyz || !out))) return PIMC_ERR_BAD_ARG;
+  if (n > PIMC_NOALLOC_MAX_QUERIES) return PIMC_ERR_SIZE;
+  for (int k = 0; k < n; k++)
+    if (atom0[k] < 0 || atom0[k] >= d.na || it[k] < 0 || it[k] >= d.P) return PIMC_ERR_BAD_ARG;
+  if (n == 0) return PIMC_OK;
+  unsigned char *base = nullptr;
+  if ((e = noalloc_scratch(h, &base))) return e;
+  double *dx = (double *)base;                                    // 3 * MAX doubles
+  double *dout = dx + 3 * PIMC_NOALLOC_MAX_QUERIES;               // MAX doubles
+  int *da = (int *)(dout + PIMC_NOALLOC_MAX_QUERIES);             // MAX ints
+  int *dt = da + PIMC_NOALLOC_MAX_QUERIES;                        // MAX ints
+  CK(cudaMemcpyAsync(da, atom0, n * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(dt, it, n * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(dx, xyz, 3 * (size_t)n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  launch_q_slice(h->ctx, h->frames, n, da, dt, dx, dout, h->stream);
+  h->launches++;
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(out, dout, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  return check_err(h);
+}
