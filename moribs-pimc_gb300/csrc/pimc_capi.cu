@@ -224,6 +224,9 @@ extern "C" pimc_status pimc_create(const pimc_system *sys, int device, pimc_hand
   size_t nr = (size_t)(d.nrotors > 0 ? d.nrotors : 1) * d.Q;
   pimc_status e;
   if ((e = dalloc(h, &st.x, nb)) || (e = dalloc(h, &st.y, nb)) || (e = dalloc(h, &st.z, nb)) ||
+      (e = dalloc(h, &st.xf, nb)) || (e = dalloc(h, &st.yf, nb)) || (e = dalloc(h, &st.zf, nb)) ||
+      (e = dalloc(h, &st.cosvf, 3 * nr)) || (e = dalloc(h, &st.rp_cache, nr)) || (e = dalloc(h, &st.rl_cache, nr)) ||
+      (e = dalloc(h, &st.rp_ok, nr)) || (e = dalloc(h, &st.rl_ok, nr)) ||
       (e = dalloc(h, &st.ang, 3 * nr)) || (e = dalloc(h, &st.cosv, 3 * nr)) || (e = dalloc(h, &st.pindex, na)) ||
       (e = dalloc(h, &st.mctype, na)) || (e = dalloc(h, &st.err, 1)) || (e = dalloc(h, &h->frames, nr)) ||
       (e = dalloc(h, &h->cnt, 12)) || (e = dalloc(h, &h->pass, 1)) || (e = dalloc(h, &h->cursors, 8))) {
@@ -236,6 +239,11 @@ extern "C" pimc_status pimc_create(const pimc_system *sys, int device, pimc_hand
   CK(cudaMemset(st.x, 0, nb * sizeof(double)));
   CK(cudaMemset(st.y, 0, nb * sizeof(double)));
   CK(cudaMemset(st.z, 0, nb * sizeof(double)));
+  CK(cudaMemset(st.xf, 0, nb * sizeof(float)));
+  CK(cudaMemset(st.yf, 0, nb * sizeof(float)));
+  CK(cudaMemset(st.zf, 0, nb * sizeof(float)));
+  CK(cudaMemset(st.rp_ok, 0, nr * sizeof(int)));
+  CK(cudaMemset(st.rl_ok, 0, nr * sizeof(int)));
   CK(cudaMemset(st.err, 0, sizeof(unsigned)));
   CK(cudaMemset(h->cnt, 0, 12 * sizeof(unsigned long long)));
   CK(cudaMemset(h->pass, 0, sizeof(unsigned)));
@@ -260,8 +268,9 @@ extern "C" pimc_status pimc_destroy(pimc_handle *h)
   if (h->stream) cudaStreamSynchronize(h->stream);
   if (h->pass_exec) cudaGraphExecDestroy(h->pass_exec);
   DevState &st = h->ctx.st;
-  void *bufs[] = {st.x, st.y, st.z, st.ang, st.cosv, st.pindex, st.mctype, st.err, h->frames, h->cnt, h->pass,
-                  h->cursors, h->ms, h->qbuf};
+  void *bufs[] = {st.x, st.y, st.z, st.xf, st.yf, st.zf, st.cosvf, st.rp_cache, st.rl_cache, st.rp_ok, st.rl_ok,
+                  st.ang, st.cosv, st.pindex, st.mctype, st.err, h->frames, h->cnt, h->pass, h->cursors, h->ms,
+                  h->qbuf};
   for (void *b : bufs)
     if (b) cudaFree(b);
   for (void *b : h->owned) cudaFree(b);
@@ -297,7 +306,8 @@ extern "C" pimc_status pimc_load_tables(pimc_handle *h, const pimc_tables *tb)
     spline_y2(tb->grid1d, tb->pot1d, n, y2.data());
     t.n1d = n;
     if ((e = upload(h, tb->grid1d, n, &t.g1d)) || (e = upload(h, tb->pot1d, n, &t.p1d)) ||
-        (e = upload(h, y2.data(), n, &t.y21d)))
+        (e = upload(h, y2.data(), n, &t.y21d)) || (e = upload_f32(h, tb->grid1d, n, &t.g1d32)) ||
+        (e = upload_f32(h, tb->pot1d, n, &t.p1d32)) || (e = upload_f32(h, y2.data(), n, &t.y21d32)))
       return e;
     // short- and long-range extrapolation constants (mc_poten.cc:418-437)
     double fr = tb->pot1d[0] / tb->pot1d[1];
@@ -313,7 +323,9 @@ extern "C" pimc_status pimc_load_tables(pimc_handle *h, const pimc_tables *tb)
       return PIMC_ERR_BAD_TABLE;
     t.nr2d = tb->nr2d; t.nc2d = tb->nc2d; t.dr2d = tb->dr2d; t.dc2d = tb->dc2d;
     if ((e = upload(h, tb->rgrid2d, tb->nr2d, &t.rg2d)) || (e = upload(h, tb->cgrid2d, tb->nc2d, &t.cg2d)) ||
-        (e = upload(h, tb->pot2d, (size_t)tb->nr2d * tb->nc2d, &t.pot2d)))
+        (e = upload(h, tb->pot2d, (size_t)tb->nr2d * tb->nc2d, &t.pot2d)) ||
+        (e = upload_f32(h, tb->rgrid2d, tb->nr2d, &t.rg2d32)) || (e = upload_f32(h, tb->cgrid2d, tb->nc2d, &t.cg2d32)) ||
+        (e = upload_f32(h, tb->pot2d, (size_t)tb->nr2d * tb->nc2d, &t.pot2d32)))
       return e;
   }
   if (need3d) {
@@ -408,10 +420,12 @@ extern "C" pimc_status pimc_set_state(pimc_handle *h, const double *coords, cons
           }
       CK(cudaMemcpy(h->ctx.st.ang, ang.data(), 3 * n * sizeof(double), cudaMemcpyHostToDevice));
       CK(cudaMemcpy(h->ctx.st.cosv, cs.data(), 3 * n * sizeof(double), cudaMemcpyHostToDevice));
-      launch_frames_init(h->ctx, h->frames, h->stream);
-      h->launches++;
-      CK(cudaGetLastError());
     }
+  }
+  if (coords || angles) {
+    launch_derive_state(h->ctx, h->frames, h->stream);     // float copies, frames, caches stale
+    h->launches++;
+    CK(cudaGetLastError());
   }
   if (pindex) {
     for (int a = 0; a < d.na; a++)
@@ -875,8 +889,12 @@ extern "C" pimc_status pimc_reset_counters(pimc_handle *h)
 extern "C" pimc_status pimc_set_precision(pimc_handle *h, int mixed)
 {
   if (!h || mixed < 0 || mixed > 1) return PIMC_ERR_BAD_ARG;
+  CK(cudaSetDevice(h->device));
   h->ctx.s.mixed = mixed;
-  if (h->pass_exec) { cudaGraphExecDestroy(h->pass_exec); h->pass_exec = nullptr; }
+  launch_invalidate_caches(h->ctx, h->stream);           // cached sums were made at the other precision
+  h->launches++;
+  CK(cudaGetLastError());
+  if (h->pass_exec) { CK(cudaGraphExecDestroy(h->pass_exec)); h->pass_exec = nullptr; }
   return PIMC_OK;
 }
 

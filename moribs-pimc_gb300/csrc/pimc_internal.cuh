@@ -10,7 +10,8 @@
 #define PIMC_PI 3.14159265358979323846
 #define PIMC_WNO2K 0.6950356          /* mc_const.h:16 */
 #define PIMC_RZERO 1.0e-10            /* mc_confg.h:59 */
-#define PIMC_BLOCK 128                /* threads per move CTA */
+#define PIMC_BLOCK 256                /* threads per move CTA */
+#define PIMC_RED_BUF 4096             /* doubles in a CTA's reduction buffer */
 #define PIMC_MAX_SEG 64               /* largest bisection segment (levels <= 6) */
 #define PIMC_MAX_ROTORS 16            /* NumbRotLim (mc_setup.cc:63) */
 
@@ -18,14 +19,16 @@
 enum { DERR_GRID_RANGE = 1, DERR_NEG_DENSITY = 2, DERR_STREAM = 4, DERR_TIMEOUT = 8 };
 
 struct DevTables {
-  // 1D spline, SPot1D (mc_poten.cc:379-438,624-639)
+  // 1D spline, SPot1D (mc_poten.cc:379-438,624-639); float copies for the FP32 path
   int n1d;
   const double *g1d, *p1d, *y21d;
+  const float *g1d32, *p1d32, *y21d32;
   double alpha1d, unode1d, c61d;
   // 2D bilinear, LPot2D (mc_poten.cc:688-729)
   int nr2d, nc2d;
   double dr2d, dc2d;
   const double *rg2d, *cg2d, *pot2d;
+  const float *rg2d32, *cg2d32, *pot2d32;
   // 3D, vcord/vcalc (vcord.f, vcalc.f) on a generalised angular grid
   int rgrd, thgrd, chgrd, chfold;
   double rvmin, rvmax, rvstep, dth3, dch3;
@@ -64,12 +67,22 @@ struct DevSys {
 //   partner sweep at one slice is a unit-stride read);
 //   ang[k*nrotors*Q + r*Q + q], k = {phi, cos theta, chi}: rotor r at rotational slice q;
 //   cosv[k*nrotors*Q + r*Q + q]: its unit vector (MCCosine).
+//   xf/yf/zf: float copies of the beads read by the FP32 table path;
+//   rp_cache/rp_ok[r*Q + q]: the rotor's potential summed over the R
+//   translational slices of rotational slice q with its current orientation,
+//   valid while no bead of those slices and no orientation at q has changed;
+//   rl_cache/rl_ok[r*Q + q]: the current link density rho(q, q+1).
+//   Both caches hold exactly the value a fresh evaluation would return.
 struct DevState {
   double *x, *y, *z;
+  float *xf, *yf, *zf;
   double *ang, *cosv;
+  float *cosvf;
   int *pindex;
   int *mctype;
   unsigned int *err;
+  double *rp_cache, *rl_cache;
+  int *rp_ok, *rl_ok;
 };
 
 struct Ctx {
@@ -85,6 +98,8 @@ struct Frame {
   double e[3];          // phi, theta, chi
   double m[9];          // rotmat(i,j) at m[i*3+j]
   double hz_norm;
+  float mf[9];          // float copy for the FP32 path
+  float hzf;
 };
 
 __device__ __forceinline__ void matpre(const double e[3], double m[9])
@@ -115,6 +130,8 @@ __device__ __forceinline__ void make_frame(double phi, double cost, double chi, 
   s = s + f.m[5] * f.m[5];
   s = s + f.m[8] * f.m[8];
   f.hz_norm = sqrt(s);
+  for (int k = 0; k < 9; k++) f.mf[k] = (float)f.m[k];
+  f.hzf = (float)f.hz_norm;
 }
 
 // ------------------------------------------------------------------ leaves
@@ -376,18 +393,65 @@ __device__ __forceinline__ double vcord(const DevTables &t, const Frame &f, doub
   return v0 + gradr * delr + gradth * delth + gradch * delch;
 }
 
-// the FP32 form of vcord for the mixed-precision path: same grid logic in
-// float arithmetic on the float copy of the table
-__device__ __forceinline__ float vcord32(const DevTables &t, const float m[9], float hzn, float Rx, float Ry, float Rz)
+// ---------------------------------------------------------- FP32 table path
+// The FP32 forms follow the same grids and interpolation as the FP64 leaves;
+// angles are taken from atan2 of a cross and a dot product, which is the same
+// angle as the reference's acos/atan but keeps full float precision near 0
+// and pi.
+
+__device__ __forceinline__ float splint32(const float *__restrict__ xa, const float *__restrict__ ya,
+                                          const float *__restrict__ y2a, int n, float x)
 {
-  const float pi = 3.14159265358979f, small = 1.e-8f;
-  float rn = sqrtf(Rx * Rx + Ry * Ry + Rz * Rz);
-  float dz = m[2] * Rx + m[5] * Ry + m[8] * Rz;
-  float da = fminf(1.0f, fmaxf(-1.0f, dz / (hzn * rn)));
-  float thewff = acosf(da);
+  int klo = 0, khi = n - 1;
+  while (khi - klo > 1) {
+    int k = (khi + klo) >> 1;
+    if (__ldg(xa + k) > x) khi = k;
+    else klo = k;
+  }
+  float xk = __ldg(xa + khi), xl = __ldg(xa + klo);
+  float h = xk - xl;
+  float a = (xk - x) / h, b = (x - xl) / h;
+  return a * __ldg(ya + klo) + b * __ldg(ya + khi) +
+         ((a * a * a - a) * __ldg(y2a + klo) + (b * b * b - b) * __ldg(y2a + khi)) * (h * h) * (1.0f / 6.0f);
+}
+
+__device__ __forceinline__ float spot1d32(const DevTables &t, float r)
+{
+  if (r >= __ldg(t.g1d32 + t.n1d - 1)) {
+    float r2 = r * r;
+    return (float)(-t.c61d) / (r2 * r2 * r2);
+  }
+  if (r <= __ldg(t.g1d32)) return (float)t.unode1d * expf(-(float)t.alpha1d * r);
+  return splint32(t.g1d32, t.p1d32, t.y21d32, t.n1d, r);
+}
+
+__device__ __forceinline__ float lpot2d32(const DevTables &t, float r, float cost)
+{
+  float rmin = __ldg(t.rg2d32), cmin = __ldg(t.cg2d32);
+  int ir = (int)floorf((r - rmin) / (float)t.dr2d);
+  int ic = (int)floorf((cost - cmin) / (float)t.dc2d);
+  ir = min(max(ir, 0), t.nr2d - 2);
+  ic = min(max(ic, 0), t.nc2d - 2);
+  const float *p = t.pot2d32 + (size_t)ir * t.nc2d + ic;
+  float y1 = __ldg(p), y4 = __ldg(p + 1), y2 = __ldg(p + t.nc2d), y3 = __ldg(p + t.nc2d + 1);
+  float r1 = __ldg(t.rg2d32 + ir), r2 = __ldg(t.rg2d32 + ir + 1);
+  float c1 = __ldg(t.cg2d32 + ic), c2 = __ldg(t.cg2d32 + ic + 1);
+  float dr = (r - r1) / (r2 - r1), dc = (cost - c1) / (c2 - c1);
+  return (1.0f - dr) * (1.0f - dc) * y1 + dr * (1.0f - dc) * y2 + dr * dc * y3 + (1.0f - dr) * dc * y4;
+}
+
+// vcord + vcalc in float: R = atom - rotor centre in the space frame
+__device__ __forceinline__ float vcord32(const DevTables &t, const Frame &f, float Rx, float Ry, float Rz)
+{
+  const float pi = 3.14159265358979f;
+  const float *m = f.mf;
   float rdotx = m[0] * Rx + m[3] * Ry + m[6] * Rz;
   float rdoty = m[1] * Rx + m[4] * Ry + m[7] * Rz;
-  float chiwff = (fabsf(rdotx) < small) ? 0.5f * pi : atanf(fabsf(rdoty / rdotx));
+  float rdotz = m[2] * Rx + m[5] * Ry + m[8] * Rz;
+  float rn2 = Rx * Rx + Ry * Ry + Rz * Rz;
+  float rn = sqrtf(rn2);
+  float thewff = atan2f(sqrtf(fmaxf(rdotx * rdotx + rdoty * rdoty, 0.0f)), rdotz);
+  float chiwff = atan2f(fabsf(rdoty), fabsf(rdotx));
   float chir;
   if (rdotx >= 0.0f && rdoty >= 0.0f) chir = chiwff;
   else if (rdotx < 0.0f && rdoty >= 0.0f) chir = pi - chiwff;

@@ -6,18 +6,40 @@
 #include "pimc_kernels.cuh"
 #include "pimc_launch.h"
 
-// ------------------------------------------------------------ frame cache
-__global__ void k_frames_init(Ctx c, Frame *frames)
+// ------------------------------------------------------------ derived state
+// after a path upload: float copies of beads and unit vectors, rotor frames,
+// and both caches marked stale
+__global__ void k_derive_state(Ctx c, Frame *frames)
 {
-  int n = c.s.nrotors * c.s.Q;
-  size_t m = (size_t)n;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    make_frame(c.st.ang[i], c.st.ang[m + i], c.st.ang[2 * m + i], frames[i]);
+  size_t nb = (size_t)c.s.P * c.s.nap;
+  size_t n = (size_t)c.s.nrotors * c.s.Q;
+  size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < nb; i += stride) {
+    c.st.xf[i] = (float)c.st.x[i];
+    c.st.yf[i] = (float)c.st.y[i];
+    c.st.zf[i] = (float)c.st.z[i];
+  }
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    make_frame(c.st.ang[i], c.st.ang[n + i], c.st.ang[2 * n + i], frames[i]);
+    for (int d = 0; d < 3; d++) c.st.cosvf[d * n + i] = (float)c.st.cosv[d * n + i];
+    c.st.rp_ok[i] = 0;
+    c.st.rl_ok[i] = 0;
+  }
+}
+
+__global__ void k_invalidate_caches(Ctx c)
+{
+  size_t n = (size_t)c.s.nrotors * c.s.Q;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    c.st.rp_ok[i] = 0;
+    c.st.rl_ok[i] = 0;
+  }
 }
 
 // ------------------------------------------------------------ bisection
 // MCBisectionMove(type, time) / MCBisectionMoveExchange: all atoms of the
 // type in order, each consuming the replayed gauss()/rnd3() streams
+template <bool MIX>
 __global__ void __launch_bounds__(PIMC_BLOCK) k_bisect_replay(Ctx c, Frame *frames, int type, int time0, int exch,
                                                                ReplaySrc src, double *ds_out, int *lvl_out,
                                                                unsigned long long *cnt)
@@ -25,7 +47,7 @@ __global__ void __launch_bounds__(PIMC_BLOCK) k_bisect_replay(Ctx c, Frame *fram
   __shared__ BisectShared sh;
   int L = c.s.levels[type];
   for (int atom = 0; atom < c.s.numb[type]; atom++) {
-    int acc = bisect_move(c, frames, type, atom, time0, exch, src, sh, ds_out + (size_t)atom * L);
+    int acc = bisect_move<MIX>(c, frames, type, atom, time0, exch, src, sh, ds_out + (size_t)atom * L);
     if (threadIdx.x == 0) {
       lvl_out[atom] = sh.passed;
       cnt[(type * 3 + 1) * 2 + 0] += 1;
@@ -37,6 +59,7 @@ __global__ void __launch_bounds__(PIMC_BLOCK) k_bisect_replay(Ctx c, Frame *fram
 
 // one phase of the production schedule: window k starts at s0 + k*M and
 // moves atom (k + j) mod numb; interiors of all windows are disjoint
+template <bool MIX>
 __global__ void __launch_bounds__(PIMC_BLOCK) k_bisect_phase(Ctx c, Frame *frames, int type, int s0, int j,
                                                               unsigned phase, uint64_t seed, const unsigned *pass,
                                                               unsigned long long *cnt)
@@ -47,7 +70,7 @@ __global__ void __launch_bounds__(PIMC_BLOCK) k_bisect_phase(Ctx c, Frame *frame
   int atom = (k + j) % c.s.numb[type];
   int time0 = s0 + k * M;
   PhiloxSrc src{seed, ((uint64_t)(*pass) << 32) | ((uint64_t)phase << 12) | (uint64_t)k};
-  int acc = bisect_move(c, frames, type, atom, time0, 0, src, sh, nullptr);
+  int acc = bisect_move<MIX>(c, frames, type, atom, time0, 0, src, sh, nullptr);
   if (threadIdx.x == 0) {
     atomicAdd(&cnt[(type * 3 + 1) * 2 + 0], 1ull);
     if (acc) atomicAdd(&cnt[(type * 3 + 1) * 2 + 1], 1ull);
@@ -57,7 +80,7 @@ __global__ void __launch_bounds__(PIMC_BLOCK) k_bisect_phase(Ctx c, Frame *frame
 // ------------------------------------------------------------ rotations
 // one even or odd half of MCRotationsMove / MCRotations3D: CTA b handles
 // slice q = parity + 2b and all rotors of the type in order
-template <bool REPLAY>
+template <bool REPLAY, bool MIX>
 __global__ void __launch_bounds__(PIMC_BLOCK) k_rot(Ctx c, Frame *frames, int parity, const double *urot, long nurot,
                                                      unsigned phase, uint64_t seed, const unsigned *pass,
                                                      double *rd_out, int *acc_out, unsigned long long *cnt)
@@ -70,7 +93,7 @@ __global__ void __launch_bounds__(PIMC_BLOCK) k_rot(Ctx c, Frame *frames, int pa
   int per = linear ? 3 : 4;
   long n_even = (c.s.Q + 1) / 2;
   for (int r = 0; r < nr; r++) {
-    double u[4];
+    double u[4] = {0.5, 0.5, 0.5, 0.5};
     if (REPLAY) {
       // serial consumption order: even slices then odd, rotors inside a slice
       long idx = ((parity ? n_even : 0) + blockIdx.x) * (long)nr + r;
@@ -86,10 +109,11 @@ __global__ void __launch_bounds__(PIMC_BLOCK) k_rot(Ctx c, Frame *frames, int pa
       u[0] = a; u[1] = b;
       philox_u2(seed, mv, 0x400000u | (uint32_t)r, 1u, &a, &b);
       u[2] = a; u[3] = b;
+      if (linear) u[2] = u[3];
     }
     int g0 = c.s.rot_first + r;
     double rd;
-    int acc = linear ? rotlin_step(c, frames, g0, q, u, sh, &rd) : rot3d_step(c, frames, g0, q, u, sh, &rd);
+    int acc = rot_step<MIX>(c, frames, g0, q, u, linear, sh, &rd);
     if (threadIdx.x == 0) {
       if (REPLAY) {
         rd_out[(size_t)q * nr + r] = rd;
@@ -105,8 +129,6 @@ __global__ void __launch_bounds__(PIMC_BLOCK) k_rot(Ctx c, Frame *frames, int pa
 // ------------------------------------------------------------ centroid move
 // MCMolecularMove (mc_piqmc.cc:54-102) split in three launches per atom:
 // propose (3 displacements), partner sums over all slices, accept/commit.
-
-
 template <bool REPLAY>
 __global__ void k_mol_propose(Ctx c, int type, ReplaySrc src, uint64_t seed, const unsigned *pass, unsigned phase,
                               int atom, MolScratch *ms)
@@ -123,28 +145,40 @@ __global__ void k_mol_propose(Ctx c, int type, ReplaySrc src, uint64_t seed, con
   }
 }
 
-// CTA = one partner atom1; threads over slices; new = old + disp
+// CTA = one partner atom1; threads over slices; new = old + disp; the two
+// whole-path sums are reduced warp by warp in a fixed order
+template <bool MIX>
 __global__ void __launch_bounds__(PIMC_BLOCK) k_mol_pairs(Ctx c, Frame *frames, int gatom, MolScratch *ms)
 {
-  __shared__ double part[2][PIMC_BLOCK];
+  __shared__ double part[2][PIMC_BLOCK / 32];
   int a1 = blockIdx.x;
   int tid = threadIdx.x;
   double an = 0.0, ao = 0.0;
   if (a1 != gatom) {
     double d0 = ms->disp[0], d1 = ms->disp[1], d2 = ms->disp[2];
-    for (int it = tid; it < c.s.P; it += PIMC_BLOCK) {
+    for (int it = tid; it < c.s.P; it += blockDim.x) {
       size_t i = sidx(c.s, it, gatom);
-      double x = c.st.x[i], y = c.st.y[i], z = c.st.z[i];
-      ao += pair_term(c, frames, gatom, a1, it, x, y, z);
-      an += pair_term(c, frames, gatom, a1, it, x + d0, y + d1, z + d2);
+      if (MIX) {
+        float x = c.st.xf[i], y = c.st.yf[i], z = c.st.zf[i];
+        ao += (double)pair_term32(c, frames, gatom, a1, it, x, y, z);
+        an += (double)pair_term32(c, frames, gatom, a1, it, (float)(c.st.x[i] + d0), (float)(c.st.y[i] + d1),
+                                  (float)(c.st.z[i] + d2));
+      } else {
+        double x = c.st.x[i], y = c.st.y[i], z = c.st.z[i];
+        ao += pair_term64(c, frames, gatom, a1, it, x, y, z);
+        an += pair_term64(c, frames, gatom, a1, it, x + d0, y + d1, z + d2);
+      }
     }
   }
-  part[0][tid] = an;
-  part[1][tid] = ao;
+  for (int o = 16; o > 0; o >>= 1) {
+    an += __shfl_xor_sync(0xffffffffu, an, o);
+    ao += __shfl_xor_sync(0xffffffffu, ao, o);
+  }
+  if ((tid & 31) == 0) { part[0][tid >> 5] = an; part[1][tid >> 5] = ao; }
   __syncthreads();
   if (tid < 2) {
     double s = 0.0;
-    for (int k = 0; k < PIMC_BLOCK; k++) s += part[tid][k];
+    for (int k = 0; k < (int)(blockDim.x >> 5); k++) s += part[tid][k];
     ms->pair[tid][a1] = s;
   }
 }
@@ -181,12 +215,12 @@ __global__ void __launch_bounds__(PIMC_BLOCK) k_mol_finish(Ctx c, int type, int 
   __syncthreads();
   if (acc) {
     double d0 = ms->disp[0], d1 = ms->disp[1], d2 = ms->disp[2];
-    for (int it = threadIdx.x; it < c.s.P; it += PIMC_BLOCK) {
+    for (int it = threadIdx.x; it < c.s.P; it += blockDim.x) {
       size_t i = sidx(c.s, it, gatom);
-      c.st.x[i] += d0;
-      c.st.y[i] += d1;
-      c.st.z[i] += d2;
+      store_bead(c, i, c.st.x[i] + d0, c.st.y[i] + d1, c.st.z[i] + d2);
     }
+    // the whole path moved: every cached rotor potential is stale
+    for (int i = threadIdx.x; i < c.s.nrotors * c.s.Q; i += blockDim.x) c.st.rp_ok[i] = 0;
   }
 }
 
@@ -195,14 +229,17 @@ __global__ void __launch_bounds__(PIMC_BLOCK) k_mol_finish(Ctx c, int type, int 
 __global__ void __launch_bounds__(PIMC_BLOCK) k_q_slice(Ctx c, Frame *frames, int n, const int *a0, const int *it,
                                                          const double *xyz, double *out)
 {
-  __shared__ double part[SLOT_CHUNK][PIMC_BLOCK];
-  __shared__ int sa, st;
-  __shared__ double sx, sy, sz, so;
+  __shared__ double buf[PIMC_RED_BUF];
+  __shared__ int sa;
+  __shared__ double so;
   int q = blockIdx.x;
   if (q >= n) return;
-  if (threadIdx.x == 0) { sa = a0[q]; st = it[q]; sx = xyz[3 * q]; sy = xyz[3 * q + 1]; sz = xyz[3 * q + 2]; }
+  if (threadIdx.x == 0) sa = a0[q];
   __syncthreads();
-  slot_energies(c, frames, 1, &sa, &st, &sx, &sy, &sz, &so, part);
+  int t = it[q];
+  double px = xyz[3 * q], py = xyz[3 * q + 1], pz = xyz[3 * q + 2];
+  slot_sums(1, c.s.na, &sa, [&](int, int p) -> double { return pair_term64(c, frames, sa, p, t, px, py, pz); }, &so,
+            buf);
   if (threadIdx.x == 0) out[q] = so;
 }
 
@@ -211,32 +248,34 @@ __global__ void __launch_bounds__(PIMC_BLOCK) k_q_slice(Ctx c, Frame *frames, in
 __global__ void __launch_bounds__(PIMC_BLOCK) k_q_rot(Ctx c, Frame *frames, int n, const int *rot, const int *it,
                                                        const double *v3, int linear, double *out)
 {
-  __shared__ double part[PIMC_BLOCK];
+  __shared__ double buf[PIMC_RED_BUF];
   __shared__ Frame f;
+  __shared__ int sg;
+  __shared__ double so;
   int q = blockIdx.x;
   if (q >= n) return;
-  int g0 = rot[q], t = it[q];
-  if (threadIdx.x == 0 && !linear) {
-    f.e[0] = v3[3 * q]; f.e[1] = v3[3 * q + 1]; f.e[2] = v3[3 * q + 2];
-    matpre(f.e, f.m);
-    double s = 0.0;
-    s = s + f.m[2] * f.m[2];
-    s = s + f.m[5] * f.m[5];
-    s = s + f.m[8] * f.m[8];
-    f.hz_norm = sqrt(s);
+  int t = it[q];
+  if (threadIdx.x == 0) {
+    sg = rot[q];
+    if (!linear) {
+      f.e[0] = v3[3 * q]; f.e[1] = v3[3 * q + 1]; f.e[2] = v3[3 * q + 2];
+      matpre(f.e, f.m);
+      double s = 0.0;
+      s = s + f.m[2] * f.m[2];
+      s = s + f.m[5] * f.m[5];
+      s = s + f.m[8] * f.m[8];
+      f.hz_norm = sqrt(s);
+    }
   }
   __syncthreads();
   double nv[3] = {v3[3 * q], v3[3 * q + 1], v3[3 * q + 2]};
-  double acc = 0.0;
-  for (int p = threadIdx.x; p < c.s.na; p += PIMC_BLOCK)
-    if (p != g0) acc += linear ? rotlin_term(c, nv, g0, p, t) : rot3d_term(c, frames, f, g0, p, t);
-  part[threadIdx.x] = acc;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double s = 0.0;
-    for (int k = 0; k < PIMC_BLOCK; k++) s += part[k];
-    out[q] = s;
-  }
+  int g0 = sg;
+  slot_sums(1, c.s.na, &sg,
+            [&](int, int p) -> double {
+              return linear ? rotlin_term64(c, nv, g0, p, t) : rot3d_term64(c, frames, f, g0, p, t);
+            },
+            &so, buf);
+  if (threadIdx.x == 0) out[q] = so;
 }
 
 // ------------------------------------------------------------ estimators
@@ -249,7 +288,7 @@ __global__ void __launch_bounds__(PIMC_BLOCK) k_est_kin(Ctx c, double *out)
   int type = c.st.mctype[a];
   int g = c.s.first[type];
   double acc = 0.0;
-  for (int it = threadIdx.x; it < P; it += PIMC_BLOCK) {
+  for (int it = threadIdx.x; it < P; it += blockDim.x) {
     int a1 = a;
     if (c.s.stat[type] == 1 && it + 1 == P) a1 = g + c.st.pindex[a - g];
     size_t i0 = sidx(c.s, it, a), i1 = sidx(c.s, (it + 1) % P, a1);
@@ -263,7 +302,7 @@ __global__ void __launch_bounds__(PIMC_BLOCK) k_est_kin(Ctx c, double *out)
   __syncthreads();
   if (threadIdx.x == 0) {
     double s = 0.0;
-    for (int k = 0; k < PIMC_BLOCK; k++) s += part[k];
+    for (int k = 0; k < (int)blockDim.x; k++) s += part[k];
     out[a] = s / (4.0 * c.s.beta * c.s.lambda[type]);
   }
 }
@@ -285,15 +324,15 @@ __global__ void __launch_bounds__(PIMC_BLOCK) k_est_pot(Ctx c, Frame *frames, do
                  (ty0 == ty1 && m0 == 0);
   double acc = 0.0;
   if (counted)
-    for (int it = threadIdx.x; it < c.s.P; it += PIMC_BLOCK) {
+    for (int it = threadIdx.x; it < c.s.P; it += blockDim.x) {
       size_t i = sidx(c.s, it, a0);
-      acc += pair_term(c, frames, a0, a1, it, c.st.x[i], c.st.y[i], c.st.z[i]);
+      acc += pair_term64(c, frames, a0, a1, it, c.st.x[i], c.st.y[i], c.st.z[i]);
     }
   part[threadIdx.x] = acc;
   __syncthreads();
   if (threadIdx.x == 0) {
     double s = 0.0;
-    for (int k = 0; k < PIMC_BLOCK; k++) s += part[k];
+    for (int k = 0; k < (int)blockDim.x; k++) s += part[k];
     out[pidx] = s;
   }
 }
@@ -340,8 +379,7 @@ __global__ void k_est_rot(Ctx c, Frame *frames, double *out)
         srot = erot;
       sesq = esq;
       sts = erot * erot;
-    } else
-      srot = sesq = sts = 0.0;
+    }
   }
   out[4 * k + 0] = srot;
   out[4 * k + 1] = sesq;
@@ -370,37 +408,50 @@ __global__ void k_est_rcf(Ctx c, double *rcf)
 __global__ void k_pass_begin(unsigned *pass) { *pass += 1; }
 
 // ------------------------------------------------------------ launchers
-void launch_frames_init(const Ctx &c, Frame *frames, cudaStream_t s)
+void launch_derive_state(const Ctx &c, Frame *frames, cudaStream_t s)
+{
+  k_derive_state<<<152, 256, 0, s>>>(c, frames);
+}
+
+void launch_invalidate_caches(const Ctx &c, cudaStream_t s)
 {
   int n = c.s.nrotors * c.s.Q;
-  if (n > 0) k_frames_init<<<(n + 127) / 128, 128, 0, s>>>(c, frames);
+  if (n > 0) k_invalidate_caches<<<(n + 255) / 256, 256, 0, s>>>(c);
 }
 
 void launch_bisect_replay(const Ctx &c, Frame *f, int type, int time0, int exch, ReplaySrc src, double *ds,
                           int *lvl, unsigned long long *cnt, cudaStream_t s)
 {
-  k_bisect_replay<<<1, PIMC_BLOCK, 0, s>>>(c, f, type, time0, exch, src, ds, lvl, cnt);
+  if (c.s.mixed) k_bisect_replay<true><<<1, PIMC_BLOCK, 0, s>>>(c, f, type, time0, exch, src, ds, lvl, cnt);
+  else k_bisect_replay<false><<<1, PIMC_BLOCK, 0, s>>>(c, f, type, time0, exch, src, ds, lvl, cnt);
 }
 
 void launch_bisect_phase(const Ctx &c, Frame *f, int type, int s0, int j, unsigned phase, uint64_t seed,
                          const unsigned *pass, unsigned long long *cnt, cudaStream_t s)
 {
   int M = 1 << c.s.levels[type];
-  k_bisect_phase<<<c.s.P / M, PIMC_BLOCK, 0, s>>>(c, f, type, s0, j, phase, seed, pass, cnt);
+  if (c.s.mixed) k_bisect_phase<true><<<c.s.P / M, PIMC_BLOCK, 0, s>>>(c, f, type, s0, j, phase, seed, pass, cnt);
+  else k_bisect_phase<false><<<c.s.P / M, PIMC_BLOCK, 0, s>>>(c, f, type, s0, j, phase, seed, pass, cnt);
 }
 
 void launch_rot_replay(const Ctx &c, Frame *f, int parity, const double *urot, long nurot, double *rd, int *acc,
                        unsigned long long *cnt, cudaStream_t s)
 {
   int nb = (c.s.Q - parity + 1) / 2;
-  if (nb > 0) k_rot<true><<<nb, PIMC_BLOCK, 0, s>>>(c, f, parity, urot, nurot, 0, 0, nullptr, rd, acc, cnt);
+  if (nb <= 0) return;
+  if (c.s.mixed) k_rot<true, true><<<nb, PIMC_BLOCK, 0, s>>>(c, f, parity, urot, nurot, 0, 0, nullptr, rd, acc, cnt);
+  else k_rot<true, false><<<nb, PIMC_BLOCK, 0, s>>>(c, f, parity, urot, nurot, 0, 0, nullptr, rd, acc, cnt);
 }
 
 void launch_rot_phase(const Ctx &c, Frame *f, int parity, unsigned phase, uint64_t seed, const unsigned *pass,
                       unsigned long long *cnt, cudaStream_t s)
 {
   int nb = (c.s.Q - parity + 1) / 2;
-  if (nb > 0) k_rot<false><<<nb, PIMC_BLOCK, 0, s>>>(c, f, parity, nullptr, 0, phase, seed, pass, nullptr, nullptr, cnt);
+  if (nb <= 0) return;
+  if (c.s.mixed)
+    k_rot<false, true><<<nb, PIMC_BLOCK, 0, s>>>(c, f, parity, nullptr, 0, phase, seed, pass, nullptr, nullptr, cnt);
+  else
+    k_rot<false, false><<<nb, PIMC_BLOCK, 0, s>>>(c, f, parity, nullptr, 0, phase, seed, pass, nullptr, nullptr, cnt);
 }
 
 void launch_mol(const Ctx &c, Frame *f, int type, int atom, bool replay, ReplaySrc src, uint64_t seed,
@@ -410,7 +461,8 @@ void launch_mol(const Ctx &c, Frame *f, int type, int atom, bool replay, ReplayS
   int g = c.s.first[type] + atom;
   if (replay) k_mol_propose<true><<<1, 32, 0, s>>>(c, type, src, seed, pass, phase, atom, ms);
   else k_mol_propose<false><<<1, 32, 0, s>>>(c, type, src, seed, pass, phase, atom, ms);
-  k_mol_pairs<<<c.s.na, PIMC_BLOCK, 0, s>>>(c, f, g, ms);
+  if (c.s.mixed) k_mol_pairs<true><<<c.s.na, PIMC_BLOCK, 0, s>>>(c, f, g, ms);
+  else k_mol_pairs<false><<<c.s.na, PIMC_BLOCK, 0, s>>>(c, f, g, ms);
   if (replay) k_mol_finish<true><<<1, PIMC_BLOCK, 0, s>>>(c, type, g, src, seed, pass, phase, atom, ms, dv, acc, cnt);
   else k_mol_finish<false><<<1, PIMC_BLOCK, 0, s>>>(c, type, g, src, seed, pass, phase, atom, ms, dv, acc, cnt);
 }

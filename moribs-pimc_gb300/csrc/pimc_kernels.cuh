@@ -1,13 +1,16 @@
 // pimc_kernels.cuh -- move and energy routines executed by one CTA of
 // PIMC_BLOCK threads, shared by the replay (parity) kernels and the
-// production phase kernels.  Partner sums are deterministic: thread k holds
-// the partners p = k, k+PIMC_BLOCK, ... and the per-thread partials are added
-// in thread order, which for natoms <= PIMC_BLOCK is the reference's own
-// sequential order over atom1 (mc_piqmc.cc:1808-1962).
+// production phase kernels.
+//
+// A move's work is a set of (slot, partner) items -- a slot is one slice
+// energy PotEnergy(atom, pos, it) or PotRotE3D/PotRotEnergy(rotor, ., it)
+// and the partners are all other atoms -- flattened over all threads of the
+// CTA; each slot's sum is then reduced by one warp in a fixed order, so the
+// result does not depend on scheduling.  MIX selects the FP32 table path:
+// pair terms from the float copies of beads and tables, sums and everything
+// after them in FP64.
 #pragma once
 #include "pimc_internal.cuh"
-
-#define SLOT_CHUNK 16
 
 __device__ __forceinline__ size_t sidx(const DevSys &s, int t, int a) { return (size_t)t * s.nap + a; }
 
@@ -15,8 +18,8 @@ __device__ __forceinline__ int rot_index(const DevSys &s, int gatom, int q) { re
 
 // one term of PotEnergy(atom0, pos, it) (mc_piqmc.cc:1824-1958): atom0 at
 // (px,py,pz), partner atom1 at its current bead, rotor frames from the cache
-__device__ __forceinline__ double pair_term(const Ctx &c, const Frame *__restrict__ frames, int a0, int a1, int it,
-                                            double px, double py, double pz)
+__device__ __forceinline__ double pair_term64(const Ctx &c, const Frame *__restrict__ frames, int a0, int a1, int it,
+                                              double px, double py, double pz)
 {
   const DevSys &s = c.s;
   int ty0 = c.st.mctype[a0], ty1 = c.st.mctype[a1];
@@ -55,27 +58,76 @@ __device__ __forceinline__ double pair_term(const Ctx &c, const Frame *__restric
   return spot1d(c.t, r);
 }
 
-// block-wide deterministic sums of PotEnergy(a0[k], pos_k, its[k]) for
-// k < nslots; results land in out[k] (shared or global)
-__device__ inline void slot_energies(const Ctx &c, const Frame *frames, int nslots, const int *a0, const int *its,
-                              const double *px, const double *py, const double *pz, double *out,
-                              double (*part)[PIMC_BLOCK])
+// the same term on the FP32 table path
+__device__ __forceinline__ float pair_term32(const Ctx &c, const Frame *__restrict__ frames, int a0, int a1, int it,
+                                             float px, float py, float pz)
 {
-  int tid = threadIdx.x;
-  for (int base = 0; base < nslots; base += SLOT_CHUNK) {
-    int ns = min(SLOT_CHUNK, nslots - base);
-    for (int k = 0; k < ns; k++) {
-      int sl = base + k;
-      double acc = 0.0;
-      for (int p = tid; p < c.s.na; p += PIMC_BLOCK)
-        if (p != a0[sl]) acc += pair_term(c, frames, a0[sl], p, its[sl], px[sl], py[sl], pz[sl]);
-      part[k][tid] = acc;
+  const DevSys &s = c.s;
+  int ty0 = c.st.mctype[a0], ty1 = c.st.mctype[a1];
+  int m0 = s.molecule[ty0], m1 = s.molecule[ty1];
+  size_t i1 = sidx(s, it, a1);
+  float qx = c.st.xf[i1], qy = c.st.yf[i1], qz = c.st.zf[i1];
+  float dx = px - qx, dy = py - qy, dz = pz - qz;
+  if (s.minimage) {
+    dx -= (float)s.box[0] * rintf(dx / (float)s.box[0]);
+    dy -= (float)s.box[1] * rintf(dy / (float)s.box[1]);
+    dz -= (float)s.box[2] * rintf(dz / (float)s.box[2]);
+  }
+  float r = sqrtf(dx * dx + dy * dy + dz * dz);
+  if (m0 == 1 || m1 == 1) {
+    int rot = (m0 == 1) ? a0 : a1;
+    size_t n = (size_t)s.nrotors * s.Q;
+    int ri = rot_index(s, rot, it / s.R);
+    float cost = (c.st.cosvf[ri] * dx + c.st.cosvf[n + ri] * dy + c.st.cosvf[2 * n + ri] * dz) / r;
+    if (m0 == 1) cost = -cost;
+    return lpot2d32(c.t, r, cost);
+  } else if ((m0 == 2 || m1 == 2) && m0 != m1) {
+    if (s.ispher) return (float)vspher(c.t, (double)r);
+    if (m0 == 2) return vcord32(c.t, frames[rot_index(s, a0, it / s.R)], -dx, -dy, -dz);
+    return vcord32(c.t, frames[rot_index(s, a1, it / s.R)], dx, dy, dz);
+  } else if (m0 == 2 && m1 == 2 && s.numb[s.imtype] > 1) {
+    return (float)caleng(frames[rot_index(s, a0, it / s.R)], frames[rot_index(s, a1, it / s.R)], (double)px,
+                         (double)py, (double)pz, (double)qx, (double)qy, (double)qz);
+  }
+  return spot1d32(c.t, r);
+}
+
+// out[s] = sum over partners p != skip[s] of f(s, p), s < nslots.  buf holds
+// PIMC_RED_BUF doubles of shared memory; slots are processed in chunks that
+// fit.  Each slot is reduced by one warp: lane l adds items l, l+32, ... in
+// order, then a fixed xor-shuffle tree; deterministic.
+template <class F>
+__device__ __forceinline__ void slot_sums(int nslots, int na, const int *skip, F f, double *out, double *buf)
+{
+  const int npart = na - 1;
+  if (npart <= 0) {
+    for (int s = threadIdx.x; s < nslots; s += blockDim.x) out[s] = 0.0;
+    __syncthreads();
+    return;
+  }
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  const int total = nslots * npart;
+  // chunks of whole slots when a slot fits the buffer, else of PIMC_RED_BUF items
+  const int chunk = (npart <= PIMC_RED_BUF) ? (PIMC_RED_BUF / npart) * npart : PIMC_RED_BUF;
+  for (int base = 0; base < total; base += chunk) {
+    int cnt = min(chunk, total - base);
+    for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
+      int g = base + i;
+      int s = g / npart, pi = g - s * npart;
+      int p = pi < skip[s] ? pi : pi + 1;
+      buf[i] = f(s, p);
     }
     __syncthreads();
-    if (tid < ns) {
-      double sum = 0.0;
-      for (int k = 0; k < PIMC_BLOCK; k++) sum += part[tid][k];
-      out[base + tid] = sum;
+    int sfirst = base / npart, slast = (base + cnt - 1) / npart;
+    for (int sl = sfirst + warp; sl <= slast; sl += nw) {
+      int lo = max(sl * npart, base) - base, hi = min((sl + 1) * npart, base + cnt) - base;
+      double acc = 0.0;
+      for (int k = lo + lane; k < hi; k += 32) acc += buf[k];
+      for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+      if (lane == 0) {
+        if (sl * npart >= base) out[sl] = acc;     // the slot starts in this chunk
+        else out[sl] += acc;                       // continuation of a slot split across chunks
+      }
     }
     __syncthreads();
   }
@@ -84,10 +136,12 @@ __device__ inline void slot_energies(const Ctx &c, const Frame *frames, int nslo
 // ------------------------------------------------------ random sources
 
 // replay of the reference's sequential generator streams (parity mode);
-// cursors live in global memory and are touched by thread 0 only
+// cursors live in global memory.  Gaussian draws of one bisection level are
+// consumed unconditionally (3 per midpoint, mc_piqmc.cc:249-253), so they are
+// indexed from the level's base; accept draws are taken one at a time.
 struct ReplaySrc {
   const double *g; long ng; long *gpos;      // gauss() x1 values
-  const double *u; long nu; long *upos;      // rnd2()/rnd3()/runif() uniforms
+  const double *u; long nu; long *upos;      // rnd2()/rnd3() uniforms
   const double *d; long nd; long *dpos;      // rnd1() displacements
   unsigned int *err;
   __device__ double take(const double *v, long n, long *pos)
@@ -97,7 +151,18 @@ struct ReplaySrc {
     *pos = p + 1;
     return v[p];
   }
-  __device__ double gauss_x1(int, int, int) { return take(g, ng, gpos); }
+  __device__ long gauss_base() { return *gpos; }
+  __device__ double gauss_at(long base, int, int j, int dim)
+  {
+    long p = base + 3 * j + dim;
+    if (p >= ng) { atomicOr(err, (unsigned)DERR_STREAM); return 0.0; }
+    return g[p];
+  }
+  __device__ void gauss_advance(long n)
+  {
+    *gpos += n;
+    if (*gpos > ng) atomicOr(err, (unsigned)DERR_STREAM);
+  }
   __device__ double accept_u(int) { return take(u, nu, upos); }
   __device__ double disp_u(int) { return take(d, nd, dpos); }
 };
@@ -105,12 +170,14 @@ struct ReplaySrc {
 // counter-based source for production moves: one Philox block per draw
 struct PhiloxSrc {
   uint64_t seed, move;
-  __device__ double gauss_x1(int level, int k, int dim)
+  __device__ long gauss_base() { return 0; }
+  __device__ double gauss_at(long, int level, int k, int dim)
   {
     double r1, r2;
     philox_u2(seed, move, 0x100000u | ((uint32_t)level << 12) | (uint32_t)k, (uint32_t)dim, &r1, &r2);
     return sqrt(-log(r1)) * cos(2.0 * PIMC_PI * r2);        // Box-Muller as gauss() (mc_randg.cc:144)
   }
+  __device__ void gauss_advance(long) {}
   __device__ double accept_u(int level)
   {
     double u0, u1;
@@ -124,6 +191,23 @@ struct PhiloxSrc {
     return u0;
   }
 };
+
+// a translational commit at slice t invalidates the cached rotor potential
+// of the rotational slice t/R for every rotor
+__device__ __forceinline__ void invalidate_rotpot(const Ctx &c, int t)
+{
+  for (int r = 0; r < c.s.nrotors; r++) c.st.rp_ok[r * c.s.Q + t / c.s.R] = 0;
+}
+
+__device__ __forceinline__ void store_bead(const Ctx &c, size_t i, double x, double y, double z)
+{
+  c.st.x[i] = x;
+  c.st.y[i] = y;
+  c.st.z[i] = z;
+  c.st.xf[i] = (float)x;
+  c.st.yf[i] = (float)y;
+  c.st.zf[i] = (float)z;
+}
 
 // ------------------------------------------------------ bisection move
 // MCBisectionMove / MCBisectionMoveExchange (mc_piqmc.cc:194-419) for the
@@ -139,10 +223,11 @@ struct BisectShared {
   int owner[PIMC_MAX_SEG + 1], slice[PIMC_MAX_SEG + 1];
   double pot0, pot1;
   int acc, passed;
-  double part[SLOT_CHUNK][PIMC_BLOCK];
+  long gbase;
+  double buf[PIMC_RED_BUF];
 };
 
-template <class Src>
+template <bool MIX, class Src>
 __device__ int bisect_move(const Ctx &c, const Frame *frames, int type, int atom, int time0, int exch, Src &src,
                            BisectShared &sh, double *ds_out)
 {
@@ -154,7 +239,7 @@ __device__ int bisect_move(const Ctx &c, const Frame *frames, int type, int atom
   // (mc_piqmc.cc:312-313)
   int gx = exch ? s.first[type] + c.st.pindex[atom] : g0;
   if (gx < s.first[type] || gx >= s.first[type] + s.numb[type]) gx = g0;
-  for (int k = tid; k <= M; k += PIMC_BLOCK) {
+  for (int k = tid; k <= M; k += blockDim.x) {
     int t = time0 + k;
     int own = (exch && t >= P) ? gx : g0;
     int pt = t % P;
@@ -165,25 +250,23 @@ __device__ int bisect_move(const Ctx &c, const Frame *frames, int type, int atom
     sh.nb[1][k] = c.st.y[i];
     sh.nb[2][k] = c.st.z[i];
   }
-  if (tid == 0) { sh.pot0 = 0.0; sh.pot1 = 0.0; sh.acc = 0; sh.passed = 0; }
+  if (tid == 0) { sh.pot0 = 0.0; sh.pot1 = 0.0; sh.acc = 0; sh.passed = 0; sh.gbase = src.gauss_base(); }
   __syncthreads();
   double bnorm = 1.0 / (s.lambda[type] * s.tau);
   for (int level = 0; level < L; level++) {
     int seg = 1 << (L - level), half = seg >> 1, nmid = M / seg;
-    double bkin_norm = bnorm / (double)seg;
-    if (tid == 0) {
-      double sq = sqrt(bkin_norm);
-      for (int j = 0; j < nmid; j++) {
-        int k0 = j * seg, k1 = k0 + half, k2 = k0 + seg;
-        for (int d = 0; d < 3; d++) {
-          sh.nb[d][k1] = 0.5 * (sh.nb[d][k0] + sh.nb[d][k2]);
-          sh.nb[d][k1] += src.gauss_x1(level, j, d) / sq;       // gauss(bkin_norm) (mc_randg.cc:149)
-        }
-      }
+    double sq = sqrt(bnorm / (double)seg);            // sqrt of gauss()'s alpha (mc_randg.cc:149)
+    // midpoints in parallel: thread (j, d)
+    for (int k = tid; k < 3 * nmid; k += blockDim.x) {
+      int j = k / 3, d = k - 3 * j;
+      int k0 = j * seg, k1 = k0 + half, k2 = k0 + seg;
+      double v = 0.5 * (sh.nb[d][k0] + sh.nb[d][k2]);
+      v += src.gauss_at(sh.gbase, level, j, d) / sq;
+      sh.nb[d][k1] = v;
     }
     __syncthreads();
     // slots: (midpoint j, new) and (midpoint j, old)
-    for (int j = tid; j < nmid; j += PIMC_BLOCK) {
+    for (int j = tid; j < nmid; j += blockDim.x) {
       int k1 = j * seg + half;
       int own = sh.owner[k1], pt = sh.slice[k1];
       size_t i = sidx(s, pt, own);
@@ -192,9 +275,22 @@ __device__ int bisect_move(const Ctx &c, const Frame *frames, int type, int atom
       sh.sa[2 * j + 1] = own; sh.st[2 * j + 1] = pt;
       sh.sx[2 * j + 1] = c.st.x[i]; sh.sy[2 * j + 1] = c.st.y[i]; sh.sz[2 * j + 1] = c.st.z[i];
     }
+    if (tid == 0) { sh.gbase += 3 * nmid; src.gauss_advance(3 * nmid); }
     __syncthreads();
-    slot_energies(c, frames, 2 * nmid, sh.sa, sh.st, sh.sx, sh.sy, sh.sz, sh.se, sh.part);
-    for (int j = tid; j < nmid; j += PIMC_BLOCK) {
+    if (MIX)
+      slot_sums(2 * nmid, s.na, sh.sa,
+                [&](int sl, int p) -> double {
+                  return (double)pair_term32(c, frames, sh.sa[sl], p, sh.st[sl], (float)sh.sx[sl], (float)sh.sy[sl],
+                                             (float)sh.sz[sl]);
+                },
+                sh.se, sh.buf);
+    else
+      slot_sums(2 * nmid, s.na, sh.sa,
+                [&](int sl, int p) -> double {
+                  return pair_term64(c, frames, sh.sa[sl], p, sh.st[sl], sh.sx[sl], sh.sy[sl], sh.sz[sl]);
+                },
+                sh.se, sh.buf);
+    for (int j = tid; j < nmid; j += blockDim.x) {
       int k1 = j * seg + half;
       sh.en[k1] = sh.se[2 * j];
       sh.eo[k1] = sh.se[2 * j + 1];
@@ -223,11 +319,10 @@ __device__ int bisect_move(const Ctx &c, const Frame *frames, int type, int atom
   }
   int accepted = sh.acc;
   if (accepted) {
-    for (int k = 1 + tid; k < M; k += PIMC_BLOCK) {
+    for (int k = 1 + tid; k < M; k += blockDim.x) {
       size_t i = sidx(s, sh.slice[k], sh.owner[k]);
-      c.st.x[i] = sh.nb[0][k];
-      c.st.y[i] = sh.nb[1][k];
-      c.st.z[i] = sh.nb[2][k];
+      store_bead(c, i, sh.nb[0][k], sh.nb[1][k], sh.nb[2][k]);
+      invalidate_rotpot(c, sh.slice[k]);
     }
   }
   __syncthreads();
@@ -246,16 +341,17 @@ struct MolScratch {
 struct RotShared {
   Frame fo[3], fn;          // old frames at q-1, q, q+1 and the proposal at q
   double rho[4], pot[2];
-  double vals[2 * 16];      // per (it, old/new) PotRot sums, R <= 16
-  double ang_new[3], cos_new[3];
-  int bad, acc;
+  double vals[2 * 16];      // per (it, old/new) partner sums, R <= 16
+  double ang_new[3], nold[3], nnew[3];
+  int bad, acc, pot_cached, link_ok[2];
+  int skip[2 * 16];
   double rd;
-  double part[SLOT_CHUNK][PIMC_BLOCK];
+  double buf[PIMC_RED_BUF];
 };
 
 // PotRotE3D term (mc_piqmc.cc:2078-2146) for rotor g0 with body frame f at
 // slice it against partner a1
-__device__ __forceinline__ double rot3d_term(const Ctx &c, const Frame *frames, const Frame &f, int g0, int a1, int it)
+__device__ __forceinline__ double rot3d_term64(const Ctx &c, const Frame *frames, const Frame &f, int g0, int a1, int it)
 {
   const DevSys &s = c.s;
   size_t i0 = sidx(s, it, g0), i1 = sidx(s, it, a1);
@@ -265,9 +361,19 @@ __device__ __forceinline__ double rot3d_term(const Ctx &c, const Frame *frames, 
                 c.st.z[i1]);
 }
 
+__device__ __forceinline__ float rot3d_term32(const Ctx &c, const Frame *frames, const Frame &f, int g0, int a1, int it)
+{
+  const DevSys &s = c.s;
+  size_t i0 = sidx(s, it, g0), i1 = sidx(s, it, a1);
+  if (c.st.mctype[a1] != s.imtype)
+    return vcord32(c.t, f, c.st.xf[i1] - c.st.xf[i0], c.st.yf[i1] - c.st.yf[i0], c.st.zf[i1] - c.st.zf[i0]);
+  return (float)caleng(f, frames[rot_index(s, a1, it / s.R)], c.st.x[i0], c.st.y[i0], c.st.z[i0], c.st.x[i1],
+                       c.st.y[i1], c.st.z[i1]);
+}
+
 // PotRotEnergy term (mc_piqmc.cc:1987-2040) for the linear rotor g0 with unit
 // vector n at slice it against partner a1
-__device__ __forceinline__ double rotlin_term(const Ctx &c, const double n[3], int g0, int a1, int it)
+__device__ __forceinline__ double rotlin_term64(const Ctx &c, const double n[3], int g0, int a1, int it)
 {
   const DevSys &s = c.s;
   size_t i0 = sidx(s, it, g0), i1 = sidx(s, it, a1);
@@ -286,203 +392,212 @@ __device__ __forceinline__ double rotlin_term(const Ctx &c, const double n[3], i
   return lpot2d(c.t, r, cost);
 }
 
-// sum over it in [q*R, q*R+R) of the rotor's partner sums for the old
-// (slot 0) and new (slot 1) orientation, in the reference's order
-__device__ inline void rot_pots(const Ctx &c, const Frame *frames, int g0, int q, bool linear, const double *nold,
-                         const double *nnew, RotShared &sh)
+__device__ __forceinline__ float rotlin_term32(const Ctx &c, const double n[3], int g0, int a1, int it)
 {
   const DevSys &s = c.s;
-  int tid = threadIdx.x, R = s.R;
-  int nslots = 2 * R;
-  for (int base = 0; base < nslots; base += SLOT_CHUNK) {
-    int ns = min(SLOT_CHUNK, nslots - base);
-    for (int k = 0; k < ns; k++) {
-      int sl = base + k, it = q * R + (sl >> 1), isnew = sl & 1;
-      double acc = 0.0;
-      for (int p = tid; p < s.na; p += PIMC_BLOCK)
-        if (p != g0) {
-          if (linear) acc += rotlin_term(c, isnew ? nnew : nold, g0, p, it);
-          else acc += rot3d_term(c, frames, isnew ? sh.fn : sh.fo[1], g0, p, it);
-        }
-      sh.part[k][tid] = acc;
-    }
-    __syncthreads();
-    if (tid < ns) {
-      double sum = 0.0;
-      for (int k = 0; k < PIMC_BLOCK; k++) sum += sh.part[tid][k];
-      sh.vals[base + tid] = sum;
-    }
-    __syncthreads();
-  }
-  if (tid == 0) {
-    double po = 0.0, pn = 0.0;
-    for (int k = 0; k < R; k++) { po += sh.vals[2 * k]; pn += sh.vals[2 * k + 1]; }
-    sh.pot[0] = po;
-    sh.pot[1] = pn;
-  }
-  __syncthreads();
+  size_t i0 = sidx(s, it, g0), i1 = sidx(s, it, a1);
+  float dx = c.st.xf[i0] - c.st.xf[i1], dy = c.st.yf[i0] - c.st.yf[i1], dz = c.st.zf[i0] - c.st.zf[i1];
+  float r = sqrtf(dx * dx + dy * dy + dz * dz);
+  float cost = -((float)n[0] * dx + (float)n[1] * dy + (float)n[2] * dz) / r;
+  return lpot2d32(c.t, r, cost);
 }
 
-// MCRot3Dstep (mc_piqmc.cc:938-1199) for rotor g0 at rotational slice q with
-// uniforms u[4]; frames of the rotor slices are read from / written to the
-// frame cache.  Returns 1 if accepted.
-__device__ inline int rot3d_step(const Ctx &c, Frame *frames, int g0, int q, const double u[4], RotShared &sh, double *rd_out)
+// link density of two neighbouring rotational slices: rotden's rho
+// (rotden.f:1-31) or rsrot's log-density for a top, SRotDens(n.n') or
+// rsline's for a linear rotor (mc_piqmc.cc:838-847, 1021-1035)
+__device__ __forceinline__ double link_density(const Ctx &c, bool linear, const Frame &a, const Frame &b,
+                                               const double *na, const double *nb, int *bad)
 {
   const DevSys &s = c.s;
-  int tid = threadIdx.x, Q = s.Q;
+  double rho = 0.0, erot = 0.0;
+  if (linear) {
+    double p = 0.0;
+    for (int d = 0; d < 3; d++) p += (na[d] * nb[d]);
+    if (s.rot_den_type == 0) rho = srotdens(c.t, p, 0);
+    else rsline(s.abc[0], p, s.rot_tau, &rho, &erot);
+  } else {
+    if (s.rot_den_type == 0) rho = rotden_rho(c.t, a, b, bad, nullptr, nullptr);
+    else rsrot(a, b, s.abc, s.rot_tau, s.rot_odevn, &rho, &erot);
+  }
+  return rho;
+}
+
+// MCRotLinStep (mc_piqmc.cc:781-936) / MCRot3Dstep (mc_piqmc.cc:938-1199)
+// for rotor g0 at rotational slice q with uniforms u (3 for a linear rotor,
+// 4 for a top).  The old potential and the old link densities come from the
+// caches when they are valid; both caches hold exactly the value a fresh
+// evaluation gives.  Returns 1 if accepted.
+template <bool MIX>
+__device__ int rot_step(const Ctx &c, Frame *frames, int g0, int q, const double u[4], bool linear, RotShared &sh,
+                        double *rd_out)
+{
+  const DevSys &s = c.s;
+  int tid = threadIdx.x, Q = s.Q, R = s.R;
   size_t n = (size_t)s.nrotors * Q;
   int q0 = q - 1, q2 = q + 1;
   if (q0 < 0) q0 += Q;
   if (q2 >= Q) q2 -= Q;
-  int r1 = rot_index(s, g0, q);
+  int r = g0 - s.rot_first;
+  int i0 = r * Q + q0, i1 = r * Q + q, i2 = r * Q + q2;
+  bool use_links = Q >= 3;
   if (tid == 0) {
-    double cost = c.st.ang[n + r1], phi = c.st.ang[r1], chi = c.st.ang[2 * n + r1];
-    const double pi2 = 2.0 * PIMC_PI;
-    cost += (s.rtstep * (u[0] - 0.5));
-    phi += 2.0 * PIMC_PI * (s.rtstep * (u[1] - 0.5));
-    chi += 2.0 * PIMC_PI * (s.rtstep * (u[2] - 0.5));
-    if (phi < 0.0) phi = pi2 + phi;
-    if (chi < 0.0) chi = pi2 + chi;
-    phi = fmod(phi, pi2);
-    chi = fmod(chi, pi2);
-    if (cost > 1.0) cost = 2.0 - cost;
-    if (cost < -1.0) cost = -2.0 - cost;
-    sh.ang_new[0] = phi; sh.ang_new[1] = cost; sh.ang_new[2] = chi;
-    make_frame(phi, cost, chi, sh.fn);
-    sh.fo[0] = frames[rot_index(s, g0, q0)];
-    sh.fo[1] = frames[r1];
-    sh.fo[2] = frames[rot_index(s, g0, q2)];
-    sh.bad = 0;
-  }
-  __syncthreads();
-  if (tid < 4) {
-    const Frame &a = (tid == 0) ? sh.fo[0] : (tid == 1 ? sh.fo[1] : (tid == 2 ? sh.fo[0] : sh.fn));
-    const Frame &b = (tid == 0) ? sh.fo[1] : (tid == 1 ? sh.fo[2] : (tid == 2 ? sh.fn : sh.fo[2]));
-    double rho = 0.0, erot = 0.0;
-    if (s.rot_den_type == 0) {
-      int bad = 0;
-      rho = rotden_rho(c.t, a, b, &bad, nullptr, nullptr);
-      if (bad) atomicOr(&sh.bad, 1);
-    } else {
-      rsrot(a, b, s.abc, s.rot_tau, s.rot_odevn, &rho, &erot);
-    }
-    sh.rho[tid] = rho;
-  }
-  rot_pots(c, frames, g0, q, false, nullptr, nullptr, sh);
-  int acc = 0;
-  if (tid == 0) {
-    double rd;
-    if (s.rot_den_type == 0) {
-      double dens_old = sh.rho[0] * sh.rho[1], dens_new = sh.rho[2] * sh.rho[3];
-      if (fabs(dens_old) < PIMC_RZERO) dens_old = 0.0;
-      if (dens_old < 0.0) dens_old = fabs(dens_old);
-      if (fabs(dens_new) < PIMC_RZERO) dens_new = 0.0;
-      if (dens_new < 0.0) dens_new = fabs(dens_new);
-      rd = (dens_old > PIMC_RZERO) ? dens_new / dens_old : 1.0;
-      rd *= exp(-s.tau * (sh.pot[1] - sh.pot[0]));
-      acc = (rd > 1.0) || (rd > u[3]);
-    } else {
-      double rhoold = sh.rho[0] + sh.rho[1], rhonew = sh.rho[2] + sh.rho[3];
-      rd = (rhonew - rhoold) / (4.0 * (s.rot_tau / PIMC_WNO2K));
-      rd -= s.tau * (sh.pot[1] - sh.pot[0]);
-      acc = (rd > 0.0) || (rd > log(u[3]));
-    }
-    if (sh.bad) { atomicOr(c.st.err, (unsigned)DERR_GRID_RANGE); acc = 0; }
-    sh.rd = rd;
-    sh.acc = acc;
-    if (rd_out) *rd_out = rd;
-    if (acc) {
-      double phi = sh.ang_new[0], cost = sh.ang_new[1], chi = sh.ang_new[2];
-      c.st.ang[r1] = phi;
-      c.st.ang[n + r1] = cost;
-      c.st.ang[2 * n + r1] = chi;
+    double cost = c.st.ang[n + i1], phi = c.st.ang[i1], chi = c.st.ang[2 * n + i1];
+    if (linear) {
+      cost += (s.rtstep * (u[0] - 0.5));
+      phi += (s.rtstep * (u[1] - 0.5));
+      if (cost > 1.0) cost = 2.0 - cost;
+      if (cost < -1.0) cost = -2.0 - cost;
       double sint = sqrt(1.0 - cost * cost);
-      c.st.cosv[r1] = sint * cos(phi);
-      c.st.cosv[n + r1] = sint * sin(phi);
-      c.st.cosv[2 * n + r1] = cost;
-      frames[r1] = sh.fn;
+      sh.nnew[0] = sint * cos(phi);
+      sh.nnew[1] = sint * sin(phi);
+      sh.nnew[2] = cost;
+      for (int d = 0; d < 3; d++) sh.nold[d] = c.st.cosv[d * n + i1];
+    } else {
+      const double pi2 = 2.0 * PIMC_PI;
+      cost += (s.rtstep * (u[0] - 0.5));
+      phi += 2.0 * PIMC_PI * (s.rtstep * (u[1] - 0.5));
+      chi += 2.0 * PIMC_PI * (s.rtstep * (u[2] - 0.5));
+      if (phi < 0.0) phi = pi2 + phi;
+      if (chi < 0.0) chi = pi2 + chi;
+      phi = fmod(phi, pi2);
+      chi = fmod(chi, pi2);
+      if (cost > 1.0) cost = 2.0 - cost;
+      if (cost < -1.0) cost = -2.0 - cost;
+      make_frame(phi, cost, chi, sh.fn);
+      sh.fo[0] = frames[i0];
+      sh.fo[1] = frames[i1];
+      sh.fo[2] = frames[i2];
     }
+    sh.ang_new[0] = phi; sh.ang_new[1] = cost; sh.ang_new[2] = chi;
+    sh.bad = 0;
+    sh.pot_cached = c.st.rp_ok[i1];
+    if (sh.pot_cached) sh.pot[0] = c.st.rp_cache[i1];
+    sh.link_ok[0] = use_links && c.st.rl_ok[i0];
+    sh.link_ok[1] = use_links && c.st.rl_ok[i1];
+    if (sh.link_ok[0]) sh.rho[0] = c.st.rl_cache[i0];
+    if (sh.link_ok[1]) sh.rho[1] = c.st.rl_cache[i1];
+    for (int k = 0; k < 2 * R; k++) sh.skip[k] = g0;
   }
   __syncthreads();
-  acc = sh.acc;
-  __syncthreads();
-  return acc;
-}
-
-// MCRotLinStep (mc_piqmc.cc:781-936) for the linear rotor g0 at slice q
-__device__ inline int rotlin_step(const Ctx &c, Frame *frames, int g0, int q, const double u[3], RotShared &sh, double *rd_out)
-{
-  const DevSys &s = c.s;
-  int tid = threadIdx.x, Q = s.Q;
-  size_t n = (size_t)s.nrotors * Q;
-  int q0 = q - 1, q2 = q + 1;
-  if (q0 < 0) q0 += Q;
-  if (q2 >= Q) q2 -= Q;
-  int r0 = rot_index(s, g0, q0), r1 = rot_index(s, g0, q), r2 = rot_index(s, g0, q2);
-  __shared__ double nold[3], nnew[3];
-  if (tid == 0) {
-    double cost = c.st.ang[n + r1], phi = c.st.ang[r1];
-    cost += (s.rtstep * (u[0] - 0.5));
-    phi += (s.rtstep * (u[1] - 0.5));
-    if (cost > 1.0) cost = 2.0 - cost;
-    if (cost < -1.0) cost = -2.0 - cost;
-    double sint = sqrt(1.0 - cost * cost);
-    sh.ang_new[0] = phi; sh.ang_new[1] = cost;
-    nnew[0] = sint * cos(phi);
-    nnew[1] = sint * sin(phi);
-    nnew[2] = cost;
-    for (int d = 0; d < 3; d++) nold[d] = c.st.cosv[d * n + r1];
-    double p0 = 0.0, p1 = 0.0, q0v = 0.0, q1v = 0.0;
-    for (int d = 0; d < 3; d++) {
-      p0 += (c.st.cosv[d * n + r0] * c.st.cosv[d * n + r1]);
-      p1 += (c.st.cosv[d * n + r1] * c.st.cosv[d * n + r2]);
+  if (tid < 4 && !(tid < 2 && sh.link_ok[tid])) {
+    // 0: (q-1, q) old, 1: (q, q+1) old, 2: (q-1, q) new, 3: (q, q+1) new
+    double na[3] = {0.0, 0.0, 0.0}, nb[3] = {0.0, 0.0, 0.0};
+    const Frame &fa = (tid == 0 || tid == 2) ? sh.fo[0] : (tid == 1 ? sh.fo[1] : sh.fn);
+    const Frame &fb = (tid == 0) ? sh.fo[1] : (tid == 2 ? sh.fn : sh.fo[2]);
+    if (linear) {
+      int ia = (tid == 0 || tid == 2) ? i0 : i1, ib = (tid == 1 || tid == 3) ? i2 : i1;
+      for (int d = 0; d < 3; d++) {
+        na[d] = (tid == 3) ? sh.nnew[d] : c.st.cosv[d * n + ia];
+        nb[d] = (tid == 2) ? sh.nnew[d] : c.st.cosv[d * n + ib];
+      }
     }
-    for (int d = 0; d < 3; d++) {
-      q0v += (c.st.cosv[d * n + r0] * nnew[d]);
-      q1v += (nnew[d] * c.st.cosv[d * n + r2]);
-    }
-    sh.rho[0] = p0; sh.rho[1] = p1; sh.rho[2] = q0v; sh.rho[3] = q1v;   // dot products for now
+    int bad = 0;
+    sh.rho[tid] = link_density(c, linear, fa, fb, na, nb, &bad);
+    if (bad) atomicOr(&sh.bad, 1);
   }
-  __syncthreads();
-  if (tid < 4) {
-    double g = sh.rho[tid];
-    double v, erot;
-    if (s.rot_den_type == 0) v = srotdens(c.t, g, 0);
-    else rsline(s.abc[0], g, s.rot_tau, &v, &erot);
-    sh.vals[tid] = v;
+  // partner sums: slots [0, R) old (unless cached), then R new
+  int first = sh.pot_cached ? R : 0;
+  int nsl = 2 * R - first;
+  if (linear) {
+    if (MIX)
+      slot_sums(nsl, s.na, sh.skip,
+                [&](int sl, int p) -> double {
+                  int k = sl + first;
+                  return (double)rotlin_term32(c, k < R ? sh.nold : sh.nnew, g0, p, q * R + (k % R));
+                },
+                sh.vals, sh.buf);
+    else
+      slot_sums(nsl, s.na, sh.skip,
+                [&](int sl, int p) -> double {
+                  int k = sl + first;
+                  return rotlin_term64(c, k < R ? sh.nold : sh.nnew, g0, p, q * R + (k % R));
+                },
+                sh.vals, sh.buf);
+  } else {
+    if (MIX)
+      slot_sums(nsl, s.na, sh.skip,
+                [&](int sl, int p) -> double {
+                  int k = sl + first;
+                  return (double)rot3d_term32(c, frames, k < R ? sh.fo[1] : sh.fn, g0, p, q * R + (k % R));
+                },
+                sh.vals, sh.buf);
+    else
+      slot_sums(nsl, s.na, sh.skip,
+                [&](int sl, int p) -> double {
+                  int k = sl + first;
+                  return rot3d_term64(c, frames, k < R ? sh.fo[1] : sh.fn, g0, p, q * R + (k % R));
+                },
+                sh.vals, sh.buf);
   }
-  __syncthreads();
   if (tid == 0) {
-    for (int k = 0; k < 4; k++) sh.rho[k] = sh.vals[k];
-  }
-  __syncthreads();
-  rot_pots(c, frames, g0, q, true, nold, nnew, sh);
-  if (tid == 0) {
+    double pot_old = 0.0, pot_new = 0.0;
+    if (sh.pot_cached) pot_old = sh.pot[0];
+    else
+      for (int k = 0; k < R; k++) pot_old += sh.vals[k];
+    for (int k = 0; k < R; k++) pot_new += sh.vals[R - first + k];
     double rd;
     int acc = 0, neg = 0;
     if (s.rot_den_type == 0) {
       double dens_old = sh.rho[0] * sh.rho[1], dens_new = sh.rho[2] * sh.rho[3];
       if (fabs(dens_old) < PIMC_RZERO) dens_old = 0.0;
-      if (dens_old < 0.0) neg = 1;
       if (fabs(dens_new) < PIMC_RZERO) dens_new = 0.0;
-      if (dens_new < 0.0) neg = 1;
+      if (linear) {
+        if (dens_old < 0.0 || dens_new < 0.0) neg = 1;          // mc_piqmc.cc:850,886
+      } else {
+        if (dens_old < 0.0) dens_old = fabs(dens_old);          // mc_piqmc.cc:1067,1133
+        if (dens_new < 0.0) dens_new = fabs(dens_new);
+      }
       rd = (dens_old > PIMC_RZERO) ? dens_new / dens_old : 1.0;
-      rd *= exp(-s.tau * (sh.pot[1] - sh.pot[0]));
-      acc = (rd > 1.0) || (rd > u[2]);
-    } else {
+      rd *= exp(-s.tau * (pot_new - pot_old));
+      acc = (rd > 1.0) || (rd > u[linear ? 2 : 3]);
+    } else if (linear) {
       double dens_old = sh.rho[0] + sh.rho[1], dens_new = sh.rho[2] + sh.rho[3];
       if (fabs(dens_old) < PIMC_RZERO) dens_old = 0.0;
       if (fabs(dens_new) < PIMC_RZERO) dens_new = 0.0;
-      rd = dens_new - dens_old - s.tau * (sh.pot[1] - sh.pot[0]);
+      rd = dens_new - dens_old - s.tau * (pot_new - pot_old);
       acc = (rd > 0.0) || (rd > log(u[2]));
+    } else {
+      double rhoold = sh.rho[0] + sh.rho[1], rhonew = sh.rho[2] + sh.rho[3];
+      rd = (rhonew - rhoold) / (4.0 * (s.rot_tau / PIMC_WNO2K));
+      rd -= s.tau * (pot_new - pot_old);
+      acc = (rd > 0.0) || (rd > log(u[3]));
     }
     if (neg) { atomicOr(c.st.err, (unsigned)DERR_NEG_DENSITY); acc = 0; }
+    if (sh.bad) { atomicOr(c.st.err, (unsigned)DERR_GRID_RANGE); acc = 0; }
+    sh.rd = rd;
     sh.acc = acc;
     if (rd_out) *rd_out = rd;
     if (acc) {
-      c.st.ang[n + r1] = sh.ang_new[1];
-      c.st.ang[r1] = sh.ang_new[0];
-      for (int d = 0; d < 3; d++) c.st.cosv[d * n + r1] = nnew[d];
+      double phi = sh.ang_new[0], cost = sh.ang_new[1];
+      c.st.ang[i1] = phi;
+      c.st.ang[n + i1] = cost;
+      if (linear) {
+        for (int d = 0; d < 3; d++) {
+          c.st.cosv[d * n + i1] = sh.nnew[d];
+          c.st.cosvf[d * n + i1] = (float)sh.nnew[d];
+        }
+      } else {
+        double chi = sh.ang_new[2];
+        c.st.ang[2 * n + i1] = chi;
+        double sint = sqrt(1.0 - cost * cost);
+        double cv[3] = {sint * cos(phi), sint * sin(phi), cost};
+        for (int d = 0; d < 3; d++) {
+          c.st.cosv[d * n + i1] = cv[d];
+          c.st.cosvf[d * n + i1] = (float)cv[d];
+        }
+        frames[i1] = sh.fn;
+        // the other rotors' potentials at slice q depend on this orientation
+        for (int rr = 0; rr < s.nrotors; rr++)
+          if (rr != r) c.st.rp_ok[rr * Q + q] = 0;
+      }
+    }
+    c.st.rp_cache[i1] = acc ? pot_new : pot_old;
+    c.st.rp_ok[i1] = 1;
+    if (use_links && !sh.bad) {
+      c.st.rl_cache[i0] = acc ? sh.rho[2] : sh.rho[0];
+      c.st.rl_cache[i1] = acc ? sh.rho[3] : sh.rho[1];
+      c.st.rl_ok[i0] = 1;
+      c.st.rl_ok[i1] = 1;
     }
   }
   __syncthreads();
