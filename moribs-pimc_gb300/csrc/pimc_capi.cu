@@ -148,6 +148,22 @@ static void spline_y2(const double *x, const double *y, int n, double *y2)
   for (int k = n - 2; k >= 0; k--) y2[k] = y2[k] * y2[k + 1] + u[k];
 }
 
+// a grid on which the spline index can be computed: monotonic, and no node
+// more than half a step away from x0 + i*h
+static bool near_uniform(const double *x, int n, double *x0, double *ih)
+{
+  if (n < 3) return false;
+  double h = (x[n - 1] - x[0]) / (double)(n - 1);
+  if (!(h > 0.0)) return false;
+  for (int i = 1; i < n; i++) {
+    if (!(x[i] > x[i - 1])) return false;
+    if (fabs(x[i] - (x[0] + i * h)) > 0.5 * h) return false;
+  }
+  *x0 = x[0];
+  *ih = 1.0 / h;
+  return true;
+}
+
 // ------------------------------------------------------------ life cycle
 
 extern "C" pimc_status pimc_create(const pimc_system *sys, int device, pimc_handle **out)
@@ -309,6 +325,7 @@ extern "C" pimc_status pimc_load_tables(pimc_handle *h, const pimc_tables *tb)
         (e = upload(h, y2.data(), n, &t.y21d)) || (e = upload_f32(h, tb->grid1d, n, &t.g1d32)) ||
         (e = upload_f32(h, tb->pot1d, n, &t.p1d32)) || (e = upload_f32(h, y2.data(), n, &t.y21d32)))
       return e;
+    t.uni1d = near_uniform(tb->grid1d, n, &t.x01d, &t.ih1d) ? 1 : 0;
     // short- and long-range extrapolation constants (mc_poten.cc:418-437)
     double fr = tb->pot1d[0] / tb->pot1d[1];
     double dr = tb->grid1d[1] - tb->grid1d[0];
@@ -351,6 +368,7 @@ extern "C" pimc_status pimc_load_tables(pimc_handle *h, const pimc_tables *tb)
     int n = tb->nrot;
     if (n < 2 || !tb->rotgrid || !tb->rotdens || !tb->rotderv || !tb->rotesqr) return PIMC_ERR_BAD_TABLE;
     std::vector<double> a(n), b(n), c(n);
+    t.unirot = near_uniform(tb->rotgrid, n, &t.x0rot, &t.ihrot) ? 1 : 0;
     spline_y2(tb->rotgrid, tb->rotdens, n, a.data());              // init_rotdens mc_poten.cc:543-545
     spline_y2(tb->rotgrid, tb->rotderv, n, b.data());
     spline_y2(tb->rotgrid, tb->rotesqr, n, c.data());

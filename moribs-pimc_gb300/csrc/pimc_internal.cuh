@@ -24,6 +24,8 @@ struct DevTables {
   const double *g1d, *p1d, *y21d;
   const float *g1d32, *p1d32, *y21d32;
   double alpha1d, unode1d, c61d;
+  int uni1d;                    // grid uniform: direct index (see splint)
+  double x01d, ih1d;
   // 2D bilinear, LPot2D (mc_poten.cc:688-729)
   int nr2d, nc2d;
   double dr2d, dc2d;
@@ -37,6 +39,8 @@ struct DevTables {
   // linear rotor density, SRotDens (mc_poten.cc:548-622)
   int nrot;
   const double *rg, *rd, *rdv, *rde, *rd_y2, *rdv_y2, *rde_y2;
+  int unirot;
+  double x0rot, ihrot;
   // nonlinear rotor density, rotden/rotpro (rotden.f, rotpro_sub.f)
   int nth, nph, nch;
   double dthd, dphd, dchd;
@@ -95,7 +99,7 @@ struct Ctx {
 // Body frame of a nonlinear rotor: the columns of matpre(phi, acos(cost), chi)
 // (rotden.f:136-163, vcord.f:31-36) plus |hatz| as dnorm computes it.
 struct Frame {
-  double e[3];          // phi, theta, chi
+  double e[3];          // phi, cos theta, chi
   double m[9];          // rotmat(i,j) at m[i*3+j]
   double hz_norm;
   float mf[9];          // float copy for the FP32 path
@@ -119,12 +123,26 @@ __device__ __forceinline__ void matpre(const double e[3], double m[9])
   m[8] = ct;
 }
 
+// cos and sin of theta = acos(cost) are cost and sqrt((1-cost)(1+cost)): the
+// same matrix as matpre(phi, acos(cost), chi) without the acos/sincos chain
 __device__ __forceinline__ void make_frame(double phi, double cost, double chi, Frame &f)
 {
+  double sp, cp, sk, ck;
+  sincos(phi, &sp, &cp);
+  sincos(chi, &sk, &ck);
+  double ct = cost, st = sqrt((1.0 - cost) * (1.0 + cost));
   f.e[0] = phi;
-  f.e[1] = acos(cost);
+  f.e[1] = cost;
   f.e[2] = chi;
-  matpre(f.e, f.m);
+  f.m[0] = cp * ct * ck - sp * sk;
+  f.m[1] = -cp * ct * sk - sp * ck;
+  f.m[2] = cp * st;
+  f.m[3] = sp * ct * ck + cp * sk;
+  f.m[4] = -sp * ct * sk + cp * ck;
+  f.m[5] = sp * st;
+  f.m[6] = -st * ck;
+  f.m[7] = st * sk;
+  f.m[8] = ct;
   double s = 0.0;
   s = s + f.m[2] * f.m[2];
   s = s + f.m[5] * f.m[5];
@@ -136,16 +154,34 @@ __device__ __forceinline__ void make_frame(double phi, double cost, double chi, 
 
 // ------------------------------------------------------------------ leaves
 
-// splint (mc_utils.cc:156-186): bisection for klo, then the cubic
-__device__ __forceinline__ double splint(const double *__restrict__ xa, const double *__restrict__ ya,
-                                         const double *__restrict__ y2a, int n, double x)
+// klo of splint's bisection (mc_utils.cc:170-176): the largest k <= n-2 with
+// xa[k] <= x.  On a uniform grid (uni != 0) the index is computed and then
+// corrected by whole steps until that condition holds, which returns the
+// bisection's klo exactly.
+__device__ __forceinline__ int spline_klo(const double *__restrict__ xa, int n, double x, int uni, double x0, double ih)
 {
+  if (uni && x == x) {
+    double g = (x - x0) * ih;
+    int k = g < 0.0 ? 0 : (g > (double)(n - 2) ? n - 2 : (int)g);
+    while (k < n - 2 && __ldg(xa + k + 1) <= x) k++;
+    while (k > 0 && __ldg(xa + k) > x) k--;
+    return k;
+  }
   int klo = 0, khi = n - 1;
   while (khi - klo > 1) {
     int k = (khi + klo) >> 1;
     if (__ldg(xa + k) > x) khi = k;
     else klo = k;
   }
+  return klo;
+}
+
+// splint (mc_utils.cc:156-186): bisection for klo, then the cubic
+__device__ __forceinline__ double splint(const double *__restrict__ xa, const double *__restrict__ ya,
+                                         const double *__restrict__ y2a, int n, double x, int uni = 0,
+                                         double x0 = 0.0, double ih = 0.0)
+{
+  int klo = spline_klo(xa, n, x, uni, x0, ih), khi = klo + 1;
   double xk = __ldg(xa + khi), xl = __ldg(xa + klo);
   double h = xk - xl;
   double a = (xk - x) / h;
@@ -159,7 +195,7 @@ __device__ __forceinline__ double spot1d(const DevTables &t, double r)
 {
   if (r >= __ldg(t.g1d + t.n1d - 1)) return -t.c61d / pow(r, 6.0);
   if (r <= __ldg(t.g1d)) return t.unode1d * exp(-t.alpha1d * r);
-  return splint(t.g1d, t.p1d, t.y21d, t.n1d, r);
+  return splint(t.g1d, t.p1d, t.y21d, t.n1d, r, t.uni1d, t.x01d, t.ih1d);
 }
 
 // LPot2D (mc_poten.cc:688-729): clamped index, unclamped fraction
@@ -195,7 +231,7 @@ __device__ __forceinline__ double srotdens(const DevTables &t, double g, int whi
     double sbeta = (__ldg(d) * rr - __ldg(d + 1) * rl) / (rr - rl);
     return salpha * g + sbeta;
   }
-  return splint(t.rg, d, y2, n, g);
+  return splint(t.rg, d, y2, n, g, t.unirot, t.x0rot, t.ihrot);
 }
 
 __device__ __forceinline__ double within1(double v)
@@ -218,7 +254,7 @@ __device__ __forceinline__ void deleul(const double m1[9], const double m2in[9],
   const double small = 1.e-08, pi = PIMC_PI;
   double cost = within1(m2[8]);
   double theta2 = acos(cost);
-  double sint = sin(theta2);
+  double sint = sqrt((1.0 - cost) * (1.0 + cost));   // sin(acos(cost)), independent of the acos
   double phi2, chi2, cchi, schi;
   if (fabs(1.0 - cost) < small) {
     phi2 = 0.0;
@@ -400,14 +436,25 @@ __device__ __forceinline__ double vcord(const DevTables &t, const Frame &f, doub
 // and pi.
 
 __device__ __forceinline__ float splint32(const float *__restrict__ xa, const float *__restrict__ ya,
-                                          const float *__restrict__ y2a, int n, float x)
+                                          const float *__restrict__ y2a, int n, float x, int uni, float x0, float ih)
 {
-  int klo = 0, khi = n - 1;
-  while (khi - klo > 1) {
-    int k = (khi + klo) >> 1;
-    if (__ldg(xa + k) > x) khi = k;
-    else klo = k;
+  int klo;
+  if (uni && x == x) {
+    float g = (x - x0) * ih;
+    int k = g < 0.0f ? 0 : (g > (float)(n - 2) ? n - 2 : (int)g);
+    while (k < n - 2 && __ldg(xa + k + 1) <= x) k++;
+    while (k > 0 && __ldg(xa + k) > x) k--;
+    klo = k;
+  } else {
+    klo = 0;
+    int khi = n - 1;
+    while (khi - klo > 1) {
+      int k = (khi + klo) >> 1;
+      if (__ldg(xa + k) > x) khi = k;
+      else klo = k;
+    }
   }
+  int khi = klo + 1;
   float xk = __ldg(xa + khi), xl = __ldg(xa + klo);
   float h = xk - xl;
   float a = (xk - x) / h, b = (x - xl) / h;
@@ -422,7 +469,7 @@ __device__ __forceinline__ float spot1d32(const DevTables &t, float r)
     return (float)(-t.c61d) / (r2 * r2 * r2);
   }
   if (r <= __ldg(t.g1d32)) return (float)t.unode1d * expf(-(float)t.alpha1d * r);
-  return splint32(t.g1d32, t.p1d32, t.y21d32, t.n1d, r);
+  return splint32(t.g1d32, t.p1d32, t.y21d32, t.n1d, r, t.uni1d, (float)t.x01d, (float)t.ih1d);
 }
 
 __device__ __forceinline__ float lpot2d32(const DevTables &t, float r, float cost)

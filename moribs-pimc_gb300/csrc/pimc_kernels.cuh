@@ -163,6 +163,8 @@ struct ReplaySrc {
     *gpos += n;
     if (*gpos > ng) atomicOr(err, (unsigned)DERR_STREAM);
   }
+  // prefetch of draw i of the move (levels not reached are never consumed)
+  __device__ double gauss_pre(long base, int i, int, int, int) { return (base + i < ng) ? g[base + i] : 0.0; }
   __device__ double accept_u(int) { return take(u, nu, upos); }
   __device__ double disp_u(int) { return take(d, nd, dpos); }
 };
@@ -178,6 +180,7 @@ struct PhiloxSrc {
     return sqrt(-log(r1)) * cos(2.0 * PIMC_PI * r2);        // Box-Muller as gauss() (mc_randg.cc:144)
   }
   __device__ void gauss_advance(long) {}
+  __device__ double gauss_pre(long, int, int level, int k, int dim) { return gauss_at(0, level, k, dim); }
   __device__ double accept_u(int level)
   {
     double u0, u1;
@@ -216,6 +219,7 @@ __device__ __forceinline__ void store_bead(const Ctx &c, size_t i, double x, dou
 // the path closes through); the midpoint energy is that of the slice's owner.
 // Returns 1 when accepted; records per-level action differences.
 struct BisectShared {
+  double gz[3 * PIMC_MAX_SEG];        // all Gaussian draws of the move, level by level
   double nb[3][PIMC_MAX_SEG + 1];
   double en[PIMC_MAX_SEG + 1], eo[PIMC_MAX_SEG + 1];
   double sx[PIMC_MAX_SEG], sy[PIMC_MAX_SEG], sz[PIMC_MAX_SEG], se[PIMC_MAX_SEG];
@@ -252,22 +256,27 @@ __device__ int bisect_move(const Ctx &c, const Frame *frames, int type, int atom
   }
   if (tid == 0) { sh.pot0 = 0.0; sh.pot1 = 0.0; sh.acc = 0; sh.passed = 0; sh.gbase = src.gauss_base(); }
   __syncthreads();
+  // the move's Gaussian draws, all levels at once: level l's midpoint j,
+  // dimension d is draw 3(2^l - 1) + 3j + d (the reference's order)
+  for (int i = tid; i < 3 * (M - 1); i += blockDim.x) {
+    int l = 31 - __clz(i / 3 + 1);
+    int off = i - 3 * ((1 << l) - 1);
+    sh.gz[i] = src.gauss_pre(sh.gbase, i, l, off / 3, off - 3 * (off / 3));
+  }
+  __syncthreads();
   double bnorm = 1.0 / (s.lambda[type] * s.tau);
   for (int level = 0; level < L; level++) {
     int seg = 1 << (L - level), half = seg >> 1, nmid = M / seg;
     double sq = sqrt(bnorm / (double)seg);            // sqrt of gauss()'s alpha (mc_randg.cc:149)
-    // midpoints in parallel: thread (j, d)
-    for (int k = tid; k < 3 * nmid; k += blockDim.x) {
-      int j = k / 3, d = k - 3 * j;
-      int k0 = j * seg, k1 = k0 + half, k2 = k0 + seg;
-      double v = 0.5 * (sh.nb[d][k0] + sh.nb[d][k2]);
-      v += src.gauss_at(sh.gbase, level, j, d) / sq;
-      sh.nb[d][k1] = v;
-    }
-    __syncthreads();
-    // slots: (midpoint j, new) and (midpoint j, old)
+    const double *gz = sh.gz + 3 * (nmid - 1);
+    // midpoint j and its (new, old) slots by thread j
     for (int j = tid; j < nmid; j += blockDim.x) {
-      int k1 = j * seg + half;
+      int k0 = j * seg, k1 = k0 + half, k2 = k0 + seg;
+      for (int d = 0; d < 3; d++) {
+        double v = 0.5 * (sh.nb[d][k0] + sh.nb[d][k2]);
+        v += gz[3 * j + d] / sq;
+        sh.nb[d][k1] = v;
+      }
       int own = sh.owner[k1], pt = sh.slice[k1];
       size_t i = sidx(s, pt, own);
       sh.sa[2 * j] = own; sh.st[2 * j] = pt;
@@ -290,17 +299,13 @@ __device__ int bisect_move(const Ctx &c, const Frame *frames, int type, int atom
                   return pair_term64(c, frames, sh.sa[sl], p, sh.st[sl], sh.sx[sl], sh.sy[sl], sh.sz[sl]);
                 },
                 sh.se, sh.buf);
-    for (int j = tid; j < nmid; j += blockDim.x) {
-      int k1 = j * seg + half;
-      sh.en[k1] = sh.se[2 * j];
-      sh.eo[k1] = sh.se[2 * j + 1];
-    }
-    __syncthreads();
     if (tid == 0) {
       sh.pot1 = sh.pot0;
       double pot0 = 0.0;
       for (int j = 0; j < nmid; j++) {
         int k0 = j * seg, k1 = k0 + half;
+        sh.en[k1] = sh.se[2 * j];
+        sh.eo[k1] = sh.se[2 * j + 1];
         pot0 += (sh.en[k1] - sh.eo[k1]);
         if (k0 != 0) pot0 += (sh.en[k0] - sh.eo[k0]);
       }
