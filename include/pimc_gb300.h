@@ -116,6 +116,12 @@ pimc_status pimc_reset_counters(pimc_handle *h);
 pimc_status pimc_synchronize(pimc_handle *h);
 /* 1: table interpolation of the rotor-atom potential in FP32 with FP64 sums */
 pimc_status pimc_set_precision(pimc_handle *h, int mixed);
+/* Production-schedule options (no reference counterpart; the reference has
+ * one schedule).  PIMC_OPT_FUSED = 1 (default): one launch per bisection
+ * block of numb phases and persistent rotational sweeps; 0: one launch per
+ * phase.  Both give identical paths for the same seed. */
+#define PIMC_OPT_FUSED 1
+pimc_status pimc_set_option(pimc_handle *h, int option, long long value);
 /* scheduled bead-moves per pass: per type N*P*(2^L-1) + N*P, plus P*Q per rotor */
 double      pimc_bead_moves_per_pass(const pimc_handle *h);
 /* kernels launched on the handle's stream so far */

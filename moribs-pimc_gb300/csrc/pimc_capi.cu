@@ -44,6 +44,11 @@ struct pimc_handle {
   // growable scratch for queries
   void *qbuf = nullptr;
   size_t qbytes = 0;
+  // production schedule: fused bisection blocks and persistent rotation sweeps
+  int fused = 1;
+  unsigned long long *prog = nullptr;  // per-CTA progress words of the persistent rotation launches
+  unsigned *abort_word = nullptr;
+  int nprog = 0;
 };
 
 extern "C" const char *pimc_status_string(pimc_status s)
@@ -245,7 +250,8 @@ extern "C" pimc_status pimc_create(const pimc_system *sys, int device, pimc_hand
       (e = dalloc(h, &st.rp_ok, nr)) || (e = dalloc(h, &st.rl_ok, nr)) ||
       (e = dalloc(h, &st.ang, 3 * nr)) || (e = dalloc(h, &st.cosv, 3 * nr)) || (e = dalloc(h, &st.pindex, na)) ||
       (e = dalloc(h, &st.mctype, na)) || (e = dalloc(h, &st.err, 1)) || (e = dalloc(h, &h->frames, nr)) ||
-      (e = dalloc(h, &h->cnt, 12)) || (e = dalloc(h, &h->pass, 1)) || (e = dalloc(h, &h->cursors, 8))) {
+      (e = dalloc(h, &h->cnt, 12)) || (e = dalloc(h, &h->pass, 1)) || (e = dalloc(h, &h->cursors, 8)) ||
+      (e = dalloc(h, &h->prog, (size_t)(d.Q / 2 > 0 ? d.Q / 2 : 1))) || (e = dalloc(h, &h->abort_word, 1))) {
     pimc_destroy(h);
     return e;
   }
@@ -263,6 +269,9 @@ extern "C" pimc_status pimc_create(const pimc_system *sys, int device, pimc_hand
   CK(cudaMemset(st.err, 0, sizeof(unsigned)));
   CK(cudaMemset(h->cnt, 0, 12 * sizeof(unsigned long long)));
   CK(cudaMemset(h->pass, 0, sizeof(unsigned)));
+  h->nprog = d.Q / 2 > 0 ? d.Q / 2 : 1;
+  CK(cudaMemset(h->prog, 0, (size_t)h->nprog * sizeof(unsigned long long)));
+  CK(cudaMemset(h->abort_word, 0, sizeof(unsigned)));
   std::vector<int> mct(na), pidx(na);
   g = 0;
   for (int t = 0; t < s.ntypes; t++)
@@ -286,7 +295,7 @@ extern "C" pimc_status pimc_destroy(pimc_handle *h)
   DevState &st = h->ctx.st;
   void *bufs[] = {st.x, st.y, st.z, st.xf, st.yf, st.zf, st.cosvf, st.rp_cache, st.rl_cache, st.rp_ok, st.rl_ok,
                   st.ang, st.cosv, st.pindex, st.mctype, st.err, h->frames, h->cnt, h->pass, h->cursors, h->ms,
-                  h->qbuf};
+                  h->qbuf, h->prog, h->abort_word};
   for (void *b : bufs)
     if (b) cudaFree(b);
   for (void *b : h->owned) cudaFree(b);
@@ -389,10 +398,21 @@ extern "C" pimc_status pimc_load_tables(pimc_handle *h, const pimc_tables *tb)
       t.dchd = 360.0 / (double)(t.nch - 1);
       size_t n = (size_t)t.nth * t.nph * t.nch;
       if ((e = upload(h, tb->rhoprp, n, &t.rho)) || (e = upload(h, tb->erotpr, n, &t.erot)) ||
-          (e = upload(h, tb->erotsq, n, &t.esq)))
+          (e = upload(h, tb->erotsq, n, &t.esq)) || (e = upload_f32(h, tb->rhoprp, n, &t.rho32)))
         return e;
     }
   }
+  // float constants of the FP32 leaves
+  const double deg = 180.0 / 3.14159265358979323846;
+  t.f_x01d = (float)t.x01d; t.f_ih1d = (float)t.ih1d; t.f_c61d = (float)t.c61d;
+  t.f_unode1d = (float)t.unode1d; t.f_alpha1d = (float)t.alpha1d;
+  t.f_dr2d = (float)t.dr2d; t.f_dc2d = (float)t.dc2d;
+  t.f_thscale = t.dth3 > 0 ? (float)(deg / t.dth3) : 0.f;
+  t.f_chscale = t.dch3 > 0 ? (float)(deg / t.dch3) : 0.f;
+  t.f_rvmin = (float)t.rvmin; t.f_rvmax = (float)t.rvmax; t.f_rvstep = (float)t.rvstep;
+  t.f_dscale[0] = t.dthd > 0 ? (float)(deg / t.dthd) : 0.f;
+  t.f_dscale[1] = t.dphd > 0 ? (float)(deg / t.dphd) : 0.f;
+  t.f_dscale[2] = t.dchd > 0 ? (float)(deg / t.dchd) : 0.f;
   CK(cudaStreamSynchronize(h->stream));
   h->tables = true;
   if (h->pass_exec) { cudaGraphExecDestroy(h->pass_exec); h->pass_exec = nullptr; }
@@ -444,6 +464,7 @@ extern "C" pimc_status pimc_set_state(pimc_handle *h, const double *coords, cons
     launch_derive_state(h->ctx, h->frames, h->stream);     // float copies, frames, caches stale
     h->launches++;
     CK(cudaGetLastError());
+    CK(cudaMemsetAsync(h->abort_word, 0, sizeof(unsigned), h->stream));   // a new path clears an aborted sweep
   }
   if (pindex) {
     for (int a = 0; a < d.na; a++)
@@ -750,47 +771,106 @@ extern "C" pimc_status pimc_rcf(pimc_handle *h, double *rcf)
 // ------------------------------------------------------------ production
 
 // one pass of the independent-set schedule, recorded on h->stream
-static long long record_pass(pimc_handle *h, uint64_t seed)
+// The production pass (PIMCPass, mc_main.cc:510-522, as independent sets):
+// the centroid move of every atom, then for each (type, s0 < 2^levels) one
+// bisection block -- numb phases of windows [s0 + kM, s0 + (k+1)M] -- each
+// followed by its share of the P rotational sweeps.  Uniform keys: phase
+// index b of bisection phase (type, s0, j) in that order, B + 2 it + parity
+// for sweep it, B + 2P + type for the centroid moves.
+struct PassPlan {
+  std::vector<int> type, s0;
+  std::vector<unsigned> phase0;
+  unsigned B = 0;
+};
+
+static PassPlan pass_plan(const DevSys &d)
+{
+  PassPlan pl;
+  unsigned b = 0;
+  for (int t = 0; t < d.ntypes; t++) {
+    int M = 1 << d.levels[t];
+    for (int s0 = 0; s0 < M; s0++) {
+      pl.type.push_back(t);
+      pl.s0.push_back(s0);
+      pl.phase0.push_back(b);
+      b += (unsigned)d.numb[t];
+    }
+  }
+  pl.B = b;
+  return pl;
+}
+
+static long long launch_bisection_block(pimc_handle *h, const PassPlan &pl, size_t i, uint64_t seed)
+{
+  const DevSys &d = h->ctx.s;
+  int t = pl.type[i];
+  if (h->fused) {
+    launch_bisect_block(h->ctx, h->frames, t, pl.s0[i], pl.phase0[i], seed, h->pass, h->cnt, h->stream);
+    return 1;
+  }
+  for (int j = 0; j < d.numb[t]; j++)
+    launch_bisect_phase(h->ctx, h->frames, t, pl.s0[i], j, pl.phase0[i] + (unsigned)j, seed, h->pass, h->cnt,
+                        h->stream);
+  return d.numb[t];
+}
+
+// rotational sweeps it0 .. it1-1; group numbers the persistent launches of a pass
+static pimc_status launch_sweeps(pimc_handle *h, const PassPlan &pl, int it0, int it1, unsigned group, uint64_t seed,
+                                 long long *n)
+{
+  const DevSys &d = h->ctx.s;
+  if (!h->sys.rotation || d.nrotors <= 0 || it1 <= it0) return PIMC_OK;
+  int nctas = 0;
+  if (h->fused && d.Q >= 2 && d.Q % 2 == 0) {
+    nctas = rot_sweeps_max_ctas(d.mixed);
+    if (nctas > d.Q / 2) nctas = d.Q / 2;
+  }
+  if (nctas > 0) {
+    CK(launch_rot_sweeps(h->ctx, h->frames, nctas, 2 * (it1 - it0), pl.B + 2u * (unsigned)it0, group, seed, h->pass,
+                         h->prog, h->abort_word, h->cnt, h->stream));
+    (*n)++;
+    return PIMC_OK;
+  }
+  for (int it = it0; it < it1; it++) {
+    *n += launch_rot_phase(h->ctx, h->frames, 0, pl.B + 2u * it, seed, h->pass, h->cnt, h->stream);
+    *n += launch_rot_phase(h->ctx, h->frames, 1, pl.B + 2u * it + 1, seed, h->pass, h->cnt, h->stream);
+  }
+  return PIMC_OK;
+}
+
+static long long launch_centroid(pimc_handle *h, const PassPlan &pl, uint64_t seed)
 {
   const DevSys &d = h->ctx.s;
   long long n = 0;
-  launch_pass_begin(h->pass, h->stream);
-  n++;
-  // bisection phases: type, start offset s0 < M, atom rotation j < numb
-  struct Ph { int type, s0, j; };
-  std::vector<Ph> bis;
-  for (int t = 0; t < d.ntypes; t++) {
-    int M = 1 << d.levels[t];
-    for (int s0 = 0; s0 < M; s0++)
-      for (int j = 0; j < d.numb[t]; j++) bis.push_back({t, s0, j});
-  }
-  unsigned B = (unsigned)bis.size();
-  unsigned mol_phase = B + 2u * (unsigned)d.P;
-  // centroid moves at time 0 (PIMCPass, mc_main.cc:512-513)
+  unsigned mol_phase = pl.B + 2u * (unsigned)d.P;
   for (int t = 0; t < d.ntypes; t++)
     for (int a = 0; a < d.numb[t]; a++) {
       ReplaySrc none{};
       none.err = h->ctx.st.err;
-      launch_mol(h->ctx, h->frames, t, a, false, none, seed, h->pass, mol_phase + (unsigned)t, h->ms, nullptr, nullptr, h->cnt,
-                 h->stream);
+      launch_mol(h->ctx, h->frames, t, a, false, none, seed, h->pass, mol_phase + (unsigned)t, h->ms, nullptr, nullptr,
+                 h->cnt, h->stream);
       n += 3;
     }
-  // time iterations: the bisection phases spread evenly, then one sweep
-  size_t b = 0;
-  for (int it = 0; it < d.P; it++) {
-    size_t bend = (size_t)((unsigned long long)(it + 1) * B / d.P);
-    for (; b < bend; b++) {
-      launch_bisect_phase(h->ctx, h->frames, bis[b].type, bis[b].s0, bis[b].j, (unsigned)b, seed, h->pass, h->cnt,
-                          h->stream);
-      n++;
-    }
-    if (h->sys.rotation && d.nrotors > 0) {
-      launch_rot_phase(h->ctx, h->frames, 0, B + 2u * it, seed, h->pass, h->cnt, h->stream);
-      launch_rot_phase(h->ctx, h->frames, 1, B + 2u * it + 1, seed, h->pass, h->cnt, h->stream);
-      n += 2;
-    }
-  }
   return n;
+}
+
+static pimc_status record_pass(pimc_handle *h, uint64_t seed, long long *nout)
+{
+  const DevSys &d = h->ctx.s;
+  PassPlan pl = pass_plan(d);
+  long long n = 0;
+  pimc_status e;
+  launch_pass_begin(h->pass, h->stream);
+  n++;
+  n += launch_centroid(h, pl, seed);          // centroid moves at time 0 (mc_main.cc:512-513)
+  size_t nbk = pl.type.size();
+  for (size_t i = 0; i < nbk; i++) {
+    n += launch_bisection_block(h, pl, i, seed);
+    int it0 = (int)((long long)i * d.P / (long long)nbk), it1 = (int)((long long)(i + 1) * d.P / (long long)nbk);
+    if ((e = launch_sweeps(h, pl, it0, it1, (unsigned)i, seed, &n))) return e;
+  }
+  *nout = n;
+  return PIMC_OK;
 }
 
 extern "C" pimc_status pimc_run_passes(pimc_handle *h, int npasses, uint64_t seed)
@@ -805,10 +885,16 @@ extern "C" pimc_status pimc_run_passes(pimc_handle *h, int npasses, uint64_t see
     if (h->pass_exec) { CK(cudaGraphExecDestroy(h->pass_exec)); h->pass_exec = nullptr; }
     cudaGraph_t graph;
     CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-    long long n = record_pass(h, seed);
+    long long n = 0;
+    pimc_status re = record_pass(h, seed, &n);
     cudaError_t le = cudaGetLastError();
-    CK(cudaStreamEndCapture(h->stream, &graph));
-    if (le != cudaSuccess) { cudaGraphDestroy(graph); h->last_cuda = le; return PIMC_ERR_CUDA; }
+    cudaError_t ce = cudaStreamEndCapture(h->stream, &graph);
+    if (re != PIMC_OK || le != cudaSuccess || ce != cudaSuccess) {
+      if (ce == cudaSuccess) cudaGraphDestroy(graph);
+      if (re != PIMC_OK) return re;
+      h->last_cuda = le != cudaSuccess ? le : ce;
+      return PIMC_ERR_CUDA;
+    }
     cudaError_t ie = cudaGraphInstantiate(&h->pass_exec, graph, 0);
     cudaGraphDestroy(graph);
     if (ie != cudaSuccess) { h->last_cuda = ie; return PIMC_ERR_CUDA; }
@@ -833,37 +919,21 @@ extern "C" pimc_status pimc_profile_pass(pimc_handle *h, uint64_t seed, double *
   cudaEvent_t ev[6];
   for (int k = 0; k < 6; k++) CK(cudaEventCreate(&ev[k]));
   long long n[3] = {0, 0, 0};
+  PassPlan pl = pass_plan(d);
+  size_t nbk = pl.type.size();
   launch_pass_begin(h->pass, h->stream);
-  std::vector<int> bt, bs, bj;
-  for (int t = 0; t < d.ntypes; t++) {
-    int M = 1 << d.levels[t];
-    for (int s0 = 0; s0 < M; s0++)
-      for (int j = 0; j < d.numb[t]; j++) { bt.push_back(t); bs.push_back(s0); bj.push_back(j); }
-  }
-  unsigned B = (unsigned)bt.size();
   CK(cudaEventRecord(ev[0], h->stream));
-  for (int t = 0; t < d.ntypes; t++)
-    for (int a = 0; a < d.numb[t]; a++) {
-      ReplaySrc none{};
-      none.err = h->ctx.st.err;
-      launch_mol(h->ctx, h->frames, t, a, false, none, seed, h->pass, B + 2u * (unsigned)d.P + (unsigned)t, h->ms,
-                 nullptr, nullptr, h->cnt, h->stream);
-      n[0] += 3;
-    }
+  n[0] = launch_centroid(h, pl, seed);
   CK(cudaEventRecord(ev[1], h->stream));
   CK(cudaEventRecord(ev[2], h->stream));
-  for (unsigned b = 0; b < B; b++) {
-    launch_bisect_phase(h->ctx, h->frames, bt[b], bs[b], bj[b], b, seed, h->pass, h->cnt, h->stream);
-    n[1]++;
-  }
+  for (size_t i = 0; i < nbk; i++) n[1] += launch_bisection_block(h, pl, i, seed);
   CK(cudaEventRecord(ev[3], h->stream));
   CK(cudaEventRecord(ev[4], h->stream));
-  if (h->sys.rotation && d.nrotors > 0)
-    for (int it = 0; it < d.P; it++) {
-      launch_rot_phase(h->ctx, h->frames, 0, B + 2u * it, seed, h->pass, h->cnt, h->stream);
-      launch_rot_phase(h->ctx, h->frames, 1, B + 2u * it + 1, seed, h->pass, h->cnt, h->stream);
-      n[2] += 2;
-    }
+  pimc_status e2;
+  for (size_t i = 0; i < nbk; i++) {
+    int it0 = (int)((long long)i * d.P / (long long)nbk), it1 = (int)((long long)(i + 1) * d.P / (long long)nbk);
+    if ((e2 = launch_sweeps(h, pl, it0, it1, (unsigned)i, seed, &n[2]))) return e2;
+  }
   CK(cudaEventRecord(ev[5], h->stream));
   CK(cudaGetLastError());
   CK(cudaEventSynchronize(ev[5]));
@@ -876,6 +946,23 @@ extern "C" pimc_status pimc_profile_pass(pimc_handle *h, uint64_t seed, double *
   for (int k = 0; k < 6; k++) cudaEventDestroy(ev[k]);
   h->launches += 1 + n[0] + n[1] + n[2];
   return check_err(h);
+}
+
+extern "C" pimc_status pimc_set_option(pimc_handle *h, int option, long long value)
+{
+  if (!h) return PIMC_ERR_BAD_ARG;
+  if (option == PIMC_OPT_FUSED) {
+    if (value != 0 && value != 1) return PIMC_ERR_BAD_ARG;
+    if (h->fused != (int)value && h->pass_exec) {
+      CK(cudaSetDevice(h->device));
+      CK(cudaStreamSynchronize(h->stream));
+      cudaGraphExecDestroy(h->pass_exec);
+      h->pass_exec = nullptr;
+    }
+    h->fused = (int)value;
+    return PIMC_OK;
+  }
+  return PIMC_ERR_BAD_ARG;
 }
 
 extern "C" pimc_status pimc_synchronize(pimc_handle *h)

@@ -11,6 +11,7 @@
 #define PIMC_WNO2K 0.6950356          /* mc_const.h:16 */
 #define PIMC_RZERO 1.0e-10            /* mc_confg.h:59 */
 #define PIMC_BLOCK 256                /* threads per move CTA */
+#define PIMC_ROT_THREADS 320          /* rotational move CTA: 8 pair warps, a density warp, a commit warp */
 #define PIMC_RED_BUF 4096             /* doubles in a CTA's reduction buffer */
 #define PIMC_MAX_SEG 64               /* largest bisection segment (levels <= 6) */
 #define PIMC_MAX_ROTORS 16            /* NumbRotLim (mc_setup.cc:63) */
@@ -50,6 +51,11 @@ struct DevTables {
   int nsph;
   double sph_r0, sph_rmax, sph_rstep;
   const double *sph;
+  // float constants of the FP32 leaves, converted once on the host so that
+  // those leaves execute no double-precision instruction
+  float f_x01d, f_ih1d, f_c61d, f_unode1d, f_alpha1d, f_dr2d, f_dc2d;
+  float f_thscale, f_chscale, f_rvmin, f_rvmax, f_rvstep;     // vcord32: degrees per grid step folded in
+  float f_dscale[3];                                            // rotden32: theta, phi, chi grid steps per radian
 };
 
 struct DevSys {
@@ -125,7 +131,27 @@ __device__ __forceinline__ void matpre(const double e[3], double m[9])
 
 // cos and sin of theta = acos(cost) are cost and sqrt((1-cost)(1+cost)): the
 // same matrix as matpre(phi, acos(cost), chi) without the acos/sincos chain
-__device__ __forceinline__ void make_frame(double phi, double cost, double chi, Frame &f)
+// the float frame of the FP32 path, from the float-rounded angles
+__device__ __forceinline__ void make_frame32(float phi, float cost, float chi, float mf[9], float *hzf)
+{
+  float sp, cp, sk, ck;
+  sincosf(phi, &sp, &cp);
+  sincosf(chi, &sk, &ck);
+  float ct = cost, st = sqrtf(fmaxf((1.0f - cost) * (1.0f + cost), 0.0f));
+  mf[0] = cp * ct * ck - sp * sk;
+  mf[1] = -cp * ct * sk - sp * ck;
+  mf[2] = cp * st;
+  mf[3] = sp * ct * ck + cp * sk;
+  mf[4] = -sp * ct * sk + cp * ck;
+  mf[5] = sp * st;
+  mf[6] = -st * ck;
+  mf[7] = st * sk;
+  mf[8] = ct;
+  *hzf = sqrtf(mf[2] * mf[2] + mf[5] * mf[5] + mf[8] * mf[8]);
+}
+
+// the double-precision frame (m, hz_norm) only
+__device__ __forceinline__ void make_frame64(double phi, double cost, double chi, Frame &f)
 {
   double sp, cp, sk, ck;
   sincos(phi, &sp, &cp);
@@ -148,8 +174,12 @@ __device__ __forceinline__ void make_frame(double phi, double cost, double chi, 
   s = s + f.m[5] * f.m[5];
   s = s + f.m[8] * f.m[8];
   f.hz_norm = sqrt(s);
-  for (int k = 0; k < 9; k++) f.mf[k] = (float)f.m[k];
-  f.hzf = (float)f.hz_norm;
+}
+
+__device__ __forceinline__ void make_frame(double phi, double cost, double chi, Frame &f)
+{
+  make_frame64(phi, cost, chi, f);
+  make_frame32((float)phi, (float)cost, (float)chi, f.mf, &f.hzf);
 }
 
 // ------------------------------------------------------------------ leaves
@@ -466,17 +496,17 @@ __device__ __forceinline__ float spot1d32(const DevTables &t, float r)
 {
   if (r >= __ldg(t.g1d32 + t.n1d - 1)) {
     float r2 = r * r;
-    return (float)(-t.c61d) / (r2 * r2 * r2);
+    return -t.f_c61d / (r2 * r2 * r2);
   }
-  if (r <= __ldg(t.g1d32)) return (float)t.unode1d * expf(-(float)t.alpha1d * r);
-  return splint32(t.g1d32, t.p1d32, t.y21d32, t.n1d, r, t.uni1d, (float)t.x01d, (float)t.ih1d);
+  if (r <= __ldg(t.g1d32)) return t.f_unode1d * expf(-t.f_alpha1d * r);
+  return splint32(t.g1d32, t.p1d32, t.y21d32, t.n1d, r, t.uni1d, t.f_x01d, t.f_ih1d);
 }
 
 __device__ __forceinline__ float lpot2d32(const DevTables &t, float r, float cost)
 {
   float rmin = __ldg(t.rg2d32), cmin = __ldg(t.cg2d32);
-  int ir = (int)floorf((r - rmin) / (float)t.dr2d);
-  int ic = (int)floorf((cost - cmin) / (float)t.dc2d);
+  int ir = (int)floorf((r - rmin) / t.f_dr2d);
+  int ic = (int)floorf((cost - cmin) / t.f_dc2d);
   ir = min(max(ir, 0), t.nr2d - 2);
   ic = min(max(ic, 0), t.nc2d - 2);
   const float *p = t.pot2d32 + (size_t)ir * t.nc2d + ic;
@@ -506,10 +536,10 @@ __device__ __forceinline__ float vcord32(const DevTables &t, const Frame &f, flo
   else chir = 2.0f * pi - chiwff;
   if (t.chfold == 180) chiwff = (chir > pi) ? 2.0f * pi - chir : chir;
   else if (t.chfold == 360) chiwff = chir;
-  float r = rn * (float)(1.0 / 0.529177249);
-  float xth = thewff * (float)(180.0 / PIMC_PI / t.dth3);
-  float xch = chiwff * (float)(180.0 / PIMC_PI / t.dch3);
-  float rvmin = (float)t.rvmin, rvmax = (float)t.rvmax, rstep = (float)t.rvstep;
+  float r = rn * 1.88972614f;          // 1 / 0.529177249 (bohr per angstrom)
+  float xth = thewff * t.f_thscale;
+  float xch = chiwff * t.f_chscale;
+  float rvmin = t.f_rvmin, rvmax = t.f_rvmax, rstep = t.f_rvstep;
   r = fminf(fmaxf(r, rvmin), rvmax);
   int maxrpt = t.rgrd - 1, mxthpt = t.thgrd - 1, mxchpt = t.chgrd - 1;
   int ir = min((int)((r - rvmin) / rstep), maxrpt);
@@ -522,6 +552,44 @@ __device__ __forceinline__ float vcord32(const DevTables &t, const Frame &f, flo
   if (ith < mxthpt) v += (__ldg(t.vtab32 + i0 + nch) - v0) * (xth - (float)ith);
   if (ich < mxchpt) v += (__ldg(t.vtab32 + i0 + 1) - v0) * (xch - (float)ich);
   return v;
+}
+
+// rotden's rho on the FP32 path: relative rotation m1^T m2 as deleul
+// (rotden.f:32-134) with its Euler angles from atan2 (stable where acos of
+// a rounded cosine is not), then rotpro's first-order interpolation
+// (rotpro_sub.f:1-64) on the float table
+__device__ __forceinline__ float rotden_rho32(const DevTables &t, const float *m1, const float *m2in, int *bad)
+{
+  const float pi2 = 6.28318530717959f;
+  float m2[9];
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) m2[i * 3 + j] = m1[i] * m2in[j] + m1[3 + i] * m2in[3 + j] + m1[6 + i] * m2in[6 + j];
+  float s2 = m2[6] * m2[6] + m2[7] * m2[7];
+  float theta = atan2f(sqrtf(s2), m2[8]);
+  float phi, chi;
+  if (s2 < 2.0e-8f) {                 // |1 -+ cos theta| < 1e-8: phi = 0 (rotden.f:73-86)
+    phi = 0.0f;
+    chi = (m2[8] > 0.0f) ? atan2f(m2[3], m2[0]) : atan2f(m2[1], m2[4]);
+  } else {
+    phi = atan2f(m2[5], m2[2]);
+    chi = atan2f(m2[7], -m2[6]);
+  }
+  if (phi < 0.0f) phi += pi2;
+  if (chi < 0.0f) chi += pi2;
+  float xt = theta * t.f_dscale[0], xp = phi * t.f_dscale[1], xc = chi * t.f_dscale[2];
+  int ichi = (int)xc, iphi = (int)xp, ith = (int)xt;
+  if (ichi > t.nch - 1 || ichi < 0) { ichi = 0; *bad = 1; }
+  if (iphi > t.nph - 1 || iphi < 0) { iphi = 0; *bad = 1; }
+  if (ith > t.nth - 1 || ith < 0) { ith = 0; *bad = 1; }
+  size_t nph = t.nph, nch = t.nch;
+  size_t i0 = ((size_t)ith * nph + iphi) * nch + ichi;
+  float r0 = __ldg(t.rho32 + i0), rho = r0;
+  if (ichi < t.nch - 1) rho += (__ldg(t.rho32 + i0 + 1) - r0) * (xc - (float)ichi);
+  if (iphi < t.nph - 1) rho += (__ldg(t.rho32 + i0 + nch) - r0) * (xp - (float)iphi);
+  if (ith < t.nth - 1) rho += (__ldg(t.rho32 + i0 + nph * nch) - r0) * (xt - (float)ith);
+  return rho;
 }
 
 // caleng (caleng_tip4p_gg.f:2-186).  kcal2k is an INTEGER parameter in the

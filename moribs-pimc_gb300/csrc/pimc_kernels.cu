@@ -77,43 +77,70 @@ __global__ void __launch_bounds__(PIMC_BLOCK) k_bisect_phase(Ctx c, Frame *frame
   }
 }
 
+// one bisection block of the production schedule: all phases j < numb of
+// one (type, s0).  Window k = [s0 + kM, s0 + (k+1)M] moves atoms (k + j) mod
+// numb for j = 0, 1, ...; the beads a window's moves read and write lie in
+// its own interior or on its fixed end points, so CTA k runs its phases one
+// after the other with no other CTA involved, and the result equals the
+// phase-by-phase launches with the same phase numbers.
+template <bool MIX>
+__global__ void __launch_bounds__(PIMC_BLOCK) k_bisect_block(Ctx c, Frame *frames, int type, int s0, unsigned phase0,
+                                                              uint64_t seed, const unsigned *pass,
+                                                              unsigned long long *cnt)
+{
+  __shared__ BisectShared sh;
+  const int M = 1 << c.s.levels[type], N = c.s.numb[type];
+  const int k = blockIdx.x;
+  const int time0 = s0 + k * M;
+  const unsigned ps = *pass;
+  unsigned long long tot = 0, nacc = 0;
+  for (int j = 0; j < N; j++) {
+    PhiloxSrc src{seed, ((uint64_t)ps << 32) | ((uint64_t)(phase0 + (unsigned)j) << 12) | (uint64_t)k};
+    int acc = bisect_move<MIX>(c, frames, type, (k + j) % N, time0, 0, src, sh, nullptr);
+    tot++;
+    nacc += acc;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    atomicAdd(&cnt[(type * 3 + 1) * 2 + 0], tot);
+    atomicAdd(&cnt[(type * 3 + 1) * 2 + 1], nacc);
+  }
+}
+
 // ------------------------------------------------------------ rotations
-// one even or odd half of MCRotationsMove / MCRotations3D: CTA b handles
-// slice q = parity + 2b and all rotors of the type in order
+// serial position of slice q in MCRotationsMove's loops: even slices, then odd
+__device__ __forceinline__ long rot_serial(int Q, int q) { return (q & 1) ? (Q + 1) / 2 + q / 2 : q / 2; }
+
+// one independent set of slices of MCRotationsMove / MCRotations3D: CTA b
+// handles slice q = q0 + 2b and all rotors of the type in order
 template <bool REPLAY, bool MIX>
-__global__ void __launch_bounds__(PIMC_BLOCK) k_rot(Ctx c, Frame *frames, int parity, const double *urot, long nurot,
-                                                     unsigned phase, uint64_t seed, const unsigned *pass,
-                                                     double *rd_out, int *acc_out, unsigned long long *cnt)
+__global__ void __launch_bounds__(PIMC_ROT_THREADS) k_rot(Ctx c, Frame *frames, int q0, int nq, const double *urot,
+                                                          long nurot, unsigned phase, uint64_t seed,
+                                                          const unsigned *pass, double *rd_out, int *acc_out,
+                                                          unsigned long long *cnt)
 {
   __shared__ RotShared sh;
-  int q = parity + 2 * blockIdx.x;
-  if (q >= c.s.Q) return;
-  int nr = c.s.nrotors;
-  bool linear = c.s.molecule[c.s.imtype] == 1;
-  int per = linear ? 3 : 4;
-  long n_even = (c.s.Q + 1) / 2;
+  if ((int)blockIdx.x >= nq) return;
+  const int q = q0 + 2 * (int)blockIdx.x;
+  const int nr = c.s.nrotors;
+  const bool linear = c.s.molecule[c.s.imtype] == 1;
+  const int per = linear ? 3 : 4;
   for (int r = 0; r < nr; r++) {
     double u[4] = {0.5, 0.5, 0.5, 0.5};
     if (REPLAY) {
       // serial consumption order: even slices then odd, rotors inside a slice
-      long idx = ((parity ? n_even : 0) + blockIdx.x) * (long)nr + r;
+      long idx = rot_serial(c.s.Q, q) * (long)nr + r;
       for (int k = 0; k < per; k++) {
         long p = idx * per + k;
         u[k] = (p < nurot) ? urot[p] : 0.5;
         if (p >= nurot && threadIdx.x == 0) atomicOr(c.st.err, (unsigned)DERR_STREAM);
       }
     } else {
-      uint64_t mv = ((uint64_t)(*pass) << 32) | ((uint64_t)phase << 12) | (uint64_t)blockIdx.x;
-      double a, b;
-      philox_u2(seed, mv, 0x400000u | (uint32_t)r, 0u, &a, &b);
-      u[0] = a; u[1] = b;
-      philox_u2(seed, mv, 0x400000u | (uint32_t)r, 1u, &a, &b);
-      u[2] = a; u[3] = b;
-      if (linear) u[2] = u[3];
+      rot_uniforms(seed, *pass, phase, q >> 1, r, linear, u);
     }
     int g0 = c.s.rot_first + r;
     double rd;
-    int acc = rot_step<MIX>(c, frames, g0, q, u, linear, sh, &rd);
+    int acc = rot_step<MIX, false>(c, frames, g0, q, u, linear, sh, &rd);
     if (threadIdx.x == 0) {
       if (REPLAY) {
         rd_out[(size_t)q * nr + r] = rd;
@@ -123,6 +150,106 @@ __global__ void __launch_bounds__(PIMC_BLOCK) k_rot(Ctx c, Frame *frames, int pa
       atomicAdd(&cnt[(ty * 3 + 2) * 2 + 0], 1ull);
       if (acc) atomicAdd(&cnt[(ty * 3 + 2) * 2 + 1], 1ull);
     }
+  }
+}
+
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long *p)
+{
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_u64(unsigned long long *p, unsigned long long v)
+{
+  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long global_ns()
+{
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// nhalf half-sweeps (even slices, odd slices, even, ...) of the rotational
+// moves in one cooperative launch, Q even.  CTA b owns the slice pairs
+// (2p, 2p+1), p in [p0, p1).  Its even slices read the odd slice of the CTA
+// on the left and its odd slices the even slice of the CTA on the right, so
+// half-sweep h waits only for that neighbour to have finished h-1; the
+// neighbour in turn waits for this CTA's h before it writes the slice read
+// here again.  Every move therefore sees exactly the state it sees in the
+// launch-per-half-sweep schedule, with the same uniforms, and the results
+// are identical.  Progress words hold (launch id << 24) | half-sweeps done;
+// the wait gives up after two seconds, sets the abort word and the timeout
+// error bit, and every CTA then leaves.
+template <bool MIX>
+__global__ void __launch_bounds__(PIMC_ROT_THREADS) k_rot_sweeps(Ctx c, Frame *frames, int nhalf, unsigned phase0,
+                                                                 unsigned group, uint64_t seed, const unsigned *pass,
+                                                                 unsigned long long *prog, unsigned *abort_word,
+                                                                 unsigned long long *cnt)
+{
+  __shared__ RotShared sh;
+  __shared__ int stop;
+  const int nc = gridDim.x, b = blockIdx.x;
+  const int npairs = c.s.Q >> 1;
+  const int p0 = (int)((long)b * npairs / nc), p1 = (int)((long)(b + 1) * npairs / nc);
+  const int nr = c.s.nrotors;
+  const bool linear = c.s.molecule[c.s.imtype] == 1;
+  const unsigned ps = *pass;
+  const unsigned long long id = ((unsigned long long)ps << 8) | (group & 255u);
+  const int left = (b + nc - 1) % nc, right = (b + 1) % nc;
+  unsigned long long tot = 0, nacc = 0;
+  for (int h = 0; h < nhalf; h++) {
+    const int parity = h & 1;
+    if (threadIdx.x == 0) {
+      int st = 0;
+      if (*(volatile unsigned *)abort_word) {
+        atomicOr(c.st.err, (unsigned)DERR_TIMEOUT);
+        st = 1;
+      } else if (nc > 1 && h > 0) {
+        const unsigned long long *w = prog + (parity ? right : left);
+        const unsigned long long t0 = global_ns();
+        for (;;) {
+          unsigned long long v = ld_acquire_u64(w);
+          if ((v >> 24) == id && (long long)(v & 0xFFFFFFull) >= h) break;
+          if (*(volatile unsigned *)abort_word) {
+            atomicOr(c.st.err, (unsigned)DERR_TIMEOUT);
+            st = 1;
+            break;
+          }
+          if (global_ns() - t0 > 2000000000ull) {
+            atomicExch(abort_word, 1u);
+            atomicOr(c.st.err, (unsigned)DERR_TIMEOUT);
+            st = 1;
+            break;
+          }
+        }
+        __threadfence();
+      }
+      stop = st;
+    }
+    __syncthreads();
+    if (stop) break;
+    const unsigned phase = phase0 + (unsigned)h;
+    for (int p = p0; p < p1; p++) {
+      const int q = 2 * p + parity;
+      for (int r = 0; r < nr; r++) {
+        double u[4];
+        rot_uniforms(seed, ps, phase, p, r, linear, u);
+        int acc = rot_step<MIX, true>(c, frames, c.s.rot_first + r, q, u, linear, sh, nullptr);
+        tot++;
+        nacc += acc;
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      __threadfence();
+      st_release_u64(prog + b, (id << 24) | (unsigned long long)(h + 1));
+    }
+  }
+  if (threadIdx.x == 0) {
+    int ty = c.s.imtype;
+    atomicAdd(&cnt[(ty * 3 + 2) * 2 + 0], tot);
+    atomicAdd(&cnt[(ty * 3 + 2) * 2 + 1], nacc);
   }
 }
 
@@ -434,24 +561,88 @@ void launch_bisect_phase(const Ctx &c, Frame *f, int type, int s0, int j, unsign
   else k_bisect_phase<false><<<c.s.P / M, PIMC_BLOCK, 0, s>>>(c, f, type, s0, j, phase, seed, pass, cnt);
 }
 
+// the slices of one half of a sweep as independent sets: with Q odd the
+// last even slice neighbours slice 0 and runs after the other even slices,
+// as in the serial loop
+template <class F>
+static void rot_sets(int Q, int parity, F launch)
+{
+  if (parity == 0) {
+    if (Q % 2 == 1 && Q >= 3) {
+      launch(0, (Q - 1) / 2);
+      launch(Q - 1, 1);
+    } else {
+      launch(0, (Q + 1) / 2);
+    }
+  } else {
+    if (Q / 2 > 0) launch(1, Q / 2);
+  }
+}
+
 void launch_rot_replay(const Ctx &c, Frame *f, int parity, const double *urot, long nurot, double *rd, int *acc,
                        unsigned long long *cnt, cudaStream_t s)
 {
-  int nb = (c.s.Q - parity + 1) / 2;
-  if (nb <= 0) return;
-  if (c.s.mixed) k_rot<true, true><<<nb, PIMC_BLOCK, 0, s>>>(c, f, parity, urot, nurot, 0, 0, nullptr, rd, acc, cnt);
-  else k_rot<true, false><<<nb, PIMC_BLOCK, 0, s>>>(c, f, parity, urot, nurot, 0, 0, nullptr, rd, acc, cnt);
+  rot_sets(c.s.Q, parity, [&](int q0, int nq) {
+    if (c.s.mixed)
+      k_rot<true, true><<<nq, PIMC_ROT_THREADS, 0, s>>>(c, f, q0, nq, urot, nurot, 0, 0, nullptr, rd, acc, cnt);
+    else
+      k_rot<true, false><<<nq, PIMC_ROT_THREADS, 0, s>>>(c, f, q0, nq, urot, nurot, 0, 0, nullptr, rd, acc, cnt);
+  });
 }
 
-void launch_rot_phase(const Ctx &c, Frame *f, int parity, unsigned phase, uint64_t seed, const unsigned *pass,
-                      unsigned long long *cnt, cudaStream_t s)
+int launch_rot_phase(const Ctx &c, Frame *f, int parity, unsigned phase, uint64_t seed, const unsigned *pass,
+                     unsigned long long *cnt, cudaStream_t s)
 {
-  int nb = (c.s.Q - parity + 1) / 2;
-  if (nb <= 0) return;
+  int n = 0;
+  rot_sets(c.s.Q, parity, [&](int q0, int nq) {
+    if (c.s.mixed)
+      k_rot<false, true><<<nq, PIMC_ROT_THREADS, 0, s>>>(c, f, q0, nq, nullptr, 0, phase, seed, pass, nullptr, nullptr,
+                                                         cnt);
+    else
+      k_rot<false, false><<<nq, PIMC_ROT_THREADS, 0, s>>>(c, f, q0, nq, nullptr, 0, phase, seed, pass, nullptr,
+                                                          nullptr, cnt);
+    n++;
+  });
+  return n;
+}
+
+int rot_sweeps_max_ctas(int mixed)
+{
+  int dev = 0, nsm = 0, per = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+  cudaError_t e = mixed ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_rot_sweeps<true>, PIMC_ROT_THREADS, 0)
+                        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_rot_sweeps<false>, PIMC_ROT_THREADS, 0);
+  if (e != cudaSuccess) return 0;
+  return nsm * per;
+}
+
+cudaError_t launch_rot_sweeps(const Ctx &c, Frame *f, int nctas, int nhalf, unsigned phase0, unsigned group,
+                              uint64_t seed, const unsigned *pass, unsigned long long *prog, unsigned *abort_word,
+                              unsigned long long *cnt, cudaStream_t s)
+{
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(nctas);
+  cfg.blockDim = dim3(PIMC_ROT_THREADS);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
   if (c.s.mixed)
-    k_rot<false, true><<<nb, PIMC_BLOCK, 0, s>>>(c, f, parity, nullptr, 0, phase, seed, pass, nullptr, nullptr, cnt);
-  else
-    k_rot<false, false><<<nb, PIMC_BLOCK, 0, s>>>(c, f, parity, nullptr, 0, phase, seed, pass, nullptr, nullptr, cnt);
+    return cudaLaunchKernelEx(&cfg, k_rot_sweeps<true>, c, f, nhalf, phase0, group, seed, pass, prog, abort_word, cnt);
+  return cudaLaunchKernelEx(&cfg, k_rot_sweeps<false>, c, f, nhalf, phase0, group, seed, pass, prog, abort_word, cnt);
+}
+
+void launch_bisect_block(const Ctx &c, Frame *f, int type, int s0, unsigned phase0, uint64_t seed,
+                         const unsigned *pass, unsigned long long *cnt, cudaStream_t s)
+{
+  int M = 1 << c.s.levels[type];
+  int nwin = c.s.P / M;
+  if (c.s.mixed) k_bisect_block<true><<<nwin, PIMC_BLOCK, 0, s>>>(c, f, type, s0, phase0, seed, pass, cnt);
+  else k_bisect_block<false><<<nwin, PIMC_BLOCK, 0, s>>>(c, f, type, s0, phase0, seed, pass, cnt);
 }
 
 void launch_mol(const Ctx &c, Frame *f, int type, int atom, bool replay, ReplaySrc src, uint64_t seed,

@@ -343,14 +343,93 @@ struct MolScratch {
 };
 
 // ------------------------------------------------------ rotational moves
+// A rotational move runs on PIMC_ROT_THREADS threads in three roles:
+//   warps 0-7  the (slot, partner) sums over the R translational slices;
+//   warp 8     the link densities rho(q-1, q) and rho(q, q+1), old and new;
+//   warp 9     the proposal's frame and unit vector in double precision for
+//              the commit (on the FP32 path nothing else waits for them).
+// Named barrier 1 joins warps 0-8 after the set-up and barrier 2 the pair
+// warps inside the partner sums; all ten meet before the accept.  Long
+// double-precision chains thus run side by side instead of one after the
+// other on one warp.
+#define PIMC_ROT_PAIR_THREADS 256
+#define PIMC_ROT_SETUP_THREADS 288
+
+template <int ID, int NT>
+__device__ __forceinline__ void group_sync()
+{
+  asm volatile("bar.sync %0, %1;" ::"n"(ID), "n"(NT) : "memory");
+}
+
+// slot_sums over threads [0, NT) of the CTA, synchronised by named barrier ID
+template <int NT, int ID, class F>
+__device__ __forceinline__ void slot_sums_group(int nslots, int na, const int *skip, F f, double *out, double *buf)
+{
+  const int npart = na - 1;
+  if (npart <= 0) {
+    for (int s = threadIdx.x; s < nslots; s += NT) out[s] = 0.0;
+    group_sync<ID, NT>();
+    return;
+  }
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = NT >> 5;
+  const int total = nslots * npart;
+  const int chunk = (npart <= PIMC_RED_BUF) ? (PIMC_RED_BUF / npart) * npart : PIMC_RED_BUF;
+  for (int base = 0; base < total; base += chunk) {
+    int cnt = min(chunk, total - base);
+    for (int i = threadIdx.x; i < cnt; i += NT) {
+      int g = base + i;
+      int s = g / npart, pi = g - s * npart;
+      int p = pi < skip[s] ? pi : pi + 1;
+      buf[i] = f(s, p);
+    }
+    group_sync<ID, NT>();
+    int sfirst = base / npart, slast = (base + cnt - 1) / npart;
+    for (int sl = sfirst + warp; sl <= slast; sl += nw) {
+      int lo = max(sl * npart, base) - base, hi = min((sl + 1) * npart, base + cnt) - base;
+      double acc = 0.0;
+      for (int k = lo + lane; k < hi; k += 32) acc += buf[k];
+      for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+      if (lane == 0) {
+        if (sl * npart >= base) out[sl] = acc;
+        else out[sl] += acc;
+      }
+    }
+    group_sync<ID, NT>();
+  }
+}
+
+// loads of state that other CTAs of a persistent launch write: through L2
+template <bool COH>
+__device__ __forceinline__ double ld_state(const double *p)
+{
+  return COH ? __ldcg(p) : *p;
+}
+template <bool COH>
+__device__ __forceinline__ int ld_state(const int *p)
+{
+  return COH ? __ldcg(p) : *p;
+}
+template <bool COH>
+__device__ __forceinline__ void copy_frame(Frame &dst, const Frame *src, int lane)
+{
+  const unsigned *a = reinterpret_cast<const unsigned *>(src);
+  unsigned *b = reinterpret_cast<unsigned *>(&dst);
+  for (int w = lane; w < (int)(sizeof(Frame) / 4); w += 32) b[w] = COH ? __ldcg(a + w) : a[w];
+}
+
 struct RotShared {
-  Frame fo[3], fn;          // old frames at q-1, q, q+1 and the proposal at q
-  double rho[4], pot[2];
-  double vals[2 * 16];      // per (it, old/new) partner sums, R <= 16
-  double ang_new[3], nold[3], nnew[3];
+  Frame fo[3];              // current frames at q-1, q, q+1
+  Frame fn;                 // the proposal as evaluated (mf; m too where needed)
+  Frame fc;                 // the proposal in double precision, for the commit
+  double rho[4], vals[2 * 16];
+  double ang_new[3];
+  double nv[3][3];          // linear rotor: current unit vectors at q-1, q, q+1
+  double nnew[3];           // linear rotor: proposal unit vector (double path)
+  double cv[3];             // MCCosine of the proposal
+  float nvf[3], nnewf[3];   // linear rotor: current and proposal unit vectors for the FP32 path
   int bad, acc, pot_cached, link_ok[2];
   int skip[2 * 16];
-  double rd;
+  double pot_c, rd;
   double buf[PIMC_RED_BUF];
 };
 
@@ -397,13 +476,13 @@ __device__ __forceinline__ double rotlin_term64(const Ctx &c, const double n[3],
   return lpot2d(c.t, r, cost);
 }
 
-__device__ __forceinline__ float rotlin_term32(const Ctx &c, const double n[3], int g0, int a1, int it)
+__device__ __forceinline__ float rotlin_term32(const Ctx &c, const float n[3], int g0, int a1, int it)
 {
   const DevSys &s = c.s;
   size_t i0 = sidx(s, it, g0), i1 = sidx(s, it, a1);
   float dx = c.st.xf[i0] - c.st.xf[i1], dy = c.st.yf[i0] - c.st.yf[i1], dz = c.st.zf[i0] - c.st.zf[i1];
   float r = sqrtf(dx * dx + dy * dy + dz * dz);
-  float cost = -((float)n[0] * dx + (float)n[1] * dy + (float)n[2] * dz) / r;
+  float cost = -(n[0] * dx + n[1] * dy + n[2] * dz) / r;
   return lpot2d32(c.t, r, cost);
 }
 
@@ -427,116 +506,218 @@ __device__ __forceinline__ double link_density(const Ctx &c, bool linear, const 
   return rho;
 }
 
+// fmod(x, 2 pi) for the proposal's angles: on [2 pi, 4 pi) the remainder
+// x - 2 pi is exact (Sterbenz), so the subtraction equals the library call
+__device__ __forceinline__ double fmod_2pi(double x, double pi2)
+{
+  if (x >= 0.0 && x < pi2) return x;
+  if (x >= pi2 && x < 2.0 * pi2) return x - pi2;
+  return fmod(x, pi2);
+}
+
+// the proposal of MCRotLinStep (mc_piqmc.cc:801-820) / MCRot3Dstep
+// (mc_piqmc.cc:955-1001): out = (phi, cos theta, chi)
+__device__ __forceinline__ void rot_propose(const DevSys &s, bool linear, double phi, double cost, double chi,
+                                            const double u[4], double out[3])
+{
+  if (linear) {
+    cost += (s.rtstep * (u[0] - 0.5));
+    phi += (s.rtstep * (u[1] - 0.5));
+    if (cost > 1.0) cost = 2.0 - cost;
+    if (cost < -1.0) cost = -2.0 - cost;
+  } else {
+    const double pi2 = 2.0 * PIMC_PI;
+    cost += (s.rtstep * (u[0] - 0.5));
+    phi += 2.0 * PIMC_PI * (s.rtstep * (u[1] - 0.5));
+    chi += 2.0 * PIMC_PI * (s.rtstep * (u[2] - 0.5));
+    if (phi < 0.0) phi = pi2 + phi;
+    if (chi < 0.0) chi = pi2 + chi;
+    phi = fmod_2pi(phi, pi2);
+    chi = fmod_2pi(chi, pi2);
+    if (cost > 1.0) cost = 2.0 - cost;
+    if (cost < -1.0) cost = -2.0 - cost;
+  }
+  out[0] = phi;
+  out[1] = cost;
+  out[2] = chi;
+}
+
+// the unit vector of (phi, cos theta) as the accept blocks write MCCosine
+__device__ __forceinline__ void unit_vector(double phi, double cost, double v[3])
+{
+  double sint = sqrt(1.0 - cost * cost);
+  v[0] = sint * cos(phi);
+  v[1] = sint * sin(phi);
+  v[2] = cost;
+}
+
+// uniforms of a production rotational move: pair index p = q / 2
+__device__ __forceinline__ void rot_uniforms(uint64_t seed, unsigned pass, unsigned phase, int p, int r, bool linear,
+                                             double u[4])
+{
+  uint64_t mv = ((uint64_t)pass << 32) | ((uint64_t)phase << 12) | (uint64_t)p;
+  double a, b;
+  philox_u2(seed, mv, 0x400000u | (uint32_t)r, 0u, &a, &b);
+  u[0] = a; u[1] = b;
+  philox_u2(seed, mv, 0x400000u | (uint32_t)r, 1u, &a, &b);
+  u[2] = a; u[3] = b;
+  if (linear) u[2] = u[3];
+}
+
 // MCRotLinStep (mc_piqmc.cc:781-936) / MCRot3Dstep (mc_piqmc.cc:938-1199)
 // for rotor g0 at rotational slice q with uniforms u (3 for a linear rotor,
-// 4 for a top).  The old potential and the old link densities come from the
-// caches when they are valid; both caches hold exactly the value a fresh
-// evaluation gives.  Returns 1 if accepted.
-template <bool MIX>
+// 4 for a top), on PIMC_ROT_THREADS threads.  The old potential and the old
+// link densities come from the caches when they are valid; both caches hold
+// exactly the value a fresh evaluation gives.  COH reads the neighbouring
+// slices' state through L2 (persistent launches, where other CTAs write it).
+// Returns 1 if accepted.
+template <bool MIX, bool COH>
 __device__ int rot_step(const Ctx &c, Frame *frames, int g0, int q, const double u[4], bool linear, RotShared &sh,
                         double *rd_out)
 {
   const DevSys &s = c.s;
-  int tid = threadIdx.x, Q = s.Q, R = s.R;
-  size_t n = (size_t)s.nrotors * Q;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int Q = s.Q, R = s.R;
+  const size_t n = (size_t)s.nrotors * Q;
   int q0 = q - 1, q2 = q + 1;
   if (q0 < 0) q0 += Q;
   if (q2 >= Q) q2 -= Q;
-  int r = g0 - s.rot_first;
-  int i0 = r * Q + q0, i1 = r * Q + q, i2 = r * Q + q2;
-  bool use_links = Q >= 3;
-  if (tid == 0) {
-    double cost = c.st.ang[n + i1], phi = c.st.ang[i1], chi = c.st.ang[2 * n + i1];
-    if (linear) {
-      cost += (s.rtstep * (u[0] - 0.5));
-      phi += (s.rtstep * (u[1] - 0.5));
-      if (cost > 1.0) cost = 2.0 - cost;
-      if (cost < -1.0) cost = -2.0 - cost;
-      double sint = sqrt(1.0 - cost * cost);
-      sh.nnew[0] = sint * cos(phi);
-      sh.nnew[1] = sint * sin(phi);
-      sh.nnew[2] = cost;
-      for (int d = 0; d < 3; d++) sh.nold[d] = c.st.cosv[d * n + i1];
-    } else {
-      const double pi2 = 2.0 * PIMC_PI;
-      cost += (s.rtstep * (u[0] - 0.5));
-      phi += 2.0 * PIMC_PI * (s.rtstep * (u[1] - 0.5));
-      chi += 2.0 * PIMC_PI * (s.rtstep * (u[2] - 0.5));
-      if (phi < 0.0) phi = pi2 + phi;
-      if (chi < 0.0) chi = pi2 + chi;
-      phi = fmod(phi, pi2);
-      chi = fmod(chi, pi2);
-      if (cost > 1.0) cost = 2.0 - cost;
-      if (cost < -1.0) cost = -2.0 - cost;
-      make_frame(phi, cost, chi, sh.fn);
-      sh.fo[0] = frames[i0];
-      sh.fo[1] = frames[i1];
-      sh.fo[2] = frames[i2];
-    }
-    sh.ang_new[0] = phi; sh.ang_new[1] = cost; sh.ang_new[2] = chi;
-    sh.bad = 0;
-    sh.pot_cached = c.st.rp_ok[i1];
-    if (sh.pot_cached) sh.pot[0] = c.st.rp_cache[i1];
-    sh.link_ok[0] = use_links && c.st.rl_ok[i0];
-    sh.link_ok[1] = use_links && c.st.rl_ok[i1];
-    if (sh.link_ok[0]) sh.rho[0] = c.st.rl_cache[i0];
-    if (sh.link_ok[1]) sh.rho[1] = c.st.rl_cache[i1];
-    for (int k = 0; k < 2 * R; k++) sh.skip[k] = g0;
-  }
-  __syncthreads();
-  if (tid < 4 && !(tid < 2 && sh.link_ok[tid])) {
-    // 0: (q-1, q) old, 1: (q, q+1) old, 2: (q-1, q) new, 3: (q, q+1) new
-    double na[3] = {0.0, 0.0, 0.0}, nb[3] = {0.0, 0.0, 0.0};
-    const Frame &fa = (tid == 0 || tid == 2) ? sh.fo[0] : (tid == 1 ? sh.fo[1] : sh.fn);
-    const Frame &fb = (tid == 0) ? sh.fo[1] : (tid == 2 ? sh.fn : sh.fo[2]);
-    if (linear) {
-      int ia = (tid == 0 || tid == 2) ? i0 : i1, ib = (tid == 1 || tid == 3) ? i2 : i1;
-      for (int d = 0; d < 3; d++) {
-        na[d] = (tid == 3) ? sh.nnew[d] : c.st.cosv[d * n + ia];
-        nb[d] = (tid == 2) ? sh.nnew[d] : c.st.cosv[d * n + ib];
+  const int r = g0 - s.rot_first;
+  const int i0 = r * Q + q0, i1 = r * Q + q, i2 = r * Q + q2;
+  const bool use_links = Q >= 3;                // link cache (with Q < 3 both links join the same two slices)
+  const bool need64 = !MIX || s.nrotors > 1;    // proposal frame in double during the evaluation
+
+  // ---------------- set-up (warps 0-2), commit values (warp 9)
+  if (warp == 0) {
+    if (lane == 0) {
+      double a[3];
+      rot_propose(s, linear, c.st.ang[i1], c.st.ang[n + i1], c.st.ang[2 * n + i1], u, a);
+      sh.ang_new[0] = a[0]; sh.ang_new[1] = a[1]; sh.ang_new[2] = a[2];
+      if (linear) {
+        if (MIX) {
+          float sp, cp, ct = (float)a[1];
+          sincosf((float)a[0], &sp, &cp);
+          float st = sqrtf(fmaxf(1.0f - ct * ct, 0.0f));
+          sh.nnewf[0] = st * cp; sh.nnewf[1] = st * sp; sh.nnewf[2] = ct;
+        } else {
+          unit_vector(a[0], a[1], sh.nnew);
+        }
+      } else if (need64) {
+        make_frame(a[0], a[1], a[2], sh.fn);
+      } else {
+        make_frame32((float)a[0], (float)a[1], (float)a[2], sh.fn.mf, &sh.fn.hzf);
       }
     }
-    int bad = 0;
-    sh.rho[tid] = link_density(c, linear, fa, fb, na, nb, &bad);
-    if (bad) atomicOr(&sh.bad, 1);
+  } else if (warp == 1) {
+    if (linear) {
+      if (lane < 9) {
+        int k = lane / 3, d = lane - 3 * (lane / 3);
+        int ii = (k == 0) ? i0 : (k == 1 ? i1 : i2);
+        sh.nv[k][d] = (k == 1) ? c.st.cosv[d * n + ii] : ld_state<COH>(c.st.cosv + d * n + ii);
+        if (k == 1) sh.nvf[d] = c.st.cosvf[d * n + ii];
+      }
+    } else {
+      copy_frame<COH>(sh.fo[0], frames + i0, lane);
+      copy_frame<false>(sh.fo[1], frames + i1, lane);
+      copy_frame<COH>(sh.fo[2], frames + i2, lane);
+    }
+  } else if (warp == 2) {
+    if (lane == 0) {
+      sh.bad = 0;
+      sh.pot_cached = c.st.rp_ok[i1];
+      if (sh.pot_cached) sh.pot_c = c.st.rp_cache[i1];
+      sh.link_ok[0] = use_links && ld_state<COH>(c.st.rl_ok + i0);
+      sh.link_ok[1] = use_links && ld_state<COH>(c.st.rl_ok + i1);
+      if (sh.link_ok[0]) sh.rho[0] = ld_state<COH>(c.st.rl_cache + i0);
+      if (sh.link_ok[1]) sh.rho[1] = ld_state<COH>(c.st.rl_cache + i1);
+    }
+    if (lane < 2 * R) sh.skip[lane] = g0;
+  } else if (warp == 9) {
+    if (lane == 0) {
+      double a[3];
+      rot_propose(s, linear, c.st.ang[i1], c.st.ang[n + i1], c.st.ang[2 * n + i1], u, a);
+      unit_vector(a[0], a[1], sh.cv);
+      if (!linear) make_frame(a[0], a[1], a[2], sh.fc);
+    }
   }
-  // partner sums: slots [0, R) old (unless cached), then R new
-  int first = sh.pot_cached ? R : 0;
-  int nsl = 2 * R - first;
-  if (linear) {
-    if (MIX)
-      slot_sums(nsl, s.na, sh.skip,
-                [&](int sl, int p) -> double {
-                  int k = sl + first;
-                  return (double)rotlin_term32(c, k < R ? sh.nold : sh.nnew, g0, p, q * R + (k % R));
-                },
-                sh.vals, sh.buf);
-    else
-      slot_sums(nsl, s.na, sh.skip,
-                [&](int sl, int p) -> double {
-                  int k = sl + first;
-                  return rotlin_term64(c, k < R ? sh.nold : sh.nnew, g0, p, q * R + (k % R));
-                },
-                sh.vals, sh.buf);
-  } else {
-    if (MIX)
-      slot_sums(nsl, s.na, sh.skip,
-                [&](int sl, int p) -> double {
-                  int k = sl + first;
-                  return (double)rot3d_term32(c, frames, k < R ? sh.fo[1] : sh.fn, g0, p, q * R + (k % R));
-                },
-                sh.vals, sh.buf);
-    else
-      slot_sums(nsl, s.na, sh.skip,
-                [&](int sl, int p) -> double {
-                  int k = sl + first;
-                  return rot3d_term64(c, frames, k < R ? sh.fo[1] : sh.fn, g0, p, q * R + (k % R));
-                },
-                sh.vals, sh.buf);
+  if (warp < 9) group_sync<1, PIMC_ROT_SETUP_THREADS>();
+
+  // ---------------- partner sums (warps 0-7) and link densities (warp 8)
+  if (warp < 8) {
+    const int first = sh.pot_cached ? R : 0;
+    const int nsl = 2 * R - first;
+    if (linear) {
+      if (MIX)
+        slot_sums_group<PIMC_ROT_PAIR_THREADS, 2>(
+            nsl, s.na, sh.skip,
+            [&](int sl, int p) -> double {
+              int k = sl + first;
+              return (double)rotlin_term32(c, k < R ? sh.nvf : sh.nnewf, g0, p, q * R + (k % R));
+            },
+            sh.vals, sh.buf);
+      else
+        slot_sums_group<PIMC_ROT_PAIR_THREADS, 2>(
+            nsl, s.na, sh.skip,
+            [&](int sl, int p) -> double {
+              int k = sl + first;
+              return rotlin_term64(c, k < R ? sh.nv[1] : sh.nnew, g0, p, q * R + (k % R));
+            },
+            sh.vals, sh.buf);
+    } else {
+      if (MIX)
+        slot_sums_group<PIMC_ROT_PAIR_THREADS, 2>(
+            nsl, s.na, sh.skip,
+            [&](int sl, int p) -> double {
+              int k = sl + first;
+              return (double)rot3d_term32(c, frames, k < R ? sh.fo[1] : sh.fn, g0, p, q * R + (k % R));
+            },
+            sh.vals, sh.buf);
+      else
+        slot_sums_group<PIMC_ROT_PAIR_THREADS, 2>(
+            nsl, s.na, sh.skip,
+            [&](int sl, int p) -> double {
+              int k = sl + first;
+              return rot3d_term64(c, frames, k < R ? sh.fo[1] : sh.fn, g0, p, q * R + (k % R));
+            },
+            sh.vals, sh.buf);
+    }
+  } else if (warp == 8) {
+    // 0: (q-1, q) old, 1: (q, q+1) old, 2: (q-1, q) new, 3: (q, q+1) new
+    if (lane < 4 && !(lane < 2 && sh.link_ok[lane])) {
+      int bad = 0;
+      double rho;
+      if (linear) {
+        double nn[3];
+        if (MIX) unit_vector(sh.ang_new[0], sh.ang_new[1], nn);
+        else for (int d = 0; d < 3; d++) nn[d] = sh.nnew[d];
+        const double *na = (lane == 0 || lane == 2) ? sh.nv[0] : (lane == 1 ? sh.nv[1] : nn);
+        const double *nb = (lane == 0) ? sh.nv[1] : (lane == 2 ? nn : sh.nv[2]);
+        rho = link_density(c, true, sh.fo[0], sh.fo[0], na, nb, &bad);
+      } else {
+        const Frame &fa = (lane == 0 || lane == 2) ? sh.fo[0] : (lane == 1 ? sh.fo[1] : sh.fn);
+        const Frame &fb = (lane == 0) ? sh.fo[1] : (lane == 2 ? sh.fn : sh.fo[2]);
+        if (MIX && s.rot_den_type == 0) {
+          rho = (double)rotden_rho32(c.t, fa.mf, fb.mf, &bad);
+        } else if (MIX && !need64 && lane >= 2) {
+          Frame f64;
+          make_frame64(sh.ang_new[0], sh.ang_new[1], sh.ang_new[2], f64);
+          rho = (lane == 2) ? link_density(c, false, fa, f64, nullptr, nullptr, &bad)
+                            : link_density(c, false, f64, fb, nullptr, nullptr, &bad);
+        } else {
+          rho = link_density(c, false, fa, fb, nullptr, nullptr, &bad);
+        }
+      }
+      sh.rho[lane] = rho;
+      if (bad) atomicOr(&sh.bad, 1);
+    }
   }
+  __syncthreads();
+
+  // ---------------- accept and commit
   if (tid == 0) {
+    const int first = sh.pot_cached ? R : 0;
     double pot_old = 0.0, pot_new = 0.0;
-    if (sh.pot_cached) pot_old = sh.pot[0];
+    if (sh.pot_cached) pot_old = sh.pot_c;
     else
       for (int k = 0; k < R; k++) pot_old += sh.vals[k];
     for (int k = 0; k < R; k++) pot_new += sh.vals[R - first + k];
@@ -573,24 +754,15 @@ __device__ int rot_step(const Ctx &c, Frame *frames, int g0, int q, const double
     sh.acc = acc;
     if (rd_out) *rd_out = rd;
     if (acc) {
-      double phi = sh.ang_new[0], cost = sh.ang_new[1];
-      c.st.ang[i1] = phi;
-      c.st.ang[n + i1] = cost;
-      if (linear) {
-        for (int d = 0; d < 3; d++) {
-          c.st.cosv[d * n + i1] = sh.nnew[d];
-          c.st.cosvf[d * n + i1] = (float)sh.nnew[d];
-        }
-      } else {
-        double chi = sh.ang_new[2];
-        c.st.ang[2 * n + i1] = chi;
-        double sint = sqrt(1.0 - cost * cost);
-        double cv[3] = {sint * cos(phi), sint * sin(phi), cost};
-        for (int d = 0; d < 3; d++) {
-          c.st.cosv[d * n + i1] = cv[d];
-          c.st.cosvf[d * n + i1] = (float)cv[d];
-        }
-        frames[i1] = sh.fn;
+      c.st.ang[i1] = sh.ang_new[0];
+      c.st.ang[n + i1] = sh.ang_new[1];
+      if (!linear) c.st.ang[2 * n + i1] = sh.ang_new[2];
+      for (int d = 0; d < 3; d++) {
+        c.st.cosv[d * n + i1] = sh.cv[d];
+        c.st.cosvf[d * n + i1] = (float)sh.cv[d];
+      }
+      if (!linear) {
+        frames[i1] = sh.fc;
         // the other rotors' potentials at slice q depend on this orientation
         for (int rr = 0; rr < s.nrotors; rr++)
           if (rr != r) c.st.rp_ok[rr * Q + q] = 0;

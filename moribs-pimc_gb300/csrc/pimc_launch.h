@@ -13,8 +13,14 @@ void launch_bisect_phase(const Ctx &c, Frame *f, int type, int s0, int j, unsign
                          const unsigned *pass, unsigned long long *cnt, cudaStream_t s);
 void launch_rot_replay(const Ctx &c, Frame *f, int parity, const double *urot, long nurot, double *rd, int *acc,
                        unsigned long long *cnt, cudaStream_t s);
-void launch_rot_phase(const Ctx &c, Frame *f, int parity, unsigned phase, uint64_t seed, const unsigned *pass,
-                      unsigned long long *cnt, cudaStream_t s);
+int launch_rot_phase(const Ctx &c, Frame *f, int parity, unsigned phase, uint64_t seed, const unsigned *pass,
+                     unsigned long long *cnt, cudaStream_t s);
+int rot_sweeps_max_ctas(int mixed);
+cudaError_t launch_rot_sweeps(const Ctx &c, Frame *f, int nctas, int nhalf, unsigned phase0, unsigned group,
+                              uint64_t seed, const unsigned *pass, unsigned long long *prog, unsigned *abort_word,
+                              unsigned long long *cnt, cudaStream_t s);
+void launch_bisect_block(const Ctx &c, Frame *f, int type, int s0, unsigned phase0, uint64_t seed,
+                         const unsigned *pass, unsigned long long *cnt, cudaStream_t s);
 void launch_mol(const Ctx &c, Frame *f, int type, int atom, bool replay, ReplaySrc src, uint64_t seed,
                 const unsigned *pass, unsigned phase, MolScratch *ms, double *dv, int *acc, unsigned long long *cnt,
                 cudaStream_t s);

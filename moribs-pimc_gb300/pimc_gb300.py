@@ -22,6 +22,7 @@ _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
 _lp = C.POINTER(C.c_long)
 _L = None
+OPT_FUSED = 1          # pimc_gb300.h PIMC_OPT_FUSED
 
 
 class PimcError(RuntimeError):
@@ -57,6 +58,7 @@ def load(path=LIBPATH):
     L.pimc_reset_counters.argtypes = [vp]
     L.pimc_synchronize.argtypes = [vp]
     L.pimc_set_precision.argtypes = [vp, C.c_int]
+    L.pimc_set_option.argtypes = [vp, C.c_int, C.c_longlong]
     L.pimc_bead_moves_per_pass.restype = C.c_double
     L.pimc_bead_moves_per_pass.argtypes = [vp]
     L.pimc_launch_count.restype = C.c_longlong
@@ -192,6 +194,9 @@ class Sampler:
         n = (C.c_longlong * 3)()
         _chk(self.L.pimc_profile_pass(self.h, C.c_uint64(seed), dptr(ms), n), "pimc_profile_pass")
         return ms, np.array(list(n))
+
+    def set_option(self, option, value):
+        _chk(self.L.pimc_set_option(self.h, int(option), int(value)), "pimc_set_option")
 
     def synchronize(self):
         _chk(self.L.pimc_synchronize(self.h), "pimc_synchronize")
