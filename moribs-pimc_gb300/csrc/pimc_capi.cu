@@ -623,7 +623,8 @@ extern "C" pimc_status pimc_rotations_move(pimc_handle *h, const double *urot, l
   int *dacc = (int *)cur;
   launch_rot_replay(h->ctx, h->frames, 0, du, nrot, drd, dacc, h->cnt, h->stream);
   launch_rot_replay(h->ctx, h->frames, 1, du, nrot, drd, dacc, h->cnt, h->stream);
-  h->launches += 2;
+  launch_refresh_frames(h->ctx, h->frames, h->stream);
+  h->launches += 3;
   CK(cudaGetLastError());
   if (rd_out) CK(cudaMemcpyAsync(rd_out, drd, nk * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   if (acc_out) CK(cudaMemcpyAsync(acc_out, dacc, nk * sizeof(int), cudaMemcpyDeviceToHost, h->stream));
@@ -905,6 +906,11 @@ extern "C" pimc_status pimc_run_passes(pimc_handle *h, int npasses, uint64_t see
     CK(cudaGraphLaunch(h->pass_exec, h->stream));
     h->launches += h->nodes_per_pass;
   }
+  if (npasses > 0 && h->sys.rotation && d.nrotors > 0) {
+    launch_refresh_frames(h->ctx, h->frames, h->stream);
+    h->launches++;
+    CK(cudaGetLastError());
+  }
   return PIMC_OK;
 }
 
@@ -935,6 +941,10 @@ extern "C" pimc_status pimc_profile_pass(pimc_handle *h, uint64_t seed, double *
     if ((e2 = launch_sweeps(h, pl, it0, it1, (unsigned)i, seed, &n[2]))) return e2;
   }
   CK(cudaEventRecord(ev[5], h->stream));
+  if (h->sys.rotation && d.nrotors > 0) {
+    launch_refresh_frames(h->ctx, h->frames, h->stream);
+    n[2]++;
+  }
   CK(cudaGetLastError());
   CK(cudaEventSynchronize(ev[5]));
   for (int k = 0; k < 3; k++) {

@@ -125,22 +125,27 @@ __global__ void __launch_bounds__(PIMC_ROT_THREADS) k_rot(Ctx c, Frame *frames, 
   const int nr = c.s.nrotors;
   const bool linear = c.s.molecule[c.s.imtype] == 1;
   const int per = linear ? 3 : 4;
+  const size_t n = (size_t)nr * c.s.Q;
   for (int r = 0; r < nr; r++) {
-    double u[4] = {0.5, 0.5, 0.5, 0.5};
-    if (REPLAY) {
-      // serial consumption order: even slices then odd, rotors inside a slice
-      long idx = rot_serial(c.s.Q, q) * (long)nr + r;
-      for (int k = 0; k < per; k++) {
-        long p = idx * per + k;
-        u[k] = (p < nurot) ? urot[p] : 0.5;
-        if (p >= nurot && threadIdx.x == 0) atomicOr(c.st.err, (unsigned)DERR_STREAM);
+    double u[4] = {0.5, 0.5, 0.5, 0.5}, prop[3] = {0.0, 0.0, 0.0};
+    if (threadIdx.x == 0) {
+      if (REPLAY) {
+        // serial consumption order: even slices then odd, rotors inside a slice
+        long idx = rot_serial(c.s.Q, q) * (long)nr + r;
+        for (int k = 0; k < per; k++) {
+          long p = idx * per + k;
+          u[k] = (p < nurot) ? urot[p] : 0.5;
+          if (p >= nurot) atomicOr(c.st.err, (unsigned)DERR_STREAM);
+        }
+      } else {
+        rot_uniforms(seed, *pass, phase, q >> 1, r, linear, u);
       }
-    } else {
-      rot_uniforms(seed, *pass, phase, q >> 1, r, linear, u);
+      size_t i1 = (size_t)r * c.s.Q + q;
+      rot_propose(c.s, linear, c.st.ang[i1], c.st.ang[n + i1], c.st.ang[2 * n + i1], u, prop);
     }
     int g0 = c.s.rot_first + r;
     double rd;
-    int acc = rot_step<MIX, false>(c, frames, g0, q, u, linear, sh, &rd);
+    int acc = rot_step<MIX, false>(c, frames, g0, q, u, prop, linear, sh, &rd);
     if (threadIdx.x == 0) {
       if (REPLAY) {
         rd_out[(size_t)q * nr + r] = rd;
@@ -197,10 +202,18 @@ __global__ void __launch_bounds__(PIMC_ROT_THREADS) k_rot_sweeps(Ctx c, Frame *f
   const unsigned ps = *pass;
   const unsigned long long id = ((unsigned long long)ps << 8) | (group & 255u);
   const int left = (b + nc - 1) % nc, right = (b + 1) % nc;
+  const size_t n = (size_t)nr * c.s.Q;
   unsigned long long tot = 0, nacc = 0;
+  double u[4] = {0.5, 0.5, 0.5, 0.5}, prop[3] = {0.0, 0.0, 0.0};
   for (int h = 0; h < nhalf; h++) {
     const int parity = h & 1;
+    const unsigned phase = phase0 + (unsigned)h;
     if (threadIdx.x == 0) {
+      // the first move's uniforms and proposal read only this CTA's own slice
+      // and are ready before the neighbour is
+      size_t i1 = (size_t)(2 * p0 + parity);
+      rot_uniforms(seed, ps, phase, p0, 0, linear, u);
+      rot_propose(c.s, linear, c.st.ang[i1], c.st.ang[n + i1], c.st.ang[2 * n + i1], u, prop);
       int st = 0;
       if (*(volatile unsigned *)abort_word) {
         atomicOr(c.st.err, (unsigned)DERR_TIMEOUT);
@@ -229,22 +242,22 @@ __global__ void __launch_bounds__(PIMC_ROT_THREADS) k_rot_sweeps(Ctx c, Frame *f
     }
     __syncthreads();
     if (stop) break;
-    const unsigned phase = phase0 + (unsigned)h;
     for (int p = p0; p < p1; p++) {
       const int q = 2 * p + parity;
       for (int r = 0; r < nr; r++) {
-        double u[4];
-        rot_uniforms(seed, ps, phase, p, r, linear, u);
-        int acc = rot_step<MIX, true>(c, frames, c.s.rot_first + r, q, u, linear, sh, nullptr);
+        if (threadIdx.x == 0 && (p != p0 || r != 0)) {
+          size_t i1 = (size_t)r * c.s.Q + q;
+          rot_uniforms(seed, ps, phase, p, r, linear, u);
+          rot_propose(c.s, linear, c.st.ang[i1], c.st.ang[n + i1], c.st.ang[2 * n + i1], u, prop);
+        }
+        int acc = rot_step<MIX, true>(c, frames, c.s.rot_first + r, q, u, prop, linear, sh, nullptr);
         tot++;
         nacc += acc;
       }
     }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      __threadfence();
-      st_release_u64(prog + b, (id << 24) | (unsigned long long)(h + 1));
-    }
+    // every global write of the moves was made by thread 0: its release
+    // store orders them before the progress word
+    if (threadIdx.x == 0) st_release_u64(prog + b, (id << 24) | (unsigned long long)(h + 1));
   }
   if (threadIdx.x == 0) {
     int ty = c.s.imtype;
@@ -535,6 +548,34 @@ __global__ void k_est_rcf(Ctx c, double *rcf)
 __global__ void k_pass_begin(unsigned *pass) { *pass += 1; }
 
 // ------------------------------------------------------------ launchers
+// the double-precision frames and MCCosine of nonlinear rotors from their
+// angles (what the rotational commits leave to be derived, see rot_step);
+// the float frames are kept as the moves evaluated them
+__global__ void k_refresh_frames(Ctx c, Frame *frames, int frames64)
+{
+  if (c.s.nrotors <= 0 || c.s.molecule[c.s.imtype] != 2) return;
+  size_t n = (size_t)c.s.nrotors * c.s.Q;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    double phi = c.st.ang[i], cost = c.st.ang[n + i], chi = c.st.ang[2 * n + i];
+    if (frames64) make_frame64(phi, cost, chi, frames[i]);
+    double v[3];
+    unit_vector(phi, cost, v);
+    for (int d = 0; d < 3; d++) {
+      c.st.cosv[d * n + i] = v[d];
+      c.st.cosvf[d * n + i] = (float)v[d];
+    }
+  }
+}
+
+void launch_refresh_frames(const Ctx &c, Frame *frames, cudaStream_t s)
+{
+  size_t n = (size_t)c.s.nrotors * c.s.Q;
+  int nb = (int)((n + 255) / 256);
+  if (nb < 1) nb = 1;
+  if (nb > 152) nb = 152;
+  k_refresh_frames<<<nb, 256, 0, s>>>(c, frames, c.s.mixed && c.s.nrotors == 1);
+}
+
 void launch_derive_state(const Ctx &c, Frame *frames, cudaStream_t s)
 {
   k_derive_state<<<152, 256, 0, s>>>(c, frames);

@@ -140,6 +140,7 @@ __device__ __forceinline__ void slot_sums(int nslots, int na, const int *skip, F
 // consumed unconditionally (3 per midpoint, mc_piqmc.cc:249-253), so they are
 // indexed from the level's base; accept draws are taken one at a time.
 struct ReplaySrc {
+  static constexpr bool kPrefetchU = false;  // rnd3() is drawn only where the reference draws it
   const double *g; long ng; long *gpos;      // gauss() x1 values
   const double *u; long nu; long *upos;      // rnd2()/rnd3() uniforms
   const double *d; long nd; long *dpos;      // rnd1() displacements
@@ -167,10 +168,12 @@ struct ReplaySrc {
   __device__ double gauss_pre(long base, int i, int, int, int) { return (base + i < ng) ? g[base + i] : 0.0; }
   __device__ double accept_u(int) { return take(u, nu, upos); }
   __device__ double disp_u(int) { return take(d, nd, dpos); }
+  __device__ double gauss_at32(int, int, int) { return 0.0; }
 };
 
 // counter-based source for production moves: one Philox block per draw
 struct PhiloxSrc {
+  static constexpr bool kPrefetchU = true;
   uint64_t seed, move;
   __device__ long gauss_base() { return 0; }
   __device__ double gauss_at(long, int level, int k, int dim)
@@ -178,6 +181,14 @@ struct PhiloxSrc {
     double r1, r2;
     philox_u2(seed, move, 0x100000u | ((uint32_t)level << 12) | (uint32_t)k, (uint32_t)dim, &r1, &r2);
     return sqrt(-log(r1)) * cos(2.0 * PIMC_PI * r2);        // Box-Muller as gauss() (mc_randg.cc:144)
+  }
+  // the same draw with float logarithm and cosine (FP32 path); the 53-bit
+  // uniform keeps the tail out to 6 sigma
+  __device__ double gauss_at32(int level, int k, int dim)
+  {
+    double r1, r2;
+    philox_u2(seed, move, 0x100000u | ((uint32_t)level << 12) | (uint32_t)k, (uint32_t)dim, &r1, &r2);
+    return (double)(sqrtf(-logf((float)r1)) * cospif(2.0f * (float)r2));
   }
   __device__ void gauss_advance(long) {}
   __device__ double gauss_pre(long, int, int level, int k, int dim) { return gauss_at(0, level, k, dim); }
@@ -220,6 +231,8 @@ __device__ __forceinline__ void store_bead(const Ctx &c, size_t i, double x, dou
 // Returns 1 when accepted; records per-level action differences.
 struct BisectShared {
   double gz[3 * PIMC_MAX_SEG];        // all Gaussian draws of the move, level by level
+  double ua[8];                       // accept uniforms per level (counter-based source)
+  double ob[3][PIMC_MAX_SEG + 1];     // the current beads of the window
   double nb[3][PIMC_MAX_SEG + 1];
   double en[PIMC_MAX_SEG + 1], eo[PIMC_MAX_SEG + 1];
   double sx[PIMC_MAX_SEG], sy[PIMC_MAX_SEG], sz[PIMC_MAX_SEG], se[PIMC_MAX_SEG];
@@ -250,9 +263,9 @@ __device__ int bisect_move(const Ctx &c, const Frame *frames, int type, int atom
     sh.owner[k] = own;
     sh.slice[k] = pt;
     size_t i = sidx(s, pt, own);
-    sh.nb[0][k] = c.st.x[i];
-    sh.nb[1][k] = c.st.y[i];
-    sh.nb[2][k] = c.st.z[i];
+    double x = c.st.x[i], y = c.st.y[i], z = c.st.z[i];
+    sh.nb[0][k] = x; sh.nb[1][k] = y; sh.nb[2][k] = z;
+    sh.ob[0][k] = x; sh.ob[1][k] = y; sh.ob[2][k] = z;
   }
   if (tid == 0) { sh.pot0 = 0.0; sh.pot1 = 0.0; sh.acc = 0; sh.passed = 0; sh.gbase = src.gauss_base(); }
   __syncthreads();
@@ -261,8 +274,11 @@ __device__ int bisect_move(const Ctx &c, const Frame *frames, int type, int atom
   for (int i = tid; i < 3 * (M - 1); i += blockDim.x) {
     int l = 31 - __clz(i / 3 + 1);
     int off = i - 3 * ((1 << l) - 1);
-    sh.gz[i] = src.gauss_pre(sh.gbase, i, l, off / 3, off - 3 * (off / 3));
+    if (MIX && Src::kPrefetchU) sh.gz[i] = src.gauss_at32(l, off / 3, off - 3 * (off / 3));
+    else sh.gz[i] = src.gauss_pre(sh.gbase, i, l, off / 3, off - 3 * (off / 3));
   }
+  if (Src::kPrefetchU)
+    for (int l = tid - 64; l >= 0 && l < L; l += blockDim.x) sh.ua[l] = src.accept_u(l);
   __syncthreads();
   double bnorm = 1.0 / (s.lambda[type] * s.tau);
   for (int level = 0; level < L; level++) {
@@ -278,11 +294,10 @@ __device__ int bisect_move(const Ctx &c, const Frame *frames, int type, int atom
         sh.nb[d][k1] = v;
       }
       int own = sh.owner[k1], pt = sh.slice[k1];
-      size_t i = sidx(s, pt, own);
       sh.sa[2 * j] = own; sh.st[2 * j] = pt;
       sh.sx[2 * j] = sh.nb[0][k1]; sh.sy[2 * j] = sh.nb[1][k1]; sh.sz[2 * j] = sh.nb[2][k1];
       sh.sa[2 * j + 1] = own; sh.st[2 * j + 1] = pt;
-      sh.sx[2 * j + 1] = c.st.x[i]; sh.sy[2 * j + 1] = c.st.y[i]; sh.sz[2 * j + 1] = c.st.z[i];
+      sh.sx[2 * j + 1] = sh.ob[0][k1]; sh.sy[2 * j + 1] = sh.ob[1][k1]; sh.sz[2 * j + 1] = sh.ob[2][k1];
     }
     if (tid == 0) { sh.gbase += 3 * nmid; src.gauss_advance(3 * nmid); }
     __syncthreads();
@@ -315,7 +330,7 @@ __device__ int bisect_move(const Ctx &c, const Frame *frames, int type, int atom
       if (ds_out) ds_out[level] = deltav;
       int a = 0;
       if (deltav < 0.0) a = 1;
-      else if (exp(-deltav) > src.accept_u(level)) a = 1;
+      else if (exp(-deltav) > (Src::kPrefetchU ? sh.ua[level] : src.accept_u(level))) a = 1;
       sh.acc = a;
       if (a) sh.passed = level + 1;
     }
@@ -346,14 +361,18 @@ struct MolScratch {
 // A rotational move runs on PIMC_ROT_THREADS threads in three roles:
 //   warps 0-7  the (slot, partner) sums over the R translational slices;
 //   warp 8     the link densities rho(q-1, q) and rho(q, q+1), old and new;
-//   warp 9     the proposal's frame and unit vector in double precision for
-//              the commit (on the FP32 path nothing else waits for them).
-// Named barrier 1 joins warps 0-8 after the set-up and barrier 2 the pair
-// warps inside the partner sums; all ten meet before the accept.  Long
-// double-precision chains thus run side by side instead of one after the
-// other on one warp.
+//   warp 9     a linear rotor's proposal unit vector in double precision on
+//              the FP32 path (the next moves' densities read it).
+// Barrier 2 joins the pair warps inside the partner sums; all ten meet after
+// the set-up and before the accept.  Long double-precision chains thus run
+// side by side instead of one after the other on one warp.
+//
+// For a nonlinear rotor the commit writes the angles and the frame the
+// evaluation used (on the FP32 path with one rotor only its float part);
+// the double-precision frame and MCCosine are then derived from the angles
+// by k_refresh_frames before anything reads them (estimators, state
+// download, queries), which gives the same values as writing them here.
 #define PIMC_ROT_PAIR_THREADS 256
-#define PIMC_ROT_SETUP_THREADS 288
 
 template <int ID, int NT>
 __device__ __forceinline__ void group_sync()
@@ -420,12 +439,11 @@ __device__ __forceinline__ void copy_frame(Frame &dst, const Frame *src, int lan
 struct RotShared {
   Frame fo[3];              // current frames at q-1, q, q+1
   Frame fn;                 // the proposal as evaluated (mf; m too where needed)
-  Frame fc;                 // the proposal in double precision, for the commit
   double rho[4], vals[2 * 16];
   double ang_new[3];
   double nv[3][3];          // linear rotor: current unit vectors at q-1, q, q+1
   double nnew[3];           // linear rotor: proposal unit vector (double path)
-  double cv[3];             // MCCosine of the proposal
+  double cv[3];             // linear rotor: MCCosine of the proposal
   float nvf[3], nnewf[3];   // linear rotor: current and proposal unit vectors for the FP32 path
   int bad, acc, pot_cached, link_ok[2];
   int skip[2 * 16];
@@ -566,14 +584,15 @@ __device__ __forceinline__ void rot_uniforms(uint64_t seed, unsigned pass, unsig
 
 // MCRotLinStep (mc_piqmc.cc:781-936) / MCRot3Dstep (mc_piqmc.cc:938-1199)
 // for rotor g0 at rotational slice q with uniforms u (3 for a linear rotor,
-// 4 for a top), on PIMC_ROT_THREADS threads.  The old potential and the old
-// link densities come from the caches when they are valid; both caches hold
-// exactly the value a fresh evaluation gives.  COH reads the neighbouring
-// slices' state through L2 (persistent launches, where other CTAs write it).
-// Returns 1 if accepted.
+// 4 for a top) and the proposal prop = rot_propose(current angles, u); u and
+// prop are read on thread 0 only.  Runs on PIMC_ROT_THREADS threads.  The
+// old potential and the old link densities come from the caches when they
+// are valid; both caches hold exactly the value a fresh evaluation gives.
+// COH reads the neighbouring slices' state through L2 (persistent launches,
+// where other CTAs write it).  Returns 1 if accepted.
 template <bool MIX, bool COH>
-__device__ int rot_step(const Ctx &c, Frame *frames, int g0, int q, const double u[4], bool linear, RotShared &sh,
-                        double *rd_out)
+__device__ int rot_step(const Ctx &c, Frame *frames, int g0, int q, const double u[4], const double prop[3],
+                        bool linear, RotShared &sh, double *rd_out)
 {
   const DevSys &s = c.s;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -587,11 +606,10 @@ __device__ int rot_step(const Ctx &c, Frame *frames, int g0, int q, const double
   const bool use_links = Q >= 3;                // link cache (with Q < 3 both links join the same two slices)
   const bool need64 = !MIX || s.nrotors > 1;    // proposal frame in double during the evaluation
 
-  // ---------------- set-up (warps 0-2), commit values (warp 9)
+  // ---------------- set-up (warps 0-2)
   if (warp == 0) {
     if (lane == 0) {
-      double a[3];
-      rot_propose(s, linear, c.st.ang[i1], c.st.ang[n + i1], c.st.ang[2 * n + i1], u, a);
+      const double a[3] = {prop[0], prop[1], prop[2]};
       sh.ang_new[0] = a[0]; sh.ang_new[1] = a[1]; sh.ang_new[2] = a[2];
       if (linear) {
         if (MIX) {
@@ -632,15 +650,8 @@ __device__ int rot_step(const Ctx &c, Frame *frames, int g0, int q, const double
       if (sh.link_ok[1]) sh.rho[1] = ld_state<COH>(c.st.rl_cache + i1);
     }
     if (lane < 2 * R) sh.skip[lane] = g0;
-  } else if (warp == 9) {
-    if (lane == 0) {
-      double a[3];
-      rot_propose(s, linear, c.st.ang[i1], c.st.ang[n + i1], c.st.ang[2 * n + i1], u, a);
-      unit_vector(a[0], a[1], sh.cv);
-      if (!linear) make_frame(a[0], a[1], a[2], sh.fc);
-    }
   }
-  if (warp < 9) group_sync<1, PIMC_ROT_SETUP_THREADS>();
+  __syncthreads();
 
   // ---------------- partner sums (warps 0-7) and link densities (warp 8)
   if (warp < 8) {
@@ -710,6 +721,11 @@ __device__ int rot_step(const Ctx &c, Frame *frames, int g0, int q, const double
       sh.rho[lane] = rho;
       if (bad) atomicOr(&sh.bad, 1);
     }
+  } else if (warp == 9) {
+    if (lane == 0 && linear) {
+      if (MIX) unit_vector(sh.ang_new[0], sh.ang_new[1], sh.cv);
+      else for (int d = 0; d < 3; d++) sh.cv[d] = sh.nnew[d];
+    }
   }
   __syncthreads();
 
@@ -723,7 +739,22 @@ __device__ int rot_step(const Ctx &c, Frame *frames, int g0, int q, const double
     for (int k = 0; k < R; k++) pot_new += sh.vals[R - first + k];
     double rd;
     int acc = 0, neg = 0;
-    if (s.rot_den_type == 0) {
+    if (MIX && s.rot_den_type == 0) {
+      // the FP32 path: densities, their ratio and the Boltzmann factor in float
+      float dens_old = (float)sh.rho[0] * (float)sh.rho[1], dens_new = (float)sh.rho[2] * (float)sh.rho[3];
+      if (fabsf(dens_old) < (float)PIMC_RZERO) dens_old = 0.0f;
+      if (fabsf(dens_new) < (float)PIMC_RZERO) dens_new = 0.0f;
+      if (linear) {
+        if (dens_old < 0.0f || dens_new < 0.0f) neg = 1;
+      } else {
+        dens_old = fabsf(dens_old);
+        dens_new = fabsf(dens_new);
+      }
+      float rf = (dens_old > (float)PIMC_RZERO) ? dens_new / dens_old : 1.0f;
+      rf *= expf((float)(-s.tau * (pot_new - pot_old)));
+      rd = (double)rf;
+      acc = (rf > 1.0f) || (rf > (float)u[linear ? 2 : 3]);
+    } else if (s.rot_den_type == 0) {
       double dens_old = sh.rho[0] * sh.rho[1], dens_new = sh.rho[2] * sh.rho[3];
       if (fabs(dens_old) < PIMC_RZERO) dens_old = 0.0;
       if (fabs(dens_new) < PIMC_RZERO) dens_new = 0.0;
@@ -756,13 +787,19 @@ __device__ int rot_step(const Ctx &c, Frame *frames, int g0, int q, const double
     if (acc) {
       c.st.ang[i1] = sh.ang_new[0];
       c.st.ang[n + i1] = sh.ang_new[1];
-      if (!linear) c.st.ang[2 * n + i1] = sh.ang_new[2];
-      for (int d = 0; d < 3; d++) {
-        c.st.cosv[d * n + i1] = sh.cv[d];
-        c.st.cosvf[d * n + i1] = (float)sh.cv[d];
-      }
-      if (!linear) {
-        frames[i1] = sh.fc;
+      if (linear) {
+        for (int d = 0; d < 3; d++) {
+          c.st.cosv[d * n + i1] = sh.cv[d];
+          c.st.cosvf[d * n + i1] = (float)sh.cv[d];
+        }
+      } else {
+        c.st.ang[2 * n + i1] = sh.ang_new[2];
+        if (need64) {
+          frames[i1] = sh.fn;
+        } else {
+          for (int k = 0; k < 9; k++) frames[i1].mf[k] = sh.fn.mf[k];
+          frames[i1].hzf = sh.fn.hzf;
+        }
         // the other rotors' potentials at slice q depend on this orientation
         for (int rr = 0; rr < s.nrotors; rr++)
           if (rr != r) c.st.rp_ok[rr * Q + q] = 0;

@@ -7,6 +7,7 @@ struct MolScratch;
 
 void launch_derive_state(const Ctx &c, Frame *frames, cudaStream_t s);
 void launch_invalidate_caches(const Ctx &c, cudaStream_t s);
+void launch_refresh_frames(const Ctx &c, Frame *frames, cudaStream_t s);
 void launch_bisect_replay(const Ctx &c, Frame *f, int type, int time0, int exch, ReplaySrc src, double *ds, int *lvl,
                           unsigned long long *cnt, cudaStream_t s);
 void launch_bisect_phase(const Ctx &c, Frame *f, int type, int s0, int j, unsigned phase, uint64_t seed,
