@@ -251,7 +251,7 @@ extern "C" pimc_status pimc_create(const pimc_system *sys, int device, pimc_hand
       (e = dalloc(h, &st.ang, 3 * nr)) || (e = dalloc(h, &st.cosv, 3 * nr)) || (e = dalloc(h, &st.pindex, na)) ||
       (e = dalloc(h, &st.mctype, na)) || (e = dalloc(h, &st.err, 1)) || (e = dalloc(h, &h->frames, nr)) ||
       (e = dalloc(h, &h->cnt, 12)) || (e = dalloc(h, &h->pass, 1)) || (e = dalloc(h, &h->cursors, 8)) ||
-      (e = dalloc(h, &h->prog, (size_t)(d.Q / 2 > 0 ? d.Q / 2 : 1))) || (e = dalloc(h, &h->abort_word, 1))) {
+      (e = dalloc(h, &h->prog, (size_t)(d.Q > 0 ? d.Q : 1))) || (e = dalloc(h, &h->abort_word, 1))) {
     pimc_destroy(h);
     return e;
   }
@@ -269,7 +269,7 @@ extern "C" pimc_status pimc_create(const pimc_system *sys, int device, pimc_hand
   CK(cudaMemset(st.err, 0, sizeof(unsigned)));
   CK(cudaMemset(h->cnt, 0, 12 * sizeof(unsigned long long)));
   CK(cudaMemset(h->pass, 0, sizeof(unsigned)));
-  h->nprog = d.Q / 2 > 0 ? d.Q / 2 : 1;
+  h->nprog = d.Q > 0 ? d.Q : 1;
   CK(cudaMemset(h->prog, 0, (size_t)h->nprog * sizeof(unsigned long long)));
   CK(cudaMemset(h->abort_word, 0, sizeof(unsigned)));
   std::vector<int> mct(na), pidx(na);
@@ -823,6 +823,13 @@ static pimc_status launch_sweeps(pimc_handle *h, const PassPlan &pl, int it0, in
   if (!h->sys.rotation || d.nrotors <= 0 || it1 <= it0) return PIMC_OK;
   int nctas = 0;
   if (h->fused && d.Q >= 2 && d.Q % 2 == 0) {
+    if (d.nrotors == 1 && rot_slices_max_ctas(d.mixed) >= d.Q) {
+      // one CTA per slice, next move prepared while the neighbours move
+      CK(launch_rot_slices(h->ctx, h->frames, 2 * (it1 - it0), pl.B + 2u * (unsigned)it0, group, seed, h->pass,
+                           h->prog, h->abort_word, h->cnt, h->stream));
+      (*n)++;
+      return PIMC_OK;
+    }
     nctas = rot_sweeps_max_ctas(d.mixed);
     if (nctas > d.Q / 2) nctas = d.Q / 2;
   }

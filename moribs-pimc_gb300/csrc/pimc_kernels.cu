@@ -108,6 +108,60 @@ __global__ void __launch_bounds__(PIMC_BLOCK) k_bisect_block(Ctx c, Frame *frame
 }
 
 // ------------------------------------------------------------ rotations
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long *p)
+{
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_u64(unsigned long long *p, unsigned long long v)
+{
+  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long global_ns()
+{
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// waits and progress of a one-slice-per-CTA persistent launch (warp 8, lane 0)
+struct RotSliceHooks {
+  const unsigned long long *wl, *wr;    // progress words of the neighbouring slices
+  unsigned long long *mine;
+  unsigned long long id;
+  unsigned *abort_word, *err;
+  int h;
+  __device__ bool wait()
+  {
+    if (*(volatile unsigned *)abort_word) {
+      atomicOr(err, (unsigned)DERR_TIMEOUT);
+      return false;
+    }
+    if (h == 0) return true;
+    const unsigned long long t0 = global_ns();
+    for (int side = 0; side < 2; side++) {
+      const unsigned long long *w = side ? wr : wl;
+      for (;;) {
+        unsigned long long v = ld_acquire_u64(w);
+        if ((v >> 24) == id && (long long)(v & 0xFFFFFFull) >= h) break;
+        if (*(volatile unsigned *)abort_word) {
+          atomicOr(err, (unsigned)DERR_TIMEOUT);
+          return false;
+        }
+        if (global_ns() - t0 > 2000000000ull) {
+          atomicExch(abort_word, 1u);
+          atomicOr(err, (unsigned)DERR_TIMEOUT);
+          return false;
+        }
+      }
+    }
+    __threadfence();
+    return true;
+  }
+  __device__ void published() { st_release_u64(mine, (id << 24) | (unsigned long long)(h + 1)); }
+};
+
 // serial position of slice q in MCRotationsMove's loops: even slices, then odd
 __device__ __forceinline__ long rot_serial(int Q, int q) { return (q & 1) ? (Q + 1) / 2 + q / 2 : q / 2; }
 
@@ -144,8 +198,8 @@ __global__ void __launch_bounds__(PIMC_ROT_THREADS) k_rot(Ctx c, Frame *frames, 
       rot_propose(c.s, linear, c.st.ang[i1], c.st.ang[n + i1], c.st.ang[2 * n + i1], u, prop);
     }
     int g0 = c.s.rot_first + r;
-    double rd;
-    int acc = rot_step<MIX, false>(c, frames, g0, q, u, prop, linear, sh, &rd);
+    int acc = rot_step<MIX, false>(c, frames, g0, q, u, prop, linear, sh, nullptr);
+    double rd = sh.rd;          // written by the finishing warp
     if (threadIdx.x == 0) {
       if (REPLAY) {
         rd_out[(size_t)q * nr + r] = rd;
@@ -156,23 +210,6 @@ __global__ void __launch_bounds__(PIMC_ROT_THREADS) k_rot(Ctx c, Frame *frames, 
       if (acc) atomicAdd(&cnt[(ty * 3 + 2) * 2 + 1], 1ull);
     }
   }
-}
-
-__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long *p)
-{
-  unsigned long long v;
-  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
-  return v;
-}
-__device__ __forceinline__ void st_release_u64(unsigned long long *p, unsigned long long v)
-{
-  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
-}
-__device__ __forceinline__ unsigned long long global_ns()
-{
-  unsigned long long t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
 }
 
 // nhalf half-sweeps (even slices, odd slices, even, ...) of the rotational
@@ -255,9 +292,11 @@ __global__ void __launch_bounds__(PIMC_ROT_THREADS) k_rot_sweeps(Ctx c, Frame *f
         nacc += acc;
       }
     }
-    // every global write of the moves was made by thread 0: its release
-    // store orders them before the progress word
-    if (threadIdx.x == 0) st_release_u64(prog + b, (id << 24) | (unsigned long long)(h + 1));
+    // the commits (warp 8) precede the barrier that ended the last move
+    if (threadIdx.x == 0) {
+      __threadfence();
+      st_release_u64(prog + b, (id << 24) | (unsigned long long)(h + 1));
+    }
   }
   if (threadIdx.x == 0) {
     int ty = c.s.imtype;
@@ -602,6 +641,62 @@ void launch_bisect_phase(const Ctx &c, Frame *f, int type, int s0, int j, unsign
   else k_bisect_phase<false><<<c.s.P / M, PIMC_BLOCK, 0, s>>>(c, f, type, s0, j, phase, seed, pass, cnt);
 }
 
+// nhalf half-sweeps with one CTA per rotational slice (one rotor, Q even,
+// all Q CTAs resident).  Slice q moves in the half-sweeps of its parity;
+// its move at h waits for both neighbours to have finished h-1, and its
+// next move is prepared (proposal, frame, partner sums: nothing a
+// neighbour writes) while they move.  The same uniforms and the same
+// states as the launch-per-half-sweep schedule: identical results.
+template <bool MIX>
+__global__ void __launch_bounds__(PIMC_ROT_THREADS) k_rot_slices(Ctx c, Frame *frames, int nhalf, unsigned phase0,
+                                                                 unsigned group, uint64_t seed, const unsigned *pass,
+                                                                 unsigned long long *prog, unsigned *abort_word,
+                                                                 unsigned long long *cnt)
+{
+  __shared__ RotShared sh;
+  const int Q = c.s.Q, q = blockIdx.x;
+  const bool linear = c.s.molecule[c.s.imtype] == 1;
+  const unsigned ps = *pass;
+  const size_t n = (size_t)Q;
+  const int g0 = c.s.rot_first;
+  RotSliceHooks hk;
+  hk.wl = prog + (q + Q - 1) % Q;
+  hk.wr = prog + (q + 1) % Q;
+  hk.mine = prog + q;
+  hk.id = ((unsigned long long)ps << 8) | (group & 255u);
+  hk.abort_word = abort_word;
+  hk.err = c.st.err;
+  unsigned long long tot = 0, nacc = 0;
+  double u[4] = {0.5, 0.5, 0.5, 0.5}, prop[3] = {0.0, 0.0, 0.0};
+  int h = q & 1;
+  if (h < nhalf) {
+    if (threadIdx.x == 0) {
+      rot_uniforms(seed, ps, phase0 + (unsigned)h, q >> 1, 0, linear, u);
+      rot_propose(c.s, linear, c.st.ang[q], c.st.ang[n + q], c.st.ang[2 * n + q], u, prop);
+    }
+    rot_prepare<MIX>(c, frames, g0, q, u, prop, linear, sh);
+  }
+  for (; h < nhalf; h += 2) {
+    hk.h = h;
+    int acc = rot_finish<MIX, true>(c, frames, g0, q, linear, sh, nullptr, hk);
+    if (sh.stop) break;
+    tot++;
+    nacc += acc;
+    if (h + 2 < nhalf) {
+      if (threadIdx.x == 0) {
+        rot_uniforms(seed, ps, phase0 + (unsigned)(h + 2), q >> 1, 0, linear, u);
+        rot_propose(c.s, linear, c.st.ang[q], c.st.ang[n + q], c.st.ang[2 * n + q], u, prop);
+      }
+      rot_prepare<MIX>(c, frames, g0, q, u, prop, linear, sh);
+    }
+  }
+  if (threadIdx.x == 0) {
+    int ty = c.s.imtype;
+    atomicAdd(&cnt[(ty * 3 + 2) * 2 + 0], tot);
+    atomicAdd(&cnt[(ty * 3 + 2) * 2 + 1], nacc);
+  }
+}
+
 // the slices of one half of a sweep as independent sets: with Q odd the
 // last even slice neighbours slice 0 and runs after the other even slices,
 // as in the serial loop
@@ -645,6 +740,36 @@ int launch_rot_phase(const Ctx &c, Frame *f, int parity, unsigned phase, uint64_
     n++;
   });
   return n;
+}
+
+int rot_slices_max_ctas(int mixed)
+{
+  int dev = 0, nsm = 0, per = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+  cudaError_t e = mixed ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_rot_slices<true>, PIMC_ROT_THREADS, 0)
+                        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_rot_slices<false>, PIMC_ROT_THREADS, 0);
+  if (e != cudaSuccess) return 0;
+  return nsm * per;
+}
+
+cudaError_t launch_rot_slices(const Ctx &c, Frame *f, int nhalf, unsigned phase0, unsigned group, uint64_t seed,
+                              const unsigned *pass, unsigned long long *prog, unsigned *abort_word,
+                              unsigned long long *cnt, cudaStream_t s)
+{
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(c.s.Q);
+  cfg.blockDim = dim3(PIMC_ROT_THREADS);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  if (c.s.mixed)
+    return cudaLaunchKernelEx(&cfg, k_rot_slices<true>, c, f, nhalf, phase0, group, seed, pass, prog, abort_word, cnt);
+  return cudaLaunchKernelEx(&cfg, k_rot_slices<false>, c, f, nhalf, phase0, group, seed, pass, prog, abort_word, cnt);
 }
 
 int rot_sweeps_max_ctas(int mixed)

@@ -358,14 +358,16 @@ struct MolScratch {
 };
 
 // ------------------------------------------------------ rotational moves
-// A rotational move runs on PIMC_ROT_THREADS threads in three roles:
-//   warps 0-7  the (slot, partner) sums over the R translational slices;
-//   warp 8     the link densities rho(q-1, q) and rho(q, q+1), old and new;
-//   warp 9     a linear rotor's proposal unit vector in double precision on
-//              the FP32 path (the next moves' densities read it).
-// Barrier 2 joins the pair warps inside the partner sums; all ten meet after
-// the set-up and before the accept.  Long double-precision chains thus run
-// side by side instead of one after the other on one warp.
+// A rotational move runs on PIMC_ROT_THREADS threads in two stages.
+// rot_prepare reads only the moved slice: the proposal's frame, the
+// (slot, partner) sums over its R translational slices (warps 0-7, named
+// barrier 2 inside the sums) and, for a linear rotor on the FP32 path, the
+// proposal's unit vector in double precision (warp 9).  rot_finish reads the
+// neighbouring slices and runs on warp 8 alone: their frames and the link
+// cache, the link densities rho(q-1, q) and rho(q, q+1) old and new (lanes
+// 0-3), the accept and the commit (lane 0).  A persistent launch that owns
+// one slice per CTA prepares the slice's next move while the neighbours
+// move, so only rot_finish lies on the chain between neighbouring slices.
 //
 // For a nonlinear rotor the commit writes the angles and the frame the
 // evaluation used (on the FP32 path with one rotor only its float part);
@@ -445,9 +447,10 @@ struct RotShared {
   double nnew[3];           // linear rotor: proposal unit vector (double path)
   double cv[3];             // linear rotor: MCCosine of the proposal
   float nvf[3], nnewf[3];   // linear rotor: current and proposal unit vectors for the FP32 path
-  int bad, acc, pot_cached, link_ok[2];
+  int bad, acc, pot_cached, link_ok[2], stop;
   int skip[2 * 16];
   double pot_c, rd;
+  double u[4], pot_old, pot_new;
   double buf[PIMC_RED_BUF];
 };
 
@@ -582,33 +585,26 @@ __device__ __forceinline__ void rot_uniforms(uint64_t seed, unsigned pass, unsig
   if (linear) u[2] = u[3];
 }
 
-// MCRotLinStep (mc_piqmc.cc:781-936) / MCRot3Dstep (mc_piqmc.cc:938-1199)
-// for rotor g0 at rotational slice q with uniforms u (3 for a linear rotor,
-// 4 for a top) and the proposal prop = rot_propose(current angles, u); u and
-// prop are read on thread 0 only.  Runs on PIMC_ROT_THREADS threads.  The
-// old potential and the old link densities come from the caches when they
-// are valid; both caches hold exactly the value a fresh evaluation gives.
-// COH reads the neighbouring slices' state through L2 (persistent launches,
-// where other CTAs write it).  Returns 1 if accepted.
-template <bool MIX, bool COH>
-__device__ int rot_step(const Ctx &c, Frame *frames, int g0, int q, const double u[4], const double prop[3],
-                        bool linear, RotShared &sh, double *rd_out)
+// MCRotLinStep (mc_piqmc.cc:781-936) / MCRot3Dstep (mc_piqmc.cc:938-1199),
+// first stage, for rotor g0 at rotational slice q with uniforms u (3 for a
+// linear rotor, 4 for a top) and the proposal prop = rot_propose(current
+// angles, u); u and prop are read on thread 0 only.  Leaves in sh the
+// proposal, its frame, and pot_old / pot_new (the old potential from the
+// cache when it is valid; the cache holds exactly what a fresh evaluation
+// gives).  All PIMC_ROT_THREADS threads call it.
+template <bool MIX>
+__device__ void rot_prepare(const Ctx &c, const Frame *frames, int g0, int q, const double u[4], const double prop[3],
+                            bool linear, RotShared &sh)
 {
   const DevSys &s = c.s;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int Q = s.Q, R = s.R;
   const size_t n = (size_t)s.nrotors * Q;
-  int q0 = q - 1, q2 = q + 1;
-  if (q0 < 0) q0 += Q;
-  if (q2 >= Q) q2 -= Q;
-  const int r = g0 - s.rot_first;
-  const int i0 = r * Q + q0, i1 = r * Q + q, i2 = r * Q + q2;
-  const bool use_links = Q >= 3;                // link cache (with Q < 3 both links join the same two slices)
+  const int i1 = (g0 - s.rot_first) * Q + q;
   const bool need64 = !MIX || s.nrotors > 1;    // proposal frame in double during the evaluation
-
-  // ---------------- set-up (warps 0-2)
   if (warp == 0) {
     if (lane == 0) {
+      for (int k = 0; k < 4; k++) sh.u[k] = u[k];
       const double a[3] = {prop[0], prop[1], prop[2]};
       sh.ang_new[0] = a[0]; sh.ang_new[1] = a[1]; sh.ang_new[2] = a[2];
       if (linear) {
@@ -628,32 +624,21 @@ __device__ int rot_step(const Ctx &c, Frame *frames, int g0, int q, const double
     }
   } else if (warp == 1) {
     if (linear) {
-      if (lane < 9) {
-        int k = lane / 3, d = lane - 3 * (lane / 3);
-        int ii = (k == 0) ? i0 : (k == 1 ? i1 : i2);
-        sh.nv[k][d] = (k == 1) ? c.st.cosv[d * n + ii] : ld_state<COH>(c.st.cosv + d * n + ii);
-        if (k == 1) sh.nvf[d] = c.st.cosvf[d * n + ii];
+      if (lane < 3) {
+        sh.nv[1][lane] = c.st.cosv[lane * n + i1];
+        sh.nvf[lane] = c.st.cosvf[lane * n + i1];
       }
     } else {
-      copy_frame<COH>(sh.fo[0], frames + i0, lane);
       copy_frame<false>(sh.fo[1], frames + i1, lane);
-      copy_frame<COH>(sh.fo[2], frames + i2, lane);
     }
   } else if (warp == 2) {
     if (lane == 0) {
-      sh.bad = 0;
       sh.pot_cached = c.st.rp_ok[i1];
       if (sh.pot_cached) sh.pot_c = c.st.rp_cache[i1];
-      sh.link_ok[0] = use_links && ld_state<COH>(c.st.rl_ok + i0);
-      sh.link_ok[1] = use_links && ld_state<COH>(c.st.rl_ok + i1);
-      if (sh.link_ok[0]) sh.rho[0] = ld_state<COH>(c.st.rl_cache + i0);
-      if (sh.link_ok[1]) sh.rho[1] = ld_state<COH>(c.st.rl_cache + i1);
     }
     if (lane < 2 * R) sh.skip[lane] = g0;
   }
   __syncthreads();
-
-  // ---------------- partner sums (warps 0-7) and link densities (warp 8)
   if (warp < 8) {
     const int first = sh.pot_cached ? R : 0;
     const int nsl = 2 * R - first;
@@ -692,34 +677,14 @@ __device__ int rot_step(const Ctx &c, Frame *frames, int g0, int q, const double
             },
             sh.vals, sh.buf);
     }
-  } else if (warp == 8) {
-    // 0: (q-1, q) old, 1: (q, q+1) old, 2: (q-1, q) new, 3: (q, q+1) new
-    if (lane < 4 && !(lane < 2 && sh.link_ok[lane])) {
-      int bad = 0;
-      double rho;
-      if (linear) {
-        double nn[3];
-        if (MIX) unit_vector(sh.ang_new[0], sh.ang_new[1], nn);
-        else for (int d = 0; d < 3; d++) nn[d] = sh.nnew[d];
-        const double *na = (lane == 0 || lane == 2) ? sh.nv[0] : (lane == 1 ? sh.nv[1] : nn);
-        const double *nb = (lane == 0) ? sh.nv[1] : (lane == 2 ? nn : sh.nv[2]);
-        rho = link_density(c, true, sh.fo[0], sh.fo[0], na, nb, &bad);
-      } else {
-        const Frame &fa = (lane == 0 || lane == 2) ? sh.fo[0] : (lane == 1 ? sh.fo[1] : sh.fn);
-        const Frame &fb = (lane == 0) ? sh.fo[1] : (lane == 2 ? sh.fn : sh.fo[2]);
-        if (MIX && s.rot_den_type == 0) {
-          rho = (double)rotden_rho32(c.t, fa.mf, fb.mf, &bad);
-        } else if (MIX && !need64 && lane >= 2) {
-          Frame f64;
-          make_frame64(sh.ang_new[0], sh.ang_new[1], sh.ang_new[2], f64);
-          rho = (lane == 2) ? link_density(c, false, fa, f64, nullptr, nullptr, &bad)
-                            : link_density(c, false, f64, fb, nullptr, nullptr, &bad);
-        } else {
-          rho = link_density(c, false, fa, fb, nullptr, nullptr, &bad);
-        }
-      }
-      sh.rho[lane] = rho;
-      if (bad) atomicOr(&sh.bad, 1);
+    if (tid == 0) {
+      double pot_old = 0.0, pot_new = 0.0;
+      if (sh.pot_cached) pot_old = sh.pot_c;
+      else
+        for (int k = 0; k < R; k++) pot_old += sh.vals[k];
+      for (int k = 0; k < R; k++) pot_new += sh.vals[R - first + k];
+      sh.pot_old = pot_old;
+      sh.pot_new = pot_new;
     }
   } else if (warp == 9) {
     if (lane == 0 && linear) {
@@ -728,94 +693,180 @@ __device__ int rot_step(const Ctx &c, Frame *frames, int g0, int q, const double
     }
   }
   __syncthreads();
+}
 
-  // ---------------- accept and commit
-  if (tid == 0) {
-    const int first = sh.pot_cached ? R : 0;
-    double pot_old = 0.0, pot_new = 0.0;
-    if (sh.pot_cached) pot_old = sh.pot_c;
-    else
-      for (int k = 0; k < R; k++) pot_old += sh.vals[k];
-    for (int k = 0; k < R; k++) pot_new += sh.vals[R - first + k];
-    double rd;
-    int acc = 0, neg = 0;
-    if (MIX && s.rot_den_type == 0) {
-      // the FP32 path: densities, their ratio and the Boltzmann factor in float
-      float dens_old = (float)sh.rho[0] * (float)sh.rho[1], dens_new = (float)sh.rho[2] * (float)sh.rho[3];
-      if (fabsf(dens_old) < (float)PIMC_RZERO) dens_old = 0.0f;
-      if (fabsf(dens_new) < (float)PIMC_RZERO) dens_new = 0.0f;
-      if (linear) {
-        if (dens_old < 0.0f || dens_new < 0.0f) neg = 1;
-      } else {
-        dens_old = fabsf(dens_old);
-        dens_new = fabsf(dens_new);
-      }
-      float rf = (dens_old > (float)PIMC_RZERO) ? dens_new / dens_old : 1.0f;
-      rf *= expf((float)(-s.tau * (pot_new - pot_old)));
-      rd = (double)rf;
-      acc = (rf > 1.0f) || (rf > (float)u[linear ? 2 : 3]);
-    } else if (s.rot_den_type == 0) {
-      double dens_old = sh.rho[0] * sh.rho[1], dens_new = sh.rho[2] * sh.rho[3];
-      if (fabs(dens_old) < PIMC_RZERO) dens_old = 0.0;
-      if (fabs(dens_new) < PIMC_RZERO) dens_new = 0.0;
-      if (linear) {
-        if (dens_old < 0.0 || dens_new < 0.0) neg = 1;          // mc_piqmc.cc:850,886
-      } else {
-        if (dens_old < 0.0) dens_old = fabs(dens_old);          // mc_piqmc.cc:1067,1133
-        if (dens_new < 0.0) dens_new = fabs(dens_new);
-      }
-      rd = (dens_old > PIMC_RZERO) ? dens_new / dens_old : 1.0;
-      rd *= exp(-s.tau * (pot_new - pot_old));
-      acc = (rd > 1.0) || (rd > u[linear ? 2 : 3]);
-    } else if (linear) {
-      double dens_old = sh.rho[0] + sh.rho[1], dens_new = sh.rho[2] + sh.rho[3];
-      if (fabs(dens_old) < PIMC_RZERO) dens_old = 0.0;
-      if (fabs(dens_new) < PIMC_RZERO) dens_new = 0.0;
-      rd = dens_new - dens_old - s.tau * (pot_new - pot_old);
-      acc = (rd > 0.0) || (rd > log(u[2]));
-    } else {
-      double rhoold = sh.rho[0] + sh.rho[1], rhonew = sh.rho[2] + sh.rho[3];
-      rd = (rhonew - rhoold) / (4.0 * (s.rot_tau / PIMC_WNO2K));
-      rd -= s.tau * (pot_new - pot_old);
-      acc = (rd > 0.0) || (rd > log(u[3]));
+// hooks of rot_finish for launches without neighbour waits
+struct RotNoHooks {
+  __device__ bool wait() { return true; }
+  __device__ void published() {}
+};
+
+// second stage of the move prepared in sh, on warp 8: hooks.wait() on lane 0
+// before the neighbours' state is read (false: leave the move undone and set
+// sh.stop), hooks.published() on lane 0 after the commit.  COH reads the
+// neighbours through L2 (persistent launches, where other CTAs write them).
+// All PIMC_ROT_THREADS threads call it; returns 1 if accepted.
+template <bool MIX, bool COH, class Hooks>
+__device__ int rot_finish(const Ctx &c, Frame *frames, int g0, int q, bool linear, RotShared &sh, double *rd_out,
+                          Hooks &hooks)
+{
+  const DevSys &s = c.s;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int Q = s.Q;
+  const size_t n = (size_t)s.nrotors * Q;
+  int q0 = q - 1, q2 = q + 1;
+  if (q0 < 0) q0 += Q;
+  if (q2 >= Q) q2 -= Q;
+  const int r = g0 - s.rot_first;
+  const int i0 = r * Q + q0, i1 = r * Q + q, i2 = r * Q + q2;
+  const bool use_links = Q >= 3;                // link cache (with Q < 3 both links join the same two slices)
+  const bool need64 = !MIX || s.nrotors > 1;
+  if (warp == 8) {
+    if (lane == 0) {
+      int go = hooks.wait();
+      sh.stop = !go;
     }
-    if (neg) { atomicOr(c.st.err, (unsigned)DERR_NEG_DENSITY); acc = 0; }
-    if (sh.bad) { atomicOr(c.st.err, (unsigned)DERR_GRID_RANGE); acc = 0; }
-    sh.rd = rd;
-    sh.acc = acc;
-    if (rd_out) *rd_out = rd;
-    if (acc) {
-      c.st.ang[i1] = sh.ang_new[0];
-      c.st.ang[n + i1] = sh.ang_new[1];
+    __syncwarp();
+    if (!sh.stop) {
       if (linear) {
-        for (int d = 0; d < 3; d++) {
-          c.st.cosv[d * n + i1] = sh.cv[d];
-          c.st.cosvf[d * n + i1] = (float)sh.cv[d];
+        if (lane < 6) {
+          int k = (lane < 3) ? 0 : 2, d = lane - (lane < 3 ? 0 : 3);
+          sh.nv[k][d] = ld_state<COH>(c.st.cosv + d * n + (k == 0 ? i0 : i2));
         }
       } else {
-        c.st.ang[2 * n + i1] = sh.ang_new[2];
-        if (need64) {
-          frames[i1] = sh.fn;
+        copy_frame<COH>(sh.fo[0], frames + i0, lane);
+        copy_frame<COH>(sh.fo[2], frames + i2, lane);
+      }
+      if (lane == 0) {
+        sh.bad = 0;
+        sh.link_ok[0] = use_links && ld_state<COH>(c.st.rl_ok + i0);
+        sh.link_ok[1] = use_links && ld_state<COH>(c.st.rl_ok + i1);
+        if (sh.link_ok[0]) sh.rho[0] = ld_state<COH>(c.st.rl_cache + i0);
+        if (sh.link_ok[1]) sh.rho[1] = ld_state<COH>(c.st.rl_cache + i1);
+      }
+      __syncwarp();
+      // 0: (q-1, q) old, 1: (q, q+1) old, 2: (q-1, q) new, 3: (q, q+1) new
+      if (lane < 4 && !(lane < 2 && sh.link_ok[lane])) {
+        int bad = 0;
+        double rho;
+        if (linear) {
+          double nn[3];
+          if (MIX) unit_vector(sh.ang_new[0], sh.ang_new[1], nn);
+          else for (int d = 0; d < 3; d++) nn[d] = sh.nnew[d];
+          const double *na = (lane == 0 || lane == 2) ? sh.nv[0] : (lane == 1 ? sh.nv[1] : nn);
+          const double *nb = (lane == 0) ? sh.nv[1] : (lane == 2 ? nn : sh.nv[2]);
+          rho = link_density(c, true, sh.fo[0], sh.fo[0], na, nb, &bad);
         } else {
-          for (int k = 0; k < 9; k++) frames[i1].mf[k] = sh.fn.mf[k];
-          frames[i1].hzf = sh.fn.hzf;
+          const Frame &fa = (lane == 0 || lane == 2) ? sh.fo[0] : (lane == 1 ? sh.fo[1] : sh.fn);
+          const Frame &fb = (lane == 0) ? sh.fo[1] : (lane == 2 ? sh.fn : sh.fo[2]);
+          if (MIX && s.rot_den_type == 0) {
+            rho = (double)rotden_rho32(c.t, fa.mf, fb.mf, &bad);
+          } else if (MIX && !need64 && lane >= 2) {
+            Frame f64;
+            make_frame64(sh.ang_new[0], sh.ang_new[1], sh.ang_new[2], f64);
+            rho = (lane == 2) ? link_density(c, false, fa, f64, nullptr, nullptr, &bad)
+                              : link_density(c, false, f64, fb, nullptr, nullptr, &bad);
+          } else {
+            rho = link_density(c, false, fa, fb, nullptr, nullptr, &bad);
+          }
         }
-        // the other rotors' potentials at slice q depend on this orientation
-        for (int rr = 0; rr < s.nrotors; rr++)
-          if (rr != r) c.st.rp_ok[rr * Q + q] = 0;
+        sh.rho[lane] = rho;
+        if (bad) atomicOr(&sh.bad, 1);
       }
-    }
-    c.st.rp_cache[i1] = acc ? pot_new : pot_old;
-    c.st.rp_ok[i1] = 1;
-    if (use_links && !sh.bad) {
-      c.st.rl_cache[i0] = acc ? sh.rho[2] : sh.rho[0];
-      c.st.rl_cache[i1] = acc ? sh.rho[3] : sh.rho[1];
-      c.st.rl_ok[i0] = 1;
-      c.st.rl_ok[i1] = 1;
+      __syncwarp();
+      if (lane == 0) {
+        const double *u = sh.u;
+        const double pot_old = sh.pot_old, pot_new = sh.pot_new;
+        double rd;
+        int acc = 0, neg = 0;
+        if (MIX && s.rot_den_type == 0) {
+          // the FP32 path: densities, their ratio and the Boltzmann factor in float
+          float dens_old = (float)sh.rho[0] * (float)sh.rho[1], dens_new = (float)sh.rho[2] * (float)sh.rho[3];
+          if (fabsf(dens_old) < (float)PIMC_RZERO) dens_old = 0.0f;
+          if (fabsf(dens_new) < (float)PIMC_RZERO) dens_new = 0.0f;
+          if (linear) {
+            if (dens_old < 0.0f || dens_new < 0.0f) neg = 1;
+          } else {
+            dens_old = fabsf(dens_old);
+            dens_new = fabsf(dens_new);
+          }
+          float rf = (dens_old > (float)PIMC_RZERO) ? dens_new / dens_old : 1.0f;
+          rf *= expf((float)(-s.tau * (pot_new - pot_old)));
+          rd = (double)rf;
+          acc = (rf > 1.0f) || (rf > (float)u[linear ? 2 : 3]);
+        } else if (s.rot_den_type == 0) {
+          double dens_old = sh.rho[0] * sh.rho[1], dens_new = sh.rho[2] * sh.rho[3];
+          if (fabs(dens_old) < PIMC_RZERO) dens_old = 0.0;
+          if (fabs(dens_new) < PIMC_RZERO) dens_new = 0.0;
+          if (linear) {
+            if (dens_old < 0.0 || dens_new < 0.0) neg = 1;          // mc_piqmc.cc:850,886
+          } else {
+            if (dens_old < 0.0) dens_old = fabs(dens_old);          // mc_piqmc.cc:1067,1133
+            if (dens_new < 0.0) dens_new = fabs(dens_new);
+          }
+          rd = (dens_old > PIMC_RZERO) ? dens_new / dens_old : 1.0;
+          rd *= exp(-s.tau * (pot_new - pot_old));
+          acc = (rd > 1.0) || (rd > u[linear ? 2 : 3]);
+        } else if (linear) {
+          double dens_old = sh.rho[0] + sh.rho[1], dens_new = sh.rho[2] + sh.rho[3];
+          if (fabs(dens_old) < PIMC_RZERO) dens_old = 0.0;
+          if (fabs(dens_new) < PIMC_RZERO) dens_new = 0.0;
+          rd = dens_new - dens_old - s.tau * (pot_new - pot_old);
+          acc = (rd > 0.0) || (rd > log(u[2]));
+        } else {
+          double rhoold = sh.rho[0] + sh.rho[1], rhonew = sh.rho[2] + sh.rho[3];
+          rd = (rhonew - rhoold) / (4.0 * (s.rot_tau / PIMC_WNO2K));
+          rd -= s.tau * (pot_new - pot_old);
+          acc = (rd > 0.0) || (rd > log(u[3]));
+        }
+        if (neg) { atomicOr(c.st.err, (unsigned)DERR_NEG_DENSITY); acc = 0; }
+        if (sh.bad) { atomicOr(c.st.err, (unsigned)DERR_GRID_RANGE); acc = 0; }
+        sh.rd = rd;
+        sh.acc = acc;
+        if (rd_out) *rd_out = rd;
+        if (acc) {
+          c.st.ang[i1] = sh.ang_new[0];
+          c.st.ang[n + i1] = sh.ang_new[1];
+          if (linear) {
+            for (int d = 0; d < 3; d++) {
+              c.st.cosv[d * n + i1] = sh.cv[d];
+              c.st.cosvf[d * n + i1] = (float)sh.cv[d];
+            }
+          } else {
+            c.st.ang[2 * n + i1] = sh.ang_new[2];
+            if (need64) {
+              frames[i1] = sh.fn;
+            } else {
+              for (int k = 0; k < 9; k++) frames[i1].mf[k] = sh.fn.mf[k];
+              frames[i1].hzf = sh.fn.hzf;
+            }
+            // the other rotors' potentials at slice q depend on this orientation
+            for (int rr = 0; rr < s.nrotors; rr++)
+              if (rr != r) c.st.rp_ok[rr * Q + q] = 0;
+          }
+        }
+        c.st.rp_cache[i1] = acc ? pot_new : pot_old;
+        c.st.rp_ok[i1] = 1;
+        if (use_links && !sh.bad) {
+          c.st.rl_cache[i0] = acc ? sh.rho[2] : sh.rho[0];
+          c.st.rl_cache[i1] = acc ? sh.rho[3] : sh.rho[1];
+          c.st.rl_ok[i0] = 1;
+          c.st.rl_ok[i1] = 1;
+        }
+        hooks.published();
+      }
     }
   }
   __syncthreads();
-  int acc = sh.acc;
-  __syncthreads();
-  return acc;
+  return sh.acc;
+}
+
+// the whole move: rot_prepare then rot_finish
+template <bool MIX, bool COH>
+__device__ int rot_step(const Ctx &c, Frame *frames, int g0, int q, const double u[4], const double prop[3],
+                        bool linear, RotShared &sh, double *rd_out)
+{
+  rot_prepare<MIX>(c, frames, g0, q, u, prop, linear, sh);
+  RotNoHooks hk;
+  return rot_finish<MIX, COH>(c, frames, g0, q, linear, sh, rd_out, hk);
 }

@@ -17,6 +17,10 @@ void launch_rot_replay(const Ctx &c, Frame *f, int parity, const double *urot, l
 int launch_rot_phase(const Ctx &c, Frame *f, int parity, unsigned phase, uint64_t seed, const unsigned *pass,
                      unsigned long long *cnt, cudaStream_t s);
 int rot_sweeps_max_ctas(int mixed);
+int rot_slices_max_ctas(int mixed);
+cudaError_t launch_rot_slices(const Ctx &c, Frame *f, int nhalf, unsigned phase0, unsigned group, uint64_t seed,
+                              const unsigned *pass, unsigned long long *prog, unsigned *abort_word,
+                              unsigned long long *cnt, cudaStream_t s);
 cudaError_t launch_rot_sweeps(const Ctx &c, Frame *f, int nctas, int nhalf, unsigned phase0, unsigned group,
                               uint64_t seed, const unsigned *pass, unsigned long long *prog, unsigned *abort_word,
                               unsigned long long *cnt, cudaStream_t s);
