@@ -177,28 +177,41 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def rotation_phase_bytes(w):
-    """Compulsory bytes of one rotational phase launch (Q/2 slice moves):
-    per slice and rotor, 2*R*(N-1) rotor-atom pair evaluations each reading
-    the partner bead (24 B) and 4 table corners (32 B), plus 4 rotational
-    density lookups of 4 corners (32 B) and the 3 neighbouring orientations
-    (3 x 24 B), plus the rotor's R beads (24 B each)."""
+def pair_bytes(mixed):
+    """Compulsory bytes of one pair evaluation: the partner bead and 4 table
+    words (FP64: 24 + 32 B; FP32 path: 12 + 16 B)."""
+    return (12 + 16) if mixed else (24 + 32)
+
+
+def rotation_pass_bytes(w, mixed):
+    """Compulsory bytes of the P rotational sweeps of one pass (2P half-sweeps
+    of Q/2 slice moves): per slice move and rotor, 2*R*(N-1) rotor-atom pair
+    evaluations, 4 rotational density lookups of 4 corners, the 3
+    neighbouring orientations (3 x 24 B) and the rotor's R beads."""
     P, Q = w.nslices, w.nrotslices
     R = P // Q
     na = w.natoms
     nr = sum(t["numb"] for t in w.types if t["molecule"] != 0)
-    per_slice = nr * (2 * R * (na - 1) * (24 + 32) + 4 * 32 + 3 * 24 + R * 24)
-    return (Q // 2) * per_slice
+    corner = 4 if mixed else 8
+    per_slice = nr * (2 * R * (na - 1) * pair_bytes(mixed) + 4 * 4 * corner + 3 * 24 + R * 24)
+    return P * Q * per_slice
 
 
-def bisection_phase_bytes(w, type_):
-    """Compulsory bytes of one bisection phase launch (P/M window moves, all
-    levels executed): each of the 2(M-1) slice energies reads N-1 partner beads
-    (24 B) and 4 spline words (32 B)."""
-    t = w.types[type_]
-    M = 1 << t["levels"]
-    na = w.natoms
-    return (w.nslices // M) * (2 * (M - 1) * (na - 1) * (24 + 32))
+def bisection_pass_bytes(w, mixed):
+    """Compulsory bytes of the bisection blocks of one pass: per type N*P
+    window moves, each with 2(M-1) slice energies over N-1 partners (all
+    levels evaluated)."""
+    tot = 0
+    for t in w.types:
+        M = 1 << t["levels"]
+        tot += t["numb"] * w.nslices * 2 * (M - 1) * (w.natoms - 1) * pair_bytes(mixed)
+    return tot
+
+
+def centroid_pass_bytes(w, mixed):
+    """Each centroid move sums the displaced and the current path of one atom
+    against all partners over all P slices."""
+    return w.natoms * 2 * w.nslices * (w.natoms - 1) * pair_bytes(mixed)
 
 
 def run_gb300(args, rank, local, world, dist):
@@ -246,22 +259,19 @@ def run_gb300(args, rank, local, world, dist):
     ms, nl = s.profile_pass(seed + 7)
     kinds = ["centroid", "bisection", "rotation"]
     dom = int(np.argmax(ms))
-    if dom == 2:
-        bytes_launch = rotation_phase_bytes(w)
-        kname = "k_rot<false> (rotational even/odd phase)"
-    elif dom == 1:
-        bytes_launch = bisection_phase_bytes(w, 0)
-        kname = "k_bisect_phase (bisection independent-set phase)"
-    else:
-        bytes_launch = 2 * w.nslices * (w.natoms - 1) * 56
-        kname = "k_mol_pairs (centroid partner sums)"
+    mixed = args.precision == "mixed"
+    bytes_pass = [centroid_pass_bytes(w, mixed), bisection_pass_bytes(w, mixed), rotation_pass_bytes(w, mixed)]
+    knames = ["k_mol_pairs (centroid partner sums)", "k_bisect_block (bisection block, one CTA per window)",
+              "k_rot_slices (persistent rotational sweeps, one CTA per slice)"]
+    kname = knames[dom]
+    bytes_launch = bytes_pass[dom] / max(1, nl[dom])
     per_launch_ms = ms[dom] / max(1, nl[dom])
     achieved = bytes_launch / (per_launch_ms / 1e3) / 1e9
     peak, peak_kind = measured_peaks()
     roofline = {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 5), "traffic": None,
                 "kernel": kname, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
-                "per_launch_us": round(per_launch_ms * 1e3, 3), "algorithmic_bytes_per_launch": bytes_launch,
+                "per_launch_us": round(per_launch_ms * 1e3, 3), "algorithmic_bytes_per_launch": int(bytes_launch),
                 "pass_ms_by_kind": {k: round(v, 3) for k, v in zip(kinds, ms)},
                 "launches_by_kind": {k: int(v) for k, v in zip(kinds, nl)}}
 

@@ -109,13 +109,24 @@ __device__ __forceinline__ void slot_sums(int nslots, int na, const int *skip, F
   const int total = nslots * npart;
   // chunks of whole slots when a slot fits the buffer, else of PIMC_RED_BUF items
   const int chunk = (npart <= PIMC_RED_BUF) ? (PIMC_RED_BUF / npart) * npart : PIMC_RED_BUF;
+  const int nt = blockDim.x;
   for (int base = 0; base < total; base += chunk) {
     int cnt = min(chunk, total - base);
-    for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
+    // two items per step so that their loads overlap
+    for (int i = threadIdx.x; i < cnt; i += 2 * nt) {
       int g = base + i;
       int s = g / npart, pi = g - s * npart;
       int p = pi < skip[s] ? pi : pi + 1;
-      buf[i] = f(s, p);
+      int i2 = i + nt;
+      double v0 = f(s, p), v1 = 0.0;
+      if (i2 < cnt) {
+        int g2 = base + i2;
+        int s2 = g2 / npart, pi2 = g2 - s2 * npart;
+        int p2 = pi2 < skip[s2] ? pi2 : pi2 + 1;
+        v1 = f(s2, p2);
+        buf[i2] = v1;
+      }
+      buf[i] = v0;
     }
     __syncthreads();
     int sfirst = base / npart, slast = (base + cnt - 1) / npart;
@@ -233,17 +244,25 @@ struct BisectShared {
   double gz[3 * PIMC_MAX_SEG];        // all Gaussian draws of the move, level by level
   double ua[8];                       // accept uniforms per level (counter-based source)
   double ob[3][PIMC_MAX_SEG + 1];     // the current beads of the window
-  double nb[3][PIMC_MAX_SEG + 1];
-  double en[PIMC_MAX_SEG + 1], eo[PIMC_MAX_SEG + 1];
-  double sx[PIMC_MAX_SEG], sy[PIMC_MAX_SEG], sz[PIMC_MAX_SEG], se[PIMC_MAX_SEG];
-  int sa[PIMC_MAX_SEG], st[PIMC_MAX_SEG];
+  double nb[3][PIMC_MAX_SEG + 1];     // the proposed beads
+  double se[2 * PIMC_MAX_SEG];        // slice energies: (bead k, new) at 2(k-1), (bead k, old) at 2(k-1)+1
+  int sa[2 * PIMC_MAX_SEG];           // owner of the slot's bead (the partner sums skip it)
   int owner[PIMC_MAX_SEG + 1], slice[PIMC_MAX_SEG + 1];
-  double pot0, pot1;
   int acc, passed;
   long gbase;
   double buf[PIMC_RED_BUF];
 };
 
+// The proposal of all levels is fixed by the Gaussian draws alone (a
+// level's midpoints are built from the previous level's new beads whether
+// or not it is then accepted), and a bead's slice energy does not change
+// once it is placed.  So all 2(M-1) slice energies are summed in one pass
+// over (slot, partner) items, and the level-by-level accept of the
+// reference (mc_piqmc.cc:243-281) then runs on thread 0 from those sums:
+// level l's pot0 is the new-minus-old energy of the beads at multiples of
+// 2^(L-l-1) (mc_piqmc.cc:256-263), its action difference
+// (pot0 - 2 pot1) tau 2^(L-l-1) (mc_piqmc.cc:265-266).  Only the levels the
+// reference reaches consume their draws.
 template <bool MIX, class Src>
 __device__ int bisect_move(const Ctx &c, const Frame *frames, int type, int atom, int time0, int exch, Src &src,
                            BisectShared &sh, double *ds_out)
@@ -267,7 +286,7 @@ __device__ int bisect_move(const Ctx &c, const Frame *frames, int type, int atom
     sh.nb[0][k] = x; sh.nb[1][k] = y; sh.nb[2][k] = z;
     sh.ob[0][k] = x; sh.ob[1][k] = y; sh.ob[2][k] = z;
   }
-  if (tid == 0) { sh.pot0 = 0.0; sh.pot1 = 0.0; sh.acc = 0; sh.passed = 0; sh.gbase = src.gauss_base(); }
+  if (tid == 0) { sh.acc = 0; sh.passed = 0; sh.gbase = src.gauss_base(); }
   __syncthreads();
   // the move's Gaussian draws, all levels at once: level l's midpoint j,
   // dimension d is draw 3(2^l - 1) + 3j + d (the reference's order)
@@ -280,12 +299,11 @@ __device__ int bisect_move(const Ctx &c, const Frame *frames, int type, int atom
   if (Src::kPrefetchU)
     for (int l = tid - 64; l >= 0 && l < L; l += blockDim.x) sh.ua[l] = src.accept_u(l);
   __syncthreads();
-  double bnorm = 1.0 / (s.lambda[type] * s.tau);
+  // the proposed beads, level by level (mc_piqmc.cc:243-254)
   for (int level = 0; level < L; level++) {
     int seg = 1 << (L - level), half = seg >> 1, nmid = M / seg;
-    double sq = sqrt(bnorm / (double)seg);            // sqrt of gauss()'s alpha (mc_randg.cc:149)
+    double sq = s.bis_sq[type][level];
     const double *gz = sh.gz + 3 * (nmid - 1);
-    // midpoint j and its (new, old) slots by thread j
     for (int j = tid; j < nmid; j += blockDim.x) {
       int k0 = j * seg, k1 = k0 + half, k2 = k0 + seg;
       for (int d = 0; d < 3; d++) {
@@ -293,50 +311,54 @@ __device__ int bisect_move(const Ctx &c, const Frame *frames, int type, int atom
         v += gz[3 * j + d] / sq;
         sh.nb[d][k1] = v;
       }
-      int own = sh.owner[k1], pt = sh.slice[k1];
-      sh.sa[2 * j] = own; sh.st[2 * j] = pt;
-      sh.sx[2 * j] = sh.nb[0][k1]; sh.sy[2 * j] = sh.nb[1][k1]; sh.sz[2 * j] = sh.nb[2][k1];
-      sh.sa[2 * j + 1] = own; sh.st[2 * j + 1] = pt;
-      sh.sx[2 * j + 1] = sh.ob[0][k1]; sh.sy[2 * j + 1] = sh.ob[1][k1]; sh.sz[2 * j + 1] = sh.ob[2][k1];
+      sh.sa[2 * (k1 - 1)] = sh.owner[k1];
+      sh.sa[2 * (k1 - 1) + 1] = sh.owner[k1];
     }
-    if (tid == 0) { sh.gbase += 3 * nmid; src.gauss_advance(3 * nmid); }
     __syncthreads();
-    if (MIX)
-      slot_sums(2 * nmid, s.na, sh.sa,
-                [&](int sl, int p) -> double {
-                  return (double)pair_term32(c, frames, sh.sa[sl], p, sh.st[sl], (float)sh.sx[sl], (float)sh.sy[sl],
-                                             (float)sh.sz[sl]);
-                },
-                sh.se, sh.buf);
-    else
-      slot_sums(2 * nmid, s.na, sh.sa,
-                [&](int sl, int p) -> double {
-                  return pair_term64(c, frames, sh.sa[sl], p, sh.st[sl], sh.sx[sl], sh.sy[sl], sh.sz[sl]);
-                },
-                sh.se, sh.buf);
-    if (tid == 0) {
-      sh.pot1 = sh.pot0;
+  }
+  // slice energies of every interior bead, new and old
+  if (MIX)
+    slot_sums(2 * (M - 1), s.na, sh.sa,
+              [&](int sl, int p) -> double {
+                int k = (sl >> 1) + 1;
+                const double(*b)[PIMC_MAX_SEG + 1] = (sl & 1) ? sh.ob : sh.nb;
+                return (double)pair_term32(c, frames, sh.owner[k], p, sh.slice[k], (float)b[0][k], (float)b[1][k],
+                                           (float)b[2][k]);
+              },
+              sh.se, sh.buf);
+  else
+    slot_sums(2 * (M - 1), s.na, sh.sa,
+              [&](int sl, int p) -> double {
+                int k = (sl >> 1) + 1;
+                const double(*b)[PIMC_MAX_SEG + 1] = (sl & 1) ? sh.ob : sh.nb;
+                return pair_term64(c, frames, sh.owner[k], p, sh.slice[k], b[0][k], b[1][k], b[2][k]);
+              },
+              sh.se, sh.buf);
+  if (tid == 0) {
+    double pot1 = 0.0;
+    int a = 0;
+    for (int level = 0; level < L; level++) {
+      int seg = 1 << (L - level), half = seg >> 1, nmid = M / seg;
+      src.gauss_advance(3 * nmid);
       double pot0 = 0.0;
       for (int j = 0; j < nmid; j++) {
         int k0 = j * seg, k1 = k0 + half;
-        sh.en[k1] = sh.se[2 * j];
-        sh.eo[k1] = sh.se[2 * j + 1];
-        pot0 += (sh.en[k1] - sh.eo[k1]);
-        if (k0 != 0) pot0 += (sh.en[k0] - sh.eo[k0]);
+        pot0 += (sh.se[2 * (k1 - 1)] - sh.se[2 * (k1 - 1) + 1]);
+        if (k0 != 0) pot0 += (sh.se[2 * (k0 - 1)] - sh.se[2 * (k0 - 1) + 1]);
       }
-      sh.pot0 = pot0;
-      double deltav = (pot0 - 2.0 * sh.pot1);
+      double deltav = (pot0 - 2.0 * pot1);
       deltav *= s.tau * (double)(seg / 2);
       if (ds_out) ds_out[level] = deltav;
-      int a = 0;
+      a = 0;
       if (deltav < 0.0) a = 1;
       else if (exp(-deltav) > (Src::kPrefetchU ? sh.ua[level] : src.accept_u(level))) a = 1;
-      sh.acc = a;
-      if (a) sh.passed = level + 1;
+      if (!a) break;
+      sh.passed = level + 1;
+      pot1 = pot0;
     }
-    __syncthreads();
-    if (!sh.acc) break;
+    sh.acc = a;
   }
+  __syncthreads();
   int accepted = sh.acc;
   if (accepted) {
     for (int k = 1 + tid; k < M; k += blockDim.x) {
