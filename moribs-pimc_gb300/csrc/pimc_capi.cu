@@ -103,6 +103,17 @@ static pimc_status upload_f32(pimc_handle *h, const double *src, size_t n, const
   return PIMC_OK;
 }
 
+static pimc_status upload_f4(pimc_handle *h, const std::vector<float4> &v, const float4 **dst)
+{
+  float4 *d = nullptr;
+  pimc_status st = dalloc(h, &d, v.size());
+  if (st) return st;
+  h->owned.push_back(d);
+  CK(cudaMemcpy(d, v.data(), v.size() * sizeof(float4), cudaMemcpyHostToDevice));
+  *dst = d;
+  return PIMC_OK;
+}
+
 static pimc_status scratch(pimc_handle *h, size_t bytes, void **p)
 {
   if (bytes > h->qbytes) {
@@ -249,7 +260,7 @@ extern "C" pimc_status pimc_create(const pimc_system *sys, int device, pimc_hand
   size_t nr = (size_t)(d.nrotors > 0 ? d.nrotors : 1) * d.Q;
   pimc_status e;
   if ((e = dalloc(h, &st.x, nb)) || (e = dalloc(h, &st.y, nb)) || (e = dalloc(h, &st.z, nb)) ||
-      (e = dalloc(h, &st.xf, nb)) || (e = dalloc(h, &st.yf, nb)) || (e = dalloc(h, &st.zf, nb)) ||
+      (e = dalloc(h, &st.b4, nb)) ||
       (e = dalloc(h, &st.cosvf, 3 * nr)) || (e = dalloc(h, &st.rp_cache, nr)) || (e = dalloc(h, &st.rl_cache, nr)) ||
       (e = dalloc(h, &st.rp_ok, nr)) || (e = dalloc(h, &st.rl_ok, nr)) ||
       (e = dalloc(h, &st.ang, 3 * nr)) || (e = dalloc(h, &st.cosv, 3 * nr)) || (e = dalloc(h, &st.pindex, na)) ||
@@ -265,9 +276,7 @@ extern "C" pimc_status pimc_create(const pimc_system *sys, int device, pimc_hand
   CK(cudaMemset(st.x, 0, nb * sizeof(double)));
   CK(cudaMemset(st.y, 0, nb * sizeof(double)));
   CK(cudaMemset(st.z, 0, nb * sizeof(double)));
-  CK(cudaMemset(st.xf, 0, nb * sizeof(float)));
-  CK(cudaMemset(st.yf, 0, nb * sizeof(float)));
-  CK(cudaMemset(st.zf, 0, nb * sizeof(float)));
+  CK(cudaMemset(st.b4, 0, nb * sizeof(float4)));
   CK(cudaMemset(st.rp_ok, 0, nr * sizeof(int)));
   CK(cudaMemset(st.rl_ok, 0, nr * sizeof(int)));
   CK(cudaMemset(st.err, 0, sizeof(unsigned)));
@@ -297,7 +306,7 @@ extern "C" pimc_status pimc_destroy(pimc_handle *h)
   if (h->stream) cudaStreamSynchronize(h->stream);
   if (h->pass_exec) cudaGraphExecDestroy(h->pass_exec);
   DevState &st = h->ctx.st;
-  void *bufs[] = {st.x, st.y, st.z, st.xf, st.yf, st.zf, st.cosvf, st.rp_cache, st.rl_cache, st.rp_ok, st.rl_ok,
+  void *bufs[] = {st.x, st.y, st.z, st.b4, st.cosvf, st.rp_cache, st.rl_cache, st.rp_ok, st.rl_ok,
                   st.ang, st.cosv, st.pindex, st.mctype, st.err, h->frames, h->cnt, h->pass, h->cursors, h->ms,
                   h->qbuf, h->prog, h->abort_word};
   for (void *b : bufs)
@@ -339,6 +348,16 @@ extern "C" pimc_status pimc_load_tables(pimc_handle *h, const pimc_tables *tb)
         (e = upload_f32(h, tb->pot1d, n, &t.p1d32)) || (e = upload_f32(h, y2.data(), n, &t.y21d32)))
       return e;
     t.uni1d = near_uniform(tb->grid1d, n, &t.x01d, &t.ih1d) ? 1 : 0;
+    if (t.uni1d) {
+      // FP32 path: the spline words of interval k in one 16-byte word
+      std::vector<float4> w(n - 1);
+      for (int k = 0; k < n - 1; k++)
+        w[k] = make_float4((float)tb->pot1d[k], (float)y2[k], (float)tb->pot1d[k + 1], (float)y2[k + 1]);
+      if ((e = upload_f4(h, w, &t.sp1d4))) return e;
+      double hstep = 1.0 / t.ih1d;
+      t.f_h1d = (float)hstep;
+      t.f_h2_6 = (float)(hstep * hstep / 6.0);
+    }
     // short- and long-range extrapolation constants (mc_poten.cc:418-437)
     double fr = tb->pot1d[0] / tb->pot1d[1];
     double dr = tb->grid1d[1] - tb->grid1d[0];
@@ -357,6 +376,17 @@ extern "C" pimc_status pimc_load_tables(pimc_handle *h, const pimc_tables *tb)
         (e = upload_f32(h, tb->rgrid2d, tb->nr2d, &t.rg2d32)) || (e = upload_f32(h, tb->cgrid2d, tb->nc2d, &t.cg2d32)) ||
         (e = upload_f32(h, tb->pot2d, (size_t)tb->nr2d * tb->nc2d, &t.pot2d32)))
       return e;
+    // FP32 path: the four corners of each cell in one 16-byte word
+    int nr = tb->nr2d, nc = tb->nc2d;
+    std::vector<float4> w((size_t)(nr - 1) * (nc - 1));
+    for (int ir = 0; ir < nr - 1; ir++)
+      for (int ic = 0; ic < nc - 1; ic++) {
+        const double *q = tb->pot2d + (size_t)ir * nc + ic;
+        w[(size_t)ir * (nc - 1) + ic] = make_float4((float)q[0], (float)q[nc], (float)q[nc + 1], (float)q[1]);
+      }
+    if ((e = upload_f4(h, w, &t.pot2d4))) return e;
+    t.f_rmin2d = (float)tb->rgrid2d[0];
+    t.f_cmin2d = (float)tb->cgrid2d[0];
   }
   if (need3d) {
     if (tb->rgrd < 2 || tb->thgrd < 2 || tb->chgrd < 2 || !tb->vtable || tb->rvmax <= tb->rvmin) return PIMC_ERR_BAD_TABLE;
@@ -371,6 +401,24 @@ extern "C" pimc_status pimc_load_tables(pimc_handle *h, const pimc_tables *tb)
     t.dch3 = (double)fold / (double)(t.chgrd - 1);
     size_t n = (size_t)t.rgrd * t.thgrd * t.chgrd;
     if ((e = upload(h, tb->vtable, n, &t.vtab)) || (e = upload_f32(h, tb->vtable, n, &t.vtab32))) return e;
+    // FP32 path: each point's value and vcalc's one-sided differences
+    // (vcalc.f:40-60) in one 16-byte word
+    {
+      size_t nth = t.thgrd, nch = t.chgrd;
+      std::vector<float4> w(n);
+      for (int ir = 0; ir < t.rgrd; ir++)
+        for (int it = 0; it < t.thgrd; it++)
+          for (int ic = 0; ic < t.chgrd; ic++) {
+            size_t i0 = ((size_t)ir * nth + it) * nch + ic;
+            double v0 = tb->vtable[i0];
+            double dr = ir < t.rgrd - 1 ? tb->vtable[i0 + nth * nch] - v0 : 0.0;
+            double dt = it < t.thgrd - 1 ? tb->vtable[i0 + nch] - v0 : 0.0;
+            double dc = ic < t.chgrd - 1 ? tb->vtable[i0 + 1] - v0 : 0.0;
+            w[i0] = make_float4((float)v0, (float)dr, (float)dt, (float)dc);
+          }
+      if ((e = upload_f4(h, w, &t.vtab4))) return e;
+      t.f_irstep = (float)(1.0 / t.rvstep);
+    }
   }
   if (d.ispher && d.ntypes > 1) {
     if (tb->nsph < 2 || !tb->sph_table || tb->sph_rstep <= 0) return PIMC_ERR_BAD_TABLE;
@@ -404,6 +452,21 @@ extern "C" pimc_status pimc_load_tables(pimc_handle *h, const pimc_tables *tb)
       if ((e = upload(h, tb->rhoprp, n, &t.rho)) || (e = upload(h, tb->erotpr, n, &t.erot)) ||
           (e = upload(h, tb->erotsq, n, &t.esq)) || (e = upload_f32(h, tb->rhoprp, n, &t.rho32)))
         return e;
+      // FP32 path: value and rotpro's one-sided differences along chi, phi,
+      // theta (rotpro_sub.f:30-60) in one 16-byte word
+      size_t nph = t.nph, nch = t.nch;
+      std::vector<float4> w(n);
+      for (int it = 0; it < t.nth; it++)
+        for (int ip = 0; ip < t.nph; ip++)
+          for (int ic = 0; ic < t.nch; ic++) {
+            size_t i0 = ((size_t)it * nph + ip) * nch + ic;
+            double r0 = tb->rhoprp[i0];
+            double dc = ic < t.nch - 1 ? tb->rhoprp[i0 + 1] - r0 : 0.0;
+            double dp = ip < t.nph - 1 ? tb->rhoprp[i0 + nch] - r0 : 0.0;
+            double dt = it < t.nth - 1 ? tb->rhoprp[i0 + nph * nch] - r0 : 0.0;
+            w[i0] = make_float4((float)r0, (float)dc, (float)dp, (float)dt);
+          }
+      if ((e = upload_f4(h, w, &t.rho4))) return e;
     }
   }
   // float constants of the FP32 leaves

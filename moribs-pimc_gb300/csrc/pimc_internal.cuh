@@ -56,6 +56,14 @@ struct DevTables {
   float f_x01d, f_ih1d, f_c61d, f_unode1d, f_alpha1d, f_dr2d, f_dc2d;
   float f_thscale, f_chscale, f_rvmin, f_rvmax, f_rvstep;     // vcord32: degrees per grid step folded in
   float f_dscale[3];                                            // rotden32: theta, phi, chi grid steps per radian
+  // packed float tables of the FP32 path: one 16-byte load per evaluation
+  const float4 *sp1d4;          // 1D spline interval k: (y_k, y2_k, y_k+1, y2_k+1); uniform grids only
+  float f_h1d, f_h2_6;          // step and step^2 / 6
+  const float4 *pot2d4;         // 2D cell (ir, ic): corners (ir,ic), (ir+1,ic), (ir+1,ic+1), (ir,ic+1)
+  float f_rmin2d, f_cmin2d;
+  const float4 *vtab4;          // 3D point: value and its one-sided differences along r, theta, chi
+  float f_irstep;
+  const float4 *rho4;           // top density point: value and differences along chi, phi, theta
 };
 
 struct DevSys {
@@ -78,7 +86,7 @@ struct DevSys {
 //   partner sweep at one slice is a unit-stride read);
 //   ang[k*nrotors*Q + r*Q + q], k = {phi, cos theta, chi}: rotor r at rotational slice q;
 //   cosv[k*nrotors*Q + r*Q + q]: its unit vector (MCCosine).
-//   xf/yf/zf: float copies of the beads read by the FP32 table path;
+//   b4: float copies of the beads, one 16-byte word each, read by the FP32 path;
 //   rp_cache/rp_ok[r*Q + q]: the rotor's potential summed over the R
 //   translational slices of rotational slice q with its current orientation,
 //   valid while no bead of those slices and no orientation at q has changed;
@@ -86,7 +94,7 @@ struct DevSys {
 //   Both caches hold exactly the value a fresh evaluation would return.
 struct DevState {
   double *x, *y, *z;
-  float *xf, *yf, *zf;
+  float4 *b4;                   // float copy of the beads (x, y, z, 0) for the FP32 path
   double *ang, *cosv;
   float *cosvf;
   int *pindex;
@@ -500,22 +508,28 @@ __device__ __forceinline__ float spot1d32(const DevTables &t, float r)
     return -t.f_c61d / (r2 * r2 * r2);
   }
   if (r <= __ldg(t.g1d32)) return t.f_unode1d * expf(-t.f_alpha1d * r);
+  if (t.sp1d4) {
+    // uniform grid: the interval from the index formula, its four spline
+    // words in one load, the node positions from the grid formula
+    float g = (r - t.f_x01d) * t.f_ih1d;
+    int k = min(max((int)g, 0), t.n1d - 2);
+    float4 w = __ldg(t.sp1d4 + k);
+    float b = g - (float)k, a = 1.0f - b;
+    return a * w.x + b * w.z + ((a * a * a - a) * w.y + (b * b * b - b) * w.w) * t.f_h2_6;
+  }
   return splint32(t.g1d32, t.p1d32, t.y21d32, t.n1d, r, t.uni1d, t.f_x01d, t.f_ih1d);
 }
 
 __device__ __forceinline__ float lpot2d32(const DevTables &t, float r, float cost)
 {
-  float rmin = __ldg(t.rg2d32), cmin = __ldg(t.cg2d32);
-  int ir = (int)floorf((r - rmin) / t.f_dr2d);
-  int ic = (int)floorf((cost - cmin) / t.f_dc2d);
-  ir = min(max(ir, 0), t.nr2d - 2);
-  ic = min(max(ic, 0), t.nc2d - 2);
-  const float *p = t.pot2d32 + (size_t)ir * t.nc2d + ic;
-  float y1 = __ldg(p), y4 = __ldg(p + 1), y2 = __ldg(p + t.nc2d), y3 = __ldg(p + t.nc2d + 1);
-  float r1 = __ldg(t.rg2d32 + ir), r2 = __ldg(t.rg2d32 + ir + 1);
-  float c1 = __ldg(t.cg2d32 + ic), c2 = __ldg(t.cg2d32 + ic + 1);
-  float dr = (r - r1) / (r2 - r1), dc = (cost - c1) / (c2 - c1);
-  return (1.0f - dr) * (1.0f - dc) * y1 + dr * (1.0f - dc) * y2 + dr * dc * y3 + (1.0f - dr) * dc * y4;
+  // LPot2D's cell from its index formula on the uniform grid, the four
+  // corners in one load
+  float gr = (r - t.f_rmin2d) / t.f_dr2d, gc = (cost - t.f_cmin2d) / t.f_dc2d;
+  int ir = min(max((int)floorf(gr), 0), t.nr2d - 2);
+  int ic = min(max((int)floorf(gc), 0), t.nc2d - 2);
+  float4 y = __ldg(t.pot2d4 + (size_t)ir * (t.nc2d - 1) + ic);
+  float dr = gr - (float)ir, dc = gc - (float)ic;
+  return (1.0f - dr) * (1.0f - dc) * y.x + dr * (1.0f - dc) * y.y + dr * dc * y.z + (1.0f - dr) * dc * y.w;
 }
 
 // vcord + vcalc in float: R = atom - rotor centre in the space frame
@@ -540,19 +554,16 @@ __device__ __forceinline__ float vcord32(const DevTables &t, const Frame &f, flo
   float r = rn * 1.88972614f;          // 1 / 0.529177249 (bohr per angstrom)
   float xth = thewff * t.f_thscale;
   float xch = chiwff * t.f_chscale;
-  float rvmin = t.f_rvmin, rvmax = t.f_rvmax, rstep = t.f_rvstep;
+  float rvmin = t.f_rvmin, rvmax = t.f_rvmax;
   r = fminf(fmaxf(r, rvmin), rvmax);
   int maxrpt = t.rgrd - 1, mxthpt = t.thgrd - 1, mxchpt = t.chgrd - 1;
-  int ir = min((int)((r - rvmin) / rstep), maxrpt);
+  float gr = (r - rvmin) * t.f_irstep;
+  int ir = min((int)gr, maxrpt);
   int ith = min(max((int)xth, 0), mxthpt), ich = min(max((int)xch, 0), mxchpt);
   size_t nth = t.thgrd, nch = t.chgrd;
-  size_t i0 = ((size_t)ir * nth + ith) * nch + ich;
-  float v0 = __ldg(t.vtab32 + i0);
-  float v = v0;
-  if (ir < maxrpt) v += (__ldg(t.vtab32 + i0 + nth * nch) - v0) / rstep * (r - (rvmin + ir * rstep));
-  if (ith < mxthpt) v += (__ldg(t.vtab32 + i0 + nch) - v0) * (xth - (float)ith);
-  if (ich < mxchpt) v += (__ldg(t.vtab32 + i0 + 1) - v0) * (xch - (float)ich);
-  return v;
+  // value and the one-sided differences of vcalc (zero at the last node)
+  float4 w = __ldg(t.vtab4 + ((size_t)ir * nth + ith) * nch + ich);
+  return w.x + w.y * (gr - (float)ir) + w.z * (xth - (float)ith) + w.w * (xch - (float)ich);
 }
 
 // rotden's rho on the FP32 path: relative rotation m1^T m2 as deleul
@@ -585,12 +596,8 @@ __device__ __forceinline__ float rotden_rho32(const DevTables &t, const float *m
   if (iphi > t.nph - 1 || iphi < 0) { iphi = 0; *bad = 1; }
   if (ith > t.nth - 1 || ith < 0) { ith = 0; *bad = 1; }
   size_t nph = t.nph, nch = t.nch;
-  size_t i0 = ((size_t)ith * nph + iphi) * nch + ichi;
-  float r0 = __ldg(t.rho32 + i0), rho = r0;
-  if (ichi < t.nch - 1) rho += (__ldg(t.rho32 + i0 + 1) - r0) * (xc - (float)ichi);
-  if (iphi < t.nph - 1) rho += (__ldg(t.rho32 + i0 + nch) - r0) * (xp - (float)iphi);
-  if (ith < t.nth - 1) rho += (__ldg(t.rho32 + i0 + nph * nch) - r0) * (xt - (float)ith);
-  return rho;
+  float4 w = __ldg(t.rho4 + ((size_t)ith * nph + iphi) * nch + ichi);
+  return w.x + w.y * (xc - (float)ichi) + w.z * (xp - (float)iphi) + w.w * (xt - (float)ith);
 }
 
 // caleng (caleng_tip4p_gg.f:2-186).  kcal2k is an INTEGER parameter in the

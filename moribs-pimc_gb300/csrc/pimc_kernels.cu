@@ -15,9 +15,7 @@ __global__ void k_derive_state(Ctx c, Frame *frames)
   size_t n = (size_t)c.s.nrotors * c.s.Q;
   size_t stride = (size_t)gridDim.x * blockDim.x;
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < nb; i += stride) {
-    c.st.xf[i] = (float)c.st.x[i];
-    c.st.yf[i] = (float)c.st.y[i];
-    c.st.zf[i] = (float)c.st.z[i];
+    c.st.b4[i] = make_float4((float)c.st.x[i], (float)c.st.y[i], (float)c.st.z[i], 0.0f);
   }
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
     make_frame(c.st.ang[i], c.st.ang[n + i], c.st.ang[2 * n + i], frames[i]);
@@ -338,8 +336,8 @@ __global__ void __launch_bounds__(PIMC_BLOCK) k_mol_pairs(Ctx c, Frame *frames, 
     for (int it = tid; it < c.s.P; it += blockDim.x) {
       size_t i = sidx(c.s, it, gatom);
       if (MIX) {
-        float x = c.st.xf[i], y = c.st.yf[i], z = c.st.zf[i];
-        ao += (double)pair_term32(c, frames, gatom, a1, it, x, y, z);
+        const float4 p4 = c.st.b4[i];
+        ao += (double)pair_term32(c, frames, gatom, a1, it, p4.x, p4.y, p4.z);
         an += (double)pair_term32(c, frames, gatom, a1, it, (float)(c.st.x[i] + d0), (float)(c.st.y[i] + d1),
                                   (float)(c.st.z[i] + d2));
       } else {

@@ -16,14 +16,16 @@ __device__ __forceinline__ size_t sidx(const DevSys &s, int t, int a) { return (
 
 __device__ __forceinline__ int rot_index(const DevSys &s, int gatom, int q) { return (gatom - s.rot_first) * s.Q + q; }
 
+// MCType of a global atom: types occupy consecutive ranges (mc_setup.cc:327-333)
+__device__ __forceinline__ int atom_type(const DevSys &s, int a) { return (s.ntypes > 1 && a >= s.first[1]) ? 1 : 0; }
+
 // one term of PotEnergy(atom0, pos, it) (mc_piqmc.cc:1824-1958): atom0 at
 // (px,py,pz), partner atom1 at its current bead, rotor frames from the cache
 __device__ __forceinline__ double pair_term64(const Ctx &c, const Frame *__restrict__ frames, int a0, int a1, int it,
                                               double px, double py, double pz)
 {
   const DevSys &s = c.s;
-  int ty0 = c.st.mctype[a0], ty1 = c.st.mctype[a1];
-  int m0 = s.molecule[ty0], m1 = s.molecule[ty1];
+  int m0 = s.molecule[atom_type(s, a0)], m1 = s.molecule[atom_type(s, a1)];
   size_t i1 = sidx(s, it, a1);
   double qx = c.st.x[i1], qy = c.st.y[i1], qz = c.st.z[i1];
   double dx = px - qx, dy = py - qy, dz = pz - qz;
@@ -63,10 +65,10 @@ __device__ __forceinline__ float pair_term32(const Ctx &c, const Frame *__restri
                                              float px, float py, float pz)
 {
   const DevSys &s = c.s;
-  int ty0 = c.st.mctype[a0], ty1 = c.st.mctype[a1];
-  int m0 = s.molecule[ty0], m1 = s.molecule[ty1];
+  int m0 = s.molecule[atom_type(s, a0)], m1 = s.molecule[atom_type(s, a1)];
   size_t i1 = sidx(s, it, a1);
-  float qx = c.st.xf[i1], qy = c.st.yf[i1], qz = c.st.zf[i1];
+  const float4 q4 = c.st.b4[i1];
+  float qx = q4.x, qy = q4.y, qz = q4.z;
   float dx = px - qx, dy = py - qy, dz = pz - qz;
   if (s.minimage) {
     dx -= (float)s.box[0] * rintf(dx / (float)s.box[0]);
@@ -229,9 +231,7 @@ __device__ __forceinline__ void store_bead(const Ctx &c, size_t i, double x, dou
   c.st.x[i] = x;
   c.st.y[i] = y;
   c.st.z[i] = z;
-  c.st.xf[i] = (float)x;
-  c.st.yf[i] = (float)y;
-  c.st.zf[i] = (float)z;
+  c.st.b4[i] = make_float4((float)x, (float)y, (float)z, 0.0f);
 }
 
 // ------------------------------------------------------ bisection move
@@ -482,7 +482,7 @@ __device__ __forceinline__ double rot3d_term64(const Ctx &c, const Frame *frames
 {
   const DevSys &s = c.s;
   size_t i0 = sidx(s, it, g0), i1 = sidx(s, it, a1);
-  if (c.st.mctype[a1] != s.imtype)
+  if (atom_type(s, a1) != s.imtype)
     return vcord(c.t, f, c.st.x[i0], c.st.y[i0], c.st.z[i0], c.st.x[i1], c.st.y[i1], c.st.z[i1]);
   return caleng(f, frames[rot_index(s, a1, it / s.R)], c.st.x[i0], c.st.y[i0], c.st.z[i0], c.st.x[i1], c.st.y[i1],
                 c.st.z[i1]);
@@ -492,8 +492,10 @@ __device__ __forceinline__ float rot3d_term32(const Ctx &c, const Frame *frames,
 {
   const DevSys &s = c.s;
   size_t i0 = sidx(s, it, g0), i1 = sidx(s, it, a1);
-  if (c.st.mctype[a1] != s.imtype)
-    return vcord32(c.t, f, c.st.xf[i1] - c.st.xf[i0], c.st.yf[i1] - c.st.yf[i0], c.st.zf[i1] - c.st.zf[i0]);
+  if (atom_type(s, a1) != s.imtype) {
+    const float4 p0 = c.st.b4[i0], p1 = c.st.b4[i1];
+    return vcord32(c.t, f, p1.x - p0.x, p1.y - p0.y, p1.z - p0.z);
+  }
   return (float)caleng(f, frames[rot_index(s, a1, it / s.R)], c.st.x[i0], c.st.y[i0], c.st.z[i0], c.st.x[i1],
                        c.st.y[i1], c.st.z[i1]);
 }
@@ -523,7 +525,8 @@ __device__ __forceinline__ float rotlin_term32(const Ctx &c, const float n[3], i
 {
   const DevSys &s = c.s;
   size_t i0 = sidx(s, it, g0), i1 = sidx(s, it, a1);
-  float dx = c.st.xf[i0] - c.st.xf[i1], dy = c.st.yf[i0] - c.st.yf[i1], dz = c.st.zf[i0] - c.st.zf[i1];
+  const float4 p0 = c.st.b4[i0], p1 = c.st.b4[i1];
+  float dx = p0.x - p1.x, dy = p0.y - p1.y, dz = p0.z - p1.z;
   float r = sqrtf(dx * dx + dy * dy + dz * dz);
   float cost = -(n[0] * dx + n[1] * dy + n[2] * dz) / r;
   return lpot2d32(c.t, r, cost);
