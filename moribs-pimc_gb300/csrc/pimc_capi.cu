@@ -242,7 +242,10 @@ extern "C" pimc_status pimc_create(const pimc_system *sys, int device, pimc_hand
   d.tau = d.beta / (double)s.nslices;
   for (int t = 0; t < s.ntypes; t++) {
     double bnorm = 1.0 / (d.lambda[t] * d.tau);
-    for (int l = 0; l < d.levels[t]; l++) d.bis_sq[t][l] = sqrt(bnorm / (double)(1 << (d.levels[t] - l)));
+    for (int l = 0; l < d.levels[t]; l++) {
+      d.bis_sq[t][l] = sqrt(bnorm / (double)(1 << (d.levels[t] - l)));
+      d.bis_isq[t][l] = 1.0 / d.bis_sq[t][l];
+    }
   }
   d.rot_tau = Q > 0 ? d.beta / (double)Q : 0.0;
   d.temperature = s.temperature;

@@ -123,41 +123,56 @@ __device__ __forceinline__ unsigned long long global_ns()
   return t;
 }
 
-// waits and progress of a one-slice-per-CTA persistent launch (warp 8, lane 0)
+// waits, progress and look-ahead of a one-slice-per-CTA persistent launch
 struct RotSliceHooks {
   const unsigned long long *wl, *wr;    // progress words of the neighbouring slices
   unsigned long long *mine;
   unsigned long long id;
   unsigned *abort_word, *err;
-  int h;
-  __device__ bool wait()
+  const DevSys *sys;
+  uint64_t seed;
+  unsigned pass, phase_next;
+  int h, pair, linear, has_next;
+  // all lanes of the finishing warp: lane 0 polls until both neighbours have
+  // finished half-sweep h-1, then every lane acquires the two progress words
+  // itself, so that its own loads of the neighbours' state come after them
+  __device__ bool wait(int lane)
   {
-    if (*(volatile unsigned *)abort_word) {
-      atomicOr(err, (unsigned)DERR_TIMEOUT);
-      return false;
-    }
-    if (h == 0) return true;
-    const unsigned long long t0 = global_ns();
-    for (int side = 0; side < 2; side++) {
-      const unsigned long long *w = side ? wr : wl;
-      for (;;) {
-        unsigned long long v = ld_acquire_u64(w);
-        if ((v >> 24) == id && (long long)(v & 0xFFFFFFull) >= h) break;
-        if (*(volatile unsigned *)abort_word) {
-          atomicOr(err, (unsigned)DERR_TIMEOUT);
-          return false;
-        }
-        if (global_ns() - t0 > 2000000000ull) {
-          atomicExch(abort_word, 1u);
-          atomicOr(err, (unsigned)DERR_TIMEOUT);
-          return false;
+    int ok = 1;
+    if (lane == 0) {
+      if (*(volatile unsigned *)abort_word) ok = 0;
+      const unsigned long long t0 = global_ns();
+      for (int side = 0; ok && h > 0 && side < 2; side++) {
+        const unsigned long long *w = side ? wr : wl;
+        for (;;) {
+          unsigned long long v = ld_acquire_u64(w);
+          if ((v >> 24) == id && (long long)(v & 0xFFFFFFull) >= h) break;
+          if (*(volatile unsigned *)abort_word) { ok = 0; break; }
+          if (global_ns() - t0 > 2000000000ull) {
+            atomicExch(abort_word, 1u);
+            ok = 0;
+            break;
+          }
         }
       }
+      if (!ok) atomicOr(err, (unsigned)DERR_TIMEOUT);
     }
-    __threadfence();
-    return true;
+    ok = __shfl_sync(0xffffffffu, ok, 0);
+    if (ok && h > 0) {
+      (void)ld_acquire_u64(wl);
+      (void)ld_acquire_u64(wr);
+    }
+    return ok != 0;
   }
   __device__ void published() { st_release_u64(mine, (id << 24) | (unsigned long long)(h + 1)); }
+  // the slice's next move, for both outcomes of this one
+  __device__ void ahead(RotShared &sh)
+  {
+    if (!has_next) return;
+    rot_uniforms(seed, pass, phase_next, pair, 0, linear, sh.nxt_u);
+    rot_propose(*sys, linear, sh.ang_old[0], sh.ang_old[1], sh.ang_old[2], sh.nxt_u, sh.nxt_prop[0]);
+    rot_propose(*sys, linear, sh.ang_new[0], sh.ang_new[1], sh.ang_new[2], sh.nxt_u, sh.nxt_prop[1]);
+  }
 };
 
 // serial position of slice q in MCRotationsMove's loops: even slices, then odd
@@ -664,6 +679,11 @@ __global__ void __launch_bounds__(PIMC_ROT_THREADS) k_rot_slices(Ctx c, Frame *f
   hk.id = ((unsigned long long)ps << 8) | (group & 255u);
   hk.abort_word = abort_word;
   hk.err = c.st.err;
+  hk.sys = &c.s;
+  hk.seed = seed;
+  hk.pass = ps;
+  hk.pair = q >> 1;
+  hk.linear = linear;
   unsigned long long tot = 0, nacc = 0;
   double u[4] = {0.5, 0.5, 0.5, 0.5}, prop[3] = {0.0, 0.0, 0.0};
   int h = q & 1;
@@ -676,14 +696,16 @@ __global__ void __launch_bounds__(PIMC_ROT_THREADS) k_rot_slices(Ctx c, Frame *f
   }
   for (; h < nhalf; h += 2) {
     hk.h = h;
+    hk.has_next = h + 2 < nhalf;
+    hk.phase_next = phase0 + (unsigned)(h + 2);
     int acc = rot_finish<MIX, true>(c, frames, g0, q, linear, sh, nullptr, hk);
     if (sh.stop) break;
     tot++;
     nacc += acc;
     if (h + 2 < nhalf) {
       if (threadIdx.x == 0) {
-        rot_uniforms(seed, ps, phase0 + (unsigned)(h + 2), q >> 1, 0, linear, u);
-        rot_propose(c.s, linear, c.st.ang[q], c.st.ang[n + q], c.st.ang[2 * n + q], u, prop);
+        for (int k = 0; k < 4; k++) u[k] = sh.nxt_u[k];
+        for (int k = 0; k < 3; k++) prop[k] = sh.nxt_prop[acc ? 1 : 0][k];
       }
       rot_prepare<MIX>(c, frames, g0, q, u, prop, linear, sh);
     }

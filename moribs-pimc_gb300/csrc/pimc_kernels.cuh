@@ -97,13 +97,18 @@ __device__ __forceinline__ float pair_term32(const Ctx &c, const Frame *__restri
 // out[s] = sum over partners p != skip[s] of f(s, p), s < nslots.  buf holds
 // PIMC_RED_BUF doubles of shared memory; slots are processed in chunks that
 // fit.  Each slot is reduced by one warp: lane l adds items l, l+32, ... in
-// order, then a fixed xor-shuffle tree; deterministic.
-template <class F>
-__device__ __forceinline__ void slot_sums(int nslots, int na, const int *skip, F f, double *out, double *buf)
+// order, then a fixed xor-shuffle tree; deterministic.  The items and the
+// sum have f's type: double on the FP64 path, float on the FP32 path (one
+// float round per add instead of a serial chain of double adds, which on
+// this part costs about sixty cycles per add).
+template <class F, class O>
+__device__ __forceinline__ void slot_sums(int nslots, int na, const int *skip, F f, O *out, double *bufd)
 {
+  using T = decltype(f(0, 0));
+  T *buf = reinterpret_cast<T *>(bufd);
   const int npart = na - 1;
   if (npart <= 0) {
-    for (int s = threadIdx.x; s < nslots; s += blockDim.x) out[s] = 0.0;
+    for (int s = threadIdx.x; s < nslots; s += blockDim.x) out[s] = O(0);
     __syncthreads();
     return;
   }
@@ -120,7 +125,7 @@ __device__ __forceinline__ void slot_sums(int nslots, int na, const int *skip, F
       int s = g / npart, pi = g - s * npart;
       int p = pi < skip[s] ? pi : pi + 1;
       int i2 = i + nt;
-      double v0 = f(s, p), v1 = 0.0;
+      T v0 = f(s, p), v1 = T(0);
       if (i2 < cnt) {
         int g2 = base + i2;
         int s2 = g2 / npart, pi2 = g2 - s2 * npart;
@@ -134,12 +139,12 @@ __device__ __forceinline__ void slot_sums(int nslots, int na, const int *skip, F
     int sfirst = base / npart, slast = (base + cnt - 1) / npart;
     for (int sl = sfirst + warp; sl <= slast; sl += nw) {
       int lo = max(sl * npart, base) - base, hi = min((sl + 1) * npart, base + cnt) - base;
-      double acc = 0.0;
+      T acc = T(0);
       for (int k = lo + lane; k < hi; k += 32) acc += buf[k];
       for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
       if (lane == 0) {
-        if (sl * npart >= base) out[sl] = acc;     // the slot starts in this chunk
-        else out[sl] += acc;                       // continuation of a slot split across chunks
+        if (sl * npart >= base) out[sl] = (O)acc;     // the slot starts in this chunk
+        else out[sl] += (O)acc;                       // continuation of a slot split across chunks
       }
     }
     __syncthreads();
@@ -246,6 +251,8 @@ struct BisectShared {
   double ob[3][PIMC_MAX_SEG + 1];     // the current beads of the window
   double nb[3][PIMC_MAX_SEG + 1];     // the proposed beads
   double se[2 * PIMC_MAX_SEG];        // slice energies: (bead k, new) at 2(k-1), (bead k, old) at 2(k-1)+1
+  float sef[2 * PIMC_MAX_SEG];        // the same on the FP32 path
+  float4 bf[2][PIMC_MAX_SEG + 1];     // float copies of the proposed [0] and current [1] beads
   int sa[2 * PIMC_MAX_SEG];           // owner of the slot's bead (the partner sums skip it)
   int owner[PIMC_MAX_SEG + 1], slice[PIMC_MAX_SEG + 1];
   int acc, passed;
@@ -285,6 +292,7 @@ __device__ int bisect_move(const Ctx &c, const Frame *frames, int type, int atom
     double x = c.st.x[i], y = c.st.y[i], z = c.st.z[i];
     sh.nb[0][k] = x; sh.nb[1][k] = y; sh.nb[2][k] = z;
     sh.ob[0][k] = x; sh.ob[1][k] = y; sh.ob[2][k] = z;
+    if (MIX) sh.bf[1][k] = c.st.b4[i];
   }
   if (tid == 0) { sh.acc = 0; sh.passed = 0; sh.gbase = src.gauss_base(); }
   __syncthreads();
@@ -302,15 +310,17 @@ __device__ int bisect_move(const Ctx &c, const Frame *frames, int type, int atom
   // the proposed beads, level by level (mc_piqmc.cc:243-254)
   for (int level = 0; level < L; level++) {
     int seg = 1 << (L - level), half = seg >> 1, nmid = M / seg;
-    double sq = s.bis_sq[type][level];
+    double sq = s.bis_sq[type][level], isq = s.bis_isq[type][level];
     const double *gz = sh.gz + 3 * (nmid - 1);
     for (int j = tid; j < nmid; j += blockDim.x) {
       int k0 = j * seg, k1 = k0 + half, k2 = k0 + seg;
       for (int d = 0; d < 3; d++) {
         double v = 0.5 * (sh.nb[d][k0] + sh.nb[d][k2]);
-        v += gz[3 * j + d] / sq;
+        if (MIX) v = fma(gz[3 * j + d], isq, v);       // FP32 path: no division chain
+        else v += gz[3 * j + d] / sq;
         sh.nb[d][k1] = v;
       }
+      if (MIX) sh.bf[0][k1] = make_float4((float)sh.nb[0][k1], (float)sh.nb[1][k1], (float)sh.nb[2][k1], 0.0f);
       sh.sa[2 * (k1 - 1)] = sh.owner[k1];
       sh.sa[2 * (k1 - 1) + 1] = sh.owner[k1];
     }
@@ -319,13 +329,12 @@ __device__ int bisect_move(const Ctx &c, const Frame *frames, int type, int atom
   // slice energies of every interior bead, new and old
   if (MIX)
     slot_sums(2 * (M - 1), s.na, sh.sa,
-              [&](int sl, int p) -> double {
+              [&](int sl, int p) -> float {
                 int k = (sl >> 1) + 1;
-                const double(*b)[PIMC_MAX_SEG + 1] = (sl & 1) ? sh.ob : sh.nb;
-                return (double)pair_term32(c, frames, sh.owner[k], p, sh.slice[k], (float)b[0][k], (float)b[1][k],
-                                           (float)b[2][k]);
+                const float4 b = sh.bf[sl & 1][k];
+                return pair_term32(c, frames, sh.owner[k], p, sh.slice[k], b.x, b.y, b.z);
               },
-              sh.se, sh.buf);
+              sh.sef, sh.buf);
   else
     slot_sums(2 * (M - 1), s.na, sh.sa,
               [&](int sl, int p) -> double {
@@ -334,7 +343,30 @@ __device__ int bisect_move(const Ctx &c, const Frame *frames, int type, int atom
                 return pair_term64(c, frames, sh.owner[k], p, sh.slice[k], b[0][k], b[1][k], b[2][k]);
               },
               sh.se, sh.buf);
-  if (tid == 0) {
+  if (MIX && tid == 0) {
+    // the level accepts in float from the float slice energies
+    float pot1 = 0.0f;
+    int a = 0;
+    for (int level = 0; level < L; level++) {
+      int seg = 1 << (L - level), half = seg >> 1, nmid = M / seg;
+      src.gauss_advance(3 * nmid);
+      float pot0 = 0.0f;
+      for (int j = 0; j < nmid; j++) {
+        int k0 = j * seg, k1 = k0 + half;
+        pot0 += (sh.sef[2 * (k1 - 1)] - sh.sef[2 * (k1 - 1) + 1]);
+        if (k0 != 0) pot0 += (sh.sef[2 * (k0 - 1)] - sh.sef[2 * (k0 - 1) + 1]);
+      }
+      float deltav = (pot0 - 2.0f * pot1) * ((float)s.tau * (float)(seg / 2));
+      if (ds_out) ds_out[level] = (double)deltav;
+      a = 0;
+      if (deltav < 0.0f) a = 1;
+      else if (expf(-deltav) > (float)(Src::kPrefetchU ? sh.ua[level] : src.accept_u(level))) a = 1;
+      if (!a) break;
+      sh.passed = level + 1;
+      pot1 = pot0;
+    }
+    sh.acc = a;
+  } else if (tid == 0) {
     double pot1 = 0.0;
     int a = 0;
     for (int level = 0; level < L; level++) {
@@ -405,12 +437,14 @@ __device__ __forceinline__ void group_sync()
 }
 
 // slot_sums over threads [0, NT) of the CTA, synchronised by named barrier ID
-template <int NT, int ID, class F>
-__device__ __forceinline__ void slot_sums_group(int nslots, int na, const int *skip, F f, double *out, double *buf)
+template <int NT, int ID, class F, class O>
+__device__ __forceinline__ void slot_sums_group(int nslots, int na, const int *skip, F f, O *out, double *bufd)
 {
+  using T = decltype(f(0, 0));
+  T *buf = reinterpret_cast<T *>(bufd);
   const int npart = na - 1;
   if (npart <= 0) {
-    for (int s = threadIdx.x; s < nslots; s += NT) out[s] = 0.0;
+    for (int s = threadIdx.x; s < nslots; s += NT) out[s] = O(0);
     group_sync<ID, NT>();
     return;
   }
@@ -429,12 +463,12 @@ __device__ __forceinline__ void slot_sums_group(int nslots, int na, const int *s
     int sfirst = base / npart, slast = (base + cnt - 1) / npart;
     for (int sl = sfirst + warp; sl <= slast; sl += nw) {
       int lo = max(sl * npart, base) - base, hi = min((sl + 1) * npart, base + cnt) - base;
-      double acc = 0.0;
+      T acc = T(0);
       for (int k = lo + lane; k < hi; k += 32) acc += buf[k];
       for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
       if (lane == 0) {
-        if (sl * npart >= base) out[sl] = acc;
-        else out[sl] += acc;
+        if (sl * npart >= base) out[sl] = (O)acc;
+        else out[sl] += (O)acc;
       }
     }
     group_sync<ID, NT>();
@@ -473,6 +507,10 @@ struct RotShared {
   int skip[2 * 16];
   double pot_c, rd;
   double u[4], pot_old, pot_new;
+  double boltz;             // exp(-tau (pot_new - pot_old)), or its exponent for the RS densities
+  float valsf[2 * 16];      // partner sums on the FP32 path
+  double ang_old[3];        // the slice's current angles
+  double nxt_u[4], nxt_prop[2][3];   // the slice's next move: uniforms, proposal if this one is rejected / accepted
   double buf[PIMC_RED_BUF];
 };
 
@@ -662,6 +700,8 @@ __device__ void rot_prepare(const Ctx &c, const Frame *frames, int g0, int q, co
       if (sh.pot_cached) sh.pot_c = c.st.rp_cache[i1];
     }
     if (lane < 2 * R) sh.skip[lane] = g0;
+  } else if (warp == 3) {
+    if (lane < 3) sh.ang_old[lane] = c.st.ang[lane * n + i1];
   }
   __syncthreads();
   if (warp < 8) {
@@ -671,11 +711,11 @@ __device__ void rot_prepare(const Ctx &c, const Frame *frames, int g0, int q, co
       if (MIX)
         slot_sums_group<PIMC_ROT_PAIR_THREADS, 2>(
             nsl, s.na, sh.skip,
-            [&](int sl, int p) -> double {
+            [&](int sl, int p) -> float {
               int k = sl + first;
-              return (double)rotlin_term32(c, k < R ? sh.nvf : sh.nnewf, g0, p, q * R + (k % R));
+              return rotlin_term32(c, k < R ? sh.nvf : sh.nnewf, g0, p, q * R + (k % R));
             },
-            sh.vals, sh.buf);
+            sh.valsf, sh.buf);
       else
         slot_sums_group<PIMC_ROT_PAIR_THREADS, 2>(
             nsl, s.na, sh.skip,
@@ -688,11 +728,11 @@ __device__ void rot_prepare(const Ctx &c, const Frame *frames, int g0, int q, co
       if (MIX)
         slot_sums_group<PIMC_ROT_PAIR_THREADS, 2>(
             nsl, s.na, sh.skip,
-            [&](int sl, int p) -> double {
+            [&](int sl, int p) -> float {
               int k = sl + first;
-              return (double)rot3d_term32(c, frames, k < R ? sh.fo[1] : sh.fn, g0, p, q * R + (k % R));
+              return rot3d_term32(c, frames, k < R ? sh.fo[1] : sh.fn, g0, p, q * R + (k % R));
             },
-            sh.vals, sh.buf);
+            sh.valsf, sh.buf);
       else
         slot_sums_group<PIMC_ROT_PAIR_THREADS, 2>(
             nsl, s.na, sh.skip,
@@ -703,13 +743,27 @@ __device__ void rot_prepare(const Ctx &c, const Frame *frames, int g0, int q, co
             sh.vals, sh.buf);
     }
     if (tid == 0) {
-      double pot_old = 0.0, pot_new = 0.0;
-      if (sh.pot_cached) pot_old = sh.pot_c;
-      else
-        for (int k = 0; k < R; k++) pot_old += sh.vals[k];
-      for (int k = 0; k < R; k++) pot_new += sh.vals[R - first + k];
-      sh.pot_old = pot_old;
-      sh.pot_new = pot_new;
+      // sums and the Boltzmann factor here, off the neighbour chain
+      if (MIX) {
+        float po = 0.0f, pn = 0.0f;
+        if (sh.pot_cached) po = (float)sh.pot_c;
+        else
+          for (int k = 0; k < R; k++) po += sh.valsf[k];
+        for (int k = 0; k < R; k++) pn += sh.valsf[R - first + k];
+        sh.pot_old = sh.pot_cached ? sh.pot_c : (double)po;
+        sh.pot_new = (double)pn;
+        float x = -(float)s.tau * (pn - po);
+        sh.boltz = (s.rot_den_type == 0) ? (double)expf(x) : -s.tau * ((double)pn - (double)po);
+      } else {
+        double pot_old = 0.0, pot_new = 0.0;
+        if (sh.pot_cached) pot_old = sh.pot_c;
+        else
+          for (int k = 0; k < R; k++) pot_old += sh.vals[k];
+        for (int k = 0; k < R; k++) pot_new += sh.vals[R - first + k];
+        sh.pot_old = pot_old;
+        sh.pot_new = pot_new;
+        sh.boltz = (s.rot_den_type == 0) ? exp(-s.tau * (pot_new - pot_old)) : 0.0;
+      }
     }
   } else if (warp == 9) {
     if (lane == 0 && linear) {
@@ -722,15 +776,17 @@ __device__ void rot_prepare(const Ctx &c, const Frame *frames, int g0, int q, co
 
 // hooks of rot_finish for launches without neighbour waits
 struct RotNoHooks {
-  __device__ bool wait() { return true; }
+  __device__ bool wait(int) { return true; }
   __device__ void published() {}
+  __device__ void ahead(RotShared &) {}
 };
 
-// second stage of the move prepared in sh, on warp 8: hooks.wait() on lane 0
-// before the neighbours' state is read (false: leave the move undone and set
-// sh.stop), hooks.published() on lane 0 after the commit.  COH reads the
-// neighbours through L2 (persistent launches, where other CTAs write them).
-// All PIMC_ROT_THREADS threads call it; returns 1 if accepted.
+// second stage of the move prepared in sh, on warp 8: hooks.wait(lane) on
+// all lanes before the neighbours' state is read (false: leave the move
+// undone and set sh.stop), hooks.published() on lane 0 after the commit;
+// meanwhile warp 9 runs hooks.ahead(sh) (the slice's next proposal).  COH
+// reads the neighbours through L2 (persistent launches, where other CTAs
+// write them).  All PIMC_ROT_THREADS threads call it; returns 1 if accepted.
 template <bool MIX, bool COH, class Hooks>
 __device__ int rot_finish(const Ctx &c, Frame *frames, int g0, int q, bool linear, RotShared &sh, double *rd_out,
                           Hooks &hooks)
@@ -746,29 +802,38 @@ __device__ int rot_finish(const Ctx &c, Frame *frames, int g0, int q, bool linea
   const int i0 = r * Q + q0, i1 = r * Q + q, i2 = r * Q + q2;
   const bool use_links = Q >= 3;                // link cache (with Q < 3 both links join the same two slices)
   const bool need64 = !MIX || s.nrotors > 1;
+  const bool mf_only = MIX && !linear && s.rot_den_type == 0;   // densities read the float frames only
   if (warp == 8) {
-    if (lane == 0) {
-      int go = hooks.wait();
-      sh.stop = !go;
-    }
-    __syncwarp();
-    if (!sh.stop) {
+    bool go = hooks.wait(lane);
+    if (lane == 0) sh.stop = !go;
+    if (go) {
+      // the neighbours' orientations and the link cache, all loads issued together
       if (linear) {
         if (lane < 6) {
           int k = (lane < 3) ? 0 : 2, d = lane - (lane < 3 ? 0 : 3);
           sh.nv[k][d] = ld_state<COH>(c.st.cosv + d * n + (k == 0 ? i0 : i2));
         }
+      } else if (mf_only) {
+        // words of Frame::mf and Frame::hzf
+        const int w0 = (int)(offsetof(Frame, mf) / 4), nw = 10;
+        if (lane < 2 * nw) {
+          const Frame *src = frames + (lane < nw ? i0 : i2);
+          Frame &dst = sh.fo[lane < nw ? 0 : 2];
+          int w = w0 + (lane < nw ? lane : lane - nw);
+          reinterpret_cast<unsigned *>(&dst)[w] =
+              COH ? __ldcg(reinterpret_cast<const unsigned *>(src) + w) : reinterpret_cast<const unsigned *>(src)[w];
+        }
       } else {
         copy_frame<COH>(sh.fo[0], frames + i0, lane);
         copy_frame<COH>(sh.fo[2], frames + i2, lane);
       }
-      if (lane == 0) {
-        sh.bad = 0;
-        sh.link_ok[0] = use_links && ld_state<COH>(c.st.rl_ok + i0);
-        sh.link_ok[1] = use_links && ld_state<COH>(c.st.rl_ok + i1);
-        if (sh.link_ok[0]) sh.rho[0] = ld_state<COH>(c.st.rl_cache + i0);
-        if (sh.link_ok[1]) sh.rho[1] = ld_state<COH>(c.st.rl_cache + i1);
+      if (lane >= 24 && lane < 28) {
+        int k = lane - 24;                              // rl_ok i0, rl_ok i1, rl_cache i0, rl_cache i1
+        int ii = (k & 1) ? i1 : i0;
+        if (k < 2) sh.link_ok[k] = use_links && ld_state<COH>(c.st.rl_ok + ii);
+        else sh.rho[k - 2] = use_links ? ld_state<COH>(c.st.rl_cache + ii) : 0.0;
       }
+      if (lane == 0) sh.bad = 0;
       __syncwarp();
       // 0: (q-1, q) old, 1: (q, q+1) old, 2: (q-1, q) new, 3: (q, q+1) new
       if (lane < 4 && !(lane < 2 && sh.link_ok[lane])) {
@@ -816,7 +881,7 @@ __device__ int rot_finish(const Ctx &c, Frame *frames, int g0, int q, bool linea
             dens_new = fabsf(dens_new);
           }
           float rf = (dens_old > (float)PIMC_RZERO) ? dens_new / dens_old : 1.0f;
-          rf *= expf((float)(-s.tau * (pot_new - pot_old)));
+          rf *= (float)sh.boltz;
           rd = (double)rf;
           acc = (rf > 1.0f) || (rf > (float)u[linear ? 2 : 3]);
         } else if (s.rot_den_type == 0) {
@@ -830,7 +895,7 @@ __device__ int rot_finish(const Ctx &c, Frame *frames, int g0, int q, bool linea
             if (dens_new < 0.0) dens_new = fabs(dens_new);
           }
           rd = (dens_old > PIMC_RZERO) ? dens_new / dens_old : 1.0;
-          rd *= exp(-s.tau * (pot_new - pot_old));
+          rd *= sh.boltz;                                          // exp(-tau (pot_new - pot_old))
           acc = (rd > 1.0) || (rd > u[linear ? 2 : 3]);
         } else if (linear) {
           double dens_old = sh.rho[0] + sh.rho[1], dens_new = sh.rho[2] + sh.rho[3];
@@ -881,6 +946,8 @@ __device__ int rot_finish(const Ctx &c, Frame *frames, int g0, int q, bool linea
         hooks.published();
       }
     }
+  } else if (warp == 9 && lane == 0) {
+    hooks.ahead(sh);
   }
   __syncthreads();
   return sh.acc;
