@@ -11,6 +11,7 @@
 #define PIMC_WNO2K 0.6950356          /* mc_const.h:16 */
 #define PIMC_RZERO 1.0e-10            /* mc_confg.h:59 */
 #define PIMC_BLOCK 256                /* threads per move CTA */
+#define PIMC_BIS_THREADS 512          /* bisection CTA: 2(M-1) slots x partners over 16 warps */
 #define PIMC_ROT_THREADS 320          /* rotational move CTA: 8 pair warps, a density warp, a commit warp */
 #define PIMC_RED_BUF 4096             /* doubles in a CTA's reduction buffer */
 #define PIMC_MAX_SEG 64               /* largest bisection segment (levels <= 6) */

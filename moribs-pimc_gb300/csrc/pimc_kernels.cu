@@ -38,7 +38,7 @@ __global__ void k_invalidate_caches(Ctx c)
 // MCBisectionMove(type, time) / MCBisectionMoveExchange: all atoms of the
 // type in order, each consuming the replayed gauss()/rnd3() streams
 template <bool MIX>
-__global__ void __launch_bounds__(PIMC_BLOCK) k_bisect_replay(Ctx c, Frame *frames, int type, int time0, int exch,
+__global__ void __launch_bounds__(PIMC_BIS_THREADS) k_bisect_replay(Ctx c, Frame *frames, int type, int time0, int exch,
                                                                ReplaySrc src, double *ds_out, int *lvl_out,
                                                                unsigned long long *cnt)
 {
@@ -58,7 +58,7 @@ __global__ void __launch_bounds__(PIMC_BLOCK) k_bisect_replay(Ctx c, Frame *fram
 // one phase of the production schedule: window k starts at s0 + k*M and
 // moves atom (k + j) mod numb; interiors of all windows are disjoint
 template <bool MIX>
-__global__ void __launch_bounds__(PIMC_BLOCK) k_bisect_phase(Ctx c, Frame *frames, int type, int s0, int j,
+__global__ void __launch_bounds__(PIMC_BIS_THREADS) k_bisect_phase(Ctx c, Frame *frames, int type, int s0, int j,
                                                               unsigned phase, uint64_t seed, const unsigned *pass,
                                                               unsigned long long *cnt)
 {
@@ -82,7 +82,7 @@ __global__ void __launch_bounds__(PIMC_BLOCK) k_bisect_phase(Ctx c, Frame *frame
 // after the other with no other CTA involved, and the result equals the
 // phase-by-phase launches with the same phase numbers.
 template <bool MIX>
-__global__ void __launch_bounds__(PIMC_BLOCK) k_bisect_block(Ctx c, Frame *frames, int type, int s0, unsigned phase0,
+__global__ void __launch_bounds__(PIMC_BIS_THREADS) k_bisect_block(Ctx c, Frame *frames, int type, int s0, unsigned phase0,
                                                               uint64_t seed, const unsigned *pass,
                                                               unsigned long long *cnt)
 {
@@ -642,16 +642,16 @@ void launch_invalidate_caches(const Ctx &c, cudaStream_t s)
 void launch_bisect_replay(const Ctx &c, Frame *f, int type, int time0, int exch, ReplaySrc src, double *ds,
                           int *lvl, unsigned long long *cnt, cudaStream_t s)
 {
-  if (c.s.mixed) k_bisect_replay<true><<<1, PIMC_BLOCK, 0, s>>>(c, f, type, time0, exch, src, ds, lvl, cnt);
-  else k_bisect_replay<false><<<1, PIMC_BLOCK, 0, s>>>(c, f, type, time0, exch, src, ds, lvl, cnt);
+  if (c.s.mixed) k_bisect_replay<true><<<1, PIMC_BIS_THREADS, 0, s>>>(c, f, type, time0, exch, src, ds, lvl, cnt);
+  else k_bisect_replay<false><<<1, PIMC_BIS_THREADS, 0, s>>>(c, f, type, time0, exch, src, ds, lvl, cnt);
 }
 
 void launch_bisect_phase(const Ctx &c, Frame *f, int type, int s0, int j, unsigned phase, uint64_t seed,
                          const unsigned *pass, unsigned long long *cnt, cudaStream_t s)
 {
   int M = 1 << c.s.levels[type];
-  if (c.s.mixed) k_bisect_phase<true><<<c.s.P / M, PIMC_BLOCK, 0, s>>>(c, f, type, s0, j, phase, seed, pass, cnt);
-  else k_bisect_phase<false><<<c.s.P / M, PIMC_BLOCK, 0, s>>>(c, f, type, s0, j, phase, seed, pass, cnt);
+  if (c.s.mixed) k_bisect_phase<true><<<c.s.P / M, PIMC_BIS_THREADS, 0, s>>>(c, f, type, s0, j, phase, seed, pass, cnt);
+  else k_bisect_phase<false><<<c.s.P / M, PIMC_BIS_THREADS, 0, s>>>(c, f, type, s0, j, phase, seed, pass, cnt);
 }
 
 // nhalf half-sweeps with one CTA per rotational slice (one rotor, Q even,
@@ -827,8 +827,8 @@ void launch_bisect_block(const Ctx &c, Frame *f, int type, int s0, unsigned phas
 {
   int M = 1 << c.s.levels[type];
   int nwin = c.s.P / M;
-  if (c.s.mixed) k_bisect_block<true><<<nwin, PIMC_BLOCK, 0, s>>>(c, f, type, s0, phase0, seed, pass, cnt);
-  else k_bisect_block<false><<<nwin, PIMC_BLOCK, 0, s>>>(c, f, type, s0, phase0, seed, pass, cnt);
+  if (c.s.mixed) k_bisect_block<true><<<nwin, PIMC_BIS_THREADS, 0, s>>>(c, f, type, s0, phase0, seed, pass, cnt);
+  else k_bisect_block<false><<<nwin, PIMC_BIS_THREADS, 0, s>>>(c, f, type, s0, phase0, seed, pass, cnt);
 }
 
 void launch_mol(const Ctx &c, Frame *f, int type, int atom, bool replay, ReplaySrc src, uint64_t seed,

@@ -252,6 +252,8 @@ struct BisectShared {
   double nb[3][PIMC_MAX_SEG + 1];     // the proposed beads
   double se[2 * PIMC_MAX_SEG];        // slice energies: (bead k, new) at 2(k-1), (bead k, old) at 2(k-1)+1
   float sef[2 * PIMC_MAX_SEG];        // the same on the FP32 path
+  double dv[8], ex[8];                // per level: action difference, exp(-difference) (replay)
+  double lu[8];                       // log of the accept uniforms (counter-based source)
   float4 bf[2][PIMC_MAX_SEG + 1];     // float copies of the proposed [0] and current [1] beads
   int sa[2 * PIMC_MAX_SEG];           // owner of the slot's bead (the partner sums skip it)
   int owner[PIMC_MAX_SEG + 1], slice[PIMC_MAX_SEG + 1];
@@ -305,7 +307,11 @@ __device__ int bisect_move(const Ctx &c, const Frame *frames, int type, int atom
     else sh.gz[i] = src.gauss_pre(sh.gbase, i, l, off / 3, off - 3 * (off / 3));
   }
   if (Src::kPrefetchU)
-    for (int l = tid - 64; l >= 0 && l < L; l += blockDim.x) sh.ua[l] = src.accept_u(l);
+    for (int l = tid - 64; l >= 0 && l < L; l += blockDim.x) {
+      double u = src.accept_u(l);
+      sh.ua[l] = u;
+      sh.lu[l] = log(u);
+    }
   __syncthreads();
   // the proposed beads, level by level (mc_piqmc.cc:243-254)
   for (int level = 0; level < L; level++) {
@@ -343,50 +349,50 @@ __device__ int bisect_move(const Ctx &c, const Frame *frames, int type, int atom
                 return pair_term64(c, frames, sh.owner[k], p, sh.slice[k], b[0][k], b[1][k], b[2][k]);
               },
               sh.se, sh.buf);
-  if (MIX && tid == 0) {
-    // the level accepts in float from the float slice energies
-    float pot1 = 0.0f;
-    int a = 0;
-    for (int level = 0; level < L; level++) {
-      int seg = 1 << (L - level), half = seg >> 1, nmid = M / seg;
-      src.gauss_advance(3 * nmid);
-      float pot0 = 0.0f;
-      for (int j = 0; j < nmid; j++) {
-        int k0 = j * seg, k1 = k0 + half;
-        pot0 += (sh.sef[2 * (k1 - 1)] - sh.sef[2 * (k1 - 1) + 1]);
-        if (k0 != 0) pot0 += (sh.sef[2 * (k0 - 1)] - sh.sef[2 * (k0 - 1) + 1]);
-      }
-      float deltav = (pot0 - 2.0f * pot1) * ((float)s.tau * (float)(seg / 2));
-      if (ds_out) ds_out[level] = (double)deltav;
-      a = 0;
-      if (deltav < 0.0f) a = 1;
-      else if (expf(-deltav) > (float)(Src::kPrefetchU ? sh.ua[level] : src.accept_u(level))) a = 1;
-      if (!a) break;
-      sh.passed = level + 1;
-      pot1 = pot0;
-    }
-    sh.acc = a;
-  } else if (tid == 0) {
-    double pot1 = 0.0;
-    int a = 0;
-    for (int level = 0; level < L; level++) {
-      int seg = 1 << (L - level), half = seg >> 1, nmid = M / seg;
-      src.gauss_advance(3 * nmid);
+  // the action difference of every level in double precision on both paths
+  // (the energies of the FP32 path are float sums), one level per warp
+  // summing the bead differences in the reference's order
+  // (mc_piqmc.cc:256-266); thread 0 then takes the level decisions in the
+  // reference's order.  Replay draws rnd3() only where the reference does
+  // and tests exp(-dS) > u as it does; the counter-based source tests the
+  // same inequality as -dS > log u with log u computed up front.
+  if ((tid & 31) == 0 && (tid >> 5) < L) {
+    const int level = tid >> 5;                 // one warp per level: the chains issue side by side
+    auto de = [&](int k) -> double {
+      double en = MIX ? (double)sh.sef[2 * (k - 1)] : sh.se[2 * (k - 1)];
+      double eo = MIX ? (double)sh.sef[2 * (k - 1) + 1] : sh.se[2 * (k - 1) + 1];
+      return en - eo;
+    };
+    double pot[2] = {0.0, 0.0};                 // pot0 of level-1 and of level
+    for (int l = (level > 0 ? level - 1 : level), w = (level > 0 ? 0 : 1); l <= level; l++, w++) {
+      int seg = 1 << (L - l), half = seg >> 1, nmid = M / seg;
       double pot0 = 0.0;
       for (int j = 0; j < nmid; j++) {
         int k0 = j * seg, k1 = k0 + half;
-        pot0 += (sh.se[2 * (k1 - 1)] - sh.se[2 * (k1 - 1) + 1]);
-        if (k0 != 0) pot0 += (sh.se[2 * (k0 - 1)] - sh.se[2 * (k0 - 1) + 1]);
+        pot0 += de(k1);
+        if (k0 != 0) pot0 += de(k0);
       }
-      double deltav = (pot0 - 2.0 * pot1);
-      deltav *= s.tau * (double)(seg / 2);
+      pot[w] = pot0;
+    }
+    int seg = 1 << (L - level);
+    double deltav = (pot[1] - 2.0 * pot[0]);
+    deltav *= s.tau * (double)(seg / 2);
+    sh.dv[level] = deltav;
+    if (!Src::kPrefetchU) sh.ex[level] = exp(-deltav);
+  }
+  __syncthreads();
+  if (tid == 0) {
+    int a = 0;
+    for (int level = 0; level < L; level++) {
+      int seg = 1 << (L - level), nmid = M / seg;
+      src.gauss_advance(3 * nmid);
+      double deltav = sh.dv[level];
       if (ds_out) ds_out[level] = deltav;
       a = 0;
       if (deltav < 0.0) a = 1;
-      else if (exp(-deltav) > (Src::kPrefetchU ? sh.ua[level] : src.accept_u(level))) a = 1;
+      else if (Src::kPrefetchU ? (-deltav > sh.lu[level]) : (sh.ex[level] > src.accept_u(level))) a = 1;
       if (!a) break;
       sh.passed = level + 1;
-      pot1 = pot0;
     }
     sh.acc = a;
   }
@@ -507,7 +513,8 @@ struct RotShared {
   int skip[2 * 16];
   double pot_c, rd;
   double u[4], pot_old, pot_new;
-  double boltz;             // exp(-tau (pot_new - pot_old)), or its exponent for the RS densities
+  double boltz;             // exp(-tau (pot_new - pot_old)) (Noya densities) or -tau (pot_new - pot_old) (RS)
+  double logu;              // log of the accept uniform (RS densities)
   float valsf[2 * 16];      // partner sums on the FP32 path
   double ang_old[3];        // the slice's current angles
   double nxt_u[4], nxt_prop[2][3];   // the slice's next move: uniforms, proposal if this one is rejected / accepted
@@ -752,8 +759,9 @@ __device__ void rot_prepare(const Ctx &c, const Frame *frames, int g0, int q, co
         for (int k = 0; k < R; k++) pn += sh.valsf[R - first + k];
         sh.pot_old = sh.pot_cached ? sh.pot_c : (double)po;
         sh.pot_new = (double)pn;
-        float x = -(float)s.tau * (pn - po);
-        sh.boltz = (s.rot_den_type == 0) ? (double)expf(x) : -s.tau * ((double)pn - (double)po);
+        // the action difference and its exponent in double precision
+        sh.boltz = (s.rot_den_type == 0) ? exp(-s.tau * (sh.pot_new - sh.pot_old)) : -(s.tau * (sh.pot_new - sh.pot_old));
+        if (s.rot_den_type != 0) sh.logu = log(sh.u[linear ? 2 : 3]);
       } else {
         double pot_old = 0.0, pot_new = 0.0;
         if (sh.pot_cached) pot_old = sh.pot_c;
@@ -762,7 +770,8 @@ __device__ void rot_prepare(const Ctx &c, const Frame *frames, int g0, int q, co
         for (int k = 0; k < R; k++) pot_new += sh.vals[R - first + k];
         sh.pot_old = pot_old;
         sh.pot_new = pot_new;
-        sh.boltz = (s.rot_den_type == 0) ? exp(-s.tau * (pot_new - pot_old)) : 0.0;
+        sh.boltz = (s.rot_den_type == 0) ? exp(-s.tau * (pot_new - pot_old)) : -(s.tau * (pot_new - pot_old));
+        if (s.rot_den_type != 0) sh.logu = log(sh.u[linear ? 2 : 3]);
       }
     }
   } else if (warp == 9) {
@@ -870,7 +879,7 @@ __device__ int rot_finish(const Ctx &c, Frame *frames, int g0, int q, bool linea
         double rd;
         int acc = 0, neg = 0;
         if (MIX && s.rot_den_type == 0) {
-          // the FP32 path: densities, their ratio and the Boltzmann factor in float
+          // the FP32 path: the table densities and their ratio in float
           float dens_old = (float)sh.rho[0] * (float)sh.rho[1], dens_new = (float)sh.rho[2] * (float)sh.rho[3];
           if (fabsf(dens_old) < (float)PIMC_RZERO) dens_old = 0.0f;
           if (fabsf(dens_new) < (float)PIMC_RZERO) dens_new = 0.0f;
@@ -881,9 +890,8 @@ __device__ int rot_finish(const Ctx &c, Frame *frames, int g0, int q, bool linea
             dens_new = fabsf(dens_new);
           }
           float rf = (dens_old > (float)PIMC_RZERO) ? dens_new / dens_old : 1.0f;
-          rf *= (float)sh.boltz;
-          rd = (double)rf;
-          acc = (rf > 1.0f) || (rf > (float)u[linear ? 2 : 3]);
+          rd = (double)rf * sh.boltz;                              // FP64 Boltzmann factor
+          acc = (rd > 1.0) || (rd > u[linear ? 2 : 3]);
         } else if (s.rot_den_type == 0) {
           double dens_old = sh.rho[0] * sh.rho[1], dens_new = sh.rho[2] * sh.rho[3];
           if (fabs(dens_old) < PIMC_RZERO) dens_old = 0.0;
@@ -901,13 +909,13 @@ __device__ int rot_finish(const Ctx &c, Frame *frames, int g0, int q, bool linea
           double dens_old = sh.rho[0] + sh.rho[1], dens_new = sh.rho[2] + sh.rho[3];
           if (fabs(dens_old) < PIMC_RZERO) dens_old = 0.0;
           if (fabs(dens_new) < PIMC_RZERO) dens_new = 0.0;
-          rd = dens_new - dens_old - s.tau * (pot_new - pot_old);
-          acc = (rd > 0.0) || (rd > log(u[2]));
+          rd = dens_new - dens_old + sh.boltz;                    // - tau (pot_new - pot_old)
+          acc = (rd > 0.0) || (rd > sh.logu);
         } else {
           double rhoold = sh.rho[0] + sh.rho[1], rhonew = sh.rho[2] + sh.rho[3];
           rd = (rhonew - rhoold) / (4.0 * (s.rot_tau / PIMC_WNO2K));
-          rd -= s.tau * (pot_new - pot_old);
-          acc = (rd > 0.0) || (rd > log(u[3]));
+          rd += sh.boltz;                                          // - tau (pot_new - pot_old)
+          acc = (rd > 0.0) || (rd > sh.logu);
         }
         if (neg) { atomicOr(c.st.err, (unsigned)DERR_NEG_DENSITY); acc = 0; }
         if (sh.bad) { atomicOr(c.st.err, (unsigned)DERR_GRID_RANGE); acc = 0; }
