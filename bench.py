@@ -49,6 +49,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-companion", action="store_true", help="skip the other precision's measurement")
     return ap.parse_args()
 
 
@@ -214,6 +215,57 @@ def centroid_pass_bytes(w, mixed):
     return w.natoms * 2 * w.nslices * (w.natoms - 1) * pair_bytes(mixed)
 
 
+def timed_passes(s, seed, steps, flush, ext, dist):
+    """K passes, each bracketed by CUDA events on the library's stream, with
+    an L2 flush (256 MiB write) before each outside the events; returns the
+    max over ranks of the summed event time in ms."""
+    import torch
+    evs = []
+    with torch.cuda.stream(ext):
+        for k in range(steps):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(ext)
+            s.run_passes(1, seed)
+            e1.record(ext)
+            evs.append((e0, e1))
+    s.synchronize()
+    torch.cuda.synchronize()
+    return reduce_max(dist, sum(a.elapsed_time(b) for a, b in evs))
+
+
+def e2e_passes(s, w, seed, steps, dist):
+    """The same metric through the C ABI with host buffers: per step the path
+    goes in from pinned host memory, one pass runs, and the path and the
+    estimators come back."""
+    import numpy as np
+    import torch
+    import pimc_gb300 as G
+    c, a, co, p = s.get_state()
+    pin_c = torch.from_numpy(c).pin_memory().numpy()
+    pin_a = torch.from_numpy(a).pin_memory().numpy()
+    out_c = torch.empty(c.shape, dtype=torch.float64).pin_memory().numpy()
+    out_a = torch.empty(a.shape, dtype=torch.float64).pin_memory().numpy()
+    out_co = torch.empty(c.shape, dtype=torch.float64).pin_memory().numpy()
+    out_p = np.zeros(w.natoms, np.int32)
+    est = np.zeros(5)
+    barrier(dist)
+    t0 = time.perf_counter()
+    for k in range(steps):
+        G._chk(s.L.pimc_set_state(s.h, G.dptr(pin_c), G.dptr(pin_a), G.iptr(p)), "set_state")
+        s.run_passes(1, seed)
+        G._chk(s.L.pimc_get_state(s.h, G.dptr(out_c), G.dptr(out_a), G.dptr(out_co), G.iptr(out_p)), "get_state")
+        G._chk(s.L.pimc_estimators(s.h, G.dptr(est)), "estimators")
+        pin_c[...] = out_c
+        pin_a[...] = out_a
+    e2e_s = reduce_max(dist, time.perf_counter() - t0)
+    return {"value": s.bead_moves_per_pass() * steps * (dist.get_world_size() if dist else 1) / e2e_s, "unit": UNIT,
+            "h2d_bytes_per_step": int(pin_c.nbytes + pin_a.nbytes + p.nbytes),
+            "d2h_bytes_per_step": int(out_c.nbytes + out_a.nbytes + out_co.nbytes + out_p.nbytes + est.nbytes),
+            "steps": steps, "path": "pimc_set_state + pimc_run_passes(1) + pimc_get_state + pimc_estimators"}
+
+
 def run_gb300(args, rank, local, world, dist):
     import numpy as np
     import torch
@@ -221,7 +273,8 @@ def run_gb300(args, rank, local, world, dist):
 
     torch.cuda.set_device(local)
     w = workload(rank)
-    s = G.Sampler(w, device=local, mixed=(args.precision == "mixed"))
+    mixed = args.precision == "mixed"
+    s = G.Sampler(w, device=local, mixed=mixed)
     bm_pass = s.bead_moves_per_pass()
     seed = 1000 + rank
     ext = torch.cuda.ExternalStream(s.stream(), device=torch.device("cuda", local))
@@ -235,23 +288,9 @@ def run_gb300(args, rank, local, world, dist):
     clocks.start()
     time.sleep(0.3)
     l0 = s.launch_count()
-    evs = []
-    with torch.cuda.stream(ext):
-        for k in range(args.steps):
-            flush.zero_()                         # L2 flush outside the timed events
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(ext)
-            s.run_passes(1, seed)
-            e1.record(ext)
-            evs.append((e0, e1))
-    s.synchronize()
-    torch.cuda.synchronize()
+    total_ms = timed_passes(s, seed, args.steps, flush, ext, dist)
     l1 = s.launch_count()
     ck = clocks.stop()
-    barrier(dist)
-    step_ms = [a.elapsed_time(b) for a, b in evs]
-    total_ms = reduce_max(dist, sum(step_ms))
     value = bm_pass * args.steps * world / (total_ms / 1e3)
     tot, acc = s.counters()
 
@@ -259,7 +298,6 @@ def run_gb300(args, rank, local, world, dist):
     ms, nl = s.profile_pass(seed + 7)
     kinds = ["centroid", "bisection", "rotation"]
     dom = int(np.argmax(ms))
-    mixed = args.precision == "mixed"
     bytes_pass = [centroid_pass_bytes(w, mixed), bisection_pass_bytes(w, mixed), rotation_pass_bytes(w, mixed)]
     knames = ["k_mol_pairs (centroid partner sums)", "k_bisect_block (bisection block, one CTA per window)",
               "k_rot_slices (persistent rotational sweeps, one CTA per slice)"]
@@ -276,39 +314,37 @@ def run_gb300(args, rank, local, world, dist):
                 "launches_by_kind": {k: int(v) for k, v in zip(kinds, nl)}}
 
     # ---- end to end through the C ABI with host buffers
-    c, a, co, p = s.get_state()
-    pin_c = torch.from_numpy(c).pin_memory().numpy()
-    pin_a = torch.from_numpy(a).pin_memory().numpy()
-    out_c = torch.empty(c.shape, dtype=torch.float64).pin_memory().numpy()
-    out_a = torch.empty(a.shape, dtype=torch.float64).pin_memory().numpy()
-    out_co = torch.empty(c.shape, dtype=torch.float64).pin_memory().numpy()
-    out_p = np.zeros(w.natoms, np.int32)
-    est = np.zeros(5)
-    barrier(dist)
-    t0 = time.perf_counter()
-    for k in range(args.e2e_steps):
-        G._chk(s.L.pimc_set_state(s.h, G.dptr(pin_c), G.dptr(pin_a), G.iptr(p)), "set_state")
-        s.run_passes(1, seed + 11)
-        G._chk(s.L.pimc_get_state(s.h, G.dptr(out_c), G.dptr(out_a), G.dptr(out_co), G.iptr(out_p)), "get_state")
-        G._chk(s.L.pimc_estimators(s.h, G.dptr(est)), "estimators")
-        pin_c[...] = out_c
-        pin_a[...] = out_a
-    e2e_s = reduce_max(dist, time.perf_counter() - t0)
-    e2e = {"value": bm_pass * args.e2e_steps * world / e2e_s, "unit": UNIT,
-           "h2d_bytes_per_step": int(pin_c.nbytes + pin_a.nbytes + p.nbytes),
-           "d2h_bytes_per_step": int(out_c.nbytes + out_a.nbytes + out_co.nbytes + out_p.nbytes + est.nbytes),
-           "steps": args.e2e_steps, "path": "pimc_set_state + pimc_run_passes(1) + pimc_get_state + pimc_estimators"}
+    e2e = e2e_passes(s, w, seed + 11, args.e2e_steps, dist)
     s.close()
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if not mixed else "f32+f64",
             "data": "synthetic (seeded tables and paths of the config shapes; no dataset)",
             "config": {"workload": WORKLOAD, "bead_moves_per_pass": bm_pass, "precision": args.precision,
                        "replicas": world, "l2": "flushed between timed steps (256 MiB write)",
                        "accept_ratios": {"pH2 centroid": acc[0] / max(1, tot[0]), "pH2 bisection": acc[1] / max(1, tot[1]),
                                          "rotor bisection": acc[4] / max(1, tot[4]), "rotation": acc[5] / max(1, tot[5])}},
             "roofline": roofline, "e2e": e2e, "gpu_launches": int(l1 - l0), "clocks": ck}
+
+    # ---- the other precision of the same path, measured the same way
+    if not args.no_companion:
+        other = "fp64" if mixed else "mixed"
+        s2 = G.Sampler(w, device=local, mixed=not mixed)
+        ext2 = torch.cuda.ExternalStream(s2.stream(), device=torch.device("cuda", local))
+        s2.run_passes(args.warmup, seed)
+        s2.synchronize()
+        barrier(dist)
+        t2 = timed_passes(s2, seed, args.steps, flush, ext2, dist)
+        ms2, _ = s2.profile_pass(seed + 7)
+        e2 = e2e_passes(s2, w, seed + 11, args.e2e_steps, dist)
+        s2.close()
+        line["companion"] = {
+            "precision": other, "dtype": "f32+f64" if other == "mixed" else "f64",
+            "what": ("FP32 table interpolation and partner sums, FP64 action differences, exponents, "
+                     "accept tests and path" if other == "mixed" else "all arithmetic in FP64 as the reference"),
+            "value": bm_pass * args.steps * world / (t2 / 1e3), "unit": UNIT, "ms_per_step": t2 / args.steps,
+            "pass_ms_by_kind": {k: round(v, 3) for k, v in zip(kinds, ms2)}, "e2e": e2["value"]}
     return line, w
 
 

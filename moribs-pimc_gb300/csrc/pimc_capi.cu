@@ -322,12 +322,13 @@ extern "C" pimc_status pimc_destroy(pimc_handle *h)
 
 // ------------------------------------------------------------ tables
 
-extern "C" pimc_status pimc_load_tables(pimc_handle *h, const pimc_tables *tb)
+// The tables of the system d into t, buffers owned by h.  parts bit 0: the
+// potentials (1D, 2D, 3D, spherical), bit 1: the rotational density
+// matrices (linear-rotor .rot spline, top (theta, phi, chi) grid).
+#define TAB_POT 1
+#define TAB_ROT 2
+static pimc_status load_tables_into(pimc_handle *h, const pimc_tables *tb, DevTables &t, const DevSys &d, int parts)
 {
-  if (!h || !tb) return PIMC_ERR_BAD_ARG;
-  CK(cudaSetDevice(h->device));
-  DevTables &t = h->ctx.t;
-  const DevSys &d = h->ctx.s;
   pimc_status e;
   bool need1d = false, need2d = false, need3d = false, needrot = false, need3drho = false;
   for (int k = 0; k < d.ntypes; k++) {
@@ -340,6 +341,8 @@ extern "C" pimc_status pimc_load_tables(pimc_handle *h, const pimc_tables *tb)
     }
   }
   if (need1d && d.numb[0] < 2) need1d = false;                     // a single atom has no atom partner
+  if (!(parts & TAB_POT)) need1d = need2d = need3d = false;
+  if (!(parts & TAB_ROT)) needrot = need3drho = false;
   if (need1d) {
     int n = tb->n1d;
     if (n < 2 || !tb->grid1d || !tb->pot1d) return PIMC_ERR_BAD_TABLE;
@@ -423,7 +426,7 @@ extern "C" pimc_status pimc_load_tables(pimc_handle *h, const pimc_tables *tb)
       t.f_irstep = (float)(1.0 / t.rvstep);
     }
   }
-  if (d.ispher && d.ntypes > 1) {
+  if ((parts & TAB_POT) && d.ispher && d.ntypes > 1) {
     if (tb->nsph < 2 || !tb->sph_table || tb->sph_rstep <= 0) return PIMC_ERR_BAD_TABLE;
     t.nsph = tb->nsph; t.sph_r0 = tb->sph_r0; t.sph_rmax = tb->sph_rmax; t.sph_rstep = tb->sph_rstep;
     if ((e = upload(h, tb->sph_table, tb->nsph, &t.sph))) return e;
@@ -483,6 +486,23 @@ extern "C" pimc_status pimc_load_tables(pimc_handle *h, const pimc_tables *tb)
   t.f_dscale[0] = t.dthd > 0 ? (float)(deg / t.dthd) : 0.f;
   t.f_dscale[1] = t.dphd > 0 ? (float)(deg / t.dphd) : 0.f;
   t.f_dscale[2] = t.dchd > 0 ? (float)(deg / t.dchd) : 0.f;
+  t.d_thscale = t.dth3 > 0 ? deg / t.dth3 : 0.0;
+  t.d_chscale = t.dch3 > 0 ? deg / t.dch3 : 0.0;
+  t.d_irstep = t.rvstep > 0 ? 1.0 / t.rvstep : 0.0;
+  t.d_idr2d = t.dr2d > 0 ? 1.0 / t.dr2d : 0.0;
+  t.d_idc2d = t.dc2d > 0 ? 1.0 / t.dc2d : 0.0;
+  t.d_dscale[0] = t.dthd > 0 ? deg / t.dthd : 0.0;
+  t.d_dscale[1] = t.dphd > 0 ? deg / t.dphd : 0.0;
+  t.d_dscale[2] = t.dchd > 0 ? deg / t.dchd : 0.0;
+  return PIMC_OK;
+}
+
+extern "C" pimc_status pimc_load_tables(pimc_handle *h, const pimc_tables *tb)
+{
+  if (!h || !tb) return PIMC_ERR_BAD_ARG;
+  CK(cudaSetDevice(h->device));
+  pimc_status e = load_tables_into(h, tb, h->ctx.t, h->ctx.s, TAB_POT | TAB_ROT);
+  if (e) return e;
   CK(cudaStreamSynchronize(h->stream));
   h->tables = true;
   if (h->pass_exec) { cudaGraphExecDestroy(h->pass_exec); h->pass_exec = nullptr; }
@@ -925,9 +945,8 @@ static long long launch_centroid(pimc_handle *h, const PassPlan &pl, uint64_t se
     for (int a = 0; a < d.numb[t]; a++) {
       ReplaySrc none{};
       none.err = h->ctx.st.err;
-      launch_mol(h->ctx, h->frames, t, a, false, none, seed, h->pass, mol_phase + (unsigned)t, h->ms, nullptr, nullptr,
-                 h->cnt, h->stream);
-      n += 3;
+      n += launch_mol(h->ctx, h->frames, t, a, false, none, seed, h->pass, mol_phase + (unsigned)t, h->ms, nullptr,
+                      nullptr, h->cnt, h->stream);
     }
   return n;
 }

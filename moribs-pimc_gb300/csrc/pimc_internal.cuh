@@ -65,6 +65,9 @@ struct DevTables {
   const float4 *vtab4;          // 3D point: value and its one-sided differences along r, theta, chi
   float f_irstep;
   const float4 *rho4;           // top density point: value and differences along chi, phi, theta
+  // reciprocals of grid steps for the double-precision leaves: a division by
+  // a grid constant becomes a multiplication (within an ulp of the quotient)
+  double d_thscale, d_chscale, d_irstep, d_idr2d, d_idc2d, d_dscale[3];
 };
 
 struct DevSys {
@@ -225,10 +228,17 @@ __device__ __forceinline__ double splint(const double *__restrict__ xa, const do
   int klo = spline_klo(xa, n, x, uni, x0, ih), khi = klo + 1;
   double xk = __ldg(xa + khi), xl = __ldg(xa + klo);
   double h = xk - xl;
-  double a = (xk - x) / h;
-  double b = (x - xl) / h;
+  double a, b;
+  if (uni) {
+    // uniform grid: the step's reciprocal instead of two divisions
+    a = (xk - x) * ih;
+    b = (x - xl) * ih;
+  } else {
+    a = (xk - x) / h;
+    b = (x - xl) / h;
+  }
   return a * __ldg(ya + klo) + b * __ldg(ya + khi) +
-         ((a * a * a - a) * __ldg(y2a + klo) + (b * b * b - b) * __ldg(y2a + khi)) * (h * h) / 6.;
+         ((a * a * a - a) * __ldg(y2a + klo) + (b * b * b - b) * __ldg(y2a + khi)) * (h * h) * (1.0 / 6.0);
 }
 
 // SPot1D (mc_poten.cc:624-639)
@@ -243,8 +253,8 @@ __device__ __forceinline__ double spot1d(const DevTables &t, double r)
 __device__ __forceinline__ double lpot2d(const DevTables &t, double r, double cost)
 {
   double rmin = __ldg(t.rg2d), cmin = __ldg(t.cg2d);
-  int ir = (int)floor((r - rmin) / t.dr2d);
-  int ic = (int)floor((cost - cmin) / t.dc2d);
+  int ir = (int)floor((r - rmin) * t.d_idr2d);
+  int ic = (int)floor((cost - cmin) * t.d_idc2d);
   if (ir < 0) ir = 0;
   else if (ir >= t.nr2d - 1) ir = t.nr2d - 2;
   if (ic < 0) ic = 0;
@@ -254,8 +264,10 @@ __device__ __forceinline__ double lpot2d(const DevTables &t, double r, double co
   double y2 = __ldg(p + t.nc2d), y3 = __ldg(p + t.nc2d + 1);
   double r1 = __ldg(t.rg2d + ir), r2 = __ldg(t.rg2d + ir + 1);
   double c1 = __ldg(t.cg2d + ic), c2 = __ldg(t.cg2d + ic + 1);
-  double dr = (r - r1) / (r2 - r1);
-  double dc = (cost - c1) / (c2 - c1);
+  (void)r2;
+  (void)c2;
+  double dr = (r - r1) * t.d_idr2d;          // (r - r1) / (r2 - r1) on the uniform grid
+  double dc = (cost - c1) * t.d_idc2d;
   return (1.0 - dr) * (1.0 - dc) * y1 + dr * (1.0 - dc) * y2 + dr * dc * y3 + (1.0 - dr) * dc * y4;
 }
 
@@ -308,10 +320,11 @@ __device__ __forceinline__ void deleul(const double m1[9], const double m2in[9],
     schi = within1(m2[1]);
     chi2 = (schi > 0.0) ? acos(cchi) : 2.0 * pi - acos(cchi);
   } else {
-    double cphi = within1(m2[2] / sint);
-    double sphi = within1(m2[5] / sint);
-    cchi = within1(-m2[6] / sint);
-    schi = within1(m2[7] / sint);
+    double isint = 1.0 / sint;
+    double cphi = within1(m2[2] * isint);
+    double sphi = within1(m2[5] * isint);
+    cchi = within1(-m2[6] * isint);
+    schi = within1(m2[7] * isint);
     phi2 = (sphi > 0.0) ? acos(cphi) : 2.0 * pi - acos(cphi);
     chi2 = (schi > 0.0) ? acos(cchi) : 2.0 * pi - acos(cchi);
   }
@@ -334,11 +347,7 @@ __device__ __forceinline__ double rotden_rho(const DevTables &t, const Frame &f1
 {
   double rel[3];
   deleul(f1.m, f2.m, rel);
-  const double pi = PIMC_PI;
-  double phi = rel[0] * 180.0 / pi;
-  double theta = rel[1] * 180.0 / pi;
-  double chi = rel[2] * 180.0 / pi;
-  double xc = chi / t.dchd, xp = phi / t.dphd, xt = theta / t.dthd;
+  double xt = rel[1] * t.d_dscale[0], xp = rel[0] * t.d_dscale[1], xc = rel[2] * t.d_dscale[2];
   int ichi = (int)xc, iphi = (int)xp, ith = (int)xt;
   if (ichi > t.nch - 1 || ichi < 0) { ichi = 0; *bad = 1; }
   if (iphi > t.nph - 1 || iphi < 0) { iphi = 0; *bad = 1; }
@@ -437,14 +446,14 @@ __device__ __forceinline__ double vcord(const DevTables &t, const Frame &f, doub
     chiwff = chir;
   }
   if (rr) { *rr = rn; *th = thewff; *chr = chir; }
-  double r = rn / bo2ang;
-  double xth = (thewff * 180.0 / pi) / t.dth3;
-  double xch = (chiwff * 180.0 / pi) / t.dch3;
+  double r = rn * (1.0 / bo2ang);
+  double xth = thewff * t.d_thscale;           // (theta * 180 / pi) / dth
+  double xch = chiwff * t.d_chscale;
   // vcalc
   int maxrpt = t.rgrd - 1, mxthpt = t.thgrd - 1, mxchpt = t.chgrd - 1;
   if (r < t.rvmin) r = t.rvmin;
   if (r > t.rvmax) r = t.rvmax;
-  int ir = (int)((r - t.rvmin) / t.rvstep);
+  int ir = (int)((r - t.rvmin) * t.d_irstep);
   if (ir > maxrpt) ir = maxrpt;
   int ith = (int)xth, ich = (int)xch;
   if (ich > mxchpt) ich = mxchpt;
@@ -456,7 +465,7 @@ __device__ __forceinline__ double vcord(const DevTables &t, const Frame &f, doub
   double v0 = __ldg(t.vtab + i0);
   double gradr = 0.0, delr = 0.0, gradth = 0.0, delth = 0.0, gradch = 0.0, delch = 0.0;
   if (ir < maxrpt) {
-    gradr = (__ldg(t.vtab + i0 + nth * nch) - v0) / t.rvstep;
+    gradr = (__ldg(t.vtab + i0 + nth * nch) - v0) * t.d_irstep;
     delr = r - (t.rvmin + ir * t.rvstep);
   }
   if (ith < mxthpt) {

@@ -319,36 +319,44 @@ __global__ void __launch_bounds__(PIMC_ROT_THREADS) k_rot_sweeps(Ctx c, Frame *f
 }
 
 // ------------------------------------------------------------ centroid move
-// MCMolecularMove (mc_piqmc.cc:54-102) split in three launches per atom:
-// propose (3 displacements), partner sums over all slices, accept/commit.
+// MCMolecularMove (mc_piqmc.cc:54-102): replay as propose (the three rnd1()
+// displacements), partner sums over all slices, accept/commit; production
+// as partner sums (each CTA draws the displacement itself) and accept/commit
+// on several CTAs (each takes the same decision from the same sums and
+// commits its share of the slices).
 template <bool REPLAY>
 __global__ void k_mol_propose(Ctx c, int type, ReplaySrc src, uint64_t seed, const unsigned *pass, unsigned phase,
                               int atom, MolScratch *ms)
 {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  for (int d = 0; d < 3; d++) {
-    double u;
-    if (REPLAY) u = src.disp_u(d);
-    else {
-      PhiloxSrc ps{seed, ((uint64_t)(*pass) << 32) | ((uint64_t)phase << 12) | (uint64_t)atom};
-      u = ps.disp_u(d);
-    }
-    ms->disp[d] = c.s.mcstep[type] * (u - 0.5);
+  if (REPLAY) {
+    for (int d = 0; d < 3; d++) ms->disp[d] = c.s.mcstep[type] * (src.disp_u(d) - 0.5);
+  } else {
+    mol_disp(c.s, type, seed, *pass, phase, atom, ms->disp);
   }
 }
 
-// CTA = one partner atom1; threads over slices; new = old + disp; the two
-// whole-path sums are reduced warp by warp in a fixed order
-template <bool MIX>
-__global__ void __launch_bounds__(PIMC_BLOCK) k_mol_pairs(Ctx c, Frame *frames, int gatom, MolScratch *ms)
+// CTA (partner atom1, slice chunk); threads over the chunk's slices; new =
+// old + disp; both whole-path partial sums reduced in a fixed order
+template <bool MIX, bool PROD>
+__global__ void __launch_bounds__(PIMC_BLOCK) k_mol_pairs(Ctx c, Frame *frames, int type, int atom, int gatom,
+                                                          MolScratch *ms, int nchunk, uint64_t seed,
+                                                          const unsigned *pass, unsigned phase)
 {
   __shared__ double part[2][PIMC_BLOCK / 32];
-  int a1 = blockIdx.x;
-  int tid = threadIdx.x;
+  __shared__ double dd[3];
+  const int a1 = blockIdx.x, ch = blockIdx.y;
+  const int tid = threadIdx.x;
+  const int t0 = (int)((long)ch * c.s.P / nchunk), t1 = (int)((long)(ch + 1) * c.s.P / nchunk);
+  if (tid == 0) {
+    if (PROD) mol_disp(c.s, type, seed, *pass, phase, atom, dd);
+    else { dd[0] = ms->disp[0]; dd[1] = ms->disp[1]; dd[2] = ms->disp[2]; }
+  }
+  __syncthreads();
   double an = 0.0, ao = 0.0;
   if (a1 != gatom) {
-    double d0 = ms->disp[0], d1 = ms->disp[1], d2 = ms->disp[2];
-    for (int it = tid; it < c.s.P; it += blockDim.x) {
+    const double d0 = dd[0], d1 = dd[1], d2 = dd[2];
+    for (int it = t0 + tid; it < t1; it += blockDim.x) {
       size_t i = sidx(c.s, it, gatom);
       if (MIX) {
         const float4 p4 = c.st.b4[i];
@@ -371,21 +379,35 @@ __global__ void __launch_bounds__(PIMC_BLOCK) k_mol_pairs(Ctx c, Frame *frames, 
   if (tid < 2) {
     double s = 0.0;
     for (int k = 0; k < (int)(blockDim.x >> 5); k++) s += part[tid][k];
-    ms->pair[tid][a1] = s;
+    ms->pair[tid][a1 * nchunk + ch] = s;
   }
 }
 
 template <bool REPLAY>
 __global__ void __launch_bounds__(PIMC_BLOCK) k_mol_finish(Ctx c, int type, int gatom, ReplaySrc src, uint64_t seed,
                                                             const unsigned *pass, unsigned phase, int atom,
-                                                            MolScratch *ms, double *dv_out, int *acc_out,
+                                                            MolScratch *ms, int nchunk, double *dv_out, int *acc_out,
                                                             unsigned long long *cnt)
 {
   __shared__ int acc;
+  __shared__ double sd[3];
+  __shared__ double wpart[2][PIMC_BLOCK / 32];
+  {
+    // the partials in a fixed tree: thread strides, warp shuffles, warps in order
+    const int np = c.s.na * nchunk;
+    double en = 0.0, eo = 0.0;
+    for (int i = threadIdx.x; i < np; i += blockDim.x)
+      if (i / nchunk != gatom) { en += ms->pair[0][i]; eo += ms->pair[1][i]; }
+    for (int o = 16; o > 0; o >>= 1) {
+      en += __shfl_xor_sync(0xffffffffu, en, o);
+      eo += __shfl_xor_sync(0xffffffffu, eo, o);
+    }
+    if ((threadIdx.x & 31) == 0) { wpart[0][threadIdx.x >> 5] = en; wpart[1][threadIdx.x >> 5] = eo; }
+    __syncthreads();
+  }
   if (threadIdx.x == 0) {
     double en = 0.0, eo = 0.0;
-    for (int a1 = 0; a1 < c.s.na; a1++)
-      if (a1 != gatom) { en += ms->pair[0][a1]; eo += ms->pair[1][a1]; }
+    for (int k = 0; k < (int)(blockDim.x >> 5); k++) { en += wpart[0][k]; eo += wpart[1][k]; }
     double deltav = 0.0;
     deltav += (en - eo);
     int a = 0;
@@ -400,19 +422,25 @@ __global__ void __launch_bounds__(PIMC_BLOCK) k_mol_finish(Ctx c, int type, int 
       if (exp(-deltav * c.s.tau) > u) a = 1;
     }
     acc = a;
-    if (dv_out) { dv_out[atom] = deltav; acc_out[atom] = a; }
-    cnt[(type * 3 + 0) * 2 + 0] += 1;
-    if (a) cnt[(type * 3 + 0) * 2 + 1] += 1;
+    if (REPLAY) { sd[0] = ms->disp[0]; sd[1] = ms->disp[1]; sd[2] = ms->disp[2]; }
+    else mol_disp(c.s, type, seed, *pass, phase, atom, sd);
+    if (blockIdx.x == 0) {
+      if (dv_out) { dv_out[atom] = deltav; acc_out[atom] = a; }
+      cnt[(type * 3 + 0) * 2 + 0] += 1;
+      if (a) cnt[(type * 3 + 0) * 2 + 1] += 1;
+    }
   }
   __syncthreads();
   if (acc) {
-    double d0 = ms->disp[0], d1 = ms->disp[1], d2 = ms->disp[2];
-    for (int it = threadIdx.x; it < c.s.P; it += blockDim.x) {
+    const double d0 = sd[0], d1 = sd[1], d2 = sd[2];
+    const int t0 = (int)((long)blockIdx.x * c.s.P / gridDim.x), t1 = (int)((long)(blockIdx.x + 1) * c.s.P / gridDim.x);
+    for (int it = t0 + threadIdx.x; it < t1; it += blockDim.x) {
       size_t i = sidx(c.s, it, gatom);
       store_bead(c, i, c.st.x[i] + d0, c.st.y[i] + d1, c.st.z[i] + d2);
     }
     // the whole path moved: every cached rotor potential is stale
-    for (int i = threadIdx.x; i < c.s.nrotors * c.s.Q; i += blockDim.x) c.st.rp_ok[i] = 0;
+    if (blockIdx.x == 0)
+      for (int i = threadIdx.x; i < c.s.nrotors * c.s.Q; i += blockDim.x) c.st.rp_ok[i] = 0;
   }
 }
 
@@ -667,7 +695,11 @@ __global__ void __launch_bounds__(PIMC_ROT_THREADS) k_rot_slices(Ctx c, Frame *f
                                                                  unsigned long long *cnt)
 {
   __shared__ RotShared sh;
-  const int Q = c.s.Q, q = blockIdx.x;
+  // CTAs [0, Q/2) take the even slices and [Q/2, Q) the odd ones, so that
+  // two CTAs sharing an SM (blocks b and b + #SMs) mostly have opposite
+  // parity: one prepares while the other finishes
+  const int Q = c.s.Q, half = Q >> 1, b = blockIdx.x;
+  const int q = (b < half) ? 2 * b : 2 * (b - half) + 1;
   const bool linear = c.s.molecule[c.s.imtype] == 1;
   const unsigned ps = *pass;
   const size_t n = (size_t)Q;
@@ -831,17 +863,31 @@ void launch_bisect_block(const Ctx &c, Frame *f, int type, int s0, unsigned phas
   else k_bisect_block<false><<<nwin, PIMC_BIS_THREADS, 0, s>>>(c, f, type, s0, phase0, seed, pass, cnt);
 }
 
-void launch_mol(const Ctx &c, Frame *f, int type, int atom, bool replay, ReplaySrc src, uint64_t seed,
-                const unsigned *pass, unsigned phase, MolScratch *ms, double *dv, int *acc, unsigned long long *cnt,
-                cudaStream_t s)
+int launch_mol(const Ctx &c, Frame *f, int type, int atom, bool replay, ReplaySrc src, uint64_t seed,
+               const unsigned *pass, unsigned phase, MolScratch *ms, double *dv, int *acc, unsigned long long *cnt,
+               cudaStream_t s)
 {
   int g = c.s.first[type] + atom;
-  if (replay) k_mol_propose<true><<<1, 32, 0, s>>>(c, type, src, seed, pass, phase, atom, ms);
-  else k_mol_propose<false><<<1, 32, 0, s>>>(c, type, src, seed, pass, phase, atom, ms);
-  if (c.s.mixed) k_mol_pairs<true><<<c.s.na, PIMC_BLOCK, 0, s>>>(c, f, g, ms);
-  else k_mol_pairs<false><<<c.s.na, PIMC_BLOCK, 0, s>>>(c, f, g, ms);
-  if (replay) k_mol_finish<true><<<1, PIMC_BLOCK, 0, s>>>(c, type, g, src, seed, pass, phase, atom, ms, dv, acc, cnt);
-  else k_mol_finish<false><<<1, PIMC_BLOCK, 0, s>>>(c, type, g, src, seed, pass, phase, atom, ms, dv, acc, cnt);
+  // slice chunks per partner: about two CTAs per SM over all partners
+  int nchunk = (2 * 152 + c.s.na - 1) / c.s.na;
+  if (nchunk > PIMC_MOL_MAXCHUNK) nchunk = PIMC_MOL_MAXCHUNK;
+  if (nchunk > c.s.P / 32) nchunk = c.s.P / 32;
+  if (nchunk < 1) nchunk = 1;
+  dim3 grid(c.s.na, nchunk);
+  if (replay) {
+    k_mol_propose<true><<<1, 32, 0, s>>>(c, type, src, seed, pass, phase, atom, ms);
+    if (c.s.mixed) k_mol_pairs<true, false><<<grid, PIMC_BLOCK, 0, s>>>(c, f, type, atom, g, ms, nchunk, seed, pass, phase);
+    else k_mol_pairs<false, false><<<grid, PIMC_BLOCK, 0, s>>>(c, f, type, atom, g, ms, nchunk, seed, pass, phase);
+    k_mol_finish<true><<<1, PIMC_BLOCK, 0, s>>>(c, type, g, src, seed, pass, phase, atom, ms, nchunk, dv, acc, cnt);
+    return 3;
+  }
+  if (c.s.mixed) k_mol_pairs<true, true><<<grid, PIMC_BLOCK, 0, s>>>(c, f, type, atom, g, ms, nchunk, seed, pass, phase);
+  else k_mol_pairs<false, true><<<grid, PIMC_BLOCK, 0, s>>>(c, f, type, atom, g, ms, nchunk, seed, pass, phase);
+  int nfin = c.s.P / 256;
+  if (nfin < 1) nfin = 1;
+  if (nfin > 8) nfin = 8;
+  k_mol_finish<false><<<nfin, PIMC_BLOCK, 0, s>>>(c, type, g, src, seed, pass, phase, atom, ms, nchunk, dv, acc, cnt);
+  return 2;
 }
 
 void launch_q_slice(const Ctx &c, Frame *f, int n, const int *a0, const int *it, const double *xyz, double *out,

@@ -412,10 +412,19 @@ __device__ int bisect_move(const Ctx &c, const Frame *frames, int type, int atom
 // scratch of one centroid move: the displacement and per-partner whole-path
 // sums for the displaced and the current path
 #define PIMC_MAX_ATOMS 1024
+#define PIMC_MOL_MAXCHUNK 8           /* slice chunks per partner in a centroid move */
 struct MolScratch {
   double disp[3];
-  double pair[2][PIMC_MAX_ATOMS];
+  double pair[2][PIMC_MAX_ATOMS * PIMC_MOL_MAXCHUNK];   // [new/old][partner * nchunk + chunk]
 };
+
+// the displacement of a production centroid move (every CTA draws the same)
+__device__ __forceinline__ void mol_disp(const DevSys &s, int type, uint64_t seed, unsigned pass, unsigned phase,
+                                         int atom, double d[3])
+{
+  PhiloxSrc ps{seed, ((uint64_t)pass << 32) | ((uint64_t)phase << 12) | (uint64_t)atom};
+  for (int k = 0; k < 3; k++) d[k] = s.mcstep[type] * (ps.disp_u(k) - 0.5);
+}
 
 // ------------------------------------------------------ rotational moves
 // A rotational move runs on PIMC_ROT_THREADS threads in two stages.
@@ -655,6 +664,71 @@ __device__ __forceinline__ void rot_uniforms(uint64_t seed, unsigned pass, unsig
   if (linear) u[2] = u[3];
 }
 
+// The acceptance of a rotational move from its four link densities (old
+// (q-1,q), old (q,q+1), new, new), the potentials, the Boltzmann factor
+// boltz = exp(-tau (pot_new - pot_old)) (Noya densities) or its exponent
+// (RS densities) and log u (RS): MCRotLinStep mc_piqmc.cc:838-921,
+// MCRot3Dstep mc_piqmc.cc:1021-1178.  Returns 1 if accepted; *neg is set for a
+// negative linear-rotor density (the reference's nrerror).
+template <bool MIX>
+__device__ __forceinline__ int rot_decide(const DevSys &s, bool linear, const double rho[4], double pot_old,
+                                          double pot_new, double boltz, double logu, const double u[4], double *rd_out,
+                                          int *neg_out)
+{
+  double rd;
+  int acc = 0, neg = 0;
+  if (MIX && s.rot_den_type == 0) {
+    // the FP32 path: the table densities and their ratio in float
+    float dens_old = (float)rho[0] * (float)rho[1], dens_new = (float)rho[2] * (float)rho[3];
+    if (fabsf(dens_old) < (float)PIMC_RZERO) dens_old = 0.0f;
+    if (fabsf(dens_new) < (float)PIMC_RZERO) dens_new = 0.0f;
+    if (linear) {
+      if (dens_old < 0.0f || dens_new < 0.0f) neg = 1;
+    } else {
+      dens_old = fabsf(dens_old);
+      dens_new = fabsf(dens_new);
+    }
+    float rf = (dens_old > (float)PIMC_RZERO) ? dens_new / dens_old : 1.0f;
+    rd = (double)rf * boltz;                                  // FP64 Boltzmann factor
+    acc = (rd > 1.0) || (rd > u[linear ? 2 : 3]);
+  } else if (s.rot_den_type == 0) {
+    double dens_old = rho[0] * rho[1], dens_new = rho[2] * rho[3];
+    if (fabs(dens_old) < PIMC_RZERO) dens_old = 0.0;
+    if (fabs(dens_new) < PIMC_RZERO) dens_new = 0.0;
+    if (linear) {
+      if (dens_old < 0.0 || dens_new < 0.0) neg = 1;          // mc_piqmc.cc:850,886
+    } else {
+      if (dens_old < 0.0) dens_old = fabs(dens_old);          // mc_piqmc.cc:1067,1133
+      if (dens_new < 0.0) dens_new = fabs(dens_new);
+    }
+    rd = (dens_old > PIMC_RZERO) ? dens_new / dens_old : 1.0;
+    rd *= boltz;                                              // exp(-tau (pot_new - pot_old))
+    acc = (rd > 1.0) || (rd > u[linear ? 2 : 3]);
+  } else if (linear) {
+    double dens_old = rho[0] + rho[1], dens_new = rho[2] + rho[3];
+    if (fabs(dens_old) < PIMC_RZERO) dens_old = 0.0;
+    if (fabs(dens_new) < PIMC_RZERO) dens_new = 0.0;
+    rd = dens_new - dens_old + boltz;                         // - tau (pot_new - pot_old)
+    acc = (rd > 0.0) || (rd > logu);
+  } else {
+    double rhoold = rho[0] + rho[1], rhonew = rho[2] + rho[3];
+    rd = (rhonew - rhoold) / (4.0 * (s.rot_tau / PIMC_WNO2K));
+    rd += boltz;                                              // - tau (pot_new - pot_old)
+    acc = (rd > 0.0) || (rd > logu);
+  }
+  (void)pot_old;
+  (void)pot_new;
+  *rd_out = rd;
+  *neg_out = neg;
+  return acc;
+}
+
+// Boltzmann factor (Noya densities) or exponent (RS densities) of a move
+__device__ __forceinline__ double rot_boltz(const DevSys &s, double pot_old, double pot_new)
+{
+  return (s.rot_den_type == 0) ? exp(-s.tau * (pot_new - pot_old)) : -(s.tau * (pot_new - pot_old));
+}
+
 // MCRotLinStep (mc_piqmc.cc:781-936) / MCRot3Dstep (mc_piqmc.cc:938-1199),
 // first stage, for rotor g0 at rotational slice q with uniforms u (3 for a
 // linear rotor, 4 for a top) and the proposal prop = rot_propose(current
@@ -874,49 +948,10 @@ __device__ int rot_finish(const Ctx &c, Frame *frames, int g0, int q, bool linea
       }
       __syncwarp();
       if (lane == 0) {
-        const double *u = sh.u;
         const double pot_old = sh.pot_old, pot_new = sh.pot_new;
         double rd;
-        int acc = 0, neg = 0;
-        if (MIX && s.rot_den_type == 0) {
-          // the FP32 path: the table densities and their ratio in float
-          float dens_old = (float)sh.rho[0] * (float)sh.rho[1], dens_new = (float)sh.rho[2] * (float)sh.rho[3];
-          if (fabsf(dens_old) < (float)PIMC_RZERO) dens_old = 0.0f;
-          if (fabsf(dens_new) < (float)PIMC_RZERO) dens_new = 0.0f;
-          if (linear) {
-            if (dens_old < 0.0f || dens_new < 0.0f) neg = 1;
-          } else {
-            dens_old = fabsf(dens_old);
-            dens_new = fabsf(dens_new);
-          }
-          float rf = (dens_old > (float)PIMC_RZERO) ? dens_new / dens_old : 1.0f;
-          rd = (double)rf * sh.boltz;                              // FP64 Boltzmann factor
-          acc = (rd > 1.0) || (rd > u[linear ? 2 : 3]);
-        } else if (s.rot_den_type == 0) {
-          double dens_old = sh.rho[0] * sh.rho[1], dens_new = sh.rho[2] * sh.rho[3];
-          if (fabs(dens_old) < PIMC_RZERO) dens_old = 0.0;
-          if (fabs(dens_new) < PIMC_RZERO) dens_new = 0.0;
-          if (linear) {
-            if (dens_old < 0.0 || dens_new < 0.0) neg = 1;          // mc_piqmc.cc:850,886
-          } else {
-            if (dens_old < 0.0) dens_old = fabs(dens_old);          // mc_piqmc.cc:1067,1133
-            if (dens_new < 0.0) dens_new = fabs(dens_new);
-          }
-          rd = (dens_old > PIMC_RZERO) ? dens_new / dens_old : 1.0;
-          rd *= sh.boltz;                                          // exp(-tau (pot_new - pot_old))
-          acc = (rd > 1.0) || (rd > u[linear ? 2 : 3]);
-        } else if (linear) {
-          double dens_old = sh.rho[0] + sh.rho[1], dens_new = sh.rho[2] + sh.rho[3];
-          if (fabs(dens_old) < PIMC_RZERO) dens_old = 0.0;
-          if (fabs(dens_new) < PIMC_RZERO) dens_new = 0.0;
-          rd = dens_new - dens_old + sh.boltz;                    // - tau (pot_new - pot_old)
-          acc = (rd > 0.0) || (rd > sh.logu);
-        } else {
-          double rhoold = sh.rho[0] + sh.rho[1], rhonew = sh.rho[2] + sh.rho[3];
-          rd = (rhonew - rhoold) / (4.0 * (s.rot_tau / PIMC_WNO2K));
-          rd += sh.boltz;                                          // - tau (pot_new - pot_old)
-          acc = (rd > 0.0) || (rd > sh.logu);
-        }
+        int neg = 0;
+        int acc = rot_decide<MIX>(s, linear, sh.rho, pot_old, pot_new, sh.boltz, sh.logu, sh.u, &rd, &neg);
         if (neg) { atomicOr(c.st.err, (unsigned)DERR_NEG_DENSITY); acc = 0; }
         if (sh.bad) { atomicOr(c.st.err, (unsigned)DERR_GRID_RANGE); acc = 0; }
         sh.rd = rd;

@@ -26,9 +26,9 @@ cudaError_t launch_rot_sweeps(const Ctx &c, Frame *f, int nctas, int nhalf, unsi
                               unsigned long long *cnt, cudaStream_t s);
 void launch_bisect_block(const Ctx &c, Frame *f, int type, int s0, unsigned phase0, uint64_t seed,
                          const unsigned *pass, unsigned long long *cnt, cudaStream_t s);
-void launch_mol(const Ctx &c, Frame *f, int type, int atom, bool replay, ReplaySrc src, uint64_t seed,
-                const unsigned *pass, unsigned phase, MolScratch *ms, double *dv, int *acc, unsigned long long *cnt,
-                cudaStream_t s);
+int launch_mol(const Ctx &c, Frame *f, int type, int atom, bool replay, ReplaySrc src, uint64_t seed,
+               const unsigned *pass, unsigned phase, MolScratch *ms, double *dv, int *acc, unsigned long long *cnt,
+               cudaStream_t s);
 void launch_q_slice(const Ctx &c, Frame *f, int n, const int *a0, const int *it, const double *xyz, double *out,
                     cudaStream_t s);
 void launch_q_rot(const Ctx &c, Frame *f, int n, const int *rot, const int *it, const double *v3, int linear,

@@ -51,7 +51,8 @@ def build(verbose=False, extra=()):
 
     with ThreadPoolExecutor(len(SOURCES)) as ex:
         objs = list(ex.map(comp, SOURCES))
-    cmd = [nvcc(), *ARCH, "-shared", "-o", OUT, *objs, "-lcudart"]
+    # --no-undefined: a missing definition fails the build, not the first load
+    cmd = [nvcc(), *ARCH, "-shared", "-Xlinker", "--no-undefined", "-o", OUT, *objs, "-lcudart"]
     if verbose:
         print(" ".join(cmd))
     subprocess.check_call(cmd)
