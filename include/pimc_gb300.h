@@ -130,6 +130,39 @@ long long   pimc_launch_count(const pimc_handle *h);
 void       *pimc_stream(const pimc_handle *h);
 const char *pimc_status_string(pimc_status s);
 
+/* ---- replica batches (no reference counterpart) --------------------------
+ * Many independent systems of one species family -- the same types,
+ * molecules, masses, levels (<= 4) and steps, each with its own particle
+ * counts, slices, rotational slices and temperature -- sampled in one
+ * persistent launch: the reference's run of one system repeated for each
+ * replica.  Shared potentials come from tables[0]; each replica's rotational
+ * density (a .rot or top density at its own tau) from tables[r].  A replica's
+ * moves and uniforms are those of a single handle of the same system run
+ * with seed pimc_batch_replica_seed(seed, r). */
+typedef struct pimc_batch pimc_batch;
+pimc_status pimc_batch_create(int n, const pimc_system *systems, int device, pimc_batch **out);
+pimc_status pimc_batch_destroy(pimc_batch *b);
+pimc_status pimc_batch_load_tables(pimc_batch *b, const pimc_tables *tables);
+pimc_status pimc_batch_set_state(pimc_batch *b, int replica, const double *coords, const double *angles,
+                                 const int *pindex);
+pimc_status pimc_batch_get_state(pimc_batch *b, int replica, double *coords, double *angles, double *cosine,
+                                 int *pindex);
+pimc_status pimc_batch_set_precision(pimc_batch *b, int mixed);
+/* warps per CTA (2, 4 or 8); pimc_batch_autotune times one pass of each and
+ * keeps the fastest (the passes run: the replicas move on) */
+pimc_status pimc_batch_set_shape(pimc_batch *b, int warps);
+pimc_status pimc_batch_autotune(pimc_batch *b, uint64_t seed, int *warps_out, double *ms_out);
+pimc_status pimc_batch_run_passes(pimc_batch *b, int npasses, uint64_t seed);
+/* per replica 4 values: E_kin, E_pot, E_rot (as pimc_estimators out[0..2])
+ * and the mean z component of the rotor axis over the rotational slices */
+pimc_status pimc_batch_estimators(pimc_batch *b, double *out);
+/* MCTotal / MCAccep summed over the replicas (layout of pimc_counters) */
+pimc_status pimc_batch_counters(pimc_batch *b, double *total, double *accep);
+pimc_status pimc_batch_synchronize(pimc_batch *b);
+double      pimc_batch_bead_moves_per_pass(const pimc_batch *b);
+uint64_t    pimc_batch_replica_seed(uint64_t seed, int replica);
+void       *pimc_batch_stream(const pimc_batch *b);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,6 +1,7 @@
 // pimc_capi.cu -- the extern "C" entry points of include/pimc_gb300.h: handle
 // life cycle, table preparation, path transfers, replay moves, energy
 // queries, estimators and the graph-captured production pass.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -182,11 +183,10 @@ static bool near_uniform(const double *x, int n, double *x0, double *ih)
 
 // ------------------------------------------------------------ life cycle
 
-extern "C" pimc_status pimc_create(const pimc_system *sys, int device, pimc_handle **out)
+// validate a system and derive its device description (mc_setup.cc:135-163,
+// 321-453: counts, offsets, tau, RotRatio)
+static pimc_status build_devsys(const pimc_system &s, DevSys &d)
 {
-  if (!sys || !out) return PIMC_ERR_BAD_ARG;
-  *out = nullptr;
-  const pimc_system &s = *sys;
   if (s.ntypes < 1 || s.ntypes > PIMC_MAX_TYPES || s.nslices < 2 || s.temperature <= 0.0) return PIMC_ERR_BAD_ARG;
   int na = 0, imtype = -1, nmol = 0;
   for (int t = 0; t < s.ntypes; t++) {
@@ -204,17 +204,6 @@ extern "C" pimc_status pimc_create(const pimc_system *sys, int device, pimc_hand
   int Q = s.rotation ? s.nrotslices : 0;
   if (s.rotation && (imtype < 0 || Q < 1 || s.nslices % Q)) return PIMC_ERR_BAD_ARG;   // mc_setup.cc:382-389
   if (s.rotation && s.nslices / Q > 16) return PIMC_ERR_SIZE;
-  int ndev = 0;
-  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return PIMC_ERR_NO_DEVICE;
-  if (device < 0 || device >= ndev) return PIMC_ERR_BAD_ARG;
-
-  pimc_handle *h = new (std::nothrow) pimc_handle();
-  if (!h) return PIMC_ERR_SIZE;
-  h->device = device;
-  h->sys = s;
-  CK(cudaSetDevice(device));
-  CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
-  DevSys &d = h->ctx.s;
   memset(&d, 0, sizeof(d));
   d.na = na;
   d.nap = (na + 31) / 32 * 32;
@@ -257,7 +246,31 @@ extern "C" pimc_status pimc_create(const pimc_system *sys, int device, pimc_hand
   d.rot_eoff = s.rot_eoff;
   for (int k = 0; k < 3; k++) { d.abc[k] = s.rot_abc[k]; d.box[k] = s.box[k]; }
   d.minimage = s.minimage;
+  return PIMC_OK;
+}
 
+extern "C" pimc_status pimc_create(const pimc_system *sys, int device, pimc_handle **out)
+{
+  if (!sys || !out) return PIMC_ERR_BAD_ARG;
+  *out = nullptr;
+  const pimc_system &s = *sys;
+  DevSys dsys;
+  pimc_status e0 = build_devsys(s, dsys);
+  if (e0) return e0;
+  const int na = dsys.na;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return PIMC_ERR_NO_DEVICE;
+  if (device < 0 || device >= ndev) return PIMC_ERR_BAD_ARG;
+
+  pimc_handle *h = new (std::nothrow) pimc_handle();
+  if (!h) return PIMC_ERR_SIZE;
+  h->device = device;
+  h->sys = s;
+  CK(cudaSetDevice(device));
+  CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+  DevSys &d = h->ctx.s;
+  d = dsys;
+  int g;
   DevState &st = h->ctx.st;
   size_t nb = (size_t)d.P * d.nap;
   size_t nr = (size_t)(d.nrotors > 0 ? d.nrotors : 1) * d.Q;
@@ -1194,3 +1207,450 @@ extern "C" pimc_status pimc_pot_energy_noalloc(pimc_handle *h, int n, const int 
   CK(cudaMemcpyAsync(out, dout, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   return check_err(h);
 }
+
+// ------------------------------------------------------------ replica batches
+// A batch owns one base handle (device, stream, the shared potential tables
+// and every buffer, freed with it) and pools of per-replica state carved
+// into one BatchRep per replica.
+struct pimc_batch {
+  pimc_handle *base = nullptr;
+  int n = 0;
+  std::vector<pimc_system> sys;
+  std::vector<BatchRep> reps;
+  std::vector<int> state_set;
+  BatchRep *d_reps = nullptr;
+  int *d_order = nullptr;
+  unsigned *d_work = nullptr;
+  double *d_est = nullptr;
+  unsigned long long *d_cnt = nullptr;
+  unsigned *d_pass = nullptr;
+  int warps = 4;
+  int mixed = 0;
+  bool tables = false;
+  cudaGraphExec_t exec = nullptr;
+  uint64_t exec_seed = 0;
+  int exec_warps = 0, exec_mixed = -1;
+  double bm_pass = 0.0;
+};
+
+#define BK(x)                                                  \
+  do {                                                         \
+    cudaError_t e_ = (x);                                      \
+    if (e_ != cudaSuccess) {                                   \
+      b->base->last_cuda = e_;                                 \
+      return PIMC_ERR_CUDA;                                    \
+    }                                                          \
+  } while (0)
+
+extern "C" uint64_t pimc_batch_replica_seed(uint64_t seed, int r)
+{
+  return seed ^ (0x9E3779B97F4A7C15ull * (uint64_t)(r + 1));
+}
+
+template <class T>
+static pimc_status pool(pimc_handle *h, T **p, size_t n)
+{
+  pimc_status e = dalloc(h, p, n > 0 ? n : 1);
+  if (e) return e;
+  h->owned.push_back(*p);
+  CK(cudaMemset(*p, 0, (n > 0 ? n : 1) * sizeof(T)));
+  return PIMC_OK;
+}
+
+static double system_bead_moves(const DevSys &d, bool rotation)
+{
+  double bm = 0.0;
+  for (int t = 0; t < d.ntypes; t++) bm += (double)d.numb[t] * d.P * ((1 << d.levels[t]) - 1) + (double)d.numb[t] * d.P;
+  if (rotation) bm += (double)d.P * d.Q * d.nrotors;
+  return bm;
+}
+
+extern "C" pimc_status pimc_batch_create(int n, const pimc_system *systems, int device, pimc_batch **out)
+{
+  if (n < 1 || !systems || !out) return PIMC_ERR_BAD_ARG;
+  *out = nullptr;
+  const pimc_system &s0 = systems[0];
+  std::vector<DevSys> ds(n);
+  pimc_system smax = s0;
+  for (int r = 0; r < n; r++) {
+    const pimc_system &s = systems[r];
+    pimc_status e = build_devsys(s, ds[r]);
+    if (e) return e;
+    if (s.ntypes != s0.ntypes || s.rotation != s0.rotation || s.rot_den_type != s0.rot_den_type ||
+        s.ispher != s0.ispher || s.minimage != s0.minimage)
+      return PIMC_ERR_BAD_ARG;
+    for (int t = 0; t < s.ntypes; t++) {
+      const pimc_type &a = s.type[t], &c = s0.type[t];
+      if (a.molecule != c.molecule || a.stat != c.stat || a.levels != c.levels || a.lambda != c.lambda ||
+          a.mcstep != c.mcstep)
+        return PIMC_ERR_BAD_ARG;
+      if (a.levels > 4) return PIMC_ERR_SIZE;                     // PIMC_BATCH_MAX_SEG
+      if (s.nslices % (1 << a.levels)) return PIMC_ERR_BAD_ARG;   // bisection blocks tile the ring
+      if (a.numb > smax.type[t].numb) smax.type[t].numb = a.numb;
+    }
+    if (ds[r].R > 16) return PIMC_ERR_SIZE;
+  }
+  pimc_handle *base = nullptr;
+  pimc_status e = pimc_create(&smax, device, &base);
+  if (e) return e;
+  pimc_batch *b = new (std::nothrow) pimc_batch();
+  if (!b) { pimc_destroy(base); return PIMC_ERR_SIZE; }
+  b->base = base;
+  b->n = n;
+  b->sys.assign(systems, systems + n);
+  b->reps.resize(n);
+  b->state_set.assign(n, 0);
+  pimc_handle *h = base;
+  // pool sizes
+  size_t nb = 0, nq = 0, na = 0;
+  std::vector<size_t> ob(n), oq(n), oa(n);
+  for (int r = 0; r < n; r++) {
+    const DevSys &d = ds[r];
+    ob[r] = nb; oq[r] = nq; oa[r] = na;
+    nb += (size_t)d.P * d.nap;
+    nq += (size_t)(d.nrotors > 0 ? d.nrotors : 1) * d.Q;
+    na += (size_t)d.na;
+  }
+  double *x, *y, *z, *ang, *cosv, *rpc, *rlc;
+  float4 *b4;
+  float *cosvf;
+  int *rpo, *rlo, *pidx, *mct;
+  Frame *frames;
+  if ((e = pool(h, &x, nb)) || (e = pool(h, &y, nb)) || (e = pool(h, &z, nb)) || (e = pool(h, &b4, nb)) ||
+      (e = pool(h, &ang, 3 * nq)) || (e = pool(h, &cosv, 3 * nq)) || (e = pool(h, &cosvf, 3 * nq)) ||
+      (e = pool(h, &rpc, nq)) || (e = pool(h, &rlc, nq)) || (e = pool(h, &rpo, nq)) || (e = pool(h, &rlo, nq)) ||
+      (e = pool(h, &pidx, na)) || (e = pool(h, &mct, na)) || (e = pool(h, &frames, nq)) ||
+      (e = pool(h, &b->d_pass, (size_t)n)) || (e = pool(h, &b->d_cnt, (size_t)n * 12)) ||
+      (e = pool(h, &b->d_reps, (size_t)n)) || (e = pool(h, &b->d_order, (size_t)n)) ||
+      (e = pool(h, &b->d_work, 1)) || (e = pool(h, &b->d_est, (size_t)n * 6))) {
+    pimc_batch_destroy(b);
+    return e;
+  }
+  std::vector<int> hp(na), hm(na);
+  std::vector<std::pair<double, int>> work(n);
+  for (int r = 0; r < n; r++) {
+    const DevSys &d = ds[r];
+    BatchRep &rp = b->reps[r];
+    memset(&rp, 0, sizeof(rp));
+    rp.c.s = d;
+    DevState &st = rp.c.st;
+    st.x = x + ob[r]; st.y = y + ob[r]; st.z = z + ob[r]; st.b4 = b4 + ob[r];
+    st.ang = ang + 3 * oq[r]; st.cosv = cosv + 3 * oq[r]; st.cosvf = cosvf + 3 * oq[r];
+    st.rp_cache = rpc + oq[r]; st.rl_cache = rlc + oq[r]; st.rp_ok = rpo + oq[r]; st.rl_ok = rlo + oq[r];
+    st.pindex = pidx + oa[r]; st.mctype = mct + oa[r];
+    st.err = base->ctx.st.err;
+    rp.frames = frames + oq[r];
+    rp.pass = b->d_pass + r;
+    rp.cnt = b->d_cnt + 12 * (size_t)r;
+    rp.seed_mix = 0x9E3779B97F4A7C15ull * (uint64_t)(r + 1);
+    rp.rotation = systems[r].rotation;
+    int g = 0;
+    for (int t = 0; t < d.ntypes; t++)
+      for (int a = 0; a < d.numb[t]; a++) { hm[oa[r] + g] = t; hp[oa[r] + g] = g; g++; }
+    double bm = system_bead_moves(d, systems[r].rotation);
+    b->bm_pass += bm;
+    work[r] = {bm * (double)d.na, r};
+  }
+  CK(cudaMemcpy(pidx, hp.data(), na * sizeof(int), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(mct, hm.data(), na * sizeof(int), cudaMemcpyHostToDevice));
+  // the largest replicas first: the work queue ends with the short ones
+  std::sort(work.begin(), work.end(), [](const std::pair<double, int> &a, const std::pair<double, int> &c) {
+    return a.first > c.first || (a.first == c.first && a.second < c.second);
+  });
+  std::vector<int> order(n);
+  for (int k = 0; k < n; k++) order[k] = work[k].second;
+  CK(cudaMemcpy(b->d_order, order.data(), n * sizeof(int), cudaMemcpyHostToDevice));
+  *out = b;
+  return PIMC_OK;
+}
+
+extern "C" pimc_status pimc_batch_destroy(pimc_batch *b)
+{
+  if (!b) return PIMC_ERR_BAD_ARG;
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->base) pimc_destroy(b->base);
+  delete b;
+  return PIMC_OK;
+}
+
+static pimc_status batch_upload_reps(pimc_batch *b)
+{
+  pimc_handle *h = b->base;
+  CK(cudaMemcpy(b->d_reps, b->reps.data(), b->reps.size() * sizeof(BatchRep), cudaMemcpyHostToDevice));
+  return PIMC_OK;
+}
+
+extern "C" pimc_status pimc_batch_load_tables(pimc_batch *b, const pimc_tables *tables)
+{
+  if (!b || !tables) return PIMC_ERR_BAD_ARG;
+  pimc_handle *h = b->base;
+  CK(cudaSetDevice(h->device));
+  pimc_status e = load_tables_into(h, &tables[0], h->ctx.t, h->ctx.s, TAB_POT);
+  if (e) return e;
+  for (int r = 0; r < b->n; r++) {
+    DevTables t = h->ctx.t;
+    if ((e = load_tables_into(h, &tables[r], t, b->reps[r].c.s, TAB_ROT))) return e;
+    b->reps[r].c.t = t;
+  }
+  if ((e = batch_upload_reps(b))) return e;
+  CK(cudaStreamSynchronize(h->stream));
+  b->tables = true;
+  if (b->exec) { cudaGraphExecDestroy(b->exec); b->exec = nullptr; }
+  return PIMC_OK;
+}
+
+extern "C" pimc_status pimc_batch_set_state(pimc_batch *b, int r, const double *coords, const double *angles,
+                                            const int *pindex)
+{
+  if (!b || r < 0 || r >= b->n || !coords || !angles) return PIMC_ERR_BAD_ARG;
+  pimc_handle *h = b->base;
+  CK(cudaSetDevice(h->device));
+  const Ctx &c = b->reps[r].c;
+  const DevSys &d = c.s;
+  size_t nbr = (size_t)d.na * d.P;
+  std::vector<double> buf((size_t)d.P * d.nap, 0.0);
+  double *dst[3] = {c.st.x, c.st.y, c.st.z};
+  for (int k = 0; k < 3; k++) {
+    for (int a = 0; a < d.na; a++)
+      for (int t = 0; t < d.P; t++) buf[(size_t)t * d.nap + a] = coords[k * nbr + (size_t)a * d.P + t];
+    CK(cudaMemcpy(dst[k], buf.data(), buf.size() * sizeof(double), cudaMemcpyHostToDevice));
+  }
+  if (d.nrotors > 0) {
+    size_t n = (size_t)d.nrotors * d.Q;
+    std::vector<double> av(3 * n), cs(3 * n);
+    for (int rr = 0; rr < d.nrotors; rr++)
+      for (int q = 0; q < d.Q; q++) {
+        size_t src = (size_t)(d.rot_first + rr) * d.P + q;
+        double phi = angles[src], cost = angles[nbr + src];
+        double sint = sqrt(1.0 - cost * cost);                       // mc_main.cc:193-199
+        for (int k = 0; k < 3; k++) av[k * n + rr * d.Q + q] = angles[k * nbr + src];
+        cs[0 * n + rr * d.Q + q] = sint * cos(phi);
+        cs[1 * n + rr * d.Q + q] = sint * sin(phi);
+        cs[2 * n + rr * d.Q + q] = cost;
+      }
+    CK(cudaMemcpy(c.st.ang, av.data(), 3 * n * sizeof(double), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(c.st.cosv, cs.data(), 3 * n * sizeof(double), cudaMemcpyHostToDevice));
+  }
+  if (pindex) {
+    for (int a = 0; a < d.na; a++)
+      if (pindex[a] < 0 || pindex[a] >= d.na) return PIMC_ERR_BAD_ARG;
+    CK(cudaMemcpy(c.st.pindex, pindex, d.na * sizeof(int), cudaMemcpyHostToDevice));
+  }
+  launch_derive_state(c, b->reps[r].frames, h->stream);       // float copies, frames, caches stale
+  h->launches++;
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(h->stream));
+  b->state_set[r] = 1;
+  return PIMC_OK;
+}
+
+extern "C" pimc_status pimc_batch_get_state(pimc_batch *b, int r, double *coords, double *angles, double *cosine,
+                                            int *pindex)
+{
+  if (!b || r < 0 || r >= b->n) return PIMC_ERR_BAD_ARG;
+  pimc_handle *h = b->base;
+  CK(cudaSetDevice(h->device));
+  CK(cudaStreamSynchronize(h->stream));
+  const Ctx &c = b->reps[r].c;
+  const DevSys &d = c.s;
+  size_t nbr = (size_t)d.na * d.P;
+  if (coords) {
+    std::vector<double> buf((size_t)d.P * d.nap);
+    double *src[3] = {c.st.x, c.st.y, c.st.z};
+    for (int k = 0; k < 3; k++) {
+      CK(cudaMemcpy(buf.data(), src[k], buf.size() * sizeof(double), cudaMemcpyDeviceToHost));
+      for (int a = 0; a < d.na; a++)
+        for (int t = 0; t < d.P; t++) coords[k * nbr + (size_t)a * d.P + t] = buf[(size_t)t * d.nap + a];
+    }
+  }
+  if (angles || cosine) {
+    // rows of the rotors; the other rows are returned as zeros
+    if (angles) memset(angles, 0, 3 * nbr * sizeof(double));
+    if (cosine) memset(cosine, 0, 3 * nbr * sizeof(double));
+    if (d.nrotors > 0) {
+      size_t n = (size_t)d.nrotors * d.Q;
+      std::vector<double> av(3 * n), cs(3 * n);
+      CK(cudaMemcpy(av.data(), c.st.ang, 3 * n * sizeof(double), cudaMemcpyDeviceToHost));
+      CK(cudaMemcpy(cs.data(), c.st.cosv, 3 * n * sizeof(double), cudaMemcpyDeviceToHost));
+      for (int k = 0; k < 3; k++)
+        for (int rr = 0; rr < d.nrotors; rr++)
+          for (int q = 0; q < d.Q; q++) {
+            size_t dst = k * nbr + (size_t)(d.rot_first + rr) * d.P + q;
+            if (angles) angles[dst] = av[k * n + rr * d.Q + q];
+            if (cosine) cosine[dst] = cs[k * n + rr * d.Q + q];
+          }
+    }
+  }
+  if (pindex) CK(cudaMemcpy(pindex, c.st.pindex, d.na * sizeof(int), cudaMemcpyDeviceToHost));
+  return PIMC_OK;
+}
+
+extern "C" pimc_status pimc_batch_set_precision(pimc_batch *b, int mixed)
+{
+  if (!b || (mixed != 0 && mixed != 1)) return PIMC_ERR_BAD_ARG;
+  pimc_handle *h = b->base;
+  CK(cudaSetDevice(h->device));
+  CK(cudaStreamSynchronize(h->stream));
+  b->mixed = mixed;
+  for (auto &rp : b->reps) rp.c.s.mixed = mixed;
+  return batch_upload_reps(b);
+}
+
+extern "C" pimc_status pimc_batch_set_shape(pimc_batch *b, int warps)
+{
+  if (!b || (warps != 2 && warps != 4 && warps != 8)) return PIMC_ERR_BAD_ARG;
+  b->warps = warps;
+  return PIMC_OK;
+}
+
+static pimc_status batch_ready(pimc_batch *b)
+{
+  if (!b) return PIMC_ERR_BAD_ARG;
+  if (!b->tables) return PIMC_ERR_STATE;
+  for (int r = 0; r < b->n; r++)
+    if (!b->state_set[r]) return PIMC_ERR_STATE;
+  return PIMC_OK;
+}
+
+extern "C" pimc_status pimc_batch_run_passes(pimc_batch *b, int npasses, uint64_t seed)
+{
+  pimc_status e = batch_ready(b);
+  if (e) return e;
+  if (npasses < 0) return PIMC_ERR_BAD_ARG;
+  pimc_handle *h = b->base;
+  CK(cudaSetDevice(h->device));
+  if (!b->exec || b->exec_seed != seed || b->exec_warps != b->warps || b->exec_mixed != b->mixed) {
+    if (b->exec) { BK(cudaGraphExecDestroy(b->exec)); b->exec = nullptr; }
+    int nctas = batch_max_ctas(b->mixed, b->warps);
+    if (nctas <= 0) return PIMC_ERR_CUDA;
+    if (nctas > b->n) nctas = b->n;
+    cudaGraph_t graph;
+    CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    launch_batch_pass(b->d_reps, b->d_order, b->n, seed, b->d_work, b->mixed, b->warps, nctas, h->stream);
+    cudaError_t le = cudaGetLastError();
+    cudaError_t ce = cudaStreamEndCapture(h->stream, &graph);
+    if (le != cudaSuccess || ce != cudaSuccess) {
+      if (ce == cudaSuccess) cudaGraphDestroy(graph);
+      h->last_cuda = le != cudaSuccess ? le : ce;
+      return PIMC_ERR_CUDA;
+    }
+    cudaError_t ie = cudaGraphInstantiate(&b->exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ie != cudaSuccess) { h->last_cuda = ie; return PIMC_ERR_CUDA; }
+    b->exec_seed = seed;
+    b->exec_warps = b->warps;
+    b->exec_mixed = b->mixed;
+  }
+  for (int p = 0; p < npasses; p++) {
+    CK(cudaGraphLaunch(b->exec, h->stream));
+    h->launches += 2;
+  }
+  if (npasses > 0) {
+    launch_batch_refresh(b->d_reps, b->n, 0, h->stream);     // double frames and MCCosine of tops
+    h->launches++;
+    CK(cudaGetLastError());
+  }
+  return PIMC_OK;
+}
+
+extern "C" pimc_status pimc_batch_autotune(pimc_batch *b, uint64_t seed, int *warps_out, double *ms_out)
+{
+  pimc_status e = batch_ready(b);
+  if (e) return e;
+  pimc_handle *h = b->base;
+  CK(cudaSetDevice(h->device));
+  const int cand[3] = {2, 4, 8};
+  double best = 1e300;
+  int bw = b->warps;
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  for (int k = 0; k < 3; k++) {
+    b->warps = cand[k];
+    if (batch_max_ctas(b->mixed, b->warps) <= 0) continue;
+    if ((e = pimc_batch_run_passes(b, 1, seed))) return e;      // graph build and warm-up
+    CK(cudaEventRecord(e0, h->stream));
+    if ((e = pimc_batch_run_passes(b, 1, seed))) return e;
+    CK(cudaEventRecord(e1, h->stream));
+    CK(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, e0, e1));
+    if (ms_out) ms_out[k] = ms;
+    if (ms < best) { best = ms; bw = cand[k]; }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  b->warps = bw;
+  if (warps_out) *warps_out = bw;
+  return check_err(h);
+}
+
+extern "C" pimc_status pimc_batch_estimators(pimc_batch *b, double *out)
+{
+  pimc_status e = batch_ready(b);
+  if (e) return e;
+  if (!out) return PIMC_ERR_BAD_ARG;
+  pimc_handle *h = b->base;
+  CK(cudaSetDevice(h->device));
+  launch_batch_est(b->d_reps, b->n, b->d_est, h->stream);
+  h->launches++;
+  CK(cudaGetLastError());
+  std::vector<double> v((size_t)b->n * 6);
+  CK(cudaMemcpyAsync(v.data(), b->d_est, v.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  if ((e = check_err(h))) return e;
+  for (int r = 0; r < b->n; r++) {
+    const DevSys &d = b->reps[r].c.s;
+    const double *w = v.data() + 6 * (size_t)r;
+    double *o = out + 4 * (size_t)r;
+    o[0] = (double)d.P * d.temperature * (0.5 * (double)(3 * d.na) - w[0]);    // mc_estim.cc:923-934
+    o[1] = w[1] / (double)d.P;
+    double erot = 0.0, cz = 0.0;
+    if (d.nrotors > 0 && b->sys[r].rotation) {
+      if (d.molecule[d.imtype] == PIMC_LINEAR) {                                 // mc_estim.cc:953-984
+        erot = w[2];
+        if (d.rot_den_type == 1) erot = (erot / (double)d.Q) / d.rot_tau + 1.0 / d.rot_tau;
+      } else {                                                                   // mc_estim.cc:1000-1092
+        int skip = d.rot_den_type == 0 ? 1 : d.rn_ratio;
+        erot = w[2] / (double)(d.Q / skip);
+        if (d.rot_den_type == 1 && d.rn_ratio == 1) {
+          erot = erot / (4.0 * (d.rot_tau / PIMC_WNO2K) * (d.rot_tau / PIMC_WNO2K));
+          erot += 0.25 * (d.abc[0] + d.abc[1] + d.abc[2]) + 1.5 / (d.rot_tau / PIMC_WNO2K);
+          erot = erot / PIMC_WNO2K;
+        }
+      }
+      cz = w[5] / ((double)d.nrotors * d.Q);
+    }
+    o[2] = erot;
+    o[3] = cz;
+  }
+  return PIMC_OK;
+}
+
+extern "C" pimc_status pimc_batch_counters(pimc_batch *b, double *total, double *accep)
+{
+  if (!b || !total || !accep) return PIMC_ERR_BAD_ARG;
+  pimc_handle *h = b->base;
+  CK(cudaSetDevice(h->device));
+  CK(cudaStreamSynchronize(h->stream));
+  std::vector<unsigned long long> v((size_t)b->n * 12);
+  CK(cudaMemcpy(v.data(), b->d_cnt, v.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+  for (int k = 0; k < 6; k++) { total[k] = 0.0; accep[k] = 0.0; }
+  for (int r = 0; r < b->n; r++)
+    for (int k = 0; k < 6; k++) {
+      total[k] += (double)v[12 * (size_t)r + 2 * k];
+      accep[k] += (double)v[12 * (size_t)r + 2 * k + 1];
+    }
+  return PIMC_OK;
+}
+
+extern "C" pimc_status pimc_batch_synchronize(pimc_batch *b)
+{
+  if (!b) return PIMC_ERR_BAD_ARG;
+  pimc_handle *h = b->base;
+  CK(cudaSetDevice(h->device));
+  return check_err(h);
+}
+
+extern "C" double pimc_batch_bead_moves_per_pass(const pimc_batch *b) { return b ? b->bm_pass : 0.0; }
+
+extern "C" void *pimc_batch_stream(const pimc_batch *b) { return b ? (void *)b->base->stream : nullptr; }

@@ -505,19 +505,9 @@ __global__ void __launch_bounds__(PIMC_BLOCK) k_est_kin(Ctx c, double *out)
 {
   __shared__ double part[PIMC_BLOCK];
   int a = blockIdx.x, P = c.s.P;
-  int type = c.st.mctype[a];
-  int g = c.s.first[type];
+  int type = atom_type(c.s, a);
   double acc = 0.0;
-  for (int it = threadIdx.x; it < P; it += blockDim.x) {
-    int a1 = a;
-    if (c.s.stat[type] == 1 && it + 1 == P) a1 = g + c.st.pindex[a - g];
-    size_t i0 = sidx(c.s, it, a), i1 = sidx(c.s, (it + 1) % P, a1);
-    double d[3] = {c.st.x[i0] - c.st.x[i1], c.st.y[i0] - c.st.y[i1], c.st.z[i0] - c.st.z[i1]};
-    for (int k = 0; k < 3; k++) {
-      if (c.s.minimage) d[k] -= c.s.box[k] * rint(d[k] / c.s.box[k]);
-      acc += d[k] * d[k];
-    }
-  }
+  for (int it = threadIdx.x; it < P; it += blockDim.x) acc += est_spring(c, a, it);
   part[threadIdx.x] = acc;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -538,12 +528,8 @@ __global__ void __launch_bounds__(PIMC_BLOCK) k_est_pot(Ctx c, Frame *frames, do
   int a0 = 0, rem = pidx;
   while (rem >= na - 1 - a0) { rem -= na - 1 - a0; a0++; }
   int a1 = a0 + 1 + rem;
-  int ty0 = c.st.mctype[a0], ty1 = c.st.mctype[a1];
-  int m0 = c.s.molecule[ty0], m1 = c.s.molecule[ty1];
-  bool counted = (m0 == 1 || m1 == 1) || (m0 != m1) || (m0 == 2 && m1 == 2 && c.s.numb[c.s.imtype] > 1) ||
-                 (ty0 == ty1 && m0 == 0);
   double acc = 0.0;
-  if (counted)
+  if (est_pair_counted(c, a0, a1))
     for (int it = threadIdx.x; it < c.s.P; it += blockDim.x) {
       size_t i = sidx(c.s, it, a0);
       acc += pair_term64(c, frames, a0, a1, it, c.st.x[i], c.st.y[i], c.st.z[i]);
@@ -557,54 +543,12 @@ __global__ void __launch_bounds__(PIMC_BLOCK) k_est_pot(Ctx c, Frame *frames, do
   }
 }
 
-// GetRotE3D (mc_estim.cc:989-1096) per (rotor, it0) link terms and
-// GetRotEnergy (mc_estim.cc:939-987) for the linear rotor:
-// out[4*k + {srot, sesq, se_termsq, valid}]
+// per (rotor, it0) link terms: out[4*k + {srot, sesq, se_termsq, valid}]
 __global__ void k_est_rot(Ctx c, Frame *frames, double *out)
 {
-  int Q = c.s.Q, nr = c.s.nrotors;
   int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= nr * Q) return;
-  int r = k / Q, it0 = k % Q;
-  bool linear = c.s.molecule[c.s.imtype] == 1;
-  double srot = 0.0, sesq = 0.0, sts = 0.0;
-  if (linear) {
-    size_t n = (size_t)nr * Q;
-    int t0 = r * Q + it0, t1 = r * Q + (it0 + 1) % Q;
-    double p0 = 0.0;
-    for (int d = 0; d < 3; d++) p0 += (c.st.cosv[d * n + t0] * c.st.cosv[d * n + t1]);
-    if (c.s.rot_den_type == 0) {
-      double rdens = srotdens(c.t, p0, 0);
-      double dv = srotdens(c.t, p0, 1);
-      if (fabs(rdens) > PIMC_RZERO) srot = dv / rdens;
-      sts = (dv / rdens) * (dv / rdens);
-      sesq = srotdens(c.t, p0, 2) / rdens;
-    } else {
-      double rho, erot;
-      rsline(c.s.abc[0], p0, c.s.rot_tau, &rho, &erot);
-      srot = rho;
-    }
-  } else {
-    int skip = (c.s.rot_den_type == 0) ? 1 : c.s.rn_ratio;
-    if (it0 % skip == 0) {
-      const Frame &f1 = frames[r * Q + it0];
-      const Frame &f2 = frames[r * Q + (it0 + skip) % Q];
-      double rho = 0.0, erot = 0.0, esq = 0.0;
-      int bad = 0;
-      rho = rotden_rho(c.t, f1, f2, &bad, &erot, &esq);
-      if (c.s.rot_den_type == 1 && c.s.rn_ratio == 1) {
-        rsrot(f1, f2, c.s.abc, c.s.rot_tau, c.s.rot_odevn, &rho, &erot);
-        srot = rho;
-      } else
-        srot = erot;
-      sesq = esq;
-      sts = erot * erot;
-    }
-  }
-  out[4 * k + 0] = srot;
-  out[4 * k + 1] = sesq;
-  out[4 * k + 2] = sts;
-  out[4 * k + 3] = 1.0;
+  if (k >= c.s.nrotors * c.s.Q) return;
+  est_link(c, frames, k, out + 4 * (size_t)k);
 }
 
 // GetRCF (mc_estim.cc:1099-1139) row 0: rcf[itc] = sum_it0 n(it0).n(it0+itc)

@@ -21,7 +21,7 @@ __device__ __forceinline__ int atom_type(const DevSys &s, int a) { return (s.nty
 
 // one term of PotEnergy(atom0, pos, it) (mc_piqmc.cc:1824-1958): atom0 at
 // (px,py,pz), partner atom1 at its current bead, rotor frames from the cache
-__device__ __forceinline__ double pair_term64(const Ctx &c, const Frame *__restrict__ frames, int a0, int a1, int it,
+__device__ __forceinline__ double pair_term64(const Ctx &c, const Frame *frames, int a0, int a1, int it,
                                               double px, double py, double pz)
 {
   const DevSys &s = c.s;
@@ -61,7 +61,7 @@ __device__ __forceinline__ double pair_term64(const Ctx &c, const Frame *__restr
 }
 
 // the same term on the FP32 table path
-__device__ __forceinline__ float pair_term32(const Ctx &c, const Frame *__restrict__ frames, int a0, int a1, int it,
+__device__ __forceinline__ float pair_term32(const Ctx &c, const Frame *frames, int a0, int a1, int it,
                                              float px, float py, float pz)
 {
   const DevSys &s = c.s;
@@ -1004,4 +1004,80 @@ __device__ int rot_step(const Ctx &c, Frame *frames, int g0, int q, const double
   rot_prepare<MIX>(c, frames, g0, q, u, prop, linear, sh);
   RotNoHooks hk;
   return rot_finish<MIX, COH>(c, frames, g0, q, linear, sh, rd_out, hk);
+}
+
+// ------------------------------------------------------ estimator terms
+// GetKinEnergy (mc_estim.cc:876-937): |r(it) - r(it+1)|^2 of atom a, the
+// last slice of a boson joined to the atom PIndex names
+__device__ __forceinline__ double est_spring(const Ctx &c, int a, int it)
+{
+  const int P = c.s.P;
+  const int type = atom_type(c.s, a), g = c.s.first[type];
+  int a1 = a;
+  if (c.s.stat[type] == 1 && it + 1 == P) a1 = g + c.st.pindex[a - g];
+  size_t i0 = sidx(c.s, it, a), i1 = sidx(c.s, (it + 1) % P, a1);
+  double d[3] = {c.st.x[i0] - c.st.x[i1], c.st.y[i0] - c.st.y[i1], c.st.z[i0] - c.st.z[i1]};
+  double acc = 0.0;
+  for (int k = 0; k < 3; k++) {
+    if (c.s.minimage) d[k] -= c.s.box[k] * rint(d[k] / c.s.box[k]);
+    acc += d[k] * d[k];
+  }
+  return acc;
+}
+
+// the pairs GetPotEnergy_Densities (mc_estim.cc:500-687) adds to the potential
+__device__ __forceinline__ bool est_pair_counted(const Ctx &c, int a0, int a1)
+{
+  int ty0 = atom_type(c.s, a0), ty1 = atom_type(c.s, a1);
+  int m0 = c.s.molecule[ty0], m1 = c.s.molecule[ty1];
+  return (m0 == 1 || m1 == 1) || (m0 != m1) || (m0 == 2 && m1 == 2 && c.s.numb[c.s.imtype] > 1) ||
+         (ty0 == ty1 && m0 == 0);
+}
+
+// GetRotE3D (mc_estim.cc:989-1096) link terms of (rotor, it0) = k and
+// GetRotEnergy (mc_estim.cc:939-987) for the linear rotor:
+// out = {srot, sesq, se_termsq, valid}
+__device__ __forceinline__ void est_link(const Ctx &c, const Frame *frames, int k, double out[4])
+{
+  const int Q = c.s.Q, nr = c.s.nrotors;
+  const int r = k / Q, it0 = k % Q;
+  const bool linear = c.s.molecule[c.s.imtype] == 1;
+  double srot = 0.0, sesq = 0.0, sts = 0.0;
+  if (linear) {
+    size_t n = (size_t)nr * Q;
+    int t0 = r * Q + it0, t1 = r * Q + (it0 + 1) % Q;
+    double p0 = 0.0;
+    for (int d = 0; d < 3; d++) p0 += (c.st.cosv[d * n + t0] * c.st.cosv[d * n + t1]);
+    if (c.s.rot_den_type == 0) {
+      double rdens = srotdens(c.t, p0, 0);
+      double dv = srotdens(c.t, p0, 1);
+      if (fabs(rdens) > PIMC_RZERO) srot = dv / rdens;
+      sts = (dv / rdens) * (dv / rdens);
+      sesq = srotdens(c.t, p0, 2) / rdens;
+    } else {
+      double rho, erot;
+      rsline(c.s.abc[0], p0, c.s.rot_tau, &rho, &erot);
+      srot = rho;
+    }
+  } else {
+    int skip = (c.s.rot_den_type == 0) ? 1 : c.s.rn_ratio;
+    if (it0 % skip == 0) {
+      const Frame &f1 = frames[r * Q + it0];
+      const Frame &f2 = frames[r * Q + (it0 + skip) % Q];
+      double rho = 0.0, erot = 0.0, esq = 0.0;
+      int bad = 0;
+      rho = rotden_rho(c.t, f1, f2, &bad, &erot, &esq);
+      if (c.s.rot_den_type == 1 && c.s.rn_ratio == 1) {
+        rsrot(f1, f2, c.s.abc, c.s.rot_tau, c.s.rot_odevn, &rho, &erot);
+        srot = rho;
+      } else
+        srot = erot;
+      sesq = esq;
+      sts = erot * erot;
+    }
+  }
+  out[0] = srot;
+  out[1] = sesq;
+  out[2] = sts;
+  out[3] = 1.0;
 }

@@ -36,3 +36,24 @@ void launch_q_rot(const Ctx &c, Frame *f, int n, const int *rot, const int *it, 
 void launch_est(const Ctx &c, Frame *f, double *kin, double *pot, double *rot, double *rcf, cudaStream_t s);
 void launch_pass_begin(unsigned *pass, cudaStream_t s);
 size_t mol_scratch_bytes();
+
+// ------------------------------------------------------------ replica batches
+#define PIMC_BATCH_MAX_SEG 16         /* bisection segment of batched replicas (levels <= 4) */
+
+// one replica of a batch, as the batch kernels read it
+struct BatchRep {
+  Ctx c;
+  Frame *frames;
+  unsigned *pass;                    // the replica's pass counter
+  unsigned long long *cnt;           // its MCTotal / MCAccep counters [type][kind][total, accepted]
+  uint64_t seed_mix;                 // xor-ed into the run's seed
+  int rotation;
+};
+#define PIMC_BATCH_CTX_BYTES (((sizeof(Ctx) + 15) / 16) * 16)
+
+size_t batch_smem_bytes(int warps);
+int batch_max_ctas(int mixed, int warps);
+void launch_batch_pass(const BatchRep *reps, const int *order, int n, uint64_t seed, unsigned *work, int mixed,
+                       int warps, int nctas, cudaStream_t s);
+void launch_batch_est(const BatchRep *reps, int n, double *out, cudaStream_t s);
+void launch_batch_refresh(const BatchRep *reps, int n, int derive, cudaStream_t s);

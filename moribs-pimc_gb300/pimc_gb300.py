@@ -67,6 +67,25 @@ def load(path=LIBPATH):
     L.pimc_stream.argtypes = [vp]
     L.pimc_status_string.restype = C.c_char_p
     L.pimc_status_string.argtypes = [C.c_int]
+    # replica batches
+    L.pimc_batch_create.argtypes = [C.c_int, C.POINTER(PimcSystem), C.c_int, C.POINTER(vp)]
+    L.pimc_batch_destroy.argtypes = [vp]
+    L.pimc_batch_load_tables.argtypes = [vp, C.POINTER(PimcTables)]
+    L.pimc_batch_set_state.argtypes = [vp, C.c_int, _dp, _dp, _ip]
+    L.pimc_batch_get_state.argtypes = [vp, C.c_int, _dp, _dp, _dp, _ip]
+    L.pimc_batch_set_precision.argtypes = [vp, C.c_int]
+    L.pimc_batch_set_shape.argtypes = [vp, C.c_int]
+    L.pimc_batch_autotune.argtypes = [vp, C.c_uint64, _ip, _dp]
+    L.pimc_batch_run_passes.argtypes = [vp, C.c_int, C.c_uint64]
+    L.pimc_batch_estimators.argtypes = [vp, _dp]
+    L.pimc_batch_counters.argtypes = [vp, _dp, _dp]
+    L.pimc_batch_synchronize.argtypes = [vp]
+    L.pimc_batch_bead_moves_per_pass.restype = C.c_double
+    L.pimc_batch_bead_moves_per_pass.argtypes = [vp]
+    L.pimc_batch_replica_seed.restype = C.c_uint64
+    L.pimc_batch_replica_seed.argtypes = [C.c_uint64, C.c_int]
+    L.pimc_batch_stream.restype = vp
+    L.pimc_batch_stream.argtypes = [vp]
     _L = L
     return L
 
@@ -217,3 +236,87 @@ class Sampler:
 
     def stream(self):
         return self.L.pimc_stream(self.h)
+
+
+class Batch:
+    """A pimc_batch: independent replicas of one species family sampled in
+    one persistent launch (include/pimc_gb300.h, replica batches)."""
+
+    def __init__(self, workloads, device=0, mixed=False):
+        self.L = load()
+        self.ws = list(workloads)
+        n = len(self.ws)
+        systems = (PimcSystem * n)(*[make_system(w) for w in self.ws])
+        h = C.c_void_p()
+        _chk(self.L.pimc_batch_create(n, systems, device, C.byref(h)), "pimc_batch_create")
+        self.h = h
+        tabs = (PimcTables * n)()
+        keep = []
+        for i, w in enumerate(self.ws):
+            t, k = make_tables(w)
+            tabs[i] = t
+            keep.append(k)
+        _chk(self.L.pimc_batch_load_tables(self.h, tabs), "pimc_batch_load_tables")
+        if mixed:
+            _chk(self.L.pimc_batch_set_precision(self.h, 1), "pimc_batch_set_precision")
+        for i, w in enumerate(self.ws):
+            self.set_state(i, w.coords, w.angles, w.pindex)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.pimc_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_state(self, i, coords, angles, pindex=None):
+        c = np.ascontiguousarray(coords, dtype=np.float64)
+        a = np.ascontiguousarray(angles, dtype=np.float64)
+        p = None if pindex is None else np.ascontiguousarray(pindex, dtype=np.int32)
+        _chk(self.L.pimc_batch_set_state(self.h, int(i), dptr(c), dptr(a), iptr(p) if p is not None else None),
+             "pimc_batch_set_state")
+
+    def get_state(self, i):
+        w = self.ws[i]
+        n = w.natoms * w.nslices
+        c = np.zeros((3, n)); a = np.zeros((3, n)); co = np.zeros((3, n)); p = np.zeros(w.natoms, np.int32)
+        _chk(self.L.pimc_batch_get_state(self.h, int(i), dptr(c), dptr(a), dptr(co), iptr(p)), "pimc_batch_get_state")
+        return c, a, co, p
+
+    def set_shape(self, warps):
+        _chk(self.L.pimc_batch_set_shape(self.h, int(warps)), "pimc_batch_set_shape")
+
+    def autotune(self, seed):
+        wo = np.zeros(1, np.int32); ms = np.zeros(3)
+        _chk(self.L.pimc_batch_autotune(self.h, C.c_uint64(seed), iptr(wo), dptr(ms)), "pimc_batch_autotune")
+        return int(wo[0]), ms
+
+    def run_passes(self, n, seed):
+        _chk(self.L.pimc_batch_run_passes(self.h, int(n), C.c_uint64(seed)), "pimc_batch_run_passes")
+
+    def estimators(self):
+        out = np.zeros((len(self.ws), 4))
+        _chk(self.L.pimc_batch_estimators(self.h, dptr(out)), "pimc_batch_estimators")
+        return out
+
+    def counters(self):
+        tot = np.zeros(6); acc = np.zeros(6)
+        _chk(self.L.pimc_batch_counters(self.h, dptr(tot), dptr(acc)), "pimc_batch_counters")
+        return tot, acc
+
+    def synchronize(self):
+        _chk(self.L.pimc_batch_synchronize(self.h), "pimc_batch_synchronize")
+
+    def bead_moves_per_pass(self):
+        return self.L.pimc_batch_bead_moves_per_pass(self.h)
+
+    def stream(self):
+        return self.L.pimc_batch_stream(self.h)
+
+    @staticmethod
+    def replica_seed(seed, r):
+        return int(load().pimc_batch_replica_seed(C.c_uint64(seed), int(r)))

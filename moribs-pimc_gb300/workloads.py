@@ -321,6 +321,84 @@ def config0(seed=1234, nslices=512, nrotslices=128, n_he=8, r2d_step=0.01, c2d_s
                     tables=tables, coords=coords, angles=angles, pindex=np.arange(n_he + 1, dtype=np.int32))
 
 
+def linden_exarho_many(cost, taus_cm, bconst, nslices, maxl=500, eps=1.0e-16):
+    """linden_exarho for many propagator times at once (one row per tau):
+    every row sums the same Legendre series up to the largest tau's cut-off
+    (the extra terms are below eps of the first)."""
+    taus = np.asarray(taus_cm, dtype=np.float64)
+    tmin = float(taus.min())
+    lmax = maxl
+    for l in range(maxl + 1):
+        if math.exp(-tmin * bconst * l * (l + 1)) < eps:
+            lmax = l
+            break
+    boltz = 0.69503476
+    cost = np.asarray(cost, dtype=np.float64)
+    rho = np.zeros((len(taus), len(cost)))
+    erot = np.zeros_like(rho)
+    erotsq = np.zeros_like(rho)
+    p_prev, p_cur = np.ones_like(cost), cost.copy()
+    for l in range(0, lmax + 1):
+        if l == 0:
+            pl = p_prev
+        elif l == 1:
+            pl = p_cur
+        else:
+            p_next = ((2.0 * (l - 1) + 1) * cost * p_cur - (l - 1) * p_prev) / l
+            p_prev, p_cur = p_cur, p_next
+            pl = p_cur
+        w = (2 * l + 1) * np.exp(-taus * bconst * float(l * (l + 1)))
+        tmp = np.outer(w, pl)
+        rho += tmp
+        erot += tmp * l * (l + 1) * bconst
+        erotsq += tmp * (l * (l + 1) * bconst) ** 2
+    ns = np.asarray(nslices, dtype=np.float64)[:, None]
+    erot = erot / (ns * boltz)
+    erotsq = erotsq / (ns * boltz) ** 2
+    return rho / (4.0 * math.pi), erot / (4.0 * math.pi), erotsq / (4.0 * math.pi)
+
+
+def config2(n=4096, seed=2024, p_choices=(64, 128, 256, 512), n_he=(1, 64), t_range=(0.3, 2.0),
+            r2d_step=0.01, c2d_step=0.01):
+    """n independent replicas of the config-0 family: 1 linear CO2-like rotor
+    (B = 0.39 cm^-1) + N He-4, N uniform in n_he, P from p_choices, Q = P/4,
+    T uniform in t_range, each seeded.  The He-He and rotor-He tables are
+    shared; each replica has its own linear-rotor propagator at
+    tau = 1/(T Q)."""
+    rng = np.random.default_rng(seed)
+    g1, v1 = _table_1d(aziz_hfdhe2, 1.0, 30.0, 512)
+    nr = int(round(18.0 / r2d_step)) + 1
+    nc = int(round(2.0 / c2d_step)) + 1
+    rg = np.round(np.arange(nr) * r2d_step + 2.0, 10)
+    cg = np.round(np.arange(nc) * c2d_step - 1.0, 10)
+    v2 = rotor_atom_2d(rg, cg)
+    ns = rng.integers(n_he[0], n_he[1] + 1, size=n)
+    ps = rng.choice(np.asarray(p_choices), size=n)
+    ts = rng.uniform(t_range[0], t_range[1], size=n)
+    qs = ps // 4
+    taus = 1.4387752224 / (ts * qs)
+    cost = np.array([(ic - 1) * (2.0 / 1499.0) - 1.0 for ic in range(1, 1501)])
+    rho, er, esq = linden_exarho_many(cost, taus, 0.39, qs)
+    out = []
+    for r in range(n):
+        n_r, P, Q, T = int(ns[r]), int(ps[r]), int(qs[r]), float(ts[r])
+        types = [
+            dict(name="He4", numb=n_r, molecule=0, stat=1, levels=3, mcstep=0.30, lamb=lam(MASSES["He4"]), fpot="he4"),
+            dict(name="CO2", numb=1, molecule=1, stat=0, levels=3, mcstep=0.10, lamb=lam(MASSES["CO2"]),
+                 fpot="co2he"),
+        ]
+        tables = dict(grid1d=g1, pot1d=v1, rgrid2d=rg, cgrid2d=cg, pot2d=v2, dr2d=r2d_step, dc2d=c2d_step,
+                      rotgrid=cost, rotdens=rho[r], rotderv=er[r], rotesqr=esq[r])
+        rr = np.random.default_rng([seed, r])
+        radius = 10.0 * (max(n_r, 8) / 8.0) ** (1.0 / 3.0)
+        pos = _sphere_points(rr, n_r, radius, 2.6, avoid=((0, 0, 0),), avoid_sep=3.3)
+        pos = np.vstack([pos, np.zeros((1, 3))])
+        coords, angles = initial_path(n_r + 1, P, pos, rr)
+        out.append(Workload("config2-replica-%d" % r, types, P, Q, T, rtstep=0.3, rotation=True,
+                            tables=tables, coords=coords, angles=angles, pindex=np.arange(n_r + 1, dtype=np.int32)))
+    return out
+
+
 def config1(seed=4321, nslices=1024, nrotslices=256, n_h2=64, grid3d=(200, 60, 60), griddens=(61, 121, 121)):
     """1 asymmetric-top SO2-like rotor (A,B,C = 2.03, 0.344, 0.293 cm^-1) + 64 pH2 at 0.37 K."""
     T = 0.37
