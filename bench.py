@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-companion", action="store_true", help="skip the other precision's measurement")
+    ap.add_argument("--no-batched", action="store_true", help="skip the config-2 replica-batch measurement")
+    ap.add_argument("--batched-replicas", type=int, default=4096)
     return ap.parse_args()
 
 
@@ -345,7 +347,54 @@ def run_gb300(args, rank, local, world, dist):
                      "accept tests and path" if other == "mixed" else "all arithmetic in FP64 as the reference"),
             "value": bm_pass * args.steps * world / (t2 / 1e3), "unit": UNIT, "ms_per_step": t2 / args.steps,
             "pass_ms_by_kind": {k: round(v, 3) for k, v in zip(kinds, ms2)}, "e2e": e2["value"]}
+    if not args.no_batched:
+        line["batched"] = run_batched(args, local, dist)
     return line, w
+
+
+def run_batched(args, local, dist):
+    """Config 2 (spec pattern 2): independent replicas of the config-0
+    family -- N_He uniform in 1..64, P in {64, 128, 256, 512}, Q = P/4, T
+    uniform in 0.3-2.0 K, seeded -- in one persistent graph-captured launch
+    per pass, FP32 tables with FP64 action differences; warps per CTA from
+    the autotuner.  Timed like the main line: CUDA events around each pass,
+    L2 flushed between passes."""
+    import torch
+    import pimc_gb300 as G
+    import workloads as W
+    ws = W.config2(n=args.batched_replicas, seed=2024 + 7 * (dist.get_rank() if dist else 0))
+    b = G.Batch(ws, device=local, mixed=True)
+    warps, tune_ms = b.autotune(77)
+    ext = torch.cuda.ExternalStream(b.stream(), device=torch.device("cuda", local))
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    b.run_passes(1, 78)
+    b.synchronize()
+    barrier(dist)
+    steps = 2
+    evs = []
+    with torch.cuda.stream(ext):
+        for k in range(steps):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(ext)
+            b.run_passes(1, 78)
+            e1.record(ext)
+            evs.append((e0, e1))
+    b.synchronize()
+    torch.cuda.synchronize()
+    total_ms = reduce_max(dist, sum(a.elapsed_time(c) for a, c in evs))
+    bm = b.bead_moves_per_pass()
+    world = dist.get_world_size() if dist else 1
+    tot, acc = b.counters()
+    out = {"workload": "config2: %d replicas of 1 CO2-like linear rotor + N He (N in 1..64, P in "
+                       "{64,128,256,512}, Q=P/4, T in 0.3-2.0 K)" % len(ws),
+           "value": bm * steps * world / (total_ms / 1e3), "unit": UNIT, "ms_per_pass": total_ms / steps,
+           "steps": steps, "bead_moves_per_pass": bm, "precision": "mixed", "dtype": "f32+f64",
+           "warps_per_cta": warps, "autotune_ms_per_pass": {"2": tune_ms[0], "4": tune_ms[1], "8": tune_ms[2]},
+           "accept_ratios": {"He bisection": acc[1] / max(1, tot[1]), "rotation": acc[5] / max(1, tot[5])}}
+    b.close()
+    return out
 
 
 def main():
