@@ -25,8 +25,8 @@ struct WarpRot {
   double ang_new[3], nv[3][3], nnew[3];
   float nvf[3], nnewf[3];
   double vals[2 * 16];
-  double rho[4];
-  int bad;
+  double rho[4], pot_c;
+  int bad, pot_cached, link_ok[2];
 };
 
 struct __align__(16) WarpMem {
@@ -186,8 +186,15 @@ __device__ int warp_rot(const Ctx &c, Frame *frames, int g0, int q, const double
   const int r = g0 - s.rot_first;
   const int i0 = r * Q + q0, i1 = r * Q + q, i2 = r * Q + q2;
   const bool need64 = !MIX || s.nrotors > 1;
+  const bool use_links = Q >= 3;                // link cache (with Q < 3 both links join the same two slices)
   if (lane == 0) {
     w.bad = 0;
+    w.pot_cached = c.st.rp_ok[i1];
+    if (w.pot_cached) w.pot_c = c.st.rp_cache[i1];
+    w.link_ok[0] = use_links && c.st.rl_ok[i0];
+    w.link_ok[1] = use_links && c.st.rl_ok[i1];
+    if (w.link_ok[0]) w.rho[0] = c.st.rl_cache[i0];
+    if (w.link_ok[1]) w.rho[1] = c.st.rl_cache[i1];
     w.ang_new[0] = prop[0]; w.ang_new[1] = prop[1]; w.ang_new[2] = prop[2];
     if (linear) {
       if (MIX) {
@@ -217,44 +224,60 @@ __device__ int warp_rot(const Ctx &c, Frame *frames, int g0, int q, const double
     copy_frame<false>(w.fo[2], frames + i2, lane);
   }
   __syncwarp();
+  // partner sums: the R old slots unless the rotor-potential cache holds them, then the R new ones
+  const int first = w.pot_cached ? R : 0;
+  const int nsl = 2 * R - first;
   if (linear) {
     if (MIX)
-      warp_slot_sums(lane, 2 * R, s.na - 1, g0,
-                     [&](int k, int p) -> float {
+      warp_slot_sums(lane, nsl, s.na - 1, g0,
+                     [&](int sl, int p) -> float {
+                       int k = sl + first;
                        return rotlin_term32(c, k < R ? w.nvf : w.nnewf, g0, p, q * R + (k % R));
                      },
                      w.vals, buf);
     else
-      warp_slot_sums(lane, 2 * R, s.na - 1, g0,
-                     [&](int k, int p) -> double {
+      warp_slot_sums(lane, nsl, s.na - 1, g0,
+                     [&](int sl, int p) -> double {
+                       int k = sl + first;
                        return rotlin_term64(c, k < R ? w.nv[1] : w.nnew, g0, p, q * R + (k % R));
                      },
                      w.vals, buf);
   } else {
     if (MIX)
-      warp_slot_sums(lane, 2 * R, s.na - 1, g0,
-                     [&](int k, int p) -> float {
+      warp_slot_sums(lane, nsl, s.na - 1, g0,
+                     [&](int sl, int p) -> float {
+                       int k = sl + first;
                        return rot3d_term32(c, frames, k < R ? w.fo[1] : w.fn, g0, p, q * R + (k % R));
                      },
                      w.vals, buf);
     else
-      warp_slot_sums(lane, 2 * R, s.na - 1, g0,
-                     [&](int k, int p) -> double {
+      warp_slot_sums(lane, nsl, s.na - 1, g0,
+                     [&](int sl, int p) -> double {
+                       int k = sl + first;
                        return rot3d_term64(c, frames, k < R ? w.fo[1] : w.fn, g0, p, q * R + (k % R));
                      },
                      w.vals, buf);
   }
   // 0: (q-1, q) old, 1: (q, q+1) old, 2: (q-1, q) new, 3: (q, q+1) new
-  if (lane < 4) {
+  if (lane < 4 && !(lane < 2 && w.link_ok[lane])) {
     int bad = 0;
     double rho;
     if (linear) {
-      double nn[3];
-      if (MIX) unit_vector(w.ang_new[0], w.ang_new[1], nn);
-      else for (int d = 0; d < 3; d++) nn[d] = w.nnew[d];
-      const double *na = (lane == 0 || lane == 2) ? w.nv[0] : (lane == 1 ? w.nv[1] : nn);
-      const double *nb = (lane == 0) ? w.nv[1] : (lane == 2 ? nn : w.nv[2]);
-      rho = link_density(c, true, w.fo[0], w.fo[0], na, nb, &bad);
+      if (MIX && c.t.rd4 && s.rot_den_type == 0) {
+        // FP32 path: 1 - cos(gamma) from the float unit vectors, stable for small angles
+        float fo0[3], fo2[3];
+        for (int d = 0; d < 3; d++) { fo0[d] = (float)w.nv[0][d]; fo2[d] = (float)w.nv[2][d]; }
+        const float *fa = (lane == 0 || lane == 2) ? fo0 : (lane == 1 ? w.nvf : w.nnewf);
+        const float *fb = (lane == 0) ? w.nvf : (lane == 2 ? w.nnewf : fo2);
+        rho = (double)srotdens32(c.t, one_minus_dot32(fa, fb));
+      } else {
+        double nn[3];
+        if (MIX) unit_vector(w.ang_new[0], w.ang_new[1], nn);
+        else for (int d = 0; d < 3; d++) nn[d] = w.nnew[d];
+        const double *na = (lane == 0 || lane == 2) ? w.nv[0] : (lane == 1 ? w.nv[1] : nn);
+        const double *nb = (lane == 0) ? w.nv[1] : (lane == 2 ? nn : w.nv[2]);
+        rho = link_density(c, true, w.fo[0], w.fo[0], na, nb, &bad);
+      }
     } else {
       const Frame &fa = (lane == 0 || lane == 2) ? w.fo[0] : (lane == 1 ? w.fo[1] : w.fn);
       const Frame &fb = (lane == 0) ? w.fo[1] : (lane == 2 ? w.fn : w.fo[2]);
@@ -276,8 +299,10 @@ __device__ int warp_rot(const Ctx &c, Frame *frames, int g0, int q, const double
   int acc = 0;
   if (lane == 0) {
     double pot_old = 0.0, pot_new = 0.0;
-    for (int k = 0; k < R; k++) pot_old += w.vals[k];
-    for (int k = 0; k < R; k++) pot_new += w.vals[R + k];
+    if (w.pot_cached) pot_old = w.pot_c;
+    else
+      for (int k = 0; k < R; k++) pot_old += w.vals[k];
+    for (int k = 0; k < R; k++) pot_new += w.vals[R - first + k];
     double boltz = rot_boltz(s, pot_old, pot_new);
     double logu = (s.rot_den_type != 0) ? log(u[linear ? 2 : 3]) : 0.0;
     double rd;
@@ -304,7 +329,18 @@ __device__ int warp_rot(const Ctx &c, Frame *frames, int g0, int q, const double
           for (int k = 0; k < 9; k++) frames[i1].mf[k] = w.fn.mf[k];
           frames[i1].hzf = w.fn.hzf;
         }
+        // the other rotors' potentials at slice q depend on this orientation
+        for (int rr = 0; rr < s.nrotors; rr++)
+          if (rr != r) c.st.rp_ok[rr * Q + q] = 0;
       }
+    }
+    c.st.rp_cache[i1] = acc ? pot_new : pot_old;
+    c.st.rp_ok[i1] = 1;
+    if (use_links && !w.bad) {
+      c.st.rl_cache[i0] = acc ? w.rho[2] : w.rho[0];
+      c.st.rl_cache[i1] = acc ? w.rho[3] : w.rho[1];
+      c.st.rl_ok[i0] = 1;
+      c.st.rl_ok[i1] = 1;
     }
   }
   acc = __shfl_sync(0xffffffffu, acc, 0);
@@ -326,13 +362,21 @@ __device__ int cta_mol(const Ctx &c, const Frame *frames, int type, int atom, ui
   for (int it = tid; it < s.P; it += blockDim.x) {
     size_t i = sidx(s, it, g);
     double x = c.st.x[i], y = c.st.y[i], z = c.st.z[i];
-    for (int a1 = 0; a1 < s.na; a1++) {
-      if (a1 == g) continue;
-      if (MIX) {
-        const float4 p4 = c.st.b4[i];
-        ao += (double)pair_term32(c, frames, g, a1, it, p4.x, p4.y, p4.z);
-        an += (double)pair_term32(c, frames, g, a1, it, (float)(x + d0), (float)(y + d1), (float)(z + d2));
-      } else {
+    if (MIX) {
+      // the slice's partner sums in float, one double add per slice
+      const float4 p4 = c.st.b4[i];
+      const float nx = (float)(x + d0), ny = (float)(y + d1), nz = (float)(z + d2);
+      float fo = 0.0f, fn = 0.0f;
+      for (int a1 = 0; a1 < s.na; a1++) {
+        if (a1 == g) continue;
+        fo += pair_term32(c, frames, g, a1, it, p4.x, p4.y, p4.z);
+        fn += pair_term32(c, frames, g, a1, it, nx, ny, nz);
+      }
+      ao += (double)fo;
+      an += (double)fn;
+    } else {
+      for (int a1 = 0; a1 < s.na; a1++) {
+        if (a1 == g) continue;
         ao += pair_term64(c, frames, g, a1, it, x, y, z);
         an += pair_term64(c, frames, g, a1, it, x + d0, y + d1, z + d2);
       }
@@ -359,11 +403,14 @@ __device__ int cta_mol(const Ctx &c, const Frame *frames, int type, int atom, ui
   }
   __syncthreads();
   const int a = *sacc;
-  if (a)
+  if (a) {
     for (int it = tid; it < s.P; it += blockDim.x) {
       size_t i = sidx(s, it, g);
       store_bead(c, i, c.st.x[i] + d0, c.st.y[i] + d1, c.st.z[i] + d2);
     }
+    // the whole path moved: every cached rotor potential is stale
+    for (int i = tid; i < s.nrotors * s.Q; i += blockDim.x) c.st.rp_ok[i] = 0;
+  }
   __syncthreads();
   return a;
 }

@@ -458,6 +458,18 @@ static pimc_status load_tables_into(pimc_handle *h, const pimc_tables *tb, DevTa
         (e = upload(h, a.data(), n, &t.rd_y2)) || (e = upload(h, b.data(), n, &t.rdv_y2)) ||
         (e = upload(h, c.data(), n, &t.rde_y2)))
       return e;
+    // FP32 path: the density spline words per interval, counted from the top
+    // node cos(gamma) = 1 of a uniform grid
+    t.rd4 = nullptr;
+    if (t.unirot && fabs(tb->rotgrid[n - 1] - 1.0) < 1e-9) {
+      std::vector<float4> w(n - 1);
+      for (int k = 0; k < n - 1; k++)
+        w[k] = make_float4((float)tb->rotdens[k], (float)a[k], (float)tb->rotdens[k + 1], (float)a[k + 1]);
+      if ((e = upload_f4(h, w, &t.rd4))) return e;
+      double hstep = 1.0 / t.ihrot;
+      t.f_ihrot = (float)t.ihrot;
+      t.f_hrot2_6 = (float)(hstep * hstep / 6.0);
+    }
   }
   if (need3drho) {
     if (tb->nth < 2 || tb->nph < 2 || tb->nch < 2 || !tb->rhoprp || !tb->erotpr || !tb->erotsq) {

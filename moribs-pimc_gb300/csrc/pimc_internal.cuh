@@ -65,6 +65,8 @@ struct DevTables {
   const float4 *vtab4;          // 3D point: value and its one-sided differences along r, theta, chi
   float f_irstep;
   const float4 *rho4;           // top density point: value and differences along chi, phi, theta
+  const float4 *rd4;            // linear-rotor density spline interval k: (y_k, y2_k, y_k+1, y2_k+1), uniform grid
+  float f_ihrot, f_hrot2_6;
   // reciprocals of grid steps for the double-precision leaves: a division by
   // a grid constant becomes a multiplication (within an ulp of the quotient)
   double d_thscale, d_chscale, d_irstep, d_idr2d, d_idc2d, d_dscale[3];
@@ -285,6 +287,30 @@ __device__ __forceinline__ double srotdens(const DevTables &t, double g, int whi
     return salpha * g + sbeta;
   }
   return splint(t.rg, d, y2, n, g, t.unirot, t.x0rot, t.ihrot);
+}
+
+// SRotDens on the FP32 path from dc = 1 - cos(gamma) >= 0 (computed as
+// |n - n'|^2 / 2, which keeps its relative precision for small angles): the
+// spline interval is counted down from the top node cos(gamma) = 1 of the
+// uniform grid, so the weights do not lose the digits that cos(gamma) itself
+// would
+__device__ __forceinline__ float srotdens32(const DevTables &t, float dc)
+{
+  const int n = t.nrot;
+  float tt = fmaxf(dc, 0.0f) * t.f_ihrot;           // grid steps below the top node
+  int kk = min((int)tt, n - 2);
+  float b = 1.0f - (tt - (float)kk);                // weight of node n-1-kk
+  if (b < 0.0f) b = 0.0f;
+  float a = 1.0f - b;
+  float4 w = __ldg(t.rd4 + (n - 2 - kk));
+  return a * w.x + b * w.z + ((a * a * a - a) * w.y + (b * b * b - b) * w.w) * t.f_hrot2_6;
+}
+
+// 1 - n.n' of two unit vectors, stable for small angles
+__device__ __forceinline__ float one_minus_dot32(const float *na, const float *nb)
+{
+  float dx = na[0] - nb[0], dy = na[1] - nb[1], dz = na[2] - nb[2];
+  return 0.5f * (dx * dx + dy * dy + dz * dz);
 }
 
 __device__ __forceinline__ double within1(double v)
@@ -683,6 +709,16 @@ __device__ __forceinline__ U4 philox4x32(U4 c, uint32_t k0, uint32_t k1)
     k1 += W1;
   }
   return c;
+}
+
+// two uniforms in (0,1) with 32-bit resolution from one Philox block, in
+// float (the FP32 path: no double conversion)
+__device__ __forceinline__ void philox_u2f(uint64_t seed, uint64_t a, uint32_t b, uint32_t c, float *u0, float *u1)
+{
+  U4 ctr = {(uint32_t)a, (uint32_t)(a >> 32), b, c};
+  U4 r = philox4x32(ctr, (uint32_t)seed, (uint32_t)(seed >> 32));
+  *u0 = ((float)r.x + 0.5f) * 2.3283064365386963e-10f;
+  *u1 = ((float)r.z + 0.5f) * 2.3283064365386963e-10f;
 }
 
 // two uniforms in (0,1) with 53-bit resolution from one Philox block

@@ -200,13 +200,13 @@ struct PhiloxSrc {
     philox_u2(seed, move, 0x100000u | ((uint32_t)level << 12) | (uint32_t)k, (uint32_t)dim, &r1, &r2);
     return sqrt(-log(r1)) * cos(2.0 * PIMC_PI * r2);        // Box-Muller as gauss() (mc_randg.cc:144)
   }
-  // the same draw with float logarithm and cosine (FP32 path); the 53-bit
-  // uniform keeps the tail out to 6 sigma
+  // a draw with float uniforms, logarithm and cosine (FP32 path); the
+  // 32-bit uniform keeps the tail out to 6.6 standard deviations
   __device__ double gauss_at32(int level, int k, int dim)
   {
-    double r1, r2;
-    philox_u2(seed, move, 0x100000u | ((uint32_t)level << 12) | (uint32_t)k, (uint32_t)dim, &r1, &r2);
-    return (double)(sqrtf(-logf((float)r1)) * cospif(2.0f * (float)r2));
+    float r1, r2;
+    philox_u2f(seed, move, 0x100000u | ((uint32_t)level << 12) | (uint32_t)k, (uint32_t)dim, &r1, &r2);
+    return (double)(sqrtf(-logf(r1)) * cospif(2.0f * r2));
   }
   __device__ void gauss_advance(long) {}
   __device__ double gauss_pre(long, int, int level, int k, int dim) { return gauss_at(0, level, k, dim); }
@@ -923,12 +923,21 @@ __device__ int rot_finish(const Ctx &c, Frame *frames, int g0, int q, bool linea
         int bad = 0;
         double rho;
         if (linear) {
-          double nn[3];
-          if (MIX) unit_vector(sh.ang_new[0], sh.ang_new[1], nn);
-          else for (int d = 0; d < 3; d++) nn[d] = sh.nnew[d];
-          const double *na = (lane == 0 || lane == 2) ? sh.nv[0] : (lane == 1 ? sh.nv[1] : nn);
-          const double *nb = (lane == 0) ? sh.nv[1] : (lane == 2 ? nn : sh.nv[2]);
-          rho = link_density(c, true, sh.fo[0], sh.fo[0], na, nb, &bad);
+          if (MIX && c.t.rd4 && s.rot_den_type == 0) {
+            // FP32 path: 1 - cos(gamma) from the float unit vectors, stable for small angles
+            float fo0[3], fo2[3];
+            for (int d = 0; d < 3; d++) { fo0[d] = (float)sh.nv[0][d]; fo2[d] = (float)sh.nv[2][d]; }
+            const float *fa = (lane == 0 || lane == 2) ? fo0 : (lane == 1 ? sh.nvf : sh.nnewf);
+            const float *fb = (lane == 0) ? sh.nvf : (lane == 2 ? sh.nnewf : fo2);
+            rho = (double)srotdens32(c.t, one_minus_dot32(fa, fb));
+          } else {
+            double nn[3];
+            if (MIX) unit_vector(sh.ang_new[0], sh.ang_new[1], nn);
+            else for (int d = 0; d < 3; d++) nn[d] = sh.nnew[d];
+            const double *na = (lane == 0 || lane == 2) ? sh.nv[0] : (lane == 1 ? sh.nv[1] : nn);
+            const double *nb = (lane == 0) ? sh.nv[1] : (lane == 2 ? nn : sh.nv[2]);
+            rho = link_density(c, true, sh.fo[0], sh.fo[0], na, nb, &bad);
+          }
         } else {
           const Frame &fa = (lane == 0 || lane == 2) ? sh.fo[0] : (lane == 1 ? sh.fo[1] : sh.fn);
           const Frame &fb = (lane == 0) ? sh.fo[1] : (lane == 2 ? sh.fn : sh.fo[2]);
