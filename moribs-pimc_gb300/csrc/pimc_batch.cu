@@ -23,7 +23,7 @@ struct WarpBis {
 struct WarpRot {
   Frame fo[3], fn;
   double ang_new[3], nv[3][3], nnew[3];
-  float nvf[3], nnewf[3];
+  float nvf[3], nnewf[3], nvf0[3], nvf2[3];
   double vals[2 * 16];
   double rho[4], pot_c;
   int bad, pot_cached, link_ok[2];
@@ -97,9 +97,13 @@ __device__ int warp_bisect(const Ctx &c, const Frame *frames, int type, int atom
     else w.gz[i] = src.gauss_pre(0, i, l, off / 3, off - 3 * (off / 3));
   }
   if (lane < L) {
-    double u = src.accept_u(lane);
-    w.ua[lane] = u;
-    w.lu[lane] = log(u);
+    if (MIX) {
+      w.lu[lane] = (double)logf(src.accept_uf(lane));
+    } else {
+      double u = src.accept_u(lane);
+      w.ua[lane] = u;
+      w.lu[lane] = log(u);
+    }
   }
   __syncwarp();
   for (int level = 0; level < L; level++) {
@@ -211,12 +215,20 @@ __device__ int warp_rot(const Ctx &c, Frame *frames, int g0, int q, const double
       make_frame32((float)prop[0], (float)prop[1], (float)prop[2], w.fn.mf, &w.fn.hzf);
     }
   }
+  const bool lazy = linear && lazy_linear(c, MIX);
   if (linear) {
     if (lane < 9) {
       int k = lane / 3, d = lane - 3 * (lane / 3);
       int ii = (k == 0) ? i0 : (k == 1 ? i1 : i2);
-      w.nv[k][d] = c.st.cosv[d * n + ii];
-      if (k == 1) w.nvf[d] = c.st.cosvf[d * n + ii];
+      if (lazy) {
+        float v = c.st.cosvf[d * n + ii];
+        if (k == 0) w.nvf0[d] = v;
+        else if (k == 1) w.nvf[d] = v;
+        else w.nvf2[d] = v;
+      } else {
+        w.nv[k][d] = c.st.cosv[d * n + ii];
+        if (k == 1) w.nvf[d] = c.st.cosvf[d * n + ii];
+      }
     }
   } else {
     copy_frame<false>(w.fo[0], frames + i0, lane);
@@ -265,10 +277,8 @@ __device__ int warp_rot(const Ctx &c, Frame *frames, int g0, int q, const double
     if (linear) {
       if (MIX && c.t.rd4 && s.rot_den_type == 0) {
         // FP32 path: 1 - cos(gamma) from the float unit vectors, stable for small angles
-        float fo0[3], fo2[3];
-        for (int d = 0; d < 3; d++) { fo0[d] = (float)w.nv[0][d]; fo2[d] = (float)w.nv[2][d]; }
-        const float *fa = (lane == 0 || lane == 2) ? fo0 : (lane == 1 ? w.nvf : w.nnewf);
-        const float *fb = (lane == 0) ? w.nvf : (lane == 2 ? w.nnewf : fo2);
+        const float *fa = (lane == 0 || lane == 2) ? w.nvf0 : (lane == 1 ? w.nvf : w.nnewf);
+        const float *fb = (lane == 0) ? w.nvf : (lane == 2 ? w.nnewf : w.nvf2);
         rho = (double)srotdens32(c.t, one_minus_dot32(fa, fb));
       } else {
         double nn[3];
@@ -303,23 +313,27 @@ __device__ int warp_rot(const Ctx &c, Frame *frames, int g0, int q, const double
     else
       for (int k = 0; k < R; k++) pot_old += w.vals[k];
     for (int k = 0; k < R; k++) pot_new += w.vals[R - first + k];
-    double boltz = rot_boltz(s, pot_old, pot_new);
-    double logu = (s.rot_den_type != 0) ? log(u[linear ? 2 : 3]) : 0.0;
+    double boltz = rot_boltz<MIX>(s, pot_old, pot_new);
+    double logu = rot_logu<MIX>(s, u[linear ? 2 : 3]);
     double rd;
     int neg = 0;
-    acc = rot_decide<MIX>(s, linear, w.rho, pot_old, pot_new, boltz, logu, u, &rd, &neg);
+    acc = rot_decide<MIX>(s, linear, w.rho, pot_old, pot_new, boltz, logu, u, &rd, &neg, false);
     if (neg) { atomicOr(c.st.err, (unsigned)DERR_NEG_DENSITY); acc = 0; }
     if (w.bad) { atomicOr(c.st.err, (unsigned)DERR_GRID_RANGE); acc = 0; }
     if (acc) {
       c.st.ang[i1] = w.ang_new[0];
       c.st.ang[n + i1] = w.ang_new[1];
       if (linear) {
-        double cv[3];
-        if (MIX) unit_vector(w.ang_new[0], w.ang_new[1], cv);
-        else for (int d = 0; d < 3; d++) cv[d] = w.nnew[d];
-        for (int d = 0; d < 3; d++) {
-          c.st.cosv[d * n + i1] = cv[d];
-          c.st.cosvf[d * n + i1] = (float)cv[d];
+        if (lazy) {
+          for (int d = 0; d < 3; d++) c.st.cosvf[d * n + i1] = w.nnewf[d];
+        } else {
+          double cv[3];
+          if (MIX) unit_vector(w.ang_new[0], w.ang_new[1], cv);
+          else for (int d = 0; d < 3; d++) cv[d] = w.nnew[d];
+          for (int d = 0; d < 3; d++) {
+            c.st.cosv[d * n + i1] = cv[d];
+            c.st.cosvf[d * n + i1] = (float)cv[d];
+          }
         }
       } else {
         c.st.ang[2 * n + i1] = w.ang_new[2];
@@ -507,8 +521,8 @@ __global__ void __launch_bounds__(256) k_batch_pass(const BatchRep *reps, const 
                   double u[4] = {0.5, 0.5, 0.5, 0.5}, prop[3] = {0.0, 0.0, 0.0};
                   if (lane == 0) {
                     size_t i1 = (size_t)rr * s.Q + q;
-                    rot_uniforms(sr, ps, phase, q >> 1, rr, linear, u);
-                    rot_propose(s, linear, c.st.ang[i1], c.st.ang[nq + i1], c.st.ang[2 * nq + i1], u, prop);
+                    rot_uniforms_t<MIX>(sr, ps, phase, q >> 1, rr, linear, u);
+                    rot_propose_t<MIX>(s, linear, c.st.ang[i1], c.st.ang[nq + i1], c.st.ang[2 * nq + i1], u, prop);
                   }
                   int acc = warp_rot<MIX>(c, frames, s.rot_first + rr, q, u, prop, linear, wm[warp].u.r, wm[warp].buf,
                                           lane);
@@ -604,6 +618,10 @@ __global__ void k_batch_refresh(const BatchRep *reps, int n, int derive)
       }
     } else if (derive) {
       for (int d = 0; d < 3; d++) c.st.cosvf[d * nq + i] = (float)c.st.cosv[d * nq + i];
+    } else if (c.s.nrotors > 0 && lazy_linear(c, c.s.mixed != 0)) {
+      double v[3];
+      unit_vector(phi, cost, v);
+      for (int d = 0; d < 3; d++) c.st.cosv[d * nq + i] = v[d];
     }
   }
   if (derive) {

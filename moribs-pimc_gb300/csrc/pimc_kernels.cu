@@ -132,7 +132,7 @@ struct RotSliceHooks {
   const DevSys *sys;
   uint64_t seed;
   unsigned pass, phase_next;
-  int h, pair, linear, has_next;
+  int h, pair, linear, has_next, mixed;
   // all lanes of the finishing warp: lane 0 polls until both neighbours have
   // finished half-sweep h-1, then every lane acquires the two progress words
   // itself, so that its own loads of the neighbours' state come after them
@@ -169,9 +169,15 @@ struct RotSliceHooks {
   __device__ void ahead(RotShared &sh)
   {
     if (!has_next) return;
-    rot_uniforms(seed, pass, phase_next, pair, 0, linear, sh.nxt_u);
-    rot_propose(*sys, linear, sh.ang_old[0], sh.ang_old[1], sh.ang_old[2], sh.nxt_u, sh.nxt_prop[0]);
-    rot_propose(*sys, linear, sh.ang_new[0], sh.ang_new[1], sh.ang_new[2], sh.nxt_u, sh.nxt_prop[1]);
+    if (mixed) {
+      rot_uniforms_t<true>(seed, pass, phase_next, pair, 0, linear, sh.nxt_u);
+      rot_propose_t<true>(*sys, linear, sh.ang_old[0], sh.ang_old[1], sh.ang_old[2], sh.nxt_u, sh.nxt_prop[0]);
+      rot_propose_t<true>(*sys, linear, sh.ang_new[0], sh.ang_new[1], sh.ang_new[2], sh.nxt_u, sh.nxt_prop[1]);
+    } else {
+      rot_uniforms(seed, pass, phase_next, pair, 0, linear, sh.nxt_u);
+      rot_propose(*sys, linear, sh.ang_old[0], sh.ang_old[1], sh.ang_old[2], sh.nxt_u, sh.nxt_prop[0]);
+      rot_propose(*sys, linear, sh.ang_new[0], sh.ang_new[1], sh.ang_new[2], sh.nxt_u, sh.nxt_prop[1]);
+    }
   }
 };
 
@@ -205,13 +211,14 @@ __global__ void __launch_bounds__(PIMC_ROT_THREADS) k_rot(Ctx c, Frame *frames, 
           if (p >= nurot) atomicOr(c.st.err, (unsigned)DERR_STREAM);
         }
       } else {
-        rot_uniforms(seed, *pass, phase, q >> 1, r, linear, u);
+        rot_uniforms_t<MIX>(seed, *pass, phase, q >> 1, r, linear, u);
       }
       size_t i1 = (size_t)r * c.s.Q + q;
-      rot_propose(c.s, linear, c.st.ang[i1], c.st.ang[n + i1], c.st.ang[2 * n + i1], u, prop);
+      if (REPLAY) rot_propose(c.s, linear, c.st.ang[i1], c.st.ang[n + i1], c.st.ang[2 * n + i1], u, prop);
+      else rot_propose_t<MIX>(c.s, linear, c.st.ang[i1], c.st.ang[n + i1], c.st.ang[2 * n + i1], u, prop);
     }
     int g0 = c.s.rot_first + r;
-    int acc = rot_step<MIX, false>(c, frames, g0, q, u, prop, linear, sh, nullptr);
+    int acc = rot_step<MIX, false>(c, frames, g0, q, u, prop, linear, sh, nullptr, REPLAY);
     double rd = sh.rd;          // written by the finishing warp
     if (threadIdx.x == 0) {
       if (REPLAY) {
@@ -262,8 +269,8 @@ __global__ void __launch_bounds__(PIMC_ROT_THREADS) k_rot_sweeps(Ctx c, Frame *f
       // the first move's uniforms and proposal read only this CTA's own slice
       // and are ready before the neighbour is
       size_t i1 = (size_t)(2 * p0 + parity);
-      rot_uniforms(seed, ps, phase, p0, 0, linear, u);
-      rot_propose(c.s, linear, c.st.ang[i1], c.st.ang[n + i1], c.st.ang[2 * n + i1], u, prop);
+      rot_uniforms_t<MIX>(seed, ps, phase, p0, 0, linear, u);
+      rot_propose_t<MIX>(c.s, linear, c.st.ang[i1], c.st.ang[n + i1], c.st.ang[2 * n + i1], u, prop);
       int st = 0;
       if (*(volatile unsigned *)abort_word) {
         atomicOr(c.st.err, (unsigned)DERR_TIMEOUT);
@@ -297,8 +304,8 @@ __global__ void __launch_bounds__(PIMC_ROT_THREADS) k_rot_sweeps(Ctx c, Frame *f
       for (int r = 0; r < nr; r++) {
         if (threadIdx.x == 0 && (p != p0 || r != 0)) {
           size_t i1 = (size_t)r * c.s.Q + q;
-          rot_uniforms(seed, ps, phase, p, r, linear, u);
-          rot_propose(c.s, linear, c.st.ang[i1], c.st.ang[n + i1], c.st.ang[2 * n + i1], u, prop);
+          rot_uniforms_t<MIX>(seed, ps, phase, p, r, linear, u);
+          rot_propose_t<MIX>(c.s, linear, c.st.ang[i1], c.st.ang[n + i1], c.st.ang[2 * n + i1], u, prop);
         }
         int acc = rot_step<MIX, true>(c, frames, c.s.rot_first + r, q, u, prop, linear, sh, nullptr);
         tot++;
@@ -577,8 +584,18 @@ __global__ void k_pass_begin(unsigned *pass) { *pass += 1; }
 // the float frames are kept as the moves evaluated them
 __global__ void k_refresh_frames(Ctx c, Frame *frames, int frames64)
 {
-  if (c.s.nrotors <= 0 || c.s.molecule[c.s.imtype] != 2) return;
+  if (c.s.nrotors <= 0) return;
   size_t n = (size_t)c.s.nrotors * c.s.Q;
+  if (c.s.molecule[c.s.imtype] == 1) {
+    // a linear rotor on the FP32 path: the double MCCosine from the angles
+    if (!lazy_linear(c, c.s.mixed != 0)) return;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+      double v[3];
+      unit_vector(c.st.ang[i], c.st.ang[n + i], v);
+      for (int d = 0; d < 3; d++) c.st.cosv[d * n + i] = v[d];
+    }
+    return;
+  }
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
     double phi = c.st.ang[i], cost = c.st.ang[n + i], chi = c.st.ang[2 * n + i];
     if (frames64) make_frame64(phi, cost, chi, frames[i]);
@@ -660,13 +677,14 @@ __global__ void __launch_bounds__(PIMC_ROT_THREADS) k_rot_slices(Ctx c, Frame *f
   hk.pass = ps;
   hk.pair = q >> 1;
   hk.linear = linear;
+  hk.mixed = MIX;
   unsigned long long tot = 0, nacc = 0;
   double u[4] = {0.5, 0.5, 0.5, 0.5}, prop[3] = {0.0, 0.0, 0.0};
   int h = q & 1;
   if (h < nhalf) {
     if (threadIdx.x == 0) {
-      rot_uniforms(seed, ps, phase0 + (unsigned)h, q >> 1, 0, linear, u);
-      rot_propose(c.s, linear, c.st.ang[q], c.st.ang[n + q], c.st.ang[2 * n + q], u, prop);
+      rot_uniforms_t<MIX>(seed, ps, phase0 + (unsigned)h, q >> 1, 0, linear, u);
+      rot_propose_t<MIX>(c.s, linear, c.st.ang[q], c.st.ang[n + q], c.st.ang[2 * n + q], u, prop);
     }
     rot_prepare<MIX>(c, frames, g0, q, u, prop, linear, sh);
   }

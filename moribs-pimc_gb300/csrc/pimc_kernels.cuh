@@ -187,6 +187,7 @@ struct ReplaySrc {
   __device__ double accept_u(int) { return take(u, nu, upos); }
   __device__ double disp_u(int) { return take(d, nd, dpos); }
   __device__ double gauss_at32(int, int, int) { return 0.0; }
+  __device__ float accept_uf(int) { return 0.5f; }
 };
 
 // counter-based source for production moves: one Philox block per draw
@@ -214,6 +215,12 @@ struct PhiloxSrc {
   {
     double u0, u1;
     philox_u2(seed, move, 0x200000u | (uint32_t)level, 0u, &u0, &u1);
+    return u0;
+  }
+  __device__ float accept_uf(int level)
+  {
+    float u0, u1;
+    philox_u2f(seed, move, 0x200000u | (uint32_t)level, 0u, &u0, &u1);
     return u0;
   }
   __device__ double disp_u(int dim)
@@ -308,9 +315,13 @@ __device__ int bisect_move(const Ctx &c, const Frame *frames, int type, int atom
   }
   if (Src::kPrefetchU)
     for (int l = tid - 64; l >= 0 && l < L; l += blockDim.x) {
-      double u = src.accept_u(l);
-      sh.ua[l] = u;
-      sh.lu[l] = log(u);
+      if (MIX) {
+        sh.lu[l] = (double)logf(src.accept_uf(l));          // a float uniform; the test itself in double
+      } else {
+        double u = src.accept_u(l);
+        sh.ua[l] = u;
+        sh.lu[l] = log(u);
+      }
     }
   __syncthreads();
   // the proposed beads, level by level (mc_piqmc.cc:243-254)
@@ -518,6 +529,7 @@ struct RotShared {
   double nnew[3];           // linear rotor: proposal unit vector (double path)
   double cv[3];             // linear rotor: MCCosine of the proposal
   float nvf[3], nnewf[3];   // linear rotor: current and proposal unit vectors for the FP32 path
+  float nvf0[3], nvf2[3];   // linear rotor: the neighbours' float unit vectors
   int bad, acc, pot_cached, link_ok[2], stop;
   int skip[2 * 16];
   double pot_c, rd;
@@ -664,6 +676,59 @@ __device__ __forceinline__ void rot_uniforms(uint64_t seed, unsigned pass, unsig
   if (linear) u[2] = u[3];
 }
 
+// Production draws.  FP64 path: rot_uniforms + rot_propose.  FP32 path: the
+// uniforms at float resolution (philox_u2f) and the proposal's increments
+// in float, added to the double angles (the path stays double); the
+// reference's reflection and wrap on the double angles.
+template <bool MIX>
+__device__ __forceinline__ void rot_uniforms_t(uint64_t seed, unsigned pass, unsigned phase, int p, int r,
+                                               bool linear, double u[4])
+{
+  if (!MIX) {
+    rot_uniforms(seed, pass, phase, p, r, linear, u);
+    return;
+  }
+  uint64_t mv = ((uint64_t)pass << 32) | ((uint64_t)phase << 12) | (uint64_t)p;
+  float a, b;
+  philox_u2f(seed, mv, 0x400000u | (uint32_t)r, 0u, &a, &b);
+  u[0] = (double)a; u[1] = (double)b;
+  philox_u2f(seed, mv, 0x400000u | (uint32_t)r, 1u, &a, &b);
+  u[2] = (double)a; u[3] = (double)b;
+  if (linear) u[2] = u[3];
+}
+
+template <bool MIX>
+__device__ __forceinline__ void rot_propose_t(const DevSys &s, bool linear, double phi, double cost, double chi,
+                                              const double u[4], double out[3])
+{
+  if (!MIX) {
+    rot_propose(s, linear, phi, cost, chi, u, out);
+    return;
+  }
+  const float st = (float)s.rtstep;
+  if (linear) {
+    cost += (double)(st * ((float)u[0] - 0.5f));
+    phi += (double)(st * ((float)u[1] - 0.5f));
+    if (cost > 1.0) cost = 2.0 - cost;
+    if (cost < -1.0) cost = -2.0 - cost;
+  } else {
+    const double pi2 = 2.0 * PIMC_PI;
+    const float tp = 6.28318530717959f * st;
+    cost += (double)(st * ((float)u[0] - 0.5f));
+    phi += (double)(tp * ((float)u[1] - 0.5f));
+    chi += (double)(tp * ((float)u[2] - 0.5f));
+    if (phi < 0.0) phi = pi2 + phi;
+    if (chi < 0.0) chi = pi2 + chi;
+    phi = fmod_2pi(phi, pi2);
+    chi = fmod_2pi(chi, pi2);
+    if (cost > 1.0) cost = 2.0 - cost;
+    if (cost < -1.0) cost = -2.0 - cost;
+  }
+  out[0] = phi;
+  out[1] = cost;
+  out[2] = chi;
+}
+
 // The acceptance of a rotational move from its four link densities (old
 // (q-1,q), old (q,q+1), new, new), the potentials, the Boltzmann factor
 // boltz = exp(-tau (pot_new - pot_old)) (Noya densities) or its exponent
@@ -673,7 +738,7 @@ __device__ __forceinline__ void rot_uniforms(uint64_t seed, unsigned pass, unsig
 template <bool MIX>
 __device__ __forceinline__ int rot_decide(const DevSys &s, bool linear, const double rho[4], double pot_old,
                                           double pot_new, double boltz, double logu, const double u[4], double *rd_out,
-                                          int *neg_out)
+                                          int *neg_out, bool need_rd = true)
 {
   double rd;
   int acc = 0, neg = 0;
@@ -689,8 +754,11 @@ __device__ __forceinline__ int rot_decide(const DevSys &s, bool linear, const do
       dens_new = fabsf(dens_new);
     }
     float rf = (dens_old > (float)PIMC_RZERO) ? dens_new / dens_old : 1.0f;
-    rd = (double)rf * boltz;                                  // FP64 Boltzmann factor
-    acc = (rd > 1.0) || (rd > u[linear ? 2 : 3]);
+    // boltz holds the exponent -tau (pot_new - pot_old) here: the test in
+    // double as log(ratio) + exponent against 0 and log u
+    double lr = (rf > 0.0f) ? (double)logf(rf) + boltz : -1.0e300;
+    acc = (lr > 0.0) || (lr > logu);
+    rd = need_rd ? (double)rf * exp(boltz) : 0.0;
   } else if (s.rot_den_type == 0) {
     double dens_old = rho[0] * rho[1], dens_new = rho[2] * rho[3];
     if (fabs(dens_old) < PIMC_RZERO) dens_old = 0.0;
@@ -723,10 +791,27 @@ __device__ __forceinline__ int rot_decide(const DevSys &s, bool linear, const do
   return acc;
 }
 
-// Boltzmann factor (Noya densities) or exponent (RS densities) of a move
+// Boltzmann factor (FP64 path, Noya densities) or its exponent (FP32 path,
+// or RS densities) of a move, and log u of its accept uniform
+template <bool MIX>
 __device__ __forceinline__ double rot_boltz(const DevSys &s, double pot_old, double pot_new)
 {
-  return (s.rot_den_type == 0) ? exp(-s.tau * (pot_new - pot_old)) : -(s.tau * (pot_new - pot_old));
+  return (!MIX && s.rot_den_type == 0) ? exp(-s.tau * (pot_new - pot_old)) : -(s.tau * (pot_new - pot_old));
+}
+template <bool MIX>
+__device__ __forceinline__ double rot_logu(const DevSys &s, double u)
+{
+  if (MIX) return (double)logf((float)u);
+  return (s.rot_den_type != 0) ? log(u) : 0.0;
+}
+
+// A linear rotor on the FP32 path with the float density spline keeps its
+// orientation as the angles plus the float unit vector (MCCosine in float);
+// the double MCCosine is derived from the angles afterwards
+// (k_refresh_frames), like a top's double frame.
+__device__ __forceinline__ bool lazy_linear(const Ctx &c, bool mix)
+{
+  return mix && c.s.rot_den_type == 0 && c.t.rd4 != nullptr;
 }
 
 // MCRotLinStep (mc_piqmc.cc:781-936) / MCRot3Dstep (mc_piqmc.cc:938-1199),
@@ -833,9 +918,10 @@ __device__ void rot_prepare(const Ctx &c, const Frame *frames, int g0, int q, co
         for (int k = 0; k < R; k++) pn += sh.valsf[R - first + k];
         sh.pot_old = sh.pot_cached ? sh.pot_c : (double)po;
         sh.pot_new = (double)pn;
-        // the action difference and its exponent in double precision
-        sh.boltz = (s.rot_den_type == 0) ? exp(-s.tau * (sh.pot_new - sh.pot_old)) : -(s.tau * (sh.pot_new - sh.pot_old));
-        if (s.rot_den_type != 0) sh.logu = log(sh.u[linear ? 2 : 3]);
+        // the action difference in double precision; the test compares it in
+        // the log domain (rot_decide)
+        sh.boltz = rot_boltz<true>(s, sh.pot_old, sh.pot_new);
+        sh.logu = rot_logu<true>(s, sh.u[linear ? 2 : 3]);
       } else {
         double pot_old = 0.0, pot_new = 0.0;
         if (sh.pot_cached) pot_old = sh.pot_c;
@@ -849,7 +935,7 @@ __device__ void rot_prepare(const Ctx &c, const Frame *frames, int g0, int q, co
       }
     }
   } else if (warp == 9) {
-    if (lane == 0 && linear) {
+    if (lane == 0 && linear && !lazy_linear(c, MIX)) {
       if (MIX) unit_vector(sh.ang_new[0], sh.ang_new[1], sh.cv);
       else for (int d = 0; d < 3; d++) sh.cv[d] = sh.nnew[d];
     }
@@ -872,7 +958,7 @@ struct RotNoHooks {
 // write them).  All PIMC_ROT_THREADS threads call it; returns 1 if accepted.
 template <bool MIX, bool COH, class Hooks>
 __device__ int rot_finish(const Ctx &c, Frame *frames, int g0, int q, bool linear, RotShared &sh, double *rd_out,
-                          Hooks &hooks)
+                          Hooks &hooks, bool need_rd = false)
 {
   const DevSys &s = c.s;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -894,7 +980,14 @@ __device__ int rot_finish(const Ctx &c, Frame *frames, int g0, int q, bool linea
       if (linear) {
         if (lane < 6) {
           int k = (lane < 3) ? 0 : 2, d = lane - (lane < 3 ? 0 : 3);
-          sh.nv[k][d] = ld_state<COH>(c.st.cosv + d * n + (k == 0 ? i0 : i2));
+          size_t ii = d * n + (k == 0 ? i0 : i2);
+          if (lazy_linear(c, MIX)) {
+            float v = COH ? __ldcg(c.st.cosvf + ii) : c.st.cosvf[ii];
+            if (k == 0) sh.nvf0[d] = v;
+            else sh.nvf2[d] = v;
+          } else {
+            sh.nv[k][d] = ld_state<COH>(c.st.cosv + ii);
+          }
         }
       } else if (mf_only) {
         // words of Frame::mf and Frame::hzf
@@ -925,10 +1018,8 @@ __device__ int rot_finish(const Ctx &c, Frame *frames, int g0, int q, bool linea
         if (linear) {
           if (MIX && c.t.rd4 && s.rot_den_type == 0) {
             // FP32 path: 1 - cos(gamma) from the float unit vectors, stable for small angles
-            float fo0[3], fo2[3];
-            for (int d = 0; d < 3; d++) { fo0[d] = (float)sh.nv[0][d]; fo2[d] = (float)sh.nv[2][d]; }
-            const float *fa = (lane == 0 || lane == 2) ? fo0 : (lane == 1 ? sh.nvf : sh.nnewf);
-            const float *fb = (lane == 0) ? sh.nvf : (lane == 2 ? sh.nnewf : fo2);
+            const float *fa = (lane == 0 || lane == 2) ? sh.nvf0 : (lane == 1 ? sh.nvf : sh.nnewf);
+            const float *fb = (lane == 0) ? sh.nvf : (lane == 2 ? sh.nnewf : sh.nvf2);
             rho = (double)srotdens32(c.t, one_minus_dot32(fa, fb));
           } else {
             double nn[3];
@@ -960,7 +1051,8 @@ __device__ int rot_finish(const Ctx &c, Frame *frames, int g0, int q, bool linea
         const double pot_old = sh.pot_old, pot_new = sh.pot_new;
         double rd;
         int neg = 0;
-        int acc = rot_decide<MIX>(s, linear, sh.rho, pot_old, pot_new, sh.boltz, sh.logu, sh.u, &rd, &neg);
+        int acc = rot_decide<MIX>(s, linear, sh.rho, pot_old, pot_new, sh.boltz, sh.logu, sh.u, &rd, &neg,
+                                  need_rd || rd_out != nullptr);
         if (neg) { atomicOr(c.st.err, (unsigned)DERR_NEG_DENSITY); acc = 0; }
         if (sh.bad) { atomicOr(c.st.err, (unsigned)DERR_GRID_RANGE); acc = 0; }
         sh.rd = rd;
@@ -970,9 +1062,13 @@ __device__ int rot_finish(const Ctx &c, Frame *frames, int g0, int q, bool linea
           c.st.ang[i1] = sh.ang_new[0];
           c.st.ang[n + i1] = sh.ang_new[1];
           if (linear) {
-            for (int d = 0; d < 3; d++) {
-              c.st.cosv[d * n + i1] = sh.cv[d];
-              c.st.cosvf[d * n + i1] = (float)sh.cv[d];
+            if (lazy_linear(c, MIX)) {
+              for (int d = 0; d < 3; d++) c.st.cosvf[d * n + i1] = sh.nnewf[d];
+            } else {
+              for (int d = 0; d < 3; d++) {
+                c.st.cosv[d * n + i1] = sh.cv[d];
+                c.st.cosvf[d * n + i1] = (float)sh.cv[d];
+              }
             }
           } else {
             c.st.ang[2 * n + i1] = sh.ang_new[2];
@@ -1008,11 +1104,11 @@ __device__ int rot_finish(const Ctx &c, Frame *frames, int g0, int q, bool linea
 // the whole move: rot_prepare then rot_finish
 template <bool MIX, bool COH>
 __device__ int rot_step(const Ctx &c, Frame *frames, int g0, int q, const double u[4], const double prop[3],
-                        bool linear, RotShared &sh, double *rd_out)
+                        bool linear, RotShared &sh, double *rd_out, bool need_rd = false)
 {
   rot_prepare<MIX>(c, frames, g0, q, u, prop, linear, sh);
   RotNoHooks hk;
-  return rot_finish<MIX, COH>(c, frames, g0, q, linear, sh, rd_out, hk);
+  return rot_finish<MIX, COH>(c, frames, g0, q, linear, sh, rd_out, hk, need_rd);
 }
 
 // ------------------------------------------------------ estimator terms
