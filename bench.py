@@ -364,7 +364,7 @@ def run_batched(args, local, dist):
     import workloads as W
     ws = W.config2(n=args.batched_replicas, seed=2024 + 7 * (dist.get_rank() if dist else 0))
     b = G.Batch(ws, device=local, mixed=True)
-    warps, tune_ms = b.autotune(77)
+    shape, tune_ms = b.autotune(77)
     ext = torch.cuda.ExternalStream(b.stream(), device=torch.device("cuda", local))
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
     b.run_passes(1, 78)
@@ -391,7 +391,9 @@ def run_batched(args, local, dist):
                        "{64,128,256,512}, Q=P/4, T in 0.3-2.0 K)" % len(ws),
            "value": bm * steps * world / (total_ms / 1e3), "unit": UNIT, "ms_per_pass": total_ms / steps,
            "steps": steps, "bead_moves_per_pass": bm, "precision": "mixed", "dtype": "f32+f64",
-           "warps_per_cta": warps, "autotune_ms_per_pass": {"2": tune_ms[0], "4": tune_ms[1], "8": tune_ms[2]},
+           "shape": {"warps_per_cta": shape[0], "ctas_per_sm_bound": shape[1]},
+           "autotune_ms_per_pass": {"%dx%d" % sh: t for sh, t in zip(((2, 2), (4, 2), (8, 2), (4, 3), (8, 3), (2, 3)),
+                                                                         [float(x) for x in tune_ms])},
            "accept_ratios": {"He bisection": acc[1] / max(1, tot[1]), "rotation": acc[5] / max(1, tot[5])}}
     b.close()
     return out

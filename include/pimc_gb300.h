@@ -148,10 +148,12 @@ pimc_status pimc_batch_set_state(pimc_batch *b, int replica, const double *coord
 pimc_status pimc_batch_get_state(pimc_batch *b, int replica, double *coords, double *angles, double *cosine,
                                  int *pindex);
 pimc_status pimc_batch_set_precision(pimc_batch *b, int mixed);
-/* warps per CTA (2, 4 or 8); pimc_batch_autotune times one pass of each and
- * keeps the fastest (the passes run: the replicas move on) */
-pimc_status pimc_batch_set_shape(pimc_batch *b, int warps);
-pimc_status pimc_batch_autotune(pimc_batch *b, uint64_t seed, int *warps_out, double *ms_out);
+/* launch shape: warps per CTA (2, 4 or 8) and the resident CTAs per SM the
+ * kernel's registers are bounded for (2 or 3).  pimc_batch_autotune times one
+ * pass of each of six shapes (the passes run: the replicas move on), keeps
+ * the fastest and returns it in shape_out[2] and the six times in ms_out[6] */
+pimc_status pimc_batch_set_shape(pimc_batch *b, int warps, int min_blocks);
+pimc_status pimc_batch_autotune(pimc_batch *b, uint64_t seed, int *shape_out, double *ms_out);
 pimc_status pimc_batch_run_passes(pimc_batch *b, int npasses, uint64_t seed);
 /* per replica 4 values: E_kin, E_pot, E_rot (as pimc_estimators out[0..2])
  * and the mean z component of the rotor axis over the rotational slices */

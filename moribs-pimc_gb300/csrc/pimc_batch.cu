@@ -9,7 +9,7 @@
 #include "pimc_kernels.cuh"
 #include "pimc_launch.h"
 
-#define PIMC_BATCH_BUF 512            /* doubles in a warp's item buffer */
+#define PIMC_BATCH_BUF 256            /* doubles in a warp's item buffer */
 
 struct WarpBis {
   double gz[3 * PIMC_BATCH_MAX_SEG];
@@ -431,10 +431,11 @@ __device__ int cta_mol(const Ctx &c, const Frame *frames, int type, int atom, ui
 
 __global__ void k_batch_reset(unsigned *work) { *work = 0u; }
 
-// one production pass of every replica
-template <bool MIX>
-__global__ void __launch_bounds__(256) k_batch_pass(const BatchRep *reps, const int *order, int n, uint64_t seed,
-                                                    unsigned *work)
+// one production pass of every replica; MINB: resident CTAs per SM the
+// register allocation is bounded for (a shape the autotuner tries)
+template <bool MIX, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_batch_pass(const BatchRep *reps, const int *order, int n,
+                                                          uint64_t seed, unsigned *work)
 {
   extern __shared__ __align__(16) unsigned char smem[];
   Ctx &c = *reinterpret_cast<Ctx *>(smem);
@@ -634,31 +635,41 @@ __global__ void k_batch_refresh(const BatchRep *reps, int n, int derive)
 // ------------------------------------------------------------ launchers
 size_t batch_smem_bytes(int warps) { return PIMC_BATCH_CTX_BYTES + (size_t)warps * sizeof(WarpMem); }
 
-int batch_max_ctas(int mixed, int warps)
+template <bool MIX, int MINB>
+static int batch_occupancy(int warps, size_t sm)
 {
-  int dev = 0, nsm = 0, per = 0;
+  int per = 0;
+  cudaFuncSetAttribute(k_batch_pass<MIX, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  cudaFuncSetAttribute(k_batch_pass<MIX, MINB>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_batch_pass<MIX, MINB>, 32 * warps, sm) != cudaSuccess)
+    return 0;
+  return per;
+}
+
+int batch_max_ctas(int mixed, int warps, int minb)
+{
+  int dev = 0, nsm = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return 0;
   if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
   size_t sm = batch_smem_bytes(warps);
-  cudaError_t e;
-  if (mixed) {
-    cudaFuncSetAttribute(k_batch_pass<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_batch_pass<true>, 32 * warps, sm);
-  } else {
-    cudaFuncSetAttribute(k_batch_pass<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_batch_pass<false>, 32 * warps, sm);
-  }
-  if (e != cudaSuccess) return 0;
+  int per;
+  if (mixed) per = (minb >= 3) ? batch_occupancy<true, 3>(warps, sm) : batch_occupancy<true, 2>(warps, sm);
+  else per = (minb >= 3) ? batch_occupancy<false, 3>(warps, sm) : batch_occupancy<false, 2>(warps, sm);
   return nsm * per;
 }
 
 void launch_batch_pass(const BatchRep *reps, const int *order, int n, uint64_t seed, unsigned *work, int mixed,
-                       int warps, int nctas, cudaStream_t s)
+                       int warps, int minb, int nctas, cudaStream_t s)
 {
   size_t sm = batch_smem_bytes(warps);
   k_batch_reset<<<1, 1, 0, s>>>(work);
-  if (mixed) k_batch_pass<true><<<nctas, 32 * warps, sm, s>>>(reps, order, n, seed, work);
-  else k_batch_pass<false><<<nctas, 32 * warps, sm, s>>>(reps, order, n, seed, work);
+  if (mixed) {
+    if (minb >= 3) k_batch_pass<true, 3><<<nctas, 32 * warps, sm, s>>>(reps, order, n, seed, work);
+    else k_batch_pass<true, 2><<<nctas, 32 * warps, sm, s>>>(reps, order, n, seed, work);
+  } else {
+    if (minb >= 3) k_batch_pass<false, 3><<<nctas, 32 * warps, sm, s>>>(reps, order, n, seed, work);
+    else k_batch_pass<false, 2><<<nctas, 32 * warps, sm, s>>>(reps, order, n, seed, work);
+  }
 }
 
 void launch_batch_est(const BatchRep *reps, int n, double *out, cudaStream_t s)

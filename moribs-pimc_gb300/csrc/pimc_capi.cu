@@ -1236,12 +1236,12 @@ struct pimc_batch {
   double *d_est = nullptr;
   unsigned long long *d_cnt = nullptr;
   unsigned *d_pass = nullptr;
-  int warps = 4;
+  int warps = 8, minb = 2;
   int mixed = 0;
   bool tables = false;
   cudaGraphExec_t exec = nullptr;
   uint64_t exec_seed = 0;
-  int exec_warps = 0, exec_mixed = -1;
+  int exec_warps = 0, exec_minb = 0, exec_mixed = -1;
   double bm_pass = 0.0;
 };
 
@@ -1508,10 +1508,11 @@ extern "C" pimc_status pimc_batch_set_precision(pimc_batch *b, int mixed)
   return batch_upload_reps(b);
 }
 
-extern "C" pimc_status pimc_batch_set_shape(pimc_batch *b, int warps)
+extern "C" pimc_status pimc_batch_set_shape(pimc_batch *b, int warps, int min_blocks)
 {
-  if (!b || (warps != 2 && warps != 4 && warps != 8)) return PIMC_ERR_BAD_ARG;
+  if (!b || (warps != 2 && warps != 4 && warps != 8) || (min_blocks != 2 && min_blocks != 3)) return PIMC_ERR_BAD_ARG;
   b->warps = warps;
+  b->minb = min_blocks;
   return PIMC_OK;
 }
 
@@ -1531,14 +1532,15 @@ extern "C" pimc_status pimc_batch_run_passes(pimc_batch *b, int npasses, uint64_
   if (npasses < 0) return PIMC_ERR_BAD_ARG;
   pimc_handle *h = b->base;
   CK(cudaSetDevice(h->device));
-  if (!b->exec || b->exec_seed != seed || b->exec_warps != b->warps || b->exec_mixed != b->mixed) {
+  if (!b->exec || b->exec_seed != seed || b->exec_warps != b->warps || b->exec_minb != b->minb ||
+      b->exec_mixed != b->mixed) {
     if (b->exec) { BK(cudaGraphExecDestroy(b->exec)); b->exec = nullptr; }
-    int nctas = batch_max_ctas(b->mixed, b->warps);
+    int nctas = batch_max_ctas(b->mixed, b->warps, b->minb);
     if (nctas <= 0) return PIMC_ERR_CUDA;
     if (nctas > b->n) nctas = b->n;
     cudaGraph_t graph;
     CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-    launch_batch_pass(b->d_reps, b->d_order, b->n, seed, b->d_work, b->mixed, b->warps, nctas, h->stream);
+    launch_batch_pass(b->d_reps, b->d_order, b->n, seed, b->d_work, b->mixed, b->warps, b->minb, nctas, h->stream);
     cudaError_t le = cudaGetLastError();
     cudaError_t ce = cudaStreamEndCapture(h->stream, &graph);
     if (le != cudaSuccess || ce != cudaSuccess) {
@@ -1551,6 +1553,7 @@ extern "C" pimc_status pimc_batch_run_passes(pimc_batch *b, int npasses, uint64_
     if (ie != cudaSuccess) { h->last_cuda = ie; return PIMC_ERR_CUDA; }
     b->exec_seed = seed;
     b->exec_warps = b->warps;
+    b->exec_minb = b->minb;
     b->exec_mixed = b->mixed;
   }
   for (int p = 0; p < npasses; p++) {
@@ -1565,21 +1568,25 @@ extern "C" pimc_status pimc_batch_run_passes(pimc_batch *b, int npasses, uint64_
   return PIMC_OK;
 }
 
-extern "C" pimc_status pimc_batch_autotune(pimc_batch *b, uint64_t seed, int *warps_out, double *ms_out)
+// the shapes tried: warps per CTA x CTAs per SM the registers are bounded for
+static const int g_batch_shapes[6][2] = {{2, 2}, {4, 2}, {8, 2}, {4, 3}, {8, 3}, {2, 3}};
+
+extern "C" pimc_status pimc_batch_autotune(pimc_batch *b, uint64_t seed, int *shape_out, double *ms_out)
 {
   pimc_status e = batch_ready(b);
   if (e) return e;
   pimc_handle *h = b->base;
   CK(cudaSetDevice(h->device));
-  const int cand[3] = {2, 4, 8};
   double best = 1e300;
-  int bw = b->warps;
+  int bw = b->warps, bm = b->minb;
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
-  for (int k = 0; k < 3; k++) {
-    b->warps = cand[k];
-    if (batch_max_ctas(b->mixed, b->warps) <= 0) continue;
+  for (int k = 0; k < 6; k++) {
+    b->warps = g_batch_shapes[k][0];
+    b->minb = g_batch_shapes[k][1];
+    if (ms_out) ms_out[k] = 0.0;
+    if (batch_max_ctas(b->mixed, b->warps, b->minb) <= 0) continue;
     if ((e = pimc_batch_run_passes(b, 1, seed))) return e;      // graph build and warm-up
     CK(cudaEventRecord(e0, h->stream));
     if ((e = pimc_batch_run_passes(b, 1, seed))) return e;
@@ -1588,12 +1595,13 @@ extern "C" pimc_status pimc_batch_autotune(pimc_batch *b, uint64_t seed, int *wa
     float ms = 0.f;
     CK(cudaEventElapsedTime(&ms, e0, e1));
     if (ms_out) ms_out[k] = ms;
-    if (ms < best) { best = ms; bw = cand[k]; }
+    if (ms < best) { best = ms; bw = b->warps; bm = b->minb; }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   b->warps = bw;
-  if (warps_out) *warps_out = bw;
+  b->minb = bm;
+  if (shape_out) { shape_out[0] = bw; shape_out[1] = bm; }
   return check_err(h);
 }
 

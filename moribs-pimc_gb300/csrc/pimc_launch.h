@@ -52,8 +52,8 @@ struct BatchRep {
 #define PIMC_BATCH_CTX_BYTES (((sizeof(Ctx) + 15) / 16) * 16)
 
 size_t batch_smem_bytes(int warps);
-int batch_max_ctas(int mixed, int warps);
+int batch_max_ctas(int mixed, int warps, int minb);
 void launch_batch_pass(const BatchRep *reps, const int *order, int n, uint64_t seed, unsigned *work, int mixed,
-                       int warps, int nctas, cudaStream_t s);
+                       int warps, int minb, int nctas, cudaStream_t s);
 void launch_batch_est(const BatchRep *reps, int n, double *out, cudaStream_t s);
 void launch_batch_refresh(const BatchRep *reps, int n, int derive, cudaStream_t s);

@@ -74,7 +74,7 @@ def load(path=LIBPATH):
     L.pimc_batch_set_state.argtypes = [vp, C.c_int, _dp, _dp, _ip]
     L.pimc_batch_get_state.argtypes = [vp, C.c_int, _dp, _dp, _dp, _ip]
     L.pimc_batch_set_precision.argtypes = [vp, C.c_int]
-    L.pimc_batch_set_shape.argtypes = [vp, C.c_int]
+    L.pimc_batch_set_shape.argtypes = [vp, C.c_int, C.c_int]
     L.pimc_batch_autotune.argtypes = [vp, C.c_uint64, _ip, _dp]
     L.pimc_batch_run_passes.argtypes = [vp, C.c_int, C.c_uint64]
     L.pimc_batch_estimators.argtypes = [vp, _dp]
@@ -287,13 +287,14 @@ class Batch:
         _chk(self.L.pimc_batch_get_state(self.h, int(i), dptr(c), dptr(a), dptr(co), iptr(p)), "pimc_batch_get_state")
         return c, a, co, p
 
-    def set_shape(self, warps):
-        _chk(self.L.pimc_batch_set_shape(self.h, int(warps)), "pimc_batch_set_shape")
+    def set_shape(self, warps, min_blocks=2):
+        _chk(self.L.pimc_batch_set_shape(self.h, int(warps), int(min_blocks)), "pimc_batch_set_shape")
 
     def autotune(self, seed):
-        wo = np.zeros(1, np.int32); ms = np.zeros(3)
+        """(warps, min_blocks) of the fastest shape and the six times (ms per pass)."""
+        wo = np.zeros(2, np.int32); ms = np.zeros(6)
         _chk(self.L.pimc_batch_autotune(self.h, C.c_uint64(seed), iptr(wo), dptr(ms)), "pimc_batch_autotune")
-        return int(wo[0]), ms
+        return (int(wo[0]), int(wo[1])), ms
 
     def run_passes(self, n, seed):
         _chk(self.L.pimc_batch_run_passes(self.h, int(n), C.c_uint64(seed)), "pimc_batch_run_passes")

@@ -51,9 +51,9 @@ def test_batch_replicas_equal_single_systems_fp64():
 def test_batch_shape_does_not_change_the_paths(mixed):
     ws = _small(n=7, seed=8)
     states = []
-    for warps in (2, 8):
+    for warps, minb in ((2, 2), (8, 3)):
         b = G.Batch(ws, mixed=mixed)
-        b.set_shape(warps)
+        b.set_shape(warps, minb)
         b.run_passes(2, 5)
         b.synchronize()
         states.append([b.get_state(r)[0] for r in range(len(ws))])
@@ -86,8 +86,8 @@ def test_batch_estimators_equal_single_system_estimators():
 def test_batch_counts_the_reference_schedule_and_autotunes():
     ws = _small(n=6, seed=21)
     b = G.Batch(ws, mixed=True)
-    warps, ms = b.autotune(33)
-    assert warps in (2, 4, 8) and np.all(ms > 0)
+    shape, ms = b.autotune(33)
+    assert shape[0] in (2, 4, 8) and shape[1] in (2, 3) and np.all(ms > 0)
     tot0, _ = b.counters()
     b.run_passes(1, 34)
     tot, acc = b.counters()
