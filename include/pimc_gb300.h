@@ -130,6 +130,20 @@ long long   pimc_launch_count(const pimc_handle *h);
 void       *pimc_stream(const pimc_handle *h);
 const char *pimc_status_string(pimc_status s);
 
+/* ---- restart files and configurations ------------------------------------
+ * pimc_save_checkpoint / pimc_load_checkpoint: the whole path, PIndex, the
+ * pass counter and the move counters (the reference's ConfigIO,
+ * mc_input.cc:560-600, keeps the first row of MCCoords and MCCosine only);
+ * loading checks the system's sizes and temperature, and a continued run with
+ * the same seed repeats the uninterrupted one.  pimc_write_xyz /
+ * pimc_read_xyz: IOxyz's text format (mc_input.cc:690-794), labels from
+ * type_names (may be NULL); reading sets the rotor angles from the unit
+ * vectors with chi = 0, as the format keeps no third angle. */
+pimc_status pimc_save_checkpoint(pimc_handle *h, const char *path);
+pimc_status pimc_load_checkpoint(pimc_handle *h, const char *path);
+pimc_status pimc_write_xyz(pimc_handle *h, const char *path, const char *const *type_names);
+pimc_status pimc_read_xyz(pimc_handle *h, const char *path);
+
 /* ---- replica batches (no reference counterpart) --------------------------
  * Many independent systems of one species family -- the same types,
  * molecules, masses, levels (<= 4) and steps, each with its own particle

@@ -202,10 +202,7 @@ __device__ int warp_rot(const Ctx &c, Frame *frames, int g0, int q, const double
     w.ang_new[0] = prop[0]; w.ang_new[1] = prop[1]; w.ang_new[2] = prop[2];
     if (linear) {
       if (MIX) {
-        float sp, cp, ct = (float)prop[1];
-        sincosf((float)prop[0], &sp, &cp);
-        float st = sqrtf(fmaxf(1.0f - ct * ct, 0.0f));
-        w.nnewf[0] = st * cp; w.nnewf[1] = st * sp; w.nnewf[2] = ct;
+        unit_vector32((float)prop[0], (float)prop[1], w.nnewf);
       } else {
         unit_vector(prop[0], prop[1], w.nnew);
       }
@@ -618,7 +615,15 @@ __global__ void k_batch_refresh(const BatchRep *reps, int n, int derive)
         c.st.cosvf[d * nq + i] = (float)v[d];
       }
     } else if (derive) {
-      for (int d = 0; d < 3; d++) c.st.cosvf[d * nq + i] = (float)c.st.cosv[d * nq + i];
+      if (c.s.nrotors > 0 && lazy_linear(c, c.s.mixed != 0)) {
+        float v[3];
+        unit_vector32((float)phi, (float)cost, v);          // as the FP32 moves write it
+        for (int d = 0; d < 3; d++) c.st.cosvf[d * nq + i] = v[d];
+      } else {
+        for (int d = 0; d < 3; d++) c.st.cosvf[d * nq + i] = (float)c.st.cosv[d * nq + i];
+      }
+      c.st.rp_ok[i] = 0;
+      c.st.rl_ok[i] = 0;
     } else if (c.s.nrotors > 0 && lazy_linear(c, c.s.mixed != 0)) {
       double v[3];
       unit_vector(phi, cost, v);

@@ -528,6 +528,11 @@ extern "C" pimc_status pimc_load_tables(pimc_handle *h, const pimc_tables *tb)
   CK(cudaSetDevice(h->device));
   pimc_status e = load_tables_into(h, tb, h->ctx.t, h->ctx.s, TAB_POT | TAB_ROT);
   if (e) return e;
+  if (h->state) {
+    launch_derive_state(h->ctx, h->frames, h->stream);     // the float copies follow the tables' path choice
+    h->launches++;
+    CK(cudaGetLastError());
+  }
   CK(cudaStreamSynchronize(h->stream));
   h->tables = true;
   if (h->pass_exec) { cudaGraphExecDestroy(h->pass_exec); h->pass_exec = nullptr; }
@@ -1127,7 +1132,8 @@ extern "C" pimc_status pimc_set_precision(pimc_handle *h, int mixed)
   if (!h || mixed < 0 || mixed > 1) return PIMC_ERR_BAD_ARG;
   CK(cudaSetDevice(h->device));
   h->ctx.s.mixed = mixed;
-  launch_invalidate_caches(h->ctx, h->stream);           // cached sums were made at the other precision
+  // float copies as the moves of this precision write them; caches stale
+  launch_derive_state(h->ctx, h->frames, h->stream);
   h->launches++;
   CK(cudaGetLastError());
   if (h->pass_exec) { CK(cudaGraphExecDestroy(h->pass_exec)); h->pass_exec = nullptr; }
@@ -1505,7 +1511,16 @@ extern "C" pimc_status pimc_batch_set_precision(pimc_batch *b, int mixed)
   CK(cudaStreamSynchronize(h->stream));
   b->mixed = mixed;
   for (auto &rp : b->reps) rp.c.s.mixed = mixed;
-  return batch_upload_reps(b);
+  pimc_status e = batch_upload_reps(b);
+  if (e) return e;
+  if (b->tables) {
+    // float copies as the moves of this precision write them; caches stale
+    launch_batch_refresh(b->d_reps, b->n, 1, h->stream);
+    h->launches++;
+    CK(cudaGetLastError());
+  }
+  if (b->exec) { cudaGraphExecDestroy(b->exec); b->exec = nullptr; }
+  return PIMC_OK;
 }
 
 extern "C" pimc_status pimc_batch_set_shape(pimc_batch *b, int warps, int min_blocks)
@@ -1674,3 +1689,151 @@ extern "C" pimc_status pimc_batch_synchronize(pimc_batch *b)
 extern "C" double pimc_batch_bead_moves_per_pass(const pimc_batch *b) { return b ? b->bm_pass : 0.0; }
 
 extern "C" void *pimc_batch_stream(const pimc_batch *b) { return b ? (void *)b->base->stream : nullptr; }
+
+// ------------------------------------------------------------ checkpoints
+// A complete restart file (the reference's ConfigIO, mc_input.cc:560-600,
+// writes only the first row of MCCoords and MCCosine): the system's sizes for
+// validation, the whole path (MCCoords, MCAngles, PIndex), the pass counter
+// the production uniforms are keyed by, and the move counters.  A run that
+// loads it and continues with the same seed repeats the uninterrupted run.
+static const char g_ckpt_magic[8] = {'P', 'I', 'M', 'C', 'G', 'B', '3', '1'};
+
+struct CkptHead {
+  char magic[8];
+  int version, na, P, Q, nrotors, ntypes, numb[PIMC_MAX_TYPES], mixed;
+  double temperature;
+  unsigned pass;
+  unsigned long long cnt[12];
+};
+
+extern "C" pimc_status pimc_save_checkpoint(pimc_handle *h, const char *path)
+{
+  pimc_status e = ready(h);
+  if (e) return e;
+  if (!path) return PIMC_ERR_BAD_ARG;
+  const DevSys &d = h->ctx.s;
+  size_t nbr = (size_t)d.na * d.P;
+  std::vector<double> coords(3 * nbr), angles(3 * nbr), cosine(3 * nbr);
+  std::vector<int> pidx(d.na);
+  if ((e = pimc_get_state(h, coords.data(), angles.data(), cosine.data(), pidx.data()))) return e;
+  CkptHead hd;
+  memset(&hd, 0, sizeof(hd));
+  memcpy(hd.magic, g_ckpt_magic, 8);
+  hd.version = 1;
+  hd.na = d.na; hd.P = d.P; hd.Q = d.Q; hd.nrotors = d.nrotors; hd.ntypes = d.ntypes;
+  for (int t = 0; t < d.ntypes; t++) hd.numb[t] = d.numb[t];
+  hd.mixed = d.mixed;
+  hd.temperature = d.temperature;
+  CK(cudaMemcpy(&hd.pass, h->pass, sizeof(unsigned), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(hd.cnt, h->cnt, sizeof(hd.cnt), cudaMemcpyDeviceToHost));
+  FILE *f = fopen(path, "wb");
+  if (!f) return PIMC_ERR_BAD_ARG;
+  bool ok = fwrite(&hd, sizeof(hd), 1, f) == 1 && fwrite(coords.data(), sizeof(double), 3 * nbr, f) == 3 * nbr &&
+            fwrite(angles.data(), sizeof(double), 3 * nbr, f) == 3 * nbr &&
+            fwrite(cosine.data(), sizeof(double), 3 * nbr, f) == 3 * nbr &&
+            fwrite(pidx.data(), sizeof(int), d.na, f) == (size_t)d.na;
+  ok = (fclose(f) == 0) && ok;
+  return ok ? PIMC_OK : PIMC_ERR_BAD_ARG;
+}
+
+extern "C" pimc_status pimc_load_checkpoint(pimc_handle *h, const char *path)
+{
+  if (!h || !path) return PIMC_ERR_BAD_ARG;
+  CK(cudaSetDevice(h->device));
+  const DevSys &d = h->ctx.s;
+  FILE *f = fopen(path, "rb");
+  if (!f) return PIMC_ERR_BAD_ARG;
+  CkptHead hd;
+  size_t nbr = (size_t)d.na * d.P;
+  std::vector<double> coords(3 * nbr), angles(3 * nbr), cosine(3 * nbr);
+  std::vector<int> pidx(d.na);
+  bool ok = fread(&hd, sizeof(hd), 1, f) == 1;
+  ok = ok && memcmp(hd.magic, g_ckpt_magic, 8) == 0 && hd.version == 1 && hd.na == d.na && hd.P == d.P &&
+       hd.Q == d.Q && hd.nrotors == d.nrotors && hd.ntypes == d.ntypes && hd.temperature == d.temperature;
+  for (int t = 0; ok && t < d.ntypes; t++) ok = hd.numb[t] == d.numb[t];
+  ok = ok && fread(coords.data(), sizeof(double), 3 * nbr, f) == 3 * nbr &&
+       fread(angles.data(), sizeof(double), 3 * nbr, f) == 3 * nbr &&
+       fread(cosine.data(), sizeof(double), 3 * nbr, f) == 3 * nbr &&
+       fread(pidx.data(), sizeof(int), d.na, f) == (size_t)d.na;
+  fclose(f);
+  if (!ok) return PIMC_ERR_BAD_ARG;
+  pimc_status e = pimc_set_state(h, coords.data(), angles.data(), pidx.data());
+  if (e) return e;
+  if (d.nrotors > 0) {
+    // MCCosine exactly as saved (set_state derives it from the angles on the host)
+    size_t n = (size_t)d.nrotors * d.Q;
+    std::vector<double> cs(3 * n);
+    for (int k = 0; k < 3; k++)
+      for (int r = 0; r < d.nrotors; r++)
+        for (int q = 0; q < d.Q; q++) {
+          size_t src = k * nbr + (size_t)(d.rot_first + r) * d.P + q;
+          cs[k * n + r * d.Q + q] = cosine[src];
+          h->cosine_host[src] = cosine[src];
+        }
+    CK(cudaMemcpy(h->ctx.st.cosv, cs.data(), 3 * n * sizeof(double), cudaMemcpyHostToDevice));
+    launch_derive_state(h->ctx, h->frames, h->stream);
+    h->launches++;
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(h->stream));
+  }
+  CK(cudaMemcpy(h->pass, &hd.pass, sizeof(unsigned), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(h->cnt, hd.cnt, sizeof(hd.cnt), cudaMemcpyHostToDevice));
+  return PIMC_OK;
+}
+
+// IOxyz (mc_input.cc:690-760): the number of beads, a comment line, then per
+// bead "<label> x cx y cy z cz" (coordinate and MCCosine component per
+// dimension), atoms in type order, slices inside an atom
+extern "C" pimc_status pimc_write_xyz(pimc_handle *h, const char *path, const char *const *type_names)
+{
+  pimc_status e = ready(h);
+  if (e) return e;
+  if (!path) return PIMC_ERR_BAD_ARG;
+  const DevSys &d = h->ctx.s;
+  size_t nbr = (size_t)d.na * d.P;
+  std::vector<double> coords(3 * nbr), angles(3 * nbr), cosine(3 * nbr);
+  if ((e = pimc_get_state(h, coords.data(), angles.data(), cosine.data(), nullptr))) return e;
+  FILE *f = fopen(path, "w");
+  if (!f) return PIMC_ERR_BAD_ARG;
+  fprintf(f, "%zu\n# xyz + unit vector\n", nbr);
+  for (int t = 0; t < d.ntypes; t++)
+    for (int a = 0; a < d.numb[t]; a++) {
+      char label[64];
+      snprintf(label, sizeof(label), "%s%d", type_names && type_names[t] ? type_names[t] : (t ? "M" : "A"), a + 1);
+      size_t off = (size_t)(d.first[t] + a) * d.P;
+      for (int it = 0; it < d.P; it++) {
+        fprintf(f, "%5s ", label);
+        for (int k = 0; k < 3; k++)
+          fprintf(f, "%.17g %.17g ", coords[k * nbr + off + it], cosine[k * nbr + off + it]);
+        fprintf(f, "\n");
+      }
+    }
+  return fclose(f) == 0 ? PIMC_OK : PIMC_ERR_BAD_ARG;
+}
+
+// IOxyz read: coordinates and unit vectors; the angles of the rotor rows
+// follow from the unit vector (phi = atan2(cy, cx), cos theta = cz, chi = 0)
+extern "C" pimc_status pimc_read_xyz(pimc_handle *h, const char *path)
+{
+  if (!h || !path) return PIMC_ERR_BAD_ARG;
+  const DevSys &d = h->ctx.s;
+  size_t nbr = (size_t)d.na * d.P;
+  FILE *f = fopen(path, "r");
+  if (!f) return PIMC_ERR_BAD_ARG;
+  std::vector<double> coords(3 * nbr), angles(3 * nbr, 0.0);
+  size_t count = 0;
+  char line[512];
+  bool ok = fscanf(f, "%zu", &count) == 1 && count == nbr && fgets(line, sizeof(line), f) && fgets(line, sizeof(line), f);
+  for (size_t i = 0; ok && i < nbr; i++) {
+    char label[64];
+    double v[6];
+    ok = fscanf(f, "%63s %lf %lf %lf %lf %lf %lf", label, &v[0], &v[1], &v[2], &v[3], &v[4], &v[5]) == 7;
+    if (!ok) break;
+    for (int k = 0; k < 3; k++) coords[k * nbr + i] = v[2 * k];
+    angles[0 * nbr + i] = atan2(v[3], v[1]);
+    angles[1 * nbr + i] = v[5];
+  }
+  fclose(f);
+  if (!ok) return PIMC_ERR_BAD_ARG;
+  return pimc_set_state(h, coords.data(), angles.data(), nullptr);
+}

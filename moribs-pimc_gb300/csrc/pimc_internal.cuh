@@ -166,6 +166,17 @@ __device__ __forceinline__ void make_frame32(float phi, float cost, float chi, f
   *hzf = sqrtf(mf[2] * mf[2] + mf[5] * mf[5] + mf[8] * mf[8]);
 }
 
+// the float unit vector of (phi, cos theta) on the FP32 path
+__device__ __forceinline__ void unit_vector32(float phi, float cost, float v[3])
+{
+  float sp, cp;
+  sincosf(phi, &sp, &cp);
+  float st = sqrtf(fmaxf(1.0f - cost * cost, 0.0f));
+  v[0] = st * cp;
+  v[1] = st * sp;
+  v[2] = cost;
+}
+
 // the double-precision frame (m, hz_norm) only
 __device__ __forceinline__ void make_frame64(double phi, double cost, double chi, Frame &f)
 {

@@ -19,7 +19,14 @@ __global__ void k_derive_state(Ctx c, Frame *frames)
   }
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
     make_frame(c.st.ang[i], c.st.ang[n + i], c.st.ang[2 * n + i], frames[i]);
-    for (int d = 0; d < 3; d++) c.st.cosvf[d * n + i] = (float)c.st.cosv[d * n + i];
+    if (c.s.nrotors > 0 && c.s.molecule[c.s.imtype] == 1 && lazy_linear(c, c.s.mixed != 0)) {
+      // as the FP32 moves write it
+      float v[3];
+      unit_vector32((float)c.st.ang[i], (float)c.st.ang[n + i], v);
+      for (int d = 0; d < 3; d++) c.st.cosvf[d * n + i] = v[d];
+    } else {
+      for (int d = 0; d < 3; d++) c.st.cosvf[d * n + i] = (float)c.st.cosv[d * n + i];
+    }
     c.st.rp_ok[i] = 0;
     c.st.rl_ok[i] = 0;
   }

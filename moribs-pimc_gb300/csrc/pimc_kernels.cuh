@@ -838,10 +838,7 @@ __device__ void rot_prepare(const Ctx &c, const Frame *frames, int g0, int q, co
       sh.ang_new[0] = a[0]; sh.ang_new[1] = a[1]; sh.ang_new[2] = a[2];
       if (linear) {
         if (MIX) {
-          float sp, cp, ct = (float)a[1];
-          sincosf((float)a[0], &sp, &cp);
-          float st = sqrtf(fmaxf(1.0f - ct * ct, 0.0f));
-          sh.nnewf[0] = st * cp; sh.nnewf[1] = st * sp; sh.nnewf[2] = ct;
+          unit_vector32((float)a[0], (float)a[1], sh.nnewf);
         } else {
           unit_vector(a[0], a[1], sh.nnew);
         }

@@ -67,6 +67,10 @@ def load(path=LIBPATH):
     L.pimc_stream.argtypes = [vp]
     L.pimc_status_string.restype = C.c_char_p
     L.pimc_status_string.argtypes = [C.c_int]
+    L.pimc_save_checkpoint.argtypes = [vp, C.c_char_p]
+    L.pimc_load_checkpoint.argtypes = [vp, C.c_char_p]
+    L.pimc_write_xyz.argtypes = [vp, C.c_char_p, C.c_void_p]
+    L.pimc_read_xyz.argtypes = [vp, C.c_char_p]
     # replica batches
     L.pimc_batch_create.argtypes = [C.c_int, C.POINTER(PimcSystem), C.c_int, C.POINTER(vp)]
     L.pimc_batch_destroy.argtypes = [vp]
@@ -213,6 +217,22 @@ class Sampler:
         n = (C.c_longlong * 3)()
         _chk(self.L.pimc_profile_pass(self.h, C.c_uint64(seed), dptr(ms), n), "pimc_profile_pass")
         return ms, np.array(list(n))
+
+    def save_checkpoint(self, path):
+        _chk(self.L.pimc_save_checkpoint(self.h, str(path).encode()), "pimc_save_checkpoint")
+
+    def load_checkpoint(self, path):
+        _chk(self.L.pimc_load_checkpoint(self.h, str(path).encode()), "pimc_load_checkpoint")
+
+    def write_xyz(self, path, type_names=None):
+        arr = None
+        if type_names:
+            arr = (C.c_char_p * len(type_names))(*[n.encode() for n in type_names])
+        _chk(self.L.pimc_write_xyz(self.h, str(path).encode(), C.cast(arr, C.c_void_p) if arr else None),
+             "pimc_write_xyz")
+
+    def read_xyz(self, path):
+        _chk(self.L.pimc_read_xyz(self.h, str(path).encode()), "pimc_read_xyz")
 
     def set_option(self, option, value):
         _chk(self.L.pimc_set_option(self.h, int(option), int(value)), "pimc_set_option")
