@@ -94,6 +94,41 @@ pimc_status pimc_estimators(pimc_handle *h, double *out);
 /* GetRCF row 0 of one sample (mc_estim.cc:1099-1139): rcf[Q] */
 pimc_status pimc_rcf(pimc_handle *h, double *rcf);
 
+/* Pair densities of GetPotEnergy_Densities (mc_estim.cc:500-687 with
+ * bin_1Ddensity/bin_2Ddensity/bin_3Ddensity :1233-1286).  With
+ * PIMC_OPT_DENSITIES = 1 every pimc_estimators call also bins its
+ * configuration into histograms kept on the device, as the reference's
+ * _gr?D_sum accumulate: atom-atom pairs of one type by r, linear rotor-atom
+ * pairs by (r, theta), nonlinear rotor-atom pairs by vcord's (r, theta, chi).
+ * pimc_densities_accumulate bins the current configuration alone.
+ * pimc_densities_read copies the counts out as doubles:
+ * gr1d[PIMC_MAX_TYPES][PIMC_BINSR], gr2d[PIMC_MAX_TYPES][PIMC_BINSR][PIMC_BINST],
+ * gr3d[PIMC_MAX_TYPES][PIMC_BINSR*PIMC_BINST*PIMC_BINSC] indexed by the
+ * density type (the atom type) like _gr1D/_gr2D/_gr3D; any may be NULL. */
+#define PIMC_OPT_DENSITIES 2
+pimc_status pimc_densities_accumulate(pimc_handle *h);
+pimc_status pimc_densities_read(pimc_handle *h, double *gr1d, double *gr2d, double *gr3d);
+pimc_status pimc_densities_reset(pimc_handle *h);
+
+/* GetExchangeLength (mc_estim.cc:1997-2019): ploops[k] += 1 for every
+ * exchange cycle of k+1 bosons in the current permutation; ploops has one
+ * entry per boson. */
+pimc_status pimc_exchange_lengths(pimc_handle *h, double *ploops);
+
+/* GetAreaEstimators (mc_estim.cc:2087-2250): the superfluid area estimators
+ * of the boson paths about the linear dopant.  out[6] are the increments
+ * the reference adds to _areas[PERP,PARL], _area2[PERP,PARL] and
+ * _inert[PERP,PARL] (mc_estim.cc:2242-2249). */
+pimc_status pimc_area_estimators(pimc_handle *h, double *out);
+
+/* GetAreaEstim3D(iframe) (mc_estim.cc:2252-2594): iframe 0 about the
+ * instantaneous centre of mass of all atoms on the space-fixed axes, 1 about
+ * the dopant on its body axes.  mass[type] in amu (MCAtom[].mass,
+ * mc_setup.cc:244-319).  out[18] = area_proj[3], then the increments of
+ * _areas3D (area_proj[i]*area_proj[j], j <= i) and of _inert3D (inert3D/P,
+ * row-major 3x3). */
+pimc_status pimc_area_estim3d(pimc_handle *h, int iframe, const double *mass, double *out);
+
 /* ---- production sampler -------------------------------------------------- */
 
 /* npasses passes of the reference schedule's moves (mc_main.cc:348-381,

@@ -45,6 +45,15 @@ enum { PIMC_ROTDEN_TABLE = 0, PIMC_ROTDEN_RS = 1 };
 
 #define PIMC_MAX_TYPES 2
 
+/* Density histogram grids of densities_init (mc_estim.cc:25-30, 223-255):
+ * radial bins of (MAX-MIN)/BINSR Angstrom from MIN_RADIUS, theta bins of
+ * pi/(BINST-1), chi bins of 2 pi/(BINSC-1). */
+#define PIMC_BINSR 300
+#define PIMC_BINST 50
+#define PIMC_BINSC 100
+#define PIMC_DENS_MIN_RADIUS 0.0
+#define PIMC_DENS_MAX_RADIUS 15.0
+
 /* One particle type: the fields of TParticle (mc_setup.h:66-91) that the
  * sampling path reads.  lambda is hbar^2/2m in K*A^2 (mc_setup.cc:207-215). */
 typedef struct {

@@ -50,6 +50,9 @@ struct pimc_handle {
   unsigned long long *prog = nullptr;  // per-CTA progress words of the persistent rotation launches
   unsigned *abort_word = nullptr;
   int nprog = 0;
+  // pair-density histograms (allocated on first use)
+  DensHist dens{nullptr, nullptr, nullptr};
+  int dens_on = 0;
 };
 
 extern "C" const char *pimc_status_string(pimc_status s)
@@ -324,7 +327,7 @@ extern "C" pimc_status pimc_destroy(pimc_handle *h)
   DevState &st = h->ctx.st;
   void *bufs[] = {st.x, st.y, st.z, st.b4, st.cosvf, st.rp_cache, st.rl_cache, st.rp_ok, st.rl_ok,
                   st.ang, st.cosv, st.pindex, st.mctype, st.err, h->frames, h->cnt, h->pass, h->cursors, h->ms,
-                  h->qbuf, h->prog, h->abort_word};
+                  h->qbuf, h->prog, h->abort_word, h->dens.g1, h->dens.g2, h->dens.g3};
   for (void *b : bufs)
     if (b) cudaFree(b);
   for (void *b : h->owned) cudaFree(b);
@@ -824,6 +827,7 @@ extern "C" pimc_status pimc_estimators(pimc_handle *h, double *out)
   double *kin = (double *)buf, *pot = kin + d.na, *rot = pot + npairs, *rcf = rot + 4 * nk;
   launch_est(h->ctx, h->frames, kin, pot, rot, rcf, h->stream);
   h->launches += nk ? 4 : 2;
+  if (h->dens_on) h->launches += launch_est_dens(h->ctx, h->frames, h->dens, h->stream);
   CK(cudaGetLastError());
   std::vector<double> hv(nd);
   CK(cudaMemcpyAsync(hv.data(), buf, nd * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
@@ -867,6 +871,162 @@ extern "C" pimc_status pimc_estimators(pimc_handle *h, double *out)
   out[2] = erot;
   out[3] = esq;
   out[4] = ets;
+  return PIMC_OK;
+}
+
+// ------------------------------------------------ densities, cycles, areas
+
+static const size_t kDens1 = (size_t)PIMC_MAX_TYPES * PIMC_BINSR;
+static const size_t kDens2 = kDens1 * PIMC_BINST;
+static const size_t kDens3 = kDens2 * PIMC_BINSC;
+
+static pimc_status dens_alloc(pimc_handle *h)
+{
+  if (h->dens.g1) return PIMC_OK;
+  CK(cudaMalloc(&h->dens.g1, kDens1 * sizeof(unsigned long long)));
+  CK(cudaMalloc(&h->dens.g2, kDens2 * sizeof(unsigned long long)));
+  CK(cudaMemsetAsync(h->dens.g1, 0, kDens1 * sizeof(unsigned long long), h->stream));
+  CK(cudaMemsetAsync(h->dens.g2, 0, kDens2 * sizeof(unsigned long long), h->stream));
+  if (h->ctx.s.nrotors > 0 && h->ctx.s.molecule[h->ctx.s.imtype] == PIMC_NONLINEAR) {
+    CK(cudaMalloc(&h->dens.g3, kDens3 * sizeof(unsigned long long)));
+    CK(cudaMemsetAsync(h->dens.g3, 0, kDens3 * sizeof(unsigned long long), h->stream));
+  }
+  return PIMC_OK;
+}
+
+extern "C" pimc_status pimc_densities_accumulate(pimc_handle *h)
+{
+  pimc_status e = ready(h);
+  if (e) return e;
+  if ((e = dens_alloc(h))) return e;
+  h->launches += launch_est_dens(h->ctx, h->frames, h->dens, h->stream);
+  CK(cudaGetLastError());
+  return PIMC_OK;
+}
+
+extern "C" pimc_status pimc_densities_read(pimc_handle *h, double *gr1d, double *gr2d, double *gr3d)
+{
+  if (!h) return PIMC_ERR_BAD_ARG;
+  CK(cudaSetDevice(h->device));
+  double *dst[3] = {gr1d, gr2d, gr3d};
+  unsigned long long *src[3] = {h->dens.g1, h->dens.g2, h->dens.g3};
+  size_t n[3] = {kDens1, kDens2, kDens3};
+  std::vector<unsigned long long> tmp;
+  for (int k = 0; k < 3; k++) {
+    if (!dst[k]) continue;
+    if (!src[k]) {
+      std::fill(dst[k], dst[k] + n[k], 0.0);
+      continue;
+    }
+    tmp.resize(n[k]);
+    CK(cudaMemcpyAsync(tmp.data(), src[k], n[k] * sizeof(unsigned long long), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    for (size_t i = 0; i < n[k]; i++) dst[k][i] = (double)tmp[i];
+  }
+  return check_err(h);
+}
+
+extern "C" pimc_status pimc_densities_reset(pimc_handle *h)
+{
+  if (!h) return PIMC_ERR_BAD_ARG;
+  CK(cudaSetDevice(h->device));
+  unsigned long long *src[3] = {h->dens.g1, h->dens.g2, h->dens.g3};
+  size_t n[3] = {kDens1, kDens2, kDens3};
+  for (int k = 0; k < 3; k++)
+    if (src[k]) CK(cudaMemsetAsync(src[k], 0, n[k] * sizeof(unsigned long long), h->stream));
+  return PIMC_OK;
+}
+
+// BSTYPE: the last Bose type (mc_setup.cc:409-415), or -1
+static int boson_type(const pimc_handle *h)
+{
+  int bt = -1;
+  for (int t = 0; t < h->sys.ntypes; t++)
+    if (h->sys.type[t].stat == PIMC_BOSE) bt = t;
+  return bt;
+}
+
+extern "C" pimc_status pimc_exchange_lengths(pimc_handle *h, double *ploops)
+{
+  pimc_status e = ready(h);
+  if (e) return e;
+  if (!ploops) return PIMC_ERR_BAD_ARG;
+  int bt = boson_type(h);
+  if (bt < 0) return PIMC_ERR_STATE;
+  int n = h->sys.type[bt].numb;
+  std::vector<int> pidx(h->ctx.s.na);
+  CK(cudaMemcpyAsync(pidx.data(), h->ctx.st.pindex, pidx.size() * sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  std::vector<char> seen(n, 0);
+  for (int atom = 0; atom < n; atom++) {
+    if (seen[atom]) continue;
+    int len = 0, p = pidx[atom];
+    while (p != atom) {
+      if (p < 0 || p >= n || len > n) return PIMC_ERR_STATE;   // not a permutation
+      seen[p] = 1;
+      p = pidx[p];
+      len++;
+    }
+    ploops[len] += 1.0;
+  }
+  return PIMC_OK;
+}
+
+static pimc_status area_sums(pimc_handle *h, int mode, int bt, const double *mass, double *sums)
+{
+  int nb = est_area_ctas(h->ctx, bt);
+  void *buf;
+  pimc_status e;
+  if ((e = scratch(h, (size_t)nb * 12 * sizeof(double), &buf))) return e;
+  launch_est_area(h->ctx, mode, bt, mass, (double *)buf, h->stream);
+  h->launches += 1;
+  CK(cudaGetLastError());
+  std::vector<double> part((size_t)nb * 12);
+  CK(cudaMemcpyAsync(part.data(), buf, part.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  if ((e = check_err(h))) return e;
+  for (int k = 0; k < 12; k++) {
+    double v = 0.0;
+    for (int b = 0; b < nb; b++) v += part[(size_t)b * 12 + k];
+    sums[k] = v;
+  }
+  return PIMC_OK;
+}
+
+extern "C" pimc_status pimc_area_estimators(pimc_handle *h, double *out)
+{
+  pimc_status e = ready(h);
+  if (e) return e;
+  if (!out) return PIMC_ERR_BAD_ARG;
+  int bt = boson_type(h);
+  const DevSys &d = h->ctx.s;
+  if (bt < 0 || d.nrotors <= 0 || d.molecule[d.imtype] != PIMC_LINEAR) return PIMC_ERR_STATE;
+  double v[12];
+  if ((e = area_sums(h, 0, bt, nullptr, v))) return e;
+  out[0] = v[0];
+  out[1] = v[1];
+  out[2] = v[0] * v[0];
+  out[3] = v[1] * v[1];
+  out[4] = v[2] / (double)d.P;
+  out[5] = v[3] / (double)d.P;
+  return PIMC_OK;
+}
+
+extern "C" pimc_status pimc_area_estim3d(pimc_handle *h, int iframe, const double *mass, double *out)
+{
+  pimc_status e = ready(h);
+  if (e) return e;
+  if (!out || !mass || (iframe != 0 && iframe != 1)) return PIMC_ERR_BAD_ARG;
+  int bt = boson_type(h);
+  const DevSys &d = h->ctx.s;
+  if (bt < 0 || (iframe == 1 && d.nrotors <= 0)) return PIMC_ERR_STATE;
+  double m[2] = {mass[0], d.ntypes > 1 ? mass[1] : mass[0]};
+  double v[12];
+  if ((e = area_sums(h, iframe == 0 ? 1 : 2, bt, m, v))) return e;
+  for (int i = 0; i < 3; i++) out[i] = v[i];
+  int ind = 3;
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j <= i; j++) out[ind++] = v[i] * v[j];
+  for (int k = 0; k < 9; k++) out[9 + k] = v[3 + k] / (double)d.P;
   return PIMC_OK;
 }
 
@@ -1096,6 +1256,16 @@ extern "C" pimc_status pimc_set_option(pimc_handle *h, int option, long long val
       h->pass_exec = nullptr;
     }
     h->fused = (int)value;
+    return PIMC_OK;
+  }
+  if (option == PIMC_OPT_DENSITIES) {
+    if (value != 0 && value != 1) return PIMC_ERR_BAD_ARG;
+    CK(cudaSetDevice(h->device));
+    if (value) {
+      pimc_status e = dens_alloc(h);
+      if (e) return e;
+    }
+    h->dens_on = (int)value;
     return PIMC_OK;
   }
   return PIMC_ERR_BAD_ARG;

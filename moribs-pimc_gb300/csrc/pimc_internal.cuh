@@ -117,6 +117,19 @@ struct Ctx {
   DevState st;
 };
 
+// pair-density histograms (counts), [dtype][bins] as _gr1D/_gr2D/_gr3D
+// (mc_estim.cc:257-287); g3 is null without a nonlinear rotor
+#ifndef PIMC_BINSR                 /* the same values as pimc_types.h */
+#define PIMC_BINSR 300
+#define PIMC_BINST 50
+#define PIMC_BINSC 100
+#define PIMC_DENS_MIN_RADIUS 0.0
+#define PIMC_DENS_MAX_RADIUS 15.0
+#endif
+struct DensHist {
+  unsigned long long *g1, *g2, *g3;
+};
+
 // ------------------------------------------------------------------ frames
 // Body frame of a nonlinear rotor: the columns of matpre(phi, acos(cost), chi)
 // (rotden.f:136-163, vcord.f:31-36) plus |hatz| as dnorm computes it.

@@ -582,6 +582,211 @@ __global__ void k_est_rcf(Ctx c, double *rcf)
   rcf[itc] = s;
 }
 
+// ------------------------------------------------------------ densities
+// bin_1Ddensity / bin_2Ddensity / bin_3Ddensity (mc_estim.cc:1233-1286) on
+// the grids of densities_init (mc_estim.cc:223-255): the same divisions and
+// floors as the reference, counts kept as 64-bit integers indexed
+// [dtype][bins] like _gr1D/_gr2D/_gr3D
+__device__ __forceinline__ void dens_bin(const DensHist &hs, int kind, int dtype, double r, double a, double b)
+{
+  const double drad = (PIMC_DENS_MAX_RADIUS - PIMC_DENS_MIN_RADIUS) / (double)PIMC_BINSR;
+  const double dth = PIMC_PI / (double)(PIMC_BINST - 1), dch = 2.0 * PIMC_PI / (double)(PIMC_BINSC - 1);
+  int br = (int)floor((r - PIMC_DENS_MIN_RADIUS) / drad);
+  if (!(br < PIMC_BINSR && br >= 0)) return;
+  if (kind == 1) {
+    atomicAdd(hs.g1 + (size_t)dtype * PIMC_BINSR + br, 1ull);
+  } else if (kind == 2) {
+    int bt = (int)floor(acos(a) / dth);
+    if (bt < PIMC_BINST && bt >= 0) atomicAdd(hs.g2 + ((size_t)dtype * PIMC_BINSR + br) * PIMC_BINST + bt, 1ull);
+  } else if (hs.g3) {
+    int bt = (int)floor(a / dth);
+    if (bt < PIMC_BINST && bt >= 0) {
+      int bc = (int)floor(b / dch);
+      if (bc < PIMC_BINSC && bc >= 0)
+        atomicAdd(hs.g3 + (size_t)dtype * PIMC_BINSR * PIMC_BINST * PIMC_BINSC +
+                      ((size_t)br * PIMC_BINST + bt) * PIMC_BINSC + bc,
+                  1ull);
+    }
+  }
+}
+
+// the geometry GetPotEnergy_Densities (mc_estim.cc:520-662) bins for the
+// pair (a0 < a1) at slice it: r for atoms of one type, (r, n.dr/r) for a
+// linear rotor and an atom, vcord's (r, theta, chi) (or vspher's r) for a
+// nonlinear rotor and an atom; rotor pairs are not binned
+__device__ void est_pair_bin(const Ctx &c, const Frame *frames, const DensHist &hs, int a0, int a1, int it)
+{
+  const DevSys &s = c.s;
+  int ty0 = atom_type(s, a0), ty1 = atom_type(s, a1);
+  int m0 = s.molecule[ty0], m1 = s.molecule[ty1];
+  size_t i0 = sidx(s, it, a0), i1 = sidx(s, it, a1);
+  double px = c.st.x[i0], py = c.st.y[i0], pz = c.st.z[i0];
+  double qx = c.st.x[i1], qy = c.st.y[i1], qz = c.st.z[i1];
+  double dx = px - qx, dy = py - qy, dz = pz - qz;
+  if (s.minimage) {
+    dx -= s.box[0] * rint(dx / s.box[0]);
+    dy -= s.box[1] * rint(dy / s.box[1]);
+    dz -= s.box[2] * rint(dz / s.box[2]);
+  }
+  double dr2 = 0.0;
+  dr2 += dx * dx;
+  dr2 += dy * dy;
+  dr2 += dz * dz;
+  double r = sqrt(dr2);
+  if (m0 == 1 || m1 == 1) {
+    int rot = (m0 == 1) ? a0 : a1;
+    size_t n = (size_t)s.nrotors * s.Q;
+    int ri = rot_index(s, rot, it / s.R);
+    double cost = 0.0;
+    cost += c.st.cosv[ri] * dx;
+    cost += c.st.cosv[n + ri] * dy;
+    cost += c.st.cosv[2 * n + ri] * dz;
+    cost /= r;
+    if (m0 == 1) cost *= -1.0;
+    dens_bin(hs, 2, m0 == 1 ? ty1 : ty0, r, cost, 0.0);
+  } else if ((m0 == 2 || m1 == 2) && m0 != m1) {
+    double rr = r, th = 0.0, ch = 0.0;
+    if (!s.ispher) {
+      if (m0 == 2) vcord(c.t, frames[rot_index(s, a0, it / s.R)], px, py, pz, qx, qy, qz, &rr, &th, &ch);
+      else vcord(c.t, frames[rot_index(s, a1, it / s.R)], qx, qy, qz, px, py, pz, &rr, &th, &ch);
+    }
+    dens_bin(hs, 3, m0 == 2 ? ty1 : ty0, rr, th, ch);
+  } else if (!(m0 == 2 && m1 == 2) && ty0 == ty1 && m0 == 0) {
+    dens_bin(hs, 1, ty1, r, 0.0, 0.0);
+  }
+}
+
+// all pairs x slices of one configuration, one thread per (pair, slice)
+__global__ void k_est_dens(Ctx c, Frame *frames, DensHist hs)
+{
+  int na = c.s.na, P = c.s.P;
+  long npairs = (long)na * (na - 1) / 2;
+  for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < npairs * P; k += (long)gridDim.x * blockDim.x) {
+    int pidx = (int)(k / P), it = (int)(k % P);
+    int a0 = 0, rem = pidx;
+    while (rem >= na - 1 - a0) { rem -= na - 1 - a0; a0++; }
+    est_pair_bin(c, frames, hs, a0, a0 + 1 + rem, it);
+  }
+}
+
+// ------------------------------------------------------ area estimators
+// GetAreaEstimators (mc_estim.cc:2087-2250, mode 0) and GetAreaEstim3D
+// (mc_estim.cc:2252-2594; mode 1 space-fixed frame about the mass-weighted
+// centre of all atoms, mode 2 dopant-fixed frame about the first rotor).
+// Items (it0, boson) are summed per CTA in a fixed tree; out[blockIdx*12 +
+// k] are the CTA's partial sums: mode 0 {area_perp, area_parl, inert_perp,
+// inert_parl}, modes 1/2 {area_proj[3], inert3D[9]} (unscaled).
+template <int MODE>
+__global__ void __launch_bounds__(PIMC_BLOCK) k_est_area(Ctx c, int btype, double m0, double m1, double *out)
+{
+  __shared__ double red[PIMC_BLOCK];
+  const DevSys &s = c.s;
+  const int P = s.P, nbos = s.numb[btype], g = s.first[btype];
+  const long nitem = (long)nbos * P;
+  const double bmass = btype == 0 ? m0 : m1;
+  double acc[12];
+#pragma unroll
+  for (int k = 0; k < 12; k++) acc[k] = 0.0;
+  auto com = [&](int it, double v[3]) {
+    if (MODE == 1) {
+      double tmass = 0.0, sx = 0.0, sy = 0.0, sz = 0.0;
+      for (int a = 0; a < s.na; a++) {
+        double m = atom_type(s, a) == 0 ? m0 : m1;
+        size_t i = sidx(s, it, a);
+        sx += (m * c.st.x[i]);
+        sy += (m * c.st.y[i]);
+        sz += (m * c.st.z[i]);
+        tmass += m;
+      }
+      v[0] = sx / tmass; v[1] = sy / tmass; v[2] = sz / tmass;
+    } else {
+      size_t i = sidx(s, it, s.rot_first);
+      v[0] = c.st.x[i]; v[1] = c.st.y[i]; v[2] = c.st.z[i];
+    }
+  };
+  for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < nitem; k += (long)gridDim.x * blockDim.x) {
+    int it0 = (int)(k / nbos), atom = (int)(k % nbos);
+    int it1 = (it0 + 1) % P;
+    int a1 = (it1 != it0 + 1) ? g + c.st.pindex[atom] : g + atom;
+    double c0[3], c1[3];
+    com(it0, c0);
+    com(it1, c1);
+    size_t i0 = sidx(s, it0, g + atom), i1 = sidx(s, it1, a1);
+    double dr0[3] = {c.st.x[i0] - c0[0], c.st.y[i0] - c0[1], c.st.z[i0] - c0[2]};
+    double dr1[3] = {c.st.x[i1] - c1[0], c.st.y[i1] - c1[1], c.st.z[i1] - c1[2]};
+    double area[3];
+    area[0] = 0.5 * (dr0[1] * dr1[2] - dr0[2] * dr1[1]);
+    area[1] = 0.5 * (dr0[2] * dr1[0] - dr0[0] * dr1[2]);
+    area[2] = 0.5 * (dr0[0] * dr1[1] - dr0[1] * dr1[0]);
+    if (MODE == 0) {
+      size_t n = (size_t)s.nrotors * s.Q;
+      int ri = rot_index(s, s.rot_first, it0 / s.R);
+      double nl[3] = {c.st.cosv[ri], c.st.cosv[n + ri], c.st.cosv[2 * n + ri]};
+      double tg = 0.0, st = 1.0;
+      if (fabs(nl[0]) > 10e-4) {
+        tg = nl[1] / nl[0];
+        st = sqrt(1.0 + tg * tg);
+      }
+      double np[3] = {tg / st, -1.0 / st, 0.0};
+      acc[0] += np[0] * area[0] + np[1] * area[1] + np[2] * area[2];
+      acc[1] += nl[0] * area[0] + nl[1] * area[1] + nl[2] * area[2];
+      const double *nv[2] = {np, nl};
+#pragma unroll
+      for (int w = 0; w < 2; w++) {
+        const double *u = nv[w];
+        double r0[3] = {u[1] * dr0[2] - u[2] * dr0[1], u[2] * dr0[0] - u[0] * dr0[2], u[0] * dr0[1] - u[1] * dr0[0]};
+        double r1[3] = {u[1] * dr1[2] - u[2] * dr1[1], u[2] * dr1[0] - u[0] * dr1[2], u[0] * dr1[1] - u[1] * dr1[0]};
+        acc[2 + w] += r0[0] * r1[0] + r0[1] * r1[1] + r0[2] * r1[2];
+      }
+    } else {
+      double hat[3][3];
+      if (MODE == 1) {
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+          for (int j = 0; j < 3; j++) hat[i][j] = (i == j) ? 1.0 : 0.0;
+      } else {
+        int ri = rot_index(s, s.rot_first, it0 / s.R);
+        size_t n = (size_t)s.nrotors * s.Q;
+        Frame f;
+        make_frame64(c.st.ang[ri], c.st.ang[n + ri], c.st.ang[2 * n + ri], f);
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+          for (int d = 0; d < 3; d++) hat[i][d] = f.m[d * 3 + i];
+      }
+      double pr0[3], pr1[3];
+#pragma unroll
+      for (int i = 0; i < 3; i++) {
+        acc[i] += area[0] * hat[i][0] + area[1] * hat[i][1] + area[2] * hat[i][2];
+        pr0[i] = hat[i][0] * dr0[0] + hat[i][1] * dr0[1] + hat[i][2] * dr0[2];
+        pr1[i] = hat[i][0] * dr1[0] + hat[i][1] * dr1[1] + hat[i][2] * dr1[2];
+      }
+#pragma unroll
+      for (int i = 0; i < 3; i++) {
+        const double *h = hat[i];
+        double r0[3] = {dr0[1] * h[2] - dr0[2] * h[1], dr0[2] * h[0] - dr0[0] * h[2], dr0[0] * h[1] - dr0[1] * h[0]};
+        double r1[3] = {dr1[1] * h[2] - dr1[2] * h[1], dr1[2] * h[0] - dr1[0] * h[2], dr1[0] * h[1] - dr1[1] * h[0]};
+        acc[3 + 3 * i + i] += (r0[0] * r1[0] + r0[1] * r1[1] + r0[2] * r1[2]) * bmass;
+#pragma unroll
+        for (int j = 0; j < 3; j++)
+          if (j != i) acc[3 + 3 * i + j] += -bmass * pr0[i] * pr1[j];
+      }
+    }
+  }
+  const int nv = MODE == 0 ? 4 : 12;
+  for (int k = 0; k < nv; k++) {
+    red[threadIdx.x] = acc[k];
+    __syncthreads();
+    for (int w = PIMC_BLOCK / 2; w > 0; w >>= 1) {
+      if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) out[(size_t)blockIdx.x * 12 + k] = red[0];
+    __syncthreads();
+  }
+}
+
 // ------------------------------------------------------------ bookkeeping
 __global__ void k_pass_begin(unsigned *pass) { *pass += 1; }
 
@@ -884,5 +1089,31 @@ void launch_est(const Ctx &c, Frame *f, double *kin, double *pot, double *rot, d
 }
 
 void launch_pass_begin(unsigned *pass, cudaStream_t s) { k_pass_begin<<<1, 1, 0, s>>>(pass); }
+
+int launch_est_dens(const Ctx &c, Frame *f, DensHist hs, cudaStream_t s)
+{
+  long work = (long)c.s.na * (c.s.na - 1) / 2 * c.s.P;
+  if (work <= 0) return 0;
+  long nb = (work + 255) / 256;
+  k_est_dens<<<(int)(nb < 4096 ? nb : 4096), 256, 0, s>>>(c, f, hs);
+  return 1;
+}
+
+int est_area_ctas(const Ctx &c, int btype)
+{
+  long items = (long)c.s.numb[btype] * c.s.P;
+  long nb = (items + PIMC_BLOCK - 1) / PIMC_BLOCK;
+  return (int)(nb < 304 ? (nb > 0 ? nb : 1) : 304);
+}
+
+int launch_est_area(const Ctx &c, int mode, int btype, const double *mass, double *out, cudaStream_t s)
+{
+  int nb = est_area_ctas(c, btype);
+  double m0 = mass ? mass[0] : 1.0, m1 = mass ? mass[1] : 1.0;
+  if (mode == 0) k_est_area<0><<<nb, PIMC_BLOCK, 0, s>>>(c, btype, m0, m1, out);
+  else if (mode == 1) k_est_area<1><<<nb, PIMC_BLOCK, 0, s>>>(c, btype, m0, m1, out);
+  else k_est_area<2><<<nb, PIMC_BLOCK, 0, s>>>(c, btype, m0, m1, out);
+  return nb;
+}
 
 size_t mol_scratch_bytes() { return sizeof(MolScratch); }

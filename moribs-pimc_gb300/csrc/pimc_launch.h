@@ -35,6 +35,9 @@ void launch_q_rot(const Ctx &c, Frame *f, int n, const int *rot, const int *it, 
                   double *out, cudaStream_t s);
 void launch_est(const Ctx &c, Frame *f, double *kin, double *pot, double *rot, double *rcf, cudaStream_t s);
 void launch_pass_begin(unsigned *pass, cudaStream_t s);
+int launch_est_dens(const Ctx &c, Frame *f, DensHist hs, cudaStream_t s);
+int est_area_ctas(const Ctx &c, int btype);
+int launch_est_area(const Ctx &c, int mode, int btype, const double *mass, double *out, cudaStream_t s);
 size_t mol_scratch_bytes();
 
 // ------------------------------------------------------------ replica batches

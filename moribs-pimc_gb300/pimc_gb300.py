@@ -11,7 +11,7 @@ import os
 
 import numpy as np
 
-from pimc_types import PimcSystem, PimcTables, STATUS, dptr, iptr, make_system, make_tables
+from pimc_types import BINSC, BINSR, BINST, PIMC_MAX_TYPES, PimcSystem, PimcTables, STATUS, dptr, iptr, make_system, make_tables
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIBPATH = os.path.join(HERE, "libpimc_gb300.so")
@@ -23,6 +23,7 @@ _ip = C.POINTER(C.c_int)
 _lp = C.POINTER(C.c_long)
 _L = None
 OPT_FUSED = 1          # pimc_gb300.h PIMC_OPT_FUSED
+OPT_DENSITIES = 2      # pimc_gb300.h PIMC_OPT_DENSITIES
 
 
 class PimcError(RuntimeError):
@@ -52,6 +53,12 @@ def load(path=LIBPATH):
     L.pimc_pot_rot_energy.argtypes = [vp, C.c_int, _ip, _ip, _dp, _dp]
     L.pimc_estimators.argtypes = [vp, _dp]
     L.pimc_rcf.argtypes = [vp, _dp]
+    L.pimc_densities_accumulate.argtypes = [vp]
+    L.pimc_densities_read.argtypes = [vp, _dp, _dp, _dp]
+    L.pimc_densities_reset.argtypes = [vp]
+    L.pimc_exchange_lengths.argtypes = [vp, _dp]
+    L.pimc_area_estimators.argtypes = [vp, _dp]
+    L.pimc_area_estim3d.argtypes = [vp, C.c_int, _dp, _dp]
     L.pimc_run_passes.argtypes = [vp, C.c_int, C.c_uint64]
     L.pimc_counters.argtypes = [vp, _dp, _dp]
     L.pimc_profile_pass.argtypes = [vp, C.c_uint64, _dp, C.POINTER(C.c_longlong)]
@@ -206,6 +213,37 @@ class Sampler:
     def rcf(self):
         out = np.zeros(self.w.nrotslices)
         _chk(self.L.pimc_rcf(self.h, dptr(out)), "pimc_rcf")
+        return out
+
+    def densities_accumulate(self):
+        _chk(self.L.pimc_densities_accumulate(self.h), "pimc_densities_accumulate")
+
+    def densities_read(self):
+        """(gr1d[2,BINSR], gr2d[2,BINSR,BINST], gr3d[2,BINSR*BINST*BINSC]) accumulated counts."""
+        g1 = np.zeros((PIMC_MAX_TYPES, BINSR))
+        g2 = np.zeros((PIMC_MAX_TYPES, BINSR, BINST))
+        g3 = np.zeros((PIMC_MAX_TYPES, BINSR * BINST * BINSC))
+        _chk(self.L.pimc_densities_read(self.h, dptr(g1), dptr(g2), dptr(g3)), "pimc_densities_read")
+        return g1, g2, g3
+
+    def densities_reset(self):
+        _chk(self.L.pimc_densities_reset(self.h), "pimc_densities_reset")
+
+    def exchange_lengths(self, ploops=None):
+        nb = [t["numb"] for t in self.w.types if t["stat"] == 1][-1]
+        out = np.zeros(nb) if ploops is None else ploops
+        _chk(self.L.pimc_exchange_lengths(self.h, dptr(out)), "pimc_exchange_lengths")
+        return out
+
+    def area_estimators(self):
+        out = np.zeros(6)
+        _chk(self.L.pimc_area_estimators(self.h, dptr(out)), "pimc_area_estimators")
+        return out
+
+    def area_estim3d(self, iframe, masses):
+        m = np.ascontiguousarray(masses, dtype=np.float64)
+        out = np.zeros(18)
+        _chk(self.L.pimc_area_estim3d(self.h, int(iframe), dptr(m), dptr(out)), "pimc_area_estim3d")
         return out
 
     # production

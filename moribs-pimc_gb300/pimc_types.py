@@ -6,6 +6,8 @@ import ctypes as C
 import numpy as np
 
 PIMC_MAX_TYPES = 2
+# density histogram grids (mc_estim.cc:25-30); mirror of pimc_types.h
+BINSR, BINST, BINSC = 300, 50, 100
 STATUS = {
     0: "PIMC_OK", 1: "PIMC_ERR_BAD_ARG", 2: "PIMC_ERR_BAD_TABLE", 3: "PIMC_ERR_GRID_RANGE",
     4: "PIMC_ERR_NEG_DENSITY", 5: "PIMC_ERR_TIMEOUT", 6: "PIMC_ERR_CUDA", 7: "PIMC_ERR_NO_DEVICE",

@@ -18,7 +18,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(HERE)
 sys.path.insert(0, os.path.join(REPO, "moribs-pimc_gb300"))
-from pimc_types import PimcSystem, PimcTables, dptr, iptr, make_system, make_tables  # noqa: E402
+from pimc_types import BINSC, BINSR, BINST, PimcSystem, PimcTables, dptr, iptr, make_system, make_tables  # noqa: E402
 
 LIB = os.path.join(HERE, "liboracle.so")
 REFLIB = os.path.join(HERE, "_ref", "libref.so")
@@ -111,6 +111,11 @@ def _lib():
         getattr(lib, name).restype = C.c_double
         getattr(lib, name).argtypes = [C.c_void_p, _dp, _dp]
     lib.orc_rcf.argtypes = [C.c_void_p, _dp]
+    lib.orc_pot_energy_densities.restype = C.c_double
+    lib.orc_pot_energy_densities.argtypes = [C.c_void_p, _dp, _dp, _dp]
+    lib.orc_exchange_lengths.argtypes = [C.c_void_p, _dp]
+    lib.orc_area_estimators.argtypes = [C.c_void_p, _dp]
+    lib.orc_area_estim3d.argtypes = [C.c_void_p, C.c_int, _dp, _dp]
     lib.orc_run_steps.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_uint64, C.c_int, _dp]
     return lib
 
@@ -246,6 +251,32 @@ class Oracle:
         self.L.orc_rcf(self.h, dptr(r))
         return r
 
+    def densities(self):
+        """(E_pot, gr1d[2,BINSR], gr2d[2,BINSR,BINST], gr3d[2,BINSR*BINST*BINSC]) of this path."""
+        g1 = np.zeros((2, BINSR)); g2 = np.zeros((2, BINSR, BINST)); g3 = np.zeros((2, BINSR * BINST * BINSC))
+        v = self.L.orc_pot_energy_densities(self.h, dptr(g1), dptr(g2), dptr(g3))
+        return v, g1, g2, g3
+
+    def exchange_lengths(self, nboson):
+        pl = np.zeros(nboson)
+        self.L.orc_exchange_lengths(self.h, dptr(pl))
+        return pl
+
+    def area_estimators(self):
+        out = np.zeros(6)
+        st = self.L.orc_area_estimators(self.h, dptr(out))
+        if st != 0:
+            raise RuntimeError("orc_area_estimators status %d" % st)
+        return out
+
+    def area_estim3d(self, iframe, masses):
+        out = np.zeros(18)
+        m = np.ascontiguousarray(masses, dtype=np.float64)
+        st = self.L.orc_area_estim3d(self.h, int(iframe), dptr(m), dptr(out))
+        if st != 0:
+            raise RuntimeError("orc_area_estim3d status %d" % st)
+        return out
+
     def run_steps(self, t_begin, t_count, seed, nthreads=1):
         bm = C.c_double()
         st = self.L.orc_run_steps(self.h, int(t_begin), int(t_count), C.c_uint64(seed), int(nthreads), C.byref(bm))
@@ -306,6 +337,14 @@ class Reference:
         for n in ("ref_rot_energy", "ref_rot_e3d"):
             getattr(L, n).restype = C.c_double
             getattr(L, n).argtypes = [_dp, _dp]
+        L.ref_mass.restype = C.c_double
+        L.ref_mass.argtypes = [C.c_int]
+        L.ref_set_pindex.argtypes = [_ip]
+        L.ref_densities.restype = C.c_double
+        L.ref_densities.argtypes = [_dp, _dp, _dp]
+        L.ref_exchange_lengths.argtypes = [_dp]
+        L.ref_area_estimators.argtypes = [_dp]
+        L.ref_area_estim3d.argtypes = [C.c_int, _dp]
         L.ref_tau.restype = C.c_double
         L.ref_lambda.restype = C.c_double
         L.ref_lambda.argtypes = [C.c_int]
@@ -368,3 +407,27 @@ class Reference:
         tot = np.zeros(6); acc = np.zeros(6)
         self.L.ref_counters(dptr(tot), dptr(acc))
         return tot, acc
+
+    def set_pindex(self, pindex):
+        p = np.ascontiguousarray(pindex, dtype=np.int32)
+        self.L.ref_set_pindex(iptr(p))
+
+    def densities(self):
+        g1 = np.zeros((2, BINSR)); g2 = np.zeros((2, BINSR, BINST)); g3 = np.zeros((2, BINSR * BINST * BINSC))
+        v = self.L.ref_densities(dptr(g1), dptr(g2), dptr(g3))
+        return v, g1, g2, g3
+
+    def exchange_lengths(self, nboson):
+        pl = np.zeros(nboson)
+        self.L.ref_exchange_lengths(dptr(pl))
+        return pl
+
+    def area_estimators(self):
+        out = np.zeros(6)
+        self.L.ref_area_estimators(dptr(out))
+        return out
+
+    def area_estim3d(self, iframe):
+        out = np.zeros(15)
+        self.L.ref_area_estim3d(int(iframe), dptr(out))
+        return out

@@ -1359,10 +1359,39 @@ double orc_kin_energy(const orc_ctx *c)
   return (double)P * c->sys.temperature * (0.5 * (double)(NDIM * numb) - r2avr);
 }
 
-/* GetPotEnergy_Densities -- mc_estim.cc:500-687 (value only; the density
- * histograms are not restated) */
-double orc_pot_energy_est(const orc_ctx *c)
+/* bin_1Ddensity / bin_2Ddensity / bin_3Ddensity -- mc_estim.cc:1233-1286,
+ * with the grids of densities_init (mc_estim.cc:223-255): MC_BINSR radial
+ * bins on [MIN_RADIUS, MAX_RADIUS), theta bins of pi/(MC_BINST-1), chi bins
+ * of 2 pi/(MC_BINSC-1) (mc_estim.cc:25-30) */
+static void bin_density(double *gr1d, double *gr2d, double *gr3d, int kind, int dtype, double r, double a, double b)
 {
+  const double drad = (PIMC_DENS_MAX_RADIUS - PIMC_DENS_MIN_RADIUS) / (double)PIMC_BINSR;
+  const double dth = M_PI / (double)(PIMC_BINST - 1), dch = 2.0 * M_PI / (double)(PIMC_BINSC - 1);
+  int br = (int)floor((r - PIMC_DENS_MIN_RADIUS) / drad);
+  if (br >= PIMC_BINSR || br < 0) return;
+  if (kind == 1) {
+    if (gr1d) gr1d[(long)dtype * PIMC_BINSR + br] += 1.0;
+  } else if (kind == 2) {
+    double theta = acos(a);
+    int bt = (int)floor(theta / dth);
+    if (bt < PIMC_BINST && bt >= 0 && gr2d) gr2d[((long)dtype * PIMC_BINSR + br) * PIMC_BINST + bt] += 1.0;
+  } else {
+    int bt = (int)floor(a / dth);
+    if (bt < PIMC_BINST && bt >= 0) {
+      int bc = (int)floor(b / dch);
+      if (bc < PIMC_BINSC && bc >= 0 && gr3d)
+        gr3d[(long)dtype * PIMC_BINSR * PIMC_BINST * PIMC_BINSC + ((long)br * PIMC_BINST + bt) * PIMC_BINSC + bc] += 1.0;
+    }
+  }
+}
+
+/* GetPotEnergy_Densities -- mc_estim.cc:500-687: the potential energy of the
+ * path and, with non-NULL histograms, the pair densities it bins */
+double orc_pot_energy_est(const orc_ctx *c) { return orc_pot_energy_densities(c, NULL, NULL, NULL); }
+
+double orc_pot_energy_densities(const orc_ctx *c, double *gr1d, double *gr2d, double *gr3d)
+{
+  const int bin = (gr1d || gr2d || gr3d);
   const pimc_system *s = &c->sys;
   long nb = (long)c->na * c->P;
   int P = c->P, R = c->R;
@@ -1390,20 +1419,31 @@ double orc_pot_energy_est(const orc_ctx *c)
           for (int id = 0; id < NDIM; id++) cost += (c->cosine[id * nb + tm] * dr[id]);
           cost /= r;
           cost *= sgn;
+          if (bin) bin_density(gr1d, gr2d, gr3d, 2, mol0 == PIMC_LINEAR ? type1 : type0, r, cost, 0.0);
           spot_pair += orc_lpot2d(c, r, cost);
         } else if ((mol0 == PIMC_NONLINEAR || mol1 == PIMC_NONLINEAR) && mol0 != mol1) {
           double RCOM[3], Rpt[3], E[3];
           long tm;
+          int typed;
           if (mol0 == PIMC_NONLINEAR) {
+            typed = type1;
             tm = offset0 + it / R;
             for (int id = 0; id < 3; id++) { RCOM[id] = c->coords[id * nb + t0]; Rpt[id] = c->coords[id * nb + t1]; }
           } else {
+            typed = type0;
             tm = offset1 + it / R;
             for (int id = 0; id < 3; id++) { Rpt[id] = c->coords[id * nb + t0]; RCOM[id] = c->coords[id * nb + t1]; }
           }
           euler_at(c, c->angles, nb, tm, E);
-          if (s->ispher == 0) spot_pair += orc_vcord(c, E, RCOM, Rpt, NULL, NULL, NULL);
-          else spot_pair += orc_vspher(c, r);
+          double radret, theret, chiret;
+          if (s->ispher == 0) spot_pair += orc_vcord(c, E, RCOM, Rpt, &radret, &theret, &chiret);
+          else {
+            radret = r;
+            spot_pair += orc_vspher(c, r);
+            theret = 0.0;
+            chiret = 0.0;
+          }
+          if (bin) bin_density(gr1d, gr2d, gr3d, 3, typed, radret, theret, chiret);
         } else if (mol0 == PIMC_NONLINEAR && mol1 == PIMC_NONLINEAR && s->type[c->imtype].numb > 1) {
           double com1[3], com2[3], E1[3], E2[3];
           for (int id = 0; id < 3; id++) { com1[id] = c->coords[id * nb + t0]; com2[id] = c->coords[id * nb + t1]; }
@@ -1411,12 +1451,200 @@ double orc_pot_energy_est(const orc_ctx *c)
           euler_at(c, c->angles, nb, offset1 + it / R, E2);
           spot_pair += orc_caleng(com1, com2, E1, E2);
         } else if (type0 == type1 && mol0 == PIMC_ATOM) {
+          if (bin) bin_density(gr1d, gr2d, gr3d, 1, type1, r, 0.0, 0.0);
           spot_pair += orc_spot1d(c, r);
         }
       }
       spot += spot_pair;
     }
   return (spot / (double)P);
+}
+
+/* GetExchangeLength -- mc_estim.cc:1997-2019: ploops[length] += 1 for every
+ * exchange cycle of the boson type, length counted as the reference does
+ * (a cycle of k atoms has length k-1) */
+void orc_exchange_lengths(const orc_ctx *c, double *ploops)
+{
+  int bt = -1;
+  for (int t = 0; t < c->sys.ntypes; t++)
+    if (c->sys.type[t].stat == PIMC_BOSE) bt = t;
+  if (bt < 0) return;
+  int n = c->sys.type[bt].numb;
+  int *flags = (int *)calloc((size_t)n, sizeof(int));
+  for (int atom = 0; atom < n; atom++)
+    if (flags[atom] == 0) {
+      int len = 0, p = c->pindex[atom];
+      while (p != atom) {
+        flags[p] = 1;
+        p = c->pindex[p];
+        len++;
+      }
+      ploops[len] += 1.0;
+    }
+  free(flags);
+}
+
+static int boson_type(const orc_ctx *c)
+{
+  int bt = -1;
+  for (int t = 0; t < c->sys.ntypes; t++)
+    if (c->sys.type[t].stat == PIMC_BOSE) bt = t;
+  return bt;
+}
+
+/* GetAreaEstimators -- mc_estim.cc:2087-2250: projected areas and
+ * moments of inertia of the boson paths about the (first) dopant's path,
+ * parallel and perpendicular to the linear dopant's axis.  out[6] are the
+ * increments the reference adds to _areas[PERP,PARL], _area2[PERP,PARL],
+ * _inert[PERP,PARL] (mc_estim.cc:2242-2249) */
+int orc_area_estimators(const orc_ctx *c, double *out)
+{
+  int bt = boson_type(c);
+  if (bt < 0 || c->imtype < 0) return PIMC_ERR_STATE;
+  long nb = (long)c->na * c->P;
+  int P = c->P, R = c->R;
+  long imoff = c->offset[c->imtype], off = c->offset[bt];
+  double area_perp = 0.0, area_parl = 0.0, inert_perp = 0.0, inert_parl = 0.0;
+  for (int atom = 0; atom < c->sys.type[bt].numb; atom++)
+    for (int it0 = 0; it0 < P; it0++) {
+      int it1 = (it0 + 1) % P;
+      long pt0 = off + (long)P * atom, pt1 = pt0;
+      if (it1 != it0 + 1) pt1 = off + (long)P * c->pindex[atom];
+      pt0 += it0;
+      pt1 += it1;
+      double dr0[3], dr1[3], np[3], nl[3], area[3], rn0[3], rn1[3];
+      for (int d = 0; d < 3; d++) {
+        dr0[d] = c->coords[d * nb + pt0] - c->coords[d * nb + imoff + it0];
+        dr1[d] = c->coords[d * nb + pt1] - c->coords[d * nb + imoff + it1];
+      }
+      int itr = it0 / R;
+      for (int d = 0; d < 3; d++) nl[d] = c->cosine[d * nb + imoff + itr];
+      const double zero = 10e-4;
+      double tg = 0.0, st = 1.0;
+      if (fabs(nl[0]) > zero) {
+        tg = nl[1] / nl[0];
+        st = sqrt(1.0 + tg * tg);
+      }
+      np[0] = tg / st;
+      np[1] = -1.0 / st;
+      np[2] = 0.0;
+      area[0] = 0.5 * (dr0[1] * dr1[2] - dr0[2] * dr1[1]);
+      area[1] = 0.5 * (dr0[2] * dr1[0] - dr0[0] * dr1[2]);
+      area[2] = 0.5 * (dr0[0] * dr1[1] - dr0[1] * dr1[0]);
+      for (int d = 0; d < 3; d++) {
+        area_perp += (np[d] * area[d]);
+        area_parl += (nl[d] * area[d]);
+      }
+      const double *nv[2] = {np, nl};
+      double *acc[2] = {&inert_perp, &inert_parl};
+      for (int k = 0; k < 2; k++) {
+        const double *n = nv[k];
+        rn0[0] = n[1] * dr0[2] - n[2] * dr0[1];
+        rn0[1] = n[2] * dr0[0] - n[0] * dr0[2];
+        rn0[2] = n[0] * dr0[1] - n[1] * dr0[0];
+        rn1[0] = n[1] * dr1[2] - n[2] * dr1[1];
+        rn1[1] = n[2] * dr1[0] - n[0] * dr1[2];
+        rn1[2] = n[0] * dr1[1] - n[1] * dr1[0];
+        for (int d = 0; d < 3; d++) *acc[k] += (rn0[d] * rn1[d]);
+      }
+    }
+  out[0] = area_perp;
+  out[1] = area_parl;
+  out[2] = area_perp * area_perp;
+  out[3] = area_parl * area_parl;
+  out[4] = inert_perp / (double)P;
+  out[5] = inert_parl / (double)P;
+  return PIMC_OK;
+}
+
+/* GetAreaEstim3D -- mc_estim.cc:2252-2594.  iframe 0: about the
+ * instantaneous centre of mass of all atoms (mass[type] in amu), projected
+ * on the space-fixed axes; iframe 1: about the (first) dopant, projected on
+ * its body axes hat x, y, z (the columns of matpre's rotation matrix, as
+ * vcord.f:30-34 builds them).  out[18] = area_proj[3], the increments of
+ * _areas3D (area_proj[i]*area_proj[j], j <= i, mc_estim.cc:2578-2592) and
+ * of _inert3D (inert3D[9]/P, mc_estim.cc:2566-2575) */
+int orc_area_estim3d(const orc_ctx *c, int iframe, const double *mass, double *out)
+{
+  int bt = boson_type(c);
+  if (bt < 0 || (iframe == 1 && c->imtype < 0) || !mass) return PIMC_ERR_STATE;
+  long nb = (long)c->na * c->P;
+  int P = c->P, R = c->R;
+  long off = c->offset[bt];
+  double *com = (double *)malloc(sizeof(double) * 3 * (size_t)P);
+  for (int d = 0; d < 3; d++)
+    for (int it = 0; it < P; it++) {
+      if (iframe == 0) {
+        double tmass = 0.0, v = 0.0;
+        for (int atom = 0; atom < c->na; atom++) {
+          double m = mass[c->mctype[atom]];
+          v += (m * c->coords[d * nb + (long)atom * P + it]);
+          tmass += m;
+        }
+        com[d * P + it] = v / tmass;
+      } else {
+        com[d * P + it] = c->coords[d * nb + c->offset[c->imtype] + it];
+      }
+    }
+  double bmass = mass[bt];
+  double ap[3] = {0, 0, 0}, ic[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  for (int it0 = 0; it0 < P; it0++) {
+    double hat[3][3];
+    if (iframe == 0) {
+      for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) hat[i][j] = (i == j) ? 1.0 : 0.0;
+    } else {
+      double E[3], m[9];
+      euler_at(c, c->angles, nb, c->offset[c->imtype] + it0 / R, E);
+      orc_matpre(E, m);
+      for (int i = 0; i < 3; i++)
+        for (int d = 0; d < 3; d++) hat[i][d] = m[d * 3 + i];
+    }
+    for (int atom = 0; atom < c->sys.type[bt].numb; atom++) {
+      int it1 = (it0 + 1) % P;
+      long pt0 = off + (long)P * atom, pt1 = pt0;
+      if (it1 != it0 + 1) pt1 = off + (long)P * c->pindex[atom];
+      pt0 += it0;
+      pt1 += it1;
+      double dr0[3], dr1[3], area[3], rn0[3], rn1[3];
+      for (int d = 0; d < 3; d++) {
+        dr0[d] = c->coords[d * nb + pt0] - com[d * P + it0];
+        dr1[d] = c->coords[d * nb + pt1] - com[d * P + it1];
+      }
+      area[0] = 0.5 * (dr0[1] * dr1[2] - dr0[2] * dr1[1]);
+      area[1] = 0.5 * (dr0[2] * dr1[0] - dr0[0] * dr1[2]);
+      area[2] = 0.5 * (dr0[0] * dr1[1] - dr0[1] * dr1[0]);
+      for (int i = 0; i < 3; i++)
+        for (int d = 0; d < 3; d++) ap[i] += area[d] * hat[i][d];
+      for (int i = 0; i < 3; i++) {
+        const double *h = hat[i];
+        rn0[0] = dr0[1] * h[2] - dr0[2] * h[1];
+        rn0[1] = dr0[2] * h[0] - dr0[0] * h[2];
+        rn0[2] = dr0[0] * h[1] - dr0[1] * h[0];
+        rn1[0] = dr1[1] * h[2] - dr1[2] * h[1];
+        rn1[1] = dr1[2] * h[0] - dr1[0] * h[2];
+        rn1[2] = dr1[0] * h[1] - dr1[1] * h[0];
+        double sum = 0.0;
+        for (int d = 0; d < 3; d++) sum += rn0[d] * rn1[d] * bmass;
+        ic[i * 3 + i] += sum;
+        double d0 = 0.0;
+        for (int d = 0; d < 3; d++) d0 += h[d] * dr0[d];
+        for (int j = 0; j < 3; j++)
+          if (j != i) {
+            double d1 = 0.0;
+            for (int d = 0; d < 3; d++) d1 += hat[j][d] * dr1[d];
+            ic[i * 3 + j] += -bmass * d0 * d1;
+          }
+      }
+    }
+  }
+  free(com);
+  for (int i = 0; i < 3; i++) out[i] = ap[i];
+  int ind = 3;
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j <= i; j++) out[ind++] = ap[i] * ap[j];
+  for (int k = 0; k < 9; k++) out[9 + k] = ic[k] / (double)P;
+  return PIMC_OK;
 }
 
 /* GetRotEnergy -- mc_estim.cc:939-987 (single linear rotor) */

@@ -109,6 +109,13 @@ double orc_pot_energy_est(const orc_ctx *c);
 double orc_rot_energy(const orc_ctx *c, double *erotsq, double *erot_termsq);
 double orc_rot_e3d(const orc_ctx *c, double *erotsq, double *erot_termsq);
 void   orc_rcf(const orc_ctx *c, double *rcf);   /* adds this sample's <n(t0).n(t0+dt)> sums into rcf[Q] */
+/* GetPotEnergy_Densities with its histograms: counts are added to
+ * gr1d[type][BINSR], gr2d[type][BINSR][BINST], gr3d[type][BINSR*BINST*BINSC]
+ * (any may be NULL), indexed by the density type as the reference's are */
+double orc_pot_energy_densities(const orc_ctx *c, double *gr1d, double *gr2d, double *gr3d);
+void   orc_exchange_lengths(const orc_ctx *c, double *ploops);           /* ploops[numb of the boson type] += */
+int    orc_area_estimators(const orc_ctx *c, double *out);               /* out[6]  */
+int    orc_area_estim3d(const orc_ctx *c, int iframe, const double *mass, double *out);   /* out[18] */
 
 /* reference schedule (mc_main.cc:348-381 + PIMCPass mc_main.cc:510-522) for
  * time slices [t_begin, t_begin+t_count), with the internal generator.

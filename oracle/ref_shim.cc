@@ -87,7 +87,12 @@ extern "C" void vcord_(double *Eulang, double *RCOM, double *Rpt, double *vtable
                        double *Rvmax_, double *Rvmin_, double *Rvstep_, double *vpot3d, double *radret, double *theret,
                        double *chiret, double *hatx, double *haty, double *hatz, int *ivcord)
 {
-  (void)hatx; (void)haty; (void)hatz; (void)ivcord;
+  // hat x, y, z are the columns of matpre's rotation matrix (vcord.f:30-34);
+  // ivcord = 1 returns right after them (vcord.f:42)
+  double m[9];
+  orc_matpre(Eulang, m);
+  for (int i = 0; i < 3; i++) { hatx[i] = m[i * 3 + 0]; haty[i] = m[i * 3 + 1]; hatz[i] = m[i * 3 + 2]; }
+  if (*ivcord == 1) return;
   int fold = g_chfold;
   if (fold == 0) fold = (*CHgrd_ == 181) ? 180 : (*CHgrd_ == 361 ? 360 : 90);
   *vpot3d = orc_vcord_raw(Eulang, RCOM, Rpt, vtable_, *Rgrd_, *THgrd_, *CHgrd_, fold, *Rvmax_, *Rvmin_, *Rvstep_,
@@ -121,6 +126,16 @@ extern "C" void reflec_(double *, double *, double *, double *, double *) { nrer
 extern "C" void rflmfx_(double *, double *, double *, double *, double *) { nrerror("ref_shim", "rflmfx_ not bound"); }
 extern "C" void rflmfy_(double *, double *, double *, double *, double *) { nrerror("ref_shim", "rflmfy_ not bound"); }
 extern "C" void rflmfz_(double *, double *, double *, double *, double *) { nrerror("ref_shim", "rflmfz_ not bound"); }
+
+// estimator state of mc_estim.cc (file scope, not declared in its header)
+extern double **_gr1D_sum, ***_gr2D_sum, **_gr3D_sum, *_ploops;
+extern double _areas[2], _area2[2], _inert[2];
+extern double _areas3DMFF[6], _inert3DMFF[9], _areas3DSFF[6], _inert3DSFF[9];
+extern int NUMB_DENS1D, NUMB_DENS2D, NUMB_DENS3D;
+void densities_reset(int);
+void super_reset(void);
+// histogram sizes of mc_estim.cc:25-27 (file-scope constants there)
+static const int MC_BINSR_REF = PIMC_BINSR, MC_BINST_REF = PIMC_BINST, MC_BINSC_REF = PIMC_BINSC;
 
 // table readers of mc_poten.cc (file scope, not declared in its header)
 void init_pot1D(int atype);
@@ -287,5 +302,61 @@ double ref_kin_energy(void) { return GetKinEnergy(); }
 double ref_pot_energy_est(void) { return GetPotEnergy_Densities(); }
 double ref_rot_energy(double *esq, double *ets) { double s = GetRotEnergy(); *esq = ErotSQ; *ets = Erot_termSQ; return s; }
 double ref_rot_e3d(double *esq, double *ets) { double s = GetRotE3D(); *esq = ErotSQ; *ets = Erot_termSQ; return s; }
+
+double ref_mass(int type) { return MCAtom[type].mass; }
+void ref_set_pindex(const int *pindex)
+{
+  for (int a = 0; a < NumbAtoms; a++) { PIndex[a] = pindex[a]; RIndex[pindex[a]] = a; }
+}
+
+// GetPotEnergy_Densities (mc_estim.cc:500-687) from cleared histograms; the
+// accumulated ones (_gr?D_sum) are copied out as [dtype][bins]
+double ref_densities(double *gr1d, double *gr2d, double *gr3d)
+{
+  densities_reset(MC_TOTAL);
+  densities_reset(MC_BLOCK);
+  double v = GetPotEnergy_Densities();
+  for (int d = 0; d < NUMB_DENS1D; d++)
+    for (int i = 0; i < MC_BINSR_REF; i++) gr1d[d * MC_BINSR_REF + i] = _gr1D_sum[d][i];
+  if (IMPURITY && MCAtom[IMTYPE].molecule == 1)
+    for (int d = 0; d < NUMB_DENS2D; d++)
+      for (int i = 0; i < MC_BINSR_REF; i++)
+        for (int j = 0; j < MC_BINST_REF; j++) gr2d[(d * MC_BINSR_REF + i) * MC_BINST_REF + j] = _gr2D_sum[d][i][j];
+  if (IMPURITY && MCAtom[IMTYPE].molecule == 2)
+    for (int d = 0; d < NUMB_DENS3D; d++)
+      for (long i = 0; i < (long)MC_BINSR_REF * MC_BINST_REF * MC_BINSC_REF; i++)
+        gr3d[d * (long)MC_BINSR_REF * MC_BINST_REF * MC_BINSC_REF + i] = _gr3D_sum[d][i];
+  return v;
+}
+
+// GetExchangeLength (mc_estim.cc:1997-2019) into cleared _ploops
+void ref_exchange_lengths(double *ploops)
+{
+  for (int a = 0; a < MCAtom[BSTYPE].numb; a++) _ploops[a] = 0.0;
+  GetExchangeLength();
+  for (int a = 0; a < MCAtom[BSTYPE].numb; a++) ploops[a] = _ploops[a];
+}
+
+// GetAreaEstimators (mc_estim.cc:2087-2250) from cleared sums:
+// out = _areas[2], _area2[2], _inert[2]
+void ref_area_estimators(double *out)
+{
+  super_reset();
+  GetAreaEstimators();
+  out[0] = _areas[0]; out[1] = _areas[1];       // PERP = 0, PARL = 1 (mc_estim.cc:80-81)
+  out[2] = _area2[0]; out[3] = _area2[1];
+  out[4] = _inert[0]; out[5] = _inert[1];
+}
+
+// GetAreaEstim3D (mc_estim.cc:2252-2594) from cleared sums:
+// out = _areas3D[6], _inert3D[9] of the frame
+void ref_area_estim3d(int iframe, double *out)
+{
+  super_reset();
+  GetAreaEstim3D(iframe);
+  const double *a = iframe ? _areas3DMFF : _areas3DSFF, *in = iframe ? _inert3DMFF : _inert3DSFF;
+  for (int i = 0; i < 6; i++) out[i] = a[i];
+  for (int i = 0; i < 9; i++) out[6 + i] = in[i];
+}
 
 }  // extern "C"

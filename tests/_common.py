@@ -49,3 +49,40 @@ def replay_sequence(d, bisect, molec, rotate):
         else:
             consumed.append(rotate(int(typ), st["urot"][ir])); ir += 1
     return consumed
+
+
+def dense_hist(d, key, shape):
+    """A histogram stored as non-zero bins (dens_<key>_idx/_cnt) back to shape."""
+    out = np.zeros(int(np.prod(shape)))
+    out[d["dens_%s_idx" % key]] = d["dens_%s_cnt" % key]
+    return out.reshape(shape)
+
+
+def area_scales(w, coords, masses):
+    """Magnitude bounds of the area-estimator sums of one path: s_area bounds
+    sum |n . (dr0 x dr1)| / 2 over beads, s_inert sum |(n x dr0).(n x dr1)| m / P."""
+    nbos = [t["numb"] for t in w.types if t["stat"] == 1][-1]
+    c = np.asarray(coords).reshape(3, w.natoms, w.nslices)
+    span = np.max(np.linalg.norm(c - c.mean(axis=1, keepdims=True), axis=0)) * 2.0
+    s_area = nbos * w.nslices * span * span
+    return s_area, nbos * span * span * max(1.0, float(np.max(masses)))
+
+
+def check_area(got, ref, s_area, s_inert, three_d, rtol=1e-10):
+    """Area-estimator outputs against the reference's: sums within rtol of
+    their magnitude bound, products of two sums within rtol of s_area times
+    the two sums' sizes."""
+    got, ref = np.asarray(got, float), np.asarray(ref, float)
+    if three_d:      # area_proj[3] (GPU/oracle only), products[6], inert[9]
+        a = got[:3]
+        pairs = [(i, j) for i in range(3) for j in range(i + 1)]
+        ps = np.array([s_area * (abs(a[i]) + abs(a[j])) + s_area * s_area * rtol for i, j in pairs])
+        g, r = got[3:], ref
+        scale = np.concatenate([ps, np.full(9, s_inert)])
+    else:            # areas[2], area2[2], inert[2]
+        a = got[:2]
+        scale = np.array([s_area, s_area, 2 * s_area * abs(a[0]) + s_area * s_area * rtol,
+                          2 * s_area * abs(a[1]) + s_area * s_area * rtol, s_inert, s_inert])
+        g, r = got, ref
+    err = np.abs(g - r)
+    assert np.all(err <= rtol * scale), "area estimators: err/scale %s" % (err / scale)

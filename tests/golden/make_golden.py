@@ -11,7 +11,11 @@ random numbers, and stores inputs and outputs:
     MCRotations3D calls (mc_piqmc.cc:54-1199): the final path, the accept
     counters and the number of random numbers each generator consumed;
   * the estimators GetKinEnergy, GetPotEnergy_Densities, GetRotEnergy /
-    GetRotE3D (mc_estim.cc:500-1096) of the final path.
+    GetRotE3D (mc_estim.cc:500-1096) of the final path;
+  * with bosons, under a random permutation: the density histograms of
+    GetPotEnergy_Densities (non-zero bins only), GetExchangeLength,
+    GetAreaEstimators and GetAreaEstim3D in both frames
+    (mc_estim.cc:1233-1286, 1997-2594).
 
 The reference runs single-threaded: its whole-path PotEnergy shares one
 dr[3] array across OpenMP threads (mc_piqmc.cc:1210,1237) and is not
@@ -149,6 +153,25 @@ def generate(case, nsteps=4, seed=2024):
         rot = ref.L.ref_rot_e3d(O.dptr(esq), O.dptr(ets))
     pot = ref.L.ref_pot_energy_est()
     res.update(est=np.array([kin, pot, rot, esq[0], ets[0]]))
+    # ---- densities, exchange cycles and area estimators of the final path
+    # under a permutation of the bosons (mc_estim.cc:500-687, 1997-2594)
+    bos = [i for i, t in enumerate(w.types) if t["stat"] == 1]
+    if bos:
+        nbos = w.types[bos[-1]]["numb"]
+        perm = np.arange(w.natoms, dtype=np.int32)
+        perm[:nbos] = rng.permutation(nbos)
+        ref.set_pindex(perm)
+        v, g1, g2, g3 = ref.densities()
+        res.update(perm=perm, dens_pot=np.array(v), masses=np.array([ref.L.ref_mass(t) for t in range(len(w.types))]))
+        for k, g in (("g1", g1), ("g2", g2), ("g3", g3)):
+            flat = g.ravel()
+            nz = np.flatnonzero(flat)
+            res["dens_%s_idx" % k] = nz.astype(np.int64)
+            res["dens_%s_cnt" % k] = flat[nz]
+        res["ploops"] = ref.exchange_lengths(nbos)
+        if w.types[rtype]["molecule"] == 1:
+            res["area2d"] = ref.area_estimators()
+        res["area3d"] = np.stack([ref.area_estim3d(0), ref.area_estim3d(1)])
     return res
 
 

@@ -4,7 +4,7 @@ import numpy as np
 import pytest
 
 import oracle as O
-from _common import golden, golden_cases, replay_sequence
+from _common import area_scales, check_area, dense_hist, golden, golden_cases, replay_sequence
 
 RTOL = 1e-10   # FP64 parity bound of the hot path
 
@@ -95,3 +95,26 @@ def test_move_sequence(case):
     rot, esq, ets = o.rot_energy(nonlinear)
     got = np.array([o.kin_energy(), o.pot_energy_est(), rot, esq, ets])
     np.testing.assert_allclose(got, d["est"], rtol=1e-9, atol=1e-10)
+
+
+def test_densities_cycles_areas(case):
+    """GetPotEnergy_Densities histograms, GetExchangeLength, GetAreaEstimators
+    and GetAreaEstim3D (mc_estim.cc:500-687, 1233-1286, 1997-2594) of the
+    final fixture path under the fixture's boson permutation."""
+    name, w, d = case
+    if "perm" not in d:
+        pytest.skip("no bosons in this system")
+    o = O.Oracle(w)
+    o.set_state(d["coords1"], d["angles1"], d["perm"])
+    v, g1, g2, g3 = o.densities()
+    assert v == pytest.approx(float(d["dens_pot"]), rel=RTOL, abs=1e-12)
+    np.testing.assert_array_equal(g1, dense_hist(d, "g1", g1.shape))
+    np.testing.assert_array_equal(g2, dense_hist(d, "g2", g2.shape))
+    np.testing.assert_array_equal(g3, dense_hist(d, "g3", g3.shape))
+    assert g1.sum() + g2.sum() + g3.sum() > 0
+    np.testing.assert_array_equal(o.exchange_lengths(len(d["ploops"])), d["ploops"])
+    s_area, s_inert = area_scales(w, d["coords1"], d["masses"])
+    if "area2d" in d:
+        check_area(o.area_estimators(), d["area2d"], s_area, s_inert, False)
+    for fr in (0, 1):
+        check_area(o.area_estim3d(fr, d["masses"]), d["area3d"][fr], s_area, s_inert, True)
