@@ -129,6 +129,28 @@ pimc_status pimc_area_estimators(pimc_handle *h, double *out);
  * row-major 3x3). */
 pimc_status pimc_area_estim3d(pimc_handle *h, int iframe, const double *mass, double *out);
 
+/* ---- propagator tables ---------------------------------------------------- */
+
+/* The exact linear-rotor propagator of linear_prop/linden.f (tau and the l
+ * cut-off linden.f:21-37, exarho linden.f:88-122) for n (temperature K,
+ * rotational slices) pairs at once: out[(t*4 + c)*npt + i], columns c =
+ * cos gamma, rho, erot, erotsq of the .rot file rows linden.f:48-68.  bconst
+ * in cm^-1; iodevn -1 (all l), 0 (even l), 1 (odd l). */
+pimc_status pimc_linden(int device, int n, const double *temperature, const int *nslice, double bconst, int npt,
+                        int iodevn, double *out);
+
+/* The exact asymmetric-top propagator of nmv_prop/asymrho.f:34-735 on its
+ * 1-degree grid for theta = ith0..ith1 (degrees): rho, erot and esq
+ * [(ith - ith0)*361*361 + iphi*361 + ichi] as the rho.denXXX_{rho,eng,esq}
+ * slabs, energies in cm^-1; abc = A, B, C in cm^-1, J <= maxj.  info[15]
+ * (optional): Z, E, Cv of the even-K, odd-K and all states at beta, then Z, E
+ * of the three at tau (the "AT BETA" / "AT TAU" lines, asymrho.f:299-423).
+ * PIMC_ERR_BAD_ARG where the reference stops (maxj too small for the
+ * temperature: exp(-tau E_max) > 1e-8). */
+#define PIMC_ASYMRHO_MAXJ 300
+pimc_status pimc_asymrho(int device, double temperature, int nslice, int iodevn, int ith0, int ith1,
+                         const double *abc, int maxj, double *rho, double *erot, double *esq, double *info);
+
 /* ---- production sampler -------------------------------------------------- */
 
 /* npasses passes of the reference schedule's moves (mc_main.cc:348-381,

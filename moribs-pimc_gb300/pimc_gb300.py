@@ -53,6 +53,9 @@ def load(path=LIBPATH):
     L.pimc_pot_rot_energy.argtypes = [vp, C.c_int, _ip, _ip, _dp, _dp]
     L.pimc_estimators.argtypes = [vp, _dp]
     L.pimc_rcf.argtypes = [vp, _dp]
+    L.pimc_linden.argtypes = [C.c_int, C.c_int, _dp, _ip, C.c_double, C.c_int, C.c_int, _dp]
+    L.pimc_asymrho.argtypes = [C.c_int, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, _dp, C.c_int,
+                               _dp, _dp, _dp, _dp]
     L.pimc_densities_accumulate.argtypes = [vp]
     L.pimc_densities_read.argtypes = [vp, _dp, _dp, _dp]
     L.pimc_densities_reset.argtypes = [vp]
@@ -379,3 +382,30 @@ class Batch:
     @staticmethod
     def replica_seed(seed, r):
         return int(load().pimc_batch_replica_seed(C.c_uint64(seed), int(r)))
+
+
+def linden(temperatures, nslices, bconst, npt, iodevn=-1, device=0):
+    """pimc_linden: exact linear-rotor propagator tables (linear_prop/linden.f)
+    for each (temperature, nslice) pair; shape (n, 4, npt) with rows cos gamma,
+    rho, erot, erotsq."""
+    L = load()
+    T = np.ascontiguousarray(np.atleast_1d(temperatures), dtype=np.float64)
+    ns = np.ascontiguousarray(np.broadcast_to(np.atleast_1d(nslices), T.shape), dtype=np.int32)
+    out = np.zeros((len(T), 4, int(npt)))
+    _chk(L.pimc_linden(int(device), len(T), dptr(T), iptr(ns), float(bconst), int(npt), int(iodevn), dptr(out)),
+         "pimc_linden")
+    return out
+
+
+def asymrho(temperature, nslice, iodevn, ith0, ith1, abc, maxj, device=0):
+    """pimc_asymrho: exact asymmetric-top propagator (nmv_prop/asymrho.f) on
+    the 1-degree grid for theta ith0..ith1: (rho, erot, esq) each of shape
+    (ith1-ith0+1, 361, 361), and info[15]."""
+    L = load()
+    n = int(ith1) - int(ith0) + 1
+    rho, erot, esq = (np.zeros((n, 361, 361)) for _ in range(3))
+    info = np.zeros(15)
+    a = np.ascontiguousarray(abc, dtype=np.float64)
+    _chk(L.pimc_asymrho(int(device), float(temperature), int(nslice), int(iodevn), int(ith0), int(ith1), dptr(a),
+                        int(maxj), dptr(rho), dptr(erot), dptr(esq), dptr(info)), "pimc_asymrho")
+    return rho, erot, esq, info

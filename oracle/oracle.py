@@ -8,6 +8,7 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+import platform
 import shutil
 import subprocess
 import sys
@@ -28,11 +29,17 @@ _ip = C.POINTER(C.c_int)
 
 
 def build_oracle(force=False):
-    """Compile oracle/pimc_oracle.c into oracle/liboracle.so (C11 + OpenMP)."""
-    src = os.path.join(HERE, "pimc_oracle.c")
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(src):
+    """Compile oracle/pimc_oracle.c and orc_tables.c into oracle/liboracle.so
+    (C11 + OpenMP; libquadmath for the quad-precision type on x86-64).  No
+    multiply-add contraction, so that products and sums round as written on
+    every host (the reference's x86-64 builds have none)."""
+    srcs = [os.path.join(HERE, f) for f in ("pimc_oracle.c", "orc_tables.c")]
+    deps = srcs + [os.path.join(HERE, "pimc_oracle.h")]
+    if not force and os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(f) for f in deps):
         return LIB
-    cmd = ["gcc", "-std=gnu11", "-O2", "-fopenmp", "-fPIC", "-shared", src, "-o", LIB, "-lm"]
+    cmd = ["gcc", "-std=gnu11", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared"] + srcs + ["-o", LIB, "-lm"]
+    if platform.machine() in ("x86_64", "AMD64", "i686"):
+        cmd.append("-lquadmath")
     subprocess.check_call(cmd)
     return LIB
 
@@ -116,6 +123,15 @@ def _lib():
     lib.orc_exchange_lengths.argtypes = [C.c_void_p, _dp]
     lib.orc_area_estimators.argtypes = [C.c_void_p, _dp]
     lib.orc_area_estim3d.argtypes = [C.c_void_p, C.c_int, _dp, _dp]
+    lib.orc_linden.argtypes = [C.c_double, C.c_int, C.c_double, C.c_int, C.c_int, _dp, _dp, _dp, _dp]
+    lib.orc_linden_lmax.argtypes = [C.c_double, C.c_int, C.c_double, _dp]
+    lib.orc_rotmat.restype = C.c_double
+    lib.orc_rotmat.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double]
+    lib.orc_wigd.restype = C.c_double
+    lib.orc_wigd.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double]
+    lib.orc_asymrho_energies.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, _dp]
+    lib.orc_asymrho_points.argtypes = [C.c_double, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_int,
+                                       C.c_int, _ip, _ip, _ip, _dp, _dp, _dp, _dp]
     lib.orc_run_steps.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_uint64, C.c_int, _dp]
     return lib
 
@@ -431,3 +447,33 @@ class Reference:
         out = np.zeros(15)
         self.L.ref_area_estim3d(int(iframe), dptr(out))
         return out
+
+
+def linden(temprt, nslice, bconst, npt, iodevn=-1):
+    """linear_prop/linden.f: (cost, rho, erot, erotsq) rows, shape (4, npt)."""
+    out = np.zeros((4, npt))
+    st = lib().orc_linden(float(temprt), int(nslice), float(bconst), int(npt), int(iodevn),
+                          dptr(out[0]), dptr(out[1]), dptr(out[2]), dptr(out[3]))
+    if st != 0:
+        raise RuntimeError("orc_linden status %d" % st)
+    return out
+
+
+def asymrho_points(temprt, nslice, iodevn, abc, maxj, ith, iphi, ichi):
+    """nmv_prop/asymrho.f at grid points (degrees): (rho, erot, esq, info[15])."""
+    ith, iphi, ichi = (np.ascontiguousarray(a, dtype=np.int32) for a in (ith, iphi, ichi))
+    n = len(ith)
+    r, e, s, info = np.zeros(n), np.zeros(n), np.zeros(n), np.zeros(15)
+    st = lib().orc_asymrho_points(float(temprt), int(nslice), int(iodevn), float(abc[0]), float(abc[1]),
+                                  float(abc[2]), int(maxj), n, iptr(ith), iptr(iphi), iptr(ichi),
+                                  dptr(r), dptr(e), dptr(s), dptr(info))
+    if st != 0:
+        raise RuntimeError("orc_asymrho_points status %d" % st)
+    return r, e, s, info
+
+
+def asymrho_energies(maxj, abc):
+    n = (maxj + 1) * (maxj + 1)
+    out = np.zeros(n)
+    m = lib().orc_asymrho_energies(int(maxj), float(abc[0]), float(abc[1]), float(abc[2]), dptr(out))
+    return out[:m]

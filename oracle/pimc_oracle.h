@@ -117,6 +117,18 @@ void   orc_exchange_lengths(const orc_ctx *c, double *ploops);           /* ploo
 int    orc_area_estimators(const orc_ctx *c, double *out);               /* out[6]  */
 int    orc_area_estim3d(const orc_ctx *c, int iframe, const double *mass, double *out);   /* out[18] */
 
+/* propagator-table generators (orc_tables.c): linear_prop/linden.f and
+ * nmv_prop/asymrho.f restated */
+int    orc_linden_lmax(double temprt, int nslice, double bconst, double *tau_out);
+int    orc_linden(double temprt, int nslice, double bconst, int npt, int iodevn, double *cost, double *rho,
+                  double *erot, double *erotsq);
+double orc_rotmat(int j, int k, int kp, double A, double B, double C);
+double orc_wigd(int j, int m, int k, double theta);
+int    orc_asymrho_energies(int maxj, double A, double B, double C, double *eng);
+int    orc_asymrho_points(double temprt, int nslice, int iodevn, double A, double B, double C, int maxj, int npts,
+                          const int *ith, const int *iphi, const int *ichi, double *rho, double *erot, double *esq,
+                          double *info);
+
 /* reference schedule (mc_main.cc:348-381 + PIMCPass mc_main.cc:510-522) for
  * time slices [t_begin, t_begin+t_count), with the internal generator.
  * nthreads > 1 parallelises the even/odd rotational phases and the
