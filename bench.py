@@ -52,6 +52,7 @@ def parse():
     ap.add_argument("--no-companion", action="store_true", help="skip the other precision's measurement")
     ap.add_argument("--no-batched", action="store_true", help="skip the config-2 replica-batch measurement")
     ap.add_argument("--batched-replicas", type=int, default=4096)
+    ap.add_argument("--no-tables", action="store_true", help="skip the propagator-table generator measurement")
     return ap.parse_args()
 
 
@@ -399,6 +400,55 @@ def run_batched(args, local, dist):
     return out
 
 
+def run_tables(local, cpu):
+    """The propagator-table generators, end to end through the C ABI (host
+    eigen-decomposition, device sums, copy to host, symmetric fill):
+    asymrho.f's full 181 x 361 x 361 table for nmv_prop/a-run (T 0.37 K, 128
+    slices, A B C 0.6666525 0.2306476 0.1769383 cm^-1, J <= 66) and linden.f
+    tables of 1500 points for the 4096 (T, Q) pairs of the replica batch.
+    The CPU figures are the oracle's restatements of the reference's loops
+    timed on a few points or tables and scaled to the whole job."""
+    import numpy as np
+    import pimc_gb300 as G
+    import workloads as W
+    out = {}
+    abc = (0.6666525, 0.2306476, 0.1769383)
+    G.asymrho(0.37, 128, -1, 10, 10, abc, 66, device=local)          # warm-up (context, allocations)
+    t0 = time.perf_counter()
+    rho, erot, esq, info = G.asymrho(0.37, 128, -1, 0, 180, abc, 66, device=local)
+    gpu_s = time.perf_counter() - t0
+    del rho, erot, esq
+    computed = 181 * sum((p if p <= 90 else (180 - p if p <= 180 else (p - 180 if p <= 270 else 360 - p))) + 1
+                         for p in range(361))
+    out["asymrho"] = {"config": "nmv_prop/a-run: T 0.37 K, 128 slices, iodevn -1, A B C 0.6666525 0.2306476 "
+                                "0.1769383 cm^-1, maxj 66; 181 x 361 x 361 grid", "gpu_s": round(gpu_s, 3),
+                      "computed_points": computed}
+    ws = W.config2(n=4096, seed=2024)
+    T = np.array([w.temperature for w in ws])
+    Q = np.array([w.nrotslices for w in ws])
+    G.linden(T[:4], Q[:4], 0.39021, 1500, device=local)
+    t0 = time.perf_counter()
+    G.linden(T, Q, 0.39021, 1500, device=local)
+    lin_s = time.perf_counter() - t0
+    out["linden"] = {"config": "4096 tables x 1500 points, B 0.39021 cm^-1, (T, Q) of the replica batch",
+                     "gpu_s": round(lin_s, 4)}
+    if cpu:
+        import oracle as O
+        t0 = time.perf_counter()
+        O.asymrho_points(0.37, 128, -1, abc, 66, [10, 10], [40, 200], [20, 30])
+        per_pt = (time.perf_counter() - t0) / 2.0
+        out["asymrho"]["cpu_baseline"] = {"kind": "port", "cores": 1, "sample": "2 grid points (with the "
+                                          "Wigner d list of one theta)", "s_per_point": round(per_pt, 4),
+                                          "extrapolated_s": round(per_pt * computed, 1)}
+        t0 = time.perf_counter()
+        for i in range(16):
+            O.linden(T[i], int(Q[i]), 0.39021, 1500)
+        per_tab = (time.perf_counter() - t0) / 16
+        out["linden"]["cpu_baseline"] = {"kind": "port", "cores": 1, "sample": "16 tables",
+                                         "s_per_table": round(per_tab, 5), "extrapolated_s": round(per_tab * 4096, 2)}
+    return out
+
+
 def main():
     args = parse()
     rank, local, world = dist_env()
@@ -423,6 +473,8 @@ def main():
             rate, sample = cpu_baseline(w, args.cpu_seconds, ncores)
             line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": ncores, "kind": "port", "sample": sample,
                                     "host_cpu": host_cpu()}
+        if not args.no_tables and world == 1:
+            line["tables"] = run_tables(local, not args.no_cpu)
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.barrier()
