@@ -129,6 +129,28 @@ pimc_status pimc_area_estimators(pimc_handle *h, double *out);
  * row-major 3x3). */
 pimc_status pimc_area_estim3d(pimc_handle *h, int iframe, const double *mass, double *out);
 
+/* ---- worm algorithm (mc_qworm.cc) ------------------------------------------ */
+
+/* MCWormInit (mc_qworm.cc:49-82) for the atom type `type` with the WORM
+ * line's c and m (mc_input.cc:286-295) and the input DENSITY; m < P and
+ * m <= 64.  The worm starts closed. */
+pimc_status pimc_worm_init(pimc_handle *h, int type, double c, int m, double density);
+/* One MCWormMove call (mc_qworm.cc:93-125): for each atom of the worm type
+ * an open or close try, an advance or recede try and, for bosons, a swap
+ * try, with the random numbers replayed from nine streams in the order
+ * mc_qworm.cc draws them: streams[0..2] the uniforms behind nrnd1, nrnd2,
+ * nrnd3 (mc_randg.cc:159-171), streams[3..7] rnd1..rnd5, streams[8] the x1
+ * values of gauss() (mc_randg.cc:138-150).  consumed[9] (optional): draws
+ * taken from each.  Potential sums leave out partner beads in the worm's
+ * gap as PotEnergy does (WorldLine, mc_qworm.cc:553-575).  FP64 only. */
+pimc_status pimc_worm_move(pimc_handle *h, const double *const *streams, const long *lengths, long *consumed);
+/* the worm {exists, ira, masha, atom_i, atom_m} (TPathWorm, mc_qworm.h:32-48) */
+pimc_status pimc_worm_state(pimc_handle *h, int *state);
+pimc_status pimc_worm_set_state(pimc_handle *h, const int *state);
+/* QWTotal / QWAccep (mc_qworm.h:52-53): [QW_OPEN, CLOSE, INSERT, REMOVE,
+ * ADVANCE, RECEDE, SWAP] */
+pimc_status pimc_worm_counters(pimc_handle *h, double *total, double *accep);
+
 /* ---- propagator tables ---------------------------------------------------- */
 
 /* The exact linear-rotor propagator of linear_prop/linden.f (tau and the l

@@ -53,6 +53,11 @@ struct pimc_handle {
   // pair-density histograms (allocated on first use)
   DensHist dens{nullptr, nullptr, nullptr};
   int dens_on = 0;
+  // worm algorithm (allocated by pimc_worm_init)
+  DevWorm *worm = nullptr;
+  int *rindex = nullptr;
+  long *wcur = nullptr;
+  int worm_on = 0;
 };
 
 extern "C" const char *pimc_status_string(pimc_status s)
@@ -327,7 +332,8 @@ extern "C" pimc_status pimc_destroy(pimc_handle *h)
   DevState &st = h->ctx.st;
   void *bufs[] = {st.x, st.y, st.z, st.b4, st.cosvf, st.rp_cache, st.rl_cache, st.rp_ok, st.rl_ok,
                   st.ang, st.cosv, st.pindex, st.mctype, st.err, h->frames, h->cnt, h->pass, h->cursors, h->ms,
-                  h->qbuf, h->prog, h->abort_word, h->dens.g1, h->dens.g2, h->dens.g3};
+                  h->qbuf, h->prog, h->abort_word, h->dens.g1, h->dens.g2, h->dens.g3, h->worm, h->rindex,
+                  h->wcur};
   for (void *b : bufs)
     if (b) cudaFree(b);
   for (void *b : h->owned) cudaFree(b);
@@ -594,6 +600,11 @@ extern "C" pimc_status pimc_set_state(pimc_handle *h, const double *coords, cons
       if (pindex[a] < 0 || pindex[a] >= d.na) return PIMC_ERR_BAD_ARG;
     CK(cudaMemcpy(h->ctx.st.pindex, pindex, d.na * sizeof(int), cudaMemcpyHostToDevice));
     h->pindex_host.assign(pindex, pindex + d.na);
+    if (h->rindex) {
+      std::vector<int> r(d.na);
+      for (int a = 0; a < d.na; a++) r[pindex[a]] = a;
+      CK(cudaMemcpy(h->rindex, r.data(), d.na * sizeof(int), cudaMemcpyHostToDevice));
+    }
   }
   CK(cudaStreamSynchronize(h->stream));
   if (coords && angles) h->state = true;
@@ -1027,6 +1038,117 @@ extern "C" pimc_status pimc_area_estim3d(pimc_handle *h, int iframe, const doubl
   for (int i = 0; i < 3; i++)
     for (int j = 0; j <= i; j++) out[ind++] = v[i] * v[j];
   for (int k = 0; k < 9; k++) out[9 + k] = v[3 + k] / (double)d.P;
+  return PIMC_OK;
+}
+
+// ------------------------------------------------------------ worm algorithm
+
+extern "C" pimc_status pimc_worm_init(pimc_handle *h, int type, double c, int m, double density)
+{
+  if (!h) return PIMC_ERR_BAD_ARG;
+  const DevSys &d = h->ctx.s;
+  if (type < 0 || type >= d.ntypes || d.molecule[type] != PIMC_ATOM || m < 1 || m >= d.P) return PIMC_ERR_BAD_ARG;
+  if (m > PIMC_WORM_MAXM) return PIMC_ERR_SIZE;
+  CK(cudaSetDevice(h->device));
+  pimc_status e;
+  if (!h->worm) {
+    if ((e = dalloc(h, &h->worm, 1)) || (e = dalloc(h, &h->rindex, d.na)) || (e = dalloc(h, &h->wcur, 16))) return e;
+  }
+  // MCWormInit (mc_qworm.cc:49-82): Worm.c scaled by the density per bead
+  // and segment, the open-move normalisation and the neighbour cut-off
+  DevWorm w{};
+  int numb = d.numb[type];
+  double cw = c * (density / (double)(numb * d.P * m));
+  w.type = type;
+  w.m = m;
+  w.numb = numb;
+  w.first = d.first[type];
+  w.qw_norm = cw * numb * d.P * m;
+  w.twave2 = 4.0 * d.lambda[type] * d.tau;                   // mc_setup.cc:394
+  w.cut2 = 100.0 * 100.0 * ((double)m * 4.0 * d.lambda[type] * d.tau);
+  CK(cudaMemcpy(h->worm, &w, sizeof(DevWorm), cudaMemcpyHostToDevice));
+  std::vector<int> r(d.na);
+  for (int a = 0; a < d.na; a++) r[h->pindex_host[a]] = a;
+  CK(cudaMemcpy(h->rindex, r.data(), d.na * sizeof(int), cudaMemcpyHostToDevice));
+  h->worm_on = 1;
+  return PIMC_OK;
+}
+
+extern "C" pimc_status pimc_worm_move(pimc_handle *h, const double *const *streams, const long *lengths,
+                                      long *consumed)
+{
+  pimc_status e = ready(h);
+  if (e) return e;
+  if (!h->worm_on) return PIMC_ERR_STATE;
+  if (!streams || !lengths) return PIMC_ERR_BAD_ARG;
+  if (h->ctx.s.mixed) return PIMC_ERR_STATE;          // the worm moves run on the FP64 path
+  size_t bytes = 4096;
+  for (int k = 0; k < 9; k++) {
+    if (lengths[k] < 0 || (lengths[k] && !streams[k])) return PIMC_ERR_BAD_ARG;
+    bytes += ((size_t)(lengths[k] > 0 ? lengths[k] : 1) * sizeof(double) + 255) / 256 * 256;
+  }
+  int numb = h->ctx.s.numb[0];
+  for (int t = 0; t < h->ctx.s.ntypes; t++) numb = std::max(numb, h->ctx.s.numb[t]);
+  bytes += worm_scratch_bytes(numb) + 256;
+  void *buf;
+  if ((e = scratch(h, bytes, &buf))) return e;
+  char *cur = (char *)buf;
+  double *dv[9];
+  for (int k = 0; k < 9; k++)
+    if ((e = put_stream(h, streams[k], lengths[k], &dv[k], cur))) return e;
+  CK(cudaMemsetAsync(h->wcur, 0, 16 * sizeof(long), h->stream));
+  launch_worm_move(h->ctx, h->frames, h->worm, h->rindex, dv, lengths, h->wcur, cur, numb, h->stream);
+  launch_invalidate_caches(h->ctx, h->stream);       // beads of the worm type moved
+  h->launches += 2;
+  CK(cudaGetLastError());
+  long cz[16];
+  CK(cudaMemcpyAsync(cz, h->wcur, 16 * sizeof(long), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaMemcpyAsync(h->pindex_host.data(), h->ctx.st.pindex, h->ctx.s.na * sizeof(int), cudaMemcpyDeviceToHost,
+                     h->stream));
+  e = check_err(h);
+  if (consumed)
+    for (int k = 0; k < 9; k++) consumed[k] = cz[k];
+  return e;
+}
+
+extern "C" pimc_status pimc_worm_state(pimc_handle *h, int *state)
+{
+  if (!h || !state) return PIMC_ERR_BAD_ARG;
+  if (!h->worm_on) return PIMC_ERR_STATE;
+  CK(cudaSetDevice(h->device));
+  DevWorm w;
+  CK(cudaMemcpyAsync(&w, h->worm, sizeof(DevWorm), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  state[0] = w.exists; state[1] = w.ira; state[2] = w.masha; state[3] = w.atom_i; state[4] = w.atom_m;
+  return PIMC_OK;
+}
+
+extern "C" pimc_status pimc_worm_set_state(pimc_handle *h, const int *state)
+{
+  if (!h || !state) return PIMC_ERR_BAD_ARG;
+  if (!h->worm_on) return PIMC_ERR_STATE;
+  CK(cudaSetDevice(h->device));
+  DevWorm w;
+  CK(cudaMemcpyAsync(&w, h->worm, sizeof(DevWorm), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  int P = h->ctx.s.P;
+  if (state[1] < 0 || state[1] >= P || state[2] < 0 || state[2] >= P || state[3] < 0 || state[3] >= w.numb ||
+      state[4] < 0 || state[4] >= w.numb)
+    return PIMC_ERR_BAD_ARG;
+  w.exists = state[0] ? 1 : 0; w.ira = state[1]; w.masha = state[2]; w.atom_i = state[3]; w.atom_m = state[4];
+  CK(cudaMemcpy(h->worm, &w, sizeof(DevWorm), cudaMemcpyHostToDevice));
+  return PIMC_OK;
+}
+
+extern "C" pimc_status pimc_worm_counters(pimc_handle *h, double *total, double *accep)
+{
+  if (!h || !total || !accep) return PIMC_ERR_BAD_ARG;
+  if (!h->worm_on) return PIMC_ERR_STATE;
+  CK(cudaSetDevice(h->device));
+  DevWorm w;
+  CK(cudaMemcpyAsync(&w, h->worm, sizeof(DevWorm), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  for (int k = 0; k < 7; k++) { total[k] = w.qwtot[k]; accep[k] = w.qwacc[k]; }
   return PIMC_OK;
 }
 

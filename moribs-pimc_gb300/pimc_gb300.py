@@ -53,6 +53,11 @@ def load(path=LIBPATH):
     L.pimc_pot_rot_energy.argtypes = [vp, C.c_int, _ip, _ip, _dp, _dp]
     L.pimc_estimators.argtypes = [vp, _dp]
     L.pimc_rcf.argtypes = [vp, _dp]
+    L.pimc_worm_init.argtypes = [vp, C.c_int, C.c_double, C.c_int, C.c_double]
+    L.pimc_worm_move.argtypes = [vp, C.POINTER(_dp), C.POINTER(C.c_long), C.POINTER(C.c_long)]
+    L.pimc_worm_state.argtypes = [vp, _ip]
+    L.pimc_worm_set_state.argtypes = [vp, _ip]
+    L.pimc_worm_counters.argtypes = [vp, _dp, _dp]
     L.pimc_linden.argtypes = [C.c_int, C.c_int, _dp, _ip, C.c_double, C.c_int, C.c_int, _dp]
     L.pimc_asymrho.argtypes = [C.c_int, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, _dp, C.c_int,
                                _dp, _dp, _dp, _dp]
@@ -217,6 +222,35 @@ class Sampler:
         out = np.zeros(self.w.nrotslices)
         _chk(self.L.pimc_rcf(self.h, dptr(out)), "pimc_rcf")
         return out
+
+    # worm algorithm (mc_qworm.cc)
+    WSTREAMS = ("n1", "n2", "n3", "u1", "u2", "u3", "u4", "u5", "gauss")
+
+    def worm_init(self, type_, c, m, density):
+        _chk(self.L.pimc_worm_init(self.h, int(type_), float(c), int(m), float(density)), "pimc_worm_init")
+
+    def worm_move(self, streams):
+        """One MCWormMove with the replay streams of WSTREAMS; returns the draws consumed per stream."""
+        arrs = [np.ascontiguousarray(streams.get(n, np.zeros(0)), dtype=np.float64) for n in self.WSTREAMS]
+        ptrs = (_dp * 9)(*[dptr(a) if len(a) else _dp() for a in arrs])
+        lens = (C.c_long * 9)(*[len(a) for a in arrs])
+        used = (C.c_long * 9)()
+        _chk(self.L.pimc_worm_move(self.h, ptrs, lens, used), "pimc_worm_move")
+        return list(used)
+
+    def worm_state(self):
+        st = np.zeros(5, np.int32)
+        _chk(self.L.pimc_worm_state(self.h, iptr(st)), "pimc_worm_state")
+        return st
+
+    def worm_set_state(self, st):
+        a = np.ascontiguousarray(st, dtype=np.int32)
+        _chk(self.L.pimc_worm_set_state(self.h, iptr(a)), "pimc_worm_set_state")
+
+    def worm_counters(self):
+        t, a = np.zeros(7), np.zeros(7)
+        _chk(self.L.pimc_worm_counters(self.h, dptr(t), dptr(a)), "pimc_worm_counters")
+        return t, a
 
     def densities_accumulate(self):
         _chk(self.L.pimc_densities_accumulate(self.h), "pimc_densities_accumulate")

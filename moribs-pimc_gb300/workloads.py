@@ -242,6 +242,8 @@ class Workload:
     angles: np.ndarray | None = None   # [3, natoms*P]
     pindex: np.ndarray | None = None
     chi_fold_deg: int = 0
+    worm: tuple | None = None          # (type name, c, m) of the WORM input line
+    density: float = 0.02               # DENSITY of qmc.input (the worm's normalisation)
 
     @property
     def natoms(self) -> int:
@@ -458,7 +460,7 @@ def write_reference_inputs(w: Workload, workdir: str, passes=1, blocks=1):
     """qmc.input plus the 1D/2D potential and .rot files the reference reads."""
     os.makedirs(workdir, exist_ok=True)
     lines = ["MASTERDIR ./", "OUTPUTDIR ./", "FILENAMEPREFIX ref", "DIMENSION 3",
-             "DENSITY 0.02", "TEMPERATURE %r" % w.temperature]
+             "DENSITY %r" % w.density, "TEMPERATURE %r" % w.temperature]
     for t in w.types:
         kw = "ATOM" if t["molecule"] == 0 else ("MOLECULE" if t["molecule"] == 1 else "NONLINEAR")
         stat = "BOSE" if t["stat"] == 1 else "BOLTZMANN"
@@ -469,6 +471,8 @@ def write_reference_inputs(w: Workload, workdir: str, passes=1, blocks=1):
         lines.append("ROTATION %s %r %d" % (rt["name"], w.rtstep, w.nrotslices))
         lines.append("ROTDENSI %d %d %r %r %r %r %d" % (w.rot_den_type, w.rot_odevn, w.rot_eoff,
                                                          w.rot_abc[0], w.rot_abc[1], w.rot_abc[2], w.rn_ratio))
+    if w.worm is not None:
+        lines.append("WORM %s %r %d" % (w.worm[0], float(w.worm[1]), int(w.worm[2])))
     lines += ["NUMBEROFSLICES %d" % w.nslices, "NUMBEROFPASSES %d" % passes,
               "NUMBEROFBLOCKS %d 0" % blocks, "MCSKIP_RATIO 1000000", "MCSKIP_TOTAL 1000000", "MCSKIP_AVERG 1"]
     with open(os.path.join(workdir, "qmc.input"), "w") as f:

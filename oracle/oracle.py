@@ -53,6 +53,28 @@ class Replay(C.Structure):
                 ("overrun", C.c_int)]
 
 
+WSTREAMS = ("n1", "n2", "n3", "u1", "u2", "u3", "u4", "u5", "gauss")
+
+
+class WReplay(C.Structure):
+    _fields_ = [(n, Stream) for n in WSTREAMS] + [("overrun", C.c_int)]
+
+
+def make_wreplay(streams):
+    """WReplay over a dict of the worm streams (n1..n3 = nrnd1..3, u1..u5 =
+    rnd1..5, gauss); missing streams are empty."""
+    keep = []
+    rp = WReplay()
+    for name in WSTREAMS:
+        a = streams.get(name)
+        if a is not None:
+            a = np.ascontiguousarray(a, dtype=np.float64)
+            keep.append(a)
+            st = getattr(rp, name)
+            st.v, st.n, st.pos = dptr(a), len(a), 0
+    return rp, keep
+
+
 def make_replay(u1=None, u2=None, u3=None, gauss=None, urot=None):
     keep = []
     rp = Replay()
@@ -132,6 +154,11 @@ def _lib():
     lib.orc_asymrho_energies.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, _dp]
     lib.orc_asymrho_points.argtypes = [C.c_double, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_int,
                                        C.c_int, _ip, _ip, _ip, _dp, _dp, _dp, _dp]
+    lib.orc_worm_init.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_int, C.c_double]
+    lib.orc_worm_move.argtypes = [C.c_void_p, C.POINTER(WReplay)]
+    lib.orc_worm_state.argtypes = [C.c_void_p, _ip]
+    lib.orc_worm_set_state.argtypes = [C.c_void_p, _ip]
+    lib.orc_worm_counters.argtypes = [C.c_void_p, _dp, _dp]
     lib.orc_run_steps.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_uint64, C.c_int, _dp]
     return lib
 
@@ -237,6 +264,31 @@ class Oracle:
         fn = self.L.orc_bisection_move_exchange if exchange else self.L.orc_bisection_move
         st = fn(self.h, type_, int(time), C.byref(rp), dptr(ds), iptr(lv))
         return st, ds.reshape(t["numb"], t["levels"]), lv, (rp.gauss.pos, rp.u3.pos)
+
+    # worm algorithm
+    def worm_init(self, type_, c, m, density):
+        st = self.L.orc_worm_init(self.h, int(type_), float(c), int(m), float(density))
+        if st != 0:
+            raise RuntimeError("orc_worm_init status %d" % st)
+
+    def worm_move(self, streams):
+        rp, keep = make_wreplay(streams)
+        st = self.L.orc_worm_move(self.h, C.byref(rp))
+        return st, [getattr(rp, n).pos for n in WSTREAMS]
+
+    def worm_state(self):
+        st = np.zeros(5, np.int32)
+        self.L.orc_worm_state(self.h, iptr(st))
+        return st
+
+    def worm_set_state(self, st):
+        st = np.ascontiguousarray(st, dtype=np.int32)
+        self.L.orc_worm_set_state(self.h, iptr(st))
+
+    def worm_counters(self):
+        t, a = np.zeros(7), np.zeros(7)
+        self.L.orc_worm_counters(self.h, dptr(t), dptr(a))
+        return t, a
 
     def rotations(self, type_, urot):
         rp, keep = make_replay(urot=urot)
@@ -353,6 +405,12 @@ class Reference:
         for n in ("ref_rot_energy", "ref_rot_e3d"):
             getattr(L, n).restype = C.c_double
             getattr(L, n).argtypes = [_dp, _dp]
+        L.ref_set_wreplay.argtypes = sum(([_dp, C.c_long] for _ in range(9)), [])
+        L.ref_wreplay_pos.argtypes = [C.POINTER(C.c_long)]
+        L.ref_worm_state.argtypes = [_ip]
+        L.ref_worm_set_state.argtypes = [_ip]
+        L.ref_worm_counters.argtypes = [_dp, _dp]
+        L.ref_pindex.argtypes = [_ip, _ip]
         L.ref_mass.restype = C.c_double
         L.ref_mass.argtypes = [C.c_int]
         L.ref_set_pindex.argtypes = [_ip]
@@ -423,6 +481,38 @@ class Reference:
         tot = np.zeros(6); acc = np.zeros(6)
         self.L.ref_counters(dptr(tot), dptr(acc))
         return tot, acc
+
+    def worm_move(self, streams):
+        self._wp = []
+        args = []
+        for n in WSTREAMS:
+            a = streams.get(n)
+            if a is None:
+                args += [None, 0]
+            else:
+                a = np.ascontiguousarray(a, dtype=np.float64)
+                self._wp.append(a)
+                args += [dptr(a), len(a)]
+        self.L.ref_set_wreplay(*args)
+        self.L.ref_worm_move()
+        p = (C.c_long * 10)()
+        self.L.ref_wreplay_pos(p)
+        return list(p)
+
+    def worm_state(self):
+        st = np.zeros(5, np.int32)
+        self.L.ref_worm_state(iptr(st))
+        return st
+
+    def worm_counters(self):
+        t, a = np.zeros(7), np.zeros(7)
+        self.L.ref_worm_counters(dptr(t), dptr(a))
+        return t, a
+
+    def pindex(self):
+        p, r = np.zeros(self.na, np.int32), np.zeros(self.na, np.int32)
+        self.L.ref_pindex(iptr(p), iptr(r))
+        return p, r
 
     def set_pindex(self, pindex):
         p = np.ascontiguousarray(pindex, dtype=np.int32)

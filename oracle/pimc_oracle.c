@@ -45,6 +45,14 @@ struct orc_ctx {
   double tau, rot_tau, beta;
   int *mctype;
   int *pindex;
+  int *rindex;            /* RIndex: the inverse of pindex */
+  /* worm state (TPathWorm, mc_qworm.h:32-48) and its derived constants
+   * (MCWormInit, mc_qworm.cc:49-82) */
+  int worm_on, wtype, wexists, ira, masha, atom_i, atom_m, wm;
+  double wc, qw_norm, wcut2;
+  double *dr2_list, *ptable;
+  int *atm_list;
+  double qwtot[7], qwacc[7];
   double *coords, *cosine, *angles, *newc;  /* [3][na*P] */
   int *pflags, *atom_list;
   /* 1D spline */
@@ -160,12 +168,13 @@ orc_ctx *orc_create(const pimc_system *sys, const pimc_tables *tab, int *status)
   size_t nb = (size_t)c->na * (size_t)c->P;
   c->mctype = (int *)malloc(sizeof(int) * (size_t)c->na);
   c->pindex = (int *)malloc(sizeof(int) * (size_t)c->na);
+  c->rindex = (int *)malloc(sizeof(int) * (size_t)c->na);
   c->pflags = (int *)malloc(sizeof(int) * (size_t)c->na);
   c->atom_list = (int *)malloc(sizeof(int) * (size_t)c->na);
   int g = 0;
   for (int t = 0; t < sys->ntypes; t++)
     for (int a = 0; a < sys->type[t].numb; a++) c->mctype[g++] = t;   /* mc_setup.cc:327-333 */
-  for (int a = 0; a < c->na; a++) c->pindex[a] = a;
+  for (int a = 0; a < c->na; a++) c->pindex[a] = c->rindex[a] = a;
   c->coords = (double *)calloc(3 * nb, sizeof(double));
   c->cosine = (double *)calloc(3 * nb, sizeof(double));
   c->angles = (double *)calloc(3 * nb, sizeof(double));
@@ -252,7 +261,8 @@ orc_ctx *orc_create(const pimc_system *sys, const pimc_tables *tab, int *status)
 void orc_destroy(orc_ctx *c)
 {
   if (!c) return;
-  free(c->mctype); free(c->pindex); free(c->pflags); free(c->atom_list);
+  free(c->mctype); free(c->pindex); free(c->rindex); free(c->pflags); free(c->atom_list);
+  free(c->dr2_list); free(c->ptable); free(c->atm_list);
   free(c->coords); free(c->cosine); free(c->angles); free(c->newc);
   free(c->g1d); free(c->p1d); free(c->y2_1d);
   free(c->rg2d); free(c->cg2d); free(c->pot2d);
@@ -281,7 +291,10 @@ int orc_set_state(orc_ctx *c, const double *coords, const double *angles, const 
       c->cosine[2 * nb + i] = cost;
     }
   }
-  if (pindex) memcpy(c->pindex, pindex, sizeof(int) * (size_t)c->na);
+  if (pindex) {
+    memcpy(c->pindex, pindex, sizeof(int) * (size_t)c->na);
+    for (int a = 0; a < c->na; a++) c->rindex[c->pindex[a]] = a;
+  }
   return PIMC_OK;
 }
 
@@ -721,9 +734,35 @@ static void euler_at(const orc_ctx *c, const double *ang, long nb, long tm, doub
   (void)c;
 }
 
+/* WorldLine -- mc_qworm.cc:553-575: whether bead pt of the worm type's atom
+ * (index within the type) lies on a world line, not in the gap between
+ * masha and ira */
+static int world_line(const orc_ctx *c, int atom, int pt)
+{
+  int wline = 1;
+  if (atom == c->atom_m || atom == c->atom_i) {
+    if (c->atom_i != c->atom_m || c->ira > c->masha) {
+      if ((atom == c->atom_m && pt < c->masha) || (atom == c->atom_i && pt > c->ira)) wline = 0;
+    } else {
+      if (pt > c->ira && pt < c->masha) wline = 0;
+    }
+  }
+  return wline;
+}
+
+/* the partner test of PotEnergy / PotRotEnergy / PotRotE3D with an open
+ * worm (mc_piqmc.cc:1226-1227, 1816-1817, 2000-2001, 2082-2083) */
+static int partner_on_line(const orc_ctx *c, int atom1, int it)
+{
+  int type1 = c->mctype[atom1];
+  if (c->worm_on && c->wexists && c->wtype == type1) return world_line(c, atom1 - c->offset[type1] / c->P, it);
+  return 1;
+}
+
 /* one (atom0, atom1, it) term of PotEnergy -- mc_piqmc.cc:1824-1958 */
 static double pair_term(const orc_ctx *c, int atom0, int atom1, const double *pos, int it)
 {
+  if (!partner_on_line(c, atom1, it)) return 0.0;
   const pimc_system *s = &c->sys;
   long nb = (long)c->na * c->P;
   int P = c->P, R = c->R;
@@ -807,7 +846,7 @@ double orc_pot_rot_energy(const orc_ctx *c, int atom0, const double *cosine, int
   long offset0 = (long)atom0 * c->P;
   double spot = 0.0;
   for (int atom1 = 0; atom1 < c->na; atom1++)
-    if (atom1 != atom0) {
+    if (atom1 != atom0 && partner_on_line(c, atom1, it)) {
       long offset1 = (long)atom1 * c->P;
       long t0 = offset0 + it, t1 = offset1 + it;
       double dr[3], dr2 = 0.0;
@@ -836,7 +875,7 @@ double orc_pot_rot_e3d(const orc_ctx *c, int atom0, const double eul[3], int it)
   long offset0 = (long)atom0 * c->P;
   double spot = 0.0;
   for (int atom1 = 0; atom1 < c->na; atom1++)
-    if (atom1 != atom0) {
+    if (atom1 != atom0 && partner_on_line(c, atom1, it)) {
       long offset1 = (long)atom1 * c->P;
       int type1 = c->mctype[atom1];
       long t0 = offset0 + it, t1 = offset1 + it;
@@ -1736,6 +1775,354 @@ void orc_rcf(const orc_ctx *c, double *rcf)
       rcf[itc] += p0;
     }
   }
+}
+
+/* ------------------------------------------------------------------ worm */
+
+/* MCWormInit -- mc_qworm.cc:49-82 */
+int orc_worm_init(orc_ctx *c, int type, double wc, int m, double density)
+{
+  if (type < 0 || type >= c->sys.ntypes || m < 1 || m >= c->P) return PIMC_ERR_BAD_ARG;
+  int numb = c->sys.type[type].numb;
+  c->worm_on = 1;
+  c->wtype = type;
+  c->wexists = 0;
+  c->ira = c->masha = c->atom_i = c->atom_m = 0;
+  c->wm = m;
+  c->wc = wc * (density / (double)(numb * c->P * m));
+  c->qw_norm = c->wc * numb * c->P * m;
+  double twave2 = 4.0 * c->sys.type[type].lambda * c->tau;      /* mc_setup.cc:394 */
+  (void)twave2;
+  double termal2 = (double)m * 4.0 * c->sys.type[type].lambda * c->tau;
+  c->wcut2 = 100.0 * 100.0 * termal2;
+  free(c->dr2_list); free(c->ptable); free(c->atm_list);
+  c->dr2_list = (double *)calloc((size_t)numb + 1, sizeof(double));
+  c->ptable = (double *)calloc((size_t)numb + 1, sizeof(double));
+  c->atm_list = (int *)calloc((size_t)numb + 1, sizeof(int));
+  for (int k = 0; k < 7; k++) c->qwtot[k] = c->qwacc[k] = 0.0;
+  return PIMC_OK;
+}
+
+void orc_worm_state(const orc_ctx *c, int *st)
+{
+  st[0] = c->wexists; st[1] = c->ira; st[2] = c->masha; st[3] = c->atom_i; st[4] = c->atom_m;
+}
+
+void orc_worm_set_state(orc_ctx *c, const int *st)
+{
+  c->wexists = st[0]; c->ira = st[1]; c->masha = st[2]; c->atom_i = st[3]; c->atom_m = st[4];
+}
+
+void orc_worm_counters(const orc_ctx *c, double *total, double *accep)
+{
+  for (int k = 0; k < 7; k++) { total[k] = c->qwtot[k]; accep[k] = c->qwacc[k]; }
+}
+
+static double twave2_of(const orc_ctx *c) { return 4.0 * c->sys.type[c->wtype].lambda * c->tau; }
+
+/* get_potential -- mc_qworm.cc:402-422 */
+static double worm_potential(const orc_ctx *c, int it0, int it1, int atom0, int atom1, const double *coords)
+{
+  int aoff = c->offset[c->wtype] / c->P;
+  int pit0 = it0 % c->P;
+  double pot = 0.0;
+  int atom = atom0;
+  for (int it = it0 + 1; it < it1; it++) {
+    int pit = it % c->P;
+    if (pit != it && pit0 == it0) atom = atom1;
+    pot += orc_pot_energy_slice(c, aoff + atom, coords, pit);
+  }
+  return pot;
+}
+
+/* qw_open_prob -- mc_qworm.cc:127-153 */
+static double qw_open_prob(orc_ctx *c, int segm)
+{
+  long nb = (long)c->na * c->P;
+  long offset = c->offset[c->wtype];
+  double kin = 0.0;
+  long pt0 = offset + (long)c->atom_i * c->P + c->ira;
+  long pt1 = offset + (long)c->atom_m * c->P + c->masha;
+  for (int id = 0; id < NDIM; id++) {
+    double dr = c->coords[id * nb + pt0] - c->coords[id * nb + pt1];
+    if (c->sys.minimage) dr -= (c->sys.box[id] * rint(dr / c->sys.box[id]));
+    kin += (dr * dr);
+  }
+  kin /= (twave2_of(c) * (double)segm);
+  double pot = worm_potential(c, c->ira, c->ira + segm, c->atom_i, c->atom_m, c->coords);
+  pot *= c->tau;
+  return (c->qw_norm * pow((double)segm, 0.5 * (double)NDIM) * exp(kin + pot));
+}
+
+/* sample_middle -- mc_qworm.cc:238-283 */
+static void sample_middle(orc_ctx *c, int it0, int it2, int atom0, int atom2, double *coords, orc_wreplay *rp)
+{
+  if ((it2 - it0) < 2) return;
+  long nb = (long)c->na * c->P;
+  int P = c->P;
+  int it1 = (int)rint(0.5 * (double)(it0 + it2));
+  int pt0 = it0 % P, pt1 = it1 % P, pt2 = it2 % P;
+  int atom1 = atom0;
+  if ((pt1 != it1) && (pt0 == it0)) atom1 = atom2;
+  long offset = c->offset[c->wtype];
+  long q0 = pt0 + offset + (long)atom0 * P, q1 = pt1 + offset + (long)atom1 * P, q2 = pt2 + offset + (long)atom2 * P;
+  double s0 = (double)(it1 - it0), s2 = (double)(it2 - it1);
+  double gkin = (s0 + s2) / (twave2_of(c) * s0 * s2);
+  for (int id = 0; id < NDIM; id++) {
+    coords[id * nb + q1] = (s2 * coords[id * nb + q0] + s0 * coords[id * nb + q2]) / (s0 + s2);
+    coords[id * nb + q1] += take(&rp->gauss, &rp->overrun) / sqrt(gkin);     /* gauss(gkin), mc_randg.cc:149 */
+  }
+  sample_middle(c, it0, it1, atom0, atom1, coords, rp);
+  sample_middle(c, it1, it2, atom1, atom2, coords, rp);
+}
+
+static int nrnd(orc_stream *s, int n, int *overrun) { return (int)floor(n * take(s, overrun)); }
+
+/* qworm_open -- mc_qworm.cc:155-180 */
+static void qworm_open(orc_ctx *c, orc_wreplay *rp)
+{
+  c->qwtot[0] += 1.0;
+  int numb = c->sys.type[c->wtype].numb;
+  c->atom_i = nrnd(&rp->n1, numb, &rp->overrun);
+  c->ira = nrnd(&rp->n2, c->P, &rp->overrun);
+  int segm = nrnd(&rp->n3, c->wm, &rp->overrun) + 1;
+  c->masha = (c->ira + segm) % c->P;
+  c->atom_m = c->atom_i;
+  if (c->masha != (c->ira + segm)) c->atom_m = c->pindex[c->atom_i];
+  double prob = qw_open_prob(c, segm);
+  int acc = 0;
+  if (prob >= 1.0) acc = 1;
+  else if (prob > take(&rp->u1, &rp->overrun)) acc = 1;
+  if (acc) {
+    c->wexists = 1;
+    c->qwacc[0] += 1.0;
+  }
+}
+
+/* qworm_close -- mc_qworm.cc:182-236 */
+static void qworm_close(orc_ctx *c, orc_wreplay *rp)
+{
+  c->qwtot[1] += 1.0;
+  int segm = c->masha - c->ira;
+  if (segm < 0) segm += c->P;
+  if (segm > c->wm) return;
+  int it0 = c->ira, it2 = c->ira + segm;
+  sample_middle(c, it0, it2, c->atom_i, c->atom_m, c->coords, rp);
+  double prob = 1.0 / qw_open_prob(c, segm);
+  int acc = 0;
+  if (prob >= 1.0) acc = 1;
+  else if (prob > take(&rp->u1, &rp->overrun)) acc = 1;
+  if (acc) {
+    c->wexists = 0;
+    c->qwacc[1] += 1.0;
+  }
+}
+
+/* qworm_advance -- mc_qworm.cc:295-355 */
+static void qworm_advance(orc_ctx *c, orc_wreplay *rp)
+{
+  c->qwtot[4] += 1.0;
+  long nb = (long)c->na * c->P;
+  int P = c->P;
+  int segm = c->masha - c->ira;
+  if (segm < 0) segm += P;
+  int advance = nrnd(&rp->n3, c->wm, &rp->overrun) + 1;
+  if (segm - advance <= 0) return;
+  long offset = c->offset[c->wtype];
+  int it0 = c->ira, it2 = c->ira + advance;
+  int ira_new = it2 % P, atom_i_new = c->atom_i;
+  if (ira_new != it2) atom_i_new = c->atom_m;
+  double gvar = 1.0 / ((double)advance * twave2_of(c));
+  long pt0 = offset + (long)c->atom_i * P + it0 % P;
+  long pt2 = offset + (long)atom_i_new * P + it2 % P;
+  for (int id = 0; id < NDIM; id++)
+    c->coords[id * nb + pt2] = c->coords[id * nb + pt0] + take(&rp->gauss, &rp->overrun) / sqrt(gvar);
+  sample_middle(c, it0, it2, c->atom_i, atom_i_new, c->coords, rp);
+  double pot = worm_potential(c, it0, it2 + 1, c->atom_i, atom_i_new, c->coords);
+  int acc = 0;
+  if (pot < 0.0) acc = 1;
+  else if (exp(-pot * c->tau) > take(&rp->u2, &rp->overrun)) acc = 1;
+  if (acc) {
+    c->qwacc[4] += 1.0;
+    c->ira = ira_new;
+    c->atom_i = atom_i_new;
+  }
+}
+
+/* qworm_recede -- mc_qworm.cc:357-400 */
+static void qworm_recede(orc_ctx *c, orc_wreplay *rp)
+{
+  c->qwtot[5] += 1.0;
+  int segm = c->ira - c->masha;
+  if (segm < 0) segm += c->P;
+  int recede = nrnd(&rp->n3, c->wm, &rp->overrun) + 1;
+  if ((segm - recede) < 1) return;
+  int it0 = c->ira - recede, it1 = c->ira;
+  int atom0 = c->atom_i, atom1 = c->atom_i;
+  if (it0 < 0) {
+    it0 += c->P;
+    it1 += c->P;
+    atom0 = c->rindex[atom1];
+  }
+  double pot = worm_potential(c, it0, it1 + 1, atom0, atom1, c->coords);
+  int acc = 0;
+  if (pot > 0.0) acc = 1;
+  else if (exp(pot * c->tau) > take(&rp->u2, &rp->overrun)) acc = 1;
+  if (acc) {
+    c->ira = it0 % c->P;
+    c->atom_i = atom0;
+    c->qwacc[5] += 1.0;
+  }
+}
+
+/* get_ptable -- mc_qworm.cc:577-642 (mmsort: mc_utils.cc:206-230) */
+static int get_ptable(orc_ctx *c, int atomw, int pt0, int pt1, int segm, int t1)
+{
+  long nb = (long)c->na * c->P;
+  int P = c->P, numb = c->sys.type[c->wtype].numb;
+  long offset = c->offset[c->wtype];
+  long itw = offset + (long)atomw * P + pt0;
+  int count = 0;
+  for (int atom1 = 0; atom1 < numb; atom1++)
+    if (world_line(c, atom1, pt1)) {
+      int atom0 = atom1;
+      if (t1 != pt1) atom0 = c->rindex[atom1];
+      if (atom0 != c->atom_i) {
+        long it1 = offset + (long)atom1 * P + pt1;
+        double dr2 = 0.0;
+        for (int id = 0; id < NDIM; id++) {
+          double dx = c->coords[id * nb + itw] - c->coords[id * nb + it1];
+          if (c->sys.minimage) dx -= (c->sys.box[id] * rint(dx / c->sys.box[id]));
+          dr2 += (dx * dx);
+        }
+        if (dr2 < c->wcut2) {
+          count++;
+          c->dr2_list[count] = dr2;
+          c->atm_list[count] = atom1;
+        }
+      }
+    }
+  for (int j = 2; j <= count; j++) {
+    double dtmp = c->dr2_list[j];
+    int itmp = c->atm_list[j];
+    int i = j - 1;
+    while ((i > 0) && (c->dr2_list[i] > dtmp)) {
+      c->dr2_list[i + 1] = c->dr2_list[i];
+      c->atm_list[i + 1] = c->atm_list[i];
+      i--;
+    }
+    c->dr2_list[i + 1] = dtmp;
+    c->atm_list[i + 1] = itmp;
+  }
+  if (count > 100) count = 100;     /* MAXNEIGHBORS, mc_qworm.cc:12 */
+  double norm = 1.0 / ((double)segm * twave2_of(c));
+  for (int ic = 1; ic <= count; ic++) c->ptable[ic] = exp(-norm * c->dr2_list[ic]);
+  return count;
+}
+
+/* atom2swap -- mc_qworm.cc:644-667 */
+static int atom2swap(orc_ctx *c, int count, double *pnorm, orc_wreplay *rp)
+{
+  *pnorm = 0.0;
+  for (int ic = 1; ic <= count; ic++) *pnorm += c->ptable[ic];
+  double prand = *pnorm * take(&rp->u3, &rp->overrun);
+  double sum = 0.0;
+  int ic = 1;
+  while ((ic <= count) && (sum < prand)) {
+    sum += c->ptable[ic];
+    ic++;
+  }
+  ic--;
+  return c->atm_list[ic];
+}
+
+/* qworm_swap -- mc_qworm.cc:424-551 */
+static void qworm_swap(orc_ctx *c, orc_wreplay *rp)
+{
+  c->qwtot[6] += 1.0;
+  long nb = (long)c->na * c->P;
+  int P = c->P;
+  int segm = c->wm;
+  int it0 = c->ira, it1 = it0 + segm;
+  int pit0 = it0, pit1 = it1 % P;
+  int atomw = c->atom_i;
+  int count = get_ptable(c, atomw, pit0, pit1, segm, it1);
+  if (count <= 0) return;
+  double pnorm_old, pnorm_new;
+  int atom1 = atom2swap(c, count, &pnorm_old, rp);
+  if (atom1 < 0) return;
+  int atom0 = atom1;
+  if (pit1 != it1) atom0 = c->rindex[atom1];
+  long offset0 = c->offset[c->wtype] + (long)atom0 * P;
+  long offset1 = c->offset[c->wtype] + (long)atom1 * P;
+  long offsetw = c->offset[c->wtype] + (long)atomw * P;
+  for (int id = 0; id < NDIM; id++) {
+    c->newc[id * nb + offset0 + pit0] = c->coords[id * nb + offsetw + pit0];
+    c->newc[id * nb + offset1 + pit1] = c->coords[id * nb + offset1 + pit1];
+  }
+  sample_middle(c, it0, it1, atom0, atom1, c->newc, rp);
+  int gatom0 = (int)(offset0 / P), gatom1 = (int)(offset1 / P);
+  double pot = 0.0;
+  int gatom = gatom0;
+  for (int it = it0 + 1; it < it1; it++) {
+    int pit = it % P;
+    if (pit != it) gatom = gatom1;
+    pot += orc_pot_energy_slice(c, gatom, c->newc, pit);
+    pot -= orc_pot_energy_slice(c, gatom, c->coords, pit);
+  }
+  double prob = exp(-pot * c->tau);
+  count = get_ptable(c, atom0, pit0, pit1, segm, it1);
+  pnorm_new = 0.0;
+  for (int ic = 1; ic <= count; ic++) pnorm_new += c->ptable[ic];
+  prob *= (pnorm_old / pnorm_new);
+  int acc = 0;
+  if (prob >= 1.0) acc = 1;
+  else if (prob > take(&rp->u4, &rp->overrun)) acc = 1;
+  if (acc) {
+    c->qwacc[6] += 1.0;
+    for (int id = 0; id < NDIM; id++) {
+      long offset = offset0;
+      for (int it = it0 + 1; it < it1; it++) {
+        int pit = it % P;
+        if (pit != it) offset = offset1;
+        c->coords[id * nb + offset + pit] = c->newc[id * nb + offset + pit];
+      }
+    }
+    for (int id = 0; id < NDIM; id++)
+      for (int it = 0; it <= it0; it++) {
+        c->newc[id * nb + offset0 + it] = c->coords[id * nb + offset0 + it];
+        c->coords[id * nb + offset0 + it] = c->coords[id * nb + offsetw + it];
+        c->coords[id * nb + offsetw + it] = c->newc[id * nb + offset0 + it];
+      }
+    int ratomw = c->rindex[atomw], ratom0 = c->rindex[atom0];
+    c->pindex[ratomw] = atom0;
+    c->rindex[atom0] = ratomw;
+    c->pindex[ratom0] = atomw;
+    c->rindex[atomw] = ratom0;
+    if (c->ira > c->masha) {
+      if (atom0 == c->atom_m) c->atom_m = c->atom_i;
+      else if (c->atom_i == c->atom_m) c->atom_m = atom0;
+    }
+  }
+}
+
+/* MCWormMove -- mc_qworm.cc:93-125: one try per atom of the worm type */
+int orc_worm_move(orc_ctx *c, orc_wreplay *rp)
+{
+  if (!c->worm_on) return PIMC_ERR_STATE;
+  int numb = c->sys.type[c->wtype].numb;
+  int bose = c->sys.type[c->wtype].stat == PIMC_BOSE;
+  for (int atom = 0; atom < numb; atom++) {
+    if (c->wexists) qworm_close(c, rp);
+    else qworm_open(c, rp);
+    if (c->wexists) {
+      double r = take(&rp->u5, &rp->overrun);
+      if (r > 0.5) qworm_advance(c, rp);
+      else qworm_recede(c, rp);
+    }
+    if (bose && c->wexists) qworm_swap(c, rp);
+  }
+  return rp->overrun ? PIMC_ERR_BAD_ARG : PIMC_OK;
 }
 
 /* -------------------------------------------------------- timed schedule */

@@ -48,6 +48,13 @@ typedef struct {
   int overrun;
 } orc_replay;
 
+/* worm-move replay streams: nrnd1..nrnd3 (mc_randg.cc:159-171), rnd1..rnd5
+ * and the x1 values of gauss(), each consumed where mc_qworm.cc draws it */
+typedef struct {
+  orc_stream n1, n2, n3, u1, u2, u3, u4, u5, gauss;
+  int overrun;
+} orc_wreplay;
+
 /* life cycle */
 orc_ctx *orc_create(const pimc_system *sys, const pimc_tables *tab, int *status);
 void     orc_destroy(orc_ctx *c);
@@ -116,6 +123,15 @@ double orc_pot_energy_densities(const orc_ctx *c, double *gr1d, double *gr2d, do
 void   orc_exchange_lengths(const orc_ctx *c, double *ploops);           /* ploops[numb of the boson type] += */
 int    orc_area_estimators(const orc_ctx *c, double *out);               /* out[6]  */
 int    orc_area_estim3d(const orc_ctx *c, int iframe, const double *mass, double *out);   /* out[18] */
+
+/* worm algorithm (mc_qworm.cc): MCWormInit with the WORM line's c and m and
+ * the input density; one MCWormMove call; the worm state {exists, ira,
+ * masha, atom_i, atom_m} and the QWTotal/QWAccep counters [QWMAXMOVES=7] */
+int  orc_worm_init(orc_ctx *c, int type, double wc, int m, double density);
+int  orc_worm_move(orc_ctx *c, orc_wreplay *rp);
+void orc_worm_state(const orc_ctx *c, int *st);
+void orc_worm_set_state(orc_ctx *c, const int *st);
+void orc_worm_counters(const orc_ctx *c, double *total, double *accep);
 
 /* propagator-table generators (orc_tables.c): linear_prop/linden.f and
  * nmv_prop/asymrho.f restated */

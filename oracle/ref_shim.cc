@@ -36,6 +36,7 @@ extern "C" {
 // ------------------------------------------------------------ replay RNG
 struct ReplayStream { const double *v = nullptr; long n = 0, pos = 0; };
 static ReplayStream g_u[8];       // 1..7 = rnd1..rnd7
+static ReplayStream g_n[5];       // 1..4 = nrnd1..nrnd4
 static ReplayStream g_gauss;      // x1 values of gauss()
 static ReplayStream g_runif;      // runif()
 static int g_overrun = 0;
@@ -54,10 +55,10 @@ double rnd4(void) { return take(g_u[4]); }
 double rnd5(void) { return take(g_u[5]); }
 double rnd6(void) { return take(g_u[6]); }
 double rnd7(void) { return take(g_u[7]); }
-int nrnd1(int n) { return (int)floor(n * take(g_u[0])); }
-int nrnd2(int n) { return (int)floor(n * take(g_u[0])); }
-int nrnd3(int n) { return (int)floor(n * take(g_u[0])); }
-int nrnd4(int n) { return (int)floor(n * take(g_u[0])); }
+int nrnd1(int n) { return (int)floor(n * take(g_n[1])); }   // mc_randg.cc:159-178, own streams
+int nrnd2(int n) { return (int)floor(n * take(g_n[2])); }
+int nrnd3(int n) { return (int)floor(n * take(g_n[3])); }
+int nrnd4(int n) { return (int)floor(n * take(g_n[4])); }
 double gauss(double alpha) { double x1 = take(g_gauss); return (x1 / sqrt(alpha)); }   // mc_randg.cc:149
 void RandomInit(int, int) {}
 void RandomFree(void) {}
@@ -170,6 +171,7 @@ int ref_setup(const char *workdir)
   if (ROTATION && MCAtom[IMTYPE].molecule == 1 && RotDenType == 0) init_rotdens(IMTYPE);   // InitRotDensity
   if (BOSONS) InitMCEstims();
   ResetMCCounts();
+  ResetQWCounts();                        // mc_main.cc resets them per block (MCResetBlockAverage)
   return 0;
 }
 
@@ -246,6 +248,24 @@ void ref_set_replay(const double *u1, long n1, const double *u2, long n2, const 
   g_overrun = 0;
 }
 
+// worm-move streams: nrnd1..3, rnd1..5, gauss (the other streams are left as set)
+void ref_set_wreplay(const double *n1, long nn1, const double *n2, long nn2, const double *n3, long nn3,
+                     const double *u1, long m1, const double *u2, long m2, const double *u3, long m3,
+                     const double *u4, long m4, const double *u5, long m5, const double *g, long ng)
+{
+  g_n[1] = {n1, nn1, 0}; g_n[2] = {n2, nn2, 0}; g_n[3] = {n3, nn3, 0};
+  g_u[1] = {u1, m1, 0}; g_u[2] = {u2, m2, 0}; g_u[3] = {u3, m3, 0}; g_u[4] = {u4, m4, 0}; g_u[5] = {u5, m5, 0};
+  g_gauss = {g, ng, 0};
+  g_overrun = 0;
+}
+
+void ref_wreplay_pos(long *pos)   // n1 n2 n3 u1..u5 gauss overrun
+{
+  pos[0] = g_n[1].pos; pos[1] = g_n[2].pos; pos[2] = g_n[3].pos;
+  for (int k = 1; k <= 5; k++) pos[2 + k] = g_u[k].pos;
+  pos[8] = g_gauss.pos; pos[9] = g_overrun;
+}
+
 void ref_replay_pos(long *pos)   // consumed counts: rnd1, rnd2, rnd3, gauss, runif, overrun
 {
   pos[0] = g_u[1].pos; pos[1] = g_u[2].pos; pos[2] = g_u[3].pos; pos[3] = g_gauss.pos; pos[4] = g_runif.pos;
@@ -304,6 +324,22 @@ double ref_rot_energy(double *esq, double *ets) { double s = GetRotEnergy(); *es
 double ref_rot_e3d(double *esq, double *ets) { double s = GetRotE3D(); *esq = ErotSQ; *ets = Erot_termSQ; return s; }
 
 double ref_mass(int type) { return MCAtom[type].mass; }
+
+// the worm algorithm (mc_qworm.cc); MCWormInit ran in ref_setup from the WORM line
+void ref_worm_move(void) { MCWormMove(); }
+void ref_worm_state(int *st) { st[0] = Worm.exists; st[1] = Worm.ira; st[2] = Worm.masha; st[3] = Worm.atom_i; st[4] = Worm.atom_m; }
+void ref_worm_set_state(const int *st)
+{
+  Worm.exists = st[0]; Worm.ira = st[1]; Worm.masha = st[2]; Worm.atom_i = st[3]; Worm.atom_m = st[4];
+}
+void ref_worm_counters(double *total, double *accep)
+{
+  for (int k = 0; k < QWMAXMOVES; k++) { total[k] = QWTotal[0][k]; accep[k] = QWAccep[0][k]; }
+}
+void ref_pindex(int *p, int *r)
+{
+  for (int a = 0; a < NumbAtoms; a++) { p[a] = PIndex[a]; if (r) r[a] = RIndex[a]; }
+}
 void ref_set_pindex(const int *pindex)
 {
   for (int a = 0; a < NumbAtoms; a++) { PIndex[a] = pindex[a]; RIndex[pindex[a]] = a; }

@@ -10,6 +10,9 @@ random numbers, and stores inputs and outputs:
   * a sequence of MCBisectionMove, MCMolecularMove and MCRotationsMove /
     MCRotations3D calls (mc_piqmc.cc:54-1199): the final path, the accept
     counters and the number of random numbers each generator consumed;
+  * the worm branch of the pass loop on a small He-4 system (c0w): MCWormMove
+    calls (mc_qworm.cc:93-125) and, with the worm closed,
+    MCBisectionMoveExchange under the permutations the swaps build;
   * the estimators GetKinEnergy, GetPotEnergy_Densities, GetRotEnergy /
     GetRotE3D (mc_estim.cc:500-1096) of the final path;
   * with bosons, under a random permutation: the density histograms of
@@ -175,6 +178,62 @@ def generate(case, nsteps=4, seed=2024):
     return res
 
 
+WORM_CASE = dict(seed=21, nslices=32, nrotslices=8, n_he=6, r2d_step=0.05, c2d_step=0.04)
+WORM_LINE = ("He4", 2.0, 6)
+
+
+def make_worm_workload():
+    w = W.config0(**WORM_CASE)
+    w.worm = WORM_LINE
+    return w
+
+
+def generate_worm(ncalls=40, seed=77):
+    """The worm branch of the pass loop (mc_main.cc:356-379): MCWormMove, and
+    while the worm is closed an MCBisectionMoveExchange of the boson type at
+    a drawn slice (a window inside the ring), on 6 He-4 around the linear rotor, P = 32, WORM He4 2.0 6.
+    Per call: the replayed streams, the draws consumed, the worm state; at the
+    end the path, the permutation and the worm counters."""
+    w = make_worm_workload()
+    rng = np.random.default_rng(seed)
+    ref = O.Reference(w)
+    nbos = w.types[0]["numb"]
+    res = dict(case=np.array("c0w"), coords0=w.coords.copy(), angles0=w.angles.copy())
+    streams = {n: [] for n in O.WSTREAMS}
+    cons, states, seq, bis = [], [], [], dict(gauss=[], u3=[], t=[], cons=[])
+    for k in range(ncalls):
+        st = {n: rng.uniform(1e-6, 1.0 - 1e-6, 4 * nbos) for n in O.WSTREAMS if n != "gauss"}
+        st["gauss"] = rng.normal(0.0, 1.0 / np.sqrt(2.0), 3 * nbos * (3 * WORM_LINE[2] + 8))
+        for n in O.WSTREAMS:
+            streams[n].append(st[n])
+        cons.append(ref.worm_move(st)[:9])
+        states.append(ref.worm_state())
+        if not states[-1][0]:
+            # windows that do not cross the end of the ring: across it the
+            # reference evaluates the wrong atom's bead (mc_piqmc.cc:373-376)
+            t = int(rng.integers(0, w.nslices - (1 << w.types[0]["levels"])))
+            g = rng.normal(0.0, 1.0 / np.sqrt(2.0), 3 * nbos * 8)
+            u3 = rng.uniform(size=nbos * 3)
+            ref.replay(u3=u3, gauss=g)
+            ref.L.ref_bisection_move_exchange(0, t)
+            pos = ref.replay_pos()
+            bis["gauss"].append(g); bis["u3"].append(u3); bis["t"].append(t); bis["cons"].append((pos[3], pos[2]))
+            seq.append((k, len(bis["t"]) - 1))
+    c, a, co = ref.get_state()
+    p, r = ref.pindex()
+    tot, acc = ref.worm_counters()
+    for n in O.WSTREAMS:
+        res["w_" + n] = np.concatenate(streams[n])
+        res["wn_" + n] = np.array([len(x) for x in streams[n]], dtype=np.int64)
+    res.update(w_consumed=np.array(cons, dtype=np.int64), w_states=np.array(states, dtype=np.int32),
+               w_bis_after=np.array(seq, dtype=np.int32).reshape(-1, 2), w_bis_t=np.array(bis["t"], dtype=np.int32),
+               w_bis_gauss=np.concatenate(bis["gauss"]) if bis["gauss"] else np.zeros(0),
+               w_bis_u3=np.concatenate(bis["u3"]) if bis["u3"] else np.zeros(0),
+               w_bis_cons=np.array(bis["cons"], dtype=np.int64).reshape(-1, 2),
+               coords1=c, angles1=a, pindex1=p, rindex1=r, w_total=tot[[0, 1, 4, 5, 6]], w_accep=acc[[0, 1, 4, 5, 6]])
+    return res
+
+
 def main():
     if not O.ref_available():
         sys.exit("oracle/_ref/libref.so missing: run oracle/ref_build.sh first")
@@ -183,6 +242,11 @@ def main():
         path = os.path.join(HERE, case + ".npz")
         np.savez_compressed(path, **res)
         print("wrote", path, os.path.getsize(path), "bytes")
+    res = generate_worm()
+    path = os.path.join(HERE, "c0w.npz")
+    np.savez_compressed(path, **res)
+    print("wrote", path, os.path.getsize(path), "bytes", "worm states", res["w_states"][:, 0].tolist(),
+          "bisections", len(res["w_bis_t"]), "swaps accepted", res["w_accep"][4])
 
 
 if __name__ == "__main__":

@@ -1,0 +1,85 @@
+"""The worm algorithm on the GPU (pimc_worm_move: open, close, advance,
+recede, swap with WorldLine masking) and the exchange bisection under the
+permutations it builds, against the reference's own run on the same replayed
+random numbers (tests/golden/c0w.npz) and against the oracle.
+
+The potential sums run in another order than the reference's, so paths agree
+to 1e-10 relative; every decision, every stream position and the
+permutation agree exactly."""
+import numpy as np
+import pytest
+
+import oracle as O
+import pimc_gb300 as G
+from _worm import WSTREAMS, load, replay, split
+
+pytestmark = pytest.mark.gpu
+
+
+def _gpu(w, d, line):
+    s = G.Sampler(w)
+    s.set_state(d["coords0"], d["angles0"], w.pindex)
+    s.worm_init(0, line[1], line[2], w.density)
+    return s
+
+
+def test_worm_sequence_matches_reference():
+    w, d, line = load()
+    s = _gpu(w, d, line)
+
+    def bisect(t, time, g, u3):
+        rs, ds, lv, cons = s.bisection_move(t, time, g, u3, exchange=True)
+        assert rs == 0
+        return cons
+
+    cons, states, bcons = replay(d, s.worm_move, s.worm_state, bisect)
+    np.testing.assert_array_equal(cons, d["w_consumed"])
+    np.testing.assert_array_equal(states, d["w_states"])
+    np.testing.assert_array_equal(bcons, d["w_bis_cons"])
+    c, a, co, p = s.get_state()
+    np.testing.assert_allclose(c, d["coords1"], rtol=1e-10, atol=1e-10)
+    np.testing.assert_array_equal(p, d["pindex1"])
+    tot, acc = s.worm_counters()
+    np.testing.assert_array_equal(tot[[0, 1, 4, 5, 6]], d["w_total"])
+    np.testing.assert_array_equal(acc[[0, 1, 4, 5, 6]], d["w_accep"])
+    s.close()
+
+
+def test_exchange_bisection_across_the_ring_matches_oracle():
+    """Windows that cross the end of the ring join the bead rows through the
+    permutation (here the one the recorded worm run ends with, or a cycle of
+    all bosons); the GPU and the oracle evaluate each moved bead's own energy
+    (the reference's midpoint term reads another atom's row there,
+    mc_piqmc.cc:373-376)."""
+    w, d, line = load()
+    nbos = w.types[0]["numb"]
+    rng = np.random.default_rng(5)
+    perms = [np.array(d["pindex1"], dtype=np.int32)]
+    cyc = np.arange(w.natoms, dtype=np.int32)
+    cyc[:nbos] = np.roll(np.arange(nbos), 1)
+    perms.append(cyc)
+    tested = 0
+    for perm in perms:
+        if np.array_equal(perm[:nbos], np.arange(nbos)):
+            continue
+        s = G.Sampler(w)
+        s.set_state(d["coords1"], d["angles1"], perm)
+        o = O.Oracle(w)
+        o.set_state(d["coords1"], d["angles1"], perm)
+        for time in range(w.nslices - 8, w.nslices):          # every window across the ring
+            g = rng.normal(0.0, 1.0 / np.sqrt(2.0), 3 * nbos * 8)
+            u3 = rng.uniform(size=nbos * 3)
+            rs, ds, lv, cons = s.bisection_move(0, time, g, u3, exchange=True)
+            ost, ods, olv, ocons = o.bisection_move(0, time, g, u3, exchange=True)
+            assert rs == 0 and ost == 0
+            np.testing.assert_array_equal(lv, olv)
+            assert tuple(cons) == tuple(ocons)
+            scale = np.maximum(np.abs(ods), 1.0)
+            assert np.all(np.abs(ds - ods) <= 1e-9 * scale)
+            c, _, _, _ = s.get_state()
+            oc, _, _, _ = o.get_state()
+            np.testing.assert_allclose(c, oc, rtol=1e-10, atol=1e-10)
+            o.set_state(c)           # keep the two paths identical bit for bit
+            tested += 1
+        s.close()
+    assert tested >= 8
