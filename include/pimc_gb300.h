@@ -50,6 +50,12 @@ pimc_status pimc_get_state(pimc_handle *h, double *coords, double *angles, doubl
 pimc_status pimc_molecular_move(pimc_handle *h, int type, const double *u1, long n1, const double *u2, long n2,
                                 long *consumed, double *dv_out, int *acc_out);
 
+/* MCMolecularMoveExchange(type) (mc_piqmc.cc:104-192) for the boson type:
+ * every exchange cycle of the permutation moved rigidly, u1 = rnd1() draws
+ * (3 per cycle), u2 = rnd2() draws (one per tested atom whose dV >= 0). */
+pimc_status pimc_molecular_move_exchange(pimc_handle *h, int type, const double *u1, long n1, const double *u2,
+                                         long n2, long *consumed);
+
 /* MCBisectionMove(type, time) (mc_piqmc.cc:194-294) and, with exchange = 1,
  * MCBisectionMoveExchange(type, time) (mc_piqmc.cc:296-419): gauss holds the
  * x1 = sqrt(-log r1) cos(2 pi r2) values of gauss() (mc_randg.cc:138-150),

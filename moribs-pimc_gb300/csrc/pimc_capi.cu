@@ -666,6 +666,36 @@ static pimc_status put_stream(pimc_handle *h, const double *v, long n, double **
   return PIMC_OK;
 }
 
+extern "C" pimc_status pimc_molecular_move_exchange(pimc_handle *h, int type, const double *u1, long n1,
+                                                    const double *u2, long n2, long *consumed)
+{
+  pimc_status e = ready(h);
+  if (e) return e;
+  const DevSys &d = h->ctx.s;
+  if (type < 0 || type >= d.ntypes || n1 < 0 || n2 < 0 || (n1 && !u1) || (n2 && !u2)) return PIMC_ERR_BAD_ARG;
+  if (d.stat[type] != PIMC_BOSE) return PIMC_ERR_BAD_ARG;     // cycles of the boson type (mc_piqmc.cc:110-111)
+  int numb = d.numb[type];
+  for (int a = 0; a < numb; a++)
+    if (h->pindex_host[a] < 0 || h->pindex_host[a] >= numb) return PIMC_ERR_BAD_ARG;
+  size_t bytes = ((size_t)n1 + n2 + 16) * sizeof(double) + 2 * (size_t)numb * sizeof(int) + 8192;
+  void *buf;
+  if ((e = scratch(h, bytes, &buf))) return e;
+  char *cur = (char *)buf;
+  double *d1, *d2;
+  if ((e = put_stream(h, u1, n1, &d1, cur)) || (e = put_stream(h, u2, n2, &d2, cur))) return e;
+  CK(cudaMemsetAsync(h->cursors, 0, 8 * sizeof(long), h->stream));
+  ReplaySrc src{nullptr, 0, h->cursors + 0, d2, n2, h->cursors + 1, d1, n1, h->cursors + 2, h->ctx.st.err};
+  h->launches += launch_mol_exchange(h->ctx, h->frames, type, true, src, 0, h->pass, 0, cur, h->cnt, h->stream);
+  launch_invalidate_caches(h->ctx, h->stream);
+  h->launches++;
+  CK(cudaGetLastError());
+  long cz[8];
+  CK(cudaMemcpyAsync(cz, h->cursors, 8 * sizeof(long), cudaMemcpyDeviceToHost, h->stream));
+  e = check_err(h);
+  if (consumed) { consumed[0] = cz[2]; consumed[1] = cz[1]; }
+  return e;
+}
+
 extern "C" pimc_status pimc_bisection_move(pimc_handle *h, int type, int time, int exchange, const double *gauss,
                                            long ng, const double *u3, long n3, long *consumed, double *ds_out,
                                            int *lvl_out)
@@ -1071,6 +1101,12 @@ extern "C" pimc_status pimc_worm_init(pimc_handle *h, int type, double c, int m,
   for (int a = 0; a < d.na; a++) r[h->pindex_host[a]] = a;
   CK(cudaMemcpy(h->rindex, r.data(), d.na * sizeof(int), cudaMemcpyHostToDevice));
   h->worm_on = 1;
+  h->ctx.st.worm = h->worm;           // every partner sum now masks the worm's gap
+  if (h->pass_exec) {                 // a captured pass holds the old context
+    CK(cudaStreamSynchronize(h->stream));
+    cudaGraphExecDestroy(h->pass_exec);
+    h->pass_exec = nullptr;
+  }
   return PIMC_OK;
 }
 

@@ -99,6 +99,15 @@ struct DevSys {
 //   valid while no bead of those slices and no orientation at q has changed;
 //   rl_cache/rl_ok[r*Q + q]: the current link density rho(q, q+1).
 //   Both caches hold exactly the value a fresh evaluation would return.
+// TPathWorm (mc_qworm.h:32-48) with MCWormInit's constants (mc_qworm.cc:49-82)
+// and the QWTotal/QWAccep counters (mc_qworm.h:52-53) of the worm type
+struct DevWorm {
+  int exists, ira, masha, atom_i, atom_m;
+  int type, m, numb, first;
+  double qw_norm, cut2, twave2;
+  double qwtot[7], qwacc[7];
+};
+
 struct DevState {
   double *x, *y, *z;
   float4 *b4;                   // float copy of the beads (x, y, z, 0) for the FP32 path
@@ -109,6 +118,7 @@ struct DevState {
   unsigned int *err;
   double *rp_cache, *rl_cache;
   int *rp_ok, *rl_ok;
+  const DevWorm *worm;          // the worm, when the worm algorithm is on (else null)
 };
 
 struct Ctx {

@@ -21,10 +21,25 @@ __device__ __forceinline__ int atom_type(const DevSys &s, int a) { return (s.nty
 
 // one term of PotEnergy(atom0, pos, it) (mc_piqmc.cc:1824-1958): atom0 at
 // (px,py,pz), partner atom1 at its current bead, rotor frames from the cache
+// With an open worm, PotEnergy, PotRotEnergy and PotRotE3D leave out the
+// partner beads of the worm type that lie in the gap between masha and ira
+// (WorldLine, mc_qworm.cc:553-575; mc_piqmc.cc:1226-1227, 1816-1817,
+// 2000-2001, 2082-2083).
+__device__ __forceinline__ bool worm_gap(const Ctx &c, int a1, int it)
+{
+  const DevWorm *w = c.st.worm;
+  if (w == nullptr || !w->exists || atom_type(c.s, a1) != w->type) return false;
+  const int a = a1 - w->first, ai = w->atom_i, am = w->atom_m, ira = w->ira, masha = w->masha;
+  if (a != am && a != ai) return false;
+  if (ai != am || ira > masha) return (a == am && it < masha) || (a == ai && it > ira);
+  return it > ira && it < masha;
+}
+
 __device__ __forceinline__ double pair_term64(const Ctx &c, const Frame *frames, int a0, int a1, int it,
                                               double px, double py, double pz)
 {
   const DevSys &s = c.s;
+  if (worm_gap(c, a1, it)) return 0.0;
   int m0 = s.molecule[atom_type(s, a0)], m1 = s.molecule[atom_type(s, a1)];
   size_t i1 = sidx(s, it, a1);
   double qx = c.st.x[i1], qy = c.st.y[i1], qz = c.st.z[i1];
@@ -65,6 +80,7 @@ __device__ __forceinline__ float pair_term32(const Ctx &c, const Frame *frames, 
                                              float px, float py, float pz)
 {
   const DevSys &s = c.s;
+  if (worm_gap(c, a1, it)) return 0.0f;
   int m0 = s.molecule[atom_type(s, a0)], m1 = s.molecule[atom_type(s, a1)];
   size_t i1 = sidx(s, it, a1);
   const float4 q4 = c.st.b4[i1];
@@ -547,6 +563,7 @@ struct RotShared {
 __device__ __forceinline__ double rot3d_term64(const Ctx &c, const Frame *frames, const Frame &f, int g0, int a1, int it)
 {
   const DevSys &s = c.s;
+  if (worm_gap(c, a1, it)) return 0.0;
   size_t i0 = sidx(s, it, g0), i1 = sidx(s, it, a1);
   if (atom_type(s, a1) != s.imtype)
     return vcord(c.t, f, c.st.x[i0], c.st.y[i0], c.st.z[i0], c.st.x[i1], c.st.y[i1], c.st.z[i1]);
@@ -557,6 +574,7 @@ __device__ __forceinline__ double rot3d_term64(const Ctx &c, const Frame *frames
 __device__ __forceinline__ float rot3d_term32(const Ctx &c, const Frame *frames, const Frame &f, int g0, int a1, int it)
 {
   const DevSys &s = c.s;
+  if (worm_gap(c, a1, it)) return 0.0f;
   size_t i0 = sidx(s, it, g0), i1 = sidx(s, it, a1);
   if (atom_type(s, a1) != s.imtype) {
     const float4 p0 = c.st.b4[i0], p1 = c.st.b4[i1];
@@ -571,6 +589,7 @@ __device__ __forceinline__ float rot3d_term32(const Ctx &c, const Frame *frames,
 __device__ __forceinline__ double rotlin_term64(const Ctx &c, const double n[3], int g0, int a1, int it)
 {
   const DevSys &s = c.s;
+  if (worm_gap(c, a1, it)) return 0.0;
   size_t i0 = sidx(s, it, g0), i1 = sidx(s, it, a1);
   double dx = c.st.x[i0] - c.st.x[i1], dy = c.st.y[i0] - c.st.y[i1], dz = c.st.z[i0] - c.st.z[i1];
   double dr2 = 0.0;
@@ -590,6 +609,7 @@ __device__ __forceinline__ double rotlin_term64(const Ctx &c, const double n[3],
 __device__ __forceinline__ float rotlin_term32(const Ctx &c, const float n[3], int g0, int a1, int it)
 {
   const DevSys &s = c.s;
+  if (worm_gap(c, a1, it)) return 0.0f;
   size_t i0 = sidx(s, it, g0), i1 = sidx(s, it, a1);
   const float4 p0 = c.st.b4[i0], p1 = c.st.b4[i1];
   float dx = p0.x - p1.x, dy = p0.y - p1.y, dz = p0.z - p1.z;

@@ -39,15 +39,9 @@ int launch_est_dens(const Ctx &c, Frame *f, DensHist hs, cudaStream_t s);
 
 // ------------------------------------------------------------ worm algorithm
 #define PIMC_WORM_MAXM 64             /* the worm's m (Worm.m, mc_qworm.h:46) at most */
-// TPathWorm (mc_qworm.h:32-48) with MCWormInit's constants (mc_qworm.cc:49-82)
-// and the QWTotal/QWAccep counters (mc_qworm.h:52-53) of the worm type
-struct DevWorm {
-  int exists, ira, masha, atom_i, atom_m;
-  int type, m, numb, first;
-  double qw_norm, cut2, twave2;
-  double qwtot[7], qwacc[7];
-};
 size_t worm_scratch_bytes(int numb);
+int launch_mol_exchange(const Ctx &c, Frame *f, int type, bool replay, ReplaySrc src, uint64_t seed,
+                        const unsigned *pass, unsigned phase, void *scratch, unsigned long long *cnt, cudaStream_t s);
 void launch_worm_move(const Ctx &c, Frame *f, DevWorm *wk, int *rindex, const double *const *streams,
                       const long *lengths, long *cursors, void *scratch, int numb, cudaStream_t s);
 int est_area_ctas(const Ctx &c, int btype);

@@ -454,7 +454,123 @@ __global__ void __launch_bounds__(kThreads) k_worm_move(Ctx c, Frame *frames, De
   }
 }
 
+// MCMolecularMoveExchange (mc_piqmc.cc:104-192) for the boson type: each
+// exchange cycle of the permutation is displaced rigidly by one uniform
+// step; its atoms are tested in cycle order with their whole-path
+// potential change (new beads against the old partner beads) and the cycle
+// is kept when every atom passed.  One CTA: thread 0 walks the cycles and
+// decides, all threads sum the (slice, partner) terms of the current atom.
+// REPLAY takes rnd1()/rnd2() from the caller's streams; otherwise Philox
+// keyed by (seed, pass, phase, first atom of the cycle).
+constexpr int kMolThreads = 512;
+
+template <bool REPLAY>
+__global__ void __launch_bounds__(kMolThreads) k_mol_exchange(Ctx c, Frame *frames, int type, ReplaySrc src,
+                                                              uint64_t seed, const unsigned *pass, unsigned phase,
+                                                              int *cyc, char *flag, unsigned long long *cnt)
+{
+  __shared__ double dd[3];
+  __shared__ double wpart[2][kMolThreads / 32];
+  __shared__ int ncyc, accepted, stop;
+  const int numb = c.s.numb[type], g = c.s.first[type], P = c.s.P;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int a = tid; a < numb; a += kMolThreads) flag[a] = 0;
+  __syncthreads();
+  for (int atom = 0; atom < numb; atom++) {
+    if (tid == 0) {
+      ncyc = 0;
+      if (flag[atom] == 0) {
+        cyc[ncyc++] = atom;
+        int pa = c.st.pindex[atom];
+        while (pa != atom) {
+          cyc[ncyc++] = pa;
+          flag[pa] = 1;
+          pa = c.st.pindex[pa];
+        }
+        if (REPLAY) {
+          for (int k = 0; k < 3; k++) dd[k] = c.s.mcstep[type] * (src.disp_u(k) - 0.5);
+        } else {
+          mol_disp(c.s, type, seed, *pass, phase, atom, dd);
+        }
+      }
+      accepted = 1;
+      stop = 0;
+    }
+    __syncthreads();
+    const int n = ncyc;
+    for (int ia = 0; ia < n; ia++) {
+      const int ga = g + cyc[ia];
+      const double d0 = dd[0], d1 = dd[1], d2 = dd[2];
+      double en = 0.0, eo = 0.0;
+      // PotEnergy(gatom, pos) (mc_piqmc.cc:1201-1383): partners in order,
+      // slices strided over the threads
+      const long items = (long)c.s.na * P;
+      for (long k = tid; k < items; k += kMolThreads) {
+        int a1 = (int)(k / P), it = (int)(k % P);
+        if (a1 == ga) continue;
+        size_t i = sidx(c.s, it, ga);
+        double x = c.st.x[i], y = c.st.y[i], z = c.st.z[i];
+        eo += pair_term64(c, frames, ga, a1, it, x, y, z);
+        en += pair_term64(c, frames, ga, a1, it, x + d0, y + d1, z + d2);
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        en += __shfl_xor_sync(0xffffffffu, en, o);
+        eo += __shfl_xor_sync(0xffffffffu, eo, o);
+      }
+      if (lane == 0) { wpart[0][warp] = en; wpart[1][warp] = eo; }
+      __syncthreads();
+      if (tid == 0) {
+        double sn = 0.0, so = 0.0;
+        for (int w = 0; w < kMolThreads / 32; w++) { sn += wpart[0][w]; so += wpart[1][w]; }
+        double deltav = 0.0;
+        deltav += (sn - so);
+        bool acc = false;
+        if (deltav < 0.0) acc = true;
+        else {
+          double u;
+          if (REPLAY) u = src.accept_u(0);
+          else {
+            PhiloxSrc ps{seed, ((uint64_t)*pass << 32) | ((uint64_t)phase << 12) | (uint64_t)atom};
+            u = ps.accept_u(ia);
+          }
+          if (exp(-deltav * c.s.tau) > u) acc = true;
+        }
+        accepted = acc ? 1 : 0;
+        if (!acc) stop = 1;
+      }
+      __syncthreads();
+      if (stop) break;
+    }
+    if (n > 0) {
+      if (tid == 0) {
+        cnt[(type * 3 + 0) * 2] += 1;
+        if (accepted) cnt[(type * 3 + 0) * 2 + 1] += 1;
+      }
+      if (accepted) {
+        const double d0 = dd[0], d1 = dd[1], d2 = dd[2];
+        for (long k = tid; k < (long)n * P; k += kMolThreads) {
+          int ia = (int)(k / P), it = (int)(k % P);
+          size_t i = sidx(c.s, it, g + cyc[ia]);
+          store_bead(c, i, c.st.x[i] + d0, c.st.y[i] + d1, c.st.z[i] + d2);
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
 }  // namespace
+
+int launch_mol_exchange(const Ctx &c, Frame *f, int type, bool replay, ReplaySrc src, uint64_t seed,
+                        const unsigned *pass, unsigned phase, void *scratch, unsigned long long *cnt, cudaStream_t s)
+{
+  int numb = c.s.numb[type];
+  int *cyc = (int *)scratch;
+  char *flag = (char *)(cyc + numb);
+  if (replay) k_mol_exchange<true><<<1, kMolThreads, 0, s>>>(c, f, type, src, seed, pass, phase, cyc, flag, cnt);
+  else k_mol_exchange<false><<<1, kMolThreads, 0, s>>>(c, f, type, src, seed, pass, phase, cyc, flag, cnt);
+  return 1;
+}
 
 size_t worm_scratch_bytes(int numb) { return sizeof(double) * (3 * (PIMC_WORM_MAXM + 1) + 2 * (size_t)(numb + 1)) + sizeof(int) * (size_t)(numb + 1) + 64; }
 
@@ -469,5 +585,7 @@ void launch_worm_move(const Ctx &c, Frame *f, DevWorm *wk, int *rindex, const do
   double *dr2l = seg + 3 * (PIMC_WORM_MAXM + 1);
   double *ptab = dr2l + (numb + 1);
   int *atml = (int *)(ptab + (numb + 1));
-  k_worm_move<<<1, kThreads, 0, s>>>(c, f, wk, rindex, src, seg, dr2l, atml, ptab);
+  Ctx cw = c;
+  cw.st.worm = nullptr;      // the kernel masks from its own copy of the worm
+  k_worm_move<<<1, kThreads, 0, s>>>(cw, f, wk, rindex, src, seg, dr2l, atml, ptab);
 }

@@ -53,6 +53,7 @@ def load(path=LIBPATH):
     L.pimc_pot_rot_energy.argtypes = [vp, C.c_int, _ip, _ip, _dp, _dp]
     L.pimc_estimators.argtypes = [vp, _dp]
     L.pimc_rcf.argtypes = [vp, _dp]
+    L.pimc_molecular_move_exchange.argtypes = [vp, C.c_int, _dp, C.c_long, _dp, C.c_long, _lp]
     L.pimc_worm_init.argtypes = [vp, C.c_int, C.c_double, C.c_int, C.c_double]
     L.pimc_worm_move.argtypes = [vp, C.POINTER(_dp), C.POINTER(C.c_long), C.POINTER(C.c_long)]
     L.pimc_worm_state.argtypes = [vp, _ip]
@@ -222,6 +223,15 @@ class Sampler:
         out = np.zeros(self.w.nrotslices)
         _chk(self.L.pimc_rcf(self.h, dptr(out)), "pimc_rcf")
         return out
+
+    def molecular_move_exchange(self, type_, u1, u2):
+        """MCMolecularMoveExchange with replayed rnd1()/rnd2(); returns the draws consumed."""
+        a = np.ascontiguousarray(u1, dtype=np.float64)
+        b = np.ascontiguousarray(u2, dtype=np.float64)
+        cons = (C.c_long * 2)()
+        _chk(self.L.pimc_molecular_move_exchange(self.h, int(type_), dptr(a), len(a), dptr(b), len(b), cons),
+             "pimc_molecular_move_exchange")
+        return (cons[0], cons[1])
 
     # worm algorithm (mc_qworm.cc)
     WSTREAMS = ("n1", "n2", "n3", "u1", "u2", "u3", "u4", "u5", "gauss")

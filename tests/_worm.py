@@ -23,20 +23,26 @@ def split(d, key, nkey):
     return np.split(d[key], np.cumsum(n)[:-1]) if len(n) else []
 
 
-def replay(d, worm_move, worm_state, bisect):
-    """Drive the recorded sequence; returns per-call consumed counts, states and
-    the bisection consumption."""
+def replay(d, worm_move, worm_state, bisect, molec=None):
+    """Drive the recorded sequence; returns per-call consumed counts, states,
+    the bisection consumption and (with molec) the exchange centroid
+    consumption."""
     streams = {n: split(d, "w_" + n, "wn_" + n) for n in WSTREAMS}
     bis_after = {int(k): int(j) for k, j in d["w_bis_after"]}
     nb = len(d["w_bis_t"])
     nbos = 6
     bg = np.split(d["w_bis_gauss"], nb) if nb else []
     bu = np.split(d["w_bis_u3"], nb) if nb else []
-    cons, states, bcons = [], [], []
+    m1 = np.split(d["w_mol_u1"], nb) if nb else []
+    m2 = np.split(d["w_mol_u2"], nb) if nb else []
+    cons, states, bcons, mcons = [], [], [], []
     for k in range(len(d["w_states"])):
         cons.append(worm_move({n: streams[n][k] for n in WSTREAMS}))
         states.append(worm_state())
         if k in bis_after:
             j = bis_after[k]
             bcons.append(bisect(0, int(d["w_bis_t"][j]), bg[j], bu[j]))
-    return np.array(cons), np.array(states), np.array(bcons).reshape(-1, 2)
+            if molec is not None:
+                mcons.append(molec(0, m1[j], m2[j]))
+    out = (np.array(cons), np.array(states), np.array(bcons).reshape(-1, 2))
+    return out + (np.array(mcons).reshape(-1, 2),) if molec is not None else out

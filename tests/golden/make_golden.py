@@ -12,7 +12,8 @@ random numbers, and stores inputs and outputs:
     counters and the number of random numbers each generator consumed;
   * the worm branch of the pass loop on a small He-4 system (c0w): MCWormMove
     calls (mc_qworm.cc:93-125) and, with the worm closed,
-    MCBisectionMoveExchange under the permutations the swaps build;
+    MCBisectionMoveExchange and MCMolecularMoveExchange under the
+    permutations the swaps build;
   * the estimators GetKinEnergy, GetPotEnergy_Densities, GetRotEnergy /
     GetRotE3D (mc_estim.cc:500-1096) of the final path;
   * with bosons, under a random permutation: the density histograms of
@@ -191,7 +192,7 @@ def make_worm_workload():
 def generate_worm(ncalls=40, seed=77):
     """The worm branch of the pass loop (mc_main.cc:356-379): MCWormMove, and
     while the worm is closed an MCBisectionMoveExchange of the boson type at
-    a drawn slice (a window inside the ring), on 6 He-4 around the linear rotor, P = 32, WORM He4 2.0 6.
+    a drawn slice (a window inside the ring) and an MCMolecularMoveExchange, on 6 He-4 around the linear rotor, P = 32, WORM He4 2.0 6.
     Per call: the replayed streams, the draws consumed, the worm state; at the
     end the path, the permutation and the worm counters."""
     w = make_worm_workload()
@@ -219,6 +220,14 @@ def generate_worm(ncalls=40, seed=77):
             pos = ref.replay_pos()
             bis["gauss"].append(g); bis["u3"].append(u3); bis["t"].append(t); bis["cons"].append((pos[3], pos[2]))
             seq.append((k, len(bis["t"]) - 1))
+            # MCMolecularMoveExchange (mc_main.cc:371-377), one displacement per cycle
+            u1 = rng.uniform(size=3 * nbos)
+            u2 = rng.uniform(size=nbos)
+            ref.replay(u1=u1, u2=u2)
+            ref.L.ref_molecular_move_exchange(0)
+            pos = ref.replay_pos()
+            bis.setdefault("u1", []).append(u1); bis.setdefault("u2", []).append(u2)
+            bis.setdefault("mcons", []).append((pos[0], pos[1]))
     c, a, co = ref.get_state()
     p, r = ref.pindex()
     tot, acc = ref.worm_counters()
@@ -230,6 +239,8 @@ def generate_worm(ncalls=40, seed=77):
                w_bis_gauss=np.concatenate(bis["gauss"]) if bis["gauss"] else np.zeros(0),
                w_bis_u3=np.concatenate(bis["u3"]) if bis["u3"] else np.zeros(0),
                w_bis_cons=np.array(bis["cons"], dtype=np.int64).reshape(-1, 2),
+               w_mol_u1=np.concatenate(bis["u1"]), w_mol_u2=np.concatenate(bis["u2"]),
+               w_mol_cons=np.array(bis["mcons"], dtype=np.int64).reshape(-1, 2),
                coords1=c, angles1=a, pindex1=p, rindex1=r, w_total=tot[[0, 1, 4, 5, 6]], w_accep=acc[[0, 1, 4, 5, 6]])
     return res
 

@@ -32,10 +32,11 @@ def test_worm_sequence_matches_reference():
         assert rs == 0
         return cons
 
-    cons, states, bcons = replay(d, s.worm_move, s.worm_state, bisect)
+    cons, states, bcons, mcons = replay(d, s.worm_move, s.worm_state, bisect, s.molecular_move_exchange)
     np.testing.assert_array_equal(cons, d["w_consumed"])
     np.testing.assert_array_equal(states, d["w_states"])
     np.testing.assert_array_equal(bcons, d["w_bis_cons"])
+    np.testing.assert_array_equal(mcons, d["w_mol_cons"])
     c, a, co, p = s.get_state()
     np.testing.assert_allclose(c, d["coords1"], rtol=1e-10, atol=1e-10)
     np.testing.assert_array_equal(p, d["pindex1"])
@@ -83,3 +84,31 @@ def test_exchange_bisection_across_the_ring_matches_oracle():
             tested += 1
         s.close()
     assert tested >= 8
+
+
+def test_exchange_centroid_cycles_match_oracle():
+    """MCMolecularMoveExchange with cycles of two and three atoms: the GPU
+    against the oracle (which equals the reference bit for bit, see
+    tests/test_oracle_worm.py)."""
+    w, d, line = load()
+    perm = np.arange(w.natoms, dtype=np.int32)
+    perm[:6] = [1, 2, 0, 4, 3, 5]
+    rng = np.random.default_rng(11)
+    s = G.Sampler(w)
+    s.set_state(d["coords1"], d["angles1"], perm)
+    o = O.Oracle(w)
+    o.set_state(d["coords1"], d["angles1"], perm)
+    for k in range(6):
+        u1 = rng.uniform(size=18)
+        u2 = rng.uniform(size=6) * (0.2 if k % 2 else 1.0)
+        cons = s.molecular_move_exchange(0, u1, u2)
+        st, dv, acc, ocons = o.molecular_move(0, u1, u2, exchange=True)
+        assert st == 0 and tuple(cons) == tuple(ocons)
+        c, _, _, _ = s.get_state()
+        oc, _, _, _ = o.get_state()
+        np.testing.assert_allclose(c, oc, rtol=1e-10, atol=1e-10)
+        o.set_state(c)
+    tot, acc = s.counters()
+    otot, oacc = o.counters()
+    assert tot[0] == otot[0] and acc[0] == oacc[0] and acc[0] > 0
+    s.close()
