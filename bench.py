@@ -53,6 +53,7 @@ def parse():
     ap.add_argument("--no-batched", action="store_true", help="skip the config-2 replica-batch measurement")
     ap.add_argument("--batched-replicas", type=int, default=4096)
     ap.add_argument("--no-tables", action="store_true", help="skip the propagator-table generator measurement")
+    ap.add_argument("--no-worm", action="store_true", help="skip the worm-algorithm pass measurement")
     return ap.parse_args()
 
 
@@ -449,6 +450,56 @@ def run_tables(local, cpu):
     return out
 
 
+def run_worm(local, cpu, steps=5, warmup=2):
+    """The worm branch of the pass loop (mc_main.cc:348-381) on config 0
+    (CO2-like rotor + 8 He-4, P = 512, Q = 128) with WORM He4 1.0 16: per
+    time slice the worm tries, the closed-path exchange bisection and
+    centroid move, the rotor's bisection and rotational sweep.  GPU passes
+    timed with CUDA events on the library's stream; the CPU figure is the
+    oracle's port of the same loop on a 64-slice sample, scaled to a pass."""
+    import torch
+    import pimc_gb300 as G
+    import workloads as W
+    w = W.config0()
+    w.worm = ("He4", 1.0, 16)
+    s = G.Sampler(w, device=local)
+    s.worm_init(0, 1.0, 16, w.density)
+    s.worm_run(warmup, 31)
+    s.synchronize()
+    ext = torch.cuda.ExternalStream(s.stream(), device=torch.device("cuda", local))
+    l0 = s.launch_count()
+    with torch.cuda.stream(ext):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        s.worm_run(steps, 32)
+        e1.record(ext)
+    s.synchronize()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    tot, acc = s.worm_counters()
+    out = {"workload": "config0 + WORM He4 1.0 16: 1 CO2-like rotor + 8 He-4, P=512, Q=128",
+           "gpu_ms_per_pass": round(ms, 3), "slices_per_s": round(w.nslices / (ms / 1e3), 1),
+           "launches_per_pass": int((s.launch_count() - l0) / steps),
+           "worm_accept": {"open": acc[0] / max(1, tot[0]), "close": acc[1] / max(1, tot[1]),
+                           "advance": acc[4] / max(1, tot[4]), "recede": acc[5] / max(1, tot[5]),
+                           "swap": acc[6] / max(1, tot[6])}}
+    s.close()
+    if cpu:
+        import oracle as O
+        o = O.Oracle(w)
+        o.worm_init(0, 1.0, 16, w.density)
+        nth = os.cpu_count() or 1
+        o.worm_run(0, 8, 5, nth)
+        t0 = time.perf_counter()
+        o.worm_run(8, 64, 6, nth)
+        cs = time.perf_counter() - t0
+        out["cpu_baseline"] = {"kind": "port", "cores": nth, "sample": "64 time slices of the worm pass loop",
+                               "ms_per_pass": round(cs * w.nslices / 64 * 1e3, 1),
+                               "slices_per_s": round(64 / cs, 1)}
+    return out
+
+
 def main():
     args = parse()
     rank, local, world = dist_env()
@@ -475,6 +526,8 @@ def main():
                                     "host_cpu": host_cpu()}
         if not args.no_tables and world == 1:
             line["tables"] = run_tables(local, not args.no_cpu)
+        if not args.no_worm and world == 1:
+            line["worm"] = run_worm(local, not args.no_cpu)
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.barrier()

@@ -150,6 +150,13 @@ pimc_status pimc_worm_init(pimc_handle *h, int type, double c, int m, double den
  * taken from each.  Potential sums leave out partner beads in the worm's
  * gap as PotEnergy does (WorldLine, mc_qworm.cc:553-575).  FP64 only. */
 pimc_status pimc_worm_move(pimc_handle *h, const double *const *streams, const long *lengths, long *consumed);
+/* npasses passes of the worm branch of the pass loop (mc_main.cc:348-381)
+ * with counter-based draws keyed by (seed, pass, slice): per time slice the
+ * worm type's MCWormMove and, while the worm is closed, its exchange
+ * bisection at a drawn slice and (slice 0) its exchange-cycle centroid move,
+ * then the other types' PIMCPass (centroid at slice 0, bisection, the
+ * rotational sweep).  Partner sums leave out the worm's gap throughout. */
+pimc_status pimc_worm_run(pimc_handle *h, int npasses, uint64_t seed);
 /* the worm {exists, ira, masha, atom_i, atom_m} (TPathWorm, mc_qworm.h:32-48) */
 pimc_status pimc_worm_state(pimc_handle *h, int *state);
 pimc_status pimc_worm_set_state(pimc_handle *h, const int *state);

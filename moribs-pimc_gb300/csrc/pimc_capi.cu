@@ -57,6 +57,7 @@ struct pimc_handle {
   DevWorm *worm = nullptr;
   int *rindex = nullptr;
   long *wcur = nullptr;
+  void *wscr = nullptr;                // production worm scratch (bridge segment, neighbour table, cycles)
   int worm_on = 0;
 };
 
@@ -333,7 +334,7 @@ extern "C" pimc_status pimc_destroy(pimc_handle *h)
   void *bufs[] = {st.x, st.y, st.z, st.b4, st.cosvf, st.rp_cache, st.rl_cache, st.rp_ok, st.rl_ok,
                   st.ang, st.cosv, st.pindex, st.mctype, st.err, h->frames, h->cnt, h->pass, h->cursors, h->ms,
                   h->qbuf, h->prog, h->abort_word, h->dens.g1, h->dens.g2, h->dens.g3, h->worm, h->rindex,
-                  h->wcur};
+                  h->wcur, h->wscr};
   for (void *b : bufs)
     if (b) cudaFree(b);
   for (void *b : h->owned) cudaFree(b);
@@ -1083,6 +1084,7 @@ extern "C" pimc_status pimc_worm_init(pimc_handle *h, int type, double c, int m,
   pimc_status e;
   if (!h->worm) {
     if ((e = dalloc(h, &h->worm, 1)) || (e = dalloc(h, &h->rindex, d.na)) || (e = dalloc(h, &h->wcur, 16))) return e;
+    CK(cudaMalloc(&h->wscr, worm_scratch_bytes(d.na) + 2 * (size_t)d.na * sizeof(int) + 512));
   }
   // MCWormInit (mc_qworm.cc:49-82): Worm.c scaled by the density per bead
   // and segment, the open-move normalisation and the neighbour cut-off
@@ -1145,6 +1147,63 @@ extern "C" pimc_status pimc_worm_move(pimc_handle *h, const double *const *strea
   if (consumed)
     for (int k = 0; k < 9; k++) consumed[k] = cz[k];
   return e;
+}
+
+// The worm branch of the pass loop (mc_main.cc:348-381) with counter-based
+// draws: for every time slice, the worm type's MCWormMove and, while the worm
+// is closed, its bisection at a drawn slice (exchange for bosons) and at
+// slice 0 its exchange-cycle centroid move; the other types' PIMCPass
+// (mc_main.cc:510-522).  Uniform keys: phase 4t for the worm tries, 4t+1
+// the worm type's bisection, 4t+2 its centroid move, 4t+3 the other types.
+extern "C" pimc_status pimc_worm_run(pimc_handle *h, int npasses, uint64_t seed)
+{
+  pimc_status e = ready(h);
+  if (e) return e;
+  if (!h->worm_on) return PIMC_ERR_STATE;
+  if (npasses < 0) return PIMC_ERR_BAD_ARG;
+  const DevSys &d = h->ctx.s;
+  DevWorm w;
+  CK(cudaMemcpyAsync(&w, h->worm, sizeof(DevWorm), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  const int wt = w.type, P = d.P;
+  const int bose = d.stat[wt] == PIMC_BOSE;
+  char *mscr = (char *)h->wscr + ((worm_scratch_bytes(d.na) + 255) / 256) * 256;
+  ReplaySrc none{};
+  for (int p = 0; p < npasses; p++) {
+    launch_pass_begin(h->pass, h->stream);
+    h->launches++;
+    for (int t = 0; t < P; t++) {
+      for (int type = 0; type < d.ntypes; type++) {
+        if (d.numb[type] <= 0) continue;
+        if (type == wt) {
+          launch_worm_prod(h->ctx, h->frames, h->worm, h->rindex, seed, h->pass, 4u * t, h->wscr, d.na, h->stream);
+          launch_invalidate_caches(h->ctx, h->stream);
+          h->launches += 2;
+          h->launches += launch_bisect_slice(h->ctx, h->frames, type, 0, bose, h->worm, seed, h->pass, 4u * t + 1,
+                                             h->cnt, h->stream);
+          if (t == 0)
+            h->launches += launch_mol_exchange(h->ctx, h->frames, type, false, none, seed, h->pass, 4u * t + 2, mscr,
+                                               h->cnt, h->stream, h->worm);
+          continue;
+        }
+        if (t == 0)
+          for (int a = 0; a < d.numb[type]; a++)
+            h->launches += launch_mol(h->ctx, h->frames, type, a, false, none, seed, h->pass, 4u * t + 3, h->ms,
+                                      nullptr, nullptr, h->cnt, h->stream);
+        h->launches += launch_bisect_slice(h->ctx, h->frames, type, t, 0, nullptr, seed, h->pass, 4u * t + 3, h->cnt,
+                                           h->stream);
+        if (type == d.imtype && h->sys.rotation) {
+          h->launches += launch_rot_phase(h->ctx, h->frames, 0, 4u * t + 3, seed, h->pass, h->cnt, h->stream);
+          h->launches += launch_rot_phase(h->ctx, h->frames, 1, 4u * t + 3, seed, h->pass, h->cnt, h->stream);
+        }
+      }
+    }
+    launch_refresh_frames(h->ctx, h->frames, h->stream);
+    h->launches++;
+    CK(cudaGetLastError());
+  }
+  CK(cudaMemcpyAsync(h->pindex_host.data(), h->ctx.st.pindex, d.na * sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  return check_err(h);
 }
 
 extern "C" pimc_status pimc_worm_state(pimc_handle *h, int *state)

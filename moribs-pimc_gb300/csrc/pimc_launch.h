@@ -41,7 +41,12 @@ int launch_est_dens(const Ctx &c, Frame *f, DensHist hs, cudaStream_t s);
 #define PIMC_WORM_MAXM 64             /* the worm's m (Worm.m, mc_qworm.h:46) at most */
 size_t worm_scratch_bytes(int numb);
 int launch_mol_exchange(const Ctx &c, Frame *f, int type, bool replay, ReplaySrc src, uint64_t seed,
-                        const unsigned *pass, unsigned phase, void *scratch, unsigned long long *cnt, cudaStream_t s);
+                        const unsigned *pass, unsigned phase, void *scratch, unsigned long long *cnt, cudaStream_t s,
+                        const DevWorm *gate = nullptr);
+int launch_bisect_slice(const Ctx &c, Frame *f, int type, int time0, int exch, const DevWorm *gate, uint64_t seed,
+                        const unsigned *pass, unsigned phase, unsigned long long *cnt, cudaStream_t s);
+void launch_worm_prod(const Ctx &c, Frame *f, DevWorm *wk, int *rindex, uint64_t seed, const unsigned *pass,
+                      unsigned phase, void *scratch, int numb, cudaStream_t s);
 void launch_worm_move(const Ctx &c, Frame *f, DevWorm *wk, int *rindex, const double *const *streams,
                       const long *lengths, long *cursors, void *scratch, int numb, cudaStream_t s);
 int est_area_ctas(const Ctx &c, int btype);

@@ -28,6 +28,9 @@ struct WormShared {
   double qx[kMaxQ], qy[kMaxQ], qz[kMaxQ];    // the bead the atom sits on
   double qsum[kMaxQ];
   int stack[4 * 32];                         // sample_middle's recursion
+  long gbase;                                // first gauss() draw of the current bridge
+  int gneed;                                 // its number of draws
+  double gz[3 * (PIMC_WORM_MAXM + 1)];       // the draws, generated by all threads
 };
 
 struct WormSrc {
@@ -36,6 +39,17 @@ struct WormSrc {
   long *pos;
   unsigned *err;
   // one draw of stream k: 0..2 nrnd1..3, 3..7 rnd1..5, 8 gauss's x1
+  __device__ void init() {}
+  __device__ long gbase() const { return pos[8]; }
+  __device__ double gauss_at(long i) const
+  {
+    if (i >= n[8]) {
+      atomicOr(err, (unsigned)DERR_STREAM);
+      return 0.0;
+    }
+    return v[8][i];
+  }
+  __device__ void gskip(long k) { pos[8] += k; }
   __device__ double take(int k)
   {
     long p = pos[k];
@@ -48,7 +62,33 @@ struct WormSrc {
   }
 };
 
-__device__ __forceinline__ int nrnd(WormSrc &src, int k, int n) { return (int)floor(n * src.take(k)); }
+// the production draws: Philox keyed by (seed, pass, phase, stream k, count)
+struct WormPhilox {
+  uint64_t seed;
+  const unsigned *pass;
+  unsigned phase;
+  uint64_t move;
+  unsigned cnt[9];
+  __device__ void init()
+  {
+    move = ((uint64_t)(*pass) << 32) | ((uint64_t)phase << 12) | 0xFFFu;
+    for (int k = 0; k < 9; k++) cnt[k] = 0;
+  }
+  __device__ double draw(int k, unsigned n) const
+  {
+    double u0, u1;
+    philox_u2(seed, move, 0x500000u | ((uint32_t)k << 16) | (n & 0xFFFFu), n >> 16, &u0, &u1);
+    if (k == 8) return sqrt(-log(u0)) * cos(2.0 * PIMC_PI * u1);   // gauss()'s x1 (mc_randg.cc:144)
+    return u0;
+  }
+  __device__ double take(int k) { return draw(k, cnt[k]++); }
+  __device__ long gbase() const { return cnt[8]; }
+  __device__ double gauss_at(long i) const { return draw(8, (unsigned)i); }
+  __device__ void gskip(long k) { cnt[8] += (unsigned)k; }
+};
+
+template <class Src>
+__device__ __forceinline__ int nrnd(Src &src, int k, int n) { return (int)floor(n * src.take(k)); }
 
 // WorldLine (mc_qworm.cc:553-575) for atom index a of the worm type
 __device__ __forceinline__ bool world_line(const WormShared &sh, int a, int pt)
@@ -117,7 +157,7 @@ __device__ double potential_total(const WormShared &sh)
 // reference's recursion (middle bead, then the left half, then the right
 // half) with an explicit stack.  seg != nullptr writes the segment copy
 // seg[3][it - base] (newcoords of the swap) instead of the path.
-__device__ void sample_middle(const Ctx &c, const DevWorm &wk, WormShared &sh, WormSrc &src, int it0, int it2,
+__device__ void sample_middle(const Ctx &c, const DevWorm &wk, WormShared &sh, int &gi, int it0, int it2,
                               int atom0, int atom2, double *seg, int base)
 {
   const int P = c.s.P;
@@ -142,7 +182,7 @@ __device__ void sample_middle(const Ctx &c, const DevWorm &wk, WormShared &sh, W
     }
     for (int d = 0; d < 3; d++) {
       r1[d] = (s2 * r0[d] + s0 * r2[d]) / (s0 + s2);
-      r1[d] += src.take(8) / sqrt(gkin);                 // gauss(gkin), mc_randg.cc:149
+      r1[d] += sh.gz[gi++] / sqrt(gkin);                 // gauss(gkin), mc_randg.cc:149
     }
     if (seg) {
       for (int d = 0; d < 3; d++) seg[3 * (t1 - base) + d] = r1[d];
@@ -215,8 +255,19 @@ __device__ int get_ptable(const Ctx &c, const DevWorm &wk, const WormShared &sh,
   return count;
 }
 
+// gauss() draws gbase .. gbase+gneed-1 of the next bridge, one per thread
+// (thread 0 set gbase and gneed before the barrier)
+template <class Src>
+__device__ __forceinline__ void prefetch_gauss(const Src &src, WormShared &sh)
+{
+  __syncthreads();
+  for (int j = threadIdx.x; j < sh.gneed; j += kThreads) sh.gz[j] = src.gauss_at(sh.gbase + j);
+  __syncthreads();
+}
+
+template <class Src>
 __global__ void __launch_bounds__(kThreads) k_worm_move(Ctx c, Frame *frames, DevWorm *wkp, int *rindex,
-                                                       WormSrc src, double *seg, double *dr2l, int *atml,
+                                                       Src src, double *seg, double *dr2l, int *atml,
                                                        double *ptab)
 {
   __shared__ WormShared sh;
@@ -224,6 +275,7 @@ __global__ void __launch_bounds__(kThreads) k_worm_move(Ctx c, Frame *frames, De
   const DevWorm wk = *wkp;
   const int P = c.s.P;
   const bool t0 = threadIdx.x == 0;
+  src.init();
   if (t0) {
     sh.exists = wkp->exists; sh.ira = wkp->ira; sh.masha = wkp->masha;
     sh.atom_i = wkp->atom_i; sh.atom_m = wkp->atom_m;
@@ -234,13 +286,23 @@ __global__ void __launch_bounds__(kThreads) k_worm_move(Ctx c, Frame *frames, De
     // ---------------- open (mc_qworm.cc:155-180) / close (:182-236)
     int segm = 0;
     if (t0) {
+      sh.gneed = 0;
       if (sh.exists) {
         wkp->qwtot[1] += 1.0;
         segm = sh.masha - sh.ira;
         if (segm < 0) segm += P;
         sh.flag = segm > wk.m ? 0 : 1;
+        if (sh.flag && segm >= 2) sh.gneed = 3 * (segm - 1);
+        sh.gbase = src.gbase();
+      }
+    }
+    prefetch_gauss(src, sh);
+    if (t0) {
+      if (sh.exists) {
         if (sh.flag) {
-          sample_middle(c, wk, sh, src, sh.ira, sh.ira + segm, sh.atom_i, sh.atom_m, nullptr, 0);
+          int gi = 0;
+          src.gskip(sh.gneed);
+          sample_middle(c, wk, sh, gi, sh.ira, sh.ira + segm, sh.atom_i, sh.atom_m, nullptr, 0);
           potential_queries(c, wk, sh, sh.ira, sh.ira + segm, sh.atom_i, sh.atom_m);
         }
       } else {
@@ -275,17 +337,27 @@ __global__ void __launch_bounds__(kThreads) k_worm_move(Ctx c, Frame *frames, De
     __syncthreads();   // every thread is past the reads of sh.flag / sh.exists above
     // ---------------- advance (mc_qworm.cc:295-355) / recede (:357-400)
     if (sh.exists) {
-      int ira_new = 0, atomi_new = 0, adv = 0;
+      int ira_new = 0, atomi_new = 0, adv = 0, advance = 0;
       if (t0) {
         double r = src.take(7);
         adv = r > 0.5;
         sh.flag = 0;
+        sh.gneed = 0;
         if (adv) {
           wkp->qwtot[4] += 1.0;
           int sg = sh.masha - sh.ira;
           if (sg < 0) sg += P;
-          int advance = nrnd(src, 2, wk.m) + 1;
-          if (sg - advance > 0) {
+          advance = nrnd(src, 2, wk.m) + 1;
+          if (sg - advance > 0) sh.gneed = 3 * advance;   // the end point, then the bridge
+        }
+        sh.gbase = src.gbase();
+      }
+      prefetch_gauss(src, sh);
+      if (t0) {
+        if (adv) {
+          if (sh.gneed > 0) {
+            int gi = 0;
+            src.gskip(sh.gneed);
             int it0 = sh.ira, it2 = sh.ira + advance;
             ira_new = it2 % P;
             atomi_new = sh.atom_i;
@@ -293,9 +365,9 @@ __global__ void __launch_bounds__(kThreads) k_worm_move(Ctx c, Frame *frames, De
             double gvar = 1.0 / ((double)advance * wk.twave2);
             size_t i0 = bead(c, wk.first + sh.atom_i, it0 % P);
             double r0[3] = {c.st.x[i0], c.st.y[i0], c.st.z[i0]}, r2[3];
-            for (int d = 0; d < 3; d++) r2[d] = r0[d] + src.take(8) / sqrt(gvar);
+            for (int d = 0; d < 3; d++) r2[d] = r0[d] + sh.gz[gi++] / sqrt(gvar);
             store_bead(c, bead(c, wk.first + atomi_new, it2 % P), r2[0], r2[1], r2[2]);
-            sample_middle(c, wk, sh, src, it0, it2, sh.atom_i, atomi_new, nullptr, 0);
+            sample_middle(c, wk, sh, gi, it0, it2, sh.atom_i, atomi_new, nullptr, 0);
             potential_queries(c, wk, sh, it0, it2 + 1, sh.atom_i, atomi_new);
             sh.flag = 1;
           }
@@ -370,11 +442,25 @@ __global__ void __launch_bounds__(kThreads) k_worm_move(Ctx c, Frame *frames, De
           pnorm_old = pn;
           a0 = a1;
           if (pit1 != it1) a0 = rindex[a1];
+          sh.flag = 1;
+          sh.stack[0] = it0; sh.stack[1] = it1; sh.stack[2] = atomw; sh.stack[3] = a0; sh.stack[4] = a1;
+        }
+        sh.gneed = sh.flag && wk.m >= 2 ? 3 * (wk.m - 1) : 0;
+        sh.gbase = src.gbase();
+      }
+      prefetch_gauss(src, sh);
+      if (t0 && sh.flag) {
+        const int sg = wk.m;
+        it0 = sh.stack[0]; it1 = sh.stack[1]; atomw = sh.stack[2]; a0 = sh.stack[3]; a1 = sh.stack[4];
+        pit1 = it1 % P;
+        {
+          int gi = 0;
+          src.gskip(sh.gneed);
           // newcoords: the end points, then the bridge between them
           size_t iw = bead(c, wk.first + atomw, it0), i1 = bead(c, wk.first + a1, pit1);
           seg[0] = c.st.x[iw]; seg[1] = c.st.y[iw]; seg[2] = c.st.z[iw];
           seg[3 * sg + 0] = c.st.x[i1]; seg[3 * sg + 1] = c.st.y[i1]; seg[3 * sg + 2] = c.st.z[i1];
-          sample_middle(c, wk, sh, src, it0, it1, a0, a1, seg, it0);
+          sample_middle(c, wk, sh, gi, it0, it1, a0, a1, seg, it0);
           // the new and the old energy of every inner slice, in that order
           int g = wk.first + a0, nq = 0;
           for (int it = it0 + 1; it < it1; it++) {
@@ -389,7 +475,6 @@ __global__ void __launch_bounds__(kThreads) k_worm_move(Ctx c, Frame *frames, De
             nq++;
           }
           sh.nq = nq;
-          sh.flag = 1;
           sh.stack[0] = it0; sh.stack[1] = it1; sh.stack[2] = atomw; sh.stack[3] = a0; sh.stack[4] = a1;
         }
       }
@@ -465,10 +550,12 @@ __global__ void __launch_bounds__(kThreads) k_worm_move(Ctx c, Frame *frames, De
 constexpr int kMolThreads = 512;
 
 template <bool REPLAY>
-__global__ void __launch_bounds__(kMolThreads) k_mol_exchange(Ctx c, Frame *frames, int type, ReplaySrc src,
-                                                              uint64_t seed, const unsigned *pass, unsigned phase,
-                                                              int *cyc, char *flag, unsigned long long *cnt)
+__global__ void __launch_bounds__(kMolThreads) k_mol_exchange(Ctx c, Frame *frames, int type, const DevWorm *gate,
+                                                              ReplaySrc src, uint64_t seed, const unsigned *pass,
+                                                              unsigned phase, int *cyc, char *flag,
+                                                              unsigned long long *cnt)
 {
+  if (gate && gate->exists) return;          // the worm branch moves closed paths only (mc_main.cc:361)
   __shared__ double dd[3];
   __shared__ double wpart[2][kMolThreads / 32];
   __shared__ int ncyc, accepted, stop;
@@ -559,17 +646,78 @@ __global__ void __launch_bounds__(kMolThreads) k_mol_exchange(Ctx c, Frame *fram
   }
 }
 
+// The bisection of one start slice for every atom of a type in turn, as
+// PIMCPass calls it (mc_main.cc:510-522) and, with gate set, as the worm
+// branch calls it while the worm is closed, at a slice drawn like nrnd2
+// (mc_main.cc:361-369); exch 1 joins the rows through the permutation.
+template <bool MIX>
+__global__ void __launch_bounds__(PIMC_BIS_THREADS) k_bisect_slice(Ctx c, Frame *frames, int type, int time0, int exch,
+                                                                const DevWorm *gate, uint64_t seed,
+                                                                const unsigned *pass, unsigned phase,
+                                                                unsigned long long *cnt)
+{
+  __shared__ BisectShared sh;
+  __shared__ int t0s;
+  if (gate && gate->exists) return;
+  if (threadIdx.x == 0) {
+    t0s = time0;
+    if (gate) {
+      PhiloxSrc ps{seed, ((uint64_t)(*pass) << 32) | ((uint64_t)phase << 12) | 0xFFFu};
+      t0s = min(c.s.P - 1, (int)floor(c.s.P * ps.accept_u(9)));
+    }
+  }
+  __syncthreads();
+  for (int atom = 0; atom < c.s.numb[type]; atom++) {
+    PhiloxSrc src{seed, ((uint64_t)(*pass) << 32) | ((uint64_t)phase << 12) | (uint64_t)atom};
+    int acc = bisect_move<MIX>(c, frames, type, atom, t0s, exch, src, sh, nullptr);
+    if (threadIdx.x == 0) {
+      cnt[(type * 3 + 1) * 2 + 0] += 1;
+      if (acc) cnt[(type * 3 + 1) * 2 + 1] += 1;
+    }
+    __syncthreads();
+  }
+}
+
 }  // namespace
 
 int launch_mol_exchange(const Ctx &c, Frame *f, int type, bool replay, ReplaySrc src, uint64_t seed,
-                        const unsigned *pass, unsigned phase, void *scratch, unsigned long long *cnt, cudaStream_t s)
+                        const unsigned *pass, unsigned phase, void *scratch, unsigned long long *cnt, cudaStream_t s,
+                        const DevWorm *gate)
 {
   int numb = c.s.numb[type];
   int *cyc = (int *)scratch;
   char *flag = (char *)(cyc + numb);
-  if (replay) k_mol_exchange<true><<<1, kMolThreads, 0, s>>>(c, f, type, src, seed, pass, phase, cyc, flag, cnt);
-  else k_mol_exchange<false><<<1, kMolThreads, 0, s>>>(c, f, type, src, seed, pass, phase, cyc, flag, cnt);
+  if (replay)
+    k_mol_exchange<true><<<1, kMolThreads, 0, s>>>(c, f, type, gate, src, seed, pass, phase, cyc, flag, cnt);
+  else
+    k_mol_exchange<false><<<1, kMolThreads, 0, s>>>(c, f, type, gate, src, seed, pass, phase, cyc, flag, cnt);
   return 1;
+}
+
+int launch_bisect_slice(const Ctx &c, Frame *f, int type, int time0, int exch, const DevWorm *gate, uint64_t seed,
+                        const unsigned *pass, unsigned phase, unsigned long long *cnt, cudaStream_t s)
+{
+  if (c.s.mixed)
+    k_bisect_slice<true><<<1, PIMC_BIS_THREADS, 0, s>>>(c, f, type, time0, exch, gate, seed, pass, phase, cnt);
+  else
+    k_bisect_slice<false><<<1, PIMC_BIS_THREADS, 0, s>>>(c, f, type, time0, exch, gate, seed, pass, phase, cnt);
+  return 1;
+}
+
+void launch_worm_prod(const Ctx &c, Frame *f, DevWorm *wk, int *rindex, uint64_t seed, const unsigned *pass,
+                      unsigned phase, void *scratch, int numb, cudaStream_t s)
+{
+  WormPhilox src;
+  src.seed = seed;
+  src.pass = pass;
+  src.phase = phase;
+  double *seg = (double *)scratch;
+  double *dr2l = seg + 3 * (PIMC_WORM_MAXM + 1);
+  double *ptab = dr2l + (numb + 1);
+  int *atml = (int *)(ptab + (numb + 1));
+  Ctx cw = c;
+  cw.st.worm = nullptr;
+  k_worm_move<WormPhilox><<<1, kThreads, 0, s>>>(cw, f, wk, rindex, src, seg, dr2l, atml, ptab);
 }
 
 size_t worm_scratch_bytes(int numb) { return sizeof(double) * (3 * (PIMC_WORM_MAXM + 1) + 2 * (size_t)(numb + 1)) + sizeof(int) * (size_t)(numb + 1) + 64; }
@@ -587,5 +735,5 @@ void launch_worm_move(const Ctx &c, Frame *f, DevWorm *wk, int *rindex, const do
   int *atml = (int *)(ptab + (numb + 1));
   Ctx cw = c;
   cw.st.worm = nullptr;      // the kernel masks from its own copy of the worm
-  k_worm_move<<<1, kThreads, 0, s>>>(cw, f, wk, rindex, src, seg, dr2l, atml, ptab);
+  k_worm_move<WormSrc><<<1, kThreads, 0, s>>>(cw, f, wk, rindex, src, seg, dr2l, atml, ptab);
 }

@@ -56,6 +56,7 @@ def load(path=LIBPATH):
     L.pimc_molecular_move_exchange.argtypes = [vp, C.c_int, _dp, C.c_long, _dp, C.c_long, _lp]
     L.pimc_worm_init.argtypes = [vp, C.c_int, C.c_double, C.c_int, C.c_double]
     L.pimc_worm_move.argtypes = [vp, C.POINTER(_dp), C.POINTER(C.c_long), C.POINTER(C.c_long)]
+    L.pimc_worm_run.argtypes = [vp, C.c_int, C.c_uint64]
     L.pimc_worm_state.argtypes = [vp, _ip]
     L.pimc_worm_set_state.argtypes = [vp, _ip]
     L.pimc_worm_counters.argtypes = [vp, _dp, _dp]
@@ -247,6 +248,9 @@ class Sampler:
         used = (C.c_long * 9)()
         _chk(self.L.pimc_worm_move(self.h, ptrs, lens, used), "pimc_worm_move")
         return list(used)
+
+    def worm_run(self, npasses, seed):
+        _chk(self.L.pimc_worm_run(self.h, int(npasses), C.c_uint64(seed)), "pimc_worm_run")
 
     def worm_state(self):
         st = np.zeros(5, np.int32)

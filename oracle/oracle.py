@@ -159,6 +159,7 @@ def _lib():
     lib.orc_worm_state.argtypes = [C.c_void_p, _ip]
     lib.orc_worm_set_state.argtypes = [C.c_void_p, _ip]
     lib.orc_worm_counters.argtypes = [C.c_void_p, _dp, _dp]
+    lib.orc_worm_run.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_uint64, C.c_int, _dp]
     lib.orc_run_steps.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_uint64, C.c_int, _dp]
     return lib
 
@@ -275,6 +276,11 @@ class Oracle:
         rp, keep = make_wreplay(streams)
         st = self.L.orc_worm_move(self.h, C.byref(rp))
         return st, [getattr(rp, n).pos for n in WSTREAMS]
+
+    def worm_run(self, t_begin, t_count, seed, nthreads=1):
+        bm = C.c_double()
+        st = self.L.orc_worm_run(self.h, int(t_begin), int(t_count), C.c_uint64(seed), int(nthreads), C.byref(bm))
+        return st, bm.value
 
     def worm_state(self):
         st = np.zeros(5, np.int32)

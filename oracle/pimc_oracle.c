@@ -53,6 +53,7 @@ struct orc_ctx {
   double *dr2_list, *ptable;
   int *atm_list;
   double qwtot[7], qwacc[7];
+  uint64_t wctr[9];       /* internal-generator counters of the worm draws */
   double *coords, *cosine, *angles, *newc;  /* [3][na*P] */
   int *pflags, *atom_list;
   /* 1D spline */
@@ -1820,6 +1821,24 @@ void orc_worm_counters(const orc_ctx *c, double *total, double *accep)
 
 static double twave2_of(const orc_ctx *c) { return 4.0 * c->sys.type[c->wtype].lambda * c->tau; }
 
+/* a worm draw: replay stream k of rp, or the internal generator (rp NULL);
+ * k = 0..2 nrnd1..3, 3..7 rnd1..5, 8 gauss's x1 (mc_randg.cc:90-174) */
+static double wt(orc_ctx *c, orc_wreplay *rp, int k)
+{
+  if (rp) {
+    orc_stream *st[9] = {&rp->n1, &rp->n2, &rp->n3, &rp->u1, &rp->u2, &rp->u3, &rp->u4, &rp->u5, &rp->gauss};
+    return take(st[k], &rp->overrun);
+  }
+  if (k == 8) {
+    double r1 = u01_key(c->seed, 40, c->wctr[8]++);
+    double r2 = u01_key(c->seed, 41, c->wctr[8]++);
+    return sqrt(-log(r1)) * cos(2.0 * M_PI * r2);
+  }
+  return u01_key(c->seed, 30 + (uint64_t)k, c->wctr[k]++);
+}
+
+static int nrnd(orc_ctx *c, orc_wreplay *rp, int k, int n) { return (int)floor(n * wt(c, rp, k)); }
+
 /* get_potential -- mc_qworm.cc:402-422 */
 static double worm_potential(const orc_ctx *c, int it0, int it1, int atom0, int atom1, const double *coords)
 {
@@ -1870,29 +1889,29 @@ static void sample_middle(orc_ctx *c, int it0, int it2, int atom0, int atom2, do
   double gkin = (s0 + s2) / (twave2_of(c) * s0 * s2);
   for (int id = 0; id < NDIM; id++) {
     coords[id * nb + q1] = (s2 * coords[id * nb + q0] + s0 * coords[id * nb + q2]) / (s0 + s2);
-    coords[id * nb + q1] += take(&rp->gauss, &rp->overrun) / sqrt(gkin);     /* gauss(gkin), mc_randg.cc:149 */
+    coords[id * nb + q1] += wt(c, rp, 8) / sqrt(gkin);     /* gauss(gkin), mc_randg.cc:149 */
   }
   sample_middle(c, it0, it1, atom0, atom1, coords, rp);
   sample_middle(c, it1, it2, atom1, atom2, coords, rp);
 }
 
-static int nrnd(orc_stream *s, int n, int *overrun) { return (int)floor(n * take(s, overrun)); }
+
 
 /* qworm_open -- mc_qworm.cc:155-180 */
 static void qworm_open(orc_ctx *c, orc_wreplay *rp)
 {
   c->qwtot[0] += 1.0;
   int numb = c->sys.type[c->wtype].numb;
-  c->atom_i = nrnd(&rp->n1, numb, &rp->overrun);
-  c->ira = nrnd(&rp->n2, c->P, &rp->overrun);
-  int segm = nrnd(&rp->n3, c->wm, &rp->overrun) + 1;
+  c->atom_i = nrnd(c, rp, 0, numb);
+  c->ira = nrnd(c, rp, 1, c->P);
+  int segm = nrnd(c, rp, 2, c->wm) + 1;
   c->masha = (c->ira + segm) % c->P;
   c->atom_m = c->atom_i;
   if (c->masha != (c->ira + segm)) c->atom_m = c->pindex[c->atom_i];
   double prob = qw_open_prob(c, segm);
   int acc = 0;
   if (prob >= 1.0) acc = 1;
-  else if (prob > take(&rp->u1, &rp->overrun)) acc = 1;
+  else if (prob > wt(c, rp, 3)) acc = 1;
   if (acc) {
     c->wexists = 1;
     c->qwacc[0] += 1.0;
@@ -1911,7 +1930,7 @@ static void qworm_close(orc_ctx *c, orc_wreplay *rp)
   double prob = 1.0 / qw_open_prob(c, segm);
   int acc = 0;
   if (prob >= 1.0) acc = 1;
-  else if (prob > take(&rp->u1, &rp->overrun)) acc = 1;
+  else if (prob > wt(c, rp, 3)) acc = 1;
   if (acc) {
     c->wexists = 0;
     c->qwacc[1] += 1.0;
@@ -1926,7 +1945,7 @@ static void qworm_advance(orc_ctx *c, orc_wreplay *rp)
   int P = c->P;
   int segm = c->masha - c->ira;
   if (segm < 0) segm += P;
-  int advance = nrnd(&rp->n3, c->wm, &rp->overrun) + 1;
+  int advance = nrnd(c, rp, 2, c->wm) + 1;
   if (segm - advance <= 0) return;
   long offset = c->offset[c->wtype];
   int it0 = c->ira, it2 = c->ira + advance;
@@ -1936,12 +1955,12 @@ static void qworm_advance(orc_ctx *c, orc_wreplay *rp)
   long pt0 = offset + (long)c->atom_i * P + it0 % P;
   long pt2 = offset + (long)atom_i_new * P + it2 % P;
   for (int id = 0; id < NDIM; id++)
-    c->coords[id * nb + pt2] = c->coords[id * nb + pt0] + take(&rp->gauss, &rp->overrun) / sqrt(gvar);
+    c->coords[id * nb + pt2] = c->coords[id * nb + pt0] + wt(c, rp, 8) / sqrt(gvar);
   sample_middle(c, it0, it2, c->atom_i, atom_i_new, c->coords, rp);
   double pot = worm_potential(c, it0, it2 + 1, c->atom_i, atom_i_new, c->coords);
   int acc = 0;
   if (pot < 0.0) acc = 1;
-  else if (exp(-pot * c->tau) > take(&rp->u2, &rp->overrun)) acc = 1;
+  else if (exp(-pot * c->tau) > wt(c, rp, 4)) acc = 1;
   if (acc) {
     c->qwacc[4] += 1.0;
     c->ira = ira_new;
@@ -1955,7 +1974,7 @@ static void qworm_recede(orc_ctx *c, orc_wreplay *rp)
   c->qwtot[5] += 1.0;
   int segm = c->ira - c->masha;
   if (segm < 0) segm += c->P;
-  int recede = nrnd(&rp->n3, c->wm, &rp->overrun) + 1;
+  int recede = nrnd(c, rp, 2, c->wm) + 1;
   if ((segm - recede) < 1) return;
   int it0 = c->ira - recede, it1 = c->ira;
   int atom0 = c->atom_i, atom1 = c->atom_i;
@@ -1967,7 +1986,7 @@ static void qworm_recede(orc_ctx *c, orc_wreplay *rp)
   double pot = worm_potential(c, it0, it1 + 1, atom0, atom1, c->coords);
   int acc = 0;
   if (pot > 0.0) acc = 1;
-  else if (exp(pot * c->tau) > take(&rp->u2, &rp->overrun)) acc = 1;
+  else if (exp(pot * c->tau) > wt(c, rp, 4)) acc = 1;
   if (acc) {
     c->ira = it0 % c->P;
     c->atom_i = atom0;
@@ -2025,7 +2044,7 @@ static int atom2swap(orc_ctx *c, int count, double *pnorm, orc_wreplay *rp)
 {
   *pnorm = 0.0;
   for (int ic = 1; ic <= count; ic++) *pnorm += c->ptable[ic];
-  double prand = *pnorm * take(&rp->u3, &rp->overrun);
+  double prand = *pnorm * wt(c, rp, 5);
   double sum = 0.0;
   int ic = 1;
   while ((ic <= count) && (sum < prand)) {
@@ -2077,7 +2096,7 @@ static void qworm_swap(orc_ctx *c, orc_wreplay *rp)
   prob *= (pnorm_old / pnorm_new);
   int acc = 0;
   if (prob >= 1.0) acc = 1;
-  else if (prob > take(&rp->u4, &rp->overrun)) acc = 1;
+  else if (prob > wt(c, rp, 6)) acc = 1;
   if (acc) {
     c->qwacc[6] += 1.0;
     for (int id = 0; id < NDIM; id++) {
@@ -2116,13 +2135,68 @@ int orc_worm_move(orc_ctx *c, orc_wreplay *rp)
     if (c->wexists) qworm_close(c, rp);
     else qworm_open(c, rp);
     if (c->wexists) {
-      double r = take(&rp->u5, &rp->overrun);
+      double r = wt(c, rp, 7);
       if (r > 0.5) qworm_advance(c, rp);
       else qworm_recede(c, rp);
     }
     if (bose && c->wexists) qworm_swap(c, rp);
   }
-  return rp->overrun ? PIMC_ERR_BAD_ARG : PIMC_OK;
+  return (rp && rp->overrun) ? PIMC_ERR_BAD_ARG : PIMC_OK;
+}
+
+/* the worm branch of the pass loop (mc_main.cc:348-381) with the internal
+ * generator: per time slice, for the worm type MCWormMove and, with the worm
+ * closed, MCBisectionMoveExchange at a drawn slice (MCBisectionMove for
+ * Boltzmann statistics) and at slice 0 the exchange centroid move; for the
+ * other types PIMCPass (mc_main.cc:510-522).  *bead_moves counts the
+ * scheduled bead moves of the non-worm moves and P per worm-type atom and
+ * slice for the worm tries. */
+static int sweep_parallel(orc_ctx *c, int type, uint64_t sweep_id, int nthreads);
+
+int orc_worm_run(orc_ctx *c, int t_begin, int t_count, uint64_t seed, int nthreads, double *bead_moves)
+{
+  if (!c->worm_on) return PIMC_ERR_STATE;
+  src_t src = {NULL, c};
+  c->seed = seed;
+  double bm = 0.0;
+  if (nthreads < 1) nthreads = 1;
+  for (int time = t_begin; time < t_begin + t_count; time++) {
+    int t = time % c->P;
+    for (int type = 0; type < c->sys.ntypes; type++) {
+      int numb = c->sys.type[type].numb;
+      if (numb <= 0) continue;
+      if (type == c->wtype) {
+        int st = orc_worm_move(c, NULL);
+        if (st) return st;
+        bm += (double)numb;
+        if (!c->wexists) {
+          int rt = (int)floor(c->P * u01_key(c->seed, 50, c->wctr[0]++));   /* nrnd2(NumbTimes) */
+          int bose = c->sys.type[type].stat == PIMC_BOSE;
+          bisection_move(c, type, rt, &src, NULL, NULL, bose);
+          bm += (double)numb * (double)(c->mlsegm[type] - 1);
+          if (t == 0) {
+            if (bose) orc_molecular_move_exchange(c, type, NULL, NULL, NULL);
+            else molecular_move(c, type, &src, NULL, NULL, nthreads);
+            bm += (double)numb * c->P;
+          }
+        }
+        continue;
+      }
+      if (t == 0) {
+        molecular_move(c, type, &src, NULL, NULL, nthreads);
+        bm += (double)numb * c->P;
+      }
+      bisection_move(c, type, t, &src, NULL, NULL, 0);
+      bm += (double)numb * (double)(c->mlsegm[type] - 1);
+      if (type == c->imtype && c->sys.rotation) {
+        int st = sweep_parallel(c, type, (uint64_t)time, nthreads);
+        if (st) return st;
+        bm += (double)c->Q * numb;
+      }
+    }
+  }
+  if (bead_moves) *bead_moves = bm;
+  return PIMC_OK;
 }
 
 /* -------------------------------------------------------- timed schedule */

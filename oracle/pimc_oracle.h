@@ -132,6 +132,9 @@ int  orc_worm_move(orc_ctx *c, orc_wreplay *rp);
 void orc_worm_state(const orc_ctx *c, int *st);
 void orc_worm_set_state(orc_ctx *c, const int *st);
 void orc_worm_counters(const orc_ctx *c, double *total, double *accep);
+/* the worm branch of the pass loop for slices [t_begin, t_begin+t_count)
+ * with the internal generator (timed CPU baseline) */
+int  orc_worm_run(orc_ctx *c, int t_begin, int t_count, uint64_t seed, int nthreads, double *bead_moves);
 
 /* propagator-table generators (orc_tables.c): linear_prop/linden.f and
  * nmv_prop/asymrho.f restated */

@@ -112,3 +112,34 @@ def test_exchange_centroid_cycles_match_oracle():
     otot, oacc = o.counters()
     assert tot[0] == otot[0] and acc[0] == oacc[0] and acc[0] > 0
     s.close()
+
+
+@pytest.mark.parametrize("mixed", [False, True])
+def test_worm_run_production(mixed):
+    """The worm branch of the pass loop with counter-based draws on the
+    config-0 family (CO2-like rotor + 6 He-4 bosons, P = 32, Q = 8): the same
+    seed gives the same path, permutation and worm on a second handle; the
+    worm opens, closes and swaps; the path stays finite and the permutation
+    a permutation."""
+    w, d, line = load()
+    runs = []
+    for rep in range(2):
+        s = G.Sampler(w, mixed=mixed)
+        s.set_state(d["coords0"], d["angles0"], w.pindex)
+        s.worm_init(0, line[1], line[2], w.density)
+        s.worm_run(6, seed=4242)
+        c, a, co, p = s.get_state()
+        runs.append((c, a, p, s.worm_state(), s.worm_counters(), s.counters()))
+        s.close()
+    (c0, a0, p0, st0, wc0, mc0), (c1, a1, p1, st1, wc1, mc1) = runs
+    np.testing.assert_array_equal(c0, c1)
+    np.testing.assert_array_equal(a0, a1)
+    np.testing.assert_array_equal(p0, p1)
+    np.testing.assert_array_equal(st0, st1)
+    assert np.isfinite(c0).all()
+    assert sorted(p0[:6]) == list(range(6))
+    tot, acc = wc0
+    assert tot[0] > 0 and acc[0] > 0 and tot[1] > 0 and acc[1] > 0     # opened and closed
+    assert tot[6] > 0                                                  # swaps tried
+    mtot, macc = mc0
+    assert mtot[5] > 0 and macc[5] > 0                                 # rotor moved
