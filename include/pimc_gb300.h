@@ -164,6 +164,20 @@ pimc_status pimc_worm_set_state(pimc_handle *h, const int *state);
  * ADVANCE, RECEDE, SWAP] */
 pimc_status pimc_worm_counters(pimc_handle *h, double *total, double *accep);
 
+/* ---- rotor-rotor surrogate (spec pattern 4) ---------------------- */
+
+/* An MLP 6 -> 256 -> 256 -> 256 -> 1 with SiLU activations: FP32 first and
+ * last layers, BF16 weights and FP32 accumulation in the two 256 x 256
+ * layers, which run on the tensor cores (tcgen05).  Weights are row-major
+ * [in][out]: w1[6*256], w2/w3[256*256], w4[256]. */
+typedef struct pimc_mlp pimc_mlp;
+pimc_status pimc_mlp_create(int device, pimc_mlp **out);
+pimc_status pimc_mlp_destroy(pimc_mlp *m);
+pimc_status pimc_mlp_set_weights(pimc_mlp *m, const float *w1, const float *b1, const float *w2, const float *b2,
+                                 const float *w3, const float *b3, const float *w4, float b4);
+/* y[i] = MLP(x[i*6 .. i*6+5]) for n inputs (host buffers) */
+pimc_status pimc_mlp_forward(pimc_mlp *m, int n, const float *x, float *y);
+
 /* ---- propagator tables ---------------------------------------------------- */
 
 /* The exact linear-rotor propagator of linear_prop/linden.f (tau and the l

@@ -60,6 +60,11 @@ def load(path=LIBPATH):
     L.pimc_worm_state.argtypes = [vp, _ip]
     L.pimc_worm_set_state.argtypes = [vp, _ip]
     L.pimc_worm_counters.argtypes = [vp, _dp, _dp]
+    L.pimc_mlp_create.argtypes = [C.c_int, C.POINTER(vp)]
+    L.pimc_mlp_destroy.argtypes = [vp]
+    _fp = C.POINTER(C.c_float)
+    L.pimc_mlp_set_weights.argtypes = [vp, _fp, _fp, _fp, _fp, _fp, _fp, _fp, C.c_float]
+    L.pimc_mlp_forward.argtypes = [vp, C.c_int, _fp, _fp]
     L.pimc_linden.argtypes = [C.c_int, C.c_int, _dp, _ip, C.c_double, C.c_int, C.c_int, _dp]
     L.pimc_asymrho.argtypes = [C.c_int, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, _dp, C.c_int,
                                _dp, _dp, _dp, _dp]
@@ -457,3 +462,37 @@ def asymrho(temperature, nslice, iodevn, ith0, ith1, abc, maxj, device=0):
     _chk(L.pimc_asymrho(int(device), float(temperature), int(nslice), int(iodevn), int(ith0), int(ith1), dptr(a),
                         int(maxj), dptr(rho), dptr(erot), dptr(esq), dptr(info)), "pimc_asymrho")
     return rho, erot, esq, info
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _fptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+class Mlp:
+    """The tcgen05 surrogate MLP 6 -> 256 -> 256 -> 256 -> 1 (include/pimc_gb300.h)."""
+
+    def __init__(self, device=0):
+        self.L = load()
+        self.h = C.c_void_p()
+        _chk(self.L.pimc_mlp_create(int(device), C.byref(self.h)), "pimc_mlp_create")
+
+    def set_weights(self, w1, b1, w2, b2, w3, b3, w4, b4):
+        arrs = [_f32(a) for a in (w1, b1, w2, b2, w3, b3, w4)]
+        assert arrs[0].shape == (6, 256) and arrs[2].shape == (256, 256) and arrs[4].shape == (256, 256)
+        _chk(self.L.pimc_mlp_set_weights(self.h, *[_fptr(a) for a in arrs], C.c_float(float(b4))),
+             "pimc_mlp_set_weights")
+
+    def forward(self, x):
+        x = _f32(x).reshape(-1, 6)
+        y = np.zeros(len(x), dtype=np.float32)
+        _chk(self.L.pimc_mlp_forward(self.h, len(x), _fptr(x), _fptr(y)), "pimc_mlp_forward")
+        return y
+
+    def close(self):
+        if self.h:
+            self.L.pimc_mlp_destroy(self.h)
+            self.h = C.c_void_p()
