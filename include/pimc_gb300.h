@@ -177,6 +177,17 @@ pimc_status pimc_mlp_set_weights(pimc_mlp *m, const float *w1, const float *b1, 
                                  const float *w3, const float *b3, const float *w4, float b4);
 /* y[i] = MLP(x[i*6 .. i*6+5]) for n inputs (host buffers) */
 pimc_status pimc_mlp_forward(pimc_mlp *m, int n, const float *x, float *y);
+/* The parameter vector: w1[6*256], b1[256], w2[256*256], b2[256],
+ * w3[256*256], b3[256], w4[256], b4 (pimc_mlp_param_count() floats). */
+int         pimc_mlp_param_count(void);
+pimc_status pimc_mlp_get_params(pimc_mlp *m, float *params);
+/* Gradient of mean((y - e)^2) over n samples (the tensor-core training
+ * kernels), in parameter-vector order; *loss = that mean (optional). */
+pimc_status pimc_mlp_gradients(pimc_mlp *m, int n, const float *x, const float *e, float *grad, double *loss);
+/* epochs of Adam over n samples in a seeded order, minibatches of `batch`
+ * (a multiple of 128); loss_out[epoch] = the epoch's mean minibatch loss. */
+pimc_status pimc_mlp_train(pimc_mlp *m, int n, const float *x, const float *e, int epochs, int batch, float lr,
+                           uint64_t seed, double *loss_out);
 
 /* ---- propagator tables ---------------------------------------------------- */
 

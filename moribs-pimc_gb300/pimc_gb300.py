@@ -65,6 +65,10 @@ def load(path=LIBPATH):
     _fp = C.POINTER(C.c_float)
     L.pimc_mlp_set_weights.argtypes = [vp, _fp, _fp, _fp, _fp, _fp, _fp, _fp, C.c_float]
     L.pimc_mlp_forward.argtypes = [vp, C.c_int, _fp, _fp]
+    L.pimc_mlp_param_count.restype = C.c_int
+    L.pimc_mlp_get_params.argtypes = [vp, _fp]
+    L.pimc_mlp_gradients.argtypes = [vp, C.c_int, _fp, _fp, _fp, _dp]
+    L.pimc_mlp_train.argtypes = [vp, C.c_int, _fp, _fp, C.c_int, C.c_int, C.c_float, C.c_uint64, _dp]
     L.pimc_linden.argtypes = [C.c_int, C.c_int, _dp, _ip, C.c_double, C.c_int, C.c_int, _dp]
     L.pimc_asymrho.argtypes = [C.c_int, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, _dp, C.c_int,
                                _dp, _dp, _dp, _dp]
@@ -491,6 +495,28 @@ class Mlp:
         y = np.zeros(len(x), dtype=np.float32)
         _chk(self.L.pimc_mlp_forward(self.h, len(x), _fptr(x), _fptr(y)), "pimc_mlp_forward")
         return y
+
+    def params(self):
+        p = np.zeros(self.L.pimc_mlp_param_count(), dtype=np.float32)
+        _chk(self.L.pimc_mlp_get_params(self.h, _fptr(p)), "pimc_mlp_get_params")
+        return p
+
+    def gradients(self, x, e):
+        x = _f32(x).reshape(-1, 6)
+        e = _f32(e)
+        g = np.zeros(self.L.pimc_mlp_param_count(), dtype=np.float32)
+        loss = C.c_double()
+        _chk(self.L.pimc_mlp_gradients(self.h, len(x), _fptr(x), _fptr(e), _fptr(g), C.byref(loss)),
+             "pimc_mlp_gradients")
+        return g, loss.value
+
+    def train(self, x, e, epochs, batch, lr, seed=0):
+        x = _f32(x).reshape(-1, 6)
+        e = _f32(e)
+        losses = np.zeros(epochs)
+        _chk(self.L.pimc_mlp_train(self.h, len(x), _fptr(x), _fptr(e), int(epochs), int(batch), C.c_float(lr),
+                                   C.c_uint64(seed), dptr(losses)), "pimc_mlp_train")
+        return losses
 
     def close(self):
         if self.h:
