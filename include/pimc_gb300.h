@@ -189,6 +189,25 @@ pimc_status pimc_mlp_gradients(pimc_mlp *m, int n, const float *x, const float *
 pimc_status pimc_mlp_train(pimc_mlp *m, int n, const float *x, const float *e, int epochs, int batch, float lr,
                            uint64_t seed, double *loss_out);
 
+/* Delayed-acceptance rotational sweeps of a water dimer (two nonlinear
+ * rotors, no atoms, tabulated densities, even Q) screened by the surrogate.
+ * pimc_da_samples: the training data the sampler emits -- for each of the
+ * P translational slices the six dimer features (distance, the unit
+ * centre-to-centre vector on rotor 0's body axes, its component on rotor
+ * 1's z axis, the cosine between the z axes) and the exact caleng energy
+ * (caleng_tip4p_gg.f, K).  pimc_da_sweeps: nsweeps sweeps of MCRot3Dstep
+ * moves (mc_piqmc.cc:938-1199) in four independent sub-phases per sweep;
+ * with use_surrogate the first stage accepts with
+ * min(1, rho'/rho exp(-tau dV_sur)), dV_sur = escale * (MLP(new) - MLP(old))
+ * summed over the rotor's slices, and the second with
+ * min(1, exp(-tau (dV - dV_sur))) from the exact caleng difference, so the
+ * sampled distribution is the exact one; without it the plain Metropolis
+ * move.  stats[4] = moves, passed the first stage, accepted, exact
+ * differences evaluated. */
+pimc_status pimc_da_samples(pimc_handle *h, float *feat, float *energy);
+pimc_status pimc_da_sweeps(pimc_handle *h, pimc_mlp *m, int nsweeps, uint64_t seed, float escale, int use_surrogate,
+                           double *stats);
+
 /* ---- propagator tables ---------------------------------------------------- */
 
 /* The exact linear-rotor propagator of linear_prop/linden.f (tau and the l

@@ -1206,6 +1206,77 @@ extern "C" pimc_status pimc_worm_run(pimc_handle *h, int npasses, uint64_t seed)
   return check_err(h);
 }
 
+// ------------------------------------------------------- delayed acceptance
+
+static pimc_status da_check(pimc_handle *h)
+{
+  const DevSys &d = h->ctx.s;
+  if (d.nrotors != 2 || d.na != 2 || d.molecule[d.imtype] != PIMC_NONLINEAR || d.rot_den_type != 0 || d.Q % 2)
+    return PIMC_ERR_STATE;     // the water dimer: two tops, no atoms, tabulated densities, even Q
+  return PIMC_OK;
+}
+
+extern "C" pimc_status pimc_da_samples(pimc_handle *h, float *feat, float *energy)
+{
+  pimc_status e = ready(h);
+  if (e) return e;
+  if ((e = da_check(h))) return e;
+  if (!feat || !energy) return PIMC_ERR_BAD_ARG;
+  const int P = h->ctx.s.P;
+  void *buf;
+  if ((e = scratch(h, (size_t)P * 7 * sizeof(float) + 512, &buf))) return e;
+  float *df = (float *)buf, *de = df + (size_t)P * 6;
+  h->launches += launch_da_samples(h->ctx, h->frames, df, de, h->stream);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(feat, df, (size_t)P * 6 * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaMemcpyAsync(energy, de, (size_t)P * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
+  return check_err(h);
+}
+
+extern "C" pimc_status pimc_da_sweeps(pimc_handle *h, pimc_mlp *m, int nsweeps, uint64_t seed, float escale,
+                                      int use_surrogate, double *stats)
+{
+  pimc_status e = ready(h);
+  if (e) return e;
+  if ((e = da_check(h))) return e;
+  if (nsweeps < 0 || (use_surrogate && !m) || nsweeps > (1 << 18)) return PIMC_ERR_BAD_ARG;
+  const DevSys &d = h->ctx.s;
+  const int nm = d.Q / 2, rows = nm * 2 * d.R;
+  size_t bytes = (size_t)rows * 7 * sizeof(float) + (size_t)nm * sizeof(DaMove) + 4096;
+  void *buf;
+  if ((e = scratch(h, bytes, &buf))) return e;
+  char *cur = (char *)buf;
+  unsigned long long *st = (unsigned long long *)cur;
+  cur += 256;
+  float *feat = (float *)cur;
+  cur += ((size_t)rows * 6 * sizeof(float) + 255) / 256 * 256;
+  float *y = (float *)cur;
+  cur += ((size_t)rows * sizeof(float) + 255) / 256 * 256;
+  DaMove *mv = (DaMove *)cur;
+  CK(cudaMemsetAsync(st, 0, 4 * sizeof(unsigned long long), h->stream));
+  launch_pass_begin(h->pass, h->stream);
+  h->launches++;
+  for (int sw = 0; sw < nsweeps; sw++)
+    for (int par = 0; par < 2; par++)
+      for (int r = 0; r < 2; r++) {
+        unsigned phase = 4u * (unsigned)sw + 2u * par + r;
+        h->launches += launch_da_propose(h->ctx, h->frames, r, par, phase, seed, h->pass, feat, mv, h->stream);
+        if (use_surrogate) h->launches += mlp_forward_device(m, feat, rows, y, h->stream);
+        h->launches += launch_da_decide(h->ctx, h->frames, r, par, phase, seed, h->pass, y, use_surrogate, escale, mv,
+                                        st, h->cnt, h->stream);
+      }
+  launch_invalidate_caches(h->ctx, h->stream);
+  launch_refresh_frames(h->ctx, h->frames, h->stream);
+  h->launches += 2;
+  CK(cudaGetLastError());
+  unsigned long long hs[4];
+  CK(cudaMemcpyAsync(hs, st, sizeof(hs), cudaMemcpyDeviceToHost, h->stream));
+  e = check_err(h);
+  if (stats)
+    for (int k = 0; k < 4; k++) stats[k] = (double)hs[k];
+  return e;
+}
+
 extern "C" pimc_status pimc_worm_state(pimc_handle *h, int *state)
 {
   if (!h || !state) return PIMC_ERR_BAD_ARG;

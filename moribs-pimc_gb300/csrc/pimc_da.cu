@@ -1,0 +1,180 @@
+// pimc_da.cu -- two-stage delayed-acceptance rotational moves for a pair of
+// rigid asymmetric tops (the water dimer of caleng_tip4p_gg.f) screened by
+// the surrogate MLP.
+//
+// A rotational sweep runs in four sub-phases (even slices of rotor 0, of
+// rotor 1, then the odd slices), each an independent set: every move of a
+// sub-phase reads only orientations the sub-phase does not change.  Per
+// sub-phase: k_da_propose draws each move's proposal (the reference's
+// MCRot3Dstep proposal, mc_piqmc.cc:955-1001), its density ratio from the
+// rotden table (mc_piqmc.cc:1021-1127) and the dimer features of the new
+// and the old orientation at the rotor's R translational slices; the MLP
+// evaluates all rows in one tensor-core launch; k_da_decide runs the first
+// stage with the surrogate's potential difference and, for the moves that
+// pass it, the second stage with the exact caleng difference
+// (acceptance min(1, exp(-tau (dV - dV_sur)))), which keeps the exact
+// stationary distribution (Christen and Fox, J. Comput. Graph. Stat. 14,
+// 795 (2005)).  With the surrogate off the same kernels make the plain
+// Metropolis move with the exact difference.
+#include "pimc_kernels.cuh"
+#include "pimc_launch.h"
+
+namespace {
+
+// Six features of a rigid-top dimer seen from rotor a (frame fa, centre ca)
+// towards rotor b: the distance (shifted and scaled), the unit vector a->b
+// on a's three body axes, its component on b's z axis and the cosine
+// between the two z axes.
+__device__ __forceinline__ void dimer_features(const Frame &fa, const double ca[3], const Frame &fb,
+                                               const double cb[3], float *f)
+{
+  double R[3] = {cb[0] - ca[0], cb[1] - ca[1], cb[2] - ca[2]};
+  double r = sqrt(R[0] * R[0] + R[1] * R[1] + R[2] * R[2]);
+  double u[3] = {R[0] / r, R[1] / r, R[2] / r};
+  const double *m = fa.m, *n = fb.m;
+  f[0] = (float)((r - 3.0) * 2.0);
+  f[1] = (float)(u[0] * m[0] + u[1] * m[3] + u[2] * m[6]);
+  f[2] = (float)(u[0] * m[1] + u[1] * m[4] + u[2] * m[7]);
+  f[3] = (float)(u[0] * m[2] + u[1] * m[5] + u[2] * m[8]);
+  f[4] = (float)(u[0] * n[2] + u[1] * n[5] + u[2] * n[8]);
+  f[5] = (float)(m[2] * n[2] + m[5] * n[5] + m[8] * n[8]);
+}
+
+__device__ __forceinline__ void centre(const Ctx &c, int g, int it, double v[3])
+{
+  size_t i = sidx(c.s, it, g);
+  v[0] = c.st.x[i];
+  v[1] = c.st.y[i];
+  v[2] = c.st.z[i];
+}
+
+// the features and the exact caleng energy of rotor 0 against rotor 1 at
+// every translational slice of the current path
+__global__ void k_da_samples(Ctx c, const Frame *frames, float *feat, float *energy)
+{
+  const DevSys &s = c.s;
+  int it = blockIdx.x * blockDim.x + threadIdx.x;
+  if (it >= s.P) return;
+  const int g0 = s.rot_first, g1 = s.rot_first + 1, q = it / s.R;
+  const Frame &f0 = frames[rot_index(s, g0, q)], &f1 = frames[rot_index(s, g1, q)];
+  double c0[3], c1[3];
+  centre(c, g0, it, c0);
+  centre(c, g1, it, c1);
+  dimer_features(f0, c0, f1, c1, feat + (size_t)it * 6);
+  energy[it] = (float)caleng(f0, f1, c0[0], c0[1], c0[2], c1[0], c1[1], c1[2]);
+}
+
+__global__ void k_da_propose(Ctx c, const Frame *frames, int r, int parity, unsigned phase, uint64_t seed,
+                             const unsigned *pass, float *feat, DaMove *mv)
+{
+  const DevSys &s = c.s;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x, q = 2 * k + parity;
+  if (q >= s.Q) return;
+  const int Q = s.Q, R = s.R, g = s.rot_first + r, o = s.rot_first + 1 - r;
+  const size_t n = (size_t)s.nrotors * Q;
+  const int ri = rot_index(s, g, q);
+  double u[4], prop[3];
+  rot_uniforms(seed, *pass, phase, q, r, false, u);
+  rot_propose(s, false, c.st.ang[ri], c.st.ang[n + ri], c.st.ang[2 * n + ri], u, prop);
+  Frame fn;
+  make_frame64(prop[0], prop[1], prop[2], fn);
+  const Frame &fo = frames[ri];
+  const Frame &fm = frames[rot_index(s, g, (q - 1 + Q) % Q)], &fp = frames[rot_index(s, g, (q + 1) % Q)];
+  int bad = 0;
+  double rn = rotden_rho(c.t, fm, fn, &bad, nullptr, nullptr) * rotden_rho(c.t, fn, fp, &bad, nullptr, nullptr);
+  double ro = rotden_rho(c.t, fm, fo, &bad, nullptr, nullptr) * rotden_rho(c.t, fo, fp, &bad, nullptr, nullptr);
+  const Frame &fb = frames[rot_index(s, o, q)];
+  for (int j = 0; j < R; j++) {
+    double ca[3], cb[3];
+    centre(c, g, q * R + j, ca);
+    centre(c, o, q * R + j, cb);
+    dimer_features(fn, ca, fb, cb, feat + ((size_t)k * 2 * R + 2 * j) * 6);
+    dimer_features(fo, ca, fb, cb, feat + ((size_t)k * 2 * R + 2 * j + 1) * 6);
+  }
+  DaMove &d = mv[k];
+  d.prop[0] = prop[0]; d.prop[1] = prop[1]; d.prop[2] = prop[2];
+  d.rn = rn;
+  d.ro = ro;
+  d.bad = bad;
+}
+
+// stats[0] moves, [1] passed the first stage (all, without the surrogate),
+// [2] accepted, [3] exact potential differences evaluated
+__global__ void k_da_decide(Ctx c, Frame *frames, int r, int parity, unsigned phase, uint64_t seed,
+                            const unsigned *pass, const float *y, int use_sur, float escale, const DaMove *mv,
+                            unsigned long long *stats, unsigned long long *cnt)
+{
+  const DevSys &s = c.s;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x, q = 2 * k + parity;
+  if (q >= s.Q) return;
+  const int Q = s.Q, R = s.R, g = s.rot_first + r, o = s.rot_first + 1 - r;
+  const size_t n = (size_t)s.nrotors * Q;
+  const int ri = rot_index(s, g, q);
+  const DaMove &d = mv[k];
+  if (d.bad) atomicOr(c.st.err, (unsigned)DERR_GRID_RANGE);
+  double u1, u2;
+  philox_u2(seed, ((uint64_t)(*pass) << 32) | ((uint64_t)phase << 12) | (uint64_t)q, 0x600000u | (uint32_t)r, 0u,
+            &u1, &u2);
+  const double lr = log(d.rn / d.ro);
+  double dvs = 0.0;
+  bool pass1 = true;
+  if (use_sur) {
+    for (int j = 0; j < R; j++) dvs += (double)y[(size_t)k * 2 * R + 2 * j] - (double)y[(size_t)k * 2 * R + 2 * j + 1];
+    dvs *= (double)escale;
+    pass1 = lr - s.tau * dvs > log(u1);
+  }
+  bool acc = false;
+  if (pass1) {
+    Frame fn;
+    make_frame64(d.prop[0], d.prop[1], d.prop[2], fn);
+    const Frame &fo = frames[ri], &fb = frames[rot_index(s, o, q)];
+    double dv = 0.0;
+    for (int j = 0; j < R; j++) {
+      double ca[3], cb[3];
+      centre(c, g, q * R + j, ca);
+      centre(c, o, q * R + j, cb);
+      dv += caleng(fn, fb, ca[0], ca[1], ca[2], cb[0], cb[1], cb[2]) -
+            caleng(fo, fb, ca[0], ca[1], ca[2], cb[0], cb[1], cb[2]);
+    }
+    if (use_sur) acc = -s.tau * (dv - dvs) > log(u2);
+    else acc = lr - s.tau * dv > log(u1);
+    atomicAdd(stats + 3, 1ull);
+    if (acc) {
+      c.st.ang[ri] = d.prop[0];
+      c.st.ang[n + ri] = d.prop[1];
+      c.st.ang[2 * n + ri] = d.prop[2];
+      make_frame(d.prop[0], d.prop[1], d.prop[2], frames[ri]);
+    }
+  }
+  atomicAdd(stats, 1ull);
+  if (pass1) atomicAdd(stats + 1, 1ull);
+  if (acc) atomicAdd(stats + 2, 1ull);
+  const int type = s.imtype;
+  atomicAdd(cnt + (type * 3 + 2) * 2, 1ull);
+  if (acc) atomicAdd(cnt + (type * 3 + 2) * 2 + 1, 1ull);
+}
+
+}  // namespace
+
+int launch_da_samples(const Ctx &c, const Frame *f, float *feat, float *energy, cudaStream_t s)
+{
+  k_da_samples<<<(c.s.P + 127) / 128, 128, 0, s>>>(c, f, feat, energy);
+  return 1;
+}
+
+int launch_da_propose(const Ctx &c, const Frame *f, int r, int parity, unsigned phase, uint64_t seed,
+                      const unsigned *pass, float *feat, DaMove *mv, cudaStream_t s)
+{
+  int nm = (c.s.Q + 1 - parity) / 2;
+  k_da_propose<<<(nm + 127) / 128, 128, 0, s>>>(c, f, r, parity, phase, seed, pass, feat, mv);
+  return 1;
+}
+
+int launch_da_decide(const Ctx &c, Frame *f, int r, int parity, unsigned phase, uint64_t seed, const unsigned *pass,
+                     const float *y, int use_sur, float escale, const DaMove *mv, unsigned long long *stats,
+                     unsigned long long *cnt, cudaStream_t s)
+{
+  int nm = (c.s.Q + 1 - parity) / 2;
+  k_da_decide<<<(nm + 127) / 128, 128, 0, s>>>(c, f, r, parity, phase, seed, pass, y, use_sur, escale, mv, stats, cnt);
+  return 1;
+}

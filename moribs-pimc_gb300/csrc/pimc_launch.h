@@ -53,6 +53,22 @@ int est_area_ctas(const Ctx &c, int btype);
 int launch_est_area(const Ctx &c, int mode, int btype, const double *mass, double *out, cudaStream_t s);
 size_t mol_scratch_bytes();
 
+// ------------------------------------------------------------ delayed acceptance
+struct DaMove {
+  double prop[3];        // the proposal (phi, cos theta, chi)
+  double rn, ro;         // rho(q-1, q) rho(q, q+1) with the new and the old orientation
+  int bad;
+};
+int launch_da_samples(const Ctx &c, const Frame *f, float *feat, float *energy, cudaStream_t s);
+int launch_da_propose(const Ctx &c, const Frame *f, int r, int parity, unsigned phase, uint64_t seed,
+                      const unsigned *pass, float *feat, DaMove *mv, cudaStream_t s);
+int launch_da_decide(const Ctx &c, Frame *f, int r, int parity, unsigned phase, uint64_t seed, const unsigned *pass,
+                     const float *y, int use_sur, float escale, const DaMove *mv, unsigned long long *stats,
+                     unsigned long long *cnt, cudaStream_t s);
+struct pimc_mlp;
+// the surrogate on device-resident rows, on stream s (pimc_mlp.cu)
+int mlp_forward_device(pimc_mlp *m, const float *x, int n, float *y, cudaStream_t s);
+
 // ------------------------------------------------------------ replica batches
 #define PIMC_BATCH_MAX_SEG 16         /* bisection segment of batched replicas (levels <= 4) */
 

@@ -833,6 +833,14 @@ extern "C" pimc_status pimc_mlp_train(pimc_mlp *m, int n, const float *x, const 
   return check_mlp_err(m);
 }
 
+int mlp_forward_device(pimc_mlp *m, const float *x, int n, float *y, cudaStream_t s)
+{
+  if (n <= 0) return 0;
+  MlpParams p = params_of(m);
+  k_mlp_forward<<<(n + kRows - 1) / kRows, kRows, kSmem, s>>>(p, x, n, y, m->err);
+  return 1;
+}
+
 extern "C" pimc_status pimc_mlp_forward(pimc_mlp *m, int n, const float *x, float *y)
 {
   if (!m || n < 0 || (n && (!x || !y))) return PIMC_ERR_BAD_ARG;

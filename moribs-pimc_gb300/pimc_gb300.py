@@ -69,6 +69,8 @@ def load(path=LIBPATH):
     L.pimc_mlp_get_params.argtypes = [vp, _fp]
     L.pimc_mlp_gradients.argtypes = [vp, C.c_int, _fp, _fp, _fp, _dp]
     L.pimc_mlp_train.argtypes = [vp, C.c_int, _fp, _fp, C.c_int, C.c_int, C.c_float, C.c_uint64, _dp]
+    L.pimc_da_samples.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(C.c_float)]
+    L.pimc_da_sweeps.argtypes = [vp, vp, C.c_int, C.c_uint64, C.c_float, C.c_int, _dp]
     L.pimc_linden.argtypes = [C.c_int, C.c_int, _dp, _ip, C.c_double, C.c_int, C.c_int, _dp]
     L.pimc_asymrho.argtypes = [C.c_int, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, _dp, C.c_int,
                                _dp, _dp, _dp, _dp]
@@ -242,6 +244,20 @@ class Sampler:
         _chk(self.L.pimc_molecular_move_exchange(self.h, int(type_), dptr(a), len(a), dptr(b), len(b), cons),
              "pimc_molecular_move_exchange")
         return (cons[0], cons[1])
+
+    # delayed acceptance with the surrogate (water dimer)
+    def da_samples(self):
+        f = np.zeros((self.P, 6), dtype=np.float32)
+        e = np.zeros(self.P, dtype=np.float32)
+        _chk(self.L.pimc_da_samples(self.h, f.ctypes.data_as(C.POINTER(C.c_float)),
+                                    e.ctypes.data_as(C.POINTER(C.c_float))), "pimc_da_samples")
+        return f, e
+
+    def da_sweeps(self, nsweeps, seed, mlp=None, escale=1.0):
+        st = np.zeros(4)
+        _chk(self.L.pimc_da_sweeps(self.h, mlp.h if mlp is not None else None, int(nsweeps), C.c_uint64(seed),
+                                   C.c_float(escale), 1 if mlp is not None else 0, dptr(st)), "pimc_da_sweeps")
+        return st
 
     # worm algorithm (mc_qworm.cc)
     WSTREAMS = ("n1", "n2", "n3", "u1", "u2", "u3", "u4", "u5", "gauss")
