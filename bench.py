@@ -54,6 +54,7 @@ def parse():
     ap.add_argument("--batched-replicas", type=int, default=4096)
     ap.add_argument("--no-tables", action="store_true", help="skip the propagator-table generator measurement")
     ap.add_argument("--no-worm", action="store_true", help="skip the worm-algorithm pass measurement")
+    ap.add_argument("--no-surrogate", action="store_true", help="skip the surrogate / delayed-acceptance measurement")
     return ap.parse_args()
 
 
@@ -500,6 +501,86 @@ def run_worm(local, cpu, steps=5, warmup=2):
     return out
 
 
+def run_surrogate(local, quick=False):
+    """North-star pattern (4) on config 3 (2 water-like tops, caleng, T 0.74 K,
+    P = 4096, Q = 2048): training data emitted by the plain sampler (dimer
+    features and exact caleng energies of every translational slice), the
+    surrogate MLP trained on the GPU by its tcgen05 kernels, then plain and
+    delayed-acceptance rotational sweeps timed with CUDA events.  Also the
+    surrogate's inference rate on a large batch against the tensor-core
+    peak."""
+    import numpy as np
+    import torch
+    import pimc_gb300 as G
+    import workloads as W
+    w = W.config3()
+    s = G.Sampler(w, device=local)
+    ext = torch.cuda.ExternalStream(s.stream(), device=torch.device("cuda", local))
+    s.da_sweeps(20, 11)
+    ncall = 64 if quick else 256
+    t0 = time.perf_counter()
+    xs, es = [], []
+    for k in range(ncall):
+        s.da_sweeps(2, 100 + k)
+        f, e = s.da_samples()
+        xs.append(f)
+        es.append(e)
+    t_collect = time.perf_counter() - t0
+    x, e = np.concatenate(xs), np.concatenate(es)
+    mu, sd = float(e.mean()), float(e.std())
+    nho = 16384
+    m = G.Mlp(device=local)
+    rng = np.random.default_rng(5)
+    m.set_weights(rng.normal(0, 1 / np.sqrt(6), (6, 256)), np.zeros(256), rng.normal(0, 1 / 16, (256, 256)),
+                  np.zeros(256), rng.normal(0, 1 / 16, (256, 256)), np.zeros(256), rng.normal(0, 1 / 16, 256), 0.0)
+    epochs = 8
+    t0 = time.perf_counter()
+    losses = m.train(x[:-nho], (e[:-nho] - mu) / sd, epochs=epochs, batch=4096, lr=1e-3, seed=6)
+    t_train = time.perf_counter() - t0
+    pred = m.forward(x[-nho:]) * sd + mu
+    rms = float(np.sqrt(np.mean((pred - e[-nho:]) ** 2)))
+
+    def timed(nsw, mlp):
+        with torch.cuda.stream(ext):
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(ext)
+            st = s.da_sweeps(nsw, 999, mlp=mlp, escale=sd)
+            b.record(ext)
+        s.synchronize()
+        torch.cuda.synchronize()
+        return a.elapsed_time(b), st
+
+    nsw = 20 if quick else 100
+    timed(5, None)
+    ms_plain, st_plain = timed(nsw, None)
+    timed(5, m)
+    ms_da, st_da = timed(nsw, m)
+    # inference rate of the tensor-core layers on one large batch
+    xb = np.tile(x[:8192], (64, 1))
+    m.forward(xb[:8192])
+    t0 = time.perf_counter()
+    m.forward(xb)
+    t_inf = time.perf_counter() - t0
+    flop_row = 2 * 2 * 256 * 256
+    out = {"workload": "config3: 2 water-like tops (A,B,C = 27.9, 14.5, 9.3 cm^-1), caleng, T=0.74 K, P=4096, Q=2048",
+           "training": {"samples": int(len(x) - nho), "collect_s": round(t_collect, 2), "epochs": epochs,
+                        "train_s": round(t_train, 2), "loss_first_last": [round(float(losses[0]), 4),
+                                                                          round(float(losses[-1]), 4)],
+                        "heldout_rms_K": round(rms, 2), "energy_std_K": round(sd, 2)},
+           "plain": {"moves_per_s": round(st_plain[0] / (ms_plain / 1e3), 1),
+                     "accept": round(st_plain[2] / st_plain[0], 4)},
+           "delayed_acceptance": {"moves_per_s": round(st_da[0] / (ms_da / 1e3), 1),
+                                  "stage1_pass": round(st_da[1] / st_da[0], 4),
+                                  "accept": round(st_da[2] / st_da[0], 4),
+                                  "exact_evals_per_move": round(st_da[3] / st_da[0], 4)},
+           "mlp_inference": {"rows": int(len(xb)), "s_end_to_end": round(t_inf, 4),
+                             "tensor_tflops_end_to_end": round(len(xb) * flop_row / t_inf / 1e12, 2)}}
+    m.close()
+    s.close()
+    return out
+
+
 def main():
     args = parse()
     rank, local, world = dist_env()
@@ -528,6 +609,8 @@ def main():
             line["tables"] = run_tables(local, not args.no_cpu)
         if not args.no_worm and world == 1:
             line["worm"] = run_worm(local, not args.no_cpu)
+        if not args.no_surrogate and world == 1:
+            line["surrogate"] = run_surrogate(local)
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.barrier()
