@@ -27,7 +27,7 @@ constexpr int kH = 256;               // hidden width (MMA N and K)
 constexpr int kIn = 6;                // input features
 constexpr int kA = kRows * kH * 2;    // A operand bytes (BF16)
 constexpr int kB = kH * kH * 2;       // B operand bytes
-constexpr int kSmem = kA + kB + 1024; // + barriers and the TMEM address
+constexpr int kSmem = kA + kB + 2048; // + barriers, the TMEM address and the half sums
 constexpr int kSmemT = kA + kB + 8192; // + the column-sum buffer of the training kernel
 // the parameter vector: w1[6][256], b1, w2[256][256], b2, w3[256][256], b3, w4, b4
 constexpr int kOW1 = 0, kOB1 = kOW1 + kIn * kH, kOW2 = kOB1 + kH, kOB2 = kOW2 + kH * kH, kOW3 = kOB2 + kH,
@@ -179,16 +179,23 @@ struct MlpParams {
   const float *b4;
 };
 
-// y[n] = MLP(x[n][0..5]); one CTA per 128 rows; err[0] |= 1 when a wait gave up
-__global__ void __launch_bounds__(kRows) k_mlp_forward(MlpParams p, const float *x, int n, float *y, unsigned *err)
+// y[n] = MLP(x[n][0..5]); one CTA of 256 threads per 128 rows: thread t
+// serves row t % 128 (TMEM lane quarter of its warp) and column half t / 128
+// of the CUDA-core layers and epilogues; err[0] |= 1 when a wait gave up
+constexpr int kFwdThreads = 256;
+
+__global__ void __launch_bounds__(kFwdThreads) k_mlp_forward(MlpParams p, const float *x, int n, float *y,
+                                                             unsigned *err)
 {
   extern __shared__ __align__(1024) char smem[];
   char *sA = smem, *sB = smem + kA;
   uint64_t *bar_w = (uint64_t *)(smem + kA + kB);
   uint64_t *bar_m = bar_w + 1;
   uint32_t *tslot = (uint32_t *)(bar_w + 2);
+  float *outp = (float *)(smem + kA + kB + 64);          // [256] half sums of the last layer
   const int tid = threadIdx.x, warp = tid >> 5;
-  const int row = blockIdx.x * kRows + tid;
+  const int r = tid & (kRows - 1), half = tid >> 7, c0 = half * (kH / 2);
+  const int row = blockIdx.x * kRows + r;
   if (tid == 0) {
     mbar_init(bar_w, 1);
     mbar_init(bar_m, 1);
@@ -203,37 +210,36 @@ __global__ void __launch_bounds__(kRows) k_mlp_forward(MlpParams p, const float 
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tslot;
-  const uint32_t tlane = tmem + ((uint32_t)(warp * 32) << 16);
+  const uint32_t tlane = tmem + ((uint32_t)((warp & 3) * 32) << 16);
   if (tid == 0) bulk_load(sB, p.w2c, kB, bar_w);
   // layer 1 on the CUDA cores, written as the A operand
   float xin[kIn];
   for (int i = 0; i < kIn; i++) xin[i] = row < n ? x[(size_t)row * kIn + i] : 0.0f;
-  for (int j = 0; j < kH; j += 2) {
+  for (int j = c0; j < c0 + kH / 2; j += 2) {
     float z0 = p.b1[j], z1 = p.b1[j + 1];
     for (int i = 0; i < kIn; i++) {
       z0 = fmaf(xin[i], p.w1[i * kH + j], z0);
       z1 = fmaf(xin[i], p.w1[i * kH + j + 1], z1);
     }
-    *(__nv_bfloat162 *)(sA + canon(tid, j)) = __floats2bfloat162_rn(silu(z0), silu(z1));
+    *(__nv_bfloat162 *)(sA + canon(r, j)) = __floats2bfloat162_rn(silu(z0), silu(z1));
   }
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-  __syncthreads();
-  bool ok = mbar_wait(bar_w, 0);
+  bool ok = __syncthreads_and(mbar_wait(bar_w, 0));
   unsigned ph = 0;
-  float out = *p.b4;
+  float out = 0.0f;
   for (int layer = 0; layer < 2 && ok; layer++) {
-    ok = gemm_128x256(tmem, sA, sB, bar_m, ph);
+    ok = __syncthreads_and(gemm_128x256(tmem, sA, sB, bar_m, ph));   // every thread saw the MMAs complete
     ph ^= 1u;
-    __syncthreads();                                   // every thread saw the MMAs complete
+    if (!ok) break;
     if (layer == 0 && tid == 0) bulk_load(sB, p.w3c, kB, bar_w);
     const float *bias = layer == 0 ? p.b2 : p.b3;
-    for (int c = 0; c < kH; c += 16) {
+    for (int c = c0; c < c0 + kH / 2; c += 16) {
       float v[16];
       tmem_ld16(tlane + c, v);
       if (layer == 0) {
 #pragma unroll
         for (int i = 0; i < 16; i += 2)
-          *(__nv_bfloat162 *)(sA + canon(tid, c + i)) =
+          *(__nv_bfloat162 *)(sA + canon(r, c + i)) =
               __floats2bfloat162_rn(silu(v[i] + bias[c + i]), silu(v[i + 1] + bias[c + i + 1]));
       } else {
 #pragma unroll
@@ -242,17 +248,16 @@ __global__ void __launch_bounds__(kRows) k_mlp_forward(MlpParams p, const float 
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    __syncthreads();
-    if (layer == 0) ok = ok && mbar_wait(bar_w, 1);
+    if (layer == 0) ok = __syncthreads_and(mbar_wait(bar_w, 1));
   }
   if (!ok && tid == 0) atomicOr(err, 1u);
-  if (row < n) y[row] = out;
+  outp[tid] = out;
   __syncthreads();
+  if (half == 0 && row < n) y[row] = (outp[r] + outp[r + kRows]) + *p.b4;
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   if (warp == 0)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kH) : "memory");
 }
-
 
 // ------------------------------------------------------------- training
 // D(tmem) = A[128 x K] . B[256 x K]^T, both K-major canonical with SBO =
@@ -837,7 +842,7 @@ int mlp_forward_device(pimc_mlp *m, const float *x, int n, float *y, cudaStream_
 {
   if (n <= 0) return 0;
   MlpParams p = params_of(m);
-  k_mlp_forward<<<(n + kRows - 1) / kRows, kRows, kSmem, s>>>(p, x, n, y, m->err);
+  k_mlp_forward<<<(n + kRows - 1) / kRows, kFwdThreads, kSmem, s>>>(p, x, n, y, m->err);
   return 1;
 }
 
@@ -850,7 +855,7 @@ extern "C" pimc_status pimc_mlp_forward(pimc_mlp *m, int n, const float *x, floa
   if (st) return st;
   MCK(cudaMemcpyAsync(m->xbuf, x, (size_t)n * kIn * sizeof(float), cudaMemcpyHostToDevice, m->stream));
   MlpParams p = params_of(m);
-  k_mlp_forward<<<(n + kRows - 1) / kRows, kRows, kSmem, m->stream>>>(p, m->xbuf, n, m->ybuf, m->err);
+  k_mlp_forward<<<(n + kRows - 1) / kRows, kFwdThreads, kSmem, m->stream>>>(p, m->xbuf, n, m->ybuf, m->err);
   MCK(cudaGetLastError());
   MCK(cudaMemcpyAsync(y, m->ybuf, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, m->stream));
   MCK(cudaStreamSynchronize(m->stream));
