@@ -177,6 +177,10 @@ pimc_status pimc_mlp_set_weights(pimc_mlp *m, const float *w1, const float *b1, 
                                  const float *w3, const float *b3, const float *w4, float b4);
 /* y[i] = MLP(x[i*6 .. i*6+5]) for n inputs (host buffers) */
 pimc_status pimc_mlp_forward(pimc_mlp *m, int n, const float *x, float *y);
+/* the forward kernel again on the n rows the last pimc_mlp_forward uploaded
+ * (outputs stay on the device), on the stream pimc_mlp_stream returns */
+pimc_status pimc_mlp_forward_resident(pimc_mlp *m, int n);
+void       *pimc_mlp_stream(const pimc_mlp *m);
 /* The parameter vector: w1[6*256], b1[256], w2[256*256], b2[256],
  * w3[256*256], b3[256], w4[256], b4 (pimc_mlp_param_count() floats). */
 int         pimc_mlp_param_count(void);

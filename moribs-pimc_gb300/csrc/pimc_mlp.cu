@@ -152,7 +152,9 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float v[16])
   for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
 }
 
-__device__ __forceinline__ float silu(float z) { return z / (1.0f + __expf(-z)); }
+// SiLU and its derivative with the fast exponential and division (the
+// surrogate is BF16 throughout; 2-ulp FP32 activations are far below that)
+__device__ __forceinline__ float silu(float z) { return __fdividef(z, 1.0f + __expf(-z)); }
 
 // D[128 x 256] (TMEM) = A[128 x 256] . B[256 x 256]^T from shared memory,
 // sixteen K=16 steps issued by thread 0, completion on bar (phase `ph`)
@@ -295,7 +297,7 @@ __device__ __forceinline__ bool gemm_dw(uint32_t tmem, const char *sA, const cha
 
 __device__ __forceinline__ float dsilu(float z)
 {
-  float s = 1.0f / (1.0f + __expf(-z));
+  float s = __fdividef(1.0f, 1.0f + __expf(-z));
   return s * (1.0f + z * (1.0f - s));
 }
 
@@ -845,6 +847,19 @@ int mlp_forward_device(pimc_mlp *m, const float *x, int n, float *y, cudaStream_
   k_mlp_forward<<<(n + kRows - 1) / kRows, kFwdThreads, kSmem, s>>>(p, x, n, y, m->err);
   return 1;
 }
+
+// the forward kernel again on the rows the last pimc_mlp_forward uploaded,
+// on the surrogate's stream, results left on the device (kernel timing)
+extern "C" pimc_status pimc_mlp_forward_resident(pimc_mlp *m, int n)
+{
+  if (!m || n <= 0 || (size_t)n > m->cap) return PIMC_ERR_BAD_ARG;
+  MCK(cudaSetDevice(m->device));
+  mlp_forward_device(m, m->xbuf, n, m->ybuf, m->stream);
+  MCK(cudaGetLastError());
+  return PIMC_OK;
+}
+
+extern "C" void *pimc_mlp_stream(const pimc_mlp *m) { return m ? (void *)m->stream : nullptr; }
 
 extern "C" pimc_status pimc_mlp_forward(pimc_mlp *m, int n, const float *x, float *y)
 {

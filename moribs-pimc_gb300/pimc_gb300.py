@@ -65,6 +65,9 @@ def load(path=LIBPATH):
     _fp = C.POINTER(C.c_float)
     L.pimc_mlp_set_weights.argtypes = [vp, _fp, _fp, _fp, _fp, _fp, _fp, _fp, C.c_float]
     L.pimc_mlp_forward.argtypes = [vp, C.c_int, _fp, _fp]
+    L.pimc_mlp_forward_resident.argtypes = [vp, C.c_int]
+    L.pimc_mlp_stream.restype = vp
+    L.pimc_mlp_stream.argtypes = [vp]
     L.pimc_mlp_param_count.restype = C.c_int
     L.pimc_mlp_get_params.argtypes = [vp, _fp]
     L.pimc_mlp_gradients.argtypes = [vp, C.c_int, _fp, _fp, _fp, _dp]
@@ -511,6 +514,12 @@ class Mlp:
         y = np.zeros(len(x), dtype=np.float32)
         _chk(self.L.pimc_mlp_forward(self.h, len(x), _fptr(x), _fptr(y)), "pimc_mlp_forward")
         return y
+
+    def forward_resident(self, n):
+        _chk(self.L.pimc_mlp_forward_resident(self.h, int(n)), "pimc_mlp_forward_resident")
+
+    def stream(self):
+        return self.L.pimc_mlp_stream(self.h)
 
     def params(self):
         p = np.zeros(self.L.pimc_mlp_param_count(), dtype=np.float32)
