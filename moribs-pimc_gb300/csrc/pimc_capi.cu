@@ -1272,6 +1272,7 @@ extern "C" pimc_status pimc_da_sweeps(pimc_handle *h, pimc_mlp *m, int nsweeps, 
   unsigned long long hs[4];
   CK(cudaMemcpyAsync(hs, st, sizeof(hs), cudaMemcpyDeviceToHost, h->stream));
   e = check_err(h);
+  if (!e && use_surrogate && mlp_take_error(m)) e = PIMC_ERR_TIMEOUT;
   if (stats)
     for (int k = 0; k < 4; k++) stats[k] = (double)hs[k];
   return e;

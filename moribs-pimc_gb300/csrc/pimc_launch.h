@@ -68,6 +68,7 @@ int launch_da_decide(const Ctx &c, Frame *f, int r, int parity, unsigned phase, 
 struct pimc_mlp;
 // the surrogate on device-resident rows, on stream s (pimc_mlp.cu)
 int mlp_forward_device(pimc_mlp *m, const float *x, int n, float *y, cudaStream_t s);
+bool mlp_take_error(pimc_mlp *m);
 
 // ------------------------------------------------------------ replica batches
 #define PIMC_BATCH_MAX_SEG 16         /* bisection segment of batched replicas (levels <= 4) */

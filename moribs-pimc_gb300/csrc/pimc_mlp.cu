@@ -861,6 +861,15 @@ extern "C" pimc_status pimc_mlp_forward_resident(pimc_mlp *m, int n)
 
 extern "C" void *pimc_mlp_stream(const pimc_mlp *m) { return m ? (void *)m->stream : nullptr; }
 
+// whether a surrogate launch gave up a wait since the last call (clears it)
+bool mlp_take_error(pimc_mlp *m)
+{
+  unsigned e = 0;
+  if (cudaMemcpy(&e, m->err, sizeof(unsigned), cudaMemcpyDeviceToHost) != cudaSuccess) return true;
+  if (e) cudaMemset(m->err, 0, sizeof(unsigned));
+  return e != 0;
+}
+
 extern "C" pimc_status pimc_mlp_forward(pimc_mlp *m, int n, const float *x, float *y)
 {
   if (!m || n < 0 || (n && (!x || !y))) return PIMC_ERR_BAD_ARG;
