@@ -55,6 +55,8 @@ def parse():
     ap.add_argument("--no-tables", action="store_true", help="skip the propagator-table generator measurement")
     ap.add_argument("--no-worm", action="store_true", help="skip the worm-algorithm pass measurement")
     ap.add_argument("--no-surrogate", action="store_true", help="skip the surrogate / delayed-acceptance measurement")
+    ap.add_argument("--only", default=None, choices=["tables", "worm", "surrogate"],
+                    help="run one companion measurement alone on cuda:0 and print its JSON (for profiling)")
     return ap.parse_args()
 
 
@@ -630,6 +632,13 @@ def main():
                 "cpu_baseline": {"value": rate, "unit": UNIT, "cores": ncores, "kind": "port", "sample": sample},
                 "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
+        return 0
+    if args.only is not None:
+        if rank == 0:
+            run = {"tables": lambda: run_tables(local, not args.no_cpu),
+                   "worm": lambda: run_worm(local, not args.no_cpu, steps=args.steps, warmup=args.warmup),
+                   "surrogate": lambda: run_surrogate(local)}[args.only]
+            print(json.dumps({"part": args.only, **run()}), flush=True)
         return 0
     line, w = run_gb300(args, rank, local, world, dist)
     if rank == 0:

@@ -19,6 +19,9 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
 constexpr int kMaxQ = 2 * (PIMC_WORM_MAXM + 1);   // the swap's new and old slices
+#define PIMC_MAXNEIGHBORS 100                     // MAXNEIGHBORS (mc_qworm.cc:12)
+constexpr int kTermCap = 3072;                    // (query, partner) terms held in shared memory
+constexpr int kDrawCap = 32;                      // draws of each uniform stream held in shared memory
 
 struct WormShared {
   int exists, ira, masha, atom_i, atom_m;   // the worm (TPathWorm)
@@ -27,10 +30,27 @@ struct WormShared {
   int qa[kMaxQ], qpit[kMaxQ];                // global atom and slice of each
   double qx[kMaxQ], qy[kMaxQ], qz[kMaxQ];    // the bead the atom sits on
   double qsum[kMaxQ];
-  int stack[4 * 32];                         // sample_middle's recursion
+  int stack[4];                              // the swap's accepted segment (it0, atomw, a0)
+  int b_it0, b_len, b_a0, b_a2;              // the bridge bridge_block builds
+  int adv, advance;                          // the advance/recede branch and its length
   long gbase;                                // first gauss() draw of the current bridge
   int gneed;                                 // its number of draws
   double gz[3 * (PIMC_WORM_MAXM + 1)];       // the draws, generated by all threads
+  // bridge coefficients by segment length and split (s0 = len/2 or len - len/2):
+  // the midpoint is bca r0 + bcb r2 + bcs g, i.e. (s2 r0 + s0 r2)/(s0 + s2)
+  // + g / sqrt(gkin) of sample_middle (mc_qworm.cc:268-276)
+  double bca[2][PIMC_WORM_MAXM + 2], bcb[2][PIMC_WORM_MAXM + 2], bcs[2][PIMC_WORM_MAXM + 2];
+  double sqadv[PIMC_WORM_MAXM + 1];          // 1/sqrt(gvar) of qworm_advance (mc_qworm.cc:324-330)
+  double pw15[PIMC_WORM_MAXM + 1];           // segm^(NDIM/2) of qw_open_prob (mc_qworm.cc:152)
+  double sg3[3 * (PIMC_WORM_MAXM + 1)];      // a bridge's beads it0..it2 (newcoords)
+  int qmode, qt0, qt1, qa0, qa1;             // the queries fill_queries builds
+  int pw_atom, pw_pt0, pw_pt1, pw_segm, pw_t1; // the arguments of get_ptable
+  int pcount;                                // candidates of the neighbour table
+  double ptd[PIMC_MAXNEIGHBORS + 1], ptab[PIMC_MAXNEIGHBORS + 1];
+  int pta[PIMC_MAXNEIGHBORS + 1];
+  double qwtot[7], qwacc[7];                 // the worm's try/accept counters
+  double term[kTermCap];                     // the (query, partner) terms of query_sums
+  double dc[8 * kDrawCap];                   // the first draws of the uniform streams
 };
 
 struct WormSrc {
@@ -40,6 +60,7 @@ struct WormSrc {
   unsigned *err;
   // one draw of stream k: 0..2 nrnd1..3, 3..7 rnd1..5, 8 gauss's x1
   __device__ void init() {}
+  __device__ void fill(double *) const {}
   __device__ long gbase() const { return pos[8]; }
   __device__ double gauss_at(long i) const
   {
@@ -62,17 +83,26 @@ struct WormSrc {
   }
 };
 
-// the production draws: Philox keyed by (seed, pass, phase, stream k, count)
+// the production draws: Philox keyed by (seed, pass, phase, stream k, count).
+// The first kDrawCap draws of streams 0..7 are generated by all threads at
+// the start of the call (a call of N tries takes at most 2N from any one of
+// them) so that thread 0's chain reads them from shared memory.
 struct WormPhilox {
   uint64_t seed;
   const unsigned *pass;
   unsigned phase;
   uint64_t move;
   unsigned cnt[9];
+  const double *cache;
   __device__ void init()
   {
     move = ((uint64_t)(*pass) << 32) | ((uint64_t)phase << 12) | 0xFFFu;
     for (int k = 0; k < 9; k++) cnt[k] = 0;
+  }
+  __device__ void fill(double *buf)
+  {
+    for (int i = threadIdx.x; i < 8 * kDrawCap; i += blockDim.x) buf[i] = draw(i / kDrawCap, (unsigned)(i % kDrawCap));
+    cache = buf;
   }
   __device__ double draw(int k, unsigned n) const
   {
@@ -81,7 +111,11 @@ struct WormPhilox {
     if (k == 8) return sqrt(-log(u0)) * cos(2.0 * PIMC_PI * u1);   // gauss()'s x1 (mc_randg.cc:144)
     return u0;
   }
-  __device__ double take(int k) { return draw(k, cnt[k]++); }
+  __device__ double take(int k)
+  {
+    const unsigned n = cnt[k]++;
+    return n < (unsigned)kDrawCap ? cache[k * kDrawCap + n] : draw(k, n);
+  }
   __device__ long gbase() const { return cnt[8]; }
   __device__ double gauss_at(long i) const { return draw(8, (unsigned)i); }
   __device__ void gskip(long k) { cnt[8] += (unsigned)k; }
@@ -104,19 +138,38 @@ __device__ __forceinline__ bool world_line(const WormShared &sh, int a, int pt)
   return wline;
 }
 
-// PotEnergy(qa[q], bead q, qpit[q]) for every query, one warp per query,
-// partners in a fixed per-lane order and a fixed shuffle tree
+// PotEnergy(qa[q], bead q, qpit[q]) for every query (mc_piqmc.cc:1201-1383).
+// When the (query, partner) terms fit the shared buffer they are spread
+// one per thread over the whole CTA (a warp per query would leave most
+// lanes idle: a slice has few partners) and each query's terms are then
+// summed in the partners' order; otherwise one warp per query, partners
+// in a fixed per-lane order and a fixed shuffle tree.
+__device__ __noinline__ double query_term(const Ctx &c, const Frame *frames, const DevWorm &wk,
+                                             const WormShared &sh, int q, int a1)
+{
+  const int a0 = sh.qa[q], it = sh.qpit[q];
+  if (a1 == a0) return 0.0;
+  if (sh.exists && atom_type(c.s, a1) == wk.type && !world_line(sh, a1 - wk.first, it)) return 0.0;
+  return pair_term64(c, frames, a0, a1, it, sh.qx[q], sh.qy[q], sh.qz[q]);
+}
+
 __device__ void query_sums(const Ctx &c, const Frame *frames, const DevWorm &wk, WormShared &sh)
 {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int q = warp; q < sh.nq; q += kWarps) {
-    int a0 = sh.qa[q], it = sh.qpit[q];
-    double acc = 0.0;
-    for (int a1 = lane; a1 < c.s.na; a1 += 32) {
-      if (a1 == a0) continue;
-      if (sh.exists && atom_type(c.s, a1) == wk.type && !world_line(sh, a1 - wk.first, it)) continue;
-      acc += pair_term64(c, frames, a0, a1, it, sh.qx[q], sh.qy[q], sh.qz[q]);
+  const int na = c.s.na, nq = sh.nq;
+  if (nq * na <= kTermCap) {
+    for (int k = threadIdx.x; k < nq * na; k += kThreads) sh.term[k] = query_term(c, frames, wk, sh, k / na, k % na);
+    __syncthreads();
+    for (int q = threadIdx.x; q < nq; q += kThreads) {
+      double acc = 0.0;
+      for (int a1 = 0; a1 < na; a1++) acc += sh.term[q * na + a1];
+      sh.qsum[q] = acc;
     }
+    return;
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int q = warp; q < nq; q += kWarps) {
+    double acc = 0.0;
+    for (int a1 = lane; a1 < na; a1 += 32) acc += query_term(c, frames, wk, sh, q, a1);
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
     if (lane == 0) sh.qsum[q] = acc;
   }
@@ -124,26 +177,40 @@ __device__ void query_sums(const Ctx &c, const Frame *frames, const DevWorm &wk,
 
 __device__ __forceinline__ size_t bead(const Ctx &c, int gatom, int pit) { return sidx(c.s, pit, gatom); }
 
-// the queries of get_potential(it0, it1, atom0, atom1, MCCoords)
-__device__ void potential_queries(const Ctx &c, const DevWorm &wk, WormShared &sh, int it0, int it1, int atom0,
-                                  int atom1)
+// The queries of a potential sum, filled by all threads from the
+// description thread 0 left in sh.qmode/qt0/qt1/qa0/qa1.  Mode 0 and 1:
+// get_potential(it0, it1, atom0, atom1, coords) (mc_qworm.cc:402-422), one
+// query per inner slice, the bead on atom1 past the ring's end; mode 0 reads
+// the path, mode 1 the bridge just built in sh.sg3 (based at it0).  Mode 2:
+// the swap's new and old bead of every inner slice, in that order
+// (mc_qworm.cc:470-486).
+__device__ void fill_queries(const Ctx &c, const DevWorm &wk, WormShared &sh)
 {
-  const int P = c.s.P;
-  int pit0 = it0 % P;
-  int atom = atom0, nq = 0;
-  for (int it = it0 + 1; it < it1; it++) {
-    int pit = it % P;
-    if ((pit != it) && (pit0 == it0)) atom = atom1;
-    int g = wk.first + atom;
-    size_t i = bead(c, g, pit);
-    sh.qa[nq] = g;
-    sh.qpit[nq] = pit;
-    sh.qx[nq] = c.st.x[i];
-    sh.qy[nq] = c.st.y[i];
-    sh.qz[nq] = c.st.z[i];
-    nq++;
+  const int P = c.s.P, it0 = sh.qt0, mode = sh.qmode;
+  const int n = max(0, sh.qt1 - it0 - 1);
+  const bool w0 = (it0 % P) == it0;
+  for (int j = threadIdx.x; j < n; j += kThreads) {
+    const int it = it0 + 1 + j, pit = it % P;
+    const int g = wk.first + (((pit != it) && w0) ? sh.qa1 : sh.qa0);
+    const size_t i = bead(c, g, pit);
+    const double *b = sh.sg3 + 3 * (it - it0);
+    if (mode == 2) {
+      sh.qa[2 * j] = g; sh.qpit[2 * j] = pit;
+      sh.qx[2 * j] = b[0]; sh.qy[2 * j] = b[1]; sh.qz[2 * j] = b[2];
+      sh.qa[2 * j + 1] = g; sh.qpit[2 * j + 1] = pit;
+      sh.qx[2 * j + 1] = c.st.x[i]; sh.qy[2 * j + 1] = c.st.y[i]; sh.qz[2 * j + 1] = c.st.z[i];
+    } else {
+      sh.qa[j] = g; sh.qpit[j] = pit;
+      if (mode == 1) { sh.qx[j] = b[0]; sh.qy[j] = b[1]; sh.qz[j] = b[2]; }
+      else { sh.qx[j] = c.st.x[i]; sh.qy[j] = c.st.y[i]; sh.qz[j] = c.st.z[i]; }
+    }
   }
-  sh.nq = nq;
+  if (threadIdx.x == 0) sh.nq = mode == 2 ? 2 * n : n;
+}
+
+__device__ __forceinline__ void set_queries(WormShared &sh, int mode, int it0, int it1, int atom0, int atom1)
+{
+  sh.qmode = mode; sh.qt0 = it0; sh.qt1 = it1; sh.qa0 = atom0; sh.qa1 = atom1;
 }
 
 __device__ double potential_total(const WormShared &sh)
@@ -153,46 +220,74 @@ __device__ double potential_total(const WormShared &sh)
   return pot;
 }
 
-// sample_middle(it0, it2, atom0, atom2, coords) on thread 0: the
-// reference's recursion (middle bead, then the left half, then the right
-// half) with an explicit stack.  seg != nullptr writes the segment copy
-// seg[3][it - base] (newcoords of the swap) instead of the path.
-__device__ void sample_middle(const Ctx &c, const DevWorm &wk, WormShared &sh, int &gi, int it0, int it2,
-                              int atom0, int atom2, double *seg, int base)
+// rint(0.5 (t0 + t2)) of sample_middle (mc_qworm.cc:245) in integers:
+// a half rounds to the even neighbour
+__device__ __forceinline__ int bridge_split(int t0, int t2)
 {
-  const int P = c.s.P;
-  int sp = 0;
-  sh.stack[sp++] = it0; sh.stack[sp++] = it2; sh.stack[sp++] = atom0; sh.stack[sp++] = atom2;
-  while (sp > 0) {
-    int a2 = sh.stack[--sp], a0 = sh.stack[--sp], t2 = sh.stack[--sp], t0 = sh.stack[--sp];
-    if ((t2 - t0) < 2) continue;
-    int t1 = (int)rint(0.5 * (double)(t0 + t2));
-    int p0 = t0 % P, p1 = t1 % P, p2 = t2 % P;
-    int a1 = a0;
-    if ((p1 != t1) && (p0 == t0)) a1 = a2;
-    double s0 = (double)(t1 - t0), s2 = (double)(t2 - t1);
-    double gkin = (s0 + s2) / (wk.twave2 * s0 * s2);
-    double r0[3], r2[3], r1[3];
-    if (seg) {
-      for (int d = 0; d < 3; d++) { r0[d] = seg[3 * (t0 - base) + d]; r2[d] = seg[3 * (t2 - base) + d]; }
-    } else {
-      size_t i0 = bead(c, wk.first + a0, p0), i2 = bead(c, wk.first + a2, p2);
-      r0[0] = c.st.x[i0]; r0[1] = c.st.y[i0]; r0[2] = c.st.z[i0];
-      r2[0] = c.st.x[i2]; r2[1] = c.st.y[i2]; r2[2] = c.st.z[i2];
+  const int sum = t0 + t2, h = sum >> 1;
+  return (sum & 1) && (h & 1) ? h + 1 : h;
+}
+
+// sample_middle(it0, it2, atom0, atom2, coords) (mc_qworm.cc:238-283) by all
+// threads, for the bridge thread 0 left in sh.b_* with its end beads in
+// sh.sg3[0] and sh.sg3[3 len].  The reference's recursion takes the middle
+// bead, then the left half, then the right half, drawing three gauss()
+// values per middle bead; the bead that is the middle of the sub-interval
+// (lo, hi) is therefore the k-th drawn, k its pre-order index (the left
+// child of node k is k + 1, the right one k + mid - lo).  Each thread takes
+// one coordinate of one inner bead, finds its sub-interval by descending
+// from (0, len), and the beads are built level by level:
+// (s2 r_lo + s0 r_hi)/(s0 + s2) + g sqrt(twave2 s0 s2/(s0 + s2)), s0 = mid - lo,
+// s2 = hi - mid, from the per-length coefficient table.  The draws start at
+// sh.gz[goff].  to_path writes the inner beads to the path, the ones past the
+// ring's end on atom2.
+__device__ void bridge_block(const Ctx &c, const DevWorm &wk, WormShared &sh, int goff, bool to_path)
+{
+  const int it0 = sh.b_it0, len = sh.b_len;
+  const int j = threadIdx.x, t = 1 + j / 3, d = j % 3;
+  const bool mine = j < 3 * (len - 1);
+  int lo = 0, hi = len, mid = 0, k = 0, depth = 0;
+  if (mine) {
+    for (;;) {
+      mid = bridge_split(it0 + lo, it0 + hi) - it0;
+      if (t == mid) break;
+      if (t < mid) { hi = mid; k += 1; }
+      else { k += mid - lo; lo = mid; }
+      depth++;
     }
-    for (int d = 0; d < 3; d++) {
-      r1[d] = (s2 * r0[d] + s0 * r2[d]) / (s0 + s2);
-      r1[d] += sh.gz[gi++] / sqrt(gkin);                 // gauss(gkin), mc_randg.cc:149
-    }
-    if (seg) {
-      for (int d = 0; d < 3; d++) seg[3 * (t1 - base) + d] = r1[d];
-    } else {
-      store_bead(c, bead(c, wk.first + a1, p1), r1[0], r1[1], r1[2]);
-    }
-    // right half below the left one: the left half is taken first
-    sh.stack[sp++] = t1; sh.stack[sp++] = t2; sh.stack[sp++] = a1; sh.stack[sp++] = a2;
-    sh.stack[sp++] = t0; sh.stack[sp++] = t1; sh.stack[sp++] = a0; sh.stack[sp++] = a1;
   }
+  for (int lev = 0;; lev++) {
+    if (mine && depth == lev) {
+      const int ln = hi - lo, w = (mid - lo == (ln >> 1)) ? 0 : 1;
+      sh.sg3[3 * t + d] = fma(sh.bcs[w][ln], sh.gz[goff + 3 * k + d],
+                              sh.bca[w][ln] * sh.sg3[3 * lo + d] + sh.bcb[w][ln] * sh.sg3[3 * hi + d]);
+    }
+    if (!__syncthreads_or(mine && depth > lev)) break;
+  }
+  if (to_path) {
+    const int P = c.s.P;
+    const bool w0 = (it0 % P) == it0;
+    for (int b = 1 + threadIdx.x; b < len; b += kThreads) {
+      const int it = it0 + b, pit = it % P, a = ((pit != it) && w0) ? sh.b_a2 : sh.b_a0;
+      const double *r = sh.sg3 + 3 * b;
+      store_bead(c, bead(c, wk.first + a, pit), r[0], r[1], r[2]);
+    }
+  }
+}
+
+// thread 0: the end beads of a bridge of the path from (atom0, it0) to
+// (atom2, it2), the far one copied from the path unless the caller set it
+__device__ void bridge_ends(const Ctx &c, const DevWorm &wk, WormShared &sh, int it0, int it2, int atom0, int atom2,
+                            bool have_end)
+{
+  const int P = c.s.P, len = it2 - it0;
+  const size_t i0 = bead(c, wk.first + atom0, it0 % P);
+  sh.sg3[0] = c.st.x[i0]; sh.sg3[1] = c.st.y[i0]; sh.sg3[2] = c.st.z[i0];
+  if (!have_end) {
+    const size_t i2 = bead(c, wk.first + atom2, it2 % P);
+    sh.sg3[3 * len] = c.st.x[i2]; sh.sg3[3 * len + 1] = c.st.y[i2]; sh.sg3[3 * len + 2] = c.st.z[i2];
+  }
+  sh.b_it0 = it0; sh.b_len = len; sh.b_a0 = atom0; sh.b_a2 = atom2;
 }
 
 // the kinetic part of qw_open_prob (mc_qworm.cc:131-144) on thread 0
@@ -209,50 +304,54 @@ __device__ double open_kin(const Ctx &c, const DevWorm &wk, const WormShared &sh
   return kin / (wk.twave2 * (double)segm);
 }
 
-// get_ptable (mc_qworm.cc:577-642) on thread 0 into the scratch lists
-// dr2[1..count], atm[1..count], ptab[1..count]
-__device__ int get_ptable(const Ctx &c, const DevWorm &wk, const WormShared &sh, const int *rindex, int atomw,
-                          int pt0, int pt1, int segm, int t1, double *dr2l, int *atml, double *ptab)
+// GetPTable (mc_qworm.cc:577-617) by all threads, with the arguments thread
+// 0 left in sh.pw_*: every atom's squared distance to the worm bead in
+// parallel (dall[a], -1 when the atom is no candidate), then each
+// candidate's place in the stable order by distance -- the order mmsort's
+// insertion sort gives (mc_utils.cc:206-230) -- as its rank; the first
+// MAXNEIGHBORS go to sh.ptd/pta/ptab[1..] and sh.pcount holds the number of
+// candidates.
+__device__ void get_ptable(const Ctx &c, const DevWorm &wk, WormShared &sh, const int *rindex, double *dall)
 {
-  size_t iw = bead(c, wk.first + atomw, pt0);
-  double rw[3] = {c.st.x[iw], c.st.y[iw], c.st.z[iw]};
-  int count = 0;
-  for (int a1 = 0; a1 < wk.numb; a1++)
+  const int atomw = sh.pw_atom, pt0 = sh.pw_pt0, pt1 = sh.pw_pt1, segm = sh.pw_segm, t1 = sh.pw_t1;
+  const size_t iw = bead(c, wk.first + atomw, pt0);
+  const double rw[3] = {c.st.x[iw], c.st.y[iw], c.st.z[iw]};
+  for (int a1 = threadIdx.x; a1 < wk.numb; a1 += kThreads) {
+    double v = -1.0;
     if (world_line(sh, a1, pt1)) {
       int a0 = a1;
       if (t1 != pt1) a0 = rindex[a1];
       if (a0 != sh.atom_i) {
-        size_t i1 = bead(c, wk.first + a1, pt1);
-        double r1[3] = {c.st.x[i1], c.st.y[i1], c.st.z[i1]};
+        const size_t i1 = bead(c, wk.first + a1, pt1);
+        const double r1[3] = {c.st.x[i1], c.st.y[i1], c.st.z[i1]};
         double dr2 = 0.0;
         for (int d = 0; d < 3; d++) {
           double dx = rw[d] - r1[d];
           if (c.s.minimage) dx -= (c.s.box[d] * rint(dx / c.s.box[d]));
           dr2 += (dx * dx);
         }
-        if (dr2 < wk.cut2) {
-          count++;
-          dr2l[count] = dr2;
-          atml[count] = a1;
-        }
+        if (dr2 < wk.cut2) v = dr2;
       }
     }
-  for (int j = 2; j <= count; j++) {   // mmsort (mc_utils.cc:206-230)
-    double dt = dr2l[j];
-    int it = atml[j];
-    int i = j - 1;
-    while ((i > 0) && (dr2l[i] > dt)) {
-      dr2l[i + 1] = dr2l[i];
-      atml[i + 1] = atml[i];
-      i--;
-    }
-    dr2l[i + 1] = dt;
-    atml[i + 1] = it;
+    dall[a1] = v;
   }
-  if (count > 100) count = 100;        // MAXNEIGHBORS (mc_qworm.cc:12)
-  double norm = 1.0 / ((double)segm * wk.twave2);
-  for (int ic = 1; ic <= count; ic++) ptab[ic] = exp(-norm * dr2l[ic]);
-  return count;
+  __syncthreads();
+  for (int a = threadIdx.x; a < wk.numb; a += kThreads) {
+    const double d = dall[a];
+    if (d < 0.0) continue;
+    atomicAdd(&sh.pcount, 1);
+    int r = 0;
+    for (int b = 0; b < wk.numb; b++) {
+      const double e = dall[b];
+      r += (e >= 0.0) && (e < d || (e == d && b < a));
+    }
+    if (r < PIMC_MAXNEIGHBORS) { sh.ptd[r + 1] = d; sh.pta[r + 1] = a; }
+  }
+  __syncthreads();
+  const int count = min(sh.pcount, PIMC_MAXNEIGHBORS);
+  const double norm = 1.0 / ((double)segm * wk.twave2);
+  for (int ic = 1 + threadIdx.x; ic <= count; ic += kThreads) sh.ptab[ic] = exp(-norm * sh.ptd[ic]);
+  __syncthreads();
 }
 
 // gauss() draws gbase .. gbase+gneed-1 of the next bridge, one per thread
@@ -267,8 +366,7 @@ __device__ __forceinline__ void prefetch_gauss(const Src &src, WormShared &sh)
 
 template <class Src>
 __global__ void __launch_bounds__(kThreads) k_worm_move(Ctx c, Frame *frames, DevWorm *wkp, int *rindex,
-                                                       Src src, double *seg, double *dr2l, int *atml,
-                                                       double *ptab)
+                                                       Src src, double *dall)
 {
   __shared__ WormShared sh;
   __shared__ double pnorm_old;
@@ -276,9 +374,28 @@ __global__ void __launch_bounds__(kThreads) k_worm_move(Ctx c, Frame *frames, De
   const int P = c.s.P;
   const bool t0 = threadIdx.x == 0;
   src.init();
+  src.fill(sh.dc);
+  for (int i = threadIdx.x; i < 2 * (PIMC_WORM_MAXM + 2); i += kThreads) {
+    const int w = i / (PIMC_WORM_MAXM + 2), len = i % (PIMC_WORM_MAXM + 2);
+    if (len >= 2) {
+      const double s0 = (double)(w ? len - (len >> 1) : (len >> 1)), s2 = (double)len - s0;
+      const double gkin = (s0 + s2) / (wk.twave2 * s0 * s2);
+      sh.bca[w][len] = s2 / (s0 + s2);
+      sh.bcb[w][len] = s0 / (s0 + s2);
+      sh.bcs[w][len] = 1.0 / sqrt(gkin);
+    }
+  }
+  for (int i = threadIdx.x; i <= PIMC_WORM_MAXM; i += kThreads) {
+    sh.sqadv[i] = i > 0 ? 1.0 / sqrt(1.0 / ((double)i * wk.twave2)) : 0.0;
+    sh.pw15[i] = (double)i * sqrt((double)i);
+  }
+  if (threadIdx.x < 7) {
+    sh.qwtot[threadIdx.x] = wk.qwtot[threadIdx.x];
+    sh.qwacc[threadIdx.x] = wk.qwacc[threadIdx.x];
+  }
   if (t0) {
-    sh.exists = wkp->exists; sh.ira = wkp->ira; sh.masha = wkp->masha;
-    sh.atom_i = wkp->atom_i; sh.atom_m = wkp->atom_m;
+    sh.exists = wk.exists; sh.ira = wk.ira; sh.masha = wk.masha;
+    sh.atom_i = wk.atom_i; sh.atom_m = wk.atom_m;
   }
   __syncthreads();
   const bool bose = c.s.stat[wk.type] == 1;      // PIMC_BOSE (pimc_types.h)
@@ -288,7 +405,7 @@ __global__ void __launch_bounds__(kThreads) k_worm_move(Ctx c, Frame *frames, De
     if (t0) {
       sh.gneed = 0;
       if (sh.exists) {
-        wkp->qwtot[1] += 1.0;
+        sh.qwtot[1] += 1.0;
         segm = sh.masha - sh.ira;
         if (segm < 0) segm += P;
         sh.flag = segm > wk.m ? 0 : 1;
@@ -297,16 +414,17 @@ __global__ void __launch_bounds__(kThreads) k_worm_move(Ctx c, Frame *frames, De
       }
     }
     prefetch_gauss(src, sh);
-    if (t0) {
-      if (sh.exists) {
-        if (sh.flag) {
-          int gi = 0;
-          src.gskip(sh.gneed);
-          sample_middle(c, wk, sh, gi, sh.ira, sh.ira + segm, sh.atom_i, sh.atom_m, nullptr, 0);
-          potential_queries(c, wk, sh, sh.ira, sh.ira + segm, sh.atom_i, sh.atom_m);
-        }
-      } else {
-        wkp->qwtot[0] += 1.0;
+    if (sh.exists && sh.flag) {          // close: the gap is bridged
+      if (t0) {
+        src.gskip(sh.gneed);
+        bridge_ends(c, wk, sh, sh.ira, sh.ira + segm, sh.atom_i, sh.atom_m, false);
+        set_queries(sh, 1, sh.ira, sh.ira + segm, sh.atom_i, sh.atom_m);
+      }
+      __syncthreads();
+      bridge_block(c, wk, sh, 0, true);
+    } else if (t0) {
+      if (!sh.exists) {
+        sh.qwtot[0] += 1.0;
         sh.atom_i = nrnd(src, 0, wk.numb);
         sh.ira = nrnd(src, 1, P);
         segm = nrnd(src, 2, wk.m) + 1;
@@ -314,65 +432,70 @@ __global__ void __launch_bounds__(kThreads) k_worm_move(Ctx c, Frame *frames, De
         sh.atom_m = sh.atom_i;
         if (sh.masha != (sh.ira + segm)) sh.atom_m = c.st.pindex[sh.atom_i];
         sh.flag = 2;
-        potential_queries(c, wk, sh, sh.ira, sh.ira + segm, sh.atom_i, sh.atom_m);
+        set_queries(sh, 0, sh.ira, sh.ira + segm, sh.atom_i, sh.atom_m);
       }
     }
     __syncthreads();
     if (sh.flag) {
+      fill_queries(c, wk, sh);
+      __syncthreads();
       query_sums(c, frames, wk, sh);
       __syncthreads();
       if (t0) {
-        double prob = wk.qw_norm * pow((double)segm, 1.5) *
+        double prob = wk.qw_norm * sh.pw15[segm] *
                       exp(open_kin(c, wk, sh, segm) + potential_total(sh) * c.s.tau);
         if (sh.flag == 1) prob = 1.0 / prob;
         bool acc = false;
         if (prob >= 1.0) acc = true;
         else if (prob > src.take(3)) acc = true;
         if (acc) {
-          if (sh.flag == 1) { sh.exists = 0; wkp->qwacc[1] += 1.0; }
-          else { sh.exists = 1; wkp->qwacc[0] += 1.0; }
+          if (sh.flag == 1) { sh.exists = 0; sh.qwacc[1] += 1.0; }
+          else { sh.exists = 1; sh.qwacc[0] += 1.0; }
         }
       }
     }
     __syncthreads();   // every thread is past the reads of sh.flag / sh.exists above
     // ---------------- advance (mc_qworm.cc:295-355) / recede (:357-400)
     if (sh.exists) {
-      int ira_new = 0, atomi_new = 0, adv = 0, advance = 0;
+      int ira_new = 0, atomi_new = 0;
       if (t0) {
         double r = src.take(7);
-        adv = r > 0.5;
+        sh.adv = r > 0.5;
         sh.flag = 0;
         sh.gneed = 0;
-        if (adv) {
-          wkp->qwtot[4] += 1.0;
+        if (sh.adv) {
+          sh.qwtot[4] += 1.0;
           int sg = sh.masha - sh.ira;
           if (sg < 0) sg += P;
-          advance = nrnd(src, 2, wk.m) + 1;
-          if (sg - advance > 0) sh.gneed = 3 * advance;   // the end point, then the bridge
+          sh.advance = nrnd(src, 2, wk.m) + 1;
+          if (sg - sh.advance > 0) sh.gneed = 3 * sh.advance;   // the end point, then the bridge
         }
         sh.gbase = src.gbase();
       }
       prefetch_gauss(src, sh);
-      if (t0) {
-        if (adv) {
-          if (sh.gneed > 0) {
-            int gi = 0;
-            src.gskip(sh.gneed);
-            int it0 = sh.ira, it2 = sh.ira + advance;
-            ira_new = it2 % P;
-            atomi_new = sh.atom_i;
-            if (ira_new != it2) atomi_new = sh.atom_m;
-            double gvar = 1.0 / ((double)advance * wk.twave2);
-            size_t i0 = bead(c, wk.first + sh.atom_i, it0 % P);
-            double r0[3] = {c.st.x[i0], c.st.y[i0], c.st.z[i0]}, r2[3];
-            for (int d = 0; d < 3; d++) r2[d] = r0[d] + sh.gz[gi++] / sqrt(gvar);
-            store_bead(c, bead(c, wk.first + atomi_new, it2 % P), r2[0], r2[1], r2[2]);
-            sample_middle(c, wk, sh, gi, it0, it2, sh.atom_i, atomi_new, nullptr, 0);
-            potential_queries(c, wk, sh, it0, it2 + 1, sh.atom_i, atomi_new);
-            sh.flag = 1;
-          }
-        } else {
-          wkp->qwtot[5] += 1.0;
+      if (sh.adv && sh.gneed > 0) {      // advance: a new end bead and the bridge to it
+        if (t0) {
+          const int advance = sh.advance;
+          src.gskip(sh.gneed);
+          int it0 = sh.ira, it2 = sh.ira + advance;
+          ira_new = it2 % P;
+          atomi_new = sh.atom_i;
+          if (ira_new != it2) atomi_new = sh.atom_m;
+          // the new end bead: r0 + gauss(1/(advance twave2)) (mc_qworm.cc:324-330)
+          size_t i0 = bead(c, wk.first + sh.atom_i, it0 % P);
+          const double r0[3] = {c.st.x[i0], c.st.y[i0], c.st.z[i0]};
+          double *r2 = sh.sg3 + 3 * advance;
+          for (int d = 0; d < 3; d++) r2[d] = fma(sh.sqadv[advance], sh.gz[d], r0[d]);
+          store_bead(c, bead(c, wk.first + atomi_new, it2 % P), r2[0], r2[1], r2[2]);
+          bridge_ends(c, wk, sh, it0, it2, sh.atom_i, atomi_new, true);
+          set_queries(sh, 1, it0, it2 + 1, sh.atom_i, atomi_new);
+          sh.flag = 1;
+        }
+        __syncthreads();
+        bridge_block(c, wk, sh, 3, true);
+      } else if (t0) {
+        if (!sh.adv) {
+          sh.qwtot[5] += 1.0;
           int sg = sh.ira - sh.masha;
           if (sg < 0) sg += P;
           int recede = nrnd(src, 2, wk.m) + 1;
@@ -386,13 +509,15 @@ __global__ void __launch_bounds__(kThreads) k_worm_move(Ctx c, Frame *frames, De
             }
             ira_new = it0 % P;
             atomi_new = a0;
-            potential_queries(c, wk, sh, it0, it1 + 1, a0, a1);
+            set_queries(sh, 0, it0, it1 + 1, a0, a1);
             sh.flag = 2;
           }
         }
       }
       __syncthreads();
       if (sh.flag) {
+        fill_queries(c, wk, sh);
+        __syncthreads();
         query_sums(c, frames, wk, sh);
         __syncthreads();
         if (t0) {
@@ -401,11 +526,11 @@ __global__ void __launch_bounds__(kThreads) k_worm_move(Ctx c, Frame *frames, De
           if (sh.flag == 1) {          // advance
             if (pot < 0.0) acc = true;
             else if (exp(-pot * c.s.tau) > src.take(4)) acc = true;
-            if (acc) wkp->qwacc[4] += 1.0;
+            if (acc) sh.qwacc[4] += 1.0;
           } else {                     // recede
             if (pot > 0.0) acc = true;
             else if (exp(pot * c.s.tau) > src.take(4)) acc = true;
-            if (acc) wkp->qwacc[5] += 1.0;
+            if (acc) sh.qwacc[5] += 1.0;
           }
           if (acc) {
             sh.ira = ira_new;
@@ -418,94 +543,85 @@ __global__ void __launch_bounds__(kThreads) k_worm_move(Ctx c, Frame *frames, De
     // ---------------- swap (mc_qworm.cc:424-551)
     if (bose && sh.exists) {
       int it0 = 0, it1 = 0, pit1 = 0, atomw = 0, a0 = 0, a1 = 0;
+      double prob = 0.0;
       if (t0) {
-        wkp->qwtot[6] += 1.0;
-        const int sg = wk.m;
+        sh.qwtot[6] += 1.0;
         it0 = sh.ira;
-        it1 = it0 + sg;
+        it1 = it0 + wk.m;
         pit1 = it1 % P;
         atomw = sh.atom_i;
+        sh.pw_atom = atomw; sh.pw_pt0 = it0; sh.pw_pt1 = pit1; sh.pw_segm = wk.m; sh.pw_t1 = it1;
+        sh.pcount = 0;
+      }
+      __syncthreads();
+      get_ptable(c, wk, sh, rindex, dall);
+      if (t0) {
+        const int count = min(sh.pcount, PIMC_MAXNEIGHBORS);
         sh.flag = 0;
-        int count = get_ptable(c, wk, sh, rindex, atomw, it0, pit1, sg, it1, dr2l, atml, ptab);
         if (count > 0) {
           double pn = 0.0;
-          for (int ic = 1; ic <= count; ic++) pn += ptab[ic];
+          for (int ic = 1; ic <= count; ic++) pn += sh.ptab[ic];
           double prand = pn * src.take(5);
           double sum = 0.0;
           int ic = 1;
           while ((ic <= count) && (sum < prand)) {
-            sum += ptab[ic];
+            sum += sh.ptab[ic];
             ic++;
           }
           ic--;
-          a1 = atml[ic];
+          a1 = sh.pta[ic];
           pnorm_old = pn;
           a0 = a1;
           if (pit1 != it1) a0 = rindex[a1];
           sh.flag = 1;
-          sh.stack[0] = it0; sh.stack[1] = it1; sh.stack[2] = atomw; sh.stack[3] = a0; sh.stack[4] = a1;
         }
         sh.gneed = sh.flag && wk.m >= 2 ? 3 * (wk.m - 1) : 0;
         sh.gbase = src.gbase();
       }
       prefetch_gauss(src, sh);
-      if (t0 && sh.flag) {
-        const int sg = wk.m;
-        it0 = sh.stack[0]; it1 = sh.stack[1]; atomw = sh.stack[2]; a0 = sh.stack[3]; a1 = sh.stack[4];
-        pit1 = it1 % P;
-        {
-          int gi = 0;
+      if (sh.flag) {
+        if (t0) {
           src.gskip(sh.gneed);
           // newcoords: the end points, then the bridge between them
-          size_t iw = bead(c, wk.first + atomw, it0), i1 = bead(c, wk.first + a1, pit1);
-          seg[0] = c.st.x[iw]; seg[1] = c.st.y[iw]; seg[2] = c.st.z[iw];
-          seg[3 * sg + 0] = c.st.x[i1]; seg[3 * sg + 1] = c.st.y[i1]; seg[3 * sg + 2] = c.st.z[i1];
-          sample_middle(c, wk, sh, gi, it0, it1, a0, a1, seg, it0);
+          bridge_ends(c, wk, sh, it0, it1, atomw, a1, false);
           // the new and the old energy of every inner slice, in that order
-          int g = wk.first + a0, nq = 0;
-          for (int it = it0 + 1; it < it1; it++) {
-            int pit = it % P;
-            if (pit != it) g = wk.first + a1;
-            size_t i = bead(c, g, pit);
-            sh.qa[nq] = g; sh.qpit[nq] = pit;
-            sh.qx[nq] = seg[3 * (it - it0)]; sh.qy[nq] = seg[3 * (it - it0) + 1]; sh.qz[nq] = seg[3 * (it - it0) + 2];
-            nq++;
-            sh.qa[nq] = g; sh.qpit[nq] = pit;
-            sh.qx[nq] = c.st.x[i]; sh.qy[nq] = c.st.y[i]; sh.qz[nq] = c.st.z[i];
-            nq++;
-          }
-          sh.nq = nq;
-          sh.stack[0] = it0; sh.stack[1] = it1; sh.stack[2] = atomw; sh.stack[3] = a0; sh.stack[4] = a1;
+          set_queries(sh, 2, it0, it1, a0, a1);
         }
-      }
-      __syncthreads();
-      if (sh.flag) {
+        __syncthreads();
+        bridge_block(c, wk, sh, 0, false);
+        fill_queries(c, wk, sh);
+        __syncthreads();
         query_sums(c, frames, wk, sh);
         __syncthreads();
         if (t0) {
-          it0 = sh.stack[0]; it1 = sh.stack[1]; atomw = sh.stack[2]; a0 = sh.stack[3]; a1 = sh.stack[4];
-          pit1 = it1 % P;
           double pot = 0.0;
           for (int q = 0; q < sh.nq; q += 2) {
             pot += sh.qsum[q];
             pot -= sh.qsum[q + 1];
           }
-          double prob = exp(-pot * c.s.tau);
-          int count = get_ptable(c, wk, sh, rindex, a0, it0, pit1, wk.m, it1, dr2l, atml, ptab);
+          prob = exp(-pot * c.s.tau);
+          sh.pw_atom = a0; sh.pw_pt0 = it0; sh.pw_pt1 = pit1; sh.pw_segm = wk.m; sh.pw_t1 = it1;
+          sh.pcount = 0;
+        }
+        __syncthreads();
+        get_ptable(c, wk, sh, rindex, dall);
+        if (t0) {
+          const int count = min(sh.pcount, PIMC_MAXNEIGHBORS);
           double pn = 0.0;
-          for (int ic = 1; ic <= count; ic++) pn += ptab[ic];
+          for (int ic = 1; ic <= count; ic++) pn += sh.ptab[ic];
           prob *= (pnorm_old / pn);
           bool acc = false;
           if (prob >= 1.0) acc = true;
           else if (prob > src.take(6)) acc = true;
           sh.flag = acc ? 1 : 0;
           if (acc) {
-            wkp->qwacc[6] += 1.0;
+            sh.qwacc[6] += 1.0;
             int g = wk.first + a0;
             for (int it = it0 + 1; it < it1; it++) {
               int pit = it % P;
               if (pit != it) g = wk.first + a1;
-              store_bead(c, bead(c, g, pit), seg[3 * (it - it0)], seg[3 * (it - it0) + 1], seg[3 * (it - it0) + 2]);
+              const double *b = sh.sg3 + 3 * (it - it0);
+              store_bead(c, bead(c, g, pit), b[0], b[1], b[2]);
             }
             int ratomw = rindex[atomw], ratom0 = rindex[a0];
             c.st.pindex[ratomw] = a0;
@@ -516,14 +632,15 @@ __global__ void __launch_bounds__(kThreads) k_worm_move(Ctx c, Frame *frames, De
               if (a0 == sh.atom_m) sh.atom_m = sh.atom_i;
               else if (sh.atom_i == sh.atom_m) sh.atom_m = a0;
             }
+            sh.stack[0] = it0; sh.stack[1] = atomw; sh.stack[2] = a0;
           }
         }
         __syncthreads();
         if (sh.flag) {
           // the heads of the two paths up to it0 change places
-          it0 = sh.stack[0]; atomw = sh.stack[2]; a0 = sh.stack[3];
-          for (int it = threadIdx.x; it <= it0; it += kThreads) {
-            size_t ia = bead(c, wk.first + a0, it), iw = bead(c, wk.first + atomw, it);
+          const int h0 = sh.stack[0], hw = sh.stack[1], ha = sh.stack[2];
+          for (int it = threadIdx.x; it <= h0; it += kThreads) {
+            size_t ia = bead(c, wk.first + ha, it), iw = bead(c, wk.first + hw, it);
             double xa = c.st.x[ia], ya = c.st.y[ia], za = c.st.z[ia];
             store_bead(c, ia, c.st.x[iw], c.st.y[iw], c.st.z[iw]);
             store_bead(c, iw, xa, ya, za);
@@ -536,6 +653,10 @@ __global__ void __launch_bounds__(kThreads) k_worm_move(Ctx c, Frame *frames, De
   if (t0) {
     wkp->exists = sh.exists; wkp->ira = sh.ira; wkp->masha = sh.masha;
     wkp->atom_i = sh.atom_i; wkp->atom_m = sh.atom_m;
+  }
+  if (threadIdx.x < 7) {
+    wkp->qwtot[threadIdx.x] = sh.qwtot[threadIdx.x];
+    wkp->qwacc[threadIdx.x] = sh.qwacc[threadIdx.x];
   }
 }
 
@@ -711,16 +832,13 @@ void launch_worm_prod(const Ctx &c, Frame *f, DevWorm *wk, int *rindex, uint64_t
   src.seed = seed;
   src.pass = pass;
   src.phase = phase;
-  double *seg = (double *)scratch;
-  double *dr2l = seg + 3 * (PIMC_WORM_MAXM + 1);
-  double *ptab = dr2l + (numb + 1);
-  int *atml = (int *)(ptab + (numb + 1));
+  double *dall = (double *)scratch;
   Ctx cw = c;
   cw.st.worm = nullptr;
-  k_worm_move<WormPhilox><<<1, kThreads, 0, s>>>(cw, f, wk, rindex, src, seg, dr2l, atml, ptab);
+  k_worm_move<WormPhilox><<<1, kThreads, 0, s>>>(cw, f, wk, rindex, src, dall);
 }
 
-size_t worm_scratch_bytes(int numb) { return sizeof(double) * (3 * (PIMC_WORM_MAXM + 1) + 2 * (size_t)(numb + 1)) + sizeof(int) * (size_t)(numb + 1) + 64; }
+size_t worm_scratch_bytes(int numb) { return sizeof(double) * (size_t)(numb + 1) + 64; }
 
 void launch_worm_move(const Ctx &c, Frame *f, DevWorm *wk, int *rindex, const double *const *streams,
                       const long *lengths, long *cursors, void *scratch, int numb, cudaStream_t s)
@@ -729,11 +847,8 @@ void launch_worm_move(const Ctx &c, Frame *f, DevWorm *wk, int *rindex, const do
   for (int k = 0; k < 9; k++) { src.v[k] = streams[k]; src.n[k] = lengths[k]; }
   src.pos = cursors;
   src.err = c.st.err;
-  double *seg = (double *)scratch;
-  double *dr2l = seg + 3 * (PIMC_WORM_MAXM + 1);
-  double *ptab = dr2l + (numb + 1);
-  int *atml = (int *)(ptab + (numb + 1));
+  double *dall = (double *)scratch;
   Ctx cw = c;
   cw.st.worm = nullptr;      // the kernel masks from its own copy of the worm
-  k_worm_move<WormSrc><<<1, kThreads, 0, s>>>(cw, f, wk, rindex, src, seg, dr2l, atml, ptab);
+  k_worm_move<WormSrc><<<1, kThreads, 0, s>>>(cw, f, wk, rindex, src, dall);
 }
