@@ -28,6 +28,10 @@ import subprocess
 import sys
 import time
 
+# independent chains run on their own streams: give the process enough
+# hardware work queues that they do not share them (read at CUDA start-up)
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
 REPO = os.path.dirname(os.path.abspath(__file__))
 PKG = os.path.join(REPO, "moribs-pimc_gb300")
 for p in (PKG, os.path.join(REPO, "oracle")):
@@ -55,6 +59,7 @@ def parse():
     ap.add_argument("--no-tables", action="store_true", help="skip the propagator-table generator measurement")
     ap.add_argument("--no-worm", action="store_true", help="skip the worm-algorithm pass measurement")
     ap.add_argument("--no-surrogate", action="store_true", help="skip the surrogate / delayed-acceptance measurement")
+    ap.add_argument("--worm-replicas", type=int, default=32, help="independent worm chains run at once")
     ap.add_argument("--only", default=None, choices=["tables", "worm", "surrogate"],
                     help="run one companion measurement alone on cuda:0 and print its JSON (for profiling)")
     return ap.parse_args()
@@ -466,13 +471,17 @@ def run_tables(local, cpu):
     return out
 
 
-def run_worm(local, cpu, steps=5, warmup=2):
+def run_worm(local, cpu, steps=5, warmup=2, replicas=32):
     """The worm branch of the pass loop (mc_main.cc:348-381) on config 0
     (CO2-like rotor + 8 He-4, P = 512, Q = 128) with WORM He4 1.0 16: per
     time slice the worm tries, the closed-path exchange bisection and
-    centroid move, the rotor's bisection and rotational sweep.  GPU passes
-    timed with CUDA events on the library's stream; the CPU figure is the
-    oracle's port of the same loop on a 64-slice sample, scaled to a pass."""
+    centroid move, the rotor's bisection and rotational sweep.  One chain's
+    passes (one CUDA graph per pass) timed with CUDA events on the library's
+    stream; then `replicas` independent chains (own handles, streams and
+    seeds) driven from host threads at once, timed by the wall clock between
+    device synchronisations.  The CPU figure is the oracle's port of the same
+    loop on a 64-slice sample, scaled to a pass."""
+    import threading
     import torch
     import pimc_gb300 as G
     import workloads as W
@@ -480,7 +489,7 @@ def run_worm(local, cpu, steps=5, warmup=2):
     w.worm = ("He4", 1.0, 16)
     s = G.Sampler(w, device=local)
     s.worm_init(0, 1.0, 16, w.density)
-    s.worm_run(warmup, 31)
+    s.worm_run(warmup, 32)              # the pass graph is built here, outside the timed region
     s.synchronize()
     ext = torch.cuda.ExternalStream(s.stream(), device=torch.device("cuda", local))
     l0 = s.launch_count()
@@ -501,6 +510,42 @@ def run_worm(local, cpu, steps=5, warmup=2):
                            "advance": acc[4] / max(1, tot[4]), "recede": acc[5] / max(1, tot[5]),
                            "swap": acc[6] / max(1, tot[6])}}
     s.close()
+    if replicas > 1:
+        ss = []
+        for r in range(replicas):
+            wr = W.config0(seed=1234 + 101 * r)
+            sr = G.Sampler(wr, device=local)
+            sr.worm_init(0, 1.0, 16, wr.density)
+            ss.append(sr)
+
+        def drive(n):
+            errs = []
+
+            def one(sr, seed):
+                try:
+                    sr.worm_run(n, seed)
+                except Exception as e:          # re-raised on the main thread
+                    errs.append(e)
+            th = [threading.Thread(target=one, args=(sr, 500 + r)) for r, sr in enumerate(ss)]
+            for t in th:
+                t.start()
+            for t in th:
+                t.join()
+            if errs:
+                raise errs[0]
+            for sr in ss:
+                sr.synchronize()
+            torch.cuda.synchronize()
+        drive(warmup)
+        t0 = time.perf_counter()
+        drive(steps)
+        el = time.perf_counter() - t0
+        out["replicas"] = {"chains": replicas, "passes_each": steps, "wall_s": round(el, 3),
+                           "slices_per_s": round(replicas * steps * w.nslices / el, 1),
+                           "ms_per_pass_equivalent": round(el / (replicas * steps) * 1e3, 3),
+                           "timing": "wall clock between device synchronisations, host threads one per chain"}
+        for sr in ss:
+            sr.close()
     if cpu:
         import oracle as O
         o = O.Oracle(w)
@@ -636,7 +681,8 @@ def main():
     if args.only is not None:
         if rank == 0:
             run = {"tables": lambda: run_tables(local, not args.no_cpu),
-                   "worm": lambda: run_worm(local, not args.no_cpu, steps=args.steps, warmup=args.warmup),
+                   "worm": lambda: run_worm(local, not args.no_cpu, steps=args.steps, warmup=args.warmup,
+                                            replicas=args.worm_replicas),
                    "surrogate": lambda: run_surrogate(local)}[args.only]
             print(json.dumps({"part": args.only, **run()}), flush=True)
         return 0
@@ -649,7 +695,7 @@ def main():
         if not args.no_tables and world == 1:
             line["tables"] = run_tables(local, not args.no_cpu)
         if not args.no_worm and world == 1:
-            line["worm"] = run_worm(local, not args.no_cpu)
+            line["worm"] = run_worm(local, not args.no_cpu, replicas=args.worm_replicas)
         if not args.no_surrogate and world == 1:
             line["surrogate"] = run_surrogate(local)
         print(json.dumps(line), flush=True)

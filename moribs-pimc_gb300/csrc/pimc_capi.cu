@@ -38,6 +38,9 @@ struct pimc_handle {
   std::vector<double> cosine_host;
   bool tables = false, state = false;
   cudaGraphExec_t pass_exec = nullptr;
+  cudaGraphExec_t worm_exec = nullptr;  // one captured worm-branch pass (pimc_worm_run)
+  uint64_t worm_seed = 0;
+  long long worm_nodes = 0;
   uint64_t pass_seed = 0;
   long long nodes_per_pass = 0;
   long long launches = 0;
@@ -330,6 +333,7 @@ extern "C" pimc_status pimc_destroy(pimc_handle *h)
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
   if (h->pass_exec) cudaGraphExecDestroy(h->pass_exec);
+  if (h->worm_exec) cudaGraphExecDestroy(h->worm_exec);
   DevState &st = h->ctx.st;
   void *bufs[] = {st.x, st.y, st.z, st.b4, st.cosvf, st.rp_cache, st.rl_cache, st.rp_ok, st.rl_ok,
                   st.ang, st.cosv, st.pindex, st.mctype, st.err, h->frames, h->cnt, h->pass, h->cursors, h->ms,
@@ -546,6 +550,7 @@ extern "C" pimc_status pimc_load_tables(pimc_handle *h, const pimc_tables *tb)
   CK(cudaStreamSynchronize(h->stream));
   h->tables = true;
   if (h->pass_exec) { cudaGraphExecDestroy(h->pass_exec); h->pass_exec = nullptr; }
+  if (h->worm_exec) { cudaGraphExecDestroy(h->worm_exec); h->worm_exec = nullptr; }
   return PIMC_OK;
 }
 
@@ -1104,10 +1109,12 @@ extern "C" pimc_status pimc_worm_init(pimc_handle *h, int type, double c, int m,
   CK(cudaMemcpy(h->rindex, r.data(), d.na * sizeof(int), cudaMemcpyHostToDevice));
   h->worm_on = 1;
   h->ctx.st.worm = h->worm;           // every partner sum now masks the worm's gap
-  if (h->pass_exec) {                 // a captured pass holds the old context
+  if (h->pass_exec || h->worm_exec) { // a captured pass holds the old context
     CK(cudaStreamSynchronize(h->stream));
-    cudaGraphExecDestroy(h->pass_exec);
+    if (h->pass_exec) cudaGraphExecDestroy(h->pass_exec);
+    if (h->worm_exec) cudaGraphExecDestroy(h->worm_exec);
     h->pass_exec = nullptr;
+    h->worm_exec = nullptr;
   }
   return PIMC_OK;
 }
@@ -1169,38 +1176,61 @@ extern "C" pimc_status pimc_worm_run(pimc_handle *h, int npasses, uint64_t seed)
   const int bose = d.stat[wt] == PIMC_BOSE;
   char *mscr = (char *)h->wscr + ((worm_scratch_bytes(d.na) + 255) / 256) * 256;
   ReplaySrc none{};
-  for (int p = 0; p < npasses; p++) {
+  // one pass, recorded into a CUDA graph on the first call for this seed
+  auto record = [&]() -> long long {
+    long long n = 0;
     launch_pass_begin(h->pass, h->stream);
-    h->launches++;
+    n++;
     for (int t = 0; t < P; t++) {
       for (int type = 0; type < d.ntypes; type++) {
         if (d.numb[type] <= 0) continue;
         if (type == wt) {
           launch_worm_prod(h->ctx, h->frames, h->worm, h->rindex, seed, h->pass, 4u * t, h->wscr, d.na, h->stream);
           launch_invalidate_caches(h->ctx, h->stream);
-          h->launches += 2;
-          h->launches += launch_bisect_slice(h->ctx, h->frames, type, 0, bose, h->worm, seed, h->pass, 4u * t + 1,
-                                             h->cnt, h->stream);
+          n += 2;
+          n += launch_bisect_slice(h->ctx, h->frames, type, 0, bose, h->worm, seed, h->pass, 4u * t + 1, h->cnt,
+                                   h->stream);
           if (t == 0)
-            h->launches += launch_mol_exchange(h->ctx, h->frames, type, false, none, seed, h->pass, 4u * t + 2, mscr,
-                                               h->cnt, h->stream, h->worm);
+            n += launch_mol_exchange(h->ctx, h->frames, type, false, none, seed, h->pass, 4u * t + 2, mscr, h->cnt,
+                                     h->stream, h->worm);
           continue;
         }
         if (t == 0)
           for (int a = 0; a < d.numb[type]; a++)
-            h->launches += launch_mol(h->ctx, h->frames, type, a, false, none, seed, h->pass, 4u * t + 3, h->ms,
-                                      nullptr, nullptr, h->cnt, h->stream);
-        h->launches += launch_bisect_slice(h->ctx, h->frames, type, t, 0, nullptr, seed, h->pass, 4u * t + 3, h->cnt,
-                                           h->stream);
+            n += launch_mol(h->ctx, h->frames, type, a, false, none, seed, h->pass, 4u * t + 3, h->ms, nullptr,
+                            nullptr, h->cnt, h->stream);
+        n += launch_bisect_slice(h->ctx, h->frames, type, t, 0, nullptr, seed, h->pass, 4u * t + 3, h->cnt,
+                                 h->stream);
         if (type == d.imtype && h->sys.rotation) {
-          h->launches += launch_rot_phase(h->ctx, h->frames, 0, 4u * t + 3, seed, h->pass, h->cnt, h->stream);
-          h->launches += launch_rot_phase(h->ctx, h->frames, 1, 4u * t + 3, seed, h->pass, h->cnt, h->stream);
+          n += launch_rot_phase(h->ctx, h->frames, 0, 4u * t + 3, seed, h->pass, h->cnt, h->stream);
+          n += launch_rot_phase(h->ctx, h->frames, 1, 4u * t + 3, seed, h->pass, h->cnt, h->stream);
         }
       }
     }
     launch_refresh_frames(h->ctx, h->frames, h->stream);
-    h->launches++;
-    CK(cudaGetLastError());
+    return n + 1;
+  };
+  if (npasses > 0 && (!h->worm_exec || h->worm_seed != seed)) {
+    if (h->worm_exec) { CK(cudaGraphExecDestroy(h->worm_exec)); h->worm_exec = nullptr; }
+    cudaGraph_t graph;
+    CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    long long n = record();
+    cudaError_t le = cudaGetLastError();
+    cudaError_t ce = cudaStreamEndCapture(h->stream, &graph);
+    if (le != cudaSuccess || ce != cudaSuccess) {
+      if (ce == cudaSuccess) cudaGraphDestroy(graph);
+      h->last_cuda = le != cudaSuccess ? le : ce;
+      return PIMC_ERR_CUDA;
+    }
+    cudaError_t ie = cudaGraphInstantiate(&h->worm_exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ie != cudaSuccess) { h->last_cuda = ie; return PIMC_ERR_CUDA; }
+    h->worm_seed = seed;
+    h->worm_nodes = n;
+  }
+  for (int p = 0; p < npasses; p++) {
+    CK(cudaGraphLaunch(h->worm_exec, h->stream));
+    h->launches += h->worm_nodes;
   }
   CK(cudaMemcpyAsync(h->pindex_host.data(), h->ctx.st.pindex, d.na * sizeof(int), cudaMemcpyDeviceToHost, h->stream));
   return check_err(h);
@@ -1596,6 +1626,7 @@ extern "C" pimc_status pimc_set_precision(pimc_handle *h, int mixed)
   h->launches++;
   CK(cudaGetLastError());
   if (h->pass_exec) { CK(cudaGraphExecDestroy(h->pass_exec)); h->pass_exec = nullptr; }
+  if (h->worm_exec) { CK(cudaGraphExecDestroy(h->worm_exec)); h->worm_exec = nullptr; }
   return PIMC_OK;
 }
 

@@ -27,6 +27,7 @@ struct WormShared {
   int exists, ira, masha, atom_i, atom_m;   // the worm (TPathWorm)
   int flag;                                  // a decision every thread reads
   int nq;                                    // potential queries of the current sum
+  double qtot;                               // their total (query_sums)
   int qa[kMaxQ], qpit[kMaxQ];                // global atom and slice of each
   double qx[kMaxQ], qy[kMaxQ], qz[kMaxQ];    // the bead the atom sits on
   double qsum[kMaxQ];
@@ -164,14 +165,23 @@ __device__ void query_sums(const Ctx &c, const Frame *frames, const DevWorm &wk,
       for (int a1 = 0; a1 < na; a1++) acc += sh.term[q * na + a1];
       sh.qsum[q] = acc;
     }
-    return;
+  } else {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int q = warp; q < nq; q += kWarps) {
+      double acc = 0.0;
+      for (int a1 = lane; a1 < na; a1 += 32) acc += query_term(c, frames, wk, sh, q, a1);
+      for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+      if (lane == 0) sh.qsum[q] = acc;
+    }
   }
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int q = warp; q < nq; q += kWarps) {
+  // the sum's total -- for the swap (mode 2) the new minus the old energies --
+  // by warp 0 in a fixed lane order and shuffle tree
+  __syncthreads();
+  if (threadIdx.x < 32) {
     double acc = 0.0;
-    for (int a1 = lane; a1 < na; a1 += 32) acc += query_term(c, frames, wk, sh, q, a1);
+    for (int q = threadIdx.x; q < nq; q += 32) acc += (sh.qmode == 2 && (q & 1)) ? -sh.qsum[q] : sh.qsum[q];
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if (lane == 0) sh.qsum[q] = acc;
+    if (threadIdx.x == 0) sh.qtot = acc;
   }
 }
 
@@ -211,13 +221,6 @@ __device__ void fill_queries(const Ctx &c, const DevWorm &wk, WormShared &sh)
 __device__ __forceinline__ void set_queries(WormShared &sh, int mode, int it0, int it1, int atom0, int atom1)
 {
   sh.qmode = mode; sh.qt0 = it0; sh.qt1 = it1; sh.qa0 = atom0; sh.qa1 = atom1;
-}
-
-__device__ double potential_total(const WormShared &sh)
-{
-  double pot = 0.0;
-  for (int q = 0; q < sh.nq; q++) pot += sh.qsum[q];
-  return pot;
 }
 
 // rint(0.5 (t0 + t2)) of sample_middle (mc_qworm.cc:245) in integers:
@@ -442,8 +445,7 @@ __global__ void __launch_bounds__(kThreads) k_worm_move(Ctx c, Frame *frames, De
       query_sums(c, frames, wk, sh);
       __syncthreads();
       if (t0) {
-        double prob = wk.qw_norm * sh.pw15[segm] *
-                      exp(open_kin(c, wk, sh, segm) + potential_total(sh) * c.s.tau);
+        double prob = wk.qw_norm * sh.pw15[segm] * exp(open_kin(c, wk, sh, segm) + sh.qtot * c.s.tau);
         if (sh.flag == 1) prob = 1.0 / prob;
         bool acc = false;
         if (prob >= 1.0) acc = true;
@@ -521,7 +523,7 @@ __global__ void __launch_bounds__(kThreads) k_worm_move(Ctx c, Frame *frames, De
         query_sums(c, frames, wk, sh);
         __syncthreads();
         if (t0) {
-          double pot = potential_total(sh);
+          double pot = sh.qtot;
           bool acc = false;
           if (sh.flag == 1) {          // advance
             if (pot < 0.0) acc = true;
@@ -594,12 +596,7 @@ __global__ void __launch_bounds__(kThreads) k_worm_move(Ctx c, Frame *frames, De
         query_sums(c, frames, wk, sh);
         __syncthreads();
         if (t0) {
-          double pot = 0.0;
-          for (int q = 0; q < sh.nq; q += 2) {
-            pot += sh.qsum[q];
-            pot -= sh.qsum[q + 1];
-          }
-          prob = exp(-pot * c.s.tau);
+          prob = exp(-sh.qtot * c.s.tau);
           sh.pw_atom = a0; sh.pw_pt0 = it0; sh.pw_pt1 = pit1; sh.pw_segm = wk.m; sh.pw_t1 = it1;
           sh.pcount = 0;
         }
