@@ -60,6 +60,7 @@ def parse():
     ap.add_argument("--no-worm", action="store_true", help="skip the worm-algorithm pass measurement")
     ap.add_argument("--no-surrogate", action="store_true", help="skip the surrogate / delayed-acceptance measurement")
     ap.add_argument("--worm-replicas", type=int, default=32, help="independent worm chains run at once")
+    ap.add_argument("--da-replicas", type=int, default=32, help="independent dimer systems swept at once")
     ap.add_argument("--only", default=None, choices=["tables", "worm", "surrogate"],
                     help="run one companion measurement alone on cuda:0 and print its JSON (for profiling)")
     return ap.parse_args()
@@ -558,17 +559,41 @@ def run_worm(local, cpu, steps=5, warmup=2, replicas=32):
         out["cpu_baseline"] = {"kind": "port", "cores": nth, "sample": "64 time slices of the worm pass loop",
                                "ms_per_pass": round(cs * w.nslices / 64 * 1e3, 1),
                                "slices_per_s": round(64 / cs, 1)}
+        if replicas > 1:
+            # the CPU's own best use of its cores for many chains: one
+            # single-threaded chain per core, all at once
+            os_ = []
+            for r in range(nth):
+                wr = W.config0(seed=1234 + 101 * r)
+                orr = O.Oracle(wr)
+                orr.worm_init(0, 1.0, 16, wr.density)
+                orr.worm_run(0, 8, 5, 1)
+                os_.append(orr)
+            th = [threading.Thread(target=orr.worm_run, args=(8, 64, 6, 1)) for orr in os_]
+            t0 = time.perf_counter()
+            for t in th:
+                t.start()
+            for t in th:
+                t.join()
+            cs = time.perf_counter() - t0
+            out["cpu_baseline"]["chains"] = {"chains": nth, "threads_each": 1,
+                                             "sample": "64 time slices of each chain's worm pass loop",
+                                             "slices_per_s": round(nth * 64 / cs, 1)}
     return out
 
 
-def run_surrogate(local, quick=False):
+def run_surrogate(local, quick=False, replicas=32):
     """North-star pattern (4) on config 3 (2 water-like tops, caleng, T 0.74 K,
     P = 4096, Q = 2048): training data emitted by the plain sampler (dimer
     features and exact caleng energies of every translational slice), the
     surrogate MLP trained on the GPU by its tcgen05 kernels, then plain and
     delayed-acceptance rotational sweeps timed with CUDA events.  Also the
     surrogate's inference rate on a large batch against the tensor-core
-    peak."""
+    peak.  Then `replicas` independent dimer systems (own handles, streams
+    and seeds, one trained surrogate shared read-only) make plain and
+    delayed-acceptance sweeps at once from one host thread each, timed by
+    the wall clock between device synchronisations."""
+    import threading
     import numpy as np
     import torch
     import pimc_gb300 as G
@@ -655,6 +680,43 @@ def run_surrogate(local, quick=False):
                         "achieved": round(k_tf, 2), "peak": peak_tf, "unit": "TFLOP/s",
                         "frac": round(k_tf / peak_tf, 5), "ms_per_launch": round(k_ms, 4),
                         "flop_per_row": flop_row, "peak_source": peak_kind}}
+    if replicas > 1:
+        hs = [s] + [G.Sampler(W.config3(seed=77 + 13 * r), device=local) for r in range(1, replicas)]
+
+        def drive(nsw, mlp):
+            res, errs = [None] * len(hs), []
+
+            def one(r):
+                try:
+                    res[r] = hs[r].da_sweeps(nsw, 3000 + r, mlp=mlp, escale=sd)
+                except Exception as ex:          # re-raised on the main thread
+                    errs.append(ex)
+            th = [threading.Thread(target=one, args=(r,)) for r in range(len(hs))]
+            t0 = time.perf_counter()
+            for t in th:
+                t.start()
+            for t in th:
+                t.join()
+            for h in hs:
+                h.synchronize()
+            torch.cuda.synchronize()
+            el = time.perf_counter() - t0
+            if errs:
+                raise errs[0]
+            moves = sum(float(r[0]) for r in res)
+            return {"moves_per_s": round(moves / el, 1), "wall_s": round(el, 3),
+                    "accept": round(sum(float(r[2]) for r in res) / moves, 4),
+                    "exact_evals_per_move": round(sum(float(r[3]) for r in res) / moves, 4)}
+        nb = 20 if quick else 200
+        drive(5, None)
+        bp = drive(nb, None)
+        drive(5, m)
+        bd = drive(nb, m)
+        out["batched"] = {"systems": replicas, "sweeps_each": nb, "plain": bp, "delayed_acceptance": bd,
+                          "timing": "wall clock between device synchronisations, host threads one per system",
+                          "vs_single_plain": round(bd["moves_per_s"] / out["plain"]["moves_per_s"], 2)}
+        for h in hs[1:]:
+            h.close()
     m.close()
     s.close()
     return out
@@ -683,7 +745,7 @@ def main():
             run = {"tables": lambda: run_tables(local, not args.no_cpu),
                    "worm": lambda: run_worm(local, not args.no_cpu, steps=args.steps, warmup=args.warmup,
                                             replicas=args.worm_replicas),
-                   "surrogate": lambda: run_surrogate(local)}[args.only]
+                   "surrogate": lambda: run_surrogate(local, replicas=args.da_replicas)}[args.only]
             print(json.dumps({"part": args.only, **run()}), flush=True)
         return 0
     line, w = run_gb300(args, rank, local, world, dist)
@@ -697,7 +759,7 @@ def main():
         if not args.no_worm and world == 1:
             line["worm"] = run_worm(local, not args.no_cpu, replicas=args.worm_replicas)
         if not args.no_surrogate and world == 1:
-            line["surrogate"] = run_surrogate(local)
+            line["surrogate"] = run_surrogate(local, replicas=args.da_replicas)
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.barrier()
