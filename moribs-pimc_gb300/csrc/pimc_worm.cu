@@ -20,8 +20,9 @@ constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
 constexpr int kMaxQ = 2 * (PIMC_WORM_MAXM + 1);   // the swap's new and old slices
 #define PIMC_MAXNEIGHBORS 100                     // MAXNEIGHBORS (mc_qworm.cc:12)
-constexpr int kTermCap = 3072;                    // (query, partner) terms held in shared memory
+constexpr int kTermCap = 2560;                    // (query, partner) terms held in shared memory
 constexpr int kDrawCap = 32;                      // draws of each uniform stream held in shared memory
+constexpr int kGaussCap = 640;                    // gauss() draws held in shared memory
 
 struct WormShared {
   int exists, ira, masha, atom_i, atom_m;   // the worm (TPathWorm)
@@ -52,6 +53,7 @@ struct WormShared {
   double qwtot[7], qwacc[7];                 // the worm's try/accept counters
   double term[kTermCap];                     // the (query, partner) terms of query_sums
   double dc[8 * kDrawCap];                   // the first draws of the uniform streams
+  double gc[kGaussCap];                      // the first gauss() draws of the call
 };
 
 struct WormSrc {
@@ -61,7 +63,7 @@ struct WormSrc {
   unsigned *err;
   // one draw of stream k: 0..2 nrnd1..3, 3..7 rnd1..5, 8 gauss's x1
   __device__ void init() {}
-  __device__ void fill(double *) const {}
+  __device__ void fill(double *, double *) const {}
   __device__ long gbase() const { return pos[8]; }
   __device__ double gauss_at(long i) const
   {
@@ -85,25 +87,31 @@ struct WormSrc {
 };
 
 // the production draws: Philox keyed by (seed, pass, phase, stream k, count).
-// The first kDrawCap draws of streams 0..7 are generated by all threads at
-// the start of the call (a call of N tries takes at most 2N from any one of
-// them) so that thread 0's chain reads them from shared memory.
+// The first kDrawCap draws of streams 0..7 and the first kGaussCap gauss()
+// draws are generated by all threads at the start of the call (a call of N
+// tries takes at most 2N from any one uniform stream; config 0 takes about
+// 560 gauss() draws per call), so that the decision chain and the bridges
+// read them from shared memory.
 struct WormPhilox {
   uint64_t seed;
   const unsigned *pass;
   unsigned phase;
   uint64_t move;
   unsigned cnt[9];
-  const double *cache;
+  const double *cache, *gcache;
   __device__ void init()
   {
     move = ((uint64_t)(*pass) << 32) | ((uint64_t)phase << 12) | 0xFFFu;
     for (int k = 0; k < 9; k++) cnt[k] = 0;
   }
-  __device__ void fill(double *buf)
+  __device__ void fill(double *buf, double *gbuf)
   {
-    for (int i = threadIdx.x; i < 8 * kDrawCap; i += blockDim.x) buf[i] = draw(i / kDrawCap, (unsigned)(i % kDrawCap));
+    for (int i = threadIdx.x; i < 8 * kDrawCap + kGaussCap; i += blockDim.x) {
+      if (i < 8 * kDrawCap) buf[i] = draw(i / kDrawCap, (unsigned)(i % kDrawCap));
+      else gbuf[i - 8 * kDrawCap] = draw(8, (unsigned)(i - 8 * kDrawCap));
+    }
     cache = buf;
+    gcache = gbuf;
   }
   __device__ double draw(int k, unsigned n) const
   {
@@ -118,7 +126,7 @@ struct WormPhilox {
     return n < (unsigned)kDrawCap ? cache[k * kDrawCap + n] : draw(k, n);
   }
   __device__ long gbase() const { return cnt[8]; }
-  __device__ double gauss_at(long i) const { return draw(8, (unsigned)i); }
+  __device__ double gauss_at(long i) const { return i < kGaussCap ? gcache[i] : draw(8, (unsigned)i); }
   __device__ void gskip(long k) { cnt[8] += (unsigned)k; }
 };
 
@@ -339,16 +347,19 @@ __device__ void get_ptable(const Ctx &c, const DevWorm &wk, WormShared &sh, cons
     dall[a1] = v;
   }
   __syncthreads();
+  // non-negative doubles order as their bit patterns do, so the ranks are
+  // taken with integer compares (the FP64 pipe is the scarce one); -1 marks
+  // a non-candidate and is negative as an integer too
   for (int a = threadIdx.x; a < wk.numb; a += kThreads) {
-    const double d = dall[a];
-    if (d < 0.0) continue;
+    const long long d = __double_as_longlong(dall[a]);
+    if (d < 0) continue;
     atomicAdd(&sh.pcount, 1);
     int r = 0;
     for (int b = 0; b < wk.numb; b++) {
-      const double e = dall[b];
-      r += (e >= 0.0) && (e < d || (e == d && b < a));
+      const long long e = __double_as_longlong(dall[b]);
+      r += (e >= 0) && (e < d || (e == d && b < a));
     }
-    if (r < PIMC_MAXNEIGHBORS) { sh.ptd[r + 1] = d; sh.pta[r + 1] = a; }
+    if (r < PIMC_MAXNEIGHBORS) { sh.ptd[r + 1] = __longlong_as_double(d); sh.pta[r + 1] = a; }
   }
   __syncthreads();
   const int count = min(sh.pcount, PIMC_MAXNEIGHBORS);
@@ -377,7 +388,7 @@ __global__ void __launch_bounds__(kThreads) k_worm_move(Ctx c, Frame *frames, De
   const int P = c.s.P;
   const bool t0 = threadIdx.x == 0;
   src.init();
-  src.fill(sh.dc);
+  src.fill(sh.dc, sh.gc);
   for (int i = threadIdx.x; i < 2 * (PIMC_WORM_MAXM + 2); i += kThreads) {
     const int w = i / (PIMC_WORM_MAXM + 2), len = i % (PIMC_WORM_MAXM + 2);
     if (len >= 2) {
