@@ -39,6 +39,13 @@ struct pimc_handle {
   bool tables = false, state = false;
   cudaGraphExec_t pass_exec = nullptr;
   cudaGraphExec_t worm_exec = nullptr;  // one captured worm-branch pass (pimc_worm_run)
+  cudaGraphExec_t da_exec = nullptr;    // one captured pimc_da_sweeps call and its key
+  int da_nsweeps = -1, da_use = -1;
+  uint64_t da_seed = 0;
+  float da_escale = 0.0f;
+  unsigned long long da_mlp = 0;
+  const void *da_buf = nullptr;
+  long long da_nodes = 0;
   uint64_t worm_seed = 0;
   long long worm_nodes = 0;
   uint64_t pass_seed = 0;
@@ -334,6 +341,7 @@ extern "C" pimc_status pimc_destroy(pimc_handle *h)
   if (h->stream) cudaStreamSynchronize(h->stream);
   if (h->pass_exec) cudaGraphExecDestroy(h->pass_exec);
   if (h->worm_exec) cudaGraphExecDestroy(h->worm_exec);
+  if (h->da_exec) cudaGraphExecDestroy(h->da_exec);
   DevState &st = h->ctx.st;
   void *bufs[] = {st.x, st.y, st.z, st.b4, st.cosvf, st.rp_cache, st.rl_cache, st.rp_ok, st.rl_ok,
                   st.ang, st.cosv, st.pindex, st.mctype, st.err, h->frames, h->cnt, h->pass, h->cursors, h->ms,
@@ -551,6 +559,7 @@ extern "C" pimc_status pimc_load_tables(pimc_handle *h, const pimc_tables *tb)
   h->tables = true;
   if (h->pass_exec) { cudaGraphExecDestroy(h->pass_exec); h->pass_exec = nullptr; }
   if (h->worm_exec) { cudaGraphExecDestroy(h->worm_exec); h->worm_exec = nullptr; }
+  if (h->da_exec) { cudaGraphExecDestroy(h->da_exec); h->da_exec = nullptr; }
   return PIMC_OK;
 }
 
@@ -1283,22 +1292,47 @@ extern "C" pimc_status pimc_da_sweeps(pimc_handle *h, pimc_mlp *m, int nsweeps, 
   float *y = (float *)cur;
   cur += ((size_t)rows * sizeof(float) + 255) / 256 * 256;
   DaMove *mv = (DaMove *)cur;
+  // the call's launches, recorded into a CUDA graph and replayed while the
+  // same sweep count, seed, surrogate, scale and scratch come back
+  auto record = [&]() -> long long {
+    long long n = 1;
+    launch_pass_begin(h->pass, h->stream);
+    for (int sw = 0; sw < nsweeps; sw++)
+      for (int par = 0; par < 2; par++)
+        for (int r = 0; r < 2; r++) {
+          unsigned phase = 4u * (unsigned)sw + 2u * par + r;
+          n += launch_da_propose(h->ctx, h->frames, r, par, phase, seed, h->pass, feat, mv, h->stream);
+          if (use_surrogate) n += mlp_forward_device(m, feat, rows, y, h->stream);
+          n += launch_da_decide(h->ctx, h->frames, r, par, phase, seed, h->pass, y, use_surrogate, escale, mv, st,
+                                h->cnt, h->stream);
+        }
+    launch_invalidate_caches(h->ctx, h->stream);
+    launch_refresh_frames(h->ctx, h->frames, h->stream);
+    return n + 2;
+  };
+  const unsigned long long mk = use_surrogate ? mlp_uid(m) : 0ull;
+  if (!h->da_exec || h->da_nsweeps != nsweeps || h->da_seed != seed || h->da_use != use_surrogate ||
+      h->da_escale != escale || h->da_mlp != mk || h->da_buf != buf) {
+    if (h->da_exec) { CK(cudaGraphExecDestroy(h->da_exec)); h->da_exec = nullptr; }
+    cudaGraph_t graph;
+    CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    long long n = record();
+    cudaError_t le = cudaGetLastError();
+    cudaError_t ce = cudaStreamEndCapture(h->stream, &graph);
+    if (le != cudaSuccess || ce != cudaSuccess) {
+      if (ce == cudaSuccess) cudaGraphDestroy(graph);
+      h->last_cuda = le != cudaSuccess ? le : ce;
+      return PIMC_ERR_CUDA;
+    }
+    cudaError_t ie = cudaGraphInstantiate(&h->da_exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ie != cudaSuccess) { h->last_cuda = ie; return PIMC_ERR_CUDA; }
+    h->da_nsweeps = nsweeps; h->da_seed = seed; h->da_use = use_surrogate; h->da_escale = escale;
+    h->da_mlp = mk; h->da_buf = buf; h->da_nodes = n;
+  }
   CK(cudaMemsetAsync(st, 0, 4 * sizeof(unsigned long long), h->stream));
-  launch_pass_begin(h->pass, h->stream);
-  h->launches++;
-  for (int sw = 0; sw < nsweeps; sw++)
-    for (int par = 0; par < 2; par++)
-      for (int r = 0; r < 2; r++) {
-        unsigned phase = 4u * (unsigned)sw + 2u * par + r;
-        h->launches += launch_da_propose(h->ctx, h->frames, r, par, phase, seed, h->pass, feat, mv, h->stream);
-        if (use_surrogate) h->launches += mlp_forward_device(m, feat, rows, y, h->stream);
-        h->launches += launch_da_decide(h->ctx, h->frames, r, par, phase, seed, h->pass, y, use_surrogate, escale, mv,
-                                        st, h->cnt, h->stream);
-      }
-  launch_invalidate_caches(h->ctx, h->stream);
-  launch_refresh_frames(h->ctx, h->frames, h->stream);
-  h->launches += 2;
-  CK(cudaGetLastError());
+  CK(cudaGraphLaunch(h->da_exec, h->stream));
+  h->launches += h->da_nodes;
   unsigned long long hs[4];
   CK(cudaMemcpyAsync(hs, st, sizeof(hs), cudaMemcpyDeviceToHost, h->stream));
   e = check_err(h);
@@ -1627,6 +1661,7 @@ extern "C" pimc_status pimc_set_precision(pimc_handle *h, int mixed)
   CK(cudaGetLastError());
   if (h->pass_exec) { CK(cudaGraphExecDestroy(h->pass_exec)); h->pass_exec = nullptr; }
   if (h->worm_exec) { CK(cudaGraphExecDestroy(h->worm_exec)); h->worm_exec = nullptr; }
+  if (h->da_exec) { CK(cudaGraphExecDestroy(h->da_exec)); h->da_exec = nullptr; }
   return PIMC_OK;
 }
 

@@ -11,6 +11,7 @@
 // BF16 activations as the next layer's A operand.  The weights arrive by
 // one bulk copy (cp.async.bulk) per layer, already in the B-operand layout.
 // The 6 -> 256 and 256 -> 1 layers are FP32 on the CUDA cores.
+#include <atomic>
 #include <cstdint>
 #include <cstring>
 #include <vector>
@@ -606,7 +607,12 @@ struct pimc_mlp {
   float *z2 = nullptr, *part = nullptr, *loss = nullptr;
   int tcap = 0;
   long long step = 0;
+  unsigned long long uid = 0;   // never reused within the process (keys captured graphs)
 };
+
+static std::atomic<unsigned long long> g_mlp_uid{0};
+
+unsigned long long mlp_uid(const pimc_mlp *m) { return m ? m->uid : 0ull; }
 
 #define MCK(x)                                  \
   do {                                          \
@@ -634,6 +640,7 @@ extern "C" pimc_status pimc_mlp_create(int device, pimc_mlp **out)
   if (cudaGetDeviceCount(&nd) != cudaSuccess || nd <= device) return PIMC_ERR_NO_DEVICE;
   pimc_mlp *m = new (std::nothrow) pimc_mlp();
   if (!m) return PIMC_ERR_BAD_ARG;
+  m->uid = ++g_mlp_uid;
   m->device = device;
   MCK(cudaSetDevice(device));
   MCK(cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking));
