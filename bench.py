@@ -377,7 +377,7 @@ def run_gb300(args, rank, local, world, dist):
 
 
 def run_batched(args, local, dist):
-    """Config 2 (spec pattern 2): independent replicas of the config-0
+    """Config 2, the replica batch: independent replicas of the config-0
     family -- N_He uniform in 1..64, P in {64, 128, 256, 512}, Q = P/4, T
     uniform in 0.3-2.0 K, seeded -- in one persistent graph-captured launch
     per pass, FP32 tables with FP64 action differences; warps per CTA from
@@ -583,7 +583,7 @@ def run_worm(local, cpu, steps=5, warmup=2, replicas=32):
 
 
 def run_surrogate(local, quick=False, replicas=32):
-    """North-star pattern (4) on config 3 (2 water-like tops, caleng, T 0.74 K,
+    """The surrogate with delayed acceptance on config 3 (2 water-like tops, caleng, T 0.74 K,
     P = 4096, Q = 2048): training data emitted by the plain sampler (dimer
     features and exact caleng energies of every translational slice), the
     surrogate MLP trained on the GPU by its tcgen05 kernels, then plain and

@@ -164,7 +164,7 @@ pimc_status pimc_worm_set_state(pimc_handle *h, const int *state);
  * ADVANCE, RECEDE, SWAP] */
 pimc_status pimc_worm_counters(pimc_handle *h, double *total, double *accep);
 
-/* ---- rotor-rotor surrogate (spec pattern 4) ---------------------- */
+/* ---- rotor-rotor surrogate for delayed acceptance ----------------------- */
 
 /* An MLP 6 -> 256 -> 256 -> 256 -> 1 with SiLU activations: FP32 first and
  * last layers, BF16 weights and FP32 accumulation in the two 256 x 256

@@ -1,4 +1,4 @@
-"""The surrogate in the sampler (spec pattern 4) on a small water
+"""The surrogate in the sampler (two-stage delayed acceptance) on a small water
 dimer (P = 128, Q = 64): training data emitted by the sampler, the MLP
 trained on the GPU by its tensor-core kernels, and the two-stage
 delayed-acceptance rotational move whose second stage uses the exact caleng
