@@ -332,8 +332,15 @@ def run_gb300(args, rank, local, world, dist):
     per_launch_ms = ms[dom] / max(1, nl[dom])
     achieved = bytes_launch / (per_launch_ms / 1e3) / 1e9
     peak, peak_kind = measured_peaks()
+    # DRAM bytes per launch of the same kernel and launch shape from one ncu
+    # capture (dram__bytes_read.sum + dram__bytes_write.sum; the capture's
+    # summary is profiles/k_rot_slices_config1_fp64.md): far below the
+    # algorithmic bytes, the tables stay in L2/L1 and the FP64 pipe binds
+    traffic = 6.11e6 + 0.06e6 if (dom == 2 and not mixed) else None
     roofline = {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 5), "traffic": None,
+                "frac": round(achieved / peak, 5), "traffic": traffic,
+                "traffic_source": "ncu capture (profiles/k_rot_slices_config1_fp64.md)" if traffic else None,
+                "binding_limit": "FP64 pipe (ncu: sm__pipe_fp64_cycles_active 54.7 % of peak)" if traffic else None,
                 "kernel": kname, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
                 "per_launch_us": round(per_launch_ms * 1e3, 3), "algorithmic_bytes_per_launch": int(bytes_launch),
                 "pass_ms_by_kind": {k: round(v, 3) for k, v in zip(kinds, ms)},
