@@ -135,6 +135,41 @@ pimc_status pimc_area_estimators(pimc_handle *h, double *out);
  * row-major 3x3). */
 pimc_status pimc_area_estim3d(pimc_handle *h, int iframe, const double *mass, double *out);
 
+/* The estimators' block files (host only, no handle): the reference's
+ * writers with the same file names, columns, normalisations and number
+ * format (scientific, 6 digits, width 14, three-blank separators), from the
+ * arrays the entry points above return, summed over the block by the
+ * caller.  fname is the file stem; mode 0 is a block file (MC_BLOCK), 1 the
+ * accumulated one ("_sum" before the extension, MC_TOTAL); acount is the
+ * number of samples summed.  sys->box must hold the reference's BoxSize
+ * (mc_setup.cc:361-366) for the .gra normalisation.  bstype is the boson
+ * type (BSTYPE) and mass its mass in amu.
+ *  pimc_save_densities_1d   SaveDensities1D (mc_estim.cc:1327-1443): .gra;
+ *                           with a linear impurity also .gri and .grt from gr2d
+ *  pimc_save_densities_2d   SaveDensities2D (mc_estim.cc:1666-1726): .g2d
+ *  pimc_save_densities_3d   SaveDensities3D (mc_estim.cc:1728-1800): .g3d
+ *  pimc_save_rho_1d         SaveRho1D's .gri, .grt, .grc (mc_estim.cc:1445-1590)
+ *  pimc_save_exchange_length  SaveExchangeLength (mc_estim.cc:2021-2085): .prl, appended
+ *  pimc_save_area_estimators  SaveAreaEstimators (mc_estim.cc:2596-2641): .sup, appended;
+ *                           sums[6] as pimc_area_estimators' out
+ *  pimc_save_area_estim3d   SaveAreaEstim3D (mc_estim.cc:2670-2720): .sffs3d / .mffs3d,
+ *                           appended; areas[6], inert[9] as pimc_area_estim3d's out[3..17]
+ * gr1d/gr2d/gr3d are laid out as pimc_densities_read writes them. */
+pimc_status pimc_save_densities_1d(const pimc_system *sys, const char *fname, double acount, const double *gr1d,
+                                   const double *gr2d);
+pimc_status pimc_save_densities_2d(const pimc_system *sys, const char *fname, double acount, int mode,
+                                   const double *gr2d);
+pimc_status pimc_save_densities_3d(const pimc_system *sys, const char *fname, double acount, int mode,
+                                   const double *gr3d);
+pimc_status pimc_save_rho_1d(const pimc_system *sys, const char *fname, double acount, int mode,
+                             const double *gr3d);
+pimc_status pimc_save_exchange_length(const pimc_system *sys, const char *fname, double acount, long blocknumb,
+                                      int bstype, const double *ploops, const int *pindex, int print_xyz_prl);
+pimc_status pimc_save_area_estimators(const pimc_system *sys, const char *fname, double acount, long blocknumb,
+                                      int bstype, const double *sums, double mass);
+pimc_status pimc_save_area_estim3d(const pimc_system *sys, const char *fname, double acount, long blocknumb,
+                                   int iframe, int bstype, const double *areas, const double *inert, double mass);
+
 /* ---- worm algorithm (mc_qworm.cc) ------------------------------------------ */
 
 /* MCWormInit (mc_qworm.cc:49-82) for the atom type `type` with the WORM

@@ -15,7 +15,7 @@ OUT = os.path.join(HERE, "libpimc_gb300.so")
 BUILD = os.path.join(HERE, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "--expt-relaxed-constexpr"]
-SOURCES = ["pimc_kernels.cu", "pimc_batch.cu", "pimc_capi.cu", "pimc_tables.cu", "pimc_worm.cu", "pimc_mlp.cu", "pimc_da.cu"]
+SOURCES = ["pimc_kernels.cu", "pimc_batch.cu", "pimc_capi.cu", "pimc_tables.cu", "pimc_worm.cu", "pimc_mlp.cu", "pimc_da.cu", "pimc_io.cu"]
 
 
 def nvcc():

@@ -75,6 +75,13 @@ def load(path=LIBPATH):
     L.pimc_da_samples.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(C.c_float)]
     L.pimc_da_sweeps.argtypes = [vp, vp, C.c_int, C.c_uint64, C.c_float, C.c_int, _dp]
     L.pimc_linden.argtypes = [C.c_int, C.c_int, _dp, _ip, C.c_double, C.c_int, C.c_int, _dp]
+    sp, cc = C.POINTER(PimcSystem), C.c_char_p
+    L.pimc_save_densities_1d.argtypes = [sp, cc, C.c_double, _dp, _dp]
+    for n in ("pimc_save_densities_2d", "pimc_save_densities_3d", "pimc_save_rho_1d"):
+        getattr(L, n).argtypes = [sp, cc, C.c_double, C.c_int, _dp]
+    L.pimc_save_exchange_length.argtypes = [sp, cc, C.c_double, C.c_long, C.c_int, _dp, _ip, C.c_int]
+    L.pimc_save_area_estimators.argtypes = [sp, cc, C.c_double, C.c_long, C.c_int, _dp, C.c_double]
+    L.pimc_save_area_estim3d.argtypes = [sp, cc, C.c_double, C.c_long, C.c_int, C.c_int, _dp, _dp, C.c_double]
     L.pimc_asymrho.argtypes = [C.c_int, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, _dp, C.c_int,
                                _dp, _dp, _dp, _dp]
     L.pimc_densities_accumulate.argtypes = [vp]
@@ -547,3 +554,62 @@ class Mlp:
         if self.h:
             self.L.pimc_mlp_destroy(self.h)
             self.h = C.c_void_p()
+
+
+# ---- block files of the estimators (host only)
+
+def _sysbox(w, box):
+    s = make_system(w)
+    for i in range(3):
+        s.box[i] = float(box[i])
+    return s
+
+
+def _arr(a, n=None):
+    if a is None:
+        return None
+    return dptr(np.ascontiguousarray(a, dtype=np.float64))
+
+
+def save_densities(w, box, fname, acount, mode, gr1d, gr2d, gr3d):
+    """The density files of one block (mode 0) or of the run (mode 1):
+    SaveDensities1D (block only), SaveDensities2D, SaveDensities3D and
+    SaveRho1D as the reference's block and run ends call them
+    (mc_main.cc:715-734, 445-460).  gr?d as Sampler.densities_read returns
+    them; box = the reference's BoxSize."""
+    L = load()
+    s = _sysbox(w, box)
+    keep = [np.ascontiguousarray(g, dtype=np.float64) for g in (gr1d, gr2d, gr3d)]
+    p1, p2, p3 = (dptr(k) for k in keep)
+    fn = fname.encode()
+    if mode == 0:
+        _chk(L.pimc_save_densities_1d(C.byref(s), fn, float(acount), p1, p2), "pimc_save_densities_1d")
+    _chk(L.pimc_save_densities_2d(C.byref(s), fn, float(acount), int(mode), p2), "pimc_save_densities_2d")
+    _chk(L.pimc_save_densities_3d(C.byref(s), fn, float(acount), int(mode), p3), "pimc_save_densities_3d")
+    _chk(L.pimc_save_rho_1d(C.byref(s), fn, float(acount), int(mode), p3), "pimc_save_rho_1d")
+
+
+def save_exchange_length(w, fname, acount, blocknumb, bstype, ploops, pindex, print_xyz_prl=0):
+    L = load()
+    s = make_system(w)
+    pl = np.ascontiguousarray(ploops, dtype=np.float64)
+    pi = np.ascontiguousarray(pindex, dtype=np.int32)
+    _chk(L.pimc_save_exchange_length(C.byref(s), fname.encode(), float(acount), int(blocknumb), int(bstype),
+                                     dptr(pl), iptr(pi), int(print_xyz_prl)), "pimc_save_exchange_length")
+
+
+def save_area_estimators(w, fname, acount, blocknumb, bstype, sums, mass):
+    L = load()
+    s = make_system(w)
+    sm = np.ascontiguousarray(sums, dtype=np.float64)
+    _chk(L.pimc_save_area_estimators(C.byref(s), fname.encode(), float(acount), int(blocknumb), int(bstype),
+                                     dptr(sm), float(mass)), "pimc_save_area_estimators")
+
+
+def save_area_estim3d(w, fname, acount, blocknumb, iframe, bstype, areas, inert, mass):
+    L = load()
+    s = make_system(w)
+    a = np.ascontiguousarray(areas, dtype=np.float64)
+    i = np.ascontiguousarray(inert, dtype=np.float64)
+    _chk(L.pimc_save_area_estim3d(C.byref(s), fname.encode(), float(acount), int(blocknumb), int(iframe),
+                                  int(bstype), dptr(a), dptr(i), float(mass)), "pimc_save_area_estim3d")

@@ -425,6 +425,11 @@ class Reference:
         L.ref_exchange_lengths.argtypes = [_dp]
         L.ref_area_estimators.argtypes = [_dp]
         L.ref_area_estim3d.argtypes = [C.c_int, _dp]
+        L.ref_box_size.argtypes = [_dp]
+        L.ref_save_densities.argtypes = [C.c_char_p, C.c_double, C.c_int]
+        L.ref_save_exchange_length.argtypes = [C.c_char_p, C.c_double, C.c_long]
+        L.ref_save_area_estimators.argtypes = [C.c_char_p, C.c_double, C.c_long]
+        L.ref_save_area_estim3d.argtypes = [C.c_char_p, C.c_double, C.c_long, C.c_int]
         L.ref_tau.restype = C.c_double
         L.ref_lambda.restype = C.c_double
         L.ref_lambda.argtypes = [C.c_int]
@@ -543,6 +548,24 @@ class Reference:
         out = np.zeros(15)
         self.L.ref_area_estim3d(int(iframe), dptr(out))
         return out
+
+    def box_size(self):
+        b = np.zeros(3)
+        self.L.ref_box_size(dptr(b))
+        return b
+
+    # the reference's block writers on the accumulators last filled above
+    def save_densities(self, fname, acount, mode):
+        self.L.ref_save_densities(fname.encode(), float(acount), int(mode))
+
+    def save_exchange_length(self, fname, acount, blocknumb):
+        self.L.ref_save_exchange_length(fname.encode(), float(acount), int(blocknumb))
+
+    def save_area_estimators(self, fname, acount, blocknumb):
+        self.L.ref_save_area_estimators(fname.encode(), float(acount), int(blocknumb))
+
+    def save_area_estim3d(self, fname, acount, blocknumb, iframe):
+        self.L.ref_save_area_estim3d(fname.encode(), float(acount), int(blocknumb), int(iframe))
 
 
 def linden(temprt, nslice, bconst, npt, iodevn=-1):

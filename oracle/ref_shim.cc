@@ -395,4 +395,37 @@ void ref_area_estim3d(int iframe, double *out)
   for (int i = 0; i < 9; i++) out[6 + i] = in[i];
 }
 
+// BoxSize (mc_setup.cc:361-366)
+void ref_box_size(double *b)
+{
+  for (int d = 0; d < NDIM; d++) b[d] = BoxSize[d];
+}
+
+// the reference's block writers on the accumulators the calls above filled:
+// SaveDensities1D/2D/3D and SaveRho1D (mc_estim.cc:1327-1800, block mode
+// only for SaveRho1D: its total mode also writes relative-Euler-angle
+// histograms), SaveExchangeLength, SaveAreaEstimators, SaveAreaEstim3D
+// (mc_estim.cc:2021-2085, 2596-2720)
+void ref_save_densities(const char *fname, double acount, int mode)
+{
+  SaveDensities1D(fname, acount);
+  if (IMPURITY && MCAtom[IMTYPE].molecule == 1) SaveDensities2D(fname, acount, mode);
+  if (IMPURITY && MCAtom[IMTYPE].molecule == 2) {
+    SaveDensities3D(fname, acount, mode);
+    if (mode == MC_BLOCK) SaveRho1D(fname, acount, mode);
+  }
+}
+void ref_save_exchange_length(const char *fname, double acount, long blocknumb)
+{
+  SaveExchangeLength(fname, acount, blocknumb);
+}
+void ref_save_area_estimators(const char *fname, double acount, long blocknumb)
+{
+  SaveAreaEstimators(fname, acount, blocknumb);
+}
+void ref_save_area_estim3d(const char *fname, double acount, long blocknumb, int iframe)
+{
+  SaveAreaEstim3D(fname, acount, blocknumb, iframe);
+}
+
 }  // extern "C"
