@@ -28,7 +28,10 @@ constexpr int kH = 256;               // hidden width (MMA N and K)
 constexpr int kIn = 6;                // input features
 constexpr int kA = kRows * kH * 2;    // A operand bytes (BF16)
 constexpr int kB = kH * kH * 2;       // B operand bytes
-constexpr int kSmem = kA + kB + 2048; // + barriers, the TMEM address and the half sums
+constexpr int kW1B = (kIn + 1) * kH * 4;   // W1 and b1 (contiguous parameters), FP32
+constexpr int kVecB = 3 * kH * 4;           // b2, then b3 and w4 (contiguous), FP32
+// + barriers, the TMEM address, the half sums, then W1, b1, b2, b3, w4
+constexpr int kSmem = kA + kB + 2048 + kW1B + kVecB;
 constexpr int kSmemT = kA + kB + 8192; // + the column-sum buffer of the training kernel
 // the parameter vector: w1[6][256], b1, w2[256][256], b2, w3[256][256], b3, w4, b4
 constexpr int kOW1 = 0, kOB1 = kOW1 + kIn * kH, kOW2 = kOB1 + kH, kOB2 = kOW2 + kH * kH, kOW3 = kOB2 + kH,
@@ -108,6 +111,26 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity)
 
 // bytes (a multiple of 16 KB) from global to shared memory by bulk copies of
 // 16 KB that complete on bar; one arrival with the whole transaction count
+// one arrival on bar announcing `bytes` of copies to come
+__device__ __forceinline__ void bulk_expect(uint64_t *bar, uint32_t bytes)
+{
+  asm volatile(
+      "{\n\t.reg .b64 st;\n\t"
+      "mbarrier.arrive.expect_tx.release.cta.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(smem_u32(bar)),
+      "r"(bytes)
+      : "memory");
+}
+
+// one cp.async.bulk of `bytes` (a multiple of 16) completing on bar, whose
+// bytes an earlier bulk_expect announced
+__device__ __forceinline__ void bulk_copy(void *dst, const void *src, uint32_t bytes, uint64_t *bar)
+{
+  asm volatile("cp.async.bulk.shared::cta.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+
 __device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes, uint64_t *bar)
 {
   asm volatile(
@@ -157,6 +180,20 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float v[16])
 // surrogate is BF16 throughout; 2-ulp FP32 activations are far below that)
 __device__ __forceinline__ float silu(float z) { return __fdividef(z, 1.0f + __expf(-z)); }
 
+// eight BF16 values (round to nearest even) as one 16-byte shared store
+__device__ __forceinline__ void store8(char *dst, float a, float b, float c, float d, float e, float f, float g,
+                                       float h)
+{
+  __nv_bfloat162 q0 = __floats2bfloat162_rn(a, b), q1 = __floats2bfloat162_rn(c, d);
+  __nv_bfloat162 q2 = __floats2bfloat162_rn(e, f), q3 = __floats2bfloat162_rn(g, h);
+  uint4 u;
+  u.x = *(uint32_t *)&q0;
+  u.y = *(uint32_t *)&q1;
+  u.z = *(uint32_t *)&q2;
+  u.w = *(uint32_t *)&q3;
+  *(uint4 *)dst = u;
+}
+
 // D[128 x 256] (TMEM) = A[128 x 256] . B[256 x 256]^T from shared memory,
 // sixteen K=16 steps issued by thread 0, completion on bar (phase `ph`)
 __device__ __forceinline__ bool gemm_128x256(uint32_t tmem, const char *sA, const char *sB, uint64_t *bar,
@@ -195,14 +232,28 @@ __global__ void __launch_bounds__(kFwdThreads) k_mlp_forward(MlpParams p, const 
   uint64_t *bar_w = (uint64_t *)(smem + kA + kB);
   uint64_t *bar_m = bar_w + 1;
   uint32_t *tslot = (uint32_t *)(bar_w + 2);
+  uint64_t *bar_x = bar_w + 3;                            // the copies of W1 and the vectors
   float *outp = (float *)(smem + kA + kB + 64);          // [256] half sums of the last layer
+  float *sw1 = (float *)(smem + kA + kB + 2048), *sb1 = sw1 + kIn * kH;
+  float *sb2 = sb1 + kH, *sb3 = sb2 + kH, *sw4 = sb3 + kH;
   const int tid = threadIdx.x, warp = tid >> 5;
   const int r = tid & (kRows - 1), half = tid >> 7, c0 = half * (kH / 2);
   const int row = blockIdx.x * kRows + r;
+  // the row's inputs and the weight copies are in flight while TMEM is
+  // allocated; W1 and the bias and output vectors (10 KB) on their own
+  // barrier, so that the first layer does not wait for W2
+  float xin[kIn];
+  for (int i = 0; i < kIn; i++) xin[i] = row < n ? x[(size_t)row * kIn + i] : 0.0f;
   if (tid == 0) {
     mbar_init(bar_w, 1);
     mbar_init(bar_m, 1);
+    mbar_init(bar_x, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    bulk_expect(bar_x, kW1B + kVecB);
+    bulk_copy(sw1, p.w1, kW1B, bar_x);                    // W1, b1
+    bulk_copy(sb2, p.b2, kH * 4, bar_x);
+    bulk_copy(sb3, p.b3, 2 * kH * 4, bar_x);              // b3, w4
+    bulk_load(sB, p.w2c, kB, bar_w);
   }
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)), "r"(kH)
@@ -214,20 +265,27 @@ __global__ void __launch_bounds__(kFwdThreads) k_mlp_forward(MlpParams p, const 
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tslot;
   const uint32_t tlane = tmem + ((uint32_t)((warp & 3) * 32) << 16);
-  if (tid == 0) bulk_load(sB, p.w2c, kB, bar_w);
-  // layer 1 on the CUDA cores, written as the A operand
-  float xin[kIn];
-  for (int i = 0; i < kIn; i++) xin[i] = row < n ? x[(size_t)row * kIn + i] : 0.0f;
-  for (int j = c0; j < c0 + kH / 2; j += 2) {
-    float z0 = p.b1[j], z1 = p.b1[j + 1];
+  // layer 1 on the CUDA cores, written as the A operand: eight columns of a
+  // row are one 16-byte run of the canonical layout, stored at once
+  bool ok = __syncthreads_and(mbar_wait(bar_x, 0));
+  for (int j = c0; j < c0 + kH / 2 && ok; j += 8) {
+    float z[8];
+    const float4 b0 = *(const float4 *)(sb1 + j), b1 = *(const float4 *)(sb1 + j + 4);
+    z[0] = b0.x; z[1] = b0.y; z[2] = b0.z; z[3] = b0.w;
+    z[4] = b1.x; z[5] = b1.y; z[6] = b1.z; z[7] = b1.w;
+#pragma unroll
     for (int i = 0; i < kIn; i++) {
-      z0 = fmaf(xin[i], p.w1[i * kH + j], z0);
-      z1 = fmaf(xin[i], p.w1[i * kH + j + 1], z1);
+      const float4 w0 = *(const float4 *)(sw1 + i * kH + j), w1 = *(const float4 *)(sw1 + i * kH + j + 4);
+      z[0] = fmaf(xin[i], w0.x, z[0]); z[1] = fmaf(xin[i], w0.y, z[1]);
+      z[2] = fmaf(xin[i], w0.z, z[2]); z[3] = fmaf(xin[i], w0.w, z[3]);
+      z[4] = fmaf(xin[i], w1.x, z[4]); z[5] = fmaf(xin[i], w1.y, z[5]);
+      z[6] = fmaf(xin[i], w1.z, z[6]); z[7] = fmaf(xin[i], w1.w, z[7]);
     }
-    *(__nv_bfloat162 *)(sA + canon(r, j)) = __floats2bfloat162_rn(silu(z0), silu(z1));
+    store8(sA + canon(r, j), silu(z[0]), silu(z[1]), silu(z[2]), silu(z[3]), silu(z[4]), silu(z[5]), silu(z[6]),
+           silu(z[7]));
   }
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-  bool ok = __syncthreads_and(mbar_wait(bar_w, 0));
+  ok = __syncthreads_and(mbar_wait(bar_w, 0)) && ok;
   unsigned ph = 0;
   float out = 0.0f;
   for (int layer = 0; layer < 2 && ok; layer++) {
@@ -235,18 +293,30 @@ __global__ void __launch_bounds__(kFwdThreads) k_mlp_forward(MlpParams p, const 
     ph ^= 1u;
     if (!ok) break;
     if (layer == 0 && tid == 0) bulk_load(sB, p.w3c, kB, bar_w);
-    const float *bias = layer == 0 ? p.b2 : p.b3;
+    const float *bias = layer == 0 ? sb2 : sb3;
     for (int c = c0; c < c0 + kH / 2; c += 16) {
-      float v[16];
+      float v[16], bb[16];
       tmem_ld16(tlane + c, v);
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        const float4 t = *((const float4 *)(bias + c) + q);
+        bb[4 * q] = t.x; bb[4 * q + 1] = t.y; bb[4 * q + 2] = t.z; bb[4 * q + 3] = t.w;
+      }
       if (layer == 0) {
 #pragma unroll
-        for (int i = 0; i < 16; i += 2)
-          *(__nv_bfloat162 *)(sA + canon(r, c + i)) =
-              __floats2bfloat162_rn(silu(v[i] + bias[c + i]), silu(v[i + 1] + bias[c + i + 1]));
+        for (int i = 0; i < 16; i += 8)
+          store8(sA + canon(r, c + i), silu(v[i] + bb[i]), silu(v[i + 1] + bb[i + 1]), silu(v[i + 2] + bb[i + 2]),
+                 silu(v[i + 3] + bb[i + 3]), silu(v[i + 4] + bb[i + 4]), silu(v[i + 5] + bb[i + 5]),
+                 silu(v[i + 6] + bb[i + 6]), silu(v[i + 7] + bb[i + 7]));
       } else {
+        float ww[16];
 #pragma unroll
-        for (int i = 0; i < 16; i++) out = fmaf(silu(v[i] + bias[c + i]), p.w4[c + i], out);
+        for (int q = 0; q < 4; q++) {
+          const float4 t = *((const float4 *)(sw4 + c) + q);
+          ww[4 * q] = t.x; ww[4 * q + 1] = t.y; ww[4 * q + 2] = t.z; ww[4 * q + 3] = t.w;
+        }
+#pragma unroll
+        for (int i = 0; i < 16; i++) out = fmaf(silu(v[i] + bb[i]), ww[i], out);
       }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
