@@ -341,6 +341,7 @@ def run_gb300(args, rank, local, world, dist):
                 "frac": round(achieved / peak, 5), "traffic": traffic,
                 "traffic_source": "ncu capture (profiles/k_rot_slices_config1_fp64.md)" if traffic else None,
                 "binding_limit": "FP64 pipe (ncu: sm__pipe_fp64_cycles_active 54.7 % of peak)" if traffic else None,
+                "fp64_pipe_active_frac": 0.547 if traffic else None,
                 "kernel": kname, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
                 "per_launch_us": round(per_launch_ms * 1e3, 3), "algorithmic_bytes_per_launch": int(bytes_launch),
                 "pass_ms_by_kind": {k: round(v, 3) for k, v in zip(kinds, ms)},
