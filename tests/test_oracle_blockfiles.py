@@ -61,6 +61,8 @@ def test_density_files(tmp_path, case):
         assert _files(a) == _files(b) and _files(a), (_files(a), _files(b))
         for f in _files(a):
             _same(a / f, b / f)
+            os.remove(a / f)                   # the 3D files are 2 x 10^8 bytes each
+            os.remove(b / f)
 
 
 def test_exchange_and_area_files(tmp_path):
