@@ -32,7 +32,8 @@ constexpr int kW1B = (kIn + 1) * kH * 4;   // W1 and b1 (contiguous parameters),
 constexpr int kVecB = 3 * kH * 4;           // b2, then b3 and w4 (contiguous), FP32
 // + barriers, the TMEM address, the half sums, then W1, b1, b2, b3, w4
 constexpr int kSmem = kA + kB + 2048 + kW1B + kVecB;
-constexpr int kSmemT = kA + kB + 8192; // + the column-sum buffer of the training kernel
+// + the column-sum buffer of the training kernel, then W1, b1, b2, b3, w4
+constexpr int kSmemT = kA + kB + 8192 + (kIn + 1) * kH * 4 + 3 * kH * 4;
 // the parameter vector: w1[6][256], b1, w2[256][256], b2, w3[256][256], b3, w4, b4
 constexpr int kOW1 = 0, kOB1 = kOW1 + kIn * kH, kOW2 = kOB1 + kH, kOB2 = kOW2 + kH * kH, kOW3 = kOB2 + kH,
               kOB3 = kOW3 + kH * kH, kOW4 = kOB3 + kH, kOB4 = kOW4 + kH, kNP = kOB4 + 1;
@@ -426,6 +427,9 @@ __global__ void __launch_bounds__(kRows) k_mlp_train(MlpTrainParams p, unsigned 
   uint64_t *bar_m = bar_w + 1;
   uint32_t *tslot = (uint32_t *)(bar_w + 2);
   float *red = (float *)(smem + kA + kB + 64);          // [4][256]
+  uint64_t *bar_x = bar_w + 3;                          // the copies of W1 and the vectors
+  float *sw1 = (float *)(smem + kA + kB + 8192), *sb1 = sw1 + kIn * kH;
+  float *sb2 = sb1 + kH, *sb3 = sb2 + kH, *sw4 = sb3 + kH;
   const int tid = threadIdx.x, warp = tid >> 5, cta = blockIdx.x;
   const int row = cta * kRows + tid;
   const bool live = row < p.n;
@@ -434,7 +438,12 @@ __global__ void __launch_bounds__(kRows) k_mlp_train(MlpTrainParams p, unsigned 
   if (tid == 0) {
     mbar_init(bar_w, 1);
     mbar_init(bar_m, 1);
+    mbar_init(bar_x, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    bulk_expect(bar_x, (kIn + 1) * kH * 4 + 3 * kH * 4);
+    bulk_copy(sw1, p.w.w1, (kIn + 1) * kH * 4, bar_x);    // W1, b1
+    bulk_copy(sb2, p.w.b2, kH * 4, bar_x);
+    bulk_copy(sb3, p.w.b3, 2 * kH * 4, bar_x);            // b3, w4
   }
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)), "r"(512)
@@ -446,7 +455,7 @@ __global__ void __launch_bounds__(kRows) k_mlp_train(MlpTrainParams p, unsigned 
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tslot, tlane = tmem + ((uint32_t)(warp * 32) << 16);
   unsigned pw = 0, pm = 0;
-  bool ok = true;
+  bool ok = __syncthreads_and(mbar_wait(bar_x, 0));
   auto load_b = [&](const char *src, uint32_t bytes, char *dst) {
     if (tid == 0) bulk_load(dst, src, bytes, bar_w);
     ok = ok && mbar_wait(bar_w, pw);
@@ -463,10 +472,10 @@ __global__ void __launch_bounds__(kRows) k_mlp_train(MlpTrainParams p, unsigned 
   for (int i = 0; i < kIn; i++) xin[i] = live ? p.x[(size_t)row * kIn + i] : 0.0f;
   const float ey = live ? p.e[row] : 0.0f;
   for (int j = 0; j < kH; j += 2) {
-    float z0 = p.w.b1[j], z1 = p.w.b1[j + 1];
+    float z0 = sb1[j], z1 = sb1[j + 1];
     for (int i = 0; i < kIn; i++) {
-      z0 = fmaf(xin[i], p.w.w1[i * kH + j], z0);
-      z1 = fmaf(xin[i], p.w.w1[i * kH + j + 1], z1);
+      z0 = fmaf(xin[i], sw1[i * kH + j], z0);
+      z1 = fmaf(xin[i], sw1[i * kH + j + 1], z1);
     }
     __nv_bfloat162 h = __floats2bfloat162_rn(silu(z0), silu(z1));
     *(__nv_bfloat162 *)(sA + canon(tid, j)) = h;
@@ -484,7 +493,7 @@ __global__ void __launch_bounds__(kRows) k_mlp_train(MlpTrainParams p, unsigned 
     tmem_ld16(tlane + c, v);
 #pragma unroll
     for (int i = 0; i < 16; i += 2) {
-      float za = v[i] + p.w.b2[c + i], zb = v[i + 1] + p.w.b2[c + i + 1];
+      float za = v[i] + sb2[c + i], zb = v[i + 1] + sb2[c + i + 1];
       z2g[(size_t)tid * kH + c + i] = za;
       z2g[(size_t)tid * kH + c + i + 1] = zb;
       __nv_bfloat162 h = __floats2bfloat162_rn(silu(za), silu(zb));
@@ -504,7 +513,7 @@ __global__ void __launch_bounds__(kRows) k_mlp_train(MlpTrainParams p, unsigned 
     float v[16];
     tmem_ld16(tlane + c, v);
 #pragma unroll
-    for (int i = 0; i < 16; i++) y = fmaf(silu(v[i] + p.w.b3[c + i]), p.w.w4[c + i], y);
+    for (int i = 0; i < 16; i++) y = fmaf(silu(v[i] + sb3[c + i]), sw4[c + i], y);
   }
   const float dy = live ? p.gscale * (y - ey) : 0.0f;
   // loss, db4
@@ -528,9 +537,9 @@ __global__ void __launch_bounds__(kRows) k_mlp_train(MlpTrainParams p, unsigned 
     tmem_ld16(tlane + c, v);
 #pragma unroll
     for (int i = 0; i < 16; i++) {
-      float z = v[i] + p.w.b3[c + i];
+      float z = v[i] + sb3[c + i];
       h3[i] = silu(z) * dy;
-      dz[i] = dy * p.w.w4[c + i] * dsilu(z);
+      dz[i] = dy * sw4[c + i] * dsilu(z);
     }
     col_sum16(h3, c, red);
     __syncthreads();
@@ -598,8 +607,8 @@ __global__ void __launch_bounds__(kRows) k_mlp_train(MlpTrainParams p, unsigned 
     tmem_ld16(tlane + c, v);
 #pragma unroll
     for (int i = 0; i < 16; i++) {
-      float z = p.w.b1[c + i];
-      for (int q = 0; q < kIn; q++) z = fmaf(xin[q], p.w.w1[q * kH + c + i], z);
+      float z = sb1[c + i];
+      for (int q = 0; q < kIn; q++) z = fmaf(xin[q], sw1[q * kH + c + i], z);
       dz[i] = v[i] * dsilu(z);
     }
     col_sum16(dz, c, red);
