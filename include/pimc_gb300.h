@@ -154,6 +154,9 @@ pimc_status pimc_area_estim3d(pimc_handle *h, int iframe, const double *mass, do
  *                           sums[6] as pimc_area_estimators' out
  *  pimc_save_area_estim3d   SaveAreaEstim3D (mc_estim.cc:2670-2720): .sffs3d / .mffs3d,
  *                           appended; areas[6], inert[9] as pimc_area_estim3d's out[3..17]
+ *  pimc_save_rcf            SaveRCF (mc_estim.cc:1141-1189): .rcf from rcf[10][Q], GetRCF's
+ *                           ten rows summed (row 0 = pimc_rcf's output; rows 1..9 count the
+ *                           (origin, lag) pairs, in block mode those with n.n < 0.9999999)
  * gr1d/gr2d/gr3d are laid out as pimc_densities_read writes them. */
 pimc_status pimc_save_densities_1d(const pimc_system *sys, const char *fname, double acount, const double *gr1d,
                                    const double *gr2d);
@@ -169,6 +172,7 @@ pimc_status pimc_save_area_estimators(const pimc_system *sys, const char *fname,
                                       int bstype, const double *sums, double mass);
 pimc_status pimc_save_area_estim3d(const pimc_system *sys, const char *fname, double acount, long blocknumb,
                                    int iframe, int bstype, const double *areas, const double *inert, double mass);
+pimc_status pimc_save_rcf(const pimc_system *sys, const char *fname, double acount, int mode, const double *rcf);
 
 /* ---- worm algorithm (mc_qworm.cc) ------------------------------------------ */
 

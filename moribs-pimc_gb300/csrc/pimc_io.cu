@@ -365,3 +365,36 @@ extern "C" pimc_status pimc_save_area_estim3d(const pimc_system *s, const char *
   o.end();
   return PIMC_OK;
 }
+
+// SaveRCF (mc_estim.cc:1141-1189): the .rcf file (mode 1: _sum.rcf) of the
+// rotational correlation functions.  rcf[10][Q] are the ten rows of GetRCF's
+// accumulator summed over the samples (mc_estim.cc:1099-1139): row 0 the sum
+// of n(0).n(tau) (pimc_rcf's output), rows 1..9 the Legendre rows, which the
+// reference accumulates as 1 per (origin, lag) -- in its block accumulator
+// only where n(0).n(tau) < 0.9999999 (PLONE, mc_confg.h:64).  Q + 1 lines of
+// the imaginary time it*tau_rot (tau_rot = beta/Q, mc_setup.cc:377) and row 0
+// over acount Q, two blank lines, a "#" line, then Q + 1 lines of the time
+// and rows 1..9 over acount Q.
+extern "C" pimc_status pimc_save_rcf(const pimc_system *s, const char *fname, double acount, int mode,
+                                     const double *rcf)
+{
+  if (!valid(s, fname) || !rcf || (mode != 0 && mode != 1) || s->nrotslices <= 0 || !(s->temperature > 0.0))
+    return PIMC_ERR_BAD_ARG;
+  const int Q = s->nrotslices, nrcf = 10;      // NUMB_RCF (mc_confg.h:58)
+  const double beta = 1.0 / s->temperature, rtau = beta / (double)Q;
+  Out o(std::string(fname) + (mode ? "_sum" : "") + ".rcf", false);
+  if (!o.f) return PIMC_ERR_BAD_ARG;
+  const double norm = acount * (double)Q;
+  for (int it = 0; it <= Q; it++) {
+    o.num((double)it * rtau);
+    o.num(rcf[it % Q] / norm);
+    o.end();
+  }
+  fputs("\n\n#\n", o.f);
+  for (int it = 0; it <= Q; it++) {
+    o.num((double)it * rtau);
+    for (int ip = 1; ip < nrcf; ip++) o.num(rcf[(size_t)ip * Q + it % Q] / norm);
+    o.end();
+  }
+  return PIMC_OK;
+}

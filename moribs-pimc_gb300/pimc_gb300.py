@@ -82,6 +82,7 @@ def load(path=LIBPATH):
     L.pimc_save_exchange_length.argtypes = [sp, cc, C.c_double, C.c_long, C.c_int, _dp, _ip, C.c_int]
     L.pimc_save_area_estimators.argtypes = [sp, cc, C.c_double, C.c_long, C.c_int, _dp, C.c_double]
     L.pimc_save_area_estim3d.argtypes = [sp, cc, C.c_double, C.c_long, C.c_int, C.c_int, _dp, _dp, C.c_double]
+    L.pimc_save_rcf.argtypes = [sp, cc, C.c_double, C.c_int, _dp]
     L.pimc_asymrho.argtypes = [C.c_int, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, _dp, C.c_int,
                                _dp, _dp, _dp, _dp]
     L.pimc_densities_accumulate.argtypes = [vp]
@@ -613,3 +614,11 @@ def save_area_estim3d(w, fname, acount, blocknumb, iframe, bstype, areas, inert,
     i = np.ascontiguousarray(inert, dtype=np.float64)
     _chk(L.pimc_save_area_estim3d(C.byref(s), fname.encode(), float(acount), int(blocknumb), int(iframe),
                                   int(bstype), dptr(a), dptr(i), float(mass)), "pimc_save_area_estim3d")
+
+
+def save_rcf(w, fname, acount, mode, rcf):
+    L = load()
+    s = make_system(w)
+    r = np.ascontiguousarray(rcf, dtype=np.float64)
+    _chk(L.pimc_save_rcf(C.byref(s), fname.encode(), float(acount), int(mode), dptr(r)), "pimc_save_rcf")
+

@@ -430,6 +430,7 @@ class Reference:
         L.ref_save_exchange_length.argtypes = [C.c_char_p, C.c_double, C.c_long]
         L.ref_save_area_estimators.argtypes = [C.c_char_p, C.c_double, C.c_long]
         L.ref_save_area_estim3d.argtypes = [C.c_char_p, C.c_double, C.c_long, C.c_int]
+        L.ref_rcf_save.argtypes = [C.c_char_p, C.c_double, C.c_int, _dp]
         L.ref_tau.restype = C.c_double
         L.ref_lambda.restype = C.c_double
         L.ref_lambda.argtypes = [C.c_int]
@@ -566,6 +567,12 @@ class Reference:
 
     def save_area_estim3d(self, fname, acount, blocknumb, iframe):
         self.L.ref_save_area_estim3d(fname.encode(), float(acount), int(blocknumb), int(iframe))
+
+    def rcf_save(self, fname, acount, mode):
+        """GetRCF on cleared accumulators, then SaveRCF; returns the ten rows written."""
+        r = np.zeros((10, self.w.nrotslices))
+        self.L.ref_rcf_save(fname.encode(), float(acount), int(mode), dptr(r))
+        return r
 
 
 def linden(temprt, nslice, bconst, npt, iodevn=-1):

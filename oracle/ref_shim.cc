@@ -133,8 +133,10 @@ extern double **_gr1D_sum, ***_gr2D_sum, **_gr3D_sum, *_ploops;
 extern double _areas[2], _area2[2], _inert[2];
 extern double _areas3DMFF[6], _inert3DMFF[9], _areas3DSFF[6], _inert3DSFF[9];
 extern int NUMB_DENS1D, NUMB_DENS2D, NUMB_DENS3D;
+extern double **_rcf, **_rcf_sum;
 void densities_reset(int);
 void super_reset(void);
+void rcf_reset(int);
 // histogram sizes of mc_estim.cc:25-27 (file-scope constants there)
 static const int MC_BINSR_REF = PIMC_BINSR, MC_BINST_REF = PIMC_BINST, MC_BINSC_REF = PIMC_BINSC;
 
@@ -426,6 +428,19 @@ void ref_save_area_estimators(const char *fname, double acount, long blocknumb)
 void ref_save_area_estim3d(const char *fname, double acount, long blocknumb, int iframe)
 {
   SaveAreaEstim3D(fname, acount, blocknumb, iframe);
+}
+
+// GetRCF once into cleared accumulators, then SaveRCF; rcf[10][Q] = the
+// accumulator the file was written from (block or total)
+void ref_rcf_save(const char *fname, double acount, int mode, double *rcf)
+{
+  rcf_reset(MC_BLOCK);
+  rcf_reset(MC_TOTAL);
+  GetRCF();
+  double **src = mode == MC_TOTAL ? _rcf_sum : _rcf;
+  for (int ip = 0; ip < NUMB_RCF; ip++)
+    for (int it = 0; it < NumbRotTimes; it++) rcf[ip * NumbRotTimes + it] = src[ip][it];
+  SaveRCF(fname, acount, mode);
 }
 
 }  // extern "C"

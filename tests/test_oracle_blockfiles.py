@@ -90,3 +90,20 @@ def test_exchange_and_area_files(tmp_path):
     assert _files(a) == _files(b) == ["run.mffs3d", "run.prl", "run.sffs3d", "run.sup"]
     for f in _files(a):
         _same(a / f, b / f)
+
+
+def test_rcf_file(tmp_path):
+    w = W.config0(**C0S)
+    r = O.Reference(w)
+    a, b = tmp_path / "ref", tmp_path / "gb"
+    a.mkdir()
+    b.mkdir()
+    for mode in (0, 1):
+        rows = r.rcf_save(str(a / "run"), 2.0, mode)
+        # row 0 is what pimc_rcf returns for this path (GPU-side: test_gpu_parity)
+        np.testing.assert_allclose(rows[0], O.Oracle(w).rcf(), rtol=1e-12, atol=1e-12)
+        G.save_rcf(w, str(b / "run"), 2.0, mode, rows)
+    assert _files(a) == _files(b) == ["run.rcf", "run_sum.rcf"]
+    for f in _files(a):
+        _same(a / f, b / f)
+
