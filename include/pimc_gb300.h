@@ -146,6 +146,7 @@ pimc_status pimc_area_estim3d(pimc_handle *h, int iframe, const double *mass, do
  * type (BSTYPE) and mass its mass in amu.
  *  pimc_save_densities_1d   SaveDensities1D (mc_estim.cc:1327-1443): .gra;
  *                           with a linear impurity also .gri and .grt from gr2d
+ *  pimc_save_gra_sum        SaveGraSum (mc_estim.cc:1288-1325): _sum.gra
  *  pimc_save_densities_2d   SaveDensities2D (mc_estim.cc:1666-1726): .g2d
  *  pimc_save_densities_3d   SaveDensities3D (mc_estim.cc:1728-1800): .g3d
  *  pimc_save_rho_1d         SaveRho1D's .gri, .grt, .grc (mc_estim.cc:1445-1590)
@@ -160,6 +161,7 @@ pimc_status pimc_area_estim3d(pimc_handle *h, int iframe, const double *mass, do
  * gr1d/gr2d/gr3d are laid out as pimc_densities_read writes them. */
 pimc_status pimc_save_densities_1d(const pimc_system *sys, const char *fname, double acount, const double *gr1d,
                                    const double *gr2d);
+pimc_status pimc_save_gra_sum(const pimc_system *sys, const char *fname, double acount, const double *gr1d);
 pimc_status pimc_save_densities_2d(const pimc_system *sys, const char *fname, double acount, int mode,
                                    const double *gr2d);
 pimc_status pimc_save_densities_3d(const pimc_system *sys, const char *fname, double acount, int mode,

@@ -155,6 +155,25 @@ extern "C" pimc_status pimc_save_densities_1d(const pimc_system *s, const char *
   return PIMC_OK;
 }
 
+// SaveGraSum (mc_estim.cc:1288-1325): _sum.gra, the accumulated pair
+// distributions normalised to one over r (no Jacobian)
+extern "C" pimc_status pimc_save_gra_sum(const pimc_system *s, const char *fname, double acount, const double *gr1d)
+{
+  if (!valid(s, fname) || !gr1d) return PIMC_ERR_BAD_ARG;
+  const Bins b;
+  const int nd1 = atom_types(s);
+  Out o(std::string(fname) + "_sum.gra", false);
+  if (!o.f) return PIMC_ERR_BAD_ARG;
+  const double norma = b.dr * acount * (double)(s->nslices);
+  for (int ir = 0; ir < PIMC_BINSR; ir++) {
+    o.num(b.r(ir));
+    for (int id = 0; id < nd1; id++)
+      o.num(gr1d[(size_t)id * PIMC_BINSR + ir] / (norma * (s->type[id].numb * (s->type[id].numb - 1)) / 2.0));
+    o.end();
+  }
+  return PIMC_OK;
+}
+
 // SaveDensities2D (mc_estim.cc:1666-1726): .g2d (mode 1: _sum.g2d) with a
 // linear impurity
 extern "C" pimc_status pimc_save_densities_2d(const pimc_system *s, const char *fname, double acount, int mode,

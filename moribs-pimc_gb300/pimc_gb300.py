@@ -77,6 +77,7 @@ def load(path=LIBPATH):
     L.pimc_linden.argtypes = [C.c_int, C.c_int, _dp, _ip, C.c_double, C.c_int, C.c_int, _dp]
     sp, cc = C.POINTER(PimcSystem), C.c_char_p
     L.pimc_save_densities_1d.argtypes = [sp, cc, C.c_double, _dp, _dp]
+    L.pimc_save_gra_sum.argtypes = [sp, cc, C.c_double, _dp]
     for n in ("pimc_save_densities_2d", "pimc_save_densities_3d", "pimc_save_rho_1d"):
         getattr(L, n).argtypes = [sp, cc, C.c_double, C.c_int, _dp]
     L.pimc_save_exchange_length.argtypes = [sp, cc, C.c_double, C.c_long, C.c_int, _dp, _ip, C.c_int]
@@ -574,8 +575,8 @@ def _arr(a, n=None):
 
 def save_densities(w, box, fname, acount, mode, gr1d, gr2d, gr3d):
     """The density files of one block (mode 0) or of the run (mode 1):
-    SaveDensities1D (block only), SaveDensities2D, SaveDensities3D and
-    SaveRho1D as the reference's block and run ends call them
+    SaveDensities1D (block) or SaveGraSum (run), SaveDensities2D,
+    SaveDensities3D and SaveRho1D as the reference's block and run ends call them
     (mc_main.cc:715-734, 445-460).  gr?d as Sampler.densities_read returns
     them; box = the reference's BoxSize."""
     L = load()
@@ -585,6 +586,8 @@ def save_densities(w, box, fname, acount, mode, gr1d, gr2d, gr3d):
     fn = fname.encode()
     if mode == 0:
         _chk(L.pimc_save_densities_1d(C.byref(s), fn, float(acount), p1, p2), "pimc_save_densities_1d")
+    else:
+        _chk(L.pimc_save_gra_sum(C.byref(s), fn, float(acount), p1), "pimc_save_gra_sum")
     _chk(L.pimc_save_densities_2d(C.byref(s), fn, float(acount), int(mode), p2), "pimc_save_densities_2d")
     _chk(L.pimc_save_densities_3d(C.byref(s), fn, float(acount), int(mode), p3), "pimc_save_densities_3d")
     _chk(L.pimc_save_rho_1d(C.byref(s), fn, float(acount), int(mode), p3), "pimc_save_rho_1d")

@@ -411,6 +411,7 @@ void ref_box_size(double *b)
 void ref_save_densities(const char *fname, double acount, int mode)
 {
   SaveDensities1D(fname, acount);
+  if (mode == MC_TOTAL) SaveGraSum(fname, acount);
   if (IMPURITY && MCAtom[IMTYPE].molecule == 1) SaveDensities2D(fname, acount, mode);
   if (IMPURITY && MCAtom[IMTYPE].molecule == 2) {
     SaveDensities3D(fname, acount, mode);
