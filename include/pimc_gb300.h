@@ -175,6 +175,13 @@ pimc_status pimc_save_area_estimators(const pimc_system *sys, const char *fname,
 pimc_status pimc_save_area_estim3d(const pimc_system *sys, const char *fname, double acount, long blocknumb,
                                    int iframe, int bstype, const double *areas, const double *inert, double mass);
 pimc_status pimc_save_rcf(const pimc_system *sys, const char *fname, double acount, int mode, const double *rcf);
+/* The energy block of MCGetAverage / SaveEnergy (mc_main.cc:551-616, 764-795):
+ * pimc_energy_accumulate adds one sample's terms (from pimc_estimators' out[5])
+ * to sums[7] = {E_kin, E_pot, E_rot, ErotSQ, Cv, Cv_trans, Cv_rot} block sums;
+ * pimc_save_energy appends the block's .eng line (values over acount). */
+pimc_status pimc_energy_accumulate(const pimc_system *sys, const double *est, double *sums);
+pimc_status pimc_save_energy(const pimc_system *sys, const char *fname, double acount, long blocknumb,
+                             const double *sums);
 
 /* ---- worm algorithm (mc_qworm.cc) ------------------------------------------ */
 

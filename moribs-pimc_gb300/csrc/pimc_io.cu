@@ -417,3 +417,61 @@ extern "C" pimc_status pimc_save_rcf(const pimc_system *s, const char *fname, do
   }
   return PIMC_OK;
 }
+
+// MCGetAverage's per-sample energy terms (mc_main.cc:551-616) from
+// pimc_estimators' out[5] = {E_kin, E_pot, E_rot, ErotSQ, Erot_termSQ},
+// added to the block sums[7] = {_bkin, _bpot, _brot, _brotsq, _bCv,
+// _bCv_trans, _bCv_rot}; E_rot and ErotSQ count only with ROTATION.
+// beta = 1/T, tau = beta/P (mc_setup.cc:373-377), N = all atoms, NDIM = 3.
+extern "C" pimc_status pimc_energy_accumulate(const pimc_system *s, const double *est, double *sums)
+{
+  if (!valid(s, "") || !est || !sums || !(s->temperature > 0.0)) return PIMC_ERR_BAD_ARG;
+  int natoms = 0;
+  for (int t = 0; t < s->ntypes; t++) natoms += s->type[t].numb;
+  const double beta = 1.0 / s->temperature, tau = beta / (double)s->nslices;
+  const double skin = est[0], spot = est[1];
+  double srot = 0.0;
+  sums[0] += skin;
+  sums[1] += spot;
+  if (s->rotation) {
+    srot = est[2];
+    sums[2] += srot;
+    sums[3] += est[3];
+  }
+  const double d = (double)(3 * natoms);
+  const double sCv = -0.5 * d / (beta * tau) - (d * 0.5 / tau - skin - spot - srot) * (d * 0.5 / tau - skin - spot - srot) +
+                     (2.0 / beta) * (0.5 * d / tau - skin) + est[4] - est[3];
+  const double sCv_trans = -0.5 * d / (beta * tau) - (d * 0.5 / tau - skin) * (d * 0.5 / tau - skin) +
+                           (2.0 / beta) * (0.5 * d / tau - skin);
+  const double sCv_rot = -srot * srot + est[4] - est[3];
+  sums[4] += sCv;
+  sums[5] += sCv_trans;
+  sums[6] += sCv_rot;
+  return PIMC_OK;
+}
+
+// SaveEnergy (mc_main.cc:764-795): one appended .eng line per block from the
+// block sums of pimc_energy_accumulate over acount samples -- the block
+// number, E_kin, E_pot, E_kin + E_pot, E_rot, ErotSQ, the total, Cv, Cv_trans
+// and Cv_rot, each over acount.
+extern "C" pimc_status pimc_save_energy(const pimc_system *s, const char *fname, double acount, long blocknumb,
+                                        const double *sums)
+{
+  if (!valid(s, fname) || !sums) return PIMC_ERR_BAD_ARG;
+  Out o(std::string(fname) + ".eng", true);
+  if (!o.f) return PIMC_ERR_BAD_ARG;
+  const double e = 1.0;                         // Units.energy
+  o.integer(blocknumb, kWidthBlock);
+  o.num(sums[0] * e / acount);
+  o.num(sums[1] * e / acount);
+  o.num((sums[0] + sums[1]) * e / acount);
+  o.num(sums[2] * e / acount);
+  o.num(sums[3] * (e * e) / acount);
+  o.num((sums[0] + sums[1] + sums[2]) * e / acount);
+  o.num(sums[4] / acount);
+  o.num(sums[5] / acount);
+  o.num(sums[6] / acount);
+  o.end();
+  return PIMC_OK;
+}
+

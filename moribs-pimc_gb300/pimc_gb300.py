@@ -84,6 +84,8 @@ def load(path=LIBPATH):
     L.pimc_save_area_estimators.argtypes = [sp, cc, C.c_double, C.c_long, C.c_int, _dp, C.c_double]
     L.pimc_save_area_estim3d.argtypes = [sp, cc, C.c_double, C.c_long, C.c_int, C.c_int, _dp, _dp, C.c_double]
     L.pimc_save_rcf.argtypes = [sp, cc, C.c_double, C.c_int, _dp]
+    L.pimc_energy_accumulate.argtypes = [sp, _dp, _dp]
+    L.pimc_save_energy.argtypes = [sp, cc, C.c_double, C.c_long, _dp]
     L.pimc_asymrho.argtypes = [C.c_int, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, _dp, C.c_int,
                                _dp, _dp, _dp, _dp]
     L.pimc_densities_accumulate.argtypes = [vp]
@@ -624,4 +626,22 @@ def save_rcf(w, fname, acount, mode, rcf):
     s = make_system(w)
     r = np.ascontiguousarray(rcf, dtype=np.float64)
     _chk(L.pimc_save_rcf(C.byref(s), fname.encode(), float(acount), int(mode), dptr(r)), "pimc_save_rcf")
+
+
+def energy_accumulate(w, est, sums=None):
+    """MCGetAverage's energy terms of one sample added to sums[7] (returned)."""
+    L = load()
+    s = make_system(w)
+    e = np.ascontiguousarray(est, dtype=np.float64)
+    out = np.zeros(7) if sums is None else np.ascontiguousarray(sums, dtype=np.float64)
+    _chk(L.pimc_energy_accumulate(C.byref(s), dptr(e), dptr(out)), "pimc_energy_accumulate")
+    return out
+
+
+def save_energy(w, fname, acount, blocknumb, sums):
+    L = load()
+    s = make_system(w)
+    sm = np.ascontiguousarray(sums, dtype=np.float64)
+    _chk(L.pimc_save_energy(C.byref(s), fname.encode(), float(acount), int(blocknumb), dptr(sm)),
+         "pimc_save_energy")
 

@@ -431,6 +431,7 @@ class Reference:
         L.ref_save_area_estimators.argtypes = [C.c_char_p, C.c_double, C.c_long]
         L.ref_save_area_estim3d.argtypes = [C.c_char_p, C.c_double, C.c_long, C.c_int]
         L.ref_rcf_save.argtypes = [C.c_char_p, C.c_double, C.c_int, _dp]
+        L.ref_energy_block.argtypes = [C.c_char_p, C.c_char_p, C.c_long, _dp]
         L.ref_tau.restype = C.c_double
         L.ref_lambda.restype = C.c_double
         L.ref_lambda.argtypes = [C.c_int]
@@ -567,6 +568,14 @@ class Reference:
 
     def save_area_estim3d(self, fname, acount, blocknumb, iframe):
         self.L.ref_save_area_estim3d(fname.encode(), float(acount), int(blocknumb), int(iframe))
+
+    def energy_block(self, workdir, fname, blocknumb):
+        """MCResetBlockAverage, one MCGetAverage (run in workdir), SaveEnergy;
+        returns the seven block sums."""
+        out = np.zeros(7)
+        if self.L.ref_energy_block(str(workdir).encode(), fname.encode(), int(blocknumb), dptr(out)) != 0:
+            raise RuntimeError("ref_energy_block failed")
+        return out
 
     def rcf_save(self, fname, acount, mode):
         """GetRCF on cleared accumulators, then SaveRCF; returns the ten rows written."""

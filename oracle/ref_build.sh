@@ -4,7 +4,8 @@
 # tree, together with oracle/ref_shim.cc (replay RNG + Fortran-leaf bindings)
 # and the oracle's C leaves, into oracle/_ref/libref.so.  The reference's own
 # build system is not used.  Left out on purpose:
-#   mc_main.cc  -- defines main() and the block loop (driven from the tests),
+#   mc_main.cc  -- compiled with its main() renamed (-Dmain=...): the tests
+#                  call its block averages and energy writers, not its loop,
 #   mc_randg.cc -- SPRNG streams, replaced by the replay generators in the shim,
 #   omprng.cc   -- runif()/randomseed(), replaced by the shim.
 # Usage: oracle/ref_build.sh [reference_dir]   (default: /root/reference)
@@ -23,6 +24,8 @@ for f in mc_piqmc mc_poten mc_utils mc_setup mc_input mc_estim mc_qworm rngstrea
   g++ $CXXFLAGS -c "$REF/$f.cc" -o "$OUT/$f.o" &
   pids="$pids $!"
 done
+g++ $CXXFLAGS -Dmain=pimc_reference_main_unused -c "$REF/mc_main.cc" -o "$OUT/mc_main.o" &
+pids="$pids $!"
 g++ $CXXFLAGS -c "$HERE/ref_shim.cc" -o "$OUT/ref_shim.o" &
 pids="$pids $!"
 gcc -std=gnu11 -O2 -fopenmp -fPIC -c "$HERE/pimc_oracle.c" -o "$OUT/pimc_oracle_leaves.o" &

@@ -123,6 +123,7 @@ extern "C" void caleng_(double *com_1, double *com_2, double *E_2H2O, double *Eu
 
 // reflections (vcord.f:190-546) are estimator-time symmetrisation moves that
 // the sampling path never calls; bound to a loud failure
+extern "C" void initconf_(double *, double *, int *, int *, int *, int *) { nrerror("ref_shim", "initconf_ not bound"); }
 extern "C" void reflec_(double *, double *, double *, double *, double *) { nrerror("ref_shim", "reflec_ not bound"); }
 extern "C" void rflmfx_(double *, double *, double *, double *, double *) { nrerror("ref_shim", "rflmfx_ not bound"); }
 extern "C" void rflmfy_(double *, double *, double *, double *, double *) { nrerror("ref_shim", "rflmfy_ not bound"); }
@@ -134,6 +135,11 @@ extern double _areas[2], _area2[2], _inert[2];
 extern double _areas3DMFF[6], _inert3DMFF[9], _areas3DSFF[6], _inert3DSFF[9];
 extern int NUMB_DENS1D, NUMB_DENS2D, NUMB_DENS3D;
 extern double **_rcf, **_rcf_sum;
+// block averages of mc_main.cc (file scope there)
+extern double avergCount, _bkin, _bpot, _brot, _brotsq, _bCv, _bCv_trans, _bCv_rot;
+void MCResetBlockAverage(void);
+void MCGetAverage(void);
+void SaveEnergy(const char[], double, long int);
 void densities_reset(int);
 void super_reset(void);
 void rcf_reset(int);
@@ -429,6 +435,22 @@ void ref_save_area_estimators(const char *fname, double acount, long blocknumb)
 void ref_save_area_estim3d(const char *fname, double acount, long blocknumb, int iframe)
 {
   SaveAreaEstim3D(fname, acount, blocknumb, iframe);
+}
+
+// one MCGetAverage (mc_main.cc:551-694) on a cleared block, then SaveEnergy
+// (mc_main.cc:764-795); sums = _bkin, _bpot, _brot, _brotsq, _bCv,
+// _bCv_trans, _bCv_rot.  Run in workdir: with bosons MCGetAverage appends to
+// permutation.tab in the working directory.
+int ref_energy_block(const char *workdir, const char *fname, long blocknumb, double *sums)
+{
+  char cwd[4096];
+  if (!getcwd(cwd, sizeof cwd) || chdir(workdir) != 0) return 1;
+  MCResetBlockAverage();
+  MCGetAverage();
+  const double v[7] = {_bkin, _bpot, _brot, _brotsq, _bCv, _bCv_trans, _bCv_rot};
+  for (int k = 0; k < 7; k++) sums[k] = v[k];
+  SaveEnergy(fname, avergCount, blocknumb);
+  return chdir(cwd) != 0;
 }
 
 // GetRCF once into cleared accumulators, then SaveRCF; rcf[10][Q] = the

@@ -107,3 +107,23 @@ def test_rcf_file(tmp_path):
     for f in _files(a):
         _same(a / f, b / f)
 
+
+@pytest.mark.parametrize("case", ["c0s", "c1s"])
+def test_energy_block(tmp_path, case):
+    """One MCGetAverage sample of the fixture path and its SaveEnergy line:
+    the C ABI's accumulation of the oracle's estimators (the oracle matches
+    the reference's estimators to rounding) gives the same sums and file."""
+    w = W.config0(**C0S) if case == "c0s" else W.config1(**C1S)
+    r = O.Reference(w)
+    a, b = tmp_path / "ref", tmp_path / "gb"
+    a.mkdir()
+    b.mkdir()
+    ref = r.energy_block(a, str(a / "run"), 5)
+    o = O.Oracle(w)
+    nonlinear = any(t["molecule"] == 2 for t in w.types)
+    rot, esq, ets = o.rot_energy(nonlinear)
+    sums = G.energy_accumulate(w, [o.kin_energy(), o.pot_energy_est(), rot, esq, ets])
+    np.testing.assert_allclose(sums, ref, rtol=1e-9, atol=1e-9 * np.max(np.abs(ref)))
+    G.save_energy(w, str(b / "run"), 1.0, 5, sums)
+    _same(a / "run.eng", b / "run.eng")
+
