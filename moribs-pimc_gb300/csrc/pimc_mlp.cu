@@ -381,7 +381,7 @@ struct MlpTrainParams {
   float gscale;                // d loss / d y = gscale * (y - e)
   // per-CTA scratch and partial gradients
   char *h1t, *h2t, *dzt;       // [cta][64 KB] each: h1^T, h2^T, dz^T (K = 128 canonical)
-  float *z2;                   // [cta][128][256]
+  float *z2;                   // [cta][256][128]: pre-activations of layer 2, column-major
   float *part;                 // [cta][kNP] partial gradients in the parameter order
   float *loss;                 // [cta]
 };
@@ -494,8 +494,8 @@ __global__ void __launch_bounds__(kRows) k_mlp_train(MlpTrainParams p, unsigned 
 #pragma unroll
     for (int i = 0; i < 16; i += 2) {
       float za = v[i] + sb2[c + i], zb = v[i + 1] + sb2[c + i + 1];
-      z2g[(size_t)tid * kH + c + i] = za;
-      z2g[(size_t)tid * kH + c + i + 1] = zb;
+      z2g[(size_t)(c + i) * kRows + tid] = za;             // column-major: a warp's rows are contiguous
+      z2g[(size_t)(c + i + 1) * kRows + tid] = zb;
       __nv_bfloat162 h = __floats2bfloat162_rn(silu(za), silu(zb));
       *(__nv_bfloat162 *)(sA + canon(tid, c + i)) = h;
       *(__nv_bfloat16 *)(h2t + canon128(c + i, tid)) = h.x;
@@ -575,7 +575,7 @@ __global__ void __launch_bounds__(kRows) k_mlp_train(MlpTrainParams p, unsigned 
     float v[16], dz[16];
     tmem_ld16(tlane + c, v);
 #pragma unroll
-    for (int i = 0; i < 16; i++) dz[i] = v[i] * dsilu(z2g[(size_t)tid * kH + c + i]);
+    for (int i = 0; i < 16; i++) dz[i] = v[i] * dsilu(z2g[(size_t)(c + i) * kRows + tid]);
     col_sum16(dz, c, red);
     __syncthreads();
     if (tid < 16) p.part[(size_t)cta * kNP + kOB2 + c + tid] = red[c + tid] + red[kH + c + tid] + red[2 * kH + c + tid] + red[3 * kH + c + tid];
