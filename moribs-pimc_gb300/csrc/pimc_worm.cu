@@ -23,6 +23,7 @@ constexpr int kMaxQ = 2 * (PIMC_WORM_MAXM + 1);   // the swap's new and old slic
 constexpr int kTermCap = 2560;                    // (query, partner) terms held in shared memory
 constexpr int kDrawCap = 32;                      // draws of each uniform stream held in shared memory
 constexpr int kGaussCap = 640;                    // gauss() draws held in shared memory
+constexpr int kPdCap = 512;                       // neighbour-table distances held in shared memory
 
 struct WormShared {
   int exists, ira, masha, atom_i, atom_m;   // the worm (TPathWorm)
@@ -54,6 +55,7 @@ struct WormShared {
   double term[kTermCap];                     // the (query, partner) terms of query_sums
   double dc[8 * kDrawCap];                   // the first draws of the uniform streams
   double gc[kGaussCap];                      // the first gauss() draws of the call
+  double pd[kPdCap];                         // get_ptable's distances while numb <= kPdCap
 };
 
 struct WormSrc {
@@ -322,8 +324,9 @@ __device__ double open_kin(const Ctx &c, const DevWorm &wk, const WormShared &sh
 // insertion sort gives (mc_utils.cc:206-230) -- as its rank; the first
 // MAXNEIGHBORS go to sh.ptd/pta/ptab[1..] and sh.pcount holds the number of
 // candidates.
-__device__ void get_ptable(const Ctx &c, const DevWorm &wk, WormShared &sh, const int *rindex, double *dall)
+__device__ void get_ptable(const Ctx &c, const DevWorm &wk, WormShared &sh, const int *rindex, double *gdall)
 {
+  double *dall = wk.numb <= kPdCap ? sh.pd : gdall;   // every rank reads all numb of them
   const int atomw = sh.pw_atom, pt0 = sh.pw_pt0, pt1 = sh.pw_pt1, segm = sh.pw_segm, t1 = sh.pw_t1;
   const size_t iw = bead(c, wk.first + atomw, pt0);
   const double rw[3] = {c.st.x[iw], c.st.y[iw], c.st.z[iw]};
