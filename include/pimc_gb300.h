@@ -182,6 +182,10 @@ pimc_status pimc_save_rcf(const pimc_system *sys, const char *fname, double acou
 pimc_status pimc_energy_accumulate(const pimc_system *sys, const double *est, double *sums);
 pimc_status pimc_save_energy(const pimc_system *sys, const char *fname, double acount, long blocknumb,
                              const double *sums);
+/* SaveSumEnergy (mc_main.cc:797-836): a line of the run's _sum.eng from the
+ * run sums of pimc_energy_accumulate (append = 0 starts the file). */
+pimc_status pimc_save_sum_energy(const pimc_system *sys, const char *fname, double acount, double numb,
+                                 const double *sums, int append);
 
 /* ---- worm algorithm (mc_qworm.cc) ------------------------------------------ */
 

@@ -475,3 +475,43 @@ extern "C" pimc_status pimc_save_energy(const pimc_system *s, const char *fname,
   return PIMC_OK;
 }
 
+// SaveSumEnergy (mc_main.cc:797-836): one line of the run's _sum.eng (opened
+// for writing at the start of the run, mc_main.cc:838-872: append = 0 for the
+// first line, 1 after) from the run sums of pimc_energy_accumulate over
+// acount samples: numb (the block count, printed as the reference prints a
+// double), E_kin, E_pot, their sum, E_rot, ErotSQ, the total, then the heat
+// capacities -beta/T [(3 N P T / 2 - <E>)^2 + <Cv terms>] for the total, the
+// translational part and (with -<E_rot> in place of the first term) the rotor.
+extern "C" pimc_status pimc_save_sum_energy(const pimc_system *s, const char *fname, double acount, double numb,
+                                            const double *sums, int append)
+{
+  if (!valid(s, fname) || !sums || !(s->temperature > 0.0)) return PIMC_ERR_BAD_ARG;
+  int natoms = 0;
+  for (int t = 0; t < s->ntypes; t++) natoms += s->type[t].numb;
+  const double T = s->temperature, beta = 1.0 / T, e = 1.0;   // Units.energy
+  Out o(std::string(fname) + "_sum.eng", append != 0);
+  if (!o.f) return PIMC_ERR_BAD_ARG;
+  fprintf(o.f, "%*.*e%s", kWidthBlock, 6, numb, kBlank);
+  o.num(sums[0] * e / acount);
+  o.num(sums[1] * e / acount);
+  o.num((sums[0] + sums[1]) * e / acount);
+  o.num(sums[2] * e / acount);
+  o.num(sums[3] * (e * e) / acount);
+  o.num((sums[0] + sums[1] + sums[2]) * e / acount);
+  const double npt = (double)(3 * natoms * s->nslices * T);
+  double cv = 0.5 * npt - (sums[0] + sums[1] + sums[2]) * e / acount;
+  cv = cv * cv + sums[4] * e * e / acount;
+  cv = -cv * beta / T;
+  o.num(cv);
+  double cvt = 0.5 * npt - sums[0] * e / acount;
+  cvt = cvt * cvt + sums[5] * e * e / acount;
+  cvt = -cvt * beta / T;
+  o.num(cvt);
+  double cvr = -sums[2] * e / acount;
+  cvr = cvr * cvr + sums[6] * e * e / acount;
+  cvr = -cvr * beta / T;
+  o.num(cvr);
+  o.end();
+  return PIMC_OK;
+}
+

@@ -86,6 +86,7 @@ def load(path=LIBPATH):
     L.pimc_save_rcf.argtypes = [sp, cc, C.c_double, C.c_int, _dp]
     L.pimc_energy_accumulate.argtypes = [sp, _dp, _dp]
     L.pimc_save_energy.argtypes = [sp, cc, C.c_double, C.c_long, _dp]
+    L.pimc_save_sum_energy.argtypes = [sp, cc, C.c_double, C.c_double, _dp, C.c_int]
     L.pimc_asymrho.argtypes = [C.c_int, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, _dp, C.c_int,
                                _dp, _dp, _dp, _dp]
     L.pimc_densities_accumulate.argtypes = [vp]
@@ -644,4 +645,12 @@ def save_energy(w, fname, acount, blocknumb, sums):
     sm = np.ascontiguousarray(sums, dtype=np.float64)
     _chk(L.pimc_save_energy(C.byref(s), fname.encode(), float(acount), int(blocknumb), dptr(sm)),
          "pimc_save_energy")
+
+
+def save_sum_energy(w, fname, acount, numb, sums, append=False):
+    L = load()
+    s = make_system(w)
+    sm = np.ascontiguousarray(sums, dtype=np.float64)
+    _chk(L.pimc_save_sum_energy(C.byref(s), fname.encode(), float(acount), float(numb), dptr(sm), int(bool(append))),
+         "pimc_save_sum_energy")
 

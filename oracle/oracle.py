@@ -432,6 +432,7 @@ class Reference:
         L.ref_save_area_estim3d.argtypes = [C.c_char_p, C.c_double, C.c_long, C.c_int]
         L.ref_rcf_save.argtypes = [C.c_char_p, C.c_double, C.c_int, _dp]
         L.ref_energy_block.argtypes = [C.c_char_p, C.c_char_p, C.c_long, _dp]
+        L.ref_sum_energy.argtypes = [C.c_char_p, C.c_double, _dp]
         L.ref_tau.restype = C.c_double
         L.ref_lambda.restype = C.c_double
         L.ref_lambda.argtypes = [C.c_int]
@@ -575,6 +576,14 @@ class Reference:
         out = np.zeros(7)
         if self.L.ref_energy_block(str(workdir).encode(), fname.encode(), int(blocknumb), dptr(out)) != 0:
             raise RuntimeError("ref_energy_block failed")
+        return out
+
+    def sum_energy(self, workdir, numb):
+        """InitTotalAverage, one MCGetAverage, SaveSumEnergy (into
+        workdir/<prefix>_sum.eng); returns the seven run totals."""
+        out = np.zeros(7)
+        if self.L.ref_sum_energy(str(workdir).encode(), float(numb), dptr(out)) != 0:
+            raise RuntimeError("ref_sum_energy failed")
         return out
 
     def rcf_save(self, fname, acount, mode):

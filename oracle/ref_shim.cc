@@ -140,6 +140,10 @@ extern double avergCount, _bkin, _bpot, _brot, _brotsq, _bCv, _bCv_trans, _bCv_r
 void MCResetBlockAverage(void);
 void MCGetAverage(void);
 void SaveEnergy(const char[], double, long int);
+extern double totalCount, _kin_total, _pot_total, _rot_total, _rotsq_total, _Cv_total, _Cv_trans_total, _Cv_rot_total;
+void InitTotalAverage(void);
+void DoneTotalAverage(void);
+void SaveSumEnergy(double, double);
 void densities_reset(int);
 void super_reset(void);
 void rcf_reset(int);
@@ -450,6 +454,23 @@ int ref_energy_block(const char *workdir, const char *fname, long blocknumb, dou
   const double v[7] = {_bkin, _bpot, _brot, _brotsq, _bCv, _bCv_trans, _bCv_rot};
   for (int k = 0; k < 7; k++) sums[k] = v[k];
   SaveEnergy(fname, avergCount, blocknumb);
+  return chdir(cwd) != 0;
+}
+
+// the run totals after one MCGetAverage and their SaveSumEnergy line
+// (InitTotalAverage opens <file prefix>_sum.eng in workdir); totals as the
+// seven sums of ref_energy_block
+int ref_sum_energy(const char *workdir, double numb, double *totals)
+{
+  char cwd[4096];
+  if (!getcwd(cwd, sizeof cwd) || chdir(workdir) != 0) return 1;
+  InitTotalAverage();
+  MCResetBlockAverage();
+  MCGetAverage();
+  const double v[7] = {_kin_total, _pot_total, _rot_total, _rotsq_total, _Cv_total, _Cv_trans_total, _Cv_rot_total};
+  for (int k = 0; k < 7; k++) totals[k] = v[k];
+  SaveSumEnergy(totalCount, numb);
+  DoneTotalAverage();
   return chdir(cwd) != 0;
 }
 

@@ -126,4 +126,11 @@ def test_energy_block(tmp_path, case):
     np.testing.assert_allclose(sums, ref, rtol=1e-9, atol=1e-9 * np.max(np.abs(ref)))
     G.save_energy(w, str(b / "run"), 1.0, 5, sums)
     _same(a / "run.eng", b / "run.eng")
+    # the run-total line (SaveSumEnergy) after the same single sample
+    tot = r.sum_energy(a, 3.0)
+    np.testing.assert_allclose(sums, tot, rtol=1e-9, atol=1e-9 * np.max(np.abs(tot)))
+    prefix = [f for f in os.listdir(a) if f.endswith("_sum.eng")]
+    assert len(prefix) == 1, os.listdir(a)
+    G.save_sum_energy(w, str(b / prefix[0][:-len("_sum.eng")]), 1.0, 3.0, sums)
+    _same(a / prefix[0], b / prefix[0])
 
