@@ -150,6 +150,7 @@ pimc_status pimc_area_estim3d(pimc_handle *h, int iframe, const double *mass, do
  *  pimc_save_densities_2d   SaveDensities2D (mc_estim.cc:1666-1726): .g2d
  *  pimc_save_densities_3d   SaveDensities3D (mc_estim.cc:1728-1800): .g3d
  *  pimc_save_rho_1d         SaveRho1D's .gri, .grt, .grc (mc_estim.cc:1445-1590)
+ *  pimc_save_rho_theta_chi  SaveRhoThetaChi (mc_estim.cc:1930-1996): .gtc
  *  pimc_save_exchange_length  SaveExchangeLength (mc_estim.cc:2021-2085): .prl, appended
  *  pimc_save_area_estimators  SaveAreaEstimators (mc_estim.cc:2596-2641): .sup, appended;
  *                           sums[6] as pimc_area_estimators' out
@@ -168,6 +169,8 @@ pimc_status pimc_save_densities_3d(const pimc_system *sys, const char *fname, do
                                    const double *gr3d);
 pimc_status pimc_save_rho_1d(const pimc_system *sys, const char *fname, double acount, int mode,
                              const double *gr3d);
+pimc_status pimc_save_rho_theta_chi(const pimc_system *sys, const char *fname, double acount, int mode,
+                                    const double *gr3d);
 pimc_status pimc_save_exchange_length(const pimc_system *sys, const char *fname, double acount, long blocknumb,
                                       int bstype, const double *ploops, const int *pindex, int print_xyz_prl);
 pimc_status pimc_save_area_estimators(const pimc_system *sys, const char *fname, double acount, long blocknumb,

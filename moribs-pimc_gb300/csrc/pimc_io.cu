@@ -305,6 +305,41 @@ extern "C" pimc_status pimc_save_rho_1d(const pimc_system *s, const char *fname,
   return PIMC_OK;
 }
 
+// SaveRhoThetaChi (mc_estim.cc:1930-1996): the (theta, chi) density around a
+// nonlinear impurity (.gtc, mode 1: _sum.gtc) from the 3D histogram summed
+// over r; a blank line after each theta row.
+extern "C" pimc_status pimc_save_rho_theta_chi(const pimc_system *s, const char *fname, double acount, int mode,
+                                               const double *gr3d)
+{
+  if (!valid(s, fname) || !gr3d || (mode != 0 && mode != 1)) return PIMC_ERR_BAD_ARG;
+  int kind = 0;
+  impurity(s, &kind);
+  if (kind != PIMC_NONLINEAR) return PIMC_OK;
+  const Bins b;
+  const int nd3 = atom_types(s) + 1;
+  const size_t nb = (size_t)PIMC_BINSR * PIMC_BINST * PIMC_BINSC;
+  Out o(std::string(fname) + (mode ? "_sum" : "") + ".gtc", false);
+  if (!o.f) return PIMC_ERR_BAD_ARG;
+  const double norm6 = b.dth * b.dch * (double)s->nslices * acount * (180.0 * 180.0 / (M_PI * M_PI));
+  for (int it = 0; it < PIMC_BINST; it++) {
+    const double theta = b.theta(it);
+    for (int ic = 0; ic < PIMC_BINSC; ic++) {
+      const double chi = b.chi(ic);
+      o.num(theta * 180.0 / M_PI);
+      o.num(chi * 180.0 / M_PI);
+      for (int id = 0; id < nd3; id++) {
+        double denstc = 0.0;
+        for (int ir = 0; ir < PIMC_BINSR; ir++)
+          denstc = denstc + gr3d[id * nb + ((size_t)ir * PIMC_BINST + it) * PIMC_BINSC + ic];
+        o.num(denstc / (norm6 * (double)s->type[id].numb));
+      }
+      o.end();
+    }
+    o.end();
+  }
+  return PIMC_OK;
+}
+
 // SaveExchangeLength (mc_estim.cc:2021-2085): one appended .prl line per
 // block -- the block number, the ground-state-loop and excited-loop weights
 // and their sum, the normalised count of every cycle length, PIndex and the

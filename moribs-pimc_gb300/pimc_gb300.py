@@ -78,7 +78,7 @@ def load(path=LIBPATH):
     sp, cc = C.POINTER(PimcSystem), C.c_char_p
     L.pimc_save_densities_1d.argtypes = [sp, cc, C.c_double, _dp, _dp]
     L.pimc_save_gra_sum.argtypes = [sp, cc, C.c_double, _dp]
-    for n in ("pimc_save_densities_2d", "pimc_save_densities_3d", "pimc_save_rho_1d"):
+    for n in ("pimc_save_densities_2d", "pimc_save_densities_3d", "pimc_save_rho_1d", "pimc_save_rho_theta_chi"):
         getattr(L, n).argtypes = [sp, cc, C.c_double, C.c_int, _dp]
     L.pimc_save_exchange_length.argtypes = [sp, cc, C.c_double, C.c_long, C.c_int, _dp, _ip, C.c_int]
     L.pimc_save_area_estimators.argtypes = [sp, cc, C.c_double, C.c_long, C.c_int, _dp, C.c_double]
@@ -579,7 +579,8 @@ def _arr(a, n=None):
 def save_densities(w, box, fname, acount, mode, gr1d, gr2d, gr3d):
     """The density files of one block (mode 0) or of the run (mode 1):
     SaveDensities1D (block) or SaveGraSum (run), SaveDensities2D,
-    SaveDensities3D and SaveRho1D as the reference's block and run ends call them
+    SaveDensities3D, SaveRho1D and SaveRhoThetaChi (block) as the reference's
+    block and run ends call them
     (mc_main.cc:715-734, 445-460).  gr?d as Sampler.densities_read returns
     them; box = the reference's BoxSize."""
     L = load()
@@ -594,6 +595,8 @@ def save_densities(w, box, fname, acount, mode, gr1d, gr2d, gr3d):
     _chk(L.pimc_save_densities_2d(C.byref(s), fn, float(acount), int(mode), p2), "pimc_save_densities_2d")
     _chk(L.pimc_save_densities_3d(C.byref(s), fn, float(acount), int(mode), p3), "pimc_save_densities_3d")
     _chk(L.pimc_save_rho_1d(C.byref(s), fn, float(acount), int(mode), p3), "pimc_save_rho_1d")
+    if mode == 0:
+        _chk(L.pimc_save_rho_theta_chi(C.byref(s), fn, float(acount), int(mode), p3), "pimc_save_rho_theta_chi")
 
 
 def save_exchange_length(w, fname, acount, blocknumb, bstype, ploops, pindex, print_xyz_prl=0):

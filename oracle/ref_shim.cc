@@ -425,7 +425,10 @@ void ref_save_densities(const char *fname, double acount, int mode)
   if (IMPURITY && MCAtom[IMTYPE].molecule == 1) SaveDensities2D(fname, acount, mode);
   if (IMPURITY && MCAtom[IMTYPE].molecule == 2) {
     SaveDensities3D(fname, acount, mode);
-    if (mode == MC_BLOCK) SaveRho1D(fname, acount, mode);
+    if (mode == MC_BLOCK) {
+      SaveRho1D(fname, acount, mode);
+      SaveRhoThetaChi(fname, acount, mode);
+    }
   }
 }
 void ref_save_exchange_length(const char *fname, double acount, long blocknumb)
