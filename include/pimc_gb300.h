@@ -115,6 +115,12 @@ pimc_status pimc_rcf(pimc_handle *h, double *rcf);
 pimc_status pimc_densities_accumulate(pimc_handle *h);
 pimc_status pimc_densities_read(pimc_handle *h, double *gr1d, double *gr2d, double *gr3d);
 pimc_status pimc_densities_reset(pimc_handle *h);
+/* With a nonlinear rotor the same binning also counts the relative Euler
+ * angles (theta, phi, chi) of rotational slices it0 and it0 + skip, as
+ * GetRotE3D fills _relthe_sum, _relphi_sum, _relchi_sum (mc_estim.cc:1023-1057);
+ * pimc_rel_euler_read copies the[PIMC_BINST], phi[PIMC_BINSC], chi[PIMC_BINSC]
+ * (zeros without a nonlinear rotor); pimc_densities_reset clears them. */
+pimc_status pimc_rel_euler_read(pimc_handle *h, double *the, double *phi, double *chi);
 
 /* GetExchangeLength (mc_estim.cc:1997-2019): ploops[k] += 1 for every
  * exchange cycle of k+1 bosons in the current permutation; ploops has one
@@ -151,6 +157,8 @@ pimc_status pimc_area_estim3d(pimc_handle *h, int iframe, const double *mass, do
  *  pimc_save_densities_3d   SaveDensities3D (mc_estim.cc:1728-1800): .g3d
  *  pimc_save_rho_1d         SaveRho1D's .gri, .grt, .grc (mc_estim.cc:1445-1590)
  *  pimc_save_rho_theta_chi  SaveRhoThetaChi (mc_estim.cc:1930-1996): .gtc
+ *  pimc_save_rel_euler      the run-total files of SaveRho1D (mc_estim.cc:1590-1660):
+ *                           _sum.eulphi, _sum.eulchi, _sum.eulthe from pimc_rel_euler_read
  *  pimc_save_exchange_length  SaveExchangeLength (mc_estim.cc:2021-2085): .prl, appended
  *  pimc_save_area_estimators  SaveAreaEstimators (mc_estim.cc:2596-2641): .sup, appended;
  *                           sums[6] as pimc_area_estimators' out
@@ -171,6 +179,8 @@ pimc_status pimc_save_rho_1d(const pimc_system *sys, const char *fname, double a
                              const double *gr3d);
 pimc_status pimc_save_rho_theta_chi(const pimc_system *sys, const char *fname, double acount, int mode,
                                     const double *gr3d);
+pimc_status pimc_save_rel_euler(const pimc_system *sys, const char *fname, double acount, const double *the,
+                                const double *phi, const double *chi);
 pimc_status pimc_save_exchange_length(const pimc_system *sys, const char *fname, double acount, long blocknumb,
                                       int bstype, const double *ploops, const int *pindex, int print_xyz_prl);
 pimc_status pimc_save_area_estimators(const pimc_system *sys, const char *fname, double acount, long blocknumb,

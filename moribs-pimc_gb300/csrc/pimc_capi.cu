@@ -61,7 +61,7 @@ struct pimc_handle {
   unsigned *abort_word = nullptr;
   int nprog = 0;
   // pair-density histograms (allocated on first use)
-  DensHist dens{nullptr, nullptr, nullptr};
+  DensHist dens{nullptr, nullptr, nullptr, nullptr};
   int dens_on = 0;
   // worm algorithm (allocated by pimc_worm_init)
   DevWorm *worm = nullptr;
@@ -345,7 +345,7 @@ extern "C" pimc_status pimc_destroy(pimc_handle *h)
   DevState &st = h->ctx.st;
   void *bufs[] = {st.x, st.y, st.z, st.b4, st.cosvf, st.rp_cache, st.rl_cache, st.rp_ok, st.rl_ok,
                   st.ang, st.cosv, st.pindex, st.mctype, st.err, h->frames, h->cnt, h->pass, h->cursors, h->ms,
-                  h->qbuf, h->prog, h->abort_word, h->dens.g1, h->dens.g2, h->dens.g3, h->worm, h->rindex,
+                  h->qbuf, h->prog, h->abort_word, h->dens.g1, h->dens.g2, h->dens.g3, h->dens.rel, h->worm, h->rindex,
                   h->wcur, h->wscr};
   for (void *b : bufs)
     if (b) cudaFree(b);
@@ -935,6 +935,7 @@ extern "C" pimc_status pimc_estimators(pimc_handle *h, double *out)
 static const size_t kDens1 = (size_t)PIMC_MAX_TYPES * PIMC_BINSR;
 static const size_t kDens2 = kDens1 * PIMC_BINST;
 static const size_t kDens3 = kDens2 * PIMC_BINSC;
+static const size_t kRel = PIMC_BINST + 2 * PIMC_BINSC;
 
 static pimc_status dens_alloc(pimc_handle *h)
 {
@@ -946,6 +947,8 @@ static pimc_status dens_alloc(pimc_handle *h)
   if (h->ctx.s.nrotors > 0 && h->ctx.s.molecule[h->ctx.s.imtype] == PIMC_NONLINEAR) {
     CK(cudaMalloc(&h->dens.g3, kDens3 * sizeof(unsigned long long)));
     CK(cudaMemsetAsync(h->dens.g3, 0, kDens3 * sizeof(unsigned long long), h->stream));
+    CK(cudaMalloc(&h->dens.rel, kRel * sizeof(unsigned long long)));
+    CK(cudaMemsetAsync(h->dens.rel, 0, kRel * sizeof(unsigned long long), h->stream));
   }
   return PIMC_OK;
 }
@@ -990,7 +993,23 @@ extern "C" pimc_status pimc_densities_reset(pimc_handle *h)
   size_t n[3] = {kDens1, kDens2, kDens3};
   for (int k = 0; k < 3; k++)
     if (src[k]) CK(cudaMemsetAsync(src[k], 0, n[k] * sizeof(unsigned long long), h->stream));
+  if (h->dens.rel) CK(cudaMemsetAsync(h->dens.rel, 0, kRel * sizeof(unsigned long long), h->stream));
   return PIMC_OK;
+}
+
+extern "C" pimc_status pimc_rel_euler_read(pimc_handle *h, double *the, double *phi, double *chi)
+{
+  if (!h || !the || !phi || !chi) return PIMC_ERR_BAD_ARG;
+  CK(cudaSetDevice(h->device));
+  std::vector<unsigned long long> tmp(kRel, 0ull);
+  if (h->dens.rel) {
+    CK(cudaMemcpyAsync(tmp.data(), h->dens.rel, kRel * sizeof(unsigned long long), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+  }
+  for (int i = 0; i < PIMC_BINST; i++) the[i] = (double)tmp[i];
+  for (int i = 0; i < PIMC_BINSC; i++) phi[i] = (double)tmp[PIMC_BINST + i];
+  for (int i = 0; i < PIMC_BINSC; i++) chi[i] = (double)tmp[PIMC_BINST + PIMC_BINSC + i];
+  return check_err(h);
 }
 
 // BSTYPE: the last Bose type (mc_setup.cc:409-415), or -1

@@ -138,6 +138,10 @@ struct Ctx {
 #endif
 struct DensHist {
   unsigned long long *g1, *g2, *g3;
+  // relative Euler angles of adjacent rotational slices of a nonlinear rotor
+  // (GetRotE3D's _relthe_sum[BINST], _relphi_sum[BINSC], _relchi_sum[BINSC],
+  // mc_estim.cc:1044-1057), in that order; null otherwise
+  unsigned long long *rel;
 };
 
 // ------------------------------------------------------------------ frames

@@ -340,6 +340,36 @@ extern "C" pimc_status pimc_save_rho_theta_chi(const pimc_system *s, const char 
   return PIMC_OK;
 }
 
+// The relative-Euler-angle files SaveRho1D adds at the end of the run
+// (mc_estim.cc:1590-1660): _sum.eulphi and _sum.eulchi (chi-width bins),
+// _sum.eulthe (theta bins), each line the bin centre in degrees and the count
+// over Q acount times the bin width in degrees.
+extern "C" pimc_status pimc_save_rel_euler(const pimc_system *s, const char *fname, double acount, const double *the,
+                                           const double *phi, const double *chi)
+{
+  if (!valid(s, fname) || !the || !phi || !chi || s->nrotslices <= 0) return PIMC_ERR_BAD_ARG;
+  const Bins b;
+  const double norm5 = (double)s->nrotslices * acount * b.dch * (180. / M_PI);
+  const double norm6 = (double)s->nrotslices * acount * b.dth * (180.0 / M_PI);
+  const char *ext[2] = {".eulphi", ".eulchi"};
+  const double *h[2] = {phi, chi};
+  for (int k = 0; k < 2; k++) {
+    Out o(std::string(fname) + "_sum" + ext[k], false);
+    if (!o.f) return PIMC_ERR_BAD_ARG;
+    for (int i = 0; i < PIMC_BINSC; i++) {
+      o.num(b.chi(i) * 180.0 / M_PI);
+      fprintf(o.f, "%*.*e\n", kWidth, 6, h[k][i] / norm5);
+    }
+  }
+  Out o(std::string(fname) + "_sum.eulthe", false);
+  if (!o.f) return PIMC_ERR_BAD_ARG;
+  for (int i = 0; i < PIMC_BINST; i++) {
+    o.num(b.theta(i) * 180.0 / M_PI);
+    fprintf(o.f, "%*.*e\n", kWidth, 6, the[i] / norm6);
+  }
+  return PIMC_OK;
+}
+
 // SaveExchangeLength (mc_estim.cc:2021-2085): one appended .prl line per
 // block -- the block number, the ground-state-loop and excited-loop weights
 // and their sum, the normalised count of every cycle length, PIndex and the

@@ -669,6 +669,25 @@ __global__ void k_est_dens(Ctx c, Frame *frames, DensHist hs)
   }
 }
 
+// GetRotE3D's binning of the relative Euler angles of slices it0 and
+// it0 + skip (mc_estim.cc:1023-1057): floor(angle / bin width), each in-range
+// bin counted skip times (RNskip: 1, or RNratio for rattle-and-shake)
+__global__ void k_est_releuler(Ctx c, const Frame *frames, unsigned long long *rel)
+{
+  const int Q = c.s.Q, skip = (c.s.rot_den_type == 0) ? 1 : c.s.rn_ratio;
+  const double dth = PIMC_PI / (double)(PIMC_BINST - 1), dch = 2.0 * PIMC_PI / (double)(PIMC_BINSC - 1);
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < c.s.nrotors * Q; k += gridDim.x * blockDim.x) {
+    const int r = k / Q, it0 = k % Q;
+    if (it0 % skip) continue;
+    double e[3];
+    deleul(frames[r * Q + it0].m, frames[r * Q + (it0 + skip) % Q].m, e);
+    const int bt = (int)floor(e[1] / dth), bp = (int)floor(e[0] / dch), bc = (int)floor(e[2] / dch);
+    if (bt < PIMC_BINST && bt >= 0) atomicAdd(rel + bt, (unsigned long long)skip);
+    if (bp < PIMC_BINSC && bp >= 0) atomicAdd(rel + PIMC_BINST + bp, (unsigned long long)skip);
+    if (bc < PIMC_BINSC && bc >= 0) atomicAdd(rel + PIMC_BINST + PIMC_BINSC + bc, (unsigned long long)skip);
+  }
+}
+
 // ------------------------------------------------------ area estimators
 // GetAreaEstimators (mc_estim.cc:2087-2250, mode 0) and GetAreaEstim3D
 // (mc_estim.cc:2252-2594; mode 1 space-fixed frame about the mass-weighted
@@ -1096,6 +1115,10 @@ int launch_est_dens(const Ctx &c, Frame *f, DensHist hs, cudaStream_t s)
   if (work <= 0) return 0;
   long nb = (work + 255) / 256;
   k_est_dens<<<(int)(nb < 4096 ? nb : 4096), 256, 0, s>>>(c, f, hs);
+  if (hs.rel) {
+    k_est_releuler<<<(c.s.nrotors * c.s.Q + 127) / 128, 128, 0, s>>>(c, f, hs.rel);
+    return 2;
+  }
   return 1;
 }
 

@@ -78,6 +78,8 @@ def load(path=LIBPATH):
     sp, cc = C.POINTER(PimcSystem), C.c_char_p
     L.pimc_save_densities_1d.argtypes = [sp, cc, C.c_double, _dp, _dp]
     L.pimc_save_gra_sum.argtypes = [sp, cc, C.c_double, _dp]
+    L.pimc_save_rel_euler.argtypes = [sp, cc, C.c_double, _dp, _dp, _dp]
+    L.pimc_rel_euler_read.argtypes = [vp, _dp, _dp, _dp]
     for n in ("pimc_save_densities_2d", "pimc_save_densities_3d", "pimc_save_rho_1d", "pimc_save_rho_theta_chi"):
         getattr(L, n).argtypes = [sp, cc, C.c_double, C.c_int, _dp]
     L.pimc_save_exchange_length.argtypes = [sp, cc, C.c_double, C.c_long, C.c_int, _dp, _ip, C.c_int]
@@ -316,6 +318,12 @@ class Sampler:
         g3 = np.zeros((PIMC_MAX_TYPES, BINSR * BINST * BINSC))
         _chk(self.L.pimc_densities_read(self.h, dptr(g1), dptr(g2), dptr(g3)), "pimc_densities_read")
         return g1, g2, g3
+
+    def rel_euler_read(self):
+        """GetRotE3D's relative-Euler-angle histograms (theta, phi, chi)."""
+        t, p, c = np.zeros(BINST), np.zeros(BINSC), np.zeros(BINSC)
+        _chk(self.L.pimc_rel_euler_read(self.h, dptr(t), dptr(p), dptr(c)), "pimc_rel_euler_read")
+        return t, p, c
 
     def densities_reset(self):
         _chk(self.L.pimc_densities_reset(self.h), "pimc_densities_reset")
@@ -656,4 +664,14 @@ def save_sum_energy(w, fname, acount, numb, sums, append=False):
     sm = np.ascontiguousarray(sums, dtype=np.float64)
     _chk(L.pimc_save_sum_energy(C.byref(s), fname.encode(), float(acount), float(numb), dptr(sm), int(bool(append))),
          "pimc_save_sum_energy")
+
+
+
+
+def save_rel_euler(w, fname, acount, the, phi, chi):
+    L = load()
+    s = make_system(w)
+    a = [np.ascontiguousarray(v, dtype=np.float64) for v in (the, phi, chi)]
+    _chk(L.pimc_save_rel_euler(C.byref(s), fname.encode(), float(acount), dptr(a[0]), dptr(a[1]), dptr(a[2])),
+         "pimc_save_rel_euler")
 

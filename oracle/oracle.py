@@ -433,6 +433,7 @@ class Reference:
         L.ref_rcf_save.argtypes = [C.c_char_p, C.c_double, C.c_int, _dp]
         L.ref_energy_block.argtypes = [C.c_char_p, C.c_char_p, C.c_long, _dp]
         L.ref_sum_energy.argtypes = [C.c_char_p, C.c_double, _dp]
+        L.ref_rel_euler.argtypes = [C.c_char_p, C.c_double, _dp, _dp, _dp]
         L.ref_tau.restype = C.c_double
         L.ref_lambda.restype = C.c_double
         L.ref_lambda.argtypes = [C.c_int]
@@ -585,6 +586,13 @@ class Reference:
         if self.L.ref_sum_energy(str(workdir).encode(), float(numb), dptr(out)) != 0:
             raise RuntimeError("ref_sum_energy failed")
         return out
+
+    def rel_euler(self, fname, acount):
+        """GetRotE3D's relative-angle histograms of the path and SaveRho1D's
+        run-total files (fname_sum.*)."""
+        t, p, c = np.zeros(BINST), np.zeros(BINSC), np.zeros(BINSC)
+        self.L.ref_rel_euler(fname.encode(), float(acount), dptr(t), dptr(p), dptr(c))
+        return t, p, c
 
     def rcf_save(self, fname, acount, mode):
         """GetRCF on cleared accumulators, then SaveRCF; returns the ten rows written."""

@@ -135,6 +135,7 @@ extern double _areas[2], _area2[2], _inert[2];
 extern double _areas3DMFF[6], _inert3DMFF[9], _areas3DSFF[6], _inert3DSFF[9];
 extern int NUMB_DENS1D, NUMB_DENS2D, NUMB_DENS3D;
 extern double **_rcf, **_rcf_sum;
+extern double *_relthe_sum, *_relphi_sum, *_relchi_sum;
 // block averages of mc_main.cc (file scope there)
 extern double avergCount, _bkin, _bpot, _brot, _brotsq, _bCv, _bCv_trans, _bCv_rot;
 void MCResetBlockAverage(void);
@@ -475,6 +476,19 @@ int ref_sum_energy(const char *workdir, double numb, double *totals)
   SaveSumEnergy(totalCount, numb);
   DoneTotalAverage();
   return chdir(cwd) != 0;
+}
+
+// the densities and GetRotE3D's relative-angle histograms of the path from
+// cleared accumulators, then SaveRho1D's run-total files; the histograms out
+void ref_rel_euler(const char *fname, double acount, double *the, double *phi, double *chi)
+{
+  densities_reset(MC_TOTAL);
+  densities_reset(MC_BLOCK);
+  GetPotEnergy_Densities();
+  GetRotE3D();
+  for (int i = 0; i < MC_BINST_REF; i++) the[i] = _relthe_sum[i];
+  for (int i = 0; i < MC_BINSC_REF; i++) { phi[i] = _relphi_sum[i]; chi[i] = _relchi_sum[i]; }
+  SaveRho1D(fname, acount, MC_TOTAL);
 }
 
 // GetRCF once into cleared accumulators, then SaveRCF; rcf[10][Q] = the

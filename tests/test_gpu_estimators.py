@@ -96,3 +96,36 @@ def test_estimators_after_production_passes(which):
         got, ref = s.area_estim3d(fr, masses), o.area_estim3d(fr, masses)
         check_area(got, ref[3:], s_area, s_inert, True)
     s.close()
+
+
+def test_relative_euler_histograms_match_oracle_angles():
+    """GetRotE3D's binning of the relative Euler angles of adjacent
+    rotational slices (mc_estim.cc:1023-1057) on a sampled asymmetric-top
+    path: the device histograms equal the binning of the oracle's rotden
+    relative angles of the same slices."""
+    w = W.config1(seed=12, nslices=32, nrotslices=8, n_h2=6, grid3d=(30, 37, 19), griddens=(19, 37, 37))
+    s = G.Sampler(w)
+    s.set_option(G.OPT_DENSITIES, 1)
+    s.run_passes(3, seed=5)
+    c, a, co, p = s.get_state()
+    s.densities_reset()
+    s.densities_accumulate()
+    t, ph, ch = s.rel_euler_read()
+    s.close()
+    o = O.Oracle(w)
+    o.set_state(c, a, p)
+    first = sum(tp["numb"] for tp in w.types if tp["molecule"] == 0)
+    off, Q = first * w.nslices, w.nrotslices
+    dth, dch = np.pi / (G.BINST - 1), 2.0 * np.pi / (G.BINSC - 1)
+    rt, rp, rc = np.zeros(G.BINST), np.zeros(G.BINSC), np.zeros(G.BINSC)
+    for it0 in range(Q):
+        e = [(a[0, off + i], np.arccos(a[1, off + i]), a[2, off + i]) for i in (it0, (it0 + 1) % Q)]
+        _, rel, _, _, _ = o.rotden(e[0], e[1])
+        for hist, v, d in ((rt, rel[1], dth), (rp, rel[0], dch), (rc, rel[2], dch)):
+            b = int(np.floor(v / d))
+            if 0 <= b < len(hist):
+                hist[b] += 1
+    np.testing.assert_array_equal(t, rt)
+    np.testing.assert_array_equal(ph, rp)
+    np.testing.assert_array_equal(ch, rc)
+    assert t.sum() == Q

@@ -134,3 +134,18 @@ def test_energy_block(tmp_path, case):
     G.save_sum_energy(w, str(b / prefix[0][:-len("_sum.eng")]), 1.0, 3.0, sums)
     _same(a / prefix[0], b / prefix[0])
 
+
+def test_relative_euler_files(tmp_path):
+    """SaveRho1D's run-total files: the relative Euler angles of adjacent
+    rotational slices binned as GetRotE3D bins them."""
+    w = W.config1(**C1S)
+    r = O.Reference(w)
+    a, b = tmp_path / "ref", tmp_path / "gb"
+    a.mkdir()
+    b.mkdir()
+    t, p, c = r.rel_euler(str(a / "run"), 2.0)
+    assert t.sum() == w.nrotslices and p.sum() == w.nrotslices and c.sum() == w.nrotslices
+    G.save_rel_euler(w, str(b / "run"), 2.0, t, p, c)
+    for f in ("run_sum.eulphi", "run_sum.eulchi", "run_sum.eulthe"):
+        _same(a / f, b / f)
+
