@@ -83,7 +83,9 @@ pimc_status pimc_pot_energy(pimc_handle *h, int n, const int *atom0, const int *
  * call makes no cudaMalloc/cudaFree.  n <= 4096 (PIMC_ERR_SIZE otherwise).
  * All calls on a device share the array: calls that overlap on the GPU race
  * and must be ordered by the caller.  The first call on each device looks up
- * the array's address; make it before any stream capture. */
+ * the array's address; make it before any stream capture.  The address is
+ * kept for the life of the process: after a cudaDeviceReset the library's
+ * module may load elsewhere, so this entry point must not be used after one. */
 pimc_status pimc_pot_energy_noalloc(pimc_handle *h, int n, const int *atom0, const int *it, const double *xyz,
                                     double *out);
 
@@ -254,7 +256,11 @@ pimc_status pimc_mlp_get_params(pimc_mlp *m, float *params);
  * kernels), in parameter-vector order; *loss = that mean (optional). */
 pimc_status pimc_mlp_gradients(pimc_mlp *m, int n, const float *x, const float *e, float *grad, double *loss);
 /* epochs of Adam over n samples in a seeded order, minibatches of `batch`
- * (a multiple of 128); loss_out[epoch] = the epoch's mean minibatch loss. */
+ * (a multiple of 128); loss_out[epoch] = the epoch's mean minibatch loss.
+ * PIMC_ERR_TIMEOUT when a training kernel gave up a wait: a step may then
+ * have applied an incomplete gradient, so the surrogate refuses every later
+ * forward, training and delayed-acceptance call (PIMC_ERR_TIMEOUT) until
+ * pimc_mlp_set_weights loads weights again. */
 pimc_status pimc_mlp_train(pimc_mlp *m, int n, const float *x, const float *e, int epochs, int batch, float lr,
                            uint64_t seed, double *loss_out);
 
@@ -326,6 +332,13 @@ pimc_status pimc_set_precision(pimc_handle *h, int mixed);
  * block of numb phases and persistent rotational sweeps; 0: one launch per
  * phase.  Both give identical paths for the same seed. */
 #define PIMC_OPT_FUSED 1
+/* PIMC_OPT_WAIT_NS: how long (ns of %globaltimer, default 2e9) a persistent
+ * rotational sweep's slice waits for its neighbours before it gives up, sets
+ * the abort word and ends the sweep; the next synchronising call reports
+ * PIMC_ERR_TIMEOUT, clears the abort word, and the handle is usable again
+ * (the moves of the aborted sweep that had committed stay in the path).
+ * Values 0 .. 6e10. */
+#define PIMC_OPT_WAIT_NS 3
 pimc_status pimc_set_option(pimc_handle *h, int option, long long value);
 /* scheduled bead-moves per pass: per type N*P*(2^L-1) + N*P, plus P*Q per rotor */
 double      pimc_bead_moves_per_pass(const pimc_handle *h);

@@ -156,10 +156,40 @@ static pimc_status check_err(pimc_handle *h)
     CK(cudaMemcpy(h->ctx.st.err, &z, sizeof(unsigned), cudaMemcpyHostToDevice));
     if (e & DERR_GRID_RANGE) return PIMC_ERR_GRID_RANGE;
     if (e & DERR_NEG_DENSITY) return PIMC_ERR_NEG_DENSITY;
-    if (e & DERR_TIMEOUT) return PIMC_ERR_TIMEOUT;
+    if (e & DERR_TIMEOUT) {
+      // the aborted sweep has ended; the next launches run normally, from
+      // freshly evaluated rotor caches
+      CK(cudaMemset(h->abort_word, 0, sizeof(unsigned)));
+      launch_invalidate_caches(h->ctx, h->stream);
+      h->launches++;
+      CK(cudaStreamSynchronize(h->stream));
+      return PIMC_ERR_TIMEOUT;
+    }
     if (e & DERR_STREAM) return PIMC_ERR_BAD_ARG;
+    if (e & DERR_PERM) return PIMC_ERR_BAD_ARG;
   }
   return PIMC_OK;
+}
+
+// PIndex as the reference keeps it (mc_setup.cc:337, mc_qworm.cc:538-541):
+// a bijection of [0, na) whose first numb entries, for every boson type,
+// map [0, numb) onto itself (the cycles the exchange moves and estimators
+// walk, mc_piqmc.cc:129-138, mc_estim.cc:2008-2013).  Anything else would
+// make those walks run off their cycle.
+static bool perm_ok(const DevSys &d, const int *p)
+{
+  std::vector<char> seen(d.na, 0);
+  for (int a = 0; a < d.na; a++) {
+    int v = p[a];
+    if (v < 0 || v >= d.na || seen[v]) return false;
+    seen[v] = 1;
+  }
+  for (int t = 0; t < d.ntypes; t++) {
+    if (d.stat[t] != PIMC_BOSE) continue;
+    for (int a = 0; a < d.numb[t]; a++)
+      if (p[a] >= d.numb[t]) return false;
+  }
+  return true;
 }
 
 // cubic spline second derivatives with end slopes from the first and last
@@ -265,6 +295,7 @@ static pimc_status build_devsys(const pimc_system &s, DevSys &d)
   d.rot_eoff = s.rot_eoff;
   for (int k = 0; k < 3; k++) { d.abc[k] = s.rot_abc[k]; d.box[k] = s.box[k]; }
   d.minimage = s.minimage;
+  d.wait_ns = 2000000000ull;
   return PIMC_OK;
 }
 
@@ -570,6 +601,7 @@ extern "C" pimc_status pimc_set_state(pimc_handle *h, const double *coords, cons
   if (!h) return PIMC_ERR_BAD_ARG;
   CK(cudaSetDevice(h->device));
   const DevSys &d = h->ctx.s;
+  if (pindex && !perm_ok(d, pindex)) return PIMC_ERR_BAD_ARG;
   size_t nbr = (size_t)d.na * d.P;      // reference layout length per row
   if (coords) {
     // [3][na*P] -> slice-major x/y/z[t*nap + a]
@@ -611,8 +643,6 @@ extern "C" pimc_status pimc_set_state(pimc_handle *h, const double *coords, cons
     CK(cudaMemsetAsync(h->abort_word, 0, sizeof(unsigned), h->stream));   // a new path clears an aborted sweep
   }
   if (pindex) {
-    for (int a = 0; a < d.na; a++)
-      if (pindex[a] < 0 || pindex[a] >= d.na) return PIMC_ERR_BAD_ARG;
     CK(cudaMemcpy(h->ctx.st.pindex, pindex, d.na * sizeof(int), cudaMemcpyHostToDevice));
     h->pindex_host.assign(pindex, pindex + d.na);
     if (h->rindex) {
@@ -1298,6 +1328,7 @@ extern "C" pimc_status pimc_da_sweeps(pimc_handle *h, pimc_mlp *m, int nsweeps, 
   if (e) return e;
   if ((e = da_check(h))) return e;
   if (nsweeps < 0 || (use_surrogate && !m) || nsweeps > (1 << 18)) return PIMC_ERR_BAD_ARG;
+  if (use_surrogate && mlp_poisoned(m)) return PIMC_ERR_TIMEOUT;    // reload its weights first
   const DevSys &d = h->ctx.s;
   const int nm = d.Q / 2, rows = nm * 2 * d.R;
   size_t bytes = (size_t)rows * 7 * sizeof(float) + (size_t)nm * sizeof(DaMove) + 4096;
@@ -1640,6 +1671,17 @@ extern "C" pimc_status pimc_set_option(pimc_handle *h, int option, long long val
     h->dens_on = (int)value;
     return PIMC_OK;
   }
+  if (option == PIMC_OPT_WAIT_NS) {
+    if (value < 0 || value > 60000000000ll) return PIMC_ERR_BAD_ARG;
+    CK(cudaSetDevice(h->device));
+    CK(cudaStreamSynchronize(h->stream));
+    h->ctx.s.wait_ns = (unsigned long long)value;
+    // the captured graphs hold the system by value
+    if (h->pass_exec) { cudaGraphExecDestroy(h->pass_exec); h->pass_exec = nullptr; }
+    if (h->worm_exec) { cudaGraphExecDestroy(h->worm_exec); h->worm_exec = nullptr; }
+    if (h->da_exec) { cudaGraphExecDestroy(h->da_exec); h->da_exec = nullptr; }
+    return PIMC_OK;
+  }
   return PIMC_ERR_BAD_ARG;
 }
 
@@ -1969,6 +2011,7 @@ extern "C" pimc_status pimc_batch_set_state(pimc_batch *b, int r, const double *
   CK(cudaSetDevice(h->device));
   const Ctx &c = b->reps[r].c;
   const DevSys &d = c.s;
+  if (pindex && !perm_ok(d, pindex)) return PIMC_ERR_BAD_ARG;
   size_t nbr = (size_t)d.na * d.P;
   std::vector<double> buf((size_t)d.P * d.nap, 0.0);
   double *dst[3] = {c.st.x, c.st.y, c.st.z};
@@ -1994,8 +2037,6 @@ extern "C" pimc_status pimc_batch_set_state(pimc_batch *b, int r, const double *
     CK(cudaMemcpy(c.st.cosv, cs.data(), 3 * n * sizeof(double), cudaMemcpyHostToDevice));
   }
   if (pindex) {
-    for (int a = 0; a < d.na; a++)
-      if (pindex[a] < 0 || pindex[a] >= d.na) return PIMC_ERR_BAD_ARG;
     CK(cudaMemcpy(c.st.pindex, pindex, d.na * sizeof(int), cudaMemcpyHostToDevice));
   }
   launch_derive_state(c, b->reps[r].frames, h->stream);       // float copies, frames, caches stale
@@ -2015,6 +2056,7 @@ extern "C" pimc_status pimc_batch_get_state(pimc_batch *b, int r, double *coords
   CK(cudaStreamSynchronize(h->stream));
   const Ctx &c = b->reps[r].c;
   const DevSys &d = c.s;
+  if (pindex && !perm_ok(d, pindex)) return PIMC_ERR_BAD_ARG;
   size_t nbr = (size_t)d.na * d.P;
   if (coords) {
     std::vector<double> buf((size_t)d.P * d.nap);

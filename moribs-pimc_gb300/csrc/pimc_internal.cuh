@@ -18,7 +18,7 @@
 #define PIMC_MAX_ROTORS 16            /* NumbRotLim (mc_setup.cc:63) */
 
 // error bits raised on the device and read back by the host
-enum { DERR_GRID_RANGE = 1, DERR_NEG_DENSITY = 2, DERR_STREAM = 4, DERR_TIMEOUT = 8 };
+enum { DERR_GRID_RANGE = 1, DERR_NEG_DENSITY = 2, DERR_STREAM = 4, DERR_TIMEOUT = 8, DERR_PERM = 16 };
 
 struct DevTables {
   // 1D spline, SPot1D (mc_poten.cc:379-438,624-639); float copies for the FP32 path
@@ -86,6 +86,7 @@ struct DevSys {
   int minimage;
   double box[3];
   int mixed;                   // 1: FP32 table interpolation with FP64 sums
+  unsigned long long wait_ns;  // limit of a persistent sweep's wait for its neighbours
 };
 
 // path state on the device

@@ -155,7 +155,7 @@ struct RotSliceHooks {
           unsigned long long v = ld_acquire_u64(w);
           if ((v >> 24) == id && (long long)(v & 0xFFFFFFull) >= h) break;
           if (*(volatile unsigned *)abort_word) { ok = 0; break; }
-          if (global_ns() - t0 > 2000000000ull) {
+          if (global_ns() - t0 > sys->wait_ns) {
             atomicExch(abort_word, 1u);
             ok = 0;
             break;
@@ -248,7 +248,7 @@ __global__ void __launch_bounds__(PIMC_ROT_THREADS) k_rot(Ctx c, Frame *frames, 
 // here again.  Every move therefore sees exactly the state it sees in the
 // launch-per-half-sweep schedule, with the same uniforms, and the results
 // are identical.  Progress words hold (launch id << 24) | half-sweeps done;
-// the wait gives up after two seconds, sets the abort word and the timeout
+// the wait gives up after wait_ns (two seconds unless set), sets the abort word and the timeout
 // error bit, and every CTA then leaves.
 template <bool MIX>
 __global__ void __launch_bounds__(PIMC_ROT_THREADS) k_rot_sweeps(Ctx c, Frame *frames, int nhalf, unsigned phase0,
@@ -293,7 +293,7 @@ __global__ void __launch_bounds__(PIMC_ROT_THREADS) k_rot_sweeps(Ctx c, Frame *f
             st = 1;
             break;
           }
-          if (global_ns() - t0 > 2000000000ull) {
+          if (global_ns() - t0 > c.s.wait_ns) {
             atomicExch(abort_word, 1u);
             atomicOr(c.st.err, (unsigned)DERR_TIMEOUT);
             st = 1;

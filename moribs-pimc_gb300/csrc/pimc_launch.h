@@ -69,6 +69,7 @@ struct pimc_mlp;
 // the surrogate on device-resident rows, on stream s (pimc_mlp.cu)
 int mlp_forward_device(pimc_mlp *m, const float *x, int n, float *y, cudaStream_t s);
 bool mlp_take_error(pimc_mlp *m);
+bool mlp_poisoned(const pimc_mlp *m);
 unsigned long long mlp_uid(const pimc_mlp *m);   // 0 for none; unique per created surrogate
 
 // ------------------------------------------------------------ replica batches

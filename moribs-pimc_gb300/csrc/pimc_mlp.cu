@@ -289,11 +289,15 @@ __global__ void __launch_bounds__(kFwdThreads) k_mlp_forward(MlpParams p, const 
   ok = __syncthreads_and(mbar_wait(bar_w, 0)) && ok;
   unsigned ph = 0;
   float out = 0.0f;
+  bool w3_sent = false;
+  int nmma = 0;
   for (int layer = 0; layer < 2 && ok; layer++) {
     ok = __syncthreads_and(gemm_128x256(tmem, sA, sB, bar_m, ph));   // every thread saw the MMAs complete
     ph ^= 1u;
+    nmma++;
     if (!ok) break;
     if (layer == 0 && tid == 0) bulk_load(sB, p.w3c, kB, bar_w);
+    if (layer == 0) w3_sent = true;
     const float *bias = layer == 0 ? sb2 : sb3;
     for (int c = c0; c < c0 + kH / 2; c += 16) {
       float v[16], bb[16];
@@ -324,7 +328,17 @@ __global__ void __launch_bounds__(kFwdThreads) k_mlp_forward(MlpParams p, const 
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     if (layer == 0) ok = __syncthreads_and(mbar_wait(bar_w, 1));
   }
-  if (!ok && tid == 0) atomicOr(err, 1u);
+  if (!ok) {
+    // a wait gave up (ok is uniform over the CTA): let the copies and the
+    // MMAs that may still be in flight land, each with a bounded wait,
+    // before this CTA's shared memory and TMEM are released
+    // (only the last phase issued on each barrier: phases complete in order)
+    if (tid == 0) atomicOr(err, 1u);
+    mbar_wait(bar_x, 0);
+    mbar_wait(bar_w, w3_sent ? 1u : 0u);
+    if (nmma > 0) mbar_wait(bar_m, (unsigned)(nmma - 1) & 1u);
+    __syncthreads();
+  }
   outp[tid] = out;
   __syncthreads();
   if (half == 0 && row < n) y[row] = (outp[r] + outp[r + kRows]) + *p.b4;
@@ -454,12 +468,24 @@ __global__ void __launch_bounds__(kRows) k_mlp_train(MlpTrainParams p, unsigned 
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tslot, tlane = tmem + ((uint32_t)(warp * 32) << 16);
-  unsigned pw = 0, pm = 0;
+  unsigned pw = 0, pm = 0, w_last = 0, m_last = 0;
+  int nload = 0, nmma = 0;
+  // ok stays uniform over the CTA; after a wait gives up nothing more is
+  // issued, so the last copy / MMA issued is the only one still in flight
   bool ok = __syncthreads_and(mbar_wait(bar_x, 0));
   auto load_b = [&](const char *src, uint32_t bytes, char *dst) {
+    if (!ok) return;
     if (tid == 0) bulk_load(dst, src, bytes, bar_w);
-    ok = ok && mbar_wait(bar_w, pw);
+    ok = __syncthreads_and(mbar_wait(bar_w, pw));
+    w_last = pw;
+    nload++;
     pw ^= 1u;
+  };
+  auto mma_done = [&](bool issued_ok) {
+    ok = __syncthreads_and(issued_ok);
+    m_last = pm;
+    nmma++;
+    pm ^= 1u;
   };
   auto sync_async = [&]() {
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -485,8 +511,7 @@ __global__ void __launch_bounds__(kRows) k_mlp_train(MlpTrainParams p, unsigned 
   sync_async();
   load_b(p.w.w2c, kB, sB);
   // ---- layer 2: z2 saved, h2 as A operand and h2^T
-  ok = ok && gemm_k(tmem, sA, sB, kH, bar_m, pm);
-  pm ^= 1u;
+  if (ok) mma_done(gemm_k(tmem, sA, sB, kH, bar_m, pm));
   __syncthreads();
   for (int c = 0; c < kH; c += 16) {
     float v[16];
@@ -505,8 +530,7 @@ __global__ void __launch_bounds__(kRows) k_mlp_train(MlpTrainParams p, unsigned 
   sync_async();
   load_b(p.w.w3c, kB, sB);
   // ---- layer 3 and the output
-  ok = ok && gemm_k(tmem, sA, sB, kH, bar_m, pm);
-  pm ^= 1u;
+  if (ok) mma_done(gemm_k(tmem, sA, sB, kH, bar_m, pm));
   __syncthreads();
   float y = *p.w.b4;
   for (int c = 0; c < kH; c += 16) {
@@ -561,15 +585,13 @@ __global__ void __launch_bounds__(kRows) k_mlp_train(MlpTrainParams p, unsigned 
   // ---- dW3 = h2^T dz3 (two M tiles) with h2^T and dz3^T staged in sB
   load_b(h2t, 65536, sB);
   load_b(dzt, 65536, sB + 65536);
-  ok = ok && gemm_dw(tmem, sB, sB + 65536, bar_m, pm);
-  pm ^= 1u;
+  if (ok) mma_done(gemm_dw(tmem, sB, sB + 65536, bar_m, pm));
   __syncthreads();
   store_dw(tlane, p.part + (size_t)cta * kNP + kOW3);
   sync_async();
   // ---- dh2 = dz3 W3^T; dz2 = dh2 silu'(z2) as A operand and dz2^T
   load_b(p.w3n, kB, sB);
-  ok = ok && gemm_k(tmem, sA, sB, kH, bar_m, pm);
-  pm ^= 1u;
+  if (ok) mma_done(gemm_k(tmem, sA, sB, kH, bar_m, pm));
   __syncthreads();
   for (int c = 0; c < kH; c += 16) {
     float v[16], dz[16];
@@ -592,15 +614,13 @@ __global__ void __launch_bounds__(kRows) k_mlp_train(MlpTrainParams p, unsigned 
   // ---- dW2 = h1^T dz2
   load_b(h1t, 65536, sB);
   load_b(dzt, 65536, sB + 65536);
-  ok = ok && gemm_dw(tmem, sB, sB + 65536, bar_m, pm);
-  pm ^= 1u;
+  if (ok) mma_done(gemm_dw(tmem, sB, sB + 65536, bar_m, pm));
   __syncthreads();
   store_dw(tlane, p.part + (size_t)cta * kNP + kOW2);
   sync_async();
   // ---- dh1 = dz2 W2^T; dz1 = dh1 silu'(z1); dW1 = x^T dz1, db1
   load_b(p.w2n, kB, sB);
-  ok = ok && gemm_k(tmem, sA, sB, kH, bar_m, pm);
-  pm ^= 1u;
+  if (ok) mma_done(gemm_k(tmem, sA, sB, kH, bar_m, pm));
   __syncthreads();
   for (int c = 0; c < kH; c += 16) {
     float v[16], dz[16];
@@ -627,7 +647,15 @@ __global__ void __launch_bounds__(kRows) k_mlp_train(MlpTrainParams p, unsigned 
       __syncthreads();
     }
   }
-  if (!ok && tid == 0) atomicOr(err, 1u);
+  if (!ok) {
+    // a wait gave up: the last bulk copy and the last MMA issued may still
+    // be in flight; wait for them (bounded) before the CTA's shared memory
+    // and TMEM are released
+    if (tid == 0) atomicOr(err, 1u);
+    if (nload > 0) mbar_wait(bar_w, w_last);
+    if (nmma > 0) mbar_wait(bar_m, m_last);
+    __syncthreads();
+  }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -687,6 +715,9 @@ struct pimc_mlp {
   int tcap = 0;
   long long step = 0;
   unsigned long long uid = 0;   // never reused within the process (keys captured graphs)
+  // a training step whose kernel gave up a wait has applied an incomplete
+  // gradient: the weights are unusable until pimc_mlp_set_weights loads new ones
+  bool poisoned = false;
 };
 
 static std::atomic<unsigned long long> g_mlp_uid{0};
@@ -762,6 +793,7 @@ extern "C" pimc_status pimc_mlp_set_weights(pimc_mlp *m, const float *w1, const 
 {
   if (!m || !w1 || !b1 || !w2 || !b2 || !w3 || !b3 || !w4) return PIMC_ERR_BAD_ARG;
   MCK(cudaSetDevice(m->device));
+  m->poisoned = false;
   std::vector<float> h(kNP);
   memcpy(&h[kOW1], w1, kIn * kH * sizeof(float));
   memcpy(&h[kOB1], b1, kH * sizeof(float));
@@ -870,6 +902,7 @@ extern "C" pimc_status pimc_mlp_gradients(pimc_mlp *m, int n, const float *x, co
                                           double *loss)
 {
   if (!m || n <= 0 || !x || !e || !grad) return PIMC_ERR_BAD_ARG;
+  if (m->poisoned) return PIMC_ERR_TIMEOUT;
   MCK(cudaSetDevice(m->device));
   pimc_status st = ensure_io(m, (size_t)n);
   if (st) return st;
@@ -887,6 +920,7 @@ extern "C" pimc_status pimc_mlp_train(pimc_mlp *m, int n, const float *x, const 
                                       float lr, uint64_t seed, double *loss_out)
 {
   if (!m || n <= 0 || !x || !e || epochs < 0 || batch < kRows || batch % kRows) return PIMC_ERR_BAD_ARG;
+  if (m->poisoned) return PIMC_ERR_TIMEOUT;
   MCK(cudaSetDevice(m->device));
   pimc_status st = ensure_io(m, (size_t)n);
   if (st) return st;
@@ -923,7 +957,9 @@ extern "C" pimc_status pimc_mlp_train(pimc_mlp *m, int n, const float *x, const 
     }
     if (loss_out) loss_out[ep] = nb ? lsum / nb : 0.0;
   }
-  return check_mlp_err(m);
+  st = check_mlp_err(m);
+  if (st) m->poisoned = true;
+  return st;
 }
 
 int mlp_forward_device(pimc_mlp *m, const float *x, int n, float *y, cudaStream_t s)
@@ -939,6 +975,7 @@ int mlp_forward_device(pimc_mlp *m, const float *x, int n, float *y, cudaStream_
 extern "C" pimc_status pimc_mlp_forward_resident(pimc_mlp *m, int n)
 {
   if (!m || n <= 0 || (size_t)n > m->cap) return PIMC_ERR_BAD_ARG;
+  if (m->poisoned) return PIMC_ERR_TIMEOUT;
   MCK(cudaSetDevice(m->device));
   mlp_forward_device(m, m->xbuf, n, m->ybuf, m->stream);
   MCK(cudaGetLastError());
@@ -950,6 +987,7 @@ extern "C" void *pimc_mlp_stream(const pimc_mlp *m) { return m ? (void *)m->stre
 // whether a surrogate launch gave up a wait since the last call (clears it)
 bool mlp_take_error(pimc_mlp *m)
 {
+  if (m->poisoned) return true;
   unsigned e = 0;
   if (cudaMemcpy(&e, m->err, sizeof(unsigned), cudaMemcpyDeviceToHost) != cudaSuccess) return true;
   if (e) cudaMemset(m->err, 0, sizeof(unsigned));
@@ -959,6 +997,7 @@ bool mlp_take_error(pimc_mlp *m)
 extern "C" pimc_status pimc_mlp_forward(pimc_mlp *m, int n, const float *x, float *y)
 {
   if (!m || n < 0 || (n && (!x || !y))) return PIMC_ERR_BAD_ARG;
+  if (m->poisoned) return PIMC_ERR_TIMEOUT;
   if (n == 0) return PIMC_OK;
   MCK(cudaSetDevice(m->device));
   pimc_status st = ensure_io(m, (size_t)n);
@@ -977,3 +1016,5 @@ extern "C" pimc_status pimc_mlp_forward(pimc_mlp *m, int n, const float *x, floa
   }
   return PIMC_OK;
 }
+
+bool mlp_poisoned(const pimc_mlp *m) { return m->poisoned; }

@@ -690,7 +690,7 @@ __global__ void __launch_bounds__(kMolThreads) k_mol_exchange(Ctx c, Frame *fram
   if (gate && gate->exists) return;          // the worm branch moves closed paths only (mc_main.cc:361)
   __shared__ double dd[3];
   __shared__ double wpart[2][kMolThreads / 32];
-  __shared__ int ncyc, accepted, stop;
+  __shared__ int ncyc, accepted, stop, perm_bad;
   const int numb = c.s.numb[type], g = c.s.first[type], P = c.s.P;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   for (int a = tid; a < numb; a += kMolThreads) flag[a] = 0;
@@ -698,10 +698,18 @@ __global__ void __launch_bounds__(kMolThreads) k_mol_exchange(Ctx c, Frame *fram
   for (int atom = 0; atom < numb; atom++) {
     if (tid == 0) {
       ncyc = 0;
+      perm_bad = 0;
       if (flag[atom] == 0) {
         cyc[ncyc++] = atom;
         int pa = c.st.pindex[atom];
+        // a cycle of a permutation of [0, numb) closes within numb steps;
+        // the host validates PIndex, and the walk is bounded all the same
         while (pa != atom) {
+          if (ncyc >= numb || pa < 0 || pa >= numb) {
+            atomicOr(c.st.err, (unsigned)DERR_PERM);
+            perm_bad = 1;
+            break;
+          }
           cyc[ncyc++] = pa;
           flag[pa] = 1;
           pa = c.st.pindex[pa];
@@ -716,6 +724,7 @@ __global__ void __launch_bounds__(kMolThreads) k_mol_exchange(Ctx c, Frame *fram
       stop = 0;
     }
     __syncthreads();
+    if (perm_bad) return;                    // uniform over the CTA: nothing moved
     const int n = ncyc;
     for (int ia = 0; ia < n; ia++) {
       const int ga = g + cyc[ia];
