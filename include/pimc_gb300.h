@@ -202,6 +202,18 @@ pimc_status pimc_save_energy(const pimc_system *sys, const char *fname, double a
 pimc_status pimc_save_sum_energy(const pimc_system *sys, const char *fname, double acount, double numb,
                                  const double *sums, int append);
 
+/* Standard error of the mean of a correlated series (host only, no handle):
+ * the reference writes one .eng row of block averages per block
+ * (SaveEnergy, mc_main.cc:764-795) and leaves their error analysis to the
+ * user; this is that analysis.  Blocking (Flyvbjerg and Petersen 1989) of
+ * the last 2^d of the n >= 16 values, the level chosen automatically
+ * (Jonsson 2018: the first level whose lag-one autocorrelations pass a
+ * chi-squared test at 99 %).  out[8] = mean, sample sd, naive SE, blocked
+ * SE, statistical inefficiency g = (blocked / naive SE)^2 (= 2 tau_int in
+ * samples), block size chosen, 1 if the test passed at some level (0: the
+ * top level is used), values used (2^d). */
+pimc_status pimc_blocking_se(const double *x, long n, double *out);
+
 /* ---- worm algorithm (mc_qworm.cc) ------------------------------------------ */
 
 /* MCWormInit (mc_qworm.cc:49-82) for the atom type `type` with the WORM

@@ -2056,7 +2056,6 @@ extern "C" pimc_status pimc_batch_get_state(pimc_batch *b, int r, double *coords
   CK(cudaStreamSynchronize(h->stream));
   const Ctx &c = b->reps[r].c;
   const DevSys &d = c.s;
-  if (pindex && !perm_ok(d, pindex)) return PIMC_ERR_BAD_ARG;
   size_t nbr = (size_t)d.na * d.P;
   if (coords) {
     std::vector<double> buf((size_t)d.P * d.nap);

@@ -2,8 +2,8 @@
 
     python moribs-pimc_gb300/pimc_build.py   -> moribs-pimc_gb300/libpimc_gb300.so
 
-Two translation units compiled in parallel, then linked with the CUDA
-runtime.  No cmake, no torch extension machinery."""
+The translation units of csrc/ (SOURCES) compiled in parallel, then linked
+with the CUDA runtime.  No cmake, no torch extension machinery."""
 import os
 import subprocess
 import sys
@@ -15,7 +15,8 @@ OUT = os.path.join(HERE, "libpimc_gb300.so")
 BUILD = os.path.join(HERE, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "--expt-relaxed-constexpr"]
-SOURCES = ["pimc_kernels.cu", "pimc_batch.cu", "pimc_capi.cu", "pimc_tables.cu", "pimc_worm.cu", "pimc_mlp.cu", "pimc_da.cu", "pimc_io.cu"]
+SOURCES = ["pimc_kernels.cu", "pimc_batch.cu", "pimc_capi.cu", "pimc_tables.cu", "pimc_worm.cu", "pimc_mlp.cu", "pimc_da.cu", "pimc_io.cu",
+           "pimc_stats.cu"]
 
 
 def nvcc():

@@ -88,6 +88,7 @@ def load(path=LIBPATH):
     L.pimc_save_rcf.argtypes = [sp, cc, C.c_double, C.c_int, _dp]
     L.pimc_energy_accumulate.argtypes = [sp, _dp, _dp]
     L.pimc_save_energy.argtypes = [sp, cc, C.c_double, C.c_long, _dp]
+    L.pimc_blocking_se.argtypes = [_dp, C.c_long, _dp]
     L.pimc_save_sum_energy.argtypes = [sp, cc, C.c_double, C.c_double, _dp, C.c_int]
     L.pimc_asymrho.argtypes = [C.c_int, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, _dp, C.c_int,
                                _dp, _dp, _dp, _dp]
@@ -478,6 +479,17 @@ class Batch:
     @staticmethod
     def replica_seed(seed, r):
         return int(load().pimc_batch_replica_seed(C.c_uint64(seed), int(r)))
+
+
+def blocking_se(x):
+    """pimc_blocking_se: dict of mean, sd, naive SE, blocked SE, the
+    statistical inefficiency g (2 tau_int, in samples), the block size chosen,
+    whether the level test passed, and the number of values used."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    out = np.zeros(8)
+    _chk(load().pimc_blocking_se(dptr(x), len(x), dptr(out)), "pimc_blocking_se")
+    return {"mean": out[0], "sd": out[1], "se_naive": out[2], "se": out[3], "g": out[4],
+            "block": int(out[5]), "converged": bool(out[6]), "n": int(out[7])}
 
 
 def linden(temperatures, nslices, bconst, npt, iodevn=-1, device=0):

@@ -449,6 +449,75 @@ def config3(seed=77, nslices=4096, nrotslices=2048, griddens=(61, 121, 121), sep
                     pindex=np.arange(2, dtype=np.int32))
 
 
+WATER_ABC = (27.9, 14.5, 9.3)
+
+
+def water_chain_tables(seed=4040, grid3d=(200, 60, 60)):
+    """Potentials shared by every replica of the water-chain family: the
+    pH2-pH2 Silvera-Goldman spline (1.5-30 A, 1024 points) and a water-pH2
+    V(r, theta, chi) from the same l <= 6 generator as the SO2-pH2 table, with
+    its own seed (the water-pH2 surface is not specified; this stands in)."""
+    g1, v1 = _table_1d(silvera_goldman, 1.5, 30.0, 1024)
+    nr, nth, nch = grid3d
+    rvmin, rvmax = 3.0, 30.0
+    rgrid = np.linspace(rvmin, rvmax, nr)
+    vt = rotor_atom_3d(rgrid, nth, nch, 90, seed + 7, eps0=45.0, sigma0=3.2)
+    return dict(grid1d=g1, pot1d=v1, rgrd=nr, thgrd=nth, chgrd=nch, rvmin=rvmin, rvmax=rvmax, vtable=vt,
+                chi_fold_deg=90)
+
+
+def water_chain(nrot, nh2, nslices, nrotslices, T, seed, tables, spacing=3.0, rtstep=0.3, griddens=None,
+                name="water-chain"):
+    """nrot rigid water-like tops (A, B, C = 27.9, 14.5, 9.3 cm^-1, caleng
+    between them) on a linear chain along x with `spacing` A between
+    neighbours, solvated by nh2 para-H2 bosons (possibly none), at T.  The
+    rotational propagator is the analytic rattle-and-shake one (ROTDENSI 1,
+    rotden.f:218-286) at the replica's own tau, so no density table is
+    needed; griddens=(nth, nph, nch) also tabulates it (the reference's
+    GetRotE3D reads the tabulated E^2 estimator even then)."""
+    types = [
+        dict(name="H2", numb=nh2, molecule=0, stat=1, levels=3, mcstep=0.20, lamb=lam(MASSES["H2"]), fpot="h2h2"),
+        dict(name="H2O", numb=nrot, molecule=2, stat=0, levels=3, mcstep=0.05, lamb=lam(MASSES["H2O"]),
+             fpot="h2oh2"),
+    ]
+    tb = dict(tables)
+    if griddens is not None:
+        rho, er, esq = rs_top_density(*griddens, WATER_ABC, 1.0 / (T * nrotslices))
+        tb.update(nth=griddens[0], nph=griddens[1], nch=griddens[2], rhoprp=rho, erotpr=er, erotsq=esq)
+    rng = np.random.default_rng(seed)
+    xs = (np.arange(nrot) - 0.5 * (nrot - 1)) * spacing
+    wpos = np.stack([xs, np.zeros(nrot), np.zeros(nrot)], axis=1)
+    radius = 0.5 * spacing * (nrot - 1) + 4.0 + 2.2 * (max(nh2, 1) / 8.0) ** (1.0 / 3.0)
+    hpos = _sphere_points(rng, nh2, radius, 2.9, avoid=[tuple(p) for p in wpos], avoid_sep=3.4) if nh2 else \
+        np.zeros((0, 3))
+    pos = np.vstack([hpos, wpos])
+    coords, angles = initial_path(nh2 + nrot, nslices, pos, rng, jitter=0.01)
+    # alternate orientations along the chain: even waters along z, odd ones
+    # tilted so that one H points at the next oxygen
+    for k in range(nrot):
+        a = (nh2 + k) * nslices
+        angles[1, a:a + nslices] = 1.0 if k % 2 == 0 else math.cos(math.radians(127.0))
+    return Workload(name, types, nslices, nrotslices, T, rtstep=rtstep, rotation=True, rot_den_type=1,
+                    rot_abc=WATER_ABC, tables=tb, coords=coords, angles=angles,
+                    pindex=np.arange(nh2 + nrot, dtype=np.int32), chi_fold_deg=90)
+
+
+def config4(n=512, seed=4040, p_choices=(512, 1024, 2048), n_rot=(1, 8), n_h2=(0, 32), t_range=(0.5, 2.0),
+            grid3d=(200, 60, 60)):
+    """n independent replicas of the water-chain family: per replica the
+    number of waters (n_rot), of pH2 (n_h2), the temperature (t_range) and
+    the translational slices (p_choices, rotational slices P/4: 512-2048 and
+    128-512) drawn from the seed; shared potential tables."""
+    rng = np.random.default_rng(seed)
+    tables = water_chain_tables(seed, grid3d)
+    nr = rng.integers(n_rot[0], n_rot[1] + 1, size=n)
+    nh = rng.integers(n_h2[0], n_h2[1] + 1, size=n)
+    ps = rng.choice(np.asarray(p_choices), size=n)
+    ts = rng.uniform(t_range[0], t_range[1], size=n)
+    return [water_chain(int(nr[r]), int(nh[r]), int(ps[r]), int(ps[r]) // 4, float(ts[r]), [seed, r], tables,
+                        name="config4-replica-%d" % r) for r in range(n)]
+
+
 # ------------------------------------------------ reference file formats
 
 def _fmt_temperature(T):
