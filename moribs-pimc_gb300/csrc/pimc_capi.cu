@@ -240,7 +240,10 @@ static pimc_status build_devsys(const pimc_system &s, DevSys &d)
   int na = 0, imtype = -1, nmol = 0;
   for (int t = 0; t < s.ntypes; t++) {
     const pimc_type &ty = s.type[t];
-    if (ty.numb < 1 || ty.levels < 1 || ty.levels > 6 || ty.lambda <= 0.0) return PIMC_ERR_BAD_ARG;
+    if (ty.numb < 0 || ty.levels < 1 || ty.levels > 6 || ty.lambda <= 0.0) return PIMC_ERR_BAD_ARG;
+    // an atom type may be empty beside a molecule type (a replica family whose
+    // solvent count is drawn from 0 up); it then has no moves and no partners
+    if (ty.numb == 0 && (ty.molecule != PIMC_ATOM || s.ntypes < 2)) return PIMC_ERR_BAD_ARG;
     if ((1 << ty.levels) >= s.nslices) return PIMC_ERR_BAD_ARG;       // mc_setup.cc:397-398
     if (ty.molecule < 0 || ty.molecule > 2) return PIMC_ERR_BAD_ARG;
     if (ty.molecule != PIMC_ATOM) { imtype = t; nmol++; }
@@ -943,14 +946,18 @@ extern "C" pimc_status pimc_estimators(pimc_handle *h, double *out)
           const double *v = r + 4 * ((size_t)rr * d.Q + q);
           s += v[0]; q2 += v[1]; t2 += v[2];
         }
-        erot += s / nq;
+        double er = s / nq;
         esq += q2 / (nq * nq);
         ets += t2 / (nq * nq);
+        // the rattle-and-shake energy of this rotor alone; the reference
+        // applies the conversion to the running sum of all rotors
+        // (mc_estim.cc:1084-1090), which is the same for one rotor
         if (d.rot_den_type == 1 && d.rn_ratio == 1) {
-          erot = erot / (4.0 * (d.rot_tau / PIMC_WNO2K) * (d.rot_tau / PIMC_WNO2K));
-          erot += 0.25 * (d.abc[0] + d.abc[1] + d.abc[2]) + 1.5 / (d.rot_tau / PIMC_WNO2K);
-          erot = erot / PIMC_WNO2K;
+          er = er / (4.0 * (d.rot_tau / PIMC_WNO2K) * (d.rot_tau / PIMC_WNO2K));
+          er += 0.25 * (d.abc[0] + d.abc[1] + d.abc[2]) + 1.5 / (d.rot_tau / PIMC_WNO2K);
+          er = er / PIMC_WNO2K;
         }
+        erot += er;
       }
     }
   }
@@ -2232,9 +2239,9 @@ extern "C" pimc_status pimc_batch_estimators(pimc_batch *b, double *out)
       } else {                                                                   // mc_estim.cc:1000-1092
         int skip = d.rot_den_type == 0 ? 1 : d.rn_ratio;
         erot = w[2] / (double)(d.Q / skip);
-        if (d.rot_den_type == 1 && d.rn_ratio == 1) {
+        if (d.rot_den_type == 1 && d.rn_ratio == 1) {          // per rotor, summed (see pimc_estimators)
           erot = erot / (4.0 * (d.rot_tau / PIMC_WNO2K) * (d.rot_tau / PIMC_WNO2K));
-          erot += 0.25 * (d.abc[0] + d.abc[1] + d.abc[2]) + 1.5 / (d.rot_tau / PIMC_WNO2K);
+          erot += (double)d.nrotors * (0.25 * (d.abc[0] + d.abc[1] + d.abc[2]) + 1.5 / (d.rot_tau / PIMC_WNO2K));
           erot = erot / PIMC_WNO2K;
         }
       }

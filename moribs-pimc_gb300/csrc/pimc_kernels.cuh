@@ -1188,7 +1188,9 @@ __device__ __forceinline__ void est_link(const Ctx &c, const Frame *frames, int 
       const Frame &f2 = frames[r * Q + (it0 + skip) % Q];
       double rho = 0.0, erot = 0.0, esq = 0.0;
       int bad = 0;
-      rho = rotden_rho(c.t, f1, f2, &bad, &erot, &esq);
+      // the tabulated E and E^2 (rotden.f:28-29); a rattle-and-shake run
+      // may have loaded no table, and then contributes 0 to ErotSQ
+      if (c.t.rho) rho = rotden_rho(c.t, f1, f2, &bad, &erot, &esq);
       if (c.s.rot_den_type == 1 && c.s.rn_ratio == 1) {
         rsrot(f1, f2, c.s.abc, c.s.rot_tau, c.s.rot_odevn, &rho, &erot);
         srot = rho;

@@ -401,8 +401,12 @@ def config2(n=4096, seed=2024, p_choices=(64, 128, 256, 512), n_he=(1, 64), t_ra
     return out
 
 
-def config1(seed=4321, nslices=1024, nrotslices=256, n_h2=64, grid3d=(200, 60, 60), griddens=(61, 121, 121)):
-    """1 asymmetric-top SO2-like rotor (A,B,C = 2.03, 0.344, 0.293 cm^-1) + 64 pH2 at 0.37 K."""
+def config1(seed=4321, nslices=1024, nrotslices=256, n_h2=64, grid3d=(200, 60, 60), griddens=(61, 121, 121),
+            ispher=0):
+    """1 asymmetric-top SO2-like rotor (A,B,C = 2.03, 0.344, 0.293 cm^-1) + 64 pH2 at 0.37 K.
+    ispher 1: the rotor-pH2 pair terms of the translational moves use the
+    spherical table of vspher.f (ISPHER, mc_piqmc.cc:1913-1922), here a
+    Lennard-Jones form on 3-26 bohr; the rotational moves keep vcord."""
     T = 0.37
     types = [
         dict(name="H2", numb=n_h2, molecule=0, stat=1, levels=3, mcstep=0.20, lamb=lam(MASSES["H2"]), fpot="h2h2"),
@@ -424,13 +428,19 @@ def config1(seed=4321, nslices=1024, nrotslices=256, n_h2=64, grid3d=(200, 60, 6
     pos = _sphere_points(rng, n_h2, radius, 2.9, avoid=((0, 0, 0),), avoid_sep=3.6)
     pos = np.vstack([pos, np.zeros((1, 3))])
     coords, angles = initial_path(n_h2 + 1, nslices, pos, rng)
+    if ispher:
+        rb = 3.0 + 0.046 * np.arange(501)
+        tables.update(sph_table=np.ascontiguousarray(np.minimum(lj(rb * BOHR_A, 40.0, 3.5), 2.0e5)), sph_r0=3.0,
+                      sph_rmax=26.0, sph_rstep=0.046)
     return Workload("config1-SO2-64pH2", types, nslices, nrotslices, T, rtstep=0.1, rotation=True,
-                    rot_abc=abc, tables=tables, coords=coords, angles=angles,
+                    rot_abc=abc, tables=tables, coords=coords, angles=angles, ispher=ispher,
                     pindex=np.arange(n_h2 + 1, dtype=np.int32), chi_fold_deg=90)
 
 
-def config3(seed=77, nslices=4096, nrotslices=2048, griddens=(61, 121, 121), sep=3.0):
-    """2 rigid water-like asymmetric tops (A,B,C = 27.9, 14.5, 9.3 cm^-1) at 0.74 K, caleng potential."""
+def config3(seed=77, nslices=4096, nrotslices=2048, griddens=(61, 121, 121), sep=3.0, rot_den_type=0):
+    """2 rigid water-like asymmetric tops (A,B,C = 27.9, 14.5, 9.3 cm^-1) at 0.74 K, caleng potential.
+    rot_den_type 1: the analytic rattle-and-shake propagator (ROTDENSI 1) in
+    the moves; the table is still loaded for the E^2 estimator."""
     T = 0.74
     types = [dict(name="H2O", numb=2, molecule=2, stat=0, levels=5, mcstep=0.05, lamb=lam(MASSES["H2O"]),
                   fpot="none")]
@@ -445,7 +455,7 @@ def config3(seed=77, nslices=4096, nrotslices=2048, griddens=(61, 121, 121), sep
     angles[0, :] = 0.0
     angles[1, :] = math.cos(math.radians(127.0))
     return Workload("config3-H2O-dimer", types, nslices, nrotslices, T, rtstep=0.05, rotation=True,
-                    rot_abc=abc, tables=tables, coords=coords, angles=angles,
+                    rot_abc=abc, tables=tables, coords=coords, angles=angles, rot_den_type=rot_den_type,
                     pindex=np.arange(2, dtype=np.int32))
 
 
@@ -500,6 +510,12 @@ def water_chain(nrot, nh2, nslices, nrotslices, T, seed, tables, spacing=3.0, rt
     return Workload(name, types, nslices, nrotslices, T, rtstep=rtstep, rotation=True, rot_den_type=1,
                     rot_abc=WATER_ABC, tables=tb, coords=coords, angles=angles,
                     pindex=np.arange(nh2 + nrot, dtype=np.int32), chi_fold_deg=90)
+
+
+def water_chain_case(seed, nrot, nh2, nslices, nrotslices, T, grid3d=(30, 37, 19), griddens=None):
+    """One system of the water-chain family with its own (small) tables."""
+    return water_chain(nrot, nh2, nslices, nrotslices, T, seed, water_chain_tables(seed, grid3d), griddens=griddens,
+                       name="water-chain-%dw-%dh2" % (nrot, nh2))
 
 
 def config4(n=512, seed=4040, p_choices=(512, 1024, 2048), n_rot=(1, 8), n_h2=(0, 32), t_range=(0.5, 2.0),

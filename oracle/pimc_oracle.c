@@ -12,6 +12,11 @@
  *    slice is used.  With the identity permutation both are identical.
  *  - GetRotE3D advances the rotor offset cumulatively (mc_estim.cc:1000-1003),
  *    which is correct for <= 2 rotors only; here rotor a uses offset a*P.
+ *  - GetRotE3D with the rattle-and-shake density converts the running sum of
+ *    all rotors' link sums to an energy once per rotor (mc_estim.cc:1084-1090),
+ *    so with two or more rotors the earlier rotors are converted again; here
+ *    each rotor's sum is converted once and the energies are added (the same
+ *    for one rotor).
  *  - the grids of vcalc and rotpro are generalised to n points over the same
  *    angular ranges; at the reference's 1-degree sizes the arithmetic is the
  *    reference's (the step is exactly 1.0).
@@ -1747,14 +1752,14 @@ double orc_rot_e3d(const orc_ctx *c, double *erotsq, double *erot_termsq)
     srot = srot / nq;
     sesq = sesq / (nq * nq);
     se_termsq = se_termsq / (nq * nq);
-    ERot3D += srot;
     ErotSQ += sesq;
     EtermSQ += se_termsq;
-    if (c->sys.rot_den_type == 1 && c->sys.rn_ratio == 1) {
-      ERot3D = ERot3D / (4.0 * (c->rot_tau / WNO2K) * (c->rot_tau / WNO2K));
-      ERot3D += 0.25 * (c->sys.rot_abc[0] + c->sys.rot_abc[1] + c->sys.rot_abc[2]) + 1.5 / (c->rot_tau / WNO2K);
-      ERot3D = ERot3D / WNO2K;
+    if (c->sys.rot_den_type == 1 && c->sys.rn_ratio == 1) {      /* per rotor, see header */
+      srot = srot / (4.0 * (c->rot_tau / WNO2K) * (c->rot_tau / WNO2K));
+      srot += 0.25 * (c->sys.rot_abc[0] + c->sys.rot_abc[1] + c->sys.rot_abc[2]) + 1.5 / (c->rot_tau / WNO2K);
+      srot = srot / WNO2K;
     }
+    ERot3D += srot;
   }
   if (erotsq) *erotsq = ErotSQ;
   if (erot_termsq) *erot_termsq = EtermSQ;

@@ -13,7 +13,56 @@ def load_golden(case):
 
 
 def golden_cases():
-    return ["c0s", "c1s", "c3s"]
+    return ["c0s", "c1s", "c3s", "c3r", "c4s", "c1p"]
+
+
+def nrotors(w):
+    return sum(t["numb"] for t in w.types if t["molecule"] != 0)
+
+
+def rot_est_from_reference(w):
+    """Which rotational estimators of the fixture (est[2], est[3..4]) the
+    reference computes as intended.  GetRotE3D advances the rotor offset
+    cumulatively (mc_estim.cc:1000-1003), so with three or more rotors it
+    reads past the rotors' angles; with the rattle-and-shake density it
+    converts the running sum of all rotors once per rotor
+    (mc_estim.cc:1084-1090), so E_rot of two or more rotors is not their
+    sum.  Those values are compared with the oracle, which keeps each rotor
+    at its own offset and converts each rotor's sum once."""
+    n = nrotors(w) if w.rotation else 0
+    erot_ok = n <= 1 or (n == 2 and w.rot_den_type == 0)
+    sq_ok = n <= 2
+    return erot_ok, sq_ok
+
+
+def rs_rotor_means(w, angles):
+    """Per rotor, the mean over its Q links of rsrot's rho (the
+    rattle-and-shake exponent sumaxs, rotden.f:247-284) from the reference's
+    angle array (phi, cos theta, chi)."""
+    import workloads as W
+    P, Q = w.nslices, w.nrotslices
+    rt = [i for i, t in enumerate(w.types) if t["molecule"] != 0][0]
+    first = sum(t["numb"] for t in w.types[:rt])
+    bl = 1.0 / np.asarray(w.rot_abc, dtype=np.float64)
+    out = []
+    for r in range(w.types[rt]["numb"]):
+        a = (first + r) * P
+        ph, ct, ch = angles[0, a:a + Q], angles[1, a:a + Q], angles[2, a:a + Q]
+        m = W.matpre(ph, np.arccos(ct), ch)                       # [3][3][Q]
+        m2 = np.roll(m, -1, axis=2)
+        dig = [np.sum(m[:, i, :] * m2[:, i, :], axis=0) for i in range(3)]
+        sumaxs = ((bl[0] - bl[1] - bl[2]) * (1.0 - dig[0]) + (bl[1] - bl[2] - bl[0]) * (1.0 - dig[1])
+                  + (bl[2] - bl[0] - bl[1]) * (1.0 - dig[2]))
+        out.append(float(np.mean(sumaxs)))
+    return out
+
+
+def rs_energy(w, mean_sumaxs):
+    """GetRotE3D's rattle-and-shake conversion of a link mean (mc_estim.cc:1084-1090), K."""
+    wno2k = 0.6950356
+    tau = 1.0 / (w.temperature * w.nrotslices) / wno2k
+    e = mean_sumaxs / (4.0 * tau * tau) + 0.25 * float(np.sum(w.rot_abc)) + 1.5 / tau
+    return e / wno2k
 
 
 def golden(case):

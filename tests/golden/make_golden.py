@@ -47,12 +47,24 @@ CASES = {
     "c0s": ("config0", dict(seed=11, nslices=32, nrotslices=8, n_he=4, r2d_step=0.05, c2d_step=0.04)),
     "c1s": ("config1", dict(seed=12, nslices=32, nrotslices=8, n_h2=6, grid3d=(30, 37, 19), griddens=(19, 37, 37))),
     "c3s": ("config3", dict(seed=13, nslices=64, nrotslices=16, griddens=(19, 37, 37))),
+    # the rattle-and-shake propagator (ROTDENSI 1, rotden.f:218-286) in the moves
+    "c3r": ("config3", dict(seed=14, nslices=64, nrotslices=16, griddens=(19, 37, 37), rot_den_type=1)),
+    # the water-chain family: 3 waters (caleng between them) + 4 pH2 (vcord), ROTDENSI 1
+    "c4s": ("water_chain_case", dict(seed=16, nrot=3, nh2=4, nslices=32, nrotslices=8, T=1.2,
+                                     griddens=(19, 37, 37))),
+    # ISPHER = 1: vspher for the rotor-pH2 terms of the translational moves
+    # (vspher.f); the reference allows it only without rotation (mc_input.cc)
+    "c1p": ("config1", dict(seed=15, nslices=32, nrotslices=8, n_h2=6, grid3d=(30, 37, 19), griddens=(19, 37, 37),
+                            ispher=1), dict(rotation=False)),
 }
 
 
 def make_workload(case):
-    fn, kw = CASES[case]
-    return getattr(W, fn)(**kw)
+    fn, kw = CASES[case][:2]
+    w = getattr(W, fn)(**kw)
+    for k, v in (CASES[case][2] if len(CASES[case]) > 2 else {}).items():
+        setattr(w, k, v)
+    return w
 
 
 def table_checksums(w):
@@ -90,7 +102,9 @@ def generate(case, nsteps=4, seed=2024):
     eul = np.column_stack([rng.uniform(0, 2 * np.pi, 6), np.arccos(rng.uniform(-1, 1, 6)), rng.uniform(0, 2 * np.pi, 6)])
     e_rot = np.zeros((6, len(slices)))
     cosine = None
-    if w.types[rtype]["molecule"] == 1:
+    if not w.rotation:
+        pass                              # no PotRotE3D / PotRotEnergy calls without rotation
+    elif w.types[rtype]["molecule"] == 1:
         cosine = np.zeros((3, nb))
         for k in range(6):
             cosine[:, :] = 0.0
@@ -131,6 +145,8 @@ def generate(case, nsteps=4, seed=2024):
             consumed.append(ref.replay_pos())
             seq.append((1, typ, 0))
             streams["u1"].append(u1); streams["u2"].append(u2)
+        if not w.rotation:
+            continue
         nr = w.types[rtype]["numb"]
         ur = rng.uniform(size=4 * w.nrotslices * nr)
         ref.replay(urot=ur)
@@ -151,7 +167,9 @@ def generate(case, nsteps=4, seed=2024):
     # ---- estimators on the final path
     kin = ref.L.ref_kin_energy()
     esq, ets = np.zeros(1), np.zeros(1)
-    if w.types[rtype]["molecule"] == 1:
+    if not w.rotation:
+        rot = 0.0
+    elif w.types[rtype]["molecule"] == 1:
         rot = ref.L.ref_rot_energy(O.dptr(esq), O.dptr(ets))
     else:
         rot = ref.L.ref_rot_e3d(O.dptr(esq), O.dptr(ets))

@@ -19,16 +19,26 @@ RTOL32 = 1e-5
 
 @pytest.mark.parametrize("name", golden_cases())
 def test_mixed_precision_moves_track_the_fp64_oracle(name):
+    """Every move of the fixture's sequence is compared.  Where a decision
+    differs (the uniform lies within the FP32 tolerance of the acceptance
+    probability), the quantity it was made from must still agree within the
+    tolerance; the GPU path is then set to the oracle's and the sequence goes
+    on, so no move is left out.  Such resynchronisations must stay rare."""
     w, d, _ = golden(name)
     s = G.Sampler(w, mixed=True)
     o = O.Oracle(w)
     st = split_streams(d)
     tau = 1.0 / (w.temperature * w.nslices)
     emax = float(np.max(np.abs(d["e_slice"])))
-    erot = float(np.max(np.abs(d["e_rot"])))
+    erot = float(np.max(np.abs(d["e_rot"]))) if w.rotation else 0.0
     R = w.nslices // w.nrotslices
     ib = im = ir = 0
-    compared = 0
+    compared = parted = 0
+
+    def resync():
+        c, a, _, p = o.get_state()
+        s.set_state(c, a, p)
+
     for kind, typ, t in d["seq"]:
         typ, t = int(typ), int(t)
         if kind == 0:
@@ -38,19 +48,29 @@ def test_mixed_precision_moves_track_the_fp64_oracle(name):
             assert rs == 0
             M = 1 << w.types[typ]["levels"]
             tol = RTOL32 * np.maximum(np.abs(ods), tau * M * M * emax)
-            if not (lv == olv).all():
-                break                      # a borderline level decision: paths part here
-            mask = np.arange(ds.shape[1])[None, :] <= np.minimum(lv, ds.shape[1] - 1)[:, None]
+            lvc = np.minimum(lv, olv)          # levels both reached
+            mask = np.arange(ds.shape[1])[None, :] <= np.minimum(lvc, ds.shape[1] - 1)[:, None]
+            # atoms after the first differing decision move on different paths
+            k = int(np.argmax(lv != olv)) if not (lv == olv).all() else len(lv)
+            mask[k + 1:] = False
             assert (np.abs(ds - ods)[mask] <= tol[mask]).all(), (ds, ods)
-            assert cons == ocons
+            if not (lv == olv).all():
+                parted += 1
+                resync()
+            else:
+                assert cons == ocons
         elif kind == 1:
             u1, u2 = st["u1"][im], st["u2"][im]; im += 1
             rs, dv, acc, cons = s.molecular_move(typ, u1, u2)
             _, odv, oacc, ocons = o.molecular_move(typ, u1, u2)
             assert rs == 0
-            assert (np.abs(dv - odv) <= RTOL32 * np.maximum(np.abs(odv), 2 * w.nslices * emax)).all()
-            if not (acc == oacc).all():
-                break
+            k = int(np.argmax(acc != oacc)) if not (acc == oacc).all() else len(acc)
+            # atoms up to the first differing decision read identical paths
+            sc = RTOL32 * np.maximum(np.abs(odv), 2 * w.nslices * emax)
+            assert (np.abs(dv - odv)[:k + 1] <= sc[:k + 1]).all()
+            if k < len(acc):
+                parted += 1
+                resync()
         else:
             ur = st["urot"][ir]; ir += 1
             rs, rd, acc = s.rotations(ur)
@@ -59,11 +79,14 @@ def test_mixed_precision_moves_track_the_fp64_oracle(name):
             scale = np.maximum(np.abs(ord_), 1.0) * max(1.0, tau * 2 * R * erot)
             if not (acc == oacc).all():
                 k = int(np.argmax(acc != oacc))
-                assert abs(rd[k] - ord_[k]) <= RTOL32 * scale[k]
-                break
-            assert (np.abs(rd - ord_) <= RTOL32 * scale).all(), np.max(np.abs(rd - ord_) / scale)
+                assert (np.abs(rd - ord_)[:k + 1] <= RTOL32 * scale[:k + 1]).all()
+                parted += 1
+                resync()
+            else:
+                assert (np.abs(rd - ord_) <= RTOL32 * scale).all(), np.max(np.abs(rd - ord_) / scale)
         compared += 1
-    assert compared >= 3
+    assert compared == len(d["seq"])
+    assert parted <= max(1, len(d["seq"]) // 10), (parted, compared)
     s.close()
 
 

@@ -10,7 +10,7 @@ import pytest
 import oracle as O
 import pimc_gb300 as G
 import workloads as W
-from _common import golden, golden_cases, split_streams
+from _common import golden, golden_cases, rot_est_from_reference, split_streams
 
 pytestmark = pytest.mark.gpu
 RTOL = 1e-10
@@ -47,6 +47,8 @@ def test_pot_energy_matches_reference_fixture(case):
 
 def test_rot_energy_matches_reference_fixture(case):
     name, w, d = case
+    if not w.rotation:
+        pytest.skip("no rotational slices in this system")
     s = G.Sampler(w)
     s.set_state(d["coords0"], d["angles0"], w.pindex)
     rtype = [i for i, t in enumerate(w.types) if t["molecule"] != 0][0]
@@ -127,10 +129,20 @@ def test_estimators_match_reference_fixture(case):
     s = G.Sampler(w)
     s.set_state(d["coords1"], d["angles1"], w.pindex)
     est = s.estimators()
-    _close(est, d["est"], scale=np.maximum(np.abs(d["est"]), 1.0))
     o = O.Oracle(w)
     o.set_state(d["coords1"], d["angles1"], w.pindex)
-    if any(t["molecule"] != 0 for t in w.types):
+    # the reference's values where its GetRotE3D computes what it intends,
+    # else the oracle's (each rotor at its own offset, converted once)
+    erot_ok, sq_ok = rot_est_from_reference(w)
+    want = np.array(d["est"], dtype=np.float64)
+    if w.rotation and not (erot_ok and sq_ok):
+        rot, esq, ets = o.rot_energy(True)
+        if not erot_ok:
+            want[2] = rot
+        if not sq_ok:
+            want[3], want[4] = esq, ets
+    _close(est, want, scale=np.maximum(np.abs(want), 1.0))
+    if w.rotation and any(t["molecule"] != 0 for t in w.types):
         _close(s.rcf(), o.rcf())
     s.close()
 
