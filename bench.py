@@ -60,8 +60,10 @@ def parse():
     ap.add_argument("--no-worm", action="store_true", help="skip the worm-algorithm pass measurement")
     ap.add_argument("--no-surrogate", action="store_true", help="skip the surrogate / delayed-acceptance measurement")
     ap.add_argument("--worm-replicas", type=int, default=32, help="independent worm chains run at once")
+    ap.add_argument("--quick-se", action="store_true", help="short series for the matched-SE measurement")
+    ap.add_argument("--no-matched-se", action="store_true", help="skip the matched <E> SE measurement")
     ap.add_argument("--da-replicas", type=int, default=32, help="independent dimer systems swept at once")
-    ap.add_argument("--only", default=None, choices=["tables", "worm", "surrogate"],
+    ap.add_argument("--only", default=None, choices=["tables", "worm", "surrogate", "matched_se"],
                     help="run one companion measurement alone on cuda:0 and print its JSON (for profiling)")
     return ap.parse_args()
 
@@ -590,6 +592,210 @@ def run_worm(local, cpu, steps=5, warmup=2, replicas=32):
     return out
 
 
+# ------------------------------------------------------------ matched <E> SE
+
+def pooled_inefficiency(E):
+    """Statistical inefficiency g = 2 tau_int (in passes) of E[pass, replica]:
+    each replica's series centred and scaled by its own variance, the
+    normalised autocorrelation pooled over replicas, summed with Sokal's
+    self-consistent window (the smallest W with W >= 5 tau(W))."""
+    import numpy as np
+    x = np.asarray(E, dtype=np.float64)
+    x = x - x.mean(axis=0, keepdims=True)
+    var = np.mean(x * x, axis=0)
+    x = x[:, var > 0] / np.sqrt(var[var > 0])
+    K = x.shape[0]
+    tau = 0.5
+    for k in range(1, K // 2):
+        rho = float(np.mean(np.sum(x[:-k] * x[k:], axis=0) / (K - k)))
+        tau += rho
+        if k >= 5.0 * tau:
+            break
+    return max(2.0 * tau, 1e-3)
+
+
+def series_stats(E):
+    """Per-arm summary of an energy series E[pass, replica]: pooled g, the
+    mean over replicas of the blocking SE of <E> (pimc_blocking_se) where the
+    series is long enough, and the replica variances."""
+    import numpy as np
+    import pimc_gb300 as G
+    E = np.asarray(E, dtype=np.float64)
+    g = pooled_inefficiency(E)
+    var = E.var(axis=0, ddof=1)
+    se = None
+    if E.shape[0] >= 16:
+        se = float(np.mean([G.blocking_se(E[:, r])["se"] for r in range(E.shape[1])]))
+    return {"g": round(g, 3), "passes": int(E.shape[0]), "mean_sd_K": round(float(np.mean(np.sqrt(var))), 4),
+            "mean_blocking_se_K": None if se is None else round(se, 4)}, var
+
+
+def batch_series(b, npasses, seed, eq, da=None):
+    """eq untimed passes, then npasses passes each timed with CUDA events on
+    the batch's stream; after each pass every replica's E = E_kin + E_pot +
+    E_rot (pimc_batch_estimators, outside the events).  da: (mlp, escale) for
+    delayed-acceptance passes (mlp None: the same passes without the
+    screen)."""
+    import numpy as np
+    import torch
+    ext = torch.cuda.ExternalStream(b.stream())
+    run = (lambda n, sd: b.da_passes(n, sd, mlp=da[0], escale=da[1])) if da is not None else b.run_passes
+    if eq:
+        run(eq, seed)
+    b.synchronize()
+    E, ms = [], 0.0
+    for k in range(npasses):
+        with torch.cuda.stream(ext):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(ext)
+            run(1, seed)
+            e1.record(ext)
+        b.synchronize()
+        torch.cuda.synchronize()
+        ms += e0.elapsed_time(e1)
+        est = b.estimators()
+        E.append(est[:, 0] + est[:, 1] + est[:, 2])
+    return np.array(E), ms / npasses
+
+
+def single_pass_ms(ws, idx, seed, mixed=False):
+    """One production pass of each chosen system on its own handle (the plain
+    GPU path), CUDA events on the handle's stream after one untimed pass."""
+    import torch
+    import pimc_gb300 as G
+    out = []
+    for r in idx:
+        s = G.Sampler(ws[r], mixed=mixed)
+        s.run_passes(1, seed)
+        s.synchronize()
+        ext = torch.cuda.ExternalStream(s.stream())
+        with torch.cuda.stream(ext):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(ext)
+            s.run_passes(1, seed)
+            e1.record(ext)
+        s.synchronize()
+        torch.cuda.synchronize()
+        out.append(e0.elapsed_time(e1))
+        s.close()
+    return out
+
+
+def matched(plain_pass_ms, plain_g, plain_var, arms, c=0.05):
+    """Time for every replica's <E> to reach a standard error of c times its
+    own plain-path E fluctuation: n = g (var_arm / var_plain) / c^2 passes;
+    the plain path runs the replicas one after another (its pass time is the
+    sum over replicas), a batch runs them together."""
+    import numpy as np
+    n_plain = plain_g / (c * c)
+    t_plain = n_plain * plain_pass_ms / 1e3
+    out = {"target": "SE(<E>) = %.2f sd(E) per replica" % c,
+           "plain": {"passes": round(n_plain, 1), "seconds": round(t_plain, 2)}}
+    for name, a in arms.items():
+        v = float(np.sum(a["var"]) / np.sum(plain_var))
+        n = a["g"] * v / (c * c)
+        t = n * a["pass_ms"] / 1e3
+        out[name] = {"passes": round(n, 1), "seconds": round(t, 3), "var_ratio": round(v, 4),
+                     "vs_plain": round(t_plain / t, 2)}
+    return out
+
+
+def run_matched_se(local, quick=False, c4_replicas=512, c4_passes=24, c3_replicas=64):
+    """The metric itself: bead-moves/s at matched <E> standard error.
+
+    Water chains (config 4): c4_replicas replicas of 1-8 water tops on a
+    3 A chain + 0-32 pH2, T 0.5-2.0 K, P 512-2048, Q = P/4.  Arms: the plain
+    GPU path (each replica alone on the single-system sampler, FP64; its pass
+    time measured on a seeded sample of replicas and scaled to all), the
+    batch in FP64 (replica by replica the same chains as the plain path) and
+    the batch on the FP32 table path.  g (2 tau_int of E in passes) and the
+    E variances come from each batch's own series; the plain path's are the
+    FP64 batch's.
+
+    Water dimers (config 3 molecules, T 0.74 K, P = 512, Q = 256, levels 4,
+    reduced slices so that a series fits the run): the plain GPU path, the
+    batch with its rotational sweeps in the persistent kernel, and the batch
+    with delayed-acceptance rotational sweeps screened by the surrogate,
+    trained on the plain sampler's own rows."""
+    import numpy as np
+    import pimc_gb300 as G
+    import workloads as W
+    out = {}
+    # ---------------- config 4
+    ws = W.config4(n=c4_replicas)
+    bm = sum(w.bead_moves_per_pass() for w in ws)
+    rng = np.random.default_rng(11)
+    k = 8 if quick else 24
+    idx = rng.choice(len(ws), size=min(k, len(ws)), replace=False)
+    ts = np.array(single_pass_ms(ws, idx, 5))
+    plain_ms = float(ts.mean()) * len(ws)
+    plain_ms_se = float(ts.std(ddof=1) / np.sqrt(len(ts))) * len(ws) if len(ts) > 1 else None
+    arms = {}
+    for mixed in (False, True):
+        b = G.Batch(ws, mixed=mixed)
+        E, ms = batch_series(b, 8 if quick else c4_passes, 21, 2 if quick else 4)
+        st, var = series_stats(E)
+        arms["batched_" + ("fp32" if mixed else "fp64")] = dict(g=st["g"], var=var, pass_ms=ms, stats=st)
+        b.close()
+    f64 = arms["batched_fp64"]
+    out["config4"] = {
+        "workload": "config4: %d replicas of 1-8 water tops (caleng) on a 3 A chain + 0-32 pH2 (vcord), "
+                    "T 0.5-2.0 K, P 512-2048, Q=P/4, ROTDENSI 1" % len(ws),
+        "bead_moves_per_pass": bm,
+        "plain": {"bead_moves_per_s": round(bm / (plain_ms / 1e3), 1), "pass_ms_all_replicas": round(plain_ms, 1),
+                  "pass_ms_se": None if plain_ms_se is None else round(plain_ms_se, 1),
+                  "timed_replicas": int(len(idx)), "precision": "fp64", "g": f64["g"]},
+        "arms": {n: {"bead_moves_per_s": round(bm / (a["pass_ms"] / 1e3), 1), "pass_ms": round(a["pass_ms"], 2),
+                     **a["stats"]} for n, a in arms.items()},
+        "time_to_se": matched(plain_ms, f64["g"], f64["var"], arms)}
+    # ---------------- water dimers with the surrogate
+    dims = [W.config3(seed=300 + r, nslices=512, nrotslices=256, levels=4) for r in range(c3_replicas)]
+    bmd = sum(w.bead_moves_per_pass() for w in dims)
+    ts = np.array(single_pass_ms(dims, range(min(4, len(dims))), 7))
+    plain_d_ms = float(ts.mean()) * len(dims)
+    # training rows from the plain sampler (dimer features, exact caleng energies)
+    s = G.Sampler(dims[0])
+    s.run_passes(2, 3)
+    xs, es = [], []
+    for kk in range(16 if quick else 64):
+        s.da_sweeps(4, 100 + kk)
+        f, e = s.da_samples()
+        xs.append(f)
+        es.append(e)
+    s.close()
+    x, e = np.concatenate(xs), np.concatenate(es)
+    mu, sd = float(e.mean()), float(e.std())
+    m = G.Mlp(device=local)
+    r0 = np.random.default_rng(5)
+    m.set_weights(r0.normal(0, 1 / np.sqrt(6), (6, 256)), np.zeros(256), r0.normal(0, 1 / 16, (256, 256)),
+                  np.zeros(256), r0.normal(0, 1 / 16, (256, 256)), np.zeros(256), r0.normal(0, 1 / 16, 256), 0.0)
+    m.train(x, (e - mu) / sd, epochs=4 if quick else 12, batch=8192, lr=2e-3, seed=6)
+    darms = {}
+    npd = 8 if quick else 32
+    for name, da in (("batched_plain", None), ("batched_da_exact", (None, sd)), ("batched_surrogate", (m, sd))):
+        b = G.Batch(dims)
+        E, ms = batch_series(b, npd, 31, 2 if quick else 4, da=da)
+        st, var = series_stats(E)
+        tot, acc = b.counters()
+        darms[name] = dict(g=st["g"], var=var, pass_ms=ms, stats=st, accept_rot=float(acc[2] / max(1, tot[2])))
+        b.close()
+    m.close()
+    pe = darms["batched_plain"]
+    out["config3_dimers"] = {
+        "workload": "config3 molecules: %d water dimers (caleng), T=0.74 K, P=512, Q=256, levels 4 (slices "
+                    "reduced from 4096/2048 so that a series fits the run)" % len(dims),
+        "bead_moves_per_pass": bmd,
+        "plain": {"bead_moves_per_s": round(bmd / (plain_d_ms / 1e3), 1), "pass_ms_all_replicas": round(plain_d_ms, 1),
+                  "timed_replicas": int(len(ts)), "precision": "fp64", "g": pe["g"]},
+        "arms": {n: {"bead_moves_per_s": round(bmd / (a["pass_ms"] / 1e3), 1), "pass_ms": round(a["pass_ms"], 2),
+                     "accept_rot": round(a["accept_rot"], 4), **a["stats"]} for n, a in darms.items()},
+        "surrogate": {"training_rows": int(len(x)), "energy_sd_K": round(sd, 2)},
+        "time_to_se": matched(plain_d_ms, pe["g"], pe["var"], darms)}
+    return out
+
+
 def run_surrogate(local, quick=False, replicas=32):
     """The surrogate with delayed acceptance on config 3 (2 water-like tops, caleng, T 0.74 K,
     P = 4096, Q = 2048): training data emitted by the plain sampler (dimer
@@ -754,7 +960,8 @@ def main():
             run = {"tables": lambda: run_tables(local, not args.no_cpu),
                    "worm": lambda: run_worm(local, not args.no_cpu, steps=args.steps, warmup=args.warmup,
                                             replicas=args.worm_replicas),
-                   "surrogate": lambda: run_surrogate(local, replicas=args.da_replicas)}[args.only]
+                   "surrogate": lambda: run_surrogate(local, replicas=args.da_replicas),
+                   "matched_se": lambda: run_matched_se(local, quick=args.quick_se)}[args.only]
             print(json.dumps({"part": args.only, **run()}), flush=True)
         return 0
     line, w = run_gb300(args, rank, local, world, dist)

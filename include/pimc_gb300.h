@@ -406,6 +406,20 @@ pimc_status pimc_batch_estimators(pimc_batch *b, double *out);
 pimc_status pimc_batch_counters(pimc_batch *b, double *total, double *accep);
 pimc_status pimc_batch_synchronize(pimc_batch *b);
 double      pimc_batch_bead_moves_per_pass(const pimc_batch *b);
+/* Delayed-acceptance rotational moves of a batch of water dimers (every
+ * replica two nonlinear rotors, no atoms, tabulated densities, one P, Q and
+ * R): pimc_da_sweeps of every replica at once -- per sub-phase one proposal
+ * launch over all replicas' moves, one surrogate launch over all their
+ * feature rows, one decision launch -- with replica r's moves and draws
+ * those of a single handle run with pimc_batch_replica_seed(seed, r).
+ * pimc_batch_da_passes: npasses passes, each the translational moves of
+ * the production pass (pimc_batch_run_passes without its rotational
+ * sweeps) followed by P delayed-acceptance sweeps, the pass's rotational
+ * moves.  stats[4] summed over the replicas as pimc_da_sweeps'. */
+pimc_status pimc_batch_da_sweeps(pimc_batch *b, pimc_mlp *m, int nsweeps, uint64_t seed, float escale,
+                                 int use_surrogate, double *stats);
+pimc_status pimc_batch_da_passes(pimc_batch *b, pimc_mlp *m, int npasses, uint64_t seed, float escale,
+                                 int use_surrogate, double *stats);
 uint64_t    pimc_batch_replica_seed(uint64_t seed, int replica);
 void       *pimc_batch_stream(const pimc_batch *b);
 

@@ -432,7 +432,7 @@ __global__ void k_batch_reset(unsigned *work) { *work = 0u; }
 // register allocation is bounded for (a shape the autotuner tries)
 template <bool MIX, int MINB>
 __global__ void __launch_bounds__(256, MINB) k_batch_pass(const BatchRep *reps, const int *order, int n,
-                                                          uint64_t seed, unsigned *work)
+                                                          uint64_t seed, unsigned *work, int rot_on)
 {
   extern __shared__ __align__(16) unsigned char smem[];
   Ctx &c = *reinterpret_cast<Ctx *>(smem);
@@ -459,7 +459,7 @@ __global__ void __launch_bounds__(256, MINB) k_batch_pass(const BatchRep *reps, 
     const unsigned ps = sps;
     const uint64_t sr = seed ^ reps[r].seed_mix;
     const DevSys &s = c.s;
-    const bool rot = s.nrotors > 0 && reps[r].rotation;
+    const bool rot = s.nrotors > 0 && reps[r].rotation && rot_on;
     const bool linear = rot && s.molecule[s.imtype] == 1;
     unsigned long long cnt[12];
     for (int i = 0; i < 12; i++) cnt[i] = 0;
@@ -664,17 +664,42 @@ int batch_max_ctas(int mixed, int warps, int minb)
 }
 
 void launch_batch_pass(const BatchRep *reps, const int *order, int n, uint64_t seed, unsigned *work, int mixed,
-                       int warps, int minb, int nctas, cudaStream_t s)
+                       int warps, int minb, int nctas, cudaStream_t s, int rot_on)
 {
   size_t sm = batch_smem_bytes(warps);
   k_batch_reset<<<1, 1, 0, s>>>(work);
   if (mixed) {
-    if (minb >= 3) k_batch_pass<true, 3><<<nctas, 32 * warps, sm, s>>>(reps, order, n, seed, work);
-    else k_batch_pass<true, 2><<<nctas, 32 * warps, sm, s>>>(reps, order, n, seed, work);
+    if (minb >= 3) k_batch_pass<true, 3><<<nctas, 32 * warps, sm, s>>>(reps, order, n, seed, work, rot_on);
+    else k_batch_pass<true, 2><<<nctas, 32 * warps, sm, s>>>(reps, order, n, seed, work, rot_on);
   } else {
-    if (minb >= 3) k_batch_pass<false, 3><<<nctas, 32 * warps, sm, s>>>(reps, order, n, seed, work);
-    else k_batch_pass<false, 2><<<nctas, 32 * warps, sm, s>>>(reps, order, n, seed, work);
+    if (minb >= 3) k_batch_pass<false, 3><<<nctas, 32 * warps, sm, s>>>(reps, order, n, seed, work, rot_on);
+    else k_batch_pass<false, 2><<<nctas, 32 * warps, sm, s>>>(reps, order, n, seed, work, rot_on);
   }
+}
+
+// after rotational moves made outside k_batch_pass: each replica's MCCosine
+// from its angles and its rotor caches stale
+__global__ void k_batch_rot_changed(const BatchRep *reps, int n)
+{
+  const int r = blockIdx.x;
+  if (r >= n) return;
+  const Ctx &c = reps[r].c;
+  const size_t nq = (size_t)c.s.nrotors * c.s.Q;
+  for (size_t i = threadIdx.x; i < nq; i += blockDim.x) {
+    double v[3];
+    unit_vector(c.st.ang[i], c.st.ang[nq + i], v);
+    for (int d = 0; d < 3; d++) {
+      c.st.cosv[d * nq + i] = v[d];
+      c.st.cosvf[d * nq + i] = (float)v[d];
+    }
+    c.st.rp_ok[i] = 0;
+    c.st.rl_ok[i] = 0;
+  }
+}
+
+void launch_batch_rot_changed(const BatchRep *reps, int n, cudaStream_t s)
+{
+  if (n > 0) k_batch_rot_changed<<<n, 256, 0, s>>>(reps, n);
 }
 
 void launch_batch_est(const BatchRep *reps, int n, double *out, cudaStream_t s)

@@ -1842,6 +1842,14 @@ struct pimc_batch {
   uint64_t exec_seed = 0;
   int exec_warps = 0, exec_minb = 0, exec_mixed = -1;
   double bm_pass = 0.0;
+  // the captured delayed-acceptance call and what it was captured for
+  cudaGraphExec_t da_exec = nullptr;
+  int da_count = 0, da_use = -1, da_shape = 0, da_mixed = -1;
+  uint64_t da_seed = 0;
+  float da_escale = 0.0f;
+  unsigned long long da_mlp = 0;
+  void *da_buf = nullptr;
+  long long da_nodes = 0;
 };
 
 #define BK(x)                                                  \
@@ -1979,6 +1987,7 @@ extern "C" pimc_status pimc_batch_destroy(pimc_batch *b)
 {
   if (!b) return PIMC_ERR_BAD_ARG;
   if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->da_exec) cudaGraphExecDestroy(b->da_exec);
   if (b->base) pimc_destroy(b->base);
   delete b;
   return PIMC_OK;
@@ -2173,6 +2182,135 @@ extern "C" pimc_status pimc_batch_run_passes(pimc_batch *b, int npasses, uint64_
     CK(cudaGetLastError());
   }
   return PIMC_OK;
+}
+
+// ---- delayed acceptance over a batch of water dimers
+
+// every replica a water dimer of one shape (two tops, no atoms, tabulated
+// densities, the same P, Q and R, even Q): the moves of a sub-phase of all
+// replicas are then one flat index range
+static pimc_status batch_da_check(pimc_batch *b)
+{
+  const DevSys &d0 = b->reps[0].c.s;
+  for (int r = 0; r < b->n; r++) {
+    const DevSys &d = b->reps[r].c.s;
+    if (d.nrotors != 2 || d.na != 2 || d.molecule[d.imtype] != PIMC_NONLINEAR || d.rot_den_type != 0 || d.Q % 2 ||
+        d.Q != d0.Q || d.R != d0.R || d.P != d0.P || !b->sys[r].rotation)
+      return PIMC_ERR_STATE;
+  }
+  return PIMC_OK;
+}
+
+// nsweeps delayed-acceptance sweeps of every replica (pimc_da_sweeps of each,
+// with the replica's seed); with translation = 1, `npasses` passes instead:
+// each the translational moves of the production pass (rotation off), then
+// P sweeps.  One CUDA graph per call shape.
+static pimc_status batch_da_run(pimc_batch *b, pimc_mlp *m, int count, int passes, uint64_t seed, float escale,
+                                int use_surrogate, double *stats)
+{
+  pimc_status e = batch_ready(b);
+  if (e) return e;
+  if ((e = batch_da_check(b))) return e;
+  if (count < 0 || (use_surrogate && !m)) return PIMC_ERR_BAD_ARG;
+  if (use_surrogate && mlp_poisoned(m)) return PIMC_ERR_TIMEOUT;
+  pimc_handle *h = b->base;
+  CK(cudaSetDevice(h->device));
+  const DevSys &d = b->reps[0].c.s;
+  const int nm = d.Q / 2, nsw = passes ? d.P : count;
+  if ((long long)nsw * (passes ? count : 1) > (1 << 20)) return PIMC_ERR_SIZE;
+  const size_t moves = (size_t)nm * b->n, rows = moves * 2 * d.R;
+  size_t bytes = rows * 7 * sizeof(float) + moves * sizeof(DaMove) + 4096;
+  void *buf;
+  if ((e = scratch(h, bytes, &buf))) return e;
+  char *cur = (char *)buf;
+  unsigned long long *st = (unsigned long long *)cur;
+  cur += 256;
+  float *feat = (float *)cur;
+  cur += (rows * 6 * sizeof(float) + 255) / 256 * 256;
+  float *y = (float *)cur;
+  cur += (rows * sizeof(float) + 255) / 256 * 256;
+  DaMove *mv = (DaMove *)cur;
+  int nctas = 0;
+  if (passes) {
+    nctas = batch_max_ctas(b->mixed, b->warps, b->minb);
+    if (nctas <= 0) return PIMC_ERR_CUDA;
+    if (nctas > b->n) nctas = b->n;
+  }
+  auto sweeps = [&]() -> long long {
+    long long n = 0;
+    for (int sw = 0; sw < nsw; sw++)
+      for (int par = 0; par < 2; par++)
+        for (int r = 0; r < 2; r++) {
+          unsigned phase = 4u * (unsigned)sw + 2u * par + r;
+          n += launch_da_propose_b(b->d_reps, nm, b->n, r, par, phase, seed, feat, mv, h->stream);
+          if (use_surrogate) n += mlp_forward_device(m, feat, (int)rows, y, h->stream);
+          n += launch_da_decide_b(b->d_reps, nm, b->n, r, par, phase, seed, y, use_surrogate, escale, mv, st,
+                                  h->stream);
+        }
+    return n;
+  };
+  auto record = [&]() -> long long {
+    long long n = 0;
+    if (passes) {
+      // the translational moves advance the pass counters that key the sweeps' draws
+      launch_batch_pass(b->d_reps, b->d_order, b->n, seed, b->d_work, b->mixed, b->warps, b->minb, nctas, h->stream,
+                        0);
+      n += 2;
+    } else {
+      n += launch_da_pass_b(b->d_reps, b->n, h->stream);
+    }
+    n += sweeps();
+    launch_batch_rot_changed(b->d_reps, b->n, h->stream);
+    return n + 1;
+  };
+  const unsigned long long mk = use_surrogate ? mlp_uid(m) : 0ull;
+  const int key_count = passes ? -1 : count;
+  if (!b->da_exec || b->da_count != key_count || b->da_seed != seed || b->da_use != use_surrogate ||
+      b->da_escale != escale || b->da_mlp != mk || b->da_buf != buf || b->da_shape != b->warps * 8 + b->minb ||
+      b->da_mixed != b->mixed) {
+    if (b->da_exec) { BK(cudaGraphExecDestroy(b->da_exec)); b->da_exec = nullptr; }
+    cudaGraph_t graph;
+    CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    long long n = record();
+    cudaError_t le = cudaGetLastError();
+    cudaError_t ce = cudaStreamEndCapture(h->stream, &graph);
+    if (le != cudaSuccess || ce != cudaSuccess) {
+      if (ce == cudaSuccess) cudaGraphDestroy(graph);
+      h->last_cuda = le != cudaSuccess ? le : ce;
+      return PIMC_ERR_CUDA;
+    }
+    cudaError_t ie = cudaGraphInstantiate(&b->da_exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ie != cudaSuccess) { h->last_cuda = ie; return PIMC_ERR_CUDA; }
+    b->da_count = key_count; b->da_seed = seed; b->da_use = use_surrogate; b->da_escale = escale;
+    b->da_mlp = mk; b->da_buf = buf; b->da_nodes = n; b->da_shape = b->warps * 8 + b->minb; b->da_mixed = b->mixed;
+  }
+  CK(cudaMemsetAsync(st, 0, 4 * sizeof(unsigned long long), h->stream));
+  const int nlaunch = passes ? count : 1;
+  for (int p = 0; p < nlaunch; p++) {
+    CK(cudaGraphLaunch(b->da_exec, h->stream));
+    h->launches += b->da_nodes;
+  }
+  unsigned long long hs[4];
+  CK(cudaMemcpyAsync(hs, st, sizeof(hs), cudaMemcpyDeviceToHost, h->stream));
+  e = check_err(h);
+  if (!e && use_surrogate && mlp_take_error(m)) e = PIMC_ERR_TIMEOUT;
+  if (stats)
+    for (int k = 0; k < 4; k++) stats[k] = (double)hs[k];
+  return e;
+}
+
+extern "C" pimc_status pimc_batch_da_sweeps(pimc_batch *b, pimc_mlp *m, int nsweeps, uint64_t seed, float escale,
+                                            int use_surrogate, double *stats)
+{
+  if (nsweeps > (1 << 18)) return PIMC_ERR_BAD_ARG;
+  return batch_da_run(b, m, nsweeps, 0, seed, escale, use_surrogate, stats);
+}
+
+extern "C" pimc_status pimc_batch_da_passes(pimc_batch *b, pimc_mlp *m, int npasses, uint64_t seed, float escale,
+                                            int use_surrogate, double *stats)
+{
+  return batch_da_run(b, m, npasses, 1, seed, escale, use_surrogate, stats);
 }
 
 // the shapes tried: warps per CTA x CTAs per SM the registers are bounded for

@@ -64,17 +64,17 @@ __global__ void k_da_samples(Ctx c, const Frame *frames, float *feat, float *ene
   energy[it] = (float)caleng(f0, f1, c0[0], c0[1], c0[2], c1[0], c1[1], c1[2]);
 }
 
-__global__ void k_da_propose(Ctx c, const Frame *frames, int r, int parity, unsigned phase, uint64_t seed,
-                             const unsigned *pass, float *feat, DaMove *mv)
+// move k of the sub-phase (rotor r, slices of parity `parity`) of one system
+__device__ __forceinline__ void da_propose_move(const Ctx &c, const Frame *frames, int k, int r, int parity,
+                                                unsigned phase, uint64_t seed, unsigned ps, float *feat, DaMove &d)
 {
   const DevSys &s = c.s;
-  const int k = blockIdx.x * blockDim.x + threadIdx.x, q = 2 * k + parity;
-  if (q >= s.Q) return;
+  const int q = 2 * k + parity;
   const int Q = s.Q, R = s.R, g = s.rot_first + r, o = s.rot_first + 1 - r;
   const size_t n = (size_t)s.nrotors * Q;
   const int ri = rot_index(s, g, q);
   double u[4], prop[3];
-  rot_uniforms(seed, *pass, phase, q, r, false, u);
+  rot_uniforms(seed, ps, phase, q, r, false, u);
   rot_propose(s, false, c.st.ang[ri], c.st.ang[n + ri], c.st.ang[2 * n + ri], u, prop);
   Frame fn;
   make_frame64(prop[0], prop[1], prop[2], fn);
@@ -88,38 +88,58 @@ __global__ void k_da_propose(Ctx c, const Frame *frames, int r, int parity, unsi
     double ca[3], cb[3];
     centre(c, g, q * R + j, ca);
     centre(c, o, q * R + j, cb);
-    dimer_features(fn, ca, fb, cb, feat + ((size_t)k * 2 * R + 2 * j) * 6);
-    dimer_features(fo, ca, fb, cb, feat + ((size_t)k * 2 * R + 2 * j + 1) * 6);
+    dimer_features(fn, ca, fb, cb, feat + (2 * j) * 6);
+    dimer_features(fo, ca, fb, cb, feat + (2 * j + 1) * 6);
   }
-  DaMove &d = mv[k];
   d.prop[0] = prop[0]; d.prop[1] = prop[1]; d.prop[2] = prop[2];
   d.rn = rn;
   d.ro = ro;
   d.bad = bad;
 }
 
+__global__ void k_da_propose(Ctx c, const Frame *frames, int r, int parity, unsigned phase, uint64_t seed,
+                             const unsigned *pass, float *feat, DaMove *mv)
+{
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (2 * k + parity >= c.s.Q) return;
+  da_propose_move(c, frames, k, r, parity, phase, seed, *pass, feat + (size_t)k * 2 * c.s.R * 6, mv[k]);
+}
+
+// the same sub-phase of every replica of a batch: move j is replica j / nm's
+// move j % nm (replicas of one shape: the same Q and R)
+__global__ void k_da_propose_b(const BatchRep *reps, int nm, int nrep, int r, int parity, unsigned phase,
+                               uint64_t seed, float *feat, DaMove *mv)
+{
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= nm * nrep) return;
+  const int rep = j / nm, k = j - rep * nm;
+  const BatchRep &b = reps[rep];
+  da_propose_move(b.c, b.frames, k, r, parity, phase, seed ^ b.seed_mix, *b.pass,
+                  feat + (size_t)j * 2 * b.c.s.R * 6, mv[j]);
+}
+
 // stats[0] moves, [1] passed the first stage (all, without the surrogate),
 // [2] accepted, [3] exact potential differences evaluated
-__global__ void k_da_decide(Ctx c, Frame *frames, int r, int parity, unsigned phase, uint64_t seed,
-                            const unsigned *pass, const float *y, int use_sur, float escale, const DaMove *mv,
-                            unsigned long long *stats, unsigned long long *cnt)
+// returns bit 0: passed the first stage, bit 1: accepted, bit 2: exact
+// difference evaluated
+__device__ __forceinline__ unsigned da_decide_move(const Ctx &c, Frame *frames, int k, int r, int parity,
+                                                   unsigned phase, uint64_t seed, unsigned ps, const float *y,
+                                                   int use_sur, float escale, const DaMove &d)
 {
   const DevSys &s = c.s;
-  const int k = blockIdx.x * blockDim.x + threadIdx.x, q = 2 * k + parity;
-  if (q >= s.Q) return;
+  const int q = 2 * k + parity;
   const int Q = s.Q, R = s.R, g = s.rot_first + r, o = s.rot_first + 1 - r;
   const size_t n = (size_t)s.nrotors * Q;
   const int ri = rot_index(s, g, q);
-  const DaMove &d = mv[k];
   if (d.bad) atomicOr(c.st.err, (unsigned)DERR_GRID_RANGE);
   double u1, u2;
-  philox_u2(seed, ((uint64_t)(*pass) << 32) | ((uint64_t)phase << 12) | (uint64_t)q, 0x600000u | (uint32_t)r, 0u,
-            &u1, &u2);
+  philox_u2(seed, ((uint64_t)ps << 32) | ((uint64_t)phase << 12) | (uint64_t)q, 0x600000u | (uint32_t)r, 0u, &u1,
+            &u2);
   const double lr = log(d.rn / d.ro);
   double dvs = 0.0;
   bool pass1 = true;
   if (use_sur) {
-    for (int j = 0; j < R; j++) dvs += (double)y[(size_t)k * 2 * R + 2 * j] - (double)y[(size_t)k * 2 * R + 2 * j + 1];
+    for (int j = 0; j < R; j++) dvs += (double)y[2 * j] - (double)y[2 * j + 1];
     dvs *= (double)escale;
     pass1 = lr - s.tau * dvs > log(u1);
   }
@@ -138,7 +158,6 @@ __global__ void k_da_decide(Ctx c, Frame *frames, int r, int parity, unsigned ph
     }
     if (use_sur) acc = -s.tau * (dv - dvs) > log(u2);
     else acc = lr - s.tau * dv > log(u1);
-    atomicAdd(stats + 3, 1ull);
     if (acc) {
       c.st.ang[ri] = d.prop[0];
       c.st.ang[n + ri] = d.prop[1];
@@ -146,12 +165,68 @@ __global__ void k_da_decide(Ctx c, Frame *frames, int r, int parity, unsigned ph
       make_frame(d.prop[0], d.prop[1], d.prop[2], frames[ri]);
     }
   }
-  atomicAdd(stats, 1ull);
-  if (pass1) atomicAdd(stats + 1, 1ull);
-  if (acc) atomicAdd(stats + 2, 1ull);
-  const int type = s.imtype;
-  atomicAdd(cnt + (type * 3 + 2) * 2, 1ull);
-  if (acc) atomicAdd(cnt + (type * 3 + 2) * 2 + 1, 1ull);
+  return (pass1 ? 1u : 0u) | (acc ? 2u : 0u) | (pass1 ? 4u : 0u);
+}
+
+// the counts of a warp's moves added once per warp: stats[0..3] (moves,
+// first stage passed, accepted, exact differences) and the rotation
+// counters of MCTotal / MCAccep; cnt may differ between the lanes
+__device__ __forceinline__ void da_count(bool live, unsigned f, unsigned long long *stats, unsigned long long *cnt)
+{
+  const unsigned m = __ballot_sync(0xffffffffu, live);
+  const unsigned p1 = __ballot_sync(0xffffffffu, live && (f & 1u));
+  const unsigned ac = __ballot_sync(0xffffffffu, live && (f & 2u));
+  const unsigned ex = __ballot_sync(0xffffffffu, live && (f & 4u));
+  const int lane = threadIdx.x & 31;
+  if (lane == 0 && m) {
+    atomicAdd(stats, (unsigned long long)__popc(m));
+    atomicAdd(stats + 1, (unsigned long long)__popc(p1));
+    atomicAdd(stats + 2, (unsigned long long)__popc(ac));
+    atomicAdd(stats + 3, (unsigned long long)__popc(ex));
+  }
+  // lanes with the same counter array add together
+  const unsigned long long key = live ? (unsigned long long)cnt : 0ull;
+  const unsigned grp = __match_any_sync(0xffffffffu, key);
+  if (live && lane == __ffs(grp) - 1) {
+    atomicAdd(cnt, (unsigned long long)__popc(grp));
+    atomicAdd(cnt + 1, (unsigned long long)__popc(grp & ac));
+  }
+}
+
+// stats[0] moves, [1] passed the first stage (all, without the surrogate),
+// [2] accepted, [3] exact potential differences evaluated
+__global__ void k_da_decide(Ctx c, Frame *frames, int r, int parity, unsigned phase, uint64_t seed,
+                            const unsigned *pass, const float *y, int use_sur, float escale, const DaMove *mv,
+                            unsigned long long *stats, unsigned long long *cnt)
+{
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool live = 2 * k + parity < c.s.Q;
+  unsigned f = 0;
+  if (live) f = da_decide_move(c, frames, k, r, parity, phase, seed, *pass, y + (size_t)k * 2 * c.s.R, use_sur, escale,
+                               mv[k]);
+  da_count(live, f, stats, cnt + (c.s.imtype * 3 + 2) * 2);
+}
+
+__global__ void k_da_decide_b(const BatchRep *reps, int nm, int nrep, int r, int parity, unsigned phase,
+                              uint64_t seed, const float *y, int use_sur, float escale, const DaMove *mv,
+                              unsigned long long *stats)
+{
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool live = j < nm * nrep;
+  const int rep = live ? j / nm : 0, k = j - rep * nm;
+  const BatchRep &b = reps[rep];
+  unsigned f = 0;
+  if (live)
+    f = da_decide_move(b.c, b.frames, k, r, parity, phase, seed ^ b.seed_mix, *b.pass, y + (size_t)j * 2 * b.c.s.R,
+                       use_sur, escale, mv[j]);
+  da_count(live, f, stats, b.cnt + (b.c.s.imtype * 3 + 2) * 2);
+}
+
+// one more pass on every replica's counter (the keys of the call's draws)
+__global__ void k_da_pass_b(const BatchRep *reps, int nrep)
+{
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < nrep) ++(*reps[j].pass);
 }
 
 }  // namespace
@@ -176,5 +251,29 @@ int launch_da_decide(const Ctx &c, Frame *f, int r, int parity, unsigned phase, 
 {
   int nm = (c.s.Q + 1 - parity) / 2;
   k_da_decide<<<(nm + 127) / 128, 128, 0, s>>>(c, f, r, parity, phase, seed, pass, y, use_sur, escale, mv, stats, cnt);
+  return 1;
+}
+
+int launch_da_propose_b(const BatchRep *reps, int nm, int nrep, int r, int parity, unsigned phase, uint64_t seed,
+                        float *feat, DaMove *mv, cudaStream_t s)
+{
+  const int n = nm * nrep;
+  k_da_propose_b<<<(n + 127) / 128, 128, 0, s>>>(reps, nm, nrep, r, parity, phase, seed, feat, mv);
+  return 1;
+}
+
+int launch_da_decide_b(const BatchRep *reps, int nm, int nrep, int r, int parity, unsigned phase, uint64_t seed,
+                       const float *y, int use_sur, float escale, const DaMove *mv, unsigned long long *stats,
+                       cudaStream_t s)
+{
+  const int n = nm * nrep;
+  k_da_decide_b<<<(n + 127) / 128, 128, 0, s>>>(reps, nm, nrep, r, parity, phase, seed, y, use_sur, escale, mv,
+                                                 stats);
+  return 1;
+}
+
+int launch_da_pass_b(const BatchRep *reps, int nrep, cudaStream_t s)
+{
+  k_da_pass_b<<<(nrep + 127) / 128, 128, 0, s>>>(reps, nrep);
   return 1;
 }

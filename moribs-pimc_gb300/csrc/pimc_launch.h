@@ -87,8 +87,15 @@ struct BatchRep {
 #define PIMC_BATCH_CTX_BYTES (((sizeof(Ctx) + 15) / 16) * 16)
 
 size_t batch_smem_bytes(int warps);
+int launch_da_propose_b(const BatchRep *reps, int nm, int nrep, int r, int parity, unsigned phase, uint64_t seed,
+                        float *feat, DaMove *mv, cudaStream_t s);
+int launch_da_decide_b(const BatchRep *reps, int nm, int nrep, int r, int parity, unsigned phase, uint64_t seed,
+                       const float *y, int use_sur, float escale, const DaMove *mv, unsigned long long *stats,
+                       cudaStream_t s);
+int launch_da_pass_b(const BatchRep *reps, int nrep, cudaStream_t s);
 int batch_max_ctas(int mixed, int warps, int minb);
 void launch_batch_pass(const BatchRep *reps, const int *order, int n, uint64_t seed, unsigned *work, int mixed,
-                       int warps, int minb, int nctas, cudaStream_t s);
+                       int warps, int minb, int nctas, cudaStream_t s, int rot_on = 1);
+void launch_batch_rot_changed(const BatchRep *reps, int n, cudaStream_t s);
 void launch_batch_est(const BatchRep *reps, int n, double *out, cudaStream_t s);
 void launch_batch_refresh(const BatchRep *reps, int n, int derive, cudaStream_t s);

@@ -136,6 +136,8 @@ def load(path=LIBPATH):
     L.pimc_batch_replica_seed.argtypes = [C.c_uint64, C.c_int]
     L.pimc_batch_stream.restype = vp
     L.pimc_batch_stream.argtypes = [vp]
+    L.pimc_batch_da_sweeps.argtypes = [vp, vp, C.c_int, C.c_uint64, C.c_float, C.c_int, _dp]
+    L.pimc_batch_da_passes.argtypes = [vp, vp, C.c_int, C.c_uint64, C.c_float, C.c_int, _dp]
     _L = L
     return L
 
@@ -475,6 +477,18 @@ class Batch:
 
     def stream(self):
         return self.L.pimc_batch_stream(self.h)
+
+    def da_sweeps(self, nsweeps, seed, mlp=None, escale=1.0):
+        st = np.zeros(4)
+        _chk(self.L.pimc_batch_da_sweeps(self.h, mlp.h if mlp is not None else None, int(nsweeps), C.c_uint64(seed),
+                                         C.c_float(escale), 1 if mlp is not None else 0, dptr(st)), "pimc_batch_da_sweeps")
+        return st
+
+    def da_passes(self, npasses, seed, mlp=None, escale=1.0):
+        st = np.zeros(4)
+        _chk(self.L.pimc_batch_da_passes(self.h, mlp.h if mlp is not None else None, int(npasses), C.c_uint64(seed),
+                                         C.c_float(escale), 1 if mlp is not None else 0, dptr(st)), "pimc_batch_da_passes")
+        return st
 
     @staticmethod
     def replica_seed(seed, r):

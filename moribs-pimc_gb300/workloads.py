@@ -437,12 +437,12 @@ def config1(seed=4321, nslices=1024, nrotslices=256, n_h2=64, grid3d=(200, 60, 6
                     pindex=np.arange(n_h2 + 1, dtype=np.int32), chi_fold_deg=90)
 
 
-def config3(seed=77, nslices=4096, nrotslices=2048, griddens=(61, 121, 121), sep=3.0, rot_den_type=0):
+def config3(seed=77, nslices=4096, nrotslices=2048, griddens=(61, 121, 121), sep=3.0, rot_den_type=0, levels=5):
     """2 rigid water-like asymmetric tops (A,B,C = 27.9, 14.5, 9.3 cm^-1) at 0.74 K, caleng potential.
     rot_den_type 1: the analytic rattle-and-shake propagator (ROTDENSI 1) in
     the moves; the table is still loaded for the E^2 estimator."""
     T = 0.74
-    types = [dict(name="H2O", numb=2, molecule=2, stat=0, levels=5, mcstep=0.05, lamb=lam(MASSES["H2O"]),
+    types = [dict(name="H2O", numb=2, molecule=2, stat=0, levels=levels, mcstep=0.05, lamb=lam(MASSES["H2O"]),
                   fpot="none")]
     abc = (27.9, 14.5, 9.3)
     tau_rot = 1.0 / (T * nrotslices)

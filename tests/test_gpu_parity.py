@@ -218,11 +218,50 @@ def test_production_pass_schedules_the_reference_move_counts(case):
     for i, t in enumerate(w.types):
         assert tot[3 * i + 0] == 2 * t["numb"]
         assert tot[3 * i + 1] == 2 * t["numb"] * P
-        if t["molecule"] != 0:
+        if t["molecule"] != 0 and w.rotation:
             assert tot[3 * i + 2] == 2 * t["numb"] * P * w.nrotslices
     assert (acc <= tot).all()
     c, a, co, _ = s.get_state()
     assert np.isfinite(c).all() and np.isfinite(a).all()
     est = s.estimators()
     assert np.isfinite(est).all()
+    s.close()
+
+
+def test_vcord_at_grid_nodes():
+    """vcalc's one-sided differences jump across a grid node, so a node must
+    land in the cell the reference's divisions pick (vcord.f:88-91,
+    vcalc.f:21-23).  Each slice puts one pH2 bead where the body-frame
+    (r, theta, chi) of the rotor's identity frame is a node of the c1s grid
+    (r = rvmin + n rstep in bohr, theta = k dth, chi = m dch), computed as
+    the sampler computes it, so it lands within ulps of the node on either
+    side; the rotor-pH2 sums must equal the oracle's."""
+    w, d, _ = golden("c1s")
+    tb = w.tables
+    P, na = w.nslices, w.natoms
+    bo2ang = 0.529177249
+    rstep = (tb["rvmax"] - tb["rvmin"]) / (tb["rgrd"] - 1)
+    dth = 180.0 / (tb["thgrd"] - 1)
+    dch = float(tb["chi_fold_deg"]) / (tb["chgrd"] - 1)
+    rng = np.random.default_rng(17)
+    c = np.array(d["coords0"], copy=True)
+    roff = na - 1                       # the rotor is the last atom
+    nodes = []
+    for it in range(P):
+        n = int(rng.integers(2, tb["rgrd"] - 2))
+        k = int(rng.integers(1, tb["thgrd"] - 1))
+        m = int(rng.integers(0, tb["chgrd"] - 1))
+        rho = (tb["rvmin"] + n * rstep) * bo2ang
+        th, ch = np.radians(k * dth), np.radians(m * dch)
+        rc = c[:, roff * P + it]
+        c[:, 0 * P + it] = rc + rho * np.array([np.sin(th) * np.cos(ch), np.sin(th) * np.sin(ch), np.cos(th)])
+        nodes.append((n, k, m))
+    s = G.Sampler(w)
+    s.set_state(c, d["angles0"], w.pindex)
+    o = O.Oracle(w)
+    o.set_state(c, d["angles0"], w.pindex)
+    eul = np.zeros(3)
+    got = s.pot_rot_energy([roff] * P, list(range(P)), np.tile(eul, (P, 1)))
+    want = np.array([o.pot_rot_e3d(roff, eul, it) for it in range(P)])
+    _close(got, want)
     s.close()
