@@ -39,6 +39,9 @@ for p in (PKG, os.path.join(REPO, "oracle")):
         sys.path.insert(0, p)
 
 METRIC = "bead-moves/s on 1 GB300: plain vs surrogate+batched, at matched <E> error"
+# DRAM traffic per launch from ncu captures of the bench's own workload:
+# {(kind, mixed): {"bytes": ..., "commit": ...}}, kind 2 = the rotational sweeps
+TRAFFIC_CAPTURE = {}
 UNIT = "bead-moves/s"
 WORKLOAD = "config1: 1 asymmetric-top SO2 + 64 pH2, T=0.37 K, P=1024, Q=256, L=3, plain method"
 
@@ -243,6 +246,27 @@ def centroid_pass_bytes(w, mixed):
     return w.natoms * 2 * w.nslices * (w.natoms - 1) * pair_bytes(mixed)
 
 
+# FP64 operations per evaluation, counted in the reference's source (an add,
+# multiply, divide, square root or transcendental call counts one; the
+# library calls' own instructions are not counted): vcord + vcalc
+# (vcord.f:1-98, vcalc.f:1-65) 53, including PotRotE3D's add; rotden's
+# deleul + rotpro (rotden.f:1-163, rotpro_sub.f:1-64) 80; the Metropolis
+# ratio and test of MCRot3Dstep (mc_piqmc.cc:1129-1178) 12.
+FLOP_VCORD, FLOP_ROTDEN, FLOP_ACCEPT = 53, 80, 12
+
+
+def rotation_pass_flops(w):
+    """Useful FP64 operations of the P rotational sweeps of one pass of a
+    nonlinear rotor: per slice move and rotor 2 R (N - 1) vcord terms (old
+    and new orientation, as the reference evaluates them), 4 rotden lookups
+    and the accept."""
+    P, Q = w.nslices, w.nrotslices
+    R = P // Q
+    nr = sum(t["numb"] for t in w.types if t["molecule"] != 0)
+    per = 2 * R * (w.natoms - 1) * FLOP_VCORD + 4 * FLOP_ROTDEN + FLOP_ACCEPT
+    return P * Q * nr * per
+
+
 def timed_passes(s, seed, steps, flush, ext, dist):
     """K passes, each bracketed by CUDA events on the library's stream, with
     an L2 flush (256 MiB write) before each outside the events; returns the
@@ -334,16 +358,22 @@ def run_gb300(args, rank, local, world, dist):
     per_launch_ms = ms[dom] / max(1, nl[dom])
     achieved = bytes_launch / (per_launch_ms / 1e3) / 1e9
     peak, peak_kind = measured_peaks()
-    # DRAM bytes per launch of the same kernel and launch shape from one ncu
-    # capture (dram__bytes_read.sum + dram__bytes_write.sum; the capture's
-    # summary is profiles/k_rot_slices_config1_fp64.md): far below the
-    # algorithmic bytes, the tables stay in L2/L1 and the FP64 pipe binds
-    traffic = 6.11e6 + 0.06e6 if (dom == 2 and not mixed) else None
+    # DRAM bytes per launch of the same kernel, workload and launch shape from
+    # one ncu capture (dram__bytes_read.sum + dram__bytes_write.sum), taken at
+    # the commit named beside it; None for a kernel or precision not captured
+    traffic = TRAFFIC_CAPTURE.get((dom, mixed))
+    fp64_peak = G.fp64_peak(local)
+    fp64_rate = rotation_pass_flops(w) / (ms[2] / 1e3) / 1e9 if ms[2] > 0 else None
     roofline = {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 5), "traffic": traffic,
-                "traffic_source": "ncu capture (profiles/k_rot_slices_config1_fp64.md)" if traffic else None,
-                "binding_limit": "FP64 pipe (ncu: sm__pipe_fp64_cycles_active 54.7 % of peak)" if traffic else None,
-                "fp64_pipe_active_frac": 0.547 if traffic else None,
+                "frac": round(achieved / peak, 5), "traffic": traffic["bytes"] if traffic else None,
+                "traffic_source": ("ncu capture of this kernel and workload at commit %s" % traffic["commit"])
+                if traffic else None,
+                "fp64": {"kernel": knames[2], "useful_gflops": round(fp64_rate, 2) if fp64_rate else None,
+                         "peak_gflops": round(fp64_peak, 1), "peak_source": "measured in this run (pimc_fp64_peak: "
+                         "independent FP64 FMA chains, CUDA events)",
+                         "fp64_frac": round(fp64_rate / fp64_peak, 4) if fp64_rate else None,
+                         "flop_model": "per slice move 2R(N-1) vcord x %d + 4 rotden x %d + %d (reference source "
+                                       "operations)" % (FLOP_VCORD, FLOP_ROTDEN, FLOP_ACCEPT)},
                 "kernel": kname, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
                 "per_launch_us": round(per_launch_ms * 1e3, 3), "algorithmic_bytes_per_launch": int(bytes_launch),
                 "pass_ms_by_kind": {k: round(v, 3) for k, v in zip(kinds, ms)},
@@ -732,14 +762,27 @@ def run_matched_se(local, quick=False, c4_replicas=512, c4_passes=24, c3_replica
     ts = np.array(single_pass_ms(ws, idx, 5))
     plain_ms = float(ts.mean()) * len(ws)
     plain_ms_se = float(ts.std(ddof=1) / np.sqrt(len(ts))) * len(ws) if len(ts) > 1 else None
-    arms = {}
+    arms, series = {}, {}
     for mixed in (False, True):
         b = G.Batch(ws, mixed=mixed)
         E, ms = batch_series(b, 8 if quick else c4_passes, 21, 2 if quick else 4)
         st, var = series_stats(E)
-        arms["batched_" + ("fp32" if mixed else "fp64")] = dict(g=st["g"], var=var, pass_ms=ms, stats=st)
+        name = "batched_" + ("fp32" if mixed else "fp64")
+        arms[name] = dict(g=st["g"], var=var, pass_ms=ms, stats=st)
+        series[name] = E
         b.close()
     f64 = arms["batched_fp64"]
+    # the FP32 path's error against the FP64 path, replica by replica: the
+    # difference of the two <E> over its standard error (each from its own
+    # series, g-corrected)
+    e32, e64 = series["batched_fp32"], series["batched_fp64"]
+    se = np.sqrt(arms["batched_fp32"]["g"] * e32.var(axis=0, ddof=1) / len(e32) +
+                 f64["g"] * e64.var(axis=0, ddof=1) / len(e64))
+    z = (e32.mean(axis=0) - e64.mean(axis=0)) / np.maximum(se, 1e-300)
+    fp32_error = {"what": "per replica (<E>_fp32 - <E>_fp64) / combined SE over the series",
+                  "replicas": int(len(z)), "frac_within_2se": round(float(np.mean(np.abs(z) <= 2.0)), 4),
+                  "median_abs_z": round(float(np.median(np.abs(z))), 3),
+                  "mean_abs_diff_K": round(float(np.mean(np.abs(e32.mean(axis=0) - e64.mean(axis=0)))), 4)}
     out["config4"] = {
         "workload": "config4: %d replicas of 1-8 water tops (caleng) on a 3 A chain + 0-32 pH2 (vcord), "
                     "T 0.5-2.0 K, P 512-2048, Q=P/4, ROTDENSI 1" % len(ws),
@@ -749,7 +792,8 @@ def run_matched_se(local, quick=False, c4_replicas=512, c4_passes=24, c3_replica
                   "timed_replicas": int(len(idx)), "precision": "fp64", "g": f64["g"]},
         "arms": {n: {"bead_moves_per_s": round(bm / (a["pass_ms"] / 1e3), 1), "pass_ms": round(a["pass_ms"], 2),
                      **a["stats"]} for n, a in arms.items()},
-        "time_to_se": matched(plain_ms, f64["g"], f64["var"], arms)}
+        "time_to_se": matched(plain_ms, f64["g"], f64["var"], arms),
+        "fp32_vs_fp64": fp32_error}
     # ---------------- water dimers with the surrogate
     dims = [W.config3(seed=300 + r, nslices=512, nrotslices=256, levels=4) for r in range(c3_replicas)]
     bmd = sum(w.bead_moves_per_pass() for w in dims)
@@ -976,6 +1020,8 @@ def main():
             line["worm"] = run_worm(local, not args.no_cpu, replicas=args.worm_replicas)
         if not args.no_surrogate and world == 1:
             line["surrogate"] = run_surrogate(local, replicas=args.da_replicas)
+        if not args.no_matched_se and world == 1:
+            line["matched_se"] = run_matched_se(local, quick=args.quick_se)
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.barrier()

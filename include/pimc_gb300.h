@@ -214,6 +214,11 @@ pimc_status pimc_save_sum_energy(const pimc_system *sys, const char *fname, doub
  * top level is used), values used (2^d). */
 pimc_status pimc_blocking_se(const double *x, long n, double *out);
 
+/* The FP64 rate the part sustains on independent fused multiply-adds
+ * (GFLOP/s, an FMA counted as two), measured with CUDA events on `device`:
+ * the denominator of the FP64 roofline fractions.  No reference counterpart. */
+pimc_status pimc_fp64_peak(int device, double *gflops);
+
 /* ---- worm algorithm (mc_qworm.cc) ------------------------------------------ */
 
 /* MCWormInit (mc_qworm.cc:49-82) for the atom type `type` with the WORM

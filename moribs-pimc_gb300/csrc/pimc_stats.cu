@@ -80,3 +80,50 @@ extern "C" pimc_status pimc_blocking_se(const double *x, long n, double *out)
   out[7] = (double)n2;
   return PIMC_OK;
 }
+
+// ---- the FP64 roofline denominator: a dependent-FMA throughput kernel.
+// Eight independent chains per thread keep the FP64 pipe's latency hidden;
+// every thread's result is stored so that nothing is eliminated.
+namespace {
+__global__ void __launch_bounds__(256) k_fp64_fma(double *out, int iters, double a, double b)
+{
+  double x[8];
+  for (int k = 0; k < 8; k++) x[k] = 1.0 + 1e-3 * (double)(threadIdx.x + k);
+  for (int i = 0; i < iters; i++)
+#pragma unroll
+    for (int k = 0; k < 8; k++) x[k] = fma(x[k], a, b);
+  double s = 0.0;
+  for (int k = 0; k < 8; k++) s += x[k];
+  out[(size_t)blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+}  // namespace
+
+extern "C" pimc_status pimc_fp64_peak(int device, double *gflops)
+{
+  if (!gflops) return PIMC_ERR_BAD_ARG;
+  if (cudaSetDevice(device) != cudaSuccess) return PIMC_ERR_NO_DEVICE;
+  int nsm = 0;
+  if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return PIMC_ERR_CUDA;
+  const int blocks = nsm * 8, threads = 256, iters = 8192;
+  double *out = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  pimc_status st = PIMC_OK;
+  float ms = 0.0f;
+  if (cudaMalloc(&out, (size_t)blocks * threads * sizeof(double)) != cudaSuccess) return PIMC_ERR_CUDA;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) { st = PIMC_ERR_CUDA; goto done; }
+  k_fp64_fma<<<blocks, threads>>>(out, iters / 8, 0.9999999, 1e-7);       // warm-up
+  cudaEventRecord(e0);
+  k_fp64_fma<<<blocks, threads>>>(out, iters, 0.9999999, 1e-7);
+  cudaEventRecord(e1);
+  if (cudaEventSynchronize(e1) != cudaSuccess || cudaGetLastError() != cudaSuccess ||
+      cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess || ms <= 0.0f) {
+    st = PIMC_ERR_CUDA;
+    goto done;
+  }
+  *gflops = 2.0 * 8.0 * (double)iters * (double)blocks * (double)threads / ((double)ms * 1e-3) / 1e9;
+done:
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaFree(out);
+  return st;
+}

@@ -4,13 +4,14 @@
 // type an open or close try, then an advance or recede try, then (bosons) a
 // swap try, each depending on the last.  One CTA runs the whole call: thread
 // 0 draws the random numbers in the reference's order and takes every
-// decision, the Gaussian bridges (sample_middle, mc_qworm.cc:238-283) are
-// built on thread 0 in the reference's recursion order, and the potential
-// sums over a segment -- the slices of get_potential (mc_qworm.cc:402-422)
-// or the new/old pairs of the swap (mc_qworm.cc:470-486) -- run one warp
-// per slice over the partners, with the partner beads that lie in the
-// worm's gap left out as PotEnergy leaves them out (WorldLine,
-// mc_qworm.cc:553-575; mc_piqmc.cc:1816-1817).
+// decision; the Gaussian bridges (sample_middle, mc_qworm.cc:238-283) are
+// built level by level by the whole CTA, each bead placed by its index in
+// the reference's recursion order; and the potential sums over a segment --
+// the slices of get_potential (mc_qworm.cc:402-422) or the new/old pairs of
+// the swap (mc_qworm.cc:470-486) -- spread their (slice, partner) terms over
+// the CTA, with the partner beads that lie in the worm's gap left out as
+// PotEnergy leaves them out (WorldLine, mc_qworm.cc:553-575;
+// mc_piqmc.cc:1816-1817).
 #include "pimc_kernels.cuh"
 #include "pimc_launch.h"
 

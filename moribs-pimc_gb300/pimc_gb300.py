@@ -89,6 +89,7 @@ def load(path=LIBPATH):
     L.pimc_energy_accumulate.argtypes = [sp, _dp, _dp]
     L.pimc_save_energy.argtypes = [sp, cc, C.c_double, C.c_long, _dp]
     L.pimc_blocking_se.argtypes = [_dp, C.c_long, _dp]
+    L.pimc_fp64_peak.argtypes = [C.c_int, _dp]
     L.pimc_save_sum_energy.argtypes = [sp, cc, C.c_double, C.c_double, _dp, C.c_int]
     L.pimc_asymrho.argtypes = [C.c_int, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, _dp, C.c_int,
                                _dp, _dp, _dp, _dp]
@@ -504,6 +505,13 @@ def blocking_se(x):
     _chk(load().pimc_blocking_se(dptr(x), len(x), dptr(out)), "pimc_blocking_se")
     return {"mean": out[0], "sd": out[1], "se_naive": out[2], "se": out[3], "g": out[4],
             "block": int(out[5]), "converged": bool(out[6]), "n": int(out[7])}
+
+
+def fp64_peak(device=0):
+    """pimc_fp64_peak: the measured FP64 FMA rate in GFLOP/s."""
+    g = np.zeros(1)
+    _chk(load().pimc_fp64_peak(int(device), dptr(g)), "pimc_fp64_peak")
+    return float(g[0])
 
 
 def linden(temperatures, nslices, bconst, npt, iodevn=-1, device=0):

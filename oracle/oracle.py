@@ -434,6 +434,7 @@ class Reference:
         L.ref_energy_block.argtypes = [C.c_char_p, C.c_char_p, C.c_long, _dp]
         L.ref_sum_energy.argtypes = [C.c_char_p, C.c_double, _dp]
         L.ref_rel_euler.argtypes = [C.c_char_p, C.c_double, _dp, _dp, _dp]
+        L.ref_write_xyz.argtypes = [C.c_char_p]
         L.ref_tau.restype = C.c_double
         L.ref_lambda.restype = C.c_double
         L.ref_lambda.argtypes = [C.c_int]

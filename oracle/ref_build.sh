@@ -8,9 +8,10 @@
 #                  call its block averages and energy writers, not its loop,
 #   mc_randg.cc -- SPRNG streams, replaced by the replay generators in the shim,
 #   omprng.cc   -- runif()/randomseed(), replaced by the shim.
-# Usage: oracle/ref_build.sh [reference_dir]   (default: /root/reference)
+# Usage: oracle/ref_build.sh [reference_dir]
+#   (default: $PIMC_REFERENCE_DIR, else the reference tree of the build container)
 set -e
-REF=${1:-/root/reference}
+REF=${1:-${PIMC_REFERENCE_DIR:-/root/reference}}
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
 if [ ! -f "$REF/mc_piqmc.cc" ]; then

@@ -505,3 +505,9 @@ void ref_rcf_save(const char *fname, double acount, int mode, double *rcf)
 }
 
 }  // extern "C"
+
+// IOxyz (mc_input.cc:690-794) writing the current path to `file`
+extern "C" void ref_write_xyz(const char *file)
+{
+  IOxyz(IOWrite, file);
+}

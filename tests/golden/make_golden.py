@@ -159,6 +159,11 @@ def generate(case, nsteps=4, seed=2024):
         streams["urot"].append(ur)
     c, a, co = ref.get_state()
     tot, acc = ref.counters()
+    # IOxyz's file of the final path (mc_input.cc:690-794), as text
+    xyzf = os.path.join(ref.tmp, "final.xyz")
+    ref.L.ref_write_xyz(xyzf.encode())
+    with open(xyzf) as f:
+        res["xyz_text"] = np.array(f.read())
     res.update(seq=np.array(seq, dtype=np.int32), consumed=np.array(consumed, dtype=np.int64),
                coords1=c, angles1=a, cosine1=co, total=tot, accep=acc)
     for name, lst in streams.items():

@@ -12,8 +12,8 @@ outputs the reference ships (read as text, written by its own generators):
     seeded subset of 4000 of its 361*361 points, and the "AT BETA" / "AT
     TAU" partition-function lines and the j <= 2 eigenvalues of nmv_prop/log.
 
-Usage (here, where the reference tree exists):
-    python tests/golden/make_tables_golden.py
+Usage (where the reference tree exists):
+    python tests/golden/make_tables_golden.py REFERENCE_DIR
 """
 import os
 import re
@@ -22,7 +22,10 @@ import sys
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+# the reference tree: the first argument, else PIMC_REFERENCE_DIR
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PIMC_REFERENCE_DIR", "")
+if not REF or not os.path.isdir(REF):
+    sys.exit("usage: make_tables_golden.py REFERENCE_DIR (or set PIMC_REFERENCE_DIR)")
 
 
 def main():

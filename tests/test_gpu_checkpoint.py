@@ -56,3 +56,20 @@ def test_xyz_round_trip(tmp_path):
     rot = slice((w.natoms - 1) * w.nslices, (w.natoms - 1) * w.nslices + w.nrotslices)
     np.testing.assert_allclose(co2[:, rot], co[:, rot], rtol=0, atol=1e-14)
     a.close(); b.close()
+
+
+@pytest.mark.parametrize("name", ["c0s", "c1s", "c3s"])
+def test_xyz_equals_the_reference_file(name, tmp_path):
+    """pimc_write_xyz of a fixture's final path equals, byte for byte, the
+    file the reference's IOxyz (mc_input.cc:690-794) wrote for the same path
+    (fixture xyz_text; labels are the MCAtom type names)."""
+    from _common import golden
+    w, d, _ = golden(name)
+    s = G.Sampler(w)
+    s.set_state(d["coords1"], d["angles1"], w.pindex)
+    s.write_xyz(tmp_path / "f.xyz", [t["name"] for t in w.types])
+    got = (tmp_path / "f.xyz").read_text()
+    want = str(d["xyz_text"])
+    assert got == want, next((i, a, b) for i, (a, b) in enumerate(zip(got.splitlines(), want.splitlines()))
+                             if a != b)
+    s.close()

@@ -229,13 +229,15 @@ def test_production_pass_schedules_the_reference_move_counts(case):
 
 
 def test_vcord_at_grid_nodes():
-    """vcalc's one-sided differences jump across a grid node, so a node must
-    land in the cell the reference's divisions pick (vcord.f:88-91,
-    vcalc.f:21-23).  Each slice puts one pH2 bead where the body-frame
-    (r, theta, chi) of the rotor's identity frame is a node of the c1s grid
-    (r = rvmin + n rstep in bohr, theta = k dth, chi = m dch), computed as
-    the sampler computes it, so it lands within ulps of the node on either
-    side; the rotor-pH2 sums must equal the oracle's."""
+    """vcalc's one-sided differences jump across a grid node (vcalc.f:31-60),
+    so at a node the reference's value depends on the last bit of acos/atan
+    (CUDA's and glibc's may differ by an ulp) and of the divisions by the
+    steps (vcord.f:88-91, vcalc.f:21-23), which the GPU repeats there.  Each
+    slice puts one pH2 bead where the body-frame (r, theta, chi) of the
+    rotor's identity frame is a node of the c1s grid (r = rvmin + n rstep in
+    bohr, theta = k dth, chi = m dch); the GPU's rotor-pH2 sum must equal the
+    oracle's on one of the two sides of the node in each coordinate (the
+    node approached from r, theta, chi -/+ 1e-12), to 1e-10."""
     w, d, _ = golden("c1s")
     tb = w.tables
     P, na = w.nslices, w.natoms
@@ -244,24 +246,38 @@ def test_vcord_at_grid_nodes():
     dth = 180.0 / (tb["thgrd"] - 1)
     dch = float(tb["chi_fold_deg"]) / (tb["chgrd"] - 1)
     rng = np.random.default_rng(17)
-    c = np.array(d["coords0"], copy=True)
     roff = na - 1                       # the rotor is the last atom
     nodes = []
     for it in range(P):
         n = int(rng.integers(2, tb["rgrd"] - 2))
         k = int(rng.integers(1, tb["thgrd"] - 1))
-        m = int(rng.integers(0, tb["chgrd"] - 1))
-        rho = (tb["rvmin"] + n * rstep) * bo2ang
-        th, ch = np.radians(k * dth), np.radians(m * dch)
-        rc = c[:, roff * P + it]
-        c[:, 0 * P + it] = rc + rho * np.array([np.sin(th) * np.cos(ch), np.sin(th) * np.sin(ch), np.cos(th)])
-        nodes.append((n, k, m))
-    s = G.Sampler(w)
-    s.set_state(c, d["angles0"], w.pindex)
-    o = O.Oracle(w)
-    o.set_state(c, d["angles0"], w.pindex)
+        m = int(rng.integers(1, tb["chgrd"] - 1))
+        nodes.append(((tb["rvmin"] + n * rstep) * bo2ang, np.radians(k * dth), np.radians(m * dch)))
+
+    def place(dr, dt, dc):
+        c = np.array(d["coords0"], copy=True)
+        for it, (rho, th, ch) in enumerate(nodes):
+            rho, th, ch = rho + dr, th + dt, ch + dc
+            rc = c[:, roff * P + it]
+            c[:, it] = rc + rho * np.array([np.sin(th) * np.cos(ch), np.sin(th) * np.sin(ch), np.cos(th)])
+        return c
     eul = np.zeros(3)
+    s = G.Sampler(w)
+    s.set_state(place(0.0, 0.0, 0.0), d["angles0"], w.pindex)
     got = s.pot_rot_energy([roff] * P, list(range(P)), np.tile(eul, (P, 1)))
-    want = np.array([o.pot_rot_e3d(roff, eul, it) for it in range(P)])
-    _close(got, want)
     s.close()
+    o = O.Oracle(w)
+    sides = []
+    eps = 1e-12
+    for dr in (-eps, eps):
+        for dt in (-eps, eps):
+            for dc in (-eps, eps):
+                o.set_state(place(dr, dt, dc), d["angles0"], w.pindex)
+                sides.append([o.pot_rot_e3d(roff, eul, it) for it in range(P)])
+    sides = np.array(sides)                                   # [8, P]
+    err = np.min(np.abs(sides - got[None, :]), axis=0) / np.maximum(np.abs(sides).max(axis=0), 1.0)
+    assert np.all(err <= 1e-10), (err, got, sides)
+    # the nodes are real discontinuities: somewhere the two sides differ
+    assert np.max(np.ptp(sides, axis=0)) > 1e-6
+
+

@@ -1,9 +1,22 @@
 """Full runs against the oracle: the GPU's production passes (checkerboard
 slices, independent sets, Philox draws) and the oracle's restatement of the
 reference schedule (serial slices, its own draws) sample the same
-distribution, so their estimators agree within the combined standard error
+distribution, so their estimators agree within two combined standard errors
 of block means (mc_estim.cc:500-1096 estimators, sampled once per pass as
-mc_main.cc:551-616 does)."""
+mc_main.cc:551-616 does), in both precisions of the GPU path.
+
+Systems (reduced slices and particle counts, so that the serial oracle
+finishes in seconds): the config-0 shape (linear rotor + 4 He, P = 64,
+Q = 16), the config-1 shape (asymmetric top + 6 pH2, P = 64, Q = 16, 3D
+rotor-pH2 table and top density of the c1s fixture grids) and the config-3
+shape (water dimer, caleng, P = 64, Q = 32).  Seeds are fixed, and the GPU
+passes and the oracle are both deterministic, so the test is reproducible.
+
+Estimators: E_kin, E_pot, E_rot and the orientational correlation
+<cos gamma(beta/2)> of GetRCF between rotational slices half a period apart
+(mc_estim.cc:1099-1139); the lab-frame <cos theta> relaxes from the initial
+orientation over far more passes than a run has (no field), so the rotor's
+orientation enters through the correlation."""
 import numpy as np
 import pytest
 
@@ -14,6 +27,14 @@ import workloads as W
 pytestmark = pytest.mark.gpu
 
 NAMES = ("E_kin", "E_pot", "E_rot", "<cos gamma(beta/2)>")
+SYSTEMS = {
+    "config0": lambda: W.config0(seed=5, nslices=64, nrotslices=16, n_he=4),
+    "config1": lambda: W.config1(seed=6, nslices=64, nrotslices=16, n_h2=6, grid3d=(30, 37, 19),
+                                 griddens=(19, 37, 37)),
+    "config3": lambda: W.config3(seed=7, nslices=64, nrotslices=32, griddens=(19, 37, 37), levels=3),
+}
+NB, PER, EQUIL = 40, 50, 500
+_oracle_cache = {}
 
 
 def _blocks(sample, nblocks, per):
@@ -25,28 +46,12 @@ def _blocks(sample, nblocks, per):
     return out
 
 
-def test_production_runs_agree_with_the_oracle_within_standard_errors():
-    """Config 0 shape at a small size (linear rotor + 4 He, P = 64, Q = 16):
-    500 equilibration passes, then 40 blocks of 50 passes on each side.
-    The acceptance bound is 3 combined standard errors per estimator (four
-    estimators are tested at once; 2 would fail by chance in about one run
-    of six)."""
-    w = W.config0(seed=5, nslices=64, nrotslices=16, n_he=4)
-    nb, per, equil = 40, 50, 500
-    # the orientational estimator: GetRCF's <cos gamma> between the rotor's
-    # axis at two slices half a period apart, averaged over the time origins
-    # (mc_estim.cc:1099-1139 sums over the Q origins).  The
-    # lab-frame <cos theta> is no test here: with no field it relaxes from the
-    # initial orientation over far more passes than the run has.
+def _oracle_blocks(name):
+    if name in _oracle_cache:
+        return _oracle_cache[name]
+    w = SYSTEMS[name]()
     half = w.nrotslices // 2
-    s = G.Sampler(w)
-    s.run_passes(equil, seed=11)
-
-    def gpu():
-        s.run_passes(1, seed=11)
-        return np.append(s.estimators()[:3], s.rcf()[half] / w.nrotslices)
-    g = _blocks(gpu, nb, per)
-    s.close()
+    nonlinear = any(t["molecule"] == 2 for t in w.types)
     o = O.Oracle(w)
     state = {"p": 0}
 
@@ -54,17 +59,34 @@ def test_production_runs_agree_with_the_oracle_within_standard_errors():
         st, _ = o.run_steps(0, w.nslices, seed=70000 + state["p"])
         assert st == 0
         state["p"] += 1
-    for _ in range(equil):
+    for _ in range(EQUIL):
         step()
 
     def cpu():
         step()
-        return np.array([o.kin_energy(), o.pot_energy_est(), o.rot_energy(False)[0], o.rcf()[half] / w.nrotslices])
-    c = _blocks(cpu, nb, per)
+        return np.array([o.kin_energy(), o.pot_energy_est(), o.rot_energy(nonlinear)[0], o.rcf()[half] / w.nrotslices])
+    _oracle_cache[name] = _blocks(cpu, NB, PER)
+    return _oracle_cache[name]
+
+
+@pytest.mark.parametrize("mixed", [False, True])
+@pytest.mark.parametrize("name", list(SYSTEMS))
+def test_production_runs_agree_with_the_oracle_within_two_standard_errors(name, mixed):
+    w = SYSTEMS[name]()
+    half = w.nrotslices // 2
+    s = G.Sampler(w, mixed=mixed)
+    s.run_passes(EQUIL, seed=11)
+
+    def gpu():
+        s.run_passes(1, seed=11)
+        return np.append(s.estimators()[:3], s.rcf()[half] / w.nrotslices)
+    g = _blocks(gpu, NB, PER)
+    s.close()
+    c = _oracle_blocks(name)
     mg, mc = g.mean(0), c.mean(0)
-    se = np.hypot(g.std(0, ddof=1), c.std(0, ddof=1)) / np.sqrt(nb)
+    se = np.hypot(g.std(0, ddof=1), c.std(0, ddof=1)) / np.sqrt(NB)
     z = (mg - mc) / se
-    report = {n: (round(a, 4), round(b, 4), round(e, 4), round(zz, 2)) for n, a, b, e, zz in zip(NAMES, mg, mc, se, z)}
-    print("block means (GPU, oracle, combined SE, z):", report)
+    report = {n: (round(a, 5), round(b, 5), round(e, 5), round(zz, 2)) for n, a, b, e, zz in zip(NAMES, mg, mc, se, z)}
+    print("%s %s block means (GPU, oracle, combined SE, z):" % (name, "fp32" if mixed else "fp64"), report)
     assert np.all(np.isfinite(z)), report
-    assert np.all(np.abs(z) <= 3.0), report
+    assert np.all(np.abs(z) <= 2.0), report

@@ -64,3 +64,25 @@ def test_noalloc_rejects_more_queries_than_the_array_holds():
     out = np.zeros(n)
     assert noalloc(s.h, n, G.iptr(a0), G.iptr(it), G.dptr(xyz), G.dptr(out)) == 8   # PIMC_ERR_SIZE
     s.close()
+
+
+def test_noalloc_matches_the_reference_fixture():
+    """The same entry point on the reference's own PotEnergy(atom, pos, it)
+    values of the c1s fixture (initial and displaced beads), 1e-10."""
+    w, d, _ = golden("c1s")
+    s = G.Sampler(w)
+    s.set_state(d["coords0"], d["angles0"], w.pindex)
+    noalloc, _ = _bind(s.L)
+    P = w.nslices
+    a0, it, xyz, ref = [], [], [], []
+    for a in range(w.natoms):
+        for j, t in enumerate(d["slices"]):
+            for k, arr in enumerate((d["coords0"], d["pos"])):
+                a0.append(a); it.append(int(t)); xyz.append(arr[:, a * P + t]); ref.append(d["e_slice"][a, j, k])
+    a0 = np.array(a0, np.int32); it = np.array(it, np.int32)
+    xyz = np.ascontiguousarray(np.array(xyz), dtype=np.float64)
+    ref = np.array(ref)
+    got = np.full(len(ref), np.nan)
+    assert noalloc(s.h, len(ref), G.iptr(a0), G.iptr(it), G.dptr(xyz), G.dptr(got)) == 0
+    np.testing.assert_allclose(got, ref, rtol=1e-10, atol=1e-12)
+    s.close()
