@@ -116,11 +116,11 @@ def host_cpu():
 
 
 def cpu_baseline(w, seconds, nthreads):
-    """The oracle restatement of the reference schedule on the host cores:
-    time slices 0, 1, ... (centroid moves at slice 0) until `seconds` pass."""
+    """The oracle restatement of the reference schedule on the host cores, in
+    its timing build (the reference's -Ofast -march=native flags): time
+    slices 0, 1, ... (centroid moves at slice 0) until `seconds` pass."""
     import oracle as O
-    O.build_oracle()
-    o = O.Oracle(w)
+    o = O.Oracle(w, timing=True)
     done_t = 0
     bm = 0.0
     t0 = time.perf_counter()
@@ -135,8 +135,9 @@ def cpu_baseline(w, seconds, nthreads):
         if el >= seconds or done_t >= w.nslices:
             break
     rate = bm / el
-    sample = ("oracle port of the reference schedule, time slices 0..%d of one pass of %s "
-              "(%.3g bead-moves, %.1f s)" % (done_t - 1, WORKLOAD.split(":")[0], bm, el))
+    sample = ("oracle port of the reference schedule (%s), time slices 0..%d of one pass of %s "
+              "(%.3g bead-moves, %.1f s, %d threads)" % (O.timing_flags(), done_t - 1, WORKLOAD.split(":")[0], bm,
+                                                          el, nthreads))
     return rate, sample
 
 
@@ -1012,8 +1013,10 @@ def main():
     if rank == 0:
         if not args.no_cpu:
             rate, sample = cpu_baseline(w, args.cpu_seconds, ncores)
+            rate1, sample1 = cpu_baseline(w, args.cpu_seconds / 2, 1)
             line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": ncores, "kind": "port", "sample": sample,
-                                    "host_cpu": host_cpu()}
+                                    "host_cpu": host_cpu(),
+                                    "one_thread": {"value": rate1, "cores": 1, "sample": sample1}}
         if not args.no_tables and world == 1:
             line["tables"] = run_tables(local, not args.no_cpu)
         if not args.no_worm and world == 1:

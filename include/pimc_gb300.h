@@ -357,6 +357,8 @@ pimc_status pimc_set_precision(pimc_handle *h, int mixed);
  * Values 0 .. 6e10. */
 #define PIMC_OPT_WAIT_NS 3
 pimc_status pimc_set_option(pimc_handle *h, int option, long long value);
+/* MCAtom[type].numb and .levels (mc_setup.h:66-93) of the handle's system */
+pimc_status pimc_type_info(const pimc_handle *h, int type, int *numb, int *levels);
 /* scheduled bead-moves per pass: per type N*P*(2^L-1) + N*P, plus P*Q per rotor */
 double      pimc_bead_moves_per_pass(const pimc_handle *h);
 /* kernels launched on the handle's stream so far */

@@ -1733,6 +1733,14 @@ extern "C" pimc_status pimc_set_precision(pimc_handle *h, int mixed)
   return PIMC_OK;
 }
 
+extern "C" pimc_status pimc_type_info(const pimc_handle *h, int type, int *numb, int *levels)
+{
+  if (!h || !numb || !levels || type < 0 || type >= h->ctx.s.ntypes) return PIMC_ERR_BAD_ARG;
+  *numb = h->ctx.s.numb[type];
+  *levels = h->ctx.s.levels[type];
+  return PIMC_OK;
+}
+
 extern "C" double pimc_bead_moves_per_pass(const pimc_handle *h)
 {
   if (!h) return 0.0;

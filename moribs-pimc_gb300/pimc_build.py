@@ -39,6 +39,7 @@ def build(verbose=False, extra=()):
     deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [os.path.join(HERE, "..", "include", f)
                                                                  for f in ("pimc_gb300.h", "pimc_types.h")]
     if _newer(OUT, deps + [os.path.abspath(__file__)]) and not extra:
+        build_shim(verbose)
         return OUT
     objs = []
 
@@ -57,7 +58,27 @@ def build(verbose=False, extra=()):
     if verbose:
         print(" ".join(cmd))
     subprocess.check_call(cmd)
+    build_shim(verbose)
     return OUT
+
+
+SHIM_OUT = os.path.join(HERE, "libpimc_shim.so")
+
+
+def build_shim(verbose=False):
+    """The look-ahead core of the reference-name shim (shim/pimc_shim_core.cc)
+    as libpimc_shim.so, linked against libpimc_gb300.so beside it.  The
+    reference-facing part (shim/pimc_gpu_shim.cc) is compiled into the
+    reference's own program, with the reference's headers."""
+    src = os.path.join(HERE, "shim", "pimc_shim_core.cc")
+    if _newer(SHIM_OUT, [src, os.path.join(HERE, "shim", "pimc_shim_core.h"), OUT]):
+        return SHIM_OUT
+    cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-shared", src, "-o", SHIM_OUT, "-L" + HERE, "-lpimc_gb300",
+           "-Wl,-rpath,$ORIGIN", "-Wl,--no-undefined"]
+    if verbose:
+        print(" ".join(cmd))
+    subprocess.check_call(cmd)
+    return SHIM_OUT
 
 
 if __name__ == "__main__":

@@ -44,6 +44,42 @@ def build_oracle(force=False):
     return LIB
 
 
+LIB_TIMING = os.path.join(HERE, "liboracle_timing.so")
+
+
+def build_oracle_timing(force=False):
+    """The same sources built for speed with the reference's own optimisation
+    flags (-Ofast -march=native -fopenmp, makefile.in:3) into
+    oracle/liboracle_timing.so: the CPU baseline's build.  Not a parity
+    build (fast-math reorders); where the compiler has no -march=native for
+    the host (some aarch64 gcc builds), -mcpu=native, then -O3."""
+    srcs = [os.path.join(HERE, f) for f in ("pimc_oracle.c", "orc_tables.c")]
+    deps = srcs + [os.path.join(HERE, "pimc_oracle.h")]
+    if not force and os.path.exists(LIB_TIMING) and all(os.path.getmtime(LIB_TIMING) >= os.path.getmtime(f)
+                                                        for f in deps):
+        return LIB_TIMING
+    tail = srcs + ["-o", LIB_TIMING, "-lm"]
+    if platform.machine() in ("x86_64", "AMD64", "i686"):
+        tail.append("-lquadmath")
+    last = None
+    for arch in (["-Ofast", "-march=native"], ["-Ofast", "-mcpu=native"], ["-O3"]):
+        cmd = ["gcc", "-std=gnu11", *arch, "-fopenmp", "-fPIC", "-shared"] + tail
+        r = subprocess.run(cmd, stdout=subprocess.DEVNULL, stderr=subprocess.PIPE, text=True)
+        if r.returncode == 0:
+            with open(LIB_TIMING + ".flags", "w") as f:
+                f.write(" ".join(arch) + " -fopenmp\n")
+            return LIB_TIMING
+        last = r.stderr
+    raise RuntimeError("timing build of the oracle failed: %s" % last)
+
+
+def timing_flags():
+    try:
+        return open(LIB_TIMING + ".flags").read().strip()
+    except OSError:
+        return None
+
+
 class Stream(C.Structure):
     _fields_ = [("v", _dp), ("n", C.c_long), ("pos", C.c_long)]
 
@@ -87,9 +123,12 @@ def make_replay(u1=None, u2=None, u3=None, gauss=None, urot=None):
     return rp, keep
 
 
-def _lib():
-    build_oracle()
-    lib = C.CDLL(LIB)
+def _lib(timing=False):
+    if timing:
+        build_oracle_timing()
+    else:
+        build_oracle()
+    lib = C.CDLL(LIB_TIMING if timing else LIB)
     lib.orc_create.restype = C.c_void_p
     lib.orc_create.argtypes = [C.POINTER(PimcSystem), C.POINTER(PimcTables), _ip]
     lib.orc_destroy.argtypes = [C.c_void_p]
@@ -164,14 +203,13 @@ def _lib():
     return lib
 
 
-_LIB = None
+_LIB = {}
 
 
-def lib():
-    global _LIB
-    if _LIB is None:
-        _LIB = _lib()
-    return _LIB
+def lib(timing=False):
+    if timing not in _LIB:
+        _LIB[timing] = _lib(timing)
+    return _LIB[timing]
 
 
 def _v3(x):
@@ -182,9 +220,9 @@ def _v3(x):
 class Oracle:
     """One oracle context over a Workload (owns copies of tables and state)."""
 
-    def __init__(self, w):
+    def __init__(self, w, timing=False):
         self.w = w
-        self.L = lib()
+        self.L = lib(timing)
         self.sys = make_system(w)
         tabs, keep = make_tables(w)
         st = C.c_int(0)
