@@ -733,6 +733,28 @@ def matched(plain_pass_ms, plain_g, plain_var, arms, c=0.05):
     return out
 
 
+def crossover(w, line):
+    """What a surrogate row must cost to pay in a delayed-acceptance screen
+    of the rotor-solvent terms: the time of one exact rotor-pH2 term as the
+    rotational kernels deliver it (the pass's rotation time over the
+    reference's 2 R (N - 1) terms per slice move), FP64 and FP32 path,
+    against the time of one surrogate row of the tensor-core forward kernel."""
+    P, Q = w.nslices, w.nrotslices
+    R = P // Q
+    nr = sum(t["numb"] for t in w.types if t["molecule"] != 0)
+    terms = P * Q * nr * 2 * R * (w.natoms - 1)
+    main_ms = line["roofline"]["pass_ms_by_kind"]["rotation"]
+    comp_ms = line["companion"]["pass_ms_by_kind"]["rotation"]
+    f64, f32 = (main_ms, comp_ms) if line["config"]["precision"] == "fp64" else (comp_ms, main_ms)
+    sr = line["surrogate"]["roofline"]
+    row_ns = sr["ms_per_launch"] * 1e6 / line["surrogate"]["mlp_inference"]["rows"]
+    t64, t32 = f64 * 1e6 / terms, f32 * 1e6 / terms
+    return {"exact_term_ns_fp64": round(t64, 5), "exact_term_ns_fp32": round(t32, 5),
+            "surrogate_row_ns": round(row_ns, 5), "row_over_fp64_term": round(row_ns / t64, 3),
+            "row_over_fp32_term": round(row_ns / t32, 3),
+            "what": "a screen spares exact terms only if a surrogate row costs less than the terms it replaces"}
+
+
 def run_matched_se(local, quick=False, c4_replicas=512, c4_passes=24, c3_replicas=64):
     """The metric itself: bead-moves/s at matched <E> standard error.
 
@@ -1025,6 +1047,8 @@ def main():
             line["surrogate"] = run_surrogate(local, replicas=args.da_replicas)
         if not args.no_matched_se and world == 1:
             line["matched_se"] = run_matched_se(local, quick=args.quick_se)
+        if "surrogate" in line and "companion" in line:
+            line["surrogate_crossover"] = crossover(w, line)
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.barrier()

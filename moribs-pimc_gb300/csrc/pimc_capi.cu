@@ -2533,16 +2533,20 @@ extern "C" pimc_status pimc_write_xyz(pimc_handle *h, const char *path, const ch
   if ((e = pimc_get_state(h, coords.data(), angles.data(), cosine.data(), nullptr))) return e;
   FILE *f = fopen(path, "w");
   if (!f) return PIMC_ERR_BAD_ARG;
-  fprintf(f, "%zu\n# xyz + unit vector\n", nbr);
+  // IOxyz's layout (mc_input.cc:726-750): the count, the comment line, then
+  // per bead the label (type name and atom number, width 5) and x, cx, y,
+  // cy, z, cz in io_setout's format (scientific, 6 digits, width 14), each
+  // field followed by three blanks (mc_confg.h:28-29, mc_input.h:48, 60)
+  fprintf(f, "%zu\n#   xyz format:  [atom type]  x y z (Angstrom) \n", nbr);
   for (int t = 0; t < d.ntypes; t++)
     for (int a = 0; a < d.numb[t]; a++) {
       char label[64];
       snprintf(label, sizeof(label), "%s%d", type_names && type_names[t] ? type_names[t] : (t ? "M" : "A"), a + 1);
       size_t off = (size_t)(d.first[t] + a) * d.P;
       for (int it = 0; it < d.P; it++) {
-        fprintf(f, "%5s ", label);
+        fprintf(f, "%5s   ", label);
         for (int k = 0; k < 3; k++)
-          fprintf(f, "%.17g %.17g ", coords[k * nbr + off + it], cosine[k * nbr + off + it]);
+          fprintf(f, "%14.6e   %14.6e   ", coords[k * nbr + off + it], cosine[k * nbr + off + it]);
         fprintf(f, "\n");
       }
     }
