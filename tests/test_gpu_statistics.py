@@ -1,92 +1,130 @@
 """Full runs against the oracle: the GPU's production passes (checkerboard
 slices, independent sets, Philox draws) and the oracle's restatement of the
 reference schedule (serial slices, its own draws) sample the same
-distribution, so their estimators agree within two combined standard errors
-of block means (mc_estim.cc:500-1096 estimators, sampled once per pass as
-mc_main.cc:551-616 does), in both precisions of the GPU path.
+distribution, so their estimators (mc_estim.cc:500-1139, sampled as
+mc_main.cc:551-616 samples them) agree within the combined standard error,
+in both precisions of the GPU path.
 
-Systems (reduced slices and particle counts, so that the serial oracle
-finishes in seconds): the config-0 shape (linear rotor + 4 He, P = 64,
-Q = 16), the config-1 shape (asymmetric top + 6 pH2, P = 64, Q = 16, 3D
-rotor-pH2 table and top density of the c1s fixture grids) and the config-3
-shape (water dimer, caleng, P = 64, Q = 32).  Seeds are fixed, and the GPU
-passes and the oracle are both deterministic, so the test is reproducible.
+Standard errors come from independent chains: 16 GPU chains and 16 oracle
+chains per system, each from the same start with its own seed, 400 passes of
+equilibration and then a sample every second pass for 1200 passes; the error
+of a mean is the spread of the 16 chain means over sqrt(16).  Independent
+chains carry no autocorrelation into the error, and a chain caught in a
+long-lived state widens the spread instead of hiding in it.
+
+Systems, chosen to mix within a chain's length (checked oracle against
+oracle with other seeds): the config-0 shape (CO2-like linear rotor + 4 He,
+0.37 K, P = 64, Q = 16); the config-1 shape (SO2-like top + 3 pH2, 2 K,
+P = 64, Q = 16, the 3D table and top density of the c1s grids); the
+config-3 shape (the caleng water dimer, 5 K, P = 64, Q = 32, bisection levels
+2, centroid step 0.02 A).  At the configs' own temperatures with more
+solvent the oracle's own chains move between cluster structures over
+thousands of passes, and the dimer's translations freeze at P = 64.
 
 Estimators: E_kin, E_pot, E_rot and the orientational correlation
 <cos gamma(beta/2)> of GetRCF between rotational slices half a period apart
-(mc_estim.cc:1099-1139); the lab-frame <cos theta> relaxes from the initial
-orientation over far more passes than a run has (no field), so the rotor's
-orientation enters through the correlation."""
+(mc_estim.cc:1099-1139).  The lab-frame <cos theta> is no equilibrium
+observable here (no field: it relaxes from the start over far more passes
+than a run has, and the two schedules relax at different rates).
+
+Criterion: each estimator within 2 combined standard errors.  With 24
+comparisons (3 systems x 2 precisions x 4 estimators) and 16-chain errors
+(t-distributed, 30 degrees of freedom), about 5 % of correct comparisons lie
+beyond 2; the test requires every |z| <= 3.5 and at most 4 of the 24 beyond 2
+(a binomial tail of 1 % for a correct sampler), and prints every z.  The
+seeds are fixed and both sides are deterministic, so a run is reproducible."""
+import multiprocessing as mp
+
 import numpy as np
 import pytest
 
-import oracle as O
 import pimc_gb300 as G
 import workloads as W
 
 pytestmark = pytest.mark.gpu
 
 NAMES = ("E_kin", "E_pot", "E_rot", "<cos gamma(beta/2)>")
-SYSTEMS = {
-    "config0": lambda: W.config0(seed=5, nslices=64, nrotslices=16, n_he=4),
-    "config1": lambda: W.config1(seed=6, nslices=64, nrotslices=16, n_h2=6, grid3d=(30, 37, 19),
-                                 griddens=(19, 37, 37)),
-    "config3": lambda: W.config3(seed=7, nslices=64, nrotslices=32, griddens=(19, 37, 37), levels=3),
-}
-NB, PER, EQUIL = 40, 50, 500
-_oracle_cache = {}
+K, EQUIL, NSAMP, EVERY = 16, 400, 600, 2
+_oracle = {}
+_results = {}
 
 
-def _blocks(sample, nblocks, per):
-    out = np.zeros((nblocks, len(NAMES)))
-    for b in range(nblocks):
-        for _ in range(per):
-            out[b] += sample()
-        out[b] /= per
-    return out
+def make(name):
+    if name == "config0":
+        return W.config0(seed=5, nslices=64, nrotslices=16, n_he=4)
+    if name == "config1":
+        w = W.config1(seed=6, nslices=64, nrotslices=16, n_h2=3, grid3d=(30, 37, 19), griddens=(19, 37, 37))
+        w.temperature = 2.0
+        return w
+    w = W.config3(seed=7, nslices=64, nrotslices=32, griddens=(19, 37, 37), levels=2)
+    w.types[0]["mcstep"] = 0.02
+    w.temperature = 5.0
+    return w
 
 
-def _oracle_blocks(name):
-    if name in _oracle_cache:
-        return _oracle_cache[name]
-    w = SYSTEMS[name]()
+def _oracle_chain(args):
+    name, seed = args
+    import oracle as O
+    w = make(name)
+    o = O.Oracle(w)
     half = w.nrotslices // 2
     nonlinear = any(t["molecule"] == 2 for t in w.types)
-    o = O.Oracle(w)
-    state = {"p": 0}
-
-    def step():
-        st, _ = o.run_steps(0, w.nslices, seed=70000 + state["p"])
-        assert st == 0
-        state["p"] += 1
+    p = 0
     for _ in range(EQUIL):
-        step()
+        o.run_steps(0, w.nslices, seed=seed + p)
+        p += 1
+    acc = np.zeros(4)
+    for _ in range(NSAMP):
+        for _ in range(EVERY):
+            st, _ = o.run_steps(0, w.nslices, seed=seed + p)
+            assert st == 0
+            p += 1
+        acc += [o.kin_energy(), o.pot_energy_est(), o.rot_energy(nonlinear)[0], o.rcf()[half] / w.nrotslices]
+    return acc / NSAMP
 
-    def cpu():
-        step()
-        return np.array([o.kin_energy(), o.pot_energy_est(), o.rot_energy(nonlinear)[0], o.rcf()[half] / w.nrotslices])
-    _oracle_cache[name] = _blocks(cpu, NB, PER)
-    return _oracle_cache[name]
+
+def _oracle_means(name):
+    if name not in _oracle:
+        with mp.get_context("spawn").Pool(min(K, mp.cpu_count())) as pool:
+            _oracle[name] = np.array(pool.map(_oracle_chain, [(name, 70001 * (k + 1)) for k in range(K)]))
+    return _oracle[name]
+
+
+def _gpu_means(name, mixed):
+    out = []
+    for k in range(K):
+        w = make(name)
+        half = w.nrotslices // 2
+        s = G.Sampler(w, mixed=mixed)
+        seed = 1000 + 37 * k
+        s.run_passes(EQUIL, seed=seed)
+        acc = np.zeros(4)
+        for _ in range(NSAMP):
+            s.run_passes(EVERY, seed=seed)
+            acc += np.append(s.estimators()[:3], s.rcf()[half] / w.nrotslices)
+        out.append(acc / NSAMP)
+        s.close()
+    return np.array(out)
 
 
 @pytest.mark.parametrize("mixed", [False, True])
-@pytest.mark.parametrize("name", list(SYSTEMS))
-def test_production_runs_agree_with_the_oracle_within_two_standard_errors(name, mixed):
-    w = SYSTEMS[name]()
-    half = w.nrotslices // 2
-    s = G.Sampler(w, mixed=mixed)
-    s.run_passes(EQUIL, seed=11)
-
-    def gpu():
-        s.run_passes(1, seed=11)
-        return np.append(s.estimators()[:3], s.rcf()[half] / w.nrotslices)
-    g = _blocks(gpu, NB, PER)
-    s.close()
-    c = _oracle_blocks(name)
-    mg, mc = g.mean(0), c.mean(0)
-    se = np.hypot(g.std(0, ddof=1), c.std(0, ddof=1)) / np.sqrt(NB)
-    z = (mg - mc) / se
-    report = {n: (round(a, 5), round(b, 5), round(e, 5), round(zz, 2)) for n, a, b, e, zz in zip(NAMES, mg, mc, se, z)}
-    print("%s %s block means (GPU, oracle, combined SE, z):" % (name, "fp32" if mixed else "fp64"), report)
+@pytest.mark.parametrize("name", ["config0", "config1", "config3"])
+def test_production_runs_agree_with_the_oracle(name, mixed):
+    c = _oracle_means(name)
+    g = _gpu_means(name, mixed)
+    se = np.hypot(g.std(0, ddof=1), c.std(0, ddof=1)) / np.sqrt(K)
+    z = (g.mean(0) - c.mean(0)) / se
+    _results[(name, mixed)] = z
+    report = {n: (round(a, 5), round(b, 5), round(e, 5), round(zz, 2))
+              for n, a, b, e, zz in zip(NAMES, g.mean(0), c.mean(0), se, z)}
+    print("%s %s means (GPU, oracle, combined SE, z):" % (name, "fp32" if mixed else "fp64"), report)
     assert np.all(np.isfinite(z)), report
-    assert np.all(np.abs(z) <= 2.0), report
+    assert np.all(np.abs(z) <= 3.5), report
+
+
+def test_count_of_comparisons_beyond_two_standard_errors():
+    if len(_results) < 6:
+        pytest.skip("needs the six system x precision comparisons of this module")
+    z = np.concatenate(list(_results.values()))
+    print("all z:", np.round(z, 2), "beyond 2:", int(np.sum(np.abs(z) > 2.0)))
+    assert int(np.sum(np.abs(z) > 2.0)) <= 4, np.round(z, 2)
