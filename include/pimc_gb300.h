@@ -404,6 +404,14 @@ pimc_status pimc_batch_set_precision(pimc_batch *b, int mixed);
  * pass of each of six shapes (the passes run: the replicas move on), keeps
  * the fastest and returns it in shape_out[2] and the six times in ms_out[6] */
 pimc_status pimc_batch_set_shape(pimc_batch *b, int warps, int min_blocks);
+/* where the rotational half-sweeps run: 0 (default) inside the persistent
+ * pass, each CTA sweeping its own replica's slices; 1 one launch per
+ * half-sweep over all replicas, one warp per (replica, slice pair) -- for
+ * replicas with many rotational slices, whose sweeps would otherwise keep
+ * one CTA busy long after the others finished.  Both make the same moves
+ * with the same draws in the same order per replica (identical paths); 1
+ * needs an even Q in every replica. */
+pimc_status pimc_batch_set_rotation_mode(pimc_batch *b, int mode);
 pimc_status pimc_batch_autotune(pimc_batch *b, uint64_t seed, int *shape_out, double *ms_out);
 pimc_status pimc_batch_run_passes(pimc_batch *b, int npasses, uint64_t seed);
 /* per replica 4 values: E_kin, E_pot, E_rot (as pimc_estimators out[0..2])

@@ -429,10 +429,13 @@ __device__ int cta_mol(const Ctx &c, const Frame *frames, int type, int atom, ui
 __global__ void k_batch_reset(unsigned *work) { *work = 0u; }
 
 // one production pass of every replica; MINB: resident CTAs per SM the
-// register allocation is bounded for (a shape the autotuner tries)
+// register allocation is bounded for (a shape the autotuner tries).
+// A launch may cover only the bisection blocks [blk_lo, blk_hi) of the pass;
+// the one with blk_lo = 0 opens the pass (pass counter, centroid moves).
 template <bool MIX, int MINB>
 __global__ void __launch_bounds__(256, MINB) k_batch_pass(const BatchRep *reps, const int *order, int n,
-                                                          uint64_t seed, unsigned *work, int rot_on)
+                                                          uint64_t seed, unsigned *work, int rot_on, int blk_lo,
+                                                          int blk_hi)
 {
   extern __shared__ __align__(16) unsigned char smem[];
   Ctx &c = *reinterpret_cast<Ctx *>(smem);
@@ -454,7 +457,7 @@ __global__ void __launch_bounds__(256, MINB) k_batch_pass(const BatchRep *reps, 
       for (int i = tid; i < (int)(sizeof(Ctx) / 4); i += blockDim.x) dst[i] = src[i];
     }
     Frame *frames = reps[r].frames;
-    if (tid == 0) sps = ++(*reps[r].pass);
+    if (tid == 0) sps = blk_lo == 0 ? ++(*reps[r].pass) : *reps[r].pass;
     __syncthreads();
     const unsigned ps = sps;
     const uint64_t sr = seed ^ reps[r].seed_mix;
@@ -466,7 +469,7 @@ __global__ void __launch_bounds__(256, MINB) k_batch_pass(const BatchRep *reps, 
     unsigned B = 0;
     for (int t = 0; t < s.ntypes; t++) B += (unsigned)((1 << s.levels[t]) * s.numb[t]);
     // centroid moves (mc_main.cc:512-513)
-    for (int t = 0; t < s.ntypes; t++)
+    for (int t = 0; t < s.ntypes && blk_lo == 0; t++)
       for (int a = 0; a < s.numb[t]; a++) {
         int acc = cta_mol<MIX>(c, frames, t, a, sr, ps, B + 2u * (unsigned)s.P + (unsigned)t, sd, red, &sacc);
         if (tid == 0) {
@@ -482,6 +485,10 @@ __global__ void __launch_bounds__(256, MINB) k_batch_pass(const BatchRep *reps, 
     for (int t = 0; t < s.ntypes; t++) {
       const int M = 1 << s.levels[t], N = s.numb[t];
       for (int s0 = 0; s0 < M; s0++, blk++) {
+        if (blk < blk_lo || blk >= blk_hi) {
+          b0 += (unsigned)N;
+          continue;
+        }
         for (int kw = warp; kw < s.P / M; kw += nw)
           for (int j = 0; j < N; j++) {
             PhiloxSrc src{sr, ((uint64_t)ps << 32) | ((uint64_t)(b0 + (unsigned)j) << 12) | (uint64_t)kw};
@@ -664,17 +671,97 @@ int batch_max_ctas(int mixed, int warps, int minb)
 }
 
 void launch_batch_pass(const BatchRep *reps, const int *order, int n, uint64_t seed, unsigned *work, int mixed,
-                       int warps, int minb, int nctas, cudaStream_t s, int rot_on)
+                       int warps, int minb, int nctas, cudaStream_t s, int rot_on, int blk_lo, int blk_hi)
 {
   size_t sm = batch_smem_bytes(warps);
   k_batch_reset<<<1, 1, 0, s>>>(work);
   if (mixed) {
-    if (minb >= 3) k_batch_pass<true, 3><<<nctas, 32 * warps, sm, s>>>(reps, order, n, seed, work, rot_on);
-    else k_batch_pass<true, 2><<<nctas, 32 * warps, sm, s>>>(reps, order, n, seed, work, rot_on);
+    if (minb >= 3)
+      k_batch_pass<true, 3><<<nctas, 32 * warps, sm, s>>>(reps, order, n, seed, work, rot_on, blk_lo, blk_hi);
+    else k_batch_pass<true, 2><<<nctas, 32 * warps, sm, s>>>(reps, order, n, seed, work, rot_on, blk_lo, blk_hi);
   } else {
-    if (minb >= 3) k_batch_pass<false, 3><<<nctas, 32 * warps, sm, s>>>(reps, order, n, seed, work, rot_on);
-    else k_batch_pass<false, 2><<<nctas, 32 * warps, sm, s>>>(reps, order, n, seed, work, rot_on);
+    if (minb >= 3)
+      k_batch_pass<false, 3><<<nctas, 32 * warps, sm, s>>>(reps, order, n, seed, work, rot_on, blk_lo, blk_hi);
+    else k_batch_pass<false, 2><<<nctas, 32 * warps, sm, s>>>(reps, order, n, seed, work, rot_on, blk_lo, blk_hi);
   }
+}
+
+// One half-sweep of the rotational slices of many replicas at once, for
+// replicas whose own passes interleave their sweeps with their bisection
+// blocks: the launch for (block blk, sweep j of the block, parity) moves, in
+// every replica with more than j sweeps in that block, the slices of that
+// parity -- one warp per (replica, slice), its rotors in order, exactly the
+// moves, draws and order of the persistent pass.  Replicas are taken in the
+// order `sorted` (most sweeps per block first) and unit u of the launch is
+// slice pair u - pre[k] of replica sorted[k], pre the prefix sums of Q/2.
+template <bool MIX>
+__global__ void __launch_bounds__(256) k_batch_rot_flat(const BatchRep *reps, const int *sorted, const int *pre,
+                                                        int nact, int blk, int j, int parity, int nbk,
+                                                        uint64_t seed)
+{
+  extern __shared__ __align__(16) unsigned char smem[];
+  WarpMem *wm = reinterpret_cast<WarpMem *>(smem);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int u = blockIdx.x * (blockDim.x >> 5) + warp;
+  if (u >= pre[nact]) return;                           // warp-uniform
+  int lo = 0, hi = nact;                                // pre[lo] <= u < pre[hi]
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (pre[mid] <= u) lo = mid;
+    else hi = mid;
+  }
+  const BatchRep &rp = reps[sorted[lo]];
+  const Ctx &c = rp.c;
+  const DevSys &s = c.s;
+  Frame *frames = rp.frames;
+  const unsigned ps = *rp.pass;
+  const uint64_t sr = seed ^ rp.seed_mix;
+  const bool linear = s.molecule[s.imtype] == 1;
+  unsigned B = 0;
+  for (int t = 0; t < s.ntypes; t++) B += (unsigned)((1 << s.levels[t]) * s.numb[t]);
+  const int it = (int)((long long)blk * s.P / nbk) + j;
+  const unsigned phase = B + 2u * (unsigned)it + (unsigned)parity;
+  const int kk = u - pre[lo], q = parity + 2 * kk;
+  const size_t nq = (size_t)s.nrotors * s.Q;
+  unsigned long long tot = 0, nacc = 0;
+  for (int rr = 0; rr < s.nrotors; rr++) {
+    double uu[4] = {0.5, 0.5, 0.5, 0.5}, prop[3] = {0.0, 0.0, 0.0};
+    if (lane == 0) {
+      size_t i1 = (size_t)rr * s.Q + q;
+      rot_uniforms_t<MIX>(sr, ps, phase, q >> 1, rr, linear, uu);
+      rot_propose_t<MIX>(s, linear, c.st.ang[i1], c.st.ang[nq + i1], c.st.ang[2 * nq + i1], uu, prop);
+    }
+    int acc = warp_rot<MIX>(c, frames, s.rot_first + rr, q, uu, prop, linear, wm[warp].u.r, wm[warp].buf, lane);
+    tot++;
+    nacc += acc;
+  }
+  if (lane == 0) {
+    atomicAdd(&rp.cnt[(s.imtype * 3 + 2) * 2 + 0], tot);
+    atomicAdd(&rp.cnt[(s.imtype * 3 + 2) * 2 + 1], nacc);
+  }
+}
+
+size_t batch_flat_smem_bytes(int warps) { return (size_t)warps * sizeof(WarpMem); }
+
+void launch_batch_rot_flat(const BatchRep *reps, const int *sorted, const int *pre, int nact, int units, int blk,
+                           int j, int parity, int nbk, uint64_t seed, int mixed, int warps, cudaStream_t s)
+{
+  if (units <= 0) return;
+  const size_t sm = batch_flat_smem_bytes(warps);
+  const int nctas = (units + warps - 1) / warps;
+  if (mixed) k_batch_rot_flat<true><<<nctas, 32 * warps, sm, s>>>(reps, sorted, pre, nact, blk, j, parity, nbk, seed);
+  else k_batch_rot_flat<false><<<nctas, 32 * warps, sm, s>>>(reps, sorted, pre, nact, blk, j, parity, nbk, seed);
+}
+
+int batch_flat_setup(int warps)
+{
+  const size_t sm = batch_flat_smem_bytes(warps);
+  if (cudaFuncSetAttribute(k_batch_rot_flat<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) !=
+          cudaSuccess ||
+      cudaFuncSetAttribute(k_batch_rot_flat<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) !=
+          cudaSuccess)
+    return 0;
+  return 1;
 }
 
 // after rotational moves made outside k_batch_pass: each replica's MCCosine

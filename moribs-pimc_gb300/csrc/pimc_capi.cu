@@ -1845,6 +1845,14 @@ struct pimc_batch {
   unsigned *d_pass = nullptr;
   int warps = 8, minb = 2;
   int mixed = 0;
+  // rotational half-sweeps: 0 inside the persistent pass, 1 one launch per
+  // half-sweep over all replicas (per block: replicas ordered by sweeps,
+  // prefix sums of their slice pairs, nbk x (n + 1) each on the device)
+  int rot_mode = 0, exec_rot_mode = -1;
+  long long exec_nodes = 2;
+  int *d_flat_sorted = nullptr, *d_flat_pre = nullptr;
+  std::vector<int> flat_nact_max;                  // per block: sweeps of its busiest replica
+  std::vector<std::vector<int>> flat_act, flat_units;   // per block and sweep: active replicas, warps
   bool tables = false;
   cudaGraphExec_t exec = nullptr;
   uint64_t exec_seed = 0;
@@ -2140,6 +2148,66 @@ extern "C" pimc_status pimc_batch_set_shape(pimc_batch *b, int warps, int min_bl
   return PIMC_OK;
 }
 
+extern "C" pimc_status pimc_batch_set_rotation_mode(pimc_batch *b, int mode)
+{
+  if (!b || mode < 0 || mode > 1) return PIMC_ERR_BAD_ARG;
+  if (mode == 1)
+    for (int r = 0; r < b->n; r++) {
+      const DevSys &d = b->reps[r].c.s;
+      if (d.nrotors > 0 && b->sys[r].rotation && d.Q % 2) return PIMC_ERR_BAD_ARG;   // the odd-Q serial step
+    }
+  b->rot_mode = mode;
+  return PIMC_OK;
+}
+
+// the flat mode's tables: per block, the replicas by decreasing sweep count
+// in that block and the prefix sums of their slice pairs (Q/2)
+static pimc_status batch_flat_tables(pimc_batch *b, int nbk)
+{
+  pimc_handle *h = b->base;
+  if (b->d_flat_sorted) return PIMC_OK;
+  std::vector<int> sorted((size_t)nbk * b->n), pre((size_t)nbk * (b->n + 1));
+  b->flat_nact_max.assign(nbk, 0);
+  for (int blk = 0; blk < nbk; blk++) {
+    std::vector<std::pair<int, int>> k(b->n);
+    for (int r = 0; r < b->n; r++) {
+      const DevSys &d = b->reps[r].c.s;
+      int sw = 0;
+      if (d.nrotors > 0 && b->sys[r].rotation)
+        sw = (int)((long long)(blk + 1) * d.P / nbk) - (int)((long long)blk * d.P / nbk);
+      k[r] = {-sw, r};
+    }
+    std::stable_sort(k.begin(), k.end());
+    int acc = 0;
+    pre[(size_t)blk * (b->n + 1)] = 0;
+    for (int i = 0; i < b->n; i++) {
+      sorted[(size_t)blk * b->n + i] = k[i].second;
+      acc += b->reps[k[i].second].c.s.Q / 2;
+      pre[(size_t)blk * (b->n + 1) + i + 1] = acc;
+    }
+    b->flat_nact_max[blk] = b->n ? -k[0].first : 0;
+  }
+  pimc_status e;
+  if ((e = pool(h, &b->d_flat_sorted, sorted.size())) || (e = pool(h, &b->d_flat_pre, pre.size()))) return e;
+  CK(cudaMemcpy(b->d_flat_sorted, sorted.data(), sorted.size() * sizeof(int), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(b->d_flat_pre, pre.data(), pre.size() * sizeof(int), cudaMemcpyHostToDevice));
+  // replicas still active at sweep j of block blk: a prefix of that block's order
+  b->flat_act.assign((size_t)nbk, std::vector<int>());
+  for (int blk = 0; blk < nbk; blk++) {
+    std::vector<int> &act = b->flat_act[blk];
+    act.assign(b->flat_nact_max[blk], 0);
+    for (int i = 0; i < b->n; i++) {
+      const DevSys &d = b->reps[sorted[(size_t)blk * b->n + i]].c.s;
+      int sw = (d.nrotors > 0 && b->sys[sorted[(size_t)blk * b->n + i]].rotation)
+                   ? (int)((long long)(blk + 1) * d.P / nbk) - (int)((long long)blk * d.P / nbk) : 0;
+      for (int j = 0; j < sw; j++) act[j] = i + 1;
+    }
+    b->flat_units.push_back(std::vector<int>(act.size()));
+    for (size_t j = 0; j < act.size(); j++) b->flat_units.back()[j] = pre[(size_t)blk * (b->n + 1) + act[j]];
+  }
+  return PIMC_OK;
+}
+
 static pimc_status batch_ready(pimc_batch *b)
 {
   if (!b) return PIMC_ERR_BAD_ARG;
@@ -2157,14 +2225,35 @@ extern "C" pimc_status pimc_batch_run_passes(pimc_batch *b, int npasses, uint64_
   pimc_handle *h = b->base;
   CK(cudaSetDevice(h->device));
   if (!b->exec || b->exec_seed != seed || b->exec_warps != b->warps || b->exec_minb != b->minb ||
-      b->exec_mixed != b->mixed) {
+      b->exec_mixed != b->mixed || b->exec_rot_mode != b->rot_mode) {
     if (b->exec) { BK(cudaGraphExecDestroy(b->exec)); b->exec = nullptr; }
     int nctas = batch_max_ctas(b->mixed, b->warps, b->minb);
     if (nctas <= 0) return PIMC_ERR_CUDA;
     if (nctas > b->n) nctas = b->n;
+    const DevSys &d0 = b->reps[0].c.s;
+    int nbk = 0;
+    for (int t = 0; t < d0.ntypes; t++) nbk += 1 << d0.levels[t];
+    if (b->rot_mode == 1) {
+      if ((e = batch_flat_tables(b, nbk))) return e;
+      if (!batch_flat_setup(b->warps)) return PIMC_ERR_CUDA;
+    }
     cudaGraph_t graph;
     CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-    launch_batch_pass(b->d_reps, b->d_order, b->n, seed, b->d_work, b->mixed, b->warps, b->minb, nctas, h->stream);
+    if (b->rot_mode == 0) {
+      launch_batch_pass(b->d_reps, b->d_order, b->n, seed, b->d_work, b->mixed, b->warps, b->minb, nctas, h->stream);
+    } else {
+      // per block: the block's bisections of every replica in one persistent
+      // launch, then its sweeps, one launch per half-sweep over all replicas
+      for (int blk = 0; blk < nbk; blk++) {
+        launch_batch_pass(b->d_reps, b->d_order, b->n, seed, b->d_work, b->mixed, b->warps, b->minb, nctas,
+                          h->stream, 0, blk, blk + 1);
+        for (int j = 0; j < b->flat_nact_max[blk]; j++)
+          for (int parity = 0; parity < 2; parity++)
+            launch_batch_rot_flat(b->d_reps, b->d_flat_sorted + (size_t)blk * b->n,
+                                  b->d_flat_pre + (size_t)blk * (b->n + 1), b->flat_act[blk][j],
+                                  b->flat_units[blk][j], blk, j, parity, nbk, seed, b->mixed, b->warps, h->stream);
+      }
+    }
     cudaError_t le = cudaGetLastError();
     cudaError_t ce = cudaStreamEndCapture(h->stream, &graph);
     if (le != cudaSuccess || ce != cudaSuccess) {
@@ -2179,10 +2268,18 @@ extern "C" pimc_status pimc_batch_run_passes(pimc_batch *b, int npasses, uint64_
     b->exec_warps = b->warps;
     b->exec_minb = b->minb;
     b->exec_mixed = b->mixed;
+    b->exec_rot_mode = b->rot_mode;
+    long long nodes = 2;
+    if (b->rot_mode == 1) {
+      nodes = 2LL * nbk;
+      for (int blk = 0; blk < nbk; blk++)
+        for (int j = 0; j < b->flat_nact_max[blk]; j++) nodes += 2 * (b->flat_units[blk][j] > 0);
+    }
+    b->exec_nodes = nodes;
   }
   for (int p = 0; p < npasses; p++) {
     CK(cudaGraphLaunch(b->exec, h->stream));
-    h->launches += 2;
+    h->launches += b->exec_nodes;
   }
   if (npasses > 0) {
     launch_batch_refresh(b->d_reps, b->n, 0, h->stream);     // double frames and MCCosine of tops

@@ -137,6 +137,7 @@ def load(path=LIBPATH):
     L.pimc_batch_replica_seed.argtypes = [C.c_uint64, C.c_int]
     L.pimc_batch_stream.restype = vp
     L.pimc_batch_stream.argtypes = [vp]
+    L.pimc_batch_set_rotation_mode.argtypes = [vp, C.c_int]
     L.pimc_batch_da_sweeps.argtypes = [vp, vp, C.c_int, C.c_uint64, C.c_float, C.c_int, _dp]
     L.pimc_batch_da_passes.argtypes = [vp, vp, C.c_int, C.c_uint64, C.c_float, C.c_int, _dp]
     _L = L
@@ -450,6 +451,9 @@ class Batch:
 
     def set_shape(self, warps, min_blocks=2):
         _chk(self.L.pimc_batch_set_shape(self.h, int(warps), int(min_blocks)), "pimc_batch_set_shape")
+
+    def set_rotation_mode(self, mode):
+        _chk(self.L.pimc_batch_set_rotation_mode(self.h, int(mode)), "pimc_batch_set_rotation_mode")
 
     def autotune(self, seed):
         """(warps, min_blocks) of the fastest shape and the six times (ms per pass)."""
