@@ -733,6 +733,46 @@ __device__ __forceinline__ double caleng(const Frame &f1, const Frame &f2, doubl
   return vlj * kcal2k + (vmh + vmm + vhh) * hr2k * br2ang;
 }
 
+// caleng on the FP32 path: the same sites, charges and terms as caleng
+// above, from the float frames and float centres, summed in float (the
+// Coulomb terms of the four sites cancel to about 1/50 of their size, so
+// the result keeps about six digits)
+__device__ __forceinline__ float caleng32(const float *ma, const float *mb, float c1x, float c1y, float c1z, float c2x,
+                                          float c2y, float c2z)
+{
+  const float qm = -1.04f, qh = 0.520f, kcal2k = 503.0f;
+  const float coul = (float)(3.1577465e5 * 0.52917721092);
+  const float site[4][3] = {{0.0f, 0.0f, 0.06562f}, {0.0f, 0.0f, -0.08438f}, {0.7557f, 0.0f, -0.5223f},
+                            {-0.7557f, 0.0f, -0.5223f}};
+  float a[4][3], b[4][3];
+  const float c1[3] = {c1x, c1y, c1z}, c2[3] = {c2x, c2y, c2z};
+#pragma unroll
+  for (int s = 0; s < 4; s++)
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      float u = c1[i], v = c2[i];
+#pragma unroll
+      for (int j = 0; j < 3; j++) {
+        u = fmaf(ma[i * 3 + j], site[s][j], u);
+        v = fmaf(mb[i * 3 + j], site[s][j], v);
+      }
+      a[s][i] = u;
+      b[s][i] = v;
+    }
+  auto d2 = [](const float *p, const float *q) {
+    float x = p[0] - q[0], y = p[1] - q[1], z = p[2] - q[2];
+    return x * x + y * y + z * z;
+  };
+  const float roo = d2(a[0], b[0]);
+  const float roo6 = roo * roo * roo, roo12 = roo6 * roo6;
+  const float vlj = 6.e5f / roo12 - 610.0f / roo6;
+  auto inv = [&](const float *p, const float *q) { return 1.0f / sqrtf(d2(p, q)); };
+  const float vmh = qm * qh * (inv(a[1], b[2]) + inv(a[1], b[3]) + inv(b[1], a[2]) + inv(b[1], a[3]));
+  const float vhh = qh * qh * (inv(a[2], b[2]) + inv(a[2], b[3]) + inv(a[3], b[2]) + inv(a[3], b[3]));
+  const float vmm = qm * qm * inv(a[1], b[1]);
+  return vlj * kcal2k + (vmh + vmm + vhh) * coul;
+}
+
 // vspher (vspher.f:12-544) on the supplied table
 __device__ __forceinline__ double vspher(const DevTables &t, double r)
 {

@@ -104,8 +104,8 @@ __device__ __forceinline__ float pair_term32(const Ctx &c, const Frame *frames, 
     if (m0 == 2) return vcord32(c.t, frames[rot_index(s, a0, it / s.R)], -dx, -dy, -dz);
     return vcord32(c.t, frames[rot_index(s, a1, it / s.R)], dx, dy, dz);
   } else if (m0 == 2 && m1 == 2 && s.numb[s.imtype] > 1) {
-    return (float)caleng(frames[rot_index(s, a0, it / s.R)], frames[rot_index(s, a1, it / s.R)], (double)px,
-                         (double)py, (double)pz, (double)qx, (double)qy, (double)qz);
+    return caleng32(frames[rot_index(s, a0, it / s.R)].mf, frames[rot_index(s, a1, it / s.R)].mf, px, py, pz, qx, qy,
+                    qz);
   }
   return spot1d32(c.t, r);
 }
@@ -580,8 +580,8 @@ __device__ __forceinline__ float rot3d_term32(const Ctx &c, const Frame *frames,
     const float4 p0 = c.st.b4[i0], p1 = c.st.b4[i1];
     return vcord32(c.t, f, p1.x - p0.x, p1.y - p0.y, p1.z - p0.z);
   }
-  return (float)caleng(f, frames[rot_index(s, a1, it / s.R)], c.st.x[i0], c.st.y[i0], c.st.z[i0], c.st.x[i1],
-                       c.st.y[i1], c.st.z[i1]);
+  const float4 p0 = c.st.b4[i0], p1 = c.st.b4[i1];
+  return caleng32(f.mf, frames[rot_index(s, a1, it / s.R)].mf, p0.x, p0.y, p0.z, p1.x, p1.y, p1.z);
 }
 
 // PotRotEnergy term (mc_piqmc.cc:1987-2040) for the linear rotor g0 with unit
