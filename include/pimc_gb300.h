@@ -121,7 +121,11 @@ pimc_status pimc_densities_reset(pimc_handle *h);
  * angles (theta, phi, chi) of rotational slices it0 and it0 + skip, as
  * GetRotE3D fills _relthe_sum, _relphi_sum, _relchi_sum (mc_estim.cc:1023-1057);
  * pimc_rel_euler_read copies the[PIMC_BINST], phi[PIMC_BINSC], chi[PIMC_BINSC]
- * (zeros without a nonlinear rotor); pimc_densities_reset clears them. */
+ * (zeros without a nonlinear rotor); pimc_densities_reset clears them too.
+ * The reference keeps these counts for the whole run (_relthe_sum & co. are
+ * reset only with the run totals, mc_estim.cc:361-372): a caller that resets
+ * the densities per block reads pimc_rel_euler_read before each reset and
+ * adds the counts to its own run totals. */
 pimc_status pimc_rel_euler_read(pimc_handle *h, double *the, double *phi, double *chi);
 
 /* GetExchangeLength (mc_estim.cc:1997-2019): ploops[k] += 1 for every
@@ -400,7 +404,8 @@ pimc_status pimc_batch_get_state(pimc_batch *b, int replica, double *coords, dou
                                  int *pindex);
 pimc_status pimc_batch_set_precision(pimc_batch *b, int mixed);
 /* launch shape: warps per CTA (2, 4 or 8) and the resident CTAs per SM the
- * kernel's registers are bounded for (2 or 3).  pimc_batch_autotune times one
+ * kernels' registers are bounded for (2, 3, or 4: the half-sweep launches of
+ * rotation mode 1 take 4, the persistent pass then 3).  pimc_batch_autotune times one
  * pass of each of six shapes (the passes run: the replicas move on), keeps
  * the fastest and returns it in shape_out[2] and the six times in ms_out[6] */
 pimc_status pimc_batch_set_shape(pimc_batch *b, int warps, int min_blocks);

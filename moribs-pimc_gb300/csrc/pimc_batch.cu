@@ -694,8 +694,8 @@ void launch_batch_pass(const BatchRep *reps, const int *order, int n, uint64_t s
 // moves, draws and order of the persistent pass.  Replicas are taken in the
 // order `sorted` (most sweeps per block first) and unit u of the launch is
 // slice pair u - pre[k] of replica sorted[k], pre the prefix sums of Q/2.
-template <bool MIX>
-__global__ void __launch_bounds__(256) k_batch_rot_flat(const BatchRep *reps, const int *sorted, const int *pre,
+template <bool MIX, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_batch_rot_flat(const BatchRep *reps, const int *sorted, const int *pre,
                                                         int nact, int blk, int j, int parity, int nbk,
                                                         uint64_t seed)
 {
@@ -743,25 +743,38 @@ __global__ void __launch_bounds__(256) k_batch_rot_flat(const BatchRep *reps, co
 
 size_t batch_flat_smem_bytes(int warps) { return (size_t)warps * sizeof(WarpMem); }
 
+// minb: resident CTAs per SM the registers are bounded for (2, 3 or 4)
 void launch_batch_rot_flat(const BatchRep *reps, const int *sorted, const int *pre, int nact, int units, int blk,
-                           int j, int parity, int nbk, uint64_t seed, int mixed, int warps, cudaStream_t s)
+                           int j, int parity, int nbk, uint64_t seed, int mixed, int warps, int minb, cudaStream_t s)
 {
   if (units <= 0) return;
   const size_t sm = batch_flat_smem_bytes(warps);
   const int nctas = (units + warps - 1) / warps;
-  if (mixed) k_batch_rot_flat<true><<<nctas, 32 * warps, sm, s>>>(reps, sorted, pre, nact, blk, j, parity, nbk, seed);
-  else k_batch_rot_flat<false><<<nctas, 32 * warps, sm, s>>>(reps, sorted, pre, nact, blk, j, parity, nbk, seed);
+#define PIMC_FLAT(M, B) k_batch_rot_flat<M, B><<<nctas, 32 * warps, sm, s>>>(reps, sorted, pre, nact, blk, j, parity, nbk, seed)
+  if (mixed) {
+    if (minb >= 4) PIMC_FLAT(true, 4);
+    else if (minb == 3) PIMC_FLAT(true, 3);
+    else PIMC_FLAT(true, 2);
+  } else {
+    if (minb >= 4) PIMC_FLAT(false, 4);
+    else if (minb == 3) PIMC_FLAT(false, 3);
+    else PIMC_FLAT(false, 2);
+  }
+#undef PIMC_FLAT
+}
+
+template <bool MIX, int MINB>
+static bool flat_attr(size_t sm)
+{
+  return cudaFuncSetAttribute(k_batch_rot_flat<MIX, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) ==
+         cudaSuccess;
 }
 
 int batch_flat_setup(int warps)
 {
   const size_t sm = batch_flat_smem_bytes(warps);
-  if (cudaFuncSetAttribute(k_batch_rot_flat<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) !=
-          cudaSuccess ||
-      cudaFuncSetAttribute(k_batch_rot_flat<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) !=
-          cudaSuccess)
-    return 0;
-  return 1;
+  return flat_attr<true, 2>(sm) && flat_attr<true, 3>(sm) && flat_attr<true, 4>(sm) && flat_attr<false, 2>(sm) &&
+         flat_attr<false, 3>(sm) && flat_attr<false, 4>(sm);
 }
 
 // after rotational moves made outside k_batch_pass: each replica's MCCosine

@@ -1848,7 +1848,7 @@ struct pimc_batch {
   // rotational half-sweeps: 0 inside the persistent pass, 1 one launch per
   // half-sweep over all replicas (per block: replicas ordered by sweeps,
   // prefix sums of their slice pairs, nbk x (n + 1) each on the device)
-  int rot_mode = 0, exec_rot_mode = -1;
+  int rot_mode = 0, exec_rot_mode = -1, exec_flat_minb = 0;
   long long exec_nodes = 2;
   int *d_flat_sorted = nullptr, *d_flat_pre = nullptr;
   std::vector<int> flat_nact_max;                  // per block: sweeps of its busiest replica
@@ -2142,9 +2142,9 @@ extern "C" pimc_status pimc_batch_set_precision(pimc_batch *b, int mixed)
 
 extern "C" pimc_status pimc_batch_set_shape(pimc_batch *b, int warps, int min_blocks)
 {
-  if (!b || (warps != 2 && warps != 4 && warps != 8) || (min_blocks != 2 && min_blocks != 3)) return PIMC_ERR_BAD_ARG;
+  if (!b || (warps != 2 && warps != 4 && warps != 8) || min_blocks < 2 || min_blocks > 4) return PIMC_ERR_BAD_ARG;
   b->warps = warps;
-  b->minb = min_blocks;
+  b->minb = min_blocks;      // the persistent pass is bounded for at most 3
   return PIMC_OK;
 }
 
@@ -2225,7 +2225,7 @@ extern "C" pimc_status pimc_batch_run_passes(pimc_batch *b, int npasses, uint64_
   pimc_handle *h = b->base;
   CK(cudaSetDevice(h->device));
   if (!b->exec || b->exec_seed != seed || b->exec_warps != b->warps || b->exec_minb != b->minb ||
-      b->exec_mixed != b->mixed || b->exec_rot_mode != b->rot_mode) {
+      b->exec_mixed != b->mixed || b->exec_rot_mode != b->rot_mode || b->exec_flat_minb != b->minb) {
     if (b->exec) { BK(cudaGraphExecDestroy(b->exec)); b->exec = nullptr; }
     int nctas = batch_max_ctas(b->mixed, b->warps, b->minb);
     if (nctas <= 0) return PIMC_ERR_CUDA;
@@ -2251,7 +2251,8 @@ extern "C" pimc_status pimc_batch_run_passes(pimc_batch *b, int npasses, uint64_
           for (int parity = 0; parity < 2; parity++)
             launch_batch_rot_flat(b->d_reps, b->d_flat_sorted + (size_t)blk * b->n,
                                   b->d_flat_pre + (size_t)blk * (b->n + 1), b->flat_act[blk][j],
-                                  b->flat_units[blk][j], blk, j, parity, nbk, seed, b->mixed, b->warps, h->stream);
+                                  b->flat_units[blk][j], blk, j, parity, nbk, seed, b->mixed, b->warps,
+                                  b->minb, h->stream);
       }
     }
     cudaError_t le = cudaGetLastError();
@@ -2269,6 +2270,7 @@ extern "C" pimc_status pimc_batch_run_passes(pimc_batch *b, int npasses, uint64_
     b->exec_minb = b->minb;
     b->exec_mixed = b->mixed;
     b->exec_rot_mode = b->rot_mode;
+    b->exec_flat_minb = b->minb;
     long long nodes = 2;
     if (b->rot_mode == 1) {
       nodes = 2LL * nbk;
