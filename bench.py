@@ -65,6 +65,7 @@ def parse():
     ap.add_argument("--worm-replicas", type=int, default=32, help="independent worm chains run at once")
     ap.add_argument("--quick-se", action="store_true", help="short series for the matched-SE measurement")
     ap.add_argument("--no-matched-se", action="store_true", help="skip the matched <E> SE measurement")
+    ap.add_argument("--no-precision-error", action="store_true", help="skip the FP32-vs-FP64 per-replica comparison")
     ap.add_argument("--da-replicas", type=int, default=32, help="independent dimer systems swept at once")
     ap.add_argument("--only", default=None, choices=["tables", "worm", "surrogate", "matched_se"],
                     help="run one companion measurement alone on cuda:0 and print its JSON (for profiling)")
@@ -461,6 +462,45 @@ def run_batched(args, local, dist):
                                                                          [float(x) for x in tune_ms])},
            "accept_ratios": {"He bisection": acc[1] / max(1, tot[1]), "rotation": acc[5] / max(1, tot[5])}}
     b.close()
+    if not args.no_precision_error:
+        out["fp32_vs_fp64"] = precision_error(ws[:1024], local)
+    return out
+
+
+def precision_error(ws, local, eq=5, npass=12):
+    """The FP32 path's error against the FP64 path, replica by replica, on
+    the same replicas with the same seeds: per replica <E> and the mean rotor
+    axis z component <cos theta> over npass passes after eq, in each
+    precision; the difference over the combined standard error (the g of each
+    series from its pooled autocorrelation).  In FP64 a batch replica is the
+    single-system chain, so this is the FP32 path against the FP64 plain
+    path."""
+    import numpy as np
+    import pimc_gb300 as G
+    ser = {}
+    for mixed in (False, True):
+        b = G.Batch(ws, device=local, mixed=mixed)
+        b.run_passes(eq, 91)
+        e, cz = [], []
+        for k in range(npass):
+            b.run_passes(1, 91)
+            est = b.estimators()
+            e.append(est[:, 0] + est[:, 1] + est[:, 2])
+            cz.append(est[:, 3])
+        b.close()
+        ser[mixed] = (np.array(e), np.array(cz))
+    out = {"replicas": len(ws), "passes": npass, "after": eq}
+    for name, k in (("E", 0), ("cos_theta", 1)):
+        x64, x32 = ser[False][k], ser[True][k]
+        g64, g32 = pooled_inefficiency(x64), pooled_inefficiency(x32)
+        se = np.sqrt(g64 * x64.var(axis=0, ddof=1) / npass + g32 * x32.var(axis=0, ddof=1) / npass)
+        d = x32.mean(axis=0) - x64.mean(axis=0)
+        ok = se > 0
+        z = d[ok] / se[ok]
+        out[name] = {"frac_within_2se": round(float(np.mean(np.abs(z) <= 2.0)), 4),
+                     "median_abs_z": round(float(np.median(np.abs(z))), 3),
+                     "mean_abs_diff": round(float(np.mean(np.abs(d))), 5),
+                     "mean_diff": round(float(np.mean(d)), 5), "mean_se": round(float(np.mean(se)), 5)}
     return out
 
 
@@ -755,23 +795,25 @@ def crossover(w, line):
             "what": "a screen spares exact terms only if a surrogate row costs less than the terms it replaces"}
 
 
-def run_matched_se(local, quick=False, c4_replicas=512, c4_passes=24, c3_replicas=64):
+def run_matched_se(local, quick=False, c4_replicas=512, c4_passes=8, c3_replicas=64, c4_shape=(8, 4)):
     """The metric itself: bead-moves/s at matched <E> standard error.
 
     Water chains (config 4): c4_replicas replicas of 1-8 water tops on a
     3 A chain + 0-32 pH2, T 0.5-2.0 K, P 512-2048, Q = P/4.  Arms: the plain
-    GPU path (each replica alone on the single-system sampler, FP64; its pass
-    time measured on a seeded sample of replicas and scaled to all), the
-    batch in FP64 (replica by replica the same chains as the plain path) and
-    the batch on the FP32 table path.  g (2 tau_int of E in passes) and the
-    E variances come from each batch's own series; the plain path's are the
-    FP64 batch's.
+    GPU path -- each replica alone on the single-system sampler in FP64, the
+    reference's arithmetic; its pass time measured on a seeded sample of
+    replicas and scaled to all -- and the batch on the FP32 path with one
+    launch per half-sweep over all replicas (rotation mode 1).  g (2 tau_int
+    of E, in passes) and the E variances come from the batch's series; the
+    plain chains make the same moves in FP64 (the statistics tests compare
+    both precisions with the oracle), so their g is taken as the batch's.
+    The FP64 batch is timed on a 64-replica subset, for its rate only.
 
     Water dimers (config 3 molecules, T 0.74 K, P = 512, Q = 256, levels 4,
     reduced slices so that a series fits the run): the plain GPU path, the
-    batch with its rotational sweeps in the persistent kernel, and the batch
-    with delayed-acceptance rotational sweeps screened by the surrogate,
-    trained on the plain sampler's own rows."""
+    batch with its rotational sweeps in the persistent kernel, the batch with
+    its sweeps made by the delayed-acceptance kernels without a screen, and
+    with the screen of the surrogate trained on the plain sampler's own rows."""
     import numpy as np
     import pimc_gb300 as G
     import workloads as W
@@ -780,43 +822,42 @@ def run_matched_se(local, quick=False, c4_replicas=512, c4_passes=24, c3_replica
     ws = W.config4(n=c4_replicas)
     bm = sum(w.bead_moves_per_pass() for w in ws)
     rng = np.random.default_rng(11)
-    k = 8 if quick else 24
+    k = 6 if quick else 16
     idx = rng.choice(len(ws), size=min(k, len(ws)), replace=False)
     ts = np.array(single_pass_ms(ws, idx, 5))
     plain_ms = float(ts.mean()) * len(ws)
     plain_ms_se = float(ts.std(ddof=1) / np.sqrt(len(ts))) * len(ws) if len(ts) > 1 else None
-    arms, series = {}, {}
-    for mixed in (False, True):
-        b = G.Batch(ws, mixed=mixed)
-        E, ms = batch_series(b, 8 if quick else c4_passes, 21, 2 if quick else 4)
-        st, var = series_stats(E)
-        name = "batched_" + ("fp32" if mixed else "fp64")
-        arms[name] = dict(g=st["g"], var=var, pass_ms=ms, stats=st)
-        series[name] = E
-        b.close()
-    f64 = arms["batched_fp64"]
-    # the FP32 path's error against the FP64 path, replica by replica: the
-    # difference of the two <E> over its standard error (each from its own
-    # series, g-corrected)
-    e32, e64 = series["batched_fp32"], series["batched_fp64"]
-    se = np.sqrt(arms["batched_fp32"]["g"] * e32.var(axis=0, ddof=1) / len(e32) +
-                 f64["g"] * e64.var(axis=0, ddof=1) / len(e64))
-    z = (e32.mean(axis=0) - e64.mean(axis=0)) / np.maximum(se, 1e-300)
-    fp32_error = {"what": "per replica (<E>_fp32 - <E>_fp64) / combined SE over the series",
-                  "replicas": int(len(z)), "frac_within_2se": round(float(np.mean(np.abs(z) <= 2.0)), 4),
-                  "median_abs_z": round(float(np.median(np.abs(z))), 3),
-                  "mean_abs_diff_K": round(float(np.mean(np.abs(e32.mean(axis=0) - e64.mean(axis=0)))), 4)}
+    b = G.Batch(ws, mixed=True)
+    b.set_shape(*c4_shape)
+    b.set_rotation_mode(1)
+    E, ms = batch_series(b, 4 if quick else c4_passes, 21, 1)
+    tot, acc = b.counters()
+    b.close()
+    st, var = series_stats(E)
+    arms = {"batched_fp32": dict(g=st["g"], var=var, pass_ms=ms, stats=st)}
+    sub = [ws[i] for i in rng.choice(len(ws), size=min(64, len(ws)), replace=False)]
+    b = G.Batch(sub, mixed=False)
+    b.set_shape(*c4_shape)
+    b.set_rotation_mode(1)
+    _, ms64 = batch_series(b, 1, 22, 1)
+    b.close()
+    bm_sub = sum(w.bead_moves_per_pass() for w in sub)
     out["config4"] = {
         "workload": "config4: %d replicas of 1-8 water tops (caleng) on a 3 A chain + 0-32 pH2 (vcord), "
                     "T 0.5-2.0 K, P 512-2048, Q=P/4, ROTDENSI 1" % len(ws),
         "bead_moves_per_pass": bm,
         "plain": {"bead_moves_per_s": round(bm / (plain_ms / 1e3), 1), "pass_ms_all_replicas": round(plain_ms, 1),
                   "pass_ms_se": None if plain_ms_se is None else round(plain_ms_se, 1),
-                  "timed_replicas": int(len(idx)), "precision": "fp64", "g": f64["g"]},
+                  "timed_replicas": int(len(idx)), "precision": "fp64", "g": st["g"]},
         "arms": {n: {"bead_moves_per_s": round(bm / (a["pass_ms"] / 1e3), 1), "pass_ms": round(a["pass_ms"], 2),
-                     **a["stats"]} for n, a in arms.items()},
-        "time_to_se": matched(plain_ms, f64["g"], f64["var"], arms),
-        "fp32_vs_fp64": fp32_error}
+                     "precision": "fp32 tables and pair terms, fp64 sums and accepts", **a["stats"]}
+                 for n, a in arms.items()},
+        "accept_ratios": {"pH2 bisection": acc[1] / max(1, tot[1]), "water bisection": acc[4] / max(1, tot[4]),
+                          "rotation": acc[5] / max(1, tot[5])},
+        "batched_fp64_subset": {"replicas": len(sub), "pass_ms": round(ms64, 1),
+                                "bead_moves_per_s": round(bm_sub / (ms64 / 1e3), 1)},
+        "shape": {"warps_per_cta": c4_shape[0], "ctas_per_sm_bound": c4_shape[1], "rotation_mode": 1},
+        "time_to_se": matched(plain_ms, st["g"], var, arms)}
     # ---------------- water dimers with the surrogate
     dims = [W.config3(seed=300 + r, nslices=512, nrotslices=256, levels=4) for r in range(c3_replicas)]
     bmd = sum(w.bead_moves_per_pass() for w in dims)
@@ -840,10 +881,12 @@ def run_matched_se(local, quick=False, c4_replicas=512, c4_passes=24, c3_replica
                   np.zeros(256), r0.normal(0, 1 / 16, (256, 256)), np.zeros(256), r0.normal(0, 1 / 16, 256), 0.0)
     m.train(x, (e - mu) / sd, epochs=4 if quick else 12, batch=8192, lr=2e-3, seed=6)
     darms = {}
-    npd = 8 if quick else 32
+    npd = 6 if quick else 16
     for name, da in (("batched_plain", None), ("batched_da_exact", (None, sd)), ("batched_surrogate", (m, sd))):
         b = G.Batch(dims)
-        E, ms = batch_series(b, npd, 31, 2 if quick else 4, da=da)
+        if da is None:
+            b.set_rotation_mode(1)
+        E, ms = batch_series(b, npd, 31, 1 if quick else 2, da=da)
         st, var = series_stats(E)
         tot, acc = b.counters()
         darms[name] = dict(g=st["g"], var=var, pass_ms=ms, stats=st, accept_rot=float(acc[2] / max(1, tot[2])))

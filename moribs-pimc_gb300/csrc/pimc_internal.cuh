@@ -409,7 +409,8 @@ __device__ __forceinline__ void deleul(const double m1[9], const double m2in[9],
 // Only at a grid node can that choose the neighbouring cell, and vcalc's and
 // rotpro's one-sided differences are not continuous across a node; there the
 // coordinate is recomputed with the reference's own divisions.
-__device__ __forceinline__ bool near_node(double x) { return fabs(x - rint(x)) < 1e-9; }
+// f: the coordinate's distance above its cell's lower node, x - (int)x
+__device__ __forceinline__ bool near_node(double f) { return f < 1e-9 || f > 1.0 - 1e-9; }
 
 // rotden (rotden.f:1-31) -> rotpro (rotpro_sub.f:1-64) on the generalised
 // (theta, phi, chi) grid; returns the rho value, sets *bad on an index out
@@ -420,9 +421,9 @@ __device__ __forceinline__ double rotden_rho(const DevTables &t, const Frame &f1
   double rel[3];
   deleul(f1.m, f2.m, rel);
   double xt = rel[1] * t.d_dscale[0], xp = rel[0] * t.d_dscale[1], xc = rel[2] * t.d_dscale[2];
-  if (near_node(xt)) xt = (rel[1] * 180.0 / PIMC_PI) / t.dthd;        // rotden.f:22-24
-  if (near_node(xp)) xp = (rel[0] * 180.0 / PIMC_PI) / t.dphd;
-  if (near_node(xc)) xc = (rel[2] * 180.0 / PIMC_PI) / t.dchd;
+  if (near_node(xt - (double)(int)xt)) xt = (rel[1] * 180.0 / PIMC_PI) / t.dthd;   // rotden.f:22-24
+  if (near_node(xp - (double)(int)xp)) xp = (rel[0] * 180.0 / PIMC_PI) / t.dphd;
+  if (near_node(xc - (double)(int)xc)) xc = (rel[2] * 180.0 / PIMC_PI) / t.dchd;
   int ichi = (int)xc, iphi = (int)xp, ith = (int)xt;
   if (ichi > t.nch - 1 || ichi < 0) { ichi = 0; *bad = 1; }
   if (iphi > t.nph - 1 || iphi < 0) { iphi = 0; *bad = 1; }
@@ -524,14 +525,14 @@ __device__ __forceinline__ double vcord(const DevTables &t, const Frame &f, doub
   double r = rn * (1.0 / bo2ang);
   double xth = thewff * t.d_thscale;           // (theta * 180 / pi) / dth
   double xch = chiwff * t.d_chscale;
-  if (near_node(xth)) xth = ((thewff * 180.0) / pi) / t.dth3;      // vcord.f:90-91
-  if (near_node(xch)) xch = ((chiwff * 180.0) / pi) / t.dch3;
+  if (near_node(xth - (double)(int)xth)) xth = ((thewff * 180.0) / pi) / t.dth3;      // vcord.f:90-91
+  if (near_node(xch - (double)(int)xch)) xch = ((chiwff * 180.0) / pi) / t.dch3;
   // vcalc
   int maxrpt = t.rgrd - 1, mxthpt = t.thgrd - 1, mxchpt = t.chgrd - 1;
   if (r < t.rvmin) r = t.rvmin;
   if (r > t.rvmax) r = t.rvmax;
   double xr = (r - t.rvmin) * t.d_irstep;
-  if (near_node(xr)) {                                               // vcord.f:88, vcalc.f:21
+  if (near_node(xr - (double)(int)xr)) {                             // vcord.f:88, vcalc.f:21
     r = rn / bo2ang;
     if (r < t.rvmin) r = t.rvmin;
     if (r > t.rvmax) r = t.rvmax;
