@@ -67,7 +67,7 @@ def parse():
     ap.add_argument("--no-matched-se", action="store_true", help="skip the matched <E> SE measurement")
     ap.add_argument("--no-precision-error", action="store_true", help="skip the FP32-vs-FP64 per-replica comparison")
     ap.add_argument("--da-replicas", type=int, default=32, help="independent dimer systems swept at once")
-    ap.add_argument("--only", default=None, choices=["tables", "worm", "surrogate", "matched_se"],
+    ap.add_argument("--only", default=None, choices=["tables", "worm", "surrogate", "matched_se", "water_chains"],
                     help="run one companion measurement alone on cuda:0 and print its JSON (for profiling)")
     return ap.parse_args()
 
@@ -773,6 +773,24 @@ def matched(plain_pass_ms, plain_g, plain_var, arms, c=0.05):
     return out
 
 
+def run_water_chains(local, steps, n=64):
+    """A small case of the config-4 batch (the first n water-chain replicas'
+    worth of the family, FP32 path, rotation mode 1, shape 8 x 4): one
+    untimed pass, then `steps` passes timed with CUDA events (for profiling
+    the half-sweep kernel on a small case)."""
+    import pimc_gb300 as G
+    import workloads as W
+    ws = W.config4(n=n)
+    b = G.Batch(ws, device=local, mixed=True)
+    b.set_shape(8, 4)
+    b.set_rotation_mode(1)
+    _, ms = batch_series(b, steps, 3, 1)
+    bm = b.bead_moves_per_pass()
+    b.close()
+    return {"workload": "config4 family, %d replicas, FP32 path, rotation mode 1" % n, "pass_ms": round(ms, 2),
+            "bead_moves_per_s": round(bm / (ms / 1e3), 1)}
+
+
 def crossover(w, line):
     """What a surrogate row must cost to pay in a delayed-acceptance screen
     of the rotor-solvent terms: the time of one exact rotor-pH2 term as the
@@ -1071,7 +1089,8 @@ def main():
                    "worm": lambda: run_worm(local, not args.no_cpu, steps=args.steps, warmup=args.warmup,
                                             replicas=args.worm_replicas),
                    "surrogate": lambda: run_surrogate(local, replicas=args.da_replicas),
-                   "matched_se": lambda: run_matched_se(local, quick=args.quick_se)}[args.only]
+                   "matched_se": lambda: run_matched_se(local, quick=args.quick_se),
+                   "water_chains": lambda: run_water_chains(local, args.steps)}[args.only]
             print(json.dumps({"part": args.only, **run()}), flush=True)
         return 0
     line, w = run_gb300(args, rank, local, world, dist)
