@@ -730,6 +730,29 @@ def batch_series(b, npasses, seed, eq, da=None):
     return np.array(E), ms / npasses
 
 
+def work_units(w):
+    """A replica's work per pass for scaling sampled pass times: its
+    bead-moves, each weighted by the partners a move sums over."""
+    return w.bead_moves_per_pass() * max(1, w.natoms - 1)
+
+
+def scaled_total(ws, idx, ts):
+    """The plain path's time for all replicas from the timed sample: the
+    ratio estimator sum_r units_r * (sum_s t_s / sum_s units_s), and its
+    standard error from the sample's scatter about that ratio."""
+    import numpy as np
+    u = np.array([work_units(ws[i]) for i in idx], dtype=np.float64)
+    t = np.asarray(ts, dtype=np.float64)
+    total_u = float(sum(work_units(w) for w in ws))
+    ratio = t.sum() / u.sum()
+    resid = t - ratio * u
+    n = len(t)
+    se = None
+    if n > 1:
+        se = total_u * float(np.sqrt(np.sum(resid ** 2) / (n - 1) / n)) / float(u.mean())
+    return total_u * ratio, se
+
+
 def single_pass_ms(ws, idx, seed, mixed=False):
     """One production pass of each chosen system on its own handle (the plain
     GPU path), CUDA events on the handle's stream after one untimed pass."""
@@ -813,7 +836,7 @@ def crossover(w, line):
             "what": "a screen spares exact terms only if a surrogate row costs less than the terms it replaces"}
 
 
-def run_matched_se(local, quick=False, c4_replicas=512, c4_passes=8, c3_replicas=64, c4_shape=(8, 4)):
+def run_matched_se(local, quick=False, c4_replicas=512, c4_passes=8, c3_replicas=512, c4_shape=(8, 4)):
     """The metric itself: bead-moves/s at matched <E> standard error.
 
     Water chains (config 4): c4_replicas replicas of 1-8 water tops on a
@@ -840,11 +863,10 @@ def run_matched_se(local, quick=False, c4_replicas=512, c4_passes=8, c3_replicas
     ws = W.config4(n=c4_replicas)
     bm = sum(w.bead_moves_per_pass() for w in ws)
     rng = np.random.default_rng(11)
-    k = 6 if quick else 16
+    k = 8 if quick else 40
     idx = rng.choice(len(ws), size=min(k, len(ws)), replace=False)
     ts = np.array(single_pass_ms(ws, idx, 5))
-    plain_ms = float(ts.mean()) * len(ws)
-    plain_ms_se = float(ts.std(ddof=1) / np.sqrt(len(ts))) * len(ws) if len(ts) > 1 else None
+    plain_ms, plain_ms_se = scaled_total(ws, idx, ts)
     b = G.Batch(ws, mixed=True)
     b.set_shape(*c4_shape)
     b.set_rotation_mode(1)
@@ -866,7 +888,8 @@ def run_matched_se(local, quick=False, c4_replicas=512, c4_passes=8, c3_replicas
         "bead_moves_per_pass": bm,
         "plain": {"bead_moves_per_s": round(bm / (plain_ms / 1e3), 1), "pass_ms_all_replicas": round(plain_ms, 1),
                   "pass_ms_se": None if plain_ms_se is None else round(plain_ms_se, 1),
-                  "timed_replicas": int(len(idx)), "precision": "fp64", "g": st["g"]},
+                  "timed_replicas": int(len(idx)), "precision": "fp64", "g": st["g"],
+                  "scaling": "ratio estimator on bead-moves x partners per replica"},
         "arms": {n: {"bead_moves_per_s": round(bm / (a["pass_ms"] / 1e3), 1), "pass_ms": round(a["pass_ms"], 2),
                      "precision": "fp32 tables and pair terms, fp64 sums and accepts", **a["stats"]}
                  for n, a in arms.items()},
@@ -877,10 +900,12 @@ def run_matched_se(local, quick=False, c4_replicas=512, c4_passes=8, c3_replicas
         "shape": {"warps_per_cta": c4_shape[0], "ctas_per_sm_bound": c4_shape[1], "rotation_mode": 1},
         "time_to_se": matched(plain_ms, st["g"], var, arms)}
     # ---------------- water dimers with the surrogate
-    dims = [W.config3(seed=300 + r, nslices=512, nrotslices=256, levels=4) for r in range(c3_replicas)]
+    d0 = W.config3(seed=300, nslices=512, nrotslices=256, levels=4)
+    dims = [d0] + [W.config3(seed=300 + r, nslices=512, nrotslices=256, levels=4, tables=d0.tables)
+                   for r in range(1, c3_replicas)]
     bmd = sum(w.bead_moves_per_pass() for w in dims)
     ts = np.array(single_pass_ms(dims, range(min(4, len(dims))), 7))
-    plain_d_ms = float(ts.mean()) * len(dims)
+    plain_d_ms = float(ts.mean()) * len(dims)           # identical systems: the mean pass time
     # training rows from the plain sampler (dimer features, exact caleng energies)
     s = G.Sampler(dims[0])
     s.run_passes(2, 3)
@@ -899,7 +924,7 @@ def run_matched_se(local, quick=False, c4_replicas=512, c4_passes=8, c3_replicas
                   np.zeros(256), r0.normal(0, 1 / 16, (256, 256)), np.zeros(256), r0.normal(0, 1 / 16, 256), 0.0)
     m.train(x, (e - mu) / sd, epochs=4 if quick else 12, batch=8192, lr=2e-3, seed=6)
     darms = {}
-    npd = 6 if quick else 16
+    npd = 6 if quick else 32
     for name, da in (("batched_plain", None), ("batched_da_exact", (None, sd)), ("batched_surrogate", (m, sd))):
         b = G.Batch(dims)
         if da is None:

@@ -437,7 +437,8 @@ def config1(seed=4321, nslices=1024, nrotslices=256, n_h2=64, grid3d=(200, 60, 6
                     pindex=np.arange(n_h2 + 1, dtype=np.int32), chi_fold_deg=90)
 
 
-def config3(seed=77, nslices=4096, nrotslices=2048, griddens=(61, 121, 121), sep=3.0, rot_den_type=0, levels=5):
+def config3(seed=77, nslices=4096, nrotslices=2048, griddens=(61, 121, 121), sep=3.0, rot_den_type=0, levels=5,
+            tables=None):
     """2 rigid water-like asymmetric tops (A,B,C = 27.9, 14.5, 9.3 cm^-1) at 0.74 K, caleng potential.
     rot_den_type 1: the analytic rattle-and-shake propagator (ROTDENSI 1) in
     the moves; the table is still loaded for the E^2 estimator."""
@@ -446,8 +447,9 @@ def config3(seed=77, nslices=4096, nrotslices=2048, griddens=(61, 121, 121), sep
                   fpot="none")]
     abc = (27.9, 14.5, 9.3)
     tau_rot = 1.0 / (T * nrotslices)
-    rho, er, esq = rs_top_density(*griddens, abc, tau_rot)
-    tables = dict(nth=griddens[0], nph=griddens[1], nch=griddens[2], rhoprp=rho, erotpr=er, erotsq=esq)
+    if tables is None:       # else the density tables of another dimer of the same T and Q
+        rho, er, esq = rs_top_density(*griddens, abc, tau_rot)
+        tables = dict(nth=griddens[0], nph=griddens[1], nch=griddens[2], rhoprp=rho, erotpr=er, erotsq=esq)
     rng = np.random.default_rng(seed)
     pos = np.array([[0.0, 0.0, 0.0], [sep, 0.0, 0.0]])
     coords, angles = initial_path(2, nslices, pos, rng, jitter=0.01)
@@ -531,7 +533,7 @@ def config4(n=512, seed=4040, p_choices=(512, 1024, 2048), n_rot=(1, 8), n_h2=(0
     ps = rng.choice(np.asarray(p_choices), size=n)
     ts = rng.uniform(t_range[0], t_range[1], size=n)
     return [water_chain(int(nr[r]), int(nh[r]), int(ps[r]), int(ps[r]) // 4, float(ts[r]), [seed, r], tables,
-                        name="config4-replica-%d" % r) for r in range(n)]
+                        rtstep=0.1, name="config4-replica-%d" % r) for r in range(n)]
 
 
 # ------------------------------------------------ reference file formats
