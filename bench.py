@@ -39,9 +39,10 @@ for p in (PKG, os.path.join(REPO, "oracle")):
         sys.path.insert(0, p)
 
 METRIC = "bead-moves/s on 1 GB300: plain vs surrogate+batched, at matched <E> error"
-# DRAM traffic per launch from ncu captures of the bench's own workload:
-# {(kind, mixed): {"bytes": ..., "commit": ...}}, kind 2 = the rotational sweeps
-TRAFFIC_CAPTURE = {}
+# DRAM traffic per launch from ncu captures of the bench's own workload, and
+# the FP64 pipe's activity in the same capture:
+# {(kind, mixed): {"bytes": ..., "fp64_pipe": ..., "commit": ...}}, kind 2 = the rotational sweeps
+TRAFFIC_CAPTURE = {(2, False): {"bytes": 6116608 + 49664, "fp64_pipe": 0.5536, "commit": "d5a7f2a"}}
 UNIT = "bead-moves/s"
 WORKLOAD = "config1: 1 asymmetric-top SO2 + 64 pH2, T=0.37 K, P=1024, Q=256, L=3, plain method"
 
@@ -63,11 +64,14 @@ def parse():
     ap.add_argument("--no-worm", action="store_true", help="skip the worm-algorithm pass measurement")
     ap.add_argument("--no-surrogate", action="store_true", help="skip the surrogate / delayed-acceptance measurement")
     ap.add_argument("--worm-replicas", type=int, default=32, help="independent worm chains run at once")
-    ap.add_argument("--quick-se", action="store_true", help="short series for the matched-SE measurement")
+    ap.add_argument("--se-mode", default="default", choices=["quick", "default", "full"],
+                    help="matched-SE measurement: short series (quick), the bench line's (default), or more "
+                         "sampled plain replicas and the half-sweep dimer arm (full)")
     ap.add_argument("--no-matched-se", action="store_true", help="skip the matched <E> SE measurement")
     ap.add_argument("--no-precision-error", action="store_true", help="skip the FP32-vs-FP64 per-replica comparison")
     ap.add_argument("--da-replicas", type=int, default=32, help="independent dimer systems swept at once")
-    ap.add_argument("--only", default=None, choices=["tables", "worm", "surrogate", "matched_se", "water_chains"],
+    ap.add_argument("--only", default=None,
+                    choices=["tables", "worm", "surrogate", "matched_se", "water_chains", "config_table"],
                     help="run one companion measurement alone on cuda:0 and print its JSON (for profiling)")
     return ap.parse_args()
 
@@ -374,6 +378,7 @@ def run_gb300(args, rank, local, world, dist):
                          "peak_gflops": round(fp64_peak, 1), "peak_source": "measured in this run (pimc_fp64_peak: "
                          "independent FP64 FMA chains, CUDA events)",
                          "fp64_frac": round(fp64_rate / fp64_peak, 4) if fp64_rate else None,
+                         "fp64_pipe_active_frac": traffic.get("fp64_pipe") if traffic else None,
                          "flop_model": "per slice move 2R(N-1) vcord x %d + 4 rotden x %d + %d (reference source "
                                        "operations)" % (FLOP_VCORD, FLOP_ROTDEN, FLOP_ACCEPT)},
                 "kernel": kname, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
@@ -777,22 +782,111 @@ def single_pass_ms(ws, idx, seed, mixed=False):
     return out
 
 
-def matched(plain_pass_ms, plain_g, plain_var, arms, c=0.05):
+def matched(plain_pass_ms, plain_g, arms, c=0.05):
     """Time for every replica's <E> to reach a standard error of c times its
-    own plain-path E fluctuation: n = g (var_arm / var_plain) / c^2 passes;
-    the plain path runs the replicas one after another (its pass time is the
-    sum over replicas), a batch runs them together."""
+    own E fluctuation sd(E).  Every arm samples the same distribution (the
+    exactness tests), so sd(E) is common to them and an arm needs
+    n = g / c^2 passes, g its statistical inefficiency; the plain path runs
+    the replicas one after another (its pass time is the sum over replicas),
+    a batch runs them together.  var_ratio (each arm's replica variances over
+    the mean of all arms') is reported as a check, not used."""
     import numpy as np
     n_plain = plain_g / (c * c)
     t_plain = n_plain * plain_pass_ms / 1e3
     out = {"target": "SE(<E>) = %.2f sd(E) per replica" % c,
            "plain": {"passes": round(n_plain, 1), "seconds": round(t_plain, 2)}}
+    vbar = np.mean([np.sum(a["var"]) for a in arms.values()])
     for name, a in arms.items():
-        v = float(np.sum(a["var"]) / np.sum(plain_var))
-        n = a["g"] * v / (c * c)
+        n = a["g"] / (c * c)
         t = n * a["pass_ms"] / 1e3
-        out[name] = {"passes": round(n, 1), "seconds": round(t, 3), "var_ratio": round(v, 4),
-                     "vs_plain": round(t_plain / t, 2)}
+        out[name] = {"passes": round(n, 1), "seconds": round(t, 3),
+                     "var_ratio": round(float(np.sum(a["var"]) / vbar), 4), "vs_plain": round(t_plain / t, 2)}
+    return out
+
+
+def cpu_rate(ws, seconds, nthreads):
+    """Bead-moves/s of the oracle port of the reference schedule (its timing
+    build) over the systems ws in turn, each for an equal share of `seconds`
+    (time slices 0, 1, ... of one pass, centroid moves at slice 0)."""
+    import oracle as O
+    bm, el = 0.0, 0.0
+    for w in ws:
+        o = O.Oracle(w, timing=True)
+        t0 = time.perf_counter()
+        done = 0
+        while True:
+            st, b = o.run_steps(done, 4, seed=99, nthreads=nthreads)
+            if st != 0:
+                raise RuntimeError("oracle run_steps failed: %d" % st)
+            bm += b
+            done += 4
+            if time.perf_counter() - t0 >= seconds / len(ws) or done >= w.nslices:
+                break
+        el += time.perf_counter() - t0
+    return bm / el
+
+
+def gpu_pass_rate(w, local, mixed, passes=3):
+    """Bead-moves/s of the single-system sampler on w: one untimed pass, then
+    `passes` passes timed with CUDA events on the handle's stream."""
+    import torch
+    import pimc_gb300 as G
+    s = G.Sampler(w, device=local, mixed=mixed)
+    s.run_passes(1, 3)
+    s.synchronize()
+    ext = torch.cuda.ExternalStream(s.stream())
+    with torch.cuda.stream(ext):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        s.run_passes(passes, 4)
+        e1.record(ext)
+    s.synchronize()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / passes
+    s.close()
+    return w.bead_moves_per_pass() / (ms / 1e3)
+
+
+def run_config_table(local, cpu_seconds=6.0):
+    """Per configuration: the CPU oracle port of the reference schedule on all
+    host cores and on one, the single-system GPU sampler in FP64 and on the
+    FP32 path, and for the replica families the batch (FP32 path).  Replica
+    families: the CPU and plain-GPU rates on a seeded sample of 8 replicas,
+    the batch on all of them."""
+    import numpy as np
+    import pimc_gb300 as G
+    import workloads as W
+    ncores = os.cpu_count() or 1
+    rng = np.random.default_rng(17)
+    out = {}
+    singles = {"config0": W.config0(), "config1": W.config1(), "config3": W.config3()}
+    for name, w in singles.items():
+        out[name] = {"cpu_all_cores": round(cpu_rate([w], cpu_seconds, ncores), 1),
+                     "cpu_one_core": round(cpu_rate([w], cpu_seconds / 2, 1), 1),
+                     "gpu_fp64": round(gpu_pass_rate(w, local, False), 1),
+                     "gpu_fp32": round(gpu_pass_rate(w, local, True), 1)}
+    for name, ws, shape, mode in (("config2", W.config2(), None, 0), ("config4", W.config4(), (8, 4), 1)):
+        idx = rng.choice(len(ws), size=8, replace=False)
+        sample = [ws[i] for i in idx]
+        bm_s = sum(w.bead_moves_per_pass() for w in sample)
+        t64 = sum(w.bead_moves_per_pass() / gpu_pass_rate(w, local, False, passes=1) for w in sample)
+        t32 = sum(w.bead_moves_per_pass() / gpu_pass_rate(w, local, True, passes=1) for w in sample)
+        b = G.Batch(ws, device=local, mixed=True)
+        if shape:
+            b.set_shape(*shape)
+        if mode:
+            b.set_rotation_mode(mode)
+        _, ms = batch_series(b, 2, 23, 1)
+        bm = b.bead_moves_per_pass()
+        b.close()
+        out[name] = {"cpu_all_cores": round(cpu_rate(sample, cpu_seconds, ncores), 1),
+                     "cpu_one_core": round(cpu_rate(sample, cpu_seconds / 2, 1), 1),
+                     "gpu_fp64": round(bm_s / t64, 1), "gpu_fp32": round(bm_s / t32, 1),
+                     "gpu_batched_fp32": round(bm / (ms / 1e3), 1), "replicas": len(ws),
+                     "sampled_replicas": [int(i) for i in idx]}
+    out["cores"] = ncores
+    out["host_cpu"] = host_cpu()
     return out
 
 
@@ -836,7 +930,7 @@ def crossover(w, line):
             "what": "a screen spares exact terms only if a surrogate row costs less than the terms it replaces"}
 
 
-def run_matched_se(local, quick=False, c4_replicas=512, c4_passes=8, c3_replicas=512, c4_shape=(8, 4)):
+def run_matched_se(local, mode="default", c4_replicas=512, c3_replicas=512, c4_shape=(8, 4)):
     """The metric itself: bead-moves/s at matched <E> standard error.
 
     Water chains (config 4): c4_replicas replicas of 1-8 water tops on a
@@ -845,42 +939,60 @@ def run_matched_se(local, quick=False, c4_replicas=512, c4_passes=8, c3_replicas
     reference's arithmetic; its pass time measured on a seeded sample of
     replicas and scaled to all -- and the batch on the FP32 path with one
     launch per half-sweep over all replicas (rotation mode 1).  g (2 tau_int
-    of E, in passes) and the E variances come from the batch's series; the
-    plain chains make the same moves in FP64 (the statistics tests compare
-    both precisions with the oracle), so their g is taken as the batch's.
-    The FP64 batch is timed on a 64-replica subset, for its rate only.
+    of E, in passes) comes from the batch's series; the plain chains make the
+    same moves in FP64 (the statistics tests compare both precisions with the
+    oracle), so their g is taken as the batch's.  The FP64 batch is timed on
+    a replica subset, for its rate only.
 
     Water dimers (config 3 molecules, T 0.74 K, P = 512, Q = 256, levels 4,
     reduced slices so that a series fits the run): the plain GPU path, the
-    batch with its rotational sweeps in the persistent kernel, the batch with
-    its sweeps made by the delayed-acceptance kernels without a screen, and
-    with the screen of the surrogate trained on the plain sampler's own rows."""
+    batch with its rotational sweeps made by the delayed-acceptance kernels
+    without a screen (plain Metropolis; its g is the plain path's) and with
+    the screen of the surrogate trained on the plain sampler's own rows; in
+    the "full" mode also the batch with its sweeps in the half-sweep kernel.
+
+    mode: "quick" (short series, for tests of the harness), "default" (the
+    bench line), "full" (more sampled plain replicas, the extra dimer arm)."""
     import numpy as np
     import pimc_gb300 as G
     import workloads as W
-    out = {}
+    quick, full = mode == "quick", mode == "full"
+    out = {"mode": mode}
+    secs = {}
+    t0 = time.perf_counter()
+
+    def lap(name):
+        nonlocal t0
+        t1 = time.perf_counter()
+        secs[name] = round(t1 - t0, 1)
+        t0 = t1
     # ---------------- config 4
     ws = W.config4(n=c4_replicas)
+    lap("config4_workloads")
     bm = sum(w.bead_moves_per_pass() for w in ws)
     rng = np.random.default_rng(11)
-    k = 8 if quick else 40
+    k = 8 if quick else (40 if full else 24)
     idx = rng.choice(len(ws), size=min(k, len(ws)), replace=False)
     ts = np.array(single_pass_ms(ws, idx, 5))
     plain_ms, plain_ms_se = scaled_total(ws, idx, ts)
+    lap("config4_plain")
     b = G.Batch(ws, mixed=True)
     b.set_shape(*c4_shape)
     b.set_rotation_mode(1)
-    E, ms = batch_series(b, 4 if quick else c4_passes, 21, 1)
+    lap("config4_batch_setup")
+    E, ms = batch_series(b, 4 if quick else 8, 21, 1)
     tot, acc = b.counters()
     b.close()
+    lap("config4_batch_series")
     st, var = series_stats(E)
     arms = {"batched_fp32": dict(g=st["g"], var=var, pass_ms=ms, stats=st)}
-    sub = [ws[i] for i in rng.choice(len(ws), size=min(64, len(ws)), replace=False)]
+    sub = [ws[i] for i in rng.choice(len(ws), size=min(64 if full else 16, len(ws)), replace=False)]
     b = G.Batch(sub, mixed=False)
     b.set_shape(*c4_shape)
     b.set_rotation_mode(1)
     _, ms64 = batch_series(b, 1, 22, 1)
     b.close()
+    lap("config4_fp64_subset")
     bm_sub = sum(w.bead_moves_per_pass() for w in sub)
     out["config4"] = {
         "workload": "config4: %d replicas of 1-8 water tops (caleng) on a 3 A chain + 0-32 pH2 (vcord), "
@@ -891,19 +1003,20 @@ def run_matched_se(local, quick=False, c4_replicas=512, c4_passes=8, c3_replicas
                   "timed_replicas": int(len(idx)), "precision": "fp64", "g": st["g"],
                   "scaling": "ratio estimator on bead-moves x partners per replica"},
         "arms": {n: {"bead_moves_per_s": round(bm / (a["pass_ms"] / 1e3), 1), "pass_ms": round(a["pass_ms"], 2),
-                     "precision": "fp32 tables and pair terms, fp64 sums and accepts", **a["stats"]}
+                     "precision": "fp32 tables, pair terms and densities, fp64 sums and accepts", **a["stats"]}
                  for n, a in arms.items()},
         "accept_ratios": {"pH2 bisection": acc[1] / max(1, tot[1]), "water bisection": acc[4] / max(1, tot[4]),
                           "rotation": acc[5] / max(1, tot[5])},
         "batched_fp64_subset": {"replicas": len(sub), "pass_ms": round(ms64, 1),
                                 "bead_moves_per_s": round(bm_sub / (ms64 / 1e3), 1)},
         "shape": {"warps_per_cta": c4_shape[0], "ctas_per_sm_bound": c4_shape[1], "rotation_mode": 1},
-        "time_to_se": matched(plain_ms, st["g"], var, arms)}
+        "time_to_se": matched(plain_ms, st["g"], arms)}
     # ---------------- water dimers with the surrogate
     d0 = W.config3(seed=300, nslices=512, nrotslices=256, levels=4)
     dims = [d0] + [W.config3(seed=300 + r, nslices=512, nrotslices=256, levels=4, tables=d0.tables)
                    for r in range(1, c3_replicas)]
     bmd = sum(w.bead_moves_per_pass() for w in dims)
+    lap("dimer_workloads")
     ts = np.array(single_pass_ms(dims, range(min(4, len(dims))), 7))
     plain_d_ms = float(ts.mean()) * len(dims)           # identical systems: the mean pass time
     # training rows from the plain sampler (dimer features, exact caleng energies)
@@ -923,29 +1036,37 @@ def run_matched_se(local, quick=False, c4_replicas=512, c4_passes=8, c3_replicas
     m.set_weights(r0.normal(0, 1 / np.sqrt(6), (6, 256)), np.zeros(256), r0.normal(0, 1 / 16, (256, 256)),
                   np.zeros(256), r0.normal(0, 1 / 16, (256, 256)), np.zeros(256), r0.normal(0, 1 / 16, 256), 0.0)
     m.train(x, (e - mu) / sd, epochs=4 if quick else 12, batch=8192, lr=2e-3, seed=6)
+    lap("dimer_plain_and_training")
     darms = {}
     npd = 6 if quick else 32
-    for name, da in (("batched_plain", None), ("batched_da_exact", (None, sd)), ("batched_surrogate", (m, sd))):
+    eq = 1 if quick else 4
+    runs = [("batched_da_exact", (None, sd)), ("batched_surrogate", (m, sd))]
+    if full:
+        runs.append(("batched_plain", None))
+    for name, da in runs:
         b = G.Batch(dims)
         if da is None:
             b.set_rotation_mode(1)
-        E, ms = batch_series(b, npd, 31, 1 if quick else 2, da=da)
+        E, ms = batch_series(b, npd, 31, eq, da=da)
         st, var = series_stats(E)
         tot, acc = b.counters()
         darms[name] = dict(g=st["g"], var=var, pass_ms=ms, stats=st, accept_rot=float(acc[2] / max(1, tot[2])))
         b.close()
+        lap("dimer_" + name)
     m.close()
-    pe = darms["batched_plain"]
+    out["section_seconds"] = secs
+    g_plain = darms["batched_da_exact"]["g"]
     out["config3_dimers"] = {
         "workload": "config3 molecules: %d water dimers (caleng), T=0.74 K, P=512, Q=256, levels 4 (slices "
                     "reduced from 4096/2048 so that a series fits the run)" % len(dims),
         "bead_moves_per_pass": bmd,
         "plain": {"bead_moves_per_s": round(bmd / (plain_d_ms / 1e3), 1), "pass_ms_all_replicas": round(plain_d_ms, 1),
-                  "timed_replicas": int(len(ts)), "precision": "fp64", "g": pe["g"]},
+                  "timed_replicas": int(len(ts)), "precision": "fp64", "g": g_plain,
+                  "g_source": "the unscreened batch arm (the same Metropolis moves)"},
         "arms": {n: {"bead_moves_per_s": round(bmd / (a["pass_ms"] / 1e3), 1), "pass_ms": round(a["pass_ms"], 2),
                      "accept_rot": round(a["accept_rot"], 4), **a["stats"]} for n, a in darms.items()},
         "surrogate": {"training_rows": int(len(x)), "energy_sd_K": round(sd, 2)},
-        "time_to_se": matched(plain_d_ms, pe["g"], pe["var"], darms)}
+        "time_to_se": matched(plain_d_ms, g_plain, darms)}
     return out
 
 
@@ -1114,8 +1235,9 @@ def main():
                    "worm": lambda: run_worm(local, not args.no_cpu, steps=args.steps, warmup=args.warmup,
                                             replicas=args.worm_replicas),
                    "surrogate": lambda: run_surrogate(local, replicas=args.da_replicas),
-                   "matched_se": lambda: run_matched_se(local, quick=args.quick_se),
-                   "water_chains": lambda: run_water_chains(local, args.steps)}[args.only]
+                   "matched_se": lambda: run_matched_se(local, mode=args.se_mode),
+                   "water_chains": lambda: run_water_chains(local, args.steps),
+                   "config_table": lambda: run_config_table(local)}[args.only]
             print(json.dumps({"part": args.only, **run()}), flush=True)
         return 0
     line, w = run_gb300(args, rank, local, world, dist)
@@ -1133,7 +1255,7 @@ def main():
         if not args.no_surrogate and world == 1:
             line["surrogate"] = run_surrogate(local, replicas=args.da_replicas)
         if not args.no_matched_se and world == 1:
-            line["matched_se"] = run_matched_se(local, quick=args.quick_se)
+            line["matched_se"] = run_matched_se(local, mode=args.se_mode)
         if "surrogate" in line and "companion" in line:
             line["surrogate_crossover"] = crossover(w, line)
         print(json.dumps(line), flush=True)

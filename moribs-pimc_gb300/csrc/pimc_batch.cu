@@ -189,7 +189,7 @@ __device__ int warp_rot(const Ctx &c, Frame *frames, int g0, int q, const double
   if (q2 >= Q) q2 -= Q;
   const int r = g0 - s.rot_first;
   const int i0 = r * Q + q0, i1 = r * Q + q, i2 = r * Q + q2;
-  const bool need64 = !MIX || s.nrotors > 1;
+  const bool need64 = !MIX;                     // on the FP32 path the evaluation reads the float frames only
   const bool use_links = Q >= 3;                // link cache (with Q < 3 both links join the same two slices)
   if (lane == 0) {
     w.bad = 0;
@@ -290,11 +290,8 @@ __device__ int warp_rot(const Ctx &c, Frame *frames, int g0, int q, const double
       const Frame &fb = (lane == 0) ? w.fo[1] : (lane == 2 ? w.fn : w.fo[2]);
       if (MIX && s.rot_den_type == 0) {
         rho = (double)rotden_rho32(c.t, fa.mf, fb.mf, &bad);
-      } else if (MIX && !need64 && lane >= 2) {
-        Frame f64;
-        make_frame64(w.ang_new[0], w.ang_new[1], w.ang_new[2], f64);
-        rho = (lane == 2) ? link_density(c, false, fa, f64, nullptr, nullptr, &bad)
-                          : link_density(c, false, f64, fb, nullptr, nullptr, &bad);
+      } else if (MIX) {
+        rho = s.rot_odevn == -1 ? (double)rsrot32(fa.mf, fb.mf, s.rs_coef) : 0.0;
       } else {
         rho = link_density(c, false, fa, fb, nullptr, nullptr, &bad);
       }

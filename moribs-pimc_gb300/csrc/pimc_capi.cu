@@ -297,6 +297,14 @@ static pimc_status build_devsys(const pimc_system &s, DevSys &d)
   d.rn_ratio = s.rn_ratio > 0 ? s.rn_ratio : 1;
   d.rot_eoff = s.rot_eoff;
   for (int k = 0; k < 3; k++) { d.abc[k] = s.rot_abc[k]; d.box[k] = s.box[k]; }
+  {
+    double b[3];
+    for (int k = 0; k < 3; k++) b[k] = d.abc[k] > 0.0 ? 1.0 / d.abc[k] : 0.0;
+    d.rs_coef[0] = (float)(b[0] - b[1] - b[2]);
+    d.rs_coef[1] = (float)(b[1] - b[2] - b[0]);
+    d.rs_coef[2] = (float)(b[2] - b[0] - b[1]);
+    d.rs_scale = d.rot_tau > 0.0 ? (float)(1.0 / (4.0 * (d.rot_tau / PIMC_WNO2K))) : 0.0f;
+  }
   d.minimage = s.minimage;
   d.wait_ns = 2000000000ull;
   return PIMC_OK;
@@ -1321,6 +1329,10 @@ extern "C" pimc_status pimc_da_samples(pimc_handle *h, float *feat, float *energ
   void *buf;
   if ((e = scratch(h, (size_t)P * 7 * sizeof(float) + 512, &buf))) return e;
   float *df = (float *)buf, *de = df + (size_t)P * 6;
+  if (h->ctx.s.mixed) {              // the FP32 moves leave the double frames to be derived
+    launch_refresh_frames(h->ctx, h->frames, h->stream);
+    h->launches++;
+  }
   h->launches += launch_da_samples(h->ctx, h->frames, df, de, h->stream);
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(feat, df, (size_t)P * 6 * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
@@ -1353,6 +1365,10 @@ extern "C" pimc_status pimc_da_sweeps(pimc_handle *h, pimc_mlp *m, int nsweeps, 
   // same sweep count, seed, surrogate, scale and scratch come back
   auto record = [&]() -> long long {
     long long n = 1;
+    if (d.mixed) {                   // the delayed-acceptance moves read the double frames
+      launch_refresh_frames(h->ctx, h->frames, h->stream);
+      n++;
+    }
     launch_pass_begin(h->pass, h->stream);
     for (int sw = 0; sw < nsweeps; sw++)
       for (int par = 0; par < 2; par++)
@@ -2358,6 +2374,10 @@ static pimc_status batch_da_run(pimc_batch *b, pimc_mlp *m, int count, int passe
   };
   auto record = [&]() -> long long {
     long long n = 0;
+    if (b->mixed) {                  // the FP32 rotational moves leave the double frames to be derived
+      launch_batch_refresh(b->d_reps, b->n, 0, h->stream);
+      n++;
+    }
     if (passes) {
       // the translational moves advance the pass counters that key the sweeps' draws
       launch_batch_pass(b->d_reps, b->d_order, b->n, seed, b->d_work, b->mixed, b->warps, b->minb, nctas, h->stream,

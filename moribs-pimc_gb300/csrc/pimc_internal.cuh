@@ -83,6 +83,8 @@ struct DevSys {
   double tau, rot_tau, beta, temperature, rtstep;
   int ispher, rot_den_type, rot_odevn, rn_ratio;
   double rot_eoff, abc[3];
+  float rs_coef[3];            // FP32 rattle-and-shake density: 1/A - 1/B - 1/C and its cyclic forms (rotden.f:218-286)
+  float rs_scale;              // 1 / (4 tau_rot) in cm: the log-density difference's factor in the accept (mc_piqmc.cc:1145-1178)
   int minimage;
   double box[3];
   int mixed;                   // 1: FP32 table interpolation with FP64 sums
@@ -205,12 +207,11 @@ __device__ __forceinline__ void unit_vector32(float phi, float cost, float v[3])
   v[2] = cost;
 }
 
-// the double-precision frame (m, hz_norm) only
-__device__ __forceinline__ void make_frame64(double phi, double cost, double chi, Frame &f)
+// the double-precision frame (m, hz_norm) from the angles and the sines and
+// cosines of phi and chi
+__device__ __forceinline__ void frame_from_sincos(double phi, double cost, double chi, double sp, double cp,
+                                                  double sk, double ck, Frame &f)
 {
-  double sp, cp, sk, ck;
-  sincos(phi, &sp, &cp);
-  sincos(chi, &sk, &ck);
   double ct = cost, st = sqrt((1.0 - cost) * (1.0 + cost));
   f.e[0] = phi;
   f.e[1] = cost;
@@ -229,6 +230,15 @@ __device__ __forceinline__ void make_frame64(double phi, double cost, double chi
   s = s + f.m[5] * f.m[5];
   s = s + f.m[8] * f.m[8];
   f.hz_norm = sqrt(s);
+}
+
+// the double-precision frame (m, hz_norm) only
+__device__ __forceinline__ void make_frame64(double phi, double cost, double chi, Frame &f)
+{
+  double sp, cp, sk, ck;
+  sincos(phi, &sp, &cp);
+  sincos(chi, &sk, &ck);
+  frame_from_sincos(phi, cost, chi, sp, cp, sk, ck, f);
 }
 
 __device__ __forceinline__ void make_frame(double phi, double cost, double chi, Frame &f)
@@ -421,16 +431,28 @@ __device__ __forceinline__ double rotden_rho(const DevTables &t, const Frame &f1
   double rel[3];
   deleul(f1.m, f2.m, rel);
   double xt = rel[1] * t.d_dscale[0], xp = rel[0] * t.d_dscale[1], xc = rel[2] * t.d_dscale[2];
-  if (near_node(xt - (double)(int)xt)) xt = (rel[1] * 180.0 / PIMC_PI) / t.dthd;   // rotden.f:22-24
-  if (near_node(xp - (double)(int)xp)) xp = (rel[0] * 180.0 / PIMC_PI) / t.dphd;
-  if (near_node(xc - (double)(int)xc)) xc = (rel[2] * 180.0 / PIMC_PI) / t.dchd;
   int ichi = (int)xc, iphi = (int)xp, ith = (int)xt;
-  if (ichi > t.nch - 1 || ichi < 0) { ichi = 0; *bad = 1; }
-  if (iphi > t.nph - 1 || iphi < 0) { iphi = 0; *bad = 1; }
-  if (ith > t.nth - 1 || ith < 0) { ith = 0; *bad = 1; }
+  double fc = xc - (double)ichi, fp = xp - (double)iphi, ft = xt - (double)ith;
+  if (near_node(ft)) {                                               // rotden.f:22-24
+    xt = (rel[1] * 180.0 / PIMC_PI) / t.dthd;
+    ith = (int)xt;
+    ft = xt - (double)ith;
+  }
+  if (near_node(fp)) {
+    xp = (rel[0] * 180.0 / PIMC_PI) / t.dphd;
+    iphi = (int)xp;
+    fp = xp - (double)iphi;
+  }
+  if (near_node(fc)) {
+    xc = (rel[2] * 180.0 / PIMC_PI) / t.dchd;
+    ichi = (int)xc;
+    fc = xc - (double)ichi;
+  }
+  if (ichi > t.nch - 1 || ichi < 0) { ichi = 0; fc = xc; *bad = 1; }
+  if (iphi > t.nph - 1 || iphi < 0) { iphi = 0; fp = xp; *bad = 1; }
+  if (ith > t.nth - 1 || ith < 0) { ith = 0; ft = xt; *bad = 1; }
   size_t nph = t.nph, nch = t.nch;
   size_t i0 = ((size_t)ith * nph + iphi) * nch + ichi;
-  double fc = xc - (double)ichi, fp = xp - (double)iphi, ft = xt - (double)ith;
   double r0 = __ldg(t.rho + i0);
   double dc = 0.0, dp = 0.0, dt = 0.0;
   size_t ic = i0 + 1, ip = i0 + nch, itt = i0 + nph * nch;
@@ -448,6 +470,80 @@ __device__ __forceinline__ double rotden_rho(const DevTables &t, const Frame &f1
     *esq_out = (s0 + sc * fc + sp * fp + st * ft) / (PIMC_WNO2K * PIMC_WNO2K);
   }
   return rho;
+}
+
+// rotden_rho's rho (no energies) with deleul's three acos on three lanes:
+// lanes 3d, 3d+1, 3d+2 of the calling warp evaluate the density of frames
+// (m1, m2in) given to them (the same on the three lanes), lane 3d+k taking
+// theta, phi or chi; every lane of the warp calls it (lanes past the last
+// full group compute on whatever frames they are given and their result is
+// not used).  The same operations as deleul + rotden_rho, so the same value.
+__device__ __forceinline__ double rotden_rho_lanes(const DevTables &t, const double *m1, const double *m2in,
+                                                   int lane, int *bad)
+{
+  const int sub = lane % 3, base = lane - sub;
+  double m2[9];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) {
+      double s = 0.0;
+      for (int k = 0; k < 3; k++) s = s + m1[k * 3 + i] * m2in[k * 3 + j];
+      m2[i * 3 + j] = s;
+    }
+  const double small = 1.e-08, pi = PIMC_PI;
+  double cost = within1(m2[8]);
+  double sint = sqrt((1.0 - cost) * (1.0 + cost));
+  double cphi = 0.0, sphi = 0.0, cchi, schi;
+  const bool pole0 = fabs(1.0 - cost) < small, pole1 = !pole0 && fabs(1.0 + cost) < small;
+  if (pole0) {
+    cchi = within1(m2[0]);
+    schi = within1(m2[3]);
+  } else if (pole1) {
+    cchi = within1(m2[4]);
+    schi = within1(m2[1]);
+  } else {
+    double isint = 1.0 / sint;
+    cphi = within1(m2[2] * isint);
+    sphi = within1(m2[5] * isint);
+    cchi = within1(-m2[6] * isint);
+    schi = within1(m2[7] * isint);
+  }
+  const double a = acos(sub == 0 ? cost : (sub == 1 ? cphi : cchi));
+  const double theta2 = __shfl_sync(0xffffffffu, a, base & 31);
+  const double acphi = __shfl_sync(0xffffffffu, a, (base + 1) & 31);
+  const double acchi = __shfl_sync(0xffffffffu, a, (base + 2) & 31);
+  double rel[3];
+  rel[0] = (pole0 || pole1) ? 0.0 : ((sphi > 0.0) ? acphi : 2.0 * pi - acphi);
+  rel[1] = theta2;
+  rel[2] = (schi > 0.0) ? acchi : 2.0 * pi - acchi;
+  double xt = rel[1] * t.d_dscale[0], xp = rel[0] * t.d_dscale[1], xc = rel[2] * t.d_dscale[2];
+  int ichi = (int)xc, iphi = (int)xp, ith = (int)xt;
+  double fc = xc - (double)ichi, fp = xp - (double)iphi, ft = xt - (double)ith;
+  if (near_node(ft)) {                                               // rotden.f:22-24
+    xt = (rel[1] * 180.0 / PIMC_PI) / t.dthd;
+    ith = (int)xt;
+    ft = xt - (double)ith;
+  }
+  if (near_node(fp)) {
+    xp = (rel[0] * 180.0 / PIMC_PI) / t.dphd;
+    iphi = (int)xp;
+    fp = xp - (double)iphi;
+  }
+  if (near_node(fc)) {
+    xc = (rel[2] * 180.0 / PIMC_PI) / t.dchd;
+    ichi = (int)xc;
+    fc = xc - (double)ichi;
+  }
+  if (ichi > t.nch - 1 || ichi < 0) { ichi = 0; fc = xc; *bad = 1; }
+  if (iphi > t.nph - 1 || iphi < 0) { iphi = 0; fp = xp; *bad = 1; }
+  if (ith > t.nth - 1 || ith < 0) { ith = 0; ft = xt; *bad = 1; }
+  size_t nph = t.nph, nch = t.nch;
+  size_t i0 = ((size_t)ith * nph + iphi) * nch + ichi;
+  double r0 = __ldg(t.rho + i0);
+  double dc = 0.0, dp = 0.0, dt = 0.0;
+  if (ichi < t.nch - 1) dc = __ldg(t.rho + i0 + 1) - r0;
+  if (iphi < t.nph - 1) dp = __ldg(t.rho + i0 + nch) - r0;
+  if (ith < t.nth - 1) dt = __ldg(t.rho + i0 + nph * nch) - r0;
+  return r0 + dc * fc + dp * fp + dt * ft;
 }
 
 // rsrot (rotden.f:218-286): outputs written only for iodevn == -1
@@ -469,6 +565,21 @@ __device__ __forceinline__ void rsrot(const Frame &f1, const Frame &f2, const do
     e = e + 1.5 / tau + 0.25 * (abc[0] + abc[1] + abc[2]);
     *erot = e / PIMC_WNO2K;
   }
+}
+
+// rsrot's log-density on the FP32 path, from the float frames: each
+// 1 - (column i of m1).(column i of m2) taken as half the squared distance
+// of the two unit columns, which keeps its precision for nearby frames
+// (adjacent rotational slices) where 1 - dot in float does not
+__device__ __forceinline__ float rsrot32(const float *m1, const float *m2, const float coef[3])
+{
+  float sumaxs = 0.0f;
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    float dx = m1[i] - m2[i], dy = m1[3 + i] - m2[3 + i], dz = m1[6 + i] - m2[6 + i];
+    sumaxs += coef[i] * (0.5f * (dx * dx + dy * dy + dz * dz));
+  }
+  return sumaxs;
 }
 
 // rsline (rotden.f:356-375)
@@ -523,24 +634,37 @@ __device__ __forceinline__ double vcord(const DevTables &t, const Frame &f, doub
   }
   if (rr) { *rr = rn; *th = thewff; *chr = chir; }
   double r = rn * (1.0 / bo2ang);
+  // grid coordinates, their cells and offsets in the cells (one conversion
+  // each, reused below unless an index is clamped)
   double xth = thewff * t.d_thscale;           // (theta * 180 / pi) / dth
   double xch = chiwff * t.d_chscale;
-  if (near_node(xth - (double)(int)xth)) xth = ((thewff * 180.0) / pi) / t.dth3;      // vcord.f:90-91
-  if (near_node(xch - (double)(int)xch)) xch = ((chiwff * 180.0) / pi) / t.dch3;
+  int ith = (int)xth, ich = (int)xch;
+  double fth = xth - (double)ith, fch = xch - (double)ich;
+  if (near_node(fth)) {                                              // vcord.f:90-91
+    xth = ((thewff * 180.0) / pi) / t.dth3;
+    ith = (int)xth;
+    fth = xth - (double)ith;
+  }
+  if (near_node(fch)) {
+    xch = ((chiwff * 180.0) / pi) / t.dch3;
+    ich = (int)xch;
+    fch = xch - (double)ich;
+  }
   // vcalc
   int maxrpt = t.rgrd - 1, mxthpt = t.thgrd - 1, mxchpt = t.chgrd - 1;
   if (r < t.rvmin) r = t.rvmin;
   if (r > t.rvmax) r = t.rvmax;
   double xr = (r - t.rvmin) * t.d_irstep;
-  if (near_node(xr - (double)(int)xr)) {                             // vcord.f:88, vcalc.f:21
+  int ir = (int)xr;
+  if (near_node(xr - (double)ir)) {                                  // vcord.f:88, vcalc.f:21
     r = rn / bo2ang;
     if (r < t.rvmin) r = t.rvmin;
     if (r > t.rvmax) r = t.rvmax;
     xr = (r - t.rvmin) / t.rvstep;
+    ir = (int)xr;
   }
-  int ir = (int)xr;
   if (ir > maxrpt) ir = maxrpt;
-  int ith = (int)xth, ich = (int)xch;
+  const int ith0 = ith, ich0 = ich;
   if (ich > mxchpt) ich = mxchpt;
   if (ich < 0) ich = 0;
   if (ith > mxthpt) ith = mxthpt;
@@ -555,11 +679,11 @@ __device__ __forceinline__ double vcord(const DevTables &t, const Frame &f, doub
   }
   if (ith < mxthpt) {
     gradth = (__ldg(t.vtab + i0 + nch) - v0);
-    delth = xth - (double)ith;
+    delth = (ith == ith0) ? fth : xth - (double)ith;
   }
   if (ich < mxchpt) {
     gradch = (__ldg(t.vtab + i0 + 1) - v0);
-    delch = xch - (double)ich;
+    delch = (ich == ich0) ? fch : xch - (double)ich;
   }
   return v0 + gradr * delr + gradth * delth + gradch * delch;
 }

@@ -172,18 +172,45 @@ struct RotSliceHooks {
     return ok != 0;
   }
   __device__ void published() { st_release_u64(mine, (id << 24) | (unsigned long long)(h + 1)); }
-  // the slice's next move, for both outcomes of this one
-  __device__ void ahead(RotShared &sh)
+  // the slice's next move, for both outcomes of this one, on all lanes of a
+  // warp: lane k < 2 proposes from the current (k = 0) or the proposed
+  // (k = 1) angles; on the FP64 path lanes 0-3 then take the sines and
+  // cosines of the two proposals' phi and chi, and lanes 0 and 2 build
+  // their frames (a top) or unit vectors (a linear rotor), so that the next
+  // rot_prepare starts its partner sums at once
+  __device__ void ahead(RotShared &sh, int lane)
   {
     if (!has_next) return;
+    double u[4], prop[3] = {0.0, 0.0, 0.0};
+    const int k = lane & 1;
+    const double *a = k ? sh.ang_new : sh.ang_old;
     if (mixed) {
-      rot_uniforms_t<true>(seed, pass, phase_next, pair, 0, linear, sh.nxt_u);
-      rot_propose_t<true>(*sys, linear, sh.ang_old[0], sh.ang_old[1], sh.ang_old[2], sh.nxt_u, sh.nxt_prop[0]);
-      rot_propose_t<true>(*sys, linear, sh.ang_new[0], sh.ang_new[1], sh.ang_new[2], sh.nxt_u, sh.nxt_prop[1]);
+      rot_uniforms_t<true>(seed, pass, phase_next, pair, 0, linear, u);
+      if (lane < 2) rot_propose_t<true>(*sys, linear, a[0], a[1], a[2], u, prop);
     } else {
-      rot_uniforms(seed, pass, phase_next, pair, 0, linear, sh.nxt_u);
-      rot_propose(*sys, linear, sh.ang_old[0], sh.ang_old[1], sh.ang_old[2], sh.nxt_u, sh.nxt_prop[0]);
-      rot_propose(*sys, linear, sh.ang_new[0], sh.ang_new[1], sh.ang_new[2], sh.nxt_u, sh.nxt_prop[1]);
+      rot_uniforms(seed, pass, phase_next, pair, 0, linear, u);
+      if (lane < 2) rot_propose(*sys, linear, a[0], a[1], a[2], u, prop);
+    }
+    if (lane < 2)
+      for (int d = 0; d < 3; d++) sh.nxt_prop[k][d] = prop[d];
+    if (lane == 0)
+      for (int d = 0; d < 4; d++) sh.nxt_u[d] = u[d];
+    if (mixed) return;
+    __syncwarp();
+    // lane 2o + j: proposal o, angle phi (j = 0) or chi (j = 1)
+    const int o = (lane >> 1) & 1, j = lane & 1;
+    if (linear) {
+      if (lane < 4 && j == 0) unit_vector(sh.nxt_prop[o][0], sh.nxt_prop[o][1], sh.nxt_nv[o]);
+      return;
+    }
+    double sn = 0.0, cs = 1.0;
+    if (lane < 4) sincos(sh.nxt_prop[o][j ? 2 : 0], &sn, &cs);
+    const double sk = __shfl_down_sync(0xffffffffu, sn, 1), ck = __shfl_down_sync(0xffffffffu, cs, 1);
+    if (lane < 4 && j == 0) {
+      const double *p = sh.nxt_prop[o];
+      Frame &f = sh.nxt_fn[o];
+      frame_from_sincos(p[0], p[1], p[2], sn, cs, sk, ck, f);      // = make_frame(p[0], p[1], p[2], f)
+      make_frame32((float)p[0], (float)p[1], (float)p[2], f.mf, &f.hzf);
     }
   }
 };
@@ -845,7 +872,7 @@ void launch_refresh_frames(const Ctx &c, Frame *frames, cudaStream_t s)
   int nb = (int)((n + 255) / 256);
   if (nb < 1) nb = 1;
   if (nb > 152) nb = 152;
-  k_refresh_frames<<<nb, 256, 0, s>>>(c, frames, c.s.mixed && c.s.nrotors == 1);
+  k_refresh_frames<<<nb, 256, 0, s>>>(c, frames, c.s.mixed);
 }
 
 void launch_derive_state(const Ctx &c, Frame *frames, cudaStream_t s)
@@ -932,7 +959,7 @@ __global__ void __launch_bounds__(PIMC_ROT_THREADS) k_rot_slices(Ctx c, Frame *f
         for (int k = 0; k < 4; k++) u[k] = sh.nxt_u[k];
         for (int k = 0; k < 3; k++) prop[k] = sh.nxt_prop[acc ? 1 : 0][k];
       }
-      rot_prepare<MIX>(c, frames, g0, q, u, prop, linear, sh);
+      rot_prepare<MIX>(c, frames, g0, q, u, prop, linear, sh, MIX ? -1 : (acc ? 1 : 0));
     }
   }
   if (threadIdx.x == 0) {

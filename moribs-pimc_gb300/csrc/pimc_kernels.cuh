@@ -466,7 +466,7 @@ __device__ __forceinline__ void mol_disp(const DevSys &s, int type, uint64_t see
 // move, so only rot_finish lies on the chain between neighbouring slices.
 //
 // For a nonlinear rotor the commit writes the angles and the frame the
-// evaluation used (on the FP32 path with one rotor only its float part);
+// evaluation used (on the FP32 path only its float part);
 // the double-precision frame and MCCosine are then derived from the angles
 // by k_refresh_frames before anything reads them (estimators, state
 // download, queries), which gives the same values as writing them here.
@@ -555,6 +555,8 @@ struct RotShared {
   float valsf[2 * 16];      // partner sums on the FP32 path
   double ang_old[3];        // the slice's current angles
   double nxt_u[4], nxt_prop[2][3];   // the slice's next move: uniforms, proposal if this one is rejected / accepted
+  Frame nxt_fn[2];          // FP64 path, top: the frames of the two next proposals
+  double nxt_nv[2][3];      // FP64 path, linear rotor: their unit vectors
   double buf[PIMC_RED_BUF];
 };
 
@@ -779,6 +781,12 @@ __device__ __forceinline__ int rot_decide(const DevSys &s, bool linear, const do
     double lr = (rf > 0.0f) ? (double)logf(rf) + boltz : -1.0e300;
     acc = (lr > 0.0) || (lr > logu);
     rd = need_rd ? (double)rf * exp(boltz) : 0.0;
+  } else if (MIX && !linear) {
+    // the FP32 path with rattle-and-shake densities (float log-densities):
+    // their difference in float, the test in double against 0 and log u
+    float rhoold = (float)rho[0] + (float)rho[1], rhonew = (float)rho[2] + (float)rho[3];
+    rd = (double)((rhonew - rhoold) * s.rs_scale) + boltz;    // boltz: - tau (pot_new - pot_old)
+    acc = (rd > 0.0) || (rd > logu);
   } else if (s.rot_den_type == 0) {
     double dens_old = rho[0] * rho[1], dens_new = rho[2] * rho[3];
     if (fabs(dens_old) < PIMC_RZERO) dens_old = 0.0;
@@ -843,15 +851,17 @@ __device__ __forceinline__ bool lazy_linear(const Ctx &c, bool mix)
 // gives).  All PIMC_ROT_THREADS threads call it.
 template <bool MIX>
 __device__ void rot_prepare(const Ctx &c, const Frame *frames, int g0, int q, const double u[4], const double prop[3],
-                            bool linear, RotShared &sh)
+                            bool linear, RotShared &sh, int pre = -1)
 {
   const DevSys &s = c.s;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int Q = s.Q, R = s.R;
   const size_t n = (size_t)s.nrotors * Q;
   const int i1 = (g0 - s.rot_first) * Q + q;
-  const bool need64 = !MIX || s.nrotors > 1;    // proposal frame in double during the evaluation
+  const bool need64 = !MIX;                     // proposal frame in double during the evaluation
   if (warp == 0) {
+    // pre >= 0: the look-ahead of the previous move (FP64 path) built the
+    // proposal's frame or unit vector in sh.nxt_fn / sh.nxt_nv[pre]
     if (lane == 0) {
       for (int k = 0; k < 4; k++) sh.u[k] = u[k];
       const double a[3] = {prop[0], prop[1], prop[2]};
@@ -859,15 +869,18 @@ __device__ void rot_prepare(const Ctx &c, const Frame *frames, int g0, int q, co
       if (linear) {
         if (MIX) {
           unit_vector32((float)a[0], (float)a[1], sh.nnewf);
+        } else if (pre >= 0) {
+          for (int d = 0; d < 3; d++) sh.nnew[d] = sh.nxt_nv[pre][d];
         } else {
           unit_vector(a[0], a[1], sh.nnew);
         }
       } else if (need64) {
-        make_frame(a[0], a[1], a[2], sh.fn);
+        if (pre < 0) make_frame(a[0], a[1], a[2], sh.fn);
       } else {
         make_frame32((float)a[0], (float)a[1], (float)a[2], sh.fn.mf, &sh.fn.hzf);
       }
     }
+    if (!linear && need64 && pre >= 0) copy_frame<false>(sh.fn, &sh.nxt_fn[pre], lane);
   } else if (warp == 1) {
     if (linear) {
       if (lane < 3) {
@@ -925,8 +938,10 @@ __device__ void rot_prepare(const Ctx &c, const Frame *frames, int g0, int q, co
             },
             sh.vals, sh.buf);
     }
-    if (tid == 0) {
-      // sums and the Boltzmann factor here, off the neighbour chain
+    if (tid == 96) {
+      // sums and the Boltzmann factor here, off the neighbour chain (on warp
+      // 3: warps 0 and 8, which share an SM sub-partition, carry the other
+      // serial stages)
       if (MIX) {
         float po = 0.0f, pn = 0.0f;
         if (sh.pot_cached) po = (float)sh.pot_c;
@@ -964,13 +979,13 @@ __device__ void rot_prepare(const Ctx &c, const Frame *frames, int g0, int q, co
 struct RotNoHooks {
   __device__ bool wait(int) { return true; }
   __device__ void published() {}
-  __device__ void ahead(RotShared &) {}
+  __device__ void ahead(RotShared &, int) {}
 };
 
 // second stage of the move prepared in sh, on warp 8: hooks.wait(lane) on
 // all lanes before the neighbours' state is read (false: leave the move
 // undone and set sh.stop), hooks.published() on lane 0 after the commit;
-// meanwhile warp 9 runs hooks.ahead(sh) (the slice's next proposal).  COH
+// meanwhile warp 9 runs hooks.ahead(sh, lane) (the slice's next proposal).  COH
 // reads the neighbours through L2 (persistent launches, where other CTAs
 // write them).  All PIMC_ROT_THREADS threads call it; returns 1 if accepted.
 template <bool MIX, bool COH, class Hooks>
@@ -987,8 +1002,8 @@ __device__ int rot_finish(const Ctx &c, Frame *frames, int g0, int q, bool linea
   const int r = g0 - s.rot_first;
   const int i0 = r * Q + q0, i1 = r * Q + q, i2 = r * Q + q2;
   const bool use_links = Q >= 3;                // link cache (with Q < 3 both links join the same two slices)
-  const bool need64 = !MIX || s.nrotors > 1;
-  const bool mf_only = MIX && !linear && s.rot_den_type == 0;   // densities read the float frames only
+  const bool need64 = !MIX;
+  const bool mf_only = MIX && !linear;          // densities read the float frames only
   if (warp == 8) {
     bool go = hooks.wait(lane);
     if (lane == 0) sh.stop = !go;
@@ -1029,7 +1044,20 @@ __device__ int rot_finish(const Ctx &c, Frame *frames, int g0, int q, bool linea
       if (lane == 0) sh.bad = 0;
       __syncwarp();
       // 0: (q-1, q) old, 1: (q, q+1) old, 2: (q-1, q) new, 3: (q, q+1) new
-      if (lane < 4 && !(lane < 2 && sh.link_ok[lane])) {
+      if (!MIX && !linear && s.rot_den_type == 0) {
+        // FP64 top, tabulated densities: density d on lanes 3d..3d+2
+        const int d = lane / 3;
+        const bool act = d < 4 && !(d < 2 && sh.link_ok[d]);
+        const int dd = d < 4 ? d : 0;
+        const Frame &fa = (dd == 0 || dd == 2) ? sh.fo[0] : (dd == 1 ? sh.fo[1] : sh.fn);
+        const Frame &fb = (dd == 0) ? sh.fo[1] : (dd == 2 ? sh.fn : sh.fo[2]);
+        int bad = 0;
+        double rho = rotden_rho_lanes(c.t, fa.m, fb.m, lane, &bad);
+        if (act && lane % 3 == 0) {
+          sh.rho[d] = rho;
+          if (bad) atomicOr(&sh.bad, 1);
+        }
+      } else if (lane < 4 && !(lane < 2 && sh.link_ok[lane])) {
         int bad = 0;
         double rho;
         if (linear) {
@@ -1051,11 +1079,8 @@ __device__ int rot_finish(const Ctx &c, Frame *frames, int g0, int q, bool linea
           const Frame &fb = (lane == 0) ? sh.fo[1] : (lane == 2 ? sh.fn : sh.fo[2]);
           if (MIX && s.rot_den_type == 0) {
             rho = (double)rotden_rho32(c.t, fa.mf, fb.mf, &bad);
-          } else if (MIX && !need64 && lane >= 2) {
-            Frame f64;
-            make_frame64(sh.ang_new[0], sh.ang_new[1], sh.ang_new[2], f64);
-            rho = (lane == 2) ? link_density(c, false, fa, f64, nullptr, nullptr, &bad)
-                              : link_density(c, false, f64, fb, nullptr, nullptr, &bad);
+          } else if (MIX) {
+            rho = s.rot_odevn == -1 ? (double)rsrot32(fa.mf, fb.mf, s.rs_coef) : 0.0;
           } else {
             rho = link_density(c, false, fa, fb, nullptr, nullptr, &bad);
           }
@@ -1111,8 +1136,8 @@ __device__ int rot_finish(const Ctx &c, Frame *frames, int g0, int q, bool linea
         hooks.published();
       }
     }
-  } else if (warp == 9 && lane == 0) {
-    hooks.ahead(sh);
+  } else if (warp == 9) {
+    hooks.ahead(sh, lane);
   }
   __syncthreads();
   return sh.acc;

@@ -65,30 +65,60 @@ def test_surrogate_delayed_acceptance():
     m.close()
 
 
-def test_delayed_acceptance_samples_the_exact_distribution():
-    """Plain and surrogate-screened chains from the same start: the mean
-    dimer energy over the run agrees within the spread of block means."""
-    w, s = _dimer()
+def test_screen_is_exact_and_spares_exact_evaluations():
+    """The screened chain samples the exact distribution, and reaches a given
+    standard error of <E_pot> with fewer exact evaluations than the plain one.
+
+    K identical small dimers (P = 64, Q = 32) in one batch, each replica an
+    independent chain of rotational sweeps with its own seed.  The replicas
+    are first brought to equilibrium by EQ0 plain sweeps; both arms start
+    from those states, make EQ sweeps of their own, then sample the
+    estimators every EVERY sweeps.  The error of an arm's mean is the spread
+    of the K chain means over sqrt(K).  Exactness: E_pot (the dimer energy
+    the surrogate screens) and E_rot agree between the plain and the screened
+    arm within 2 combined standard errors.  Gain: the exact evaluations an
+    arm needs for a given error scale as (exact evaluations per sweep) x SE^2
+    at equal sweeps; the screened arm's product is below the plain arm's.
+    With K = 256 the variance ratio is known to about 13 %."""
+    K, EQ0, EQ, NS, EVERY = 256, 3000, 200, 100, 5
+    w = W.config3(seed=40, nslices=64, nrotslices=32, griddens=(19, 37, 37), levels=4)
+    s = G.Sampler(w)
     s.da_sweeps(50, seed=2)
-    x, e = _collect(s, 80, 2, seed=300)
+    x, e = _collect(s, 1000, 2, seed=500)
+    s.close()
     mu, sd = float(e.mean()), float(e.std())
     m = G.Mlp()
     rng = np.random.default_rng(1)
     m.set_weights(rng.normal(0, 1 / np.sqrt(6), (6, 256)), np.zeros(256), rng.normal(0, 1 / 16, (256, 256)),
                   np.zeros(256), rng.normal(0, 1 / 16, (256, 256)), np.zeros(256), rng.normal(0, 1 / 16, 256), 0.0)
-    m.train(x, (e - mu) / sd, epochs=15, batch=1024, lr=1e-3, seed=4)
-    c0, a0, co0, p0 = s.get_state()
-    means = {}
-    for use in (False, True):
-        sx = G.Sampler(w)
-        sx.set_state(c0, a0, p0)
-        blocks = []
-        for b in range(12):
-            sx.da_sweeps(10, seed=1000 + b, mlp=m if use else None, escale=sd)
-            blocks.append(float(sx.da_samples()[1].mean()))
-        means[use] = (np.mean(blocks[2:]), np.std(blocks[2:]) / np.sqrt(len(blocks) - 2))
-        sx.close()
-    (m0, e0), (m1, e1) = means[False], means[True]
-    assert abs(m0 - m1) <= 5 * np.hypot(e0, e1) + 0.05 * sd, (means, sd)
-    s.close()
+    m.train(x, (e - mu) / sd, epochs=25, batch=1024, lr=1e-3, seed=4)
+    b = G.Batch([w] * K)
+    b.da_sweeps(EQ0, 777)
+    start = [b.get_state(r) for r in range(K)]
+    b.close()
+    res = {}
+    for arm, mlp, base in (("plain", None, 10000), ("screened", m, 20000)):
+        b = G.Batch([w] * K)
+        for r, (c, a, _, p) in enumerate(start):
+            b.set_state(r, c, a, p)
+        b.da_sweeps(EQ, base, mlp=mlp, escale=sd)
+        acc = np.zeros((K, 2))
+        st = np.zeros(4)
+        for k in range(NS):
+            st += b.da_sweeps(EVERY, base + 1 + k, mlp=mlp, escale=sd)
+            acc += b.estimators()[:, 1:3]
+        b.close()
+        means = acc / NS
+        res[arm] = (means.mean(0), means.std(0, ddof=1) / np.sqrt(K), st)
+    (m0, e0, st0), (m1, e1, st1) = res["plain"], res["screened"]
+    z = (m1 - m0) / np.hypot(e0, e1)
+    cost = (st1[3] * e1[0] ** 2) / (st0[3] * e0[0] ** 2)
+    print("E_pot, E_rot plain", m0, "+-", e0, "screened", m1, "+-", e1, "z", z)
+    print("exact evaluations per proposal: plain %.3f screened %.3f; per accepted move: plain %.3f screened %.3f; "
+          "exact evaluations for equal SE of E_pot, screened / plain: %.3f"
+          % (st0[3] / st0[0], st1[3] / st1[0], st0[3] / st0[2], st1[3] / st1[2], cost))
+    assert st0[3] == st0[0] and st0[0] == st1[0] == NS * EVERY * K * w.nrotslices * 2
+    assert np.all(np.abs(z) <= 2.0), z
+    assert st1[3] < st1[0]
+    assert cost < 1.0, cost
     m.close()
