@@ -71,7 +71,8 @@ def parse():
     ap.add_argument("--no-precision-error", action="store_true", help="skip the FP32-vs-FP64 per-replica comparison")
     ap.add_argument("--da-replicas", type=int, default=32, help="independent dimer systems swept at once")
     ap.add_argument("--only", default=None,
-                    choices=["tables", "worm", "surrogate", "matched_se", "water_chains", "config_table"],
+                    choices=["tables", "worm", "surrogate", "matched_se", "water_chains", "config_table",
+                             "fp64_pipe"],
                     help="run one companion measurement alone on cuda:0 and print its JSON (for profiling)")
     return ap.parse_args()
 
@@ -890,6 +891,20 @@ def run_config_table(local, cpu_seconds=6.0):
     return out
 
 
+def run_fp64_pipe(local, iters=20000):
+    """The FP64 pipe's occupancy rule (pimc_fp64_probe): warp-level FP64 FMA
+    instructions retired per SM per microsecond, for one CTA per SM of 1-16
+    warps with 1, 4 or 32 active lanes."""
+    import pimc_gb300 as G
+    rows = []
+    for warps in (1, 2, 4, 8, 16):
+        for lanes in (1, 4, 32):
+            ms = G.fp64_probe(warps, lanes, iters, device=local)
+            rows.append({"warps": warps, "lanes": lanes, "ms": round(ms, 4),
+                         "warp_fma_per_sm_per_us": round(warps * iters * 8 / (ms * 1e3), 3)})
+    return {"rows": rows}
+
+
 def run_water_chains(local, steps, n=64):
     """A small case of the config-4 batch (the first n water-chain replicas'
     worth of the family, FP32 path, rotation mode 1, shape 8 x 4): one
@@ -1237,7 +1252,8 @@ def main():
                    "surrogate": lambda: run_surrogate(local, replicas=args.da_replicas),
                    "matched_se": lambda: run_matched_se(local, mode=args.se_mode),
                    "water_chains": lambda: run_water_chains(local, args.steps),
-                   "config_table": lambda: run_config_table(local)}[args.only]
+                   "config_table": lambda: run_config_table(local),
+                   "fp64_pipe": lambda: run_fp64_pipe(local)}[args.only]
             print(json.dumps({"part": args.only, **run()}), flush=True)
         return 0
     line, w = run_gb300(args, rank, local, world, dist)

@@ -223,6 +223,14 @@ pimc_status pimc_blocking_se(const double *x, long n, double *out);
  * the denominator of the FP64 roofline fractions.  No reference counterpart. */
 pimc_status pimc_fp64_peak(int device, double *gflops);
 
+/* The FP64 pipe's occupancy rule: one CTA per SM of `warps` warps (1-32),
+ * `lanes` active lanes per warp (1-32), each active lane running 8
+ * independent FMA chains of `iters` steps (1-2^24); *ms is the launch's
+ * device time (CUDA events, after a warm-up launch).  The time per warp
+ * instruction per SM follows: ms / (warps * iters * 8).  Measures how the
+ * rotational kernels' low-lane-count FP64 stages load the pipe. */
+pimc_status pimc_fp64_probe(int device, int warps, int lanes, int iters, double *ms);
+
 /* ---- worm algorithm (mc_qworm.cc) ------------------------------------------ */
 
 /* MCWormInit (mc_qworm.cc:49-82) for the atom type `type` with the WORM

@@ -60,6 +60,11 @@ struct pimc_handle {
   unsigned long long *prog = nullptr;  // per-CTA progress words of the persistent rotation launches
   unsigned *abort_word = nullptr;
   int nprog = 0;
+  // the handle as a one-replica batch, for the half-sweep kernel that makes
+  // small multi-rotor moves one warp each (uploaded before every pass launch)
+  BatchRep self_host{};
+  BatchRep *self_rep = nullptr;
+  int *self_idx = nullptr;             // the half-sweep kernel's replica order {0} and unit offsets {0, Q/2}
   // pair-density histograms (allocated on first use)
   DensHist dens{nullptr, nullptr, nullptr, nullptr};
   int dens_on = 0;
@@ -343,9 +348,14 @@ extern "C" pimc_status pimc_create(const pimc_system *sys, int device, pimc_hand
       (e = dalloc(h, &st.ang, 3 * nr)) || (e = dalloc(h, &st.cosv, 3 * nr)) || (e = dalloc(h, &st.pindex, na)) ||
       (e = dalloc(h, &st.mctype, na)) || (e = dalloc(h, &st.err, 1)) || (e = dalloc(h, &h->frames, nr)) ||
       (e = dalloc(h, &h->cnt, 12)) || (e = dalloc(h, &h->pass, 1)) || (e = dalloc(h, &h->cursors, 8)) ||
-      (e = dalloc(h, &h->prog, (size_t)(d.Q > 0 ? d.Q : 1))) || (e = dalloc(h, &h->abort_word, 1))) {
+      (e = dalloc(h, &h->prog, (size_t)(d.Q > 0 ? d.Q : 1))) || (e = dalloc(h, &h->abort_word, 1)) ||
+      (e = dalloc(h, &h->self_rep, 1)) || (e = dalloc(h, &h->self_idx, 3))) {
     pimc_destroy(h);
     return e;
+  }
+  {
+    const int idx[3] = {0, 0, d.Q / 2};
+    CK(cudaMemcpy(h->self_idx, idx, sizeof(idx), cudaMemcpyHostToDevice));
   }
   void *msv = nullptr;
   if (cudaMalloc(&msv, mol_scratch_bytes()) != cudaSuccess) { pimc_destroy(h); return PIMC_ERR_CUDA; }
@@ -388,7 +398,7 @@ extern "C" pimc_status pimc_destroy(pimc_handle *h)
   void *bufs[] = {st.x, st.y, st.z, st.b4, st.cosvf, st.rp_cache, st.rl_cache, st.rp_ok, st.rl_ok,
                   st.ang, st.cosv, st.pindex, st.mctype, st.err, h->frames, h->cnt, h->pass, h->cursors, h->ms,
                   h->qbuf, h->prog, h->abort_word, h->dens.g1, h->dens.g2, h->dens.g3, h->dens.rel, h->worm, h->rindex,
-                  h->wcur, h->wscr};
+                  h->wcur, h->wscr, h->self_rep, h->self_idx};
   for (void *b : bufs)
     if (b) cudaFree(b);
   for (void *b : h->owned) cudaFree(b);
@@ -1521,12 +1531,36 @@ static long long launch_bisection_block(pimc_handle *h, const PassPlan &pl, size
   return d.numb[t];
 }
 
+// several rotors whose slice moves have few rotor-partner terms (at most a
+// warp's worth, R (N - 1) <= 32, e.g. the water dimer): each half-sweep is
+// one launch of the batch's half-sweep kernel over this handle, a warp per
+// slice pair (its rotors one after the other), instead of a persistent CTA
+// looping over slice pairs; the same moves, draws and arithmetic
+static bool flat_sweeps(const pimc_handle *h)
+{
+  const DevSys &d = h->ctx.s;
+  return h->fused && d.nrotors > 1 && d.Q >= 4 && d.Q % 2 == 0 && (d.na - 1) * d.R <= 32;
+}
+
 // rotational sweeps it0 .. it1-1; group numbers the persistent launches of a pass
 static pimc_status launch_sweeps(pimc_handle *h, const PassPlan &pl, int it0, int it1, unsigned group, uint64_t seed,
                                  long long *n)
 {
   const DevSys &d = h->ctx.s;
   if (!h->sys.rotation || d.nrotors <= 0 || it1 <= it0) return PIMC_OK;
+  if (flat_sweeps(h)) {
+    const int units = d.Q / 2, nbk = (int)pl.type.size();
+    int warps = units / 152;                 // spread the slice pairs over the SMs
+    if (warps < 1) warps = 1;
+    if (warps > 8) warps = 8;
+    for (int it = it0; it < it1; it++)
+      for (int parity = 0; parity < 2; parity++) {
+        launch_batch_rot_flat(h->self_rep, h->self_idx, h->self_idx + 1, 1, units, (int)group, it - it0, parity, nbk,
+                              seed, d.mixed, warps, 2, h->stream);
+        (*n)++;
+      }
+    return PIMC_OK;
+  }
   int nctas = 0;
   if (h->fused && d.Q >= 2 && d.Q % 2 == 0) {
     if (d.nrotors == 1 && rot_slices_max_ctas(d.mixed) >= d.Q) {
@@ -1594,8 +1628,19 @@ extern "C" pimc_status pimc_run_passes(pimc_handle *h, int npasses, uint64_t see
   if (npasses < 0) return PIMC_ERR_BAD_ARG;
   for (int t = 0; t < d.ntypes; t++)
     if (d.P % (1 << d.levels[t])) return PIMC_ERR_BAD_ARG;
+  if (flat_sweeps(h)) {
+    // the handle's current context for the half-sweep kernel (the graph holds its address)
+    h->self_host.c = h->ctx;
+    h->self_host.frames = h->frames;
+    h->self_host.pass = h->pass;
+    h->self_host.cnt = h->cnt;
+    h->self_host.seed_mix = 0;
+    h->self_host.rotation = h->sys.rotation;
+    CK(cudaMemcpyAsync(h->self_rep, &h->self_host, sizeof(BatchRep), cudaMemcpyHostToDevice, h->stream));
+  }
   if (!h->pass_exec || h->pass_seed != seed) {
     if (h->pass_exec) { CK(cudaGraphExecDestroy(h->pass_exec)); h->pass_exec = nullptr; }
+    if (flat_sweeps(h) && !batch_flat_setup(8)) return PIMC_ERR_CUDA;
     cudaGraph_t graph;
     CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
     long long n = 0;

@@ -76,13 +76,20 @@ __device__ __forceinline__ void da_propose_move(const Ctx &c, const Frame *frame
   double u[4], prop[3];
   rot_uniforms(seed, ps, phase, q, r, false, u);
   rot_propose(s, false, c.st.ang[ri], c.st.ang[n + ri], c.st.ang[2 * n + ri], u, prop);
-  Frame fn;
-  make_frame64(prop[0], prop[1], prop[2], fn);
+  Frame &fn = d.fn;
+  make_frame(prop[0], prop[1], prop[2], fn);
   const Frame &fo = frames[ri];
-  const Frame &fm = frames[rot_index(s, g, (q - 1 + Q) % Q)], &fp = frames[rot_index(s, g, (q + 1) % Q)];
+  const int im = rot_index(s, g, (q - 1 + Q) % Q);
+  const Frame &fm = frames[im], &fp = frames[rot_index(s, g, (q + 1) % Q)];
+  // the old links from the link cache where it holds them (FP64 path: the
+  // cache then holds exactly rotden's value; link (q-1, q) at q-1's entry)
+  const bool links = !s.mixed && Q >= 3;
   int bad = 0;
-  double rn = rotden_rho(c.t, fm, fn, &bad, nullptr, nullptr) * rotden_rho(c.t, fn, fp, &bad, nullptr, nullptr);
-  double ro = rotden_rho(c.t, fm, fo, &bad, nullptr, nullptr) * rotden_rho(c.t, fo, fp, &bad, nullptr, nullptr);
+  const double l0n = rotden_rho(c.t, fm, fn, &bad, nullptr, nullptr), l1n = rotden_rho(c.t, fn, fp, &bad, nullptr, nullptr);
+  const double l0o = (links && c.st.rl_ok[im]) ? c.st.rl_cache[im] : rotden_rho(c.t, fm, fo, &bad, nullptr, nullptr);
+  const double l1o = (links && c.st.rl_ok[ri]) ? c.st.rl_cache[ri] : rotden_rho(c.t, fo, fp, &bad, nullptr, nullptr);
+  double rn = l0n * l1n;
+  double ro = l0o * l1o;
   const Frame &fb = frames[rot_index(s, o, q)];
   for (int j = 0; j < R; j++) {
     double ca[3], cb[3];
@@ -94,6 +101,8 @@ __device__ __forceinline__ void da_propose_move(const Ctx &c, const Frame *frame
   d.prop[0] = prop[0]; d.prop[1] = prop[1]; d.prop[2] = prop[2];
   d.rn = rn;
   d.ro = ro;
+  d.ln[0] = l0n; d.ln[1] = l1n;
+  d.lo[0] = l0o; d.lo[1] = l1o;
   d.bad = bad;
 }
 
@@ -145,8 +154,7 @@ __device__ __forceinline__ unsigned da_decide_move(const Ctx &c, Frame *frames, 
   }
   bool acc = false;
   if (pass1) {
-    Frame fn;
-    make_frame64(d.prop[0], d.prop[1], d.prop[2], fn);
+    const Frame &fn = d.fn;
     const Frame &fo = frames[ri], &fb = frames[rot_index(s, o, q)];
     double dv = 0.0;
     for (int j = 0; j < R; j++) {
@@ -162,8 +170,17 @@ __device__ __forceinline__ unsigned da_decide_move(const Ctx &c, Frame *frames, 
       c.st.ang[ri] = d.prop[0];
       c.st.ang[n + ri] = d.prop[1];
       c.st.ang[2 * n + ri] = d.prop[2];
-      make_frame(d.prop[0], d.prop[1], d.prop[2], frames[ri]);
+      frames[ri] = fn;
     }
+  }
+  // the link cache after the move (its two links belong to this move alone
+  // within the sub-phase)
+  if (!s.mixed && Q >= 3 && !d.bad) {
+    const int im = rot_index(s, g, (q - 1 + Q) % Q);
+    c.st.rl_cache[im] = acc ? d.ln[0] : d.lo[0];
+    c.st.rl_cache[ri] = acc ? d.ln[1] : d.lo[1];
+    c.st.rl_ok[im] = 1;
+    c.st.rl_ok[ri] = 1;
   }
   return (pass1 ? 1u : 0u) | (acc ? 2u : 0u) | (pass1 ? 4u : 0u);
 }

@@ -57,6 +57,8 @@ size_t mol_scratch_bytes();
 struct DaMove {
   double prop[3];        // the proposal (phi, cos theta, chi)
   double rn, ro;         // rho(q-1, q) rho(q, q+1) with the new and the old orientation
+  double ln[2], lo[2];   // the two link densities, new and old (the link cache's values)
+  Frame fn;              // the proposal's frame
   int bad;
 };
 int launch_da_samples(const Ctx &c, const Frame *f, float *feat, float *energy, cudaStream_t s);

@@ -85,8 +85,9 @@ extern "C" pimc_status pimc_blocking_se(const double *x, long n, double *out)
 // Eight independent chains per thread keep the FP64 pipe's latency hidden;
 // every thread's result is stored so that nothing is eliminated.
 namespace {
-__global__ void __launch_bounds__(256) k_fp64_fma(double *out, int iters, double a, double b)
+__global__ void __launch_bounds__(1024) k_fp64_fma(double *out, int iters, double a, double b, int lanes)
 {
+  if ((int)(threadIdx.x & 31) >= lanes) return;
   double x[8];
   for (int k = 0; k < 8; k++) x[k] = 1.0 + 1e-3 * (double)(threadIdx.x + k);
   for (int i = 0; i < iters; i++)
@@ -111,9 +112,9 @@ extern "C" pimc_status pimc_fp64_peak(int device, double *gflops)
   float ms = 0.0f;
   if (cudaMalloc(&out, (size_t)blocks * threads * sizeof(double)) != cudaSuccess) return PIMC_ERR_CUDA;
   if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) { st = PIMC_ERR_CUDA; goto done; }
-  k_fp64_fma<<<blocks, threads>>>(out, iters / 8, 0.9999999, 1e-7);       // warm-up
+  k_fp64_fma<<<blocks, threads>>>(out, iters / 8, 0.9999999, 1e-7, 32);       // warm-up
   cudaEventRecord(e0);
-  k_fp64_fma<<<blocks, threads>>>(out, iters, 0.9999999, 1e-7);
+  k_fp64_fma<<<blocks, threads>>>(out, iters, 0.9999999, 1e-7, 32);
   cudaEventRecord(e1);
   if (cudaEventSynchronize(e1) != cudaSuccess || cudaGetLastError() != cudaSuccess ||
       cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess || ms <= 0.0f) {
@@ -121,6 +122,37 @@ extern "C" pimc_status pimc_fp64_peak(int device, double *gflops)
     goto done;
   }
   *gflops = 2.0 * 8.0 * (double)iters * (double)blocks * (double)threads / ((double)ms * 1e-3) / 1e9;
+done:
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaFree(out);
+  return st;
+}
+
+extern "C" pimc_status pimc_fp64_probe(int device, int warps, int lanes, int iters, double *ms_out)
+{
+  if (!ms_out || warps < 1 || warps > 32 || lanes < 1 || lanes > 32 || iters < 1 || iters > (1 << 24))
+    return PIMC_ERR_BAD_ARG;
+  if (cudaSetDevice(device) != cudaSuccess) return PIMC_ERR_NO_DEVICE;
+  int nsm = 0;
+  if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return PIMC_ERR_CUDA;
+  const int threads = 32 * warps;
+  double *out = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  pimc_status st = PIMC_OK;
+  float ms = 0.0f;
+  if (cudaMalloc(&out, (size_t)nsm * threads * sizeof(double)) != cudaSuccess) return PIMC_ERR_CUDA;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) { st = PIMC_ERR_CUDA; goto done; }
+  k_fp64_fma<<<nsm, threads>>>(out, iters / 8 + 1, 0.9999999, 1e-7, lanes);      // warm-up
+  cudaEventRecord(e0);
+  k_fp64_fma<<<nsm, threads>>>(out, iters, 0.9999999, 1e-7, lanes);
+  cudaEventRecord(e1);
+  if (cudaEventSynchronize(e1) != cudaSuccess || cudaGetLastError() != cudaSuccess ||
+      cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess || ms <= 0.0f) {
+    st = PIMC_ERR_CUDA;
+    goto done;
+  }
+  *ms_out = (double)ms;
 done:
   if (e0) cudaEventDestroy(e0);
   if (e1) cudaEventDestroy(e1);

@@ -90,6 +90,7 @@ def load(path=LIBPATH):
     L.pimc_save_energy.argtypes = [sp, cc, C.c_double, C.c_long, _dp]
     L.pimc_blocking_se.argtypes = [_dp, C.c_long, _dp]
     L.pimc_fp64_peak.argtypes = [C.c_int, _dp]
+    L.pimc_fp64_probe.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, _dp]
     L.pimc_save_sum_energy.argtypes = [sp, cc, C.c_double, C.c_double, _dp, C.c_int]
     L.pimc_asymrho.argtypes = [C.c_int, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, _dp, C.c_int,
                                _dp, _dp, _dp, _dp]
@@ -516,6 +517,14 @@ def fp64_peak(device=0):
     g = np.zeros(1)
     _chk(load().pimc_fp64_peak(int(device), dptr(g)), "pimc_fp64_peak")
     return float(g[0])
+
+
+def fp64_probe(warps, lanes, iters=20000, device=0):
+    """pimc_fp64_probe: device milliseconds of one CTA per SM of `warps`
+    warps with `lanes` active lanes, 8 FMA chains of `iters` steps each."""
+    ms = C.c_double()
+    _chk(load().pimc_fp64_probe(int(device), int(warps), int(lanes), int(iters), C.byref(ms)), "pimc_fp64_probe")
+    return ms.value
 
 
 def linden(temperatures, nslices, bconst, npt, iodevn=-1, device=0):

@@ -65,3 +65,44 @@ def test_batch_da_passes_count_the_schedule():
     e = b.estimators()
     assert np.isfinite(e).all()
     b.close()
+
+
+def test_batch_da_passes_sample_the_standard_distribution():
+    """Passes whose rotational sweeps are made by the delayed-acceptance
+    kernels without a screen (plain Metropolis, the link cache of the
+    tabulated densities kept by those kernels) and the batch's standard
+    passes sample the same distribution.  K identical dimers of the
+    statistics tests' config-3 shape (5 K, P = 64, Q = 32, bisection levels 2,
+    centroid step 0.02 A), brought to equilibrium by EQ0 standard passes; each
+    arm starts from those states, makes EQ passes of its own, then samples
+    the estimators after every pass.  The error of an arm's mean is the
+    spread of the K chain means over sqrt(K).  Criterion: E_kin, E_pot and
+    E_rot each within 3 combined standard errors and at most one of the three
+    beyond 2."""
+    K, EQ0, EQ, NS = 256, 300, 30, 100
+    w = W.config3(seed=7, nslices=64, nrotslices=32, griddens=(19, 37, 37), levels=2)
+    w.types[0]["mcstep"] = 0.02
+    w.temperature = 5.0
+    b = G.Batch([w] * K)
+    b.run_passes(EQ0, 31)
+    start = [b.get_state(r) for r in range(K)]
+    b.close()
+    res = {}
+    for arm, seed in (("standard", 1000), ("delayed", 2000)):
+        b = G.Batch([w] * K)
+        for r, (c, a, _, p) in enumerate(start):
+            b.set_state(r, c, a, p)
+        run = b.run_passes if arm == "standard" else b.da_passes
+        run(EQ, seed)
+        acc = np.zeros((K, 3))
+        for k in range(NS):
+            run(1, seed)                     # the pass counters key each pass's draws
+            acc += b.estimators()[:, :3]
+        b.close()
+        means = acc / NS
+        res[arm] = (means.mean(0), means.std(0, ddof=1) / np.sqrt(K))
+    (m0, e0), (m1, e1) = res["standard"], res["delayed"]
+    z = (m1 - m0) / np.hypot(e0, e1)
+    print("E_kin, E_pot, E_rot standard", m0, "+-", e0, "delayed-acceptance kernels", m1, "+-", e1, "z", z)
+    assert np.all(np.isfinite(z)) and np.all(np.abs(z) <= 3.0), z
+    assert int(np.sum(np.abs(z) > 2.0)) <= 1, z
