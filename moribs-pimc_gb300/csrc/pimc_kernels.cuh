@@ -650,20 +650,23 @@ __device__ __forceinline__ double fmod_2pi(double x, double pi2)
 }
 
 // the proposal of MCRotLinStep (mc_piqmc.cc:801-820) / MCRot3Dstep
-// (mc_piqmc.cc:955-1001): out = (phi, cos theta, chi)
+// (mc_piqmc.cc:955-1001): out = (phi, cos theta, chi).  Each product and sum
+// rounded on its own (no fused multiply-add), as the reference's source
+// states them, so that every kernel that inlines this makes the same
+// proposal to the last bit.
 __device__ __forceinline__ void rot_propose(const DevSys &s, bool linear, double phi, double cost, double chi,
                                             const double u[4], double out[3])
 {
   if (linear) {
-    cost += (s.rtstep * (u[0] - 0.5));
-    phi += (s.rtstep * (u[1] - 0.5));
+    cost = __dadd_rn(cost, __dmul_rn(s.rtstep, __dsub_rn(u[0], 0.5)));
+    phi = __dadd_rn(phi, __dmul_rn(s.rtstep, __dsub_rn(u[1], 0.5)));
     if (cost > 1.0) cost = 2.0 - cost;
     if (cost < -1.0) cost = -2.0 - cost;
   } else {
     const double pi2 = 2.0 * PIMC_PI;
-    cost += (s.rtstep * (u[0] - 0.5));
-    phi += 2.0 * PIMC_PI * (s.rtstep * (u[1] - 0.5));
-    chi += 2.0 * PIMC_PI * (s.rtstep * (u[2] - 0.5));
+    cost = __dadd_rn(cost, __dmul_rn(s.rtstep, __dsub_rn(u[0], 0.5)));
+    phi = __dadd_rn(phi, __dmul_rn(2.0 * PIMC_PI, __dmul_rn(s.rtstep, __dsub_rn(u[1], 0.5))));
+    chi = __dadd_rn(chi, __dmul_rn(2.0 * PIMC_PI, __dmul_rn(s.rtstep, __dsub_rn(u[2], 0.5))));
     if (phi < 0.0) phi = pi2 + phi;
     if (chi < 0.0) chi = pi2 + chi;
     phi = fmod_2pi(phi, pi2);
