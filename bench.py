@@ -907,23 +907,20 @@ def run_fp64_pipe(local, iters=20000):
 
 def run_water_chains(local, steps, n=64):
     """A small case of the config-4 batch (the first n water-chain replicas'
-    worth of the family, FP32 path, shape 8 x 4) in rotation modes 1 and 2
-    (a warp or a thread per slice pair): one untimed pass, then `steps`
-    passes timed with CUDA events (for profiling the half-sweep kernels on a
-    small case)."""
+    worth of the family, FP32 path, rotation mode 1, shape 8 x 4): one
+    untimed pass, then `steps` passes timed with CUDA events (for profiling
+    the half-sweep kernel on a small case)."""
     import pimc_gb300 as G
     import workloads as W
     ws = W.config4(n=n)
-    out = {"workload": "config4 family, %d replicas, FP32 path" % n}
-    for mode in (1, 2):
-        b = G.Batch(ws, device=local, mixed=True)
-        b.set_shape(8, 4)
-        b.set_rotation_mode(mode)
-        _, ms = batch_series(b, steps, 3, 1)
-        bm = b.bead_moves_per_pass()
-        b.close()
-        out["mode%d" % mode] = {"pass_ms": round(ms, 2), "bead_moves_per_s": round(bm / (ms / 1e3), 1)}
-    return out
+    b = G.Batch(ws, device=local, mixed=True)
+    b.set_shape(8, 4)
+    b.set_rotation_mode(1)
+    _, ms = batch_series(b, steps, 3, 1)
+    bm = b.bead_moves_per_pass()
+    b.close()
+    return {"workload": "config4 family, %d replicas, FP32 path, rotation mode 1" % n, "pass_ms": round(ms, 2),
+            "bead_moves_per_s": round(bm / (ms / 1e3), 1)}
 
 
 def crossover(w, line):
@@ -956,9 +953,8 @@ def run_matched_se(local, mode="default", c4_replicas=512, c3_replicas=512, c4_s
     GPU path -- each replica alone on the single-system sampler in FP64, the
     reference's arithmetic; its pass time measured on a seeded sample of
     replicas and scaled to all -- and the batch on the FP32 path with one
-    launch per half-sweep over all replicas (rotation mode 1 or 2, the faster
-    on this pass).  g (2 tau_int of E, in passes) comes from the batch's
-    series; the plain chains make the
+    launch per half-sweep over all replicas (rotation mode 1).  g (2 tau_int
+    of E, in passes) comes from the batch's series; the plain chains make the
     same moves in FP64 (the statistics tests compare both precisions with the
     oracle), so their g is taken as the batch's.  The FP64 batch is timed on
     a replica subset, for its rate only.
@@ -997,13 +993,7 @@ def run_matched_se(local, mode="default", c4_replicas=512, c3_replicas=512, c4_s
     lap("config4_plain")
     b = G.Batch(ws, mixed=True)
     b.set_shape(*c4_shape)
-    # the half-sweep kernel: a warp (mode 1) or a thread (mode 2) per slice
-    # pair, whichever makes the faster pass (one untimed and one timed each)
-    mode_ms = {}
-    for mode in (1, 2):
-        b.set_rotation_mode(mode)
-        _, mode_ms[mode] = batch_series(b, 1, 20, 1)
-    rot_mode = min(mode_ms, key=mode_ms.get)
+    rot_mode = 1
     b.set_rotation_mode(rot_mode)
     lap("config4_batch_setup")
     E, ms = batch_series(b, 4 if quick else 8, 21, 1)
@@ -1035,8 +1025,7 @@ def run_matched_se(local, mode="default", c4_replicas=512, c3_replicas=512, c4_s
                           "rotation": acc[5] / max(1, tot[5])},
         "batched_fp64_subset": {"replicas": len(sub), "pass_ms": round(ms64, 1),
                                 "bead_moves_per_s": round(bm_sub / (ms64 / 1e3), 1)},
-        "shape": {"warps_per_cta": c4_shape[0], "ctas_per_sm_bound": c4_shape[1], "rotation_mode": rot_mode,
-                  "pass_ms_by_rotation_mode": {str(k): round(v, 1) for k, v in mode_ms.items()}},
+        "shape": {"warps_per_cta": c4_shape[0], "ctas_per_sm_bound": c4_shape[1], "rotation_mode": rot_mode},
         "time_to_se": matched(plain_ms, st["g"], arms)}
     # ---------------- water dimers with the surrogate
     d0 = W.config3(seed=300, nslices=512, nrotslices=256, levels=4)

@@ -421,11 +421,9 @@ pimc_status pimc_batch_set_shape(pimc_batch *b, int warps, int min_blocks);
  * pass, each CTA sweeping its own replica's slices; 1 one launch per
  * half-sweep over all replicas, one warp per (replica, slice pair) -- for
  * replicas with many rotational slices, whose sweeps would otherwise keep
- * one CTA busy long after the others finished; 2 as 1 with one thread per
- * (replica, slice pair) -- for moves with few enough partner terms that one
- * thread's loop over them costs less than a warp's serial stages.  All make
- * the same moves with the same draws in the same order per replica
- * (identical paths); 1 and 2 need an even Q in every replica. */
+ * one CTA busy long after the others finished.  Both make the same moves
+ * with the same draws in the same order per replica (identical paths); 1
+ * needs an even Q in every replica. */
 pimc_status pimc_batch_set_rotation_mode(pimc_batch *b, int mode);
 pimc_status pimc_batch_autotune(pimc_batch *b, uint64_t seed, int *shape_out, double *ms_out);
 pimc_status pimc_batch_run_passes(pimc_batch *b, int npasses, uint64_t seed);

@@ -6,8 +6,6 @@
 // turn, no CTA barrier inside a block), then the block's rotational sweeps
 // with one warp per slice of a half-sweep.  The warps' partner sums use a
 // per-warp item buffer; each slot is summed by one lane in item order.
-#include <type_traits>
-
 #include "pimc_kernels.cuh"
 #include "pimc_launch.h"
 
@@ -740,234 +738,6 @@ __global__ void __launch_bounds__(256, MINB) k_batch_rot_flat(const BatchRep *re
   }
 }
 
-// warp_rot on one thread: the same draws, partner terms, sums (each slot's
-// terms added in partner order, split where the warp's item buffer splits
-// them), link densities, test and commit, so the same path.  A warp then
-// makes 32 moves at once: the serial stages (proposal, frame, densities,
-// test) run on all lanes instead of one, which on the FP64 units (a
-// warp-level instruction costs the same with one lane as with 32) is the
-// dominant saving.
-template <bool MIX>
-__device__ int thread_rot(const Ctx &c, Frame *frames, int g0, int q, const double u[4], const double prop[3],
-                          bool linear)
-{
-  const DevSys &s = c.s;
-  const int Q = s.Q, R = s.R;
-  const size_t n = (size_t)s.nrotors * Q;
-  int q0 = q - 1, q2 = q + 1;
-  if (q0 < 0) q0 += Q;
-  if (q2 >= Q) q2 -= Q;
-  const int r = g0 - s.rot_first;
-  const int i0 = r * Q + q0, i1 = r * Q + q, i2 = r * Q + q2;
-  const bool need64 = !MIX;
-  const bool use_links = Q >= 3;
-  const int pot_cached = c.st.rp_ok[i1];
-  const double pot_c = pot_cached ? c.st.rp_cache[i1] : 0.0;
-  const int link_ok[2] = {use_links && c.st.rl_ok[i0], use_links && c.st.rl_ok[i1]};
-  double rho[4] = {0.0, 0.0, 0.0, 0.0};
-  if (link_ok[0]) rho[0] = c.st.rl_cache[i0];
-  if (link_ok[1]) rho[1] = c.st.rl_cache[i1];
-  Frame fn, fo[3];
-  float nnewf[3] = {0.0f, 0.0f, 0.0f}, nvf0[3] = {0.0f, 0.0f, 0.0f}, nvf[3] = {0.0f, 0.0f, 0.0f},
-        nvf2[3] = {0.0f, 0.0f, 0.0f};
-  double nnew[3] = {0.0, 0.0, 0.0}, nv[3][3] = {{0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}};
-  if (linear) {
-    if (MIX) unit_vector32((float)prop[0], (float)prop[1], nnewf);
-    else unit_vector(prop[0], prop[1], nnew);
-  } else if (need64) {
-    make_frame(prop[0], prop[1], prop[2], fn);
-  } else {
-    make_frame32((float)prop[0], (float)prop[1], (float)prop[2], fn.mf, &fn.hzf);
-  }
-  const bool lazy = linear && lazy_linear(c, MIX);
-  if (linear) {
-    for (int k = 0; k < 3; k++)
-      for (int d = 0; d < 3; d++) {
-        const int ii = (k == 0) ? i0 : (k == 1 ? i1 : i2);
-        if (lazy) {
-          const float v = c.st.cosvf[d * n + ii];
-          if (k == 0) nvf0[d] = v;
-          else if (k == 1) nvf[d] = v;
-          else nvf2[d] = v;
-        } else {
-          nv[k][d] = c.st.cosv[d * n + ii];
-          if (k == 1) nvf[d] = c.st.cosvf[d * n + ii];
-        }
-      }
-  } else if (MIX) {
-    for (int k = 0; k < 3; k++) {
-      const Frame &src = frames[k == 0 ? i0 : (k == 1 ? i1 : i2)];
-      for (int e = 0; e < 9; e++) fo[k].mf[e] = src.mf[e];
-      fo[k].hzf = src.hzf;
-    }
-  } else {
-    fo[0] = frames[i0];
-    fo[1] = frames[i1];
-    fo[2] = frames[i2];
-  }
-  // partner sums: the R old slots unless the rotor-potential cache holds them, then the R new ones
-  const int first = pot_cached ? R : 0;
-  const int nsl = 2 * R - first;
-  double vals[2 * 16];
-  const int npart = s.na - 1;
-  using T = typename std::conditional<MIX, float, double>::type;
-  const int cap = PIMC_BATCH_BUF * (int)(sizeof(double) / sizeof(T));
-  const int chunk = (npart <= cap) ? (npart > 0 ? (cap / npart) * npart : cap) : cap;
-  for (int sl = 0; sl < nsl; sl++) {
-    const int k = sl + first, it = q * R + (k % R);
-    T acc = T(0);
-    double out = 0.0;
-    bool started = false;
-    for (int pi = 0; pi < npart; pi++) {
-      if (pi > 0 && (sl * npart + pi) % chunk == 0) {        // the warp's buffer ends inside this slot
-        out = started ? out + (double)acc : (double)acc;
-        started = true;
-        acc = T(0);
-      }
-      const int p = pi < g0 ? pi : pi + 1;
-      if (linear) {
-        if (MIX) acc += (T)rotlin_term32(c, k < R ? nvf : nnewf, g0, p, it);
-        else acc += (T)rotlin_term64(c, k < R ? nv[1] : nnew, g0, p, it);
-      } else {
-        if (MIX) acc += (T)rot3d_term32(c, frames, k < R ? fo[1] : fn, g0, p, it);
-        else acc += (T)rot3d_term64(c, frames, k < R ? fo[1] : fn, g0, p, it);
-      }
-    }
-    vals[sl] = started ? out + (double)acc : (double)acc;
-  }
-  // 0: (q-1, q) old, 1: (q, q+1) old, 2: (q-1, q) new, 3: (q, q+1) new
-  int bad = 0;
-#pragma unroll
-  for (int l = 0; l < 4; l++) {
-    if (l < 2 && link_ok[l]) continue;
-    int b = 0;
-    double v;
-    if (linear) {
-      if (MIX && c.t.rd4 && s.rot_den_type == 0) {
-        const float *fa = (l == 0 || l == 2) ? nvf0 : (l == 1 ? nvf : nnewf);
-        const float *fb = (l == 0) ? nvf : (l == 2 ? nnewf : nvf2);
-        v = (double)srotdens32(c.t, one_minus_dot32(fa, fb));
-      } else {
-        double nn[3];
-        if (MIX) unit_vector(prop[0], prop[1], nn);
-        else for (int d = 0; d < 3; d++) nn[d] = nnew[d];
-        const double *na = (l == 0 || l == 2) ? nv[0] : (l == 1 ? nv[1] : nn);
-        const double *nb = (l == 0) ? nv[1] : (l == 2 ? nn : nv[2]);
-        v = link_density(c, true, fo[0], fo[0], na, nb, &b);
-      }
-    } else {
-      const Frame &fa = (l == 0 || l == 2) ? fo[0] : (l == 1 ? fo[1] : fn);
-      const Frame &fb = (l == 0) ? fo[1] : (l == 2 ? fn : fo[2]);
-      if (MIX && s.rot_den_type == 0) v = (double)rotden_rho32(c.t, fa.mf, fb.mf, &b);
-      else if (MIX) v = s.rot_odevn == -1 ? (double)rsrot32(fa.mf, fb.mf, s.rs_coef) : 0.0;
-      else v = link_density(c, false, fa, fb, nullptr, nullptr, &b);
-    }
-    rho[l] = v;
-    bad |= b;
-  }
-  double pot_old = 0.0, pot_new = 0.0;
-  if (pot_cached) pot_old = pot_c;
-  else
-    for (int k = 0; k < R; k++) pot_old += vals[k];
-  for (int k = 0; k < R; k++) pot_new += vals[R - first + k];
-  const double boltz = rot_boltz<MIX>(s, pot_old, pot_new);
-  const double logu = rot_logu<MIX>(s, u[linear ? 2 : 3]);
-  double rd;
-  int neg = 0;
-  int acc = rot_decide<MIX>(s, linear, rho, pot_old, pot_new, boltz, logu, u, &rd, &neg, false);
-  if (neg) { atomicOr(c.st.err, (unsigned)DERR_NEG_DENSITY); acc = 0; }
-  if (bad) { atomicOr(c.st.err, (unsigned)DERR_GRID_RANGE); acc = 0; }
-  if (acc) {
-    c.st.ang[i1] = prop[0];
-    c.st.ang[n + i1] = prop[1];
-    if (linear) {
-      if (lazy) {
-        for (int d = 0; d < 3; d++) c.st.cosvf[d * n + i1] = nnewf[d];
-      } else {
-        double cv[3];
-        if (MIX) unit_vector(prop[0], prop[1], cv);
-        else for (int d = 0; d < 3; d++) cv[d] = nnew[d];
-        for (int d = 0; d < 3; d++) {
-          c.st.cosv[d * n + i1] = cv[d];
-          c.st.cosvf[d * n + i1] = (float)cv[d];
-        }
-      }
-    } else {
-      c.st.ang[2 * n + i1] = prop[2];
-      if (need64) {
-        frames[i1] = fn;
-      } else {
-        for (int k = 0; k < 9; k++) frames[i1].mf[k] = fn.mf[k];
-        frames[i1].hzf = fn.hzf;
-      }
-      for (int rr = 0; rr < s.nrotors; rr++)
-        if (rr != r) c.st.rp_ok[rr * Q + q] = 0;
-    }
-  }
-  c.st.rp_cache[i1] = acc ? pot_new : pot_old;
-  c.st.rp_ok[i1] = 1;
-  if (use_links && !bad) {
-    c.st.rl_cache[i0] = acc ? rho[2] : rho[0];
-    c.st.rl_cache[i1] = acc ? rho[3] : rho[1];
-    c.st.rl_ok[i0] = 1;
-    c.st.rl_ok[i1] = 1;
-  }
-  return acc;
-}
-
-// one half-sweep of block blk's time slice j over the active replicas, one
-// thread per (replica, slice of the parity): k_batch_rot_flat's moves, each
-// made by thread_rot; rotation mode 2
-template <bool MIX>
-__global__ void __launch_bounds__(128, 3) k_batch_rot_thr(const BatchRep *reps, const int *sorted, const int *pre,
-                                                       int nact, int blk, int j, int parity, int nbk,
-                                                       uint64_t seed)
-{
-  const int u = blockIdx.x * blockDim.x + threadIdx.x;
-  const bool live = u < pre[nact];
-  unsigned long long *cnt = nullptr;
-  unsigned tot = 0, nacc = 0;
-  if (live) {
-    int lo = 0, hi = nact;                              // pre[lo] <= u < pre[hi]
-    while (hi - lo > 1) {
-      const int mid = (lo + hi) >> 1;
-      if (pre[mid] <= u) lo = mid;
-      else hi = mid;
-    }
-    const BatchRep &rp = reps[sorted[lo]];
-    const Ctx &c = rp.c;
-    const DevSys &s = c.s;
-    const unsigned ps = *rp.pass;
-    const uint64_t sr = seed ^ rp.seed_mix;
-    const bool linear = s.molecule[s.imtype] == 1;
-    unsigned B = 0;
-    for (int t = 0; t < s.ntypes; t++) B += (unsigned)((1 << s.levels[t]) * s.numb[t]);
-    const int it = (int)((long long)blk * s.P / nbk) + j;
-    const unsigned phase = B + 2u * (unsigned)it + (unsigned)parity;
-    const int q = parity + 2 * (u - pre[lo]);
-    const size_t nq = (size_t)s.nrotors * s.Q;
-    for (int rr = 0; rr < s.nrotors; rr++) {
-      double uu[4], prop[3];
-      const size_t i1 = (size_t)rr * s.Q + q;
-      rot_uniforms_t<MIX>(sr, ps, phase, q >> 1, rr, linear, uu);
-      rot_propose_t<MIX>(s, linear, c.st.ang[i1], c.st.ang[nq + i1], c.st.ang[2 * nq + i1], uu, prop);
-      nacc += (unsigned)thread_rot<MIX>(c, rp.frames, s.rot_first + rr, q, uu, prop, linear);
-      tot++;
-    }
-    cnt = rp.cnt + (s.imtype * 3 + 2) * 2;
-  }
-  // the counters once per (warp, replica)
-  __syncwarp();
-  const unsigned long long key = live ? (unsigned long long)cnt : 0ull;
-  const unsigned grp = __match_any_sync(0xffffffffu, key);
-  const unsigned gt = __reduce_add_sync(grp, tot), ga = __reduce_add_sync(grp, nacc);
-  const int lane = threadIdx.x & 31;
-  if (live && lane == __ffs(grp) - 1) {
-    atomicAdd(cnt, (unsigned long long)gt);
-    atomicAdd(cnt + 1, (unsigned long long)ga);
-  }
-}
-
 size_t batch_flat_smem_bytes(int warps) { return (size_t)warps * sizeof(WarpMem); }
 
 // minb: resident CTAs per SM the registers are bounded for (2, 3 or 4)
@@ -988,15 +758,6 @@ void launch_batch_rot_flat(const BatchRep *reps, const int *sorted, const int *p
     else PIMC_FLAT(false, 2);
   }
 #undef PIMC_FLAT
-}
-
-void launch_batch_rot_thr(const BatchRep *reps, const int *sorted, const int *pre, int nact, int units, int blk,
-                          int j, int parity, int nbk, uint64_t seed, int mixed, cudaStream_t s)
-{
-  if (units <= 0) return;
-  const int nctas = (units + 127) / 128;
-  if (mixed) k_batch_rot_thr<true><<<nctas, 128, 0, s>>>(reps, sorted, pre, nact, blk, j, parity, nbk, seed);
-  else k_batch_rot_thr<false><<<nctas, 128, 0, s>>>(reps, sorted, pre, nact, blk, j, parity, nbk, seed);
 }
 
 template <bool MIX, int MINB>

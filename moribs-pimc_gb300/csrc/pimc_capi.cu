@@ -2211,8 +2211,8 @@ extern "C" pimc_status pimc_batch_set_shape(pimc_batch *b, int warps, int min_bl
 
 extern "C" pimc_status pimc_batch_set_rotation_mode(pimc_batch *b, int mode)
 {
-  if (!b || mode < 0 || mode > 2) return PIMC_ERR_BAD_ARG;
-  if (mode >= 1)
+  if (!b || mode < 0 || mode > 1) return PIMC_ERR_BAD_ARG;
+  if (mode == 1)
     for (int r = 0; r < b->n; r++) {
       const DevSys &d = b->reps[r].c.s;
       if (d.nrotors > 0 && b->sys[r].rotation && d.Q % 2) return PIMC_ERR_BAD_ARG;   // the odd-Q serial step
@@ -2294,7 +2294,7 @@ extern "C" pimc_status pimc_batch_run_passes(pimc_batch *b, int npasses, uint64_
     const DevSys &d0 = b->reps[0].c.s;
     int nbk = 0;
     for (int t = 0; t < d0.ntypes; t++) nbk += 1 << d0.levels[t];
-    if (b->rot_mode >= 1) {
+    if (b->rot_mode == 1) {
       if ((e = batch_flat_tables(b, nbk))) return e;
       if (!batch_flat_setup(b->warps)) return PIMC_ERR_CUDA;
     }
@@ -2309,16 +2309,11 @@ extern "C" pimc_status pimc_batch_run_passes(pimc_batch *b, int npasses, uint64_
         launch_batch_pass(b->d_reps, b->d_order, b->n, seed, b->d_work, b->mixed, b->warps, b->minb, nctas,
                           h->stream, 0, blk, blk + 1);
         for (int j = 0; j < b->flat_nact_max[blk]; j++)
-          for (int parity = 0; parity < 2; parity++) {
-            const int *sorted = b->d_flat_sorted + (size_t)blk * b->n;
-            const int *pre = b->d_flat_pre + (size_t)blk * (b->n + 1);
-            if (b->rot_mode == 2)
-              launch_batch_rot_thr(b->d_reps, sorted, pre, b->flat_act[blk][j], b->flat_units[blk][j], blk, j,
-                                   parity, nbk, seed, b->mixed, h->stream);
-            else
-              launch_batch_rot_flat(b->d_reps, sorted, pre, b->flat_act[blk][j], b->flat_units[blk][j], blk, j,
-                                    parity, nbk, seed, b->mixed, b->warps, b->minb, h->stream);
-          }
+          for (int parity = 0; parity < 2; parity++)
+            launch_batch_rot_flat(b->d_reps, b->d_flat_sorted + (size_t)blk * b->n,
+                                  b->d_flat_pre + (size_t)blk * (b->n + 1), b->flat_act[blk][j],
+                                  b->flat_units[blk][j], blk, j, parity, nbk, seed, b->mixed, b->warps,
+                                  b->minb, h->stream);
       }
     }
     cudaError_t le = cudaGetLastError();
@@ -2338,7 +2333,7 @@ extern "C" pimc_status pimc_batch_run_passes(pimc_batch *b, int npasses, uint64_
     b->exec_rot_mode = b->rot_mode;
     b->exec_flat_minb = b->minb;
     long long nodes = 2;
-    if (b->rot_mode >= 1) {
+    if (b->rot_mode == 1) {
       nodes = 2LL * nbk;
       for (int blk = 0; blk < nbk; blk++)
         for (int j = 0; j < b->flat_nact_max[blk]; j++) nodes += 2 * (b->flat_units[blk][j] > 0);

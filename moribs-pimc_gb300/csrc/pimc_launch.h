@@ -103,8 +103,6 @@ void launch_batch_rot_flat(const BatchRep *reps, const int *sorted, const int *p
                            int j, int parity, int nbk, uint64_t seed, int mixed, int warps, int minb,
                            cudaStream_t s);
 int batch_flat_setup(int warps);
-void launch_batch_rot_thr(const BatchRep *reps, const int *sorted, const int *pre, int nact, int units, int blk,
-                          int j, int parity, int nbk, uint64_t seed, int mixed, cudaStream_t s);
 void launch_batch_rot_changed(const BatchRep *reps, int n, cudaStream_t s);
 void launch_batch_est(const BatchRep *reps, int n, double *out, cudaStream_t s);
 void launch_batch_refresh(const BatchRep *reps, int n, int derive, cudaStream_t s);

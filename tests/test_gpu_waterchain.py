@@ -92,13 +92,13 @@ def test_water_chain_counts_the_reference_schedule():
 
 @pytest.mark.parametrize("mixed", [False, True])
 def test_flat_half_sweeps_equal_the_persistent_pass(mixed):
-    """Rotation modes 1 and 2 (one launch per half-sweep over all replicas, a
-    warp or a thread per slice pair) make the persistent pass's moves with
-    its draws in its order per replica: the same paths and counters, bit for
-    bit, for the water chains and for the linear-rotor family."""
+    """Rotation mode 1 (one launch per half-sweep over all replicas, a warp
+    per slice pair) makes the persistent pass's moves with its draws in its
+    order per replica: the same paths and counters, bit for bit, for the
+    water chains and for the linear-rotor family."""
     for ws in (_family(), W.config2(n=5, seed=3, p_choices=(64, 128), n_he=(1, 6), t_range=(0.4, 1.5))):
         out = []
-        for mode in (0, 1, 2):
+        for mode in (0, 1):
             b = G.Batch(ws, mixed=mixed)
             b.set_shape(4)
             b.set_rotation_mode(mode)
@@ -106,7 +106,7 @@ def test_flat_half_sweeps_equal_the_persistent_pass(mixed):
             b.synchronize()
             out.append(([b.get_state(r)[:2] for r in range(len(ws))], b.counters()))
             b.close()
-        for m in (1, 2):
+        for m in (1,):
             for (c0, a0), (c1, a1) in zip(out[0][0], out[m][0]):
                 np.testing.assert_array_equal(c0, c1)
                 np.testing.assert_array_equal(a0, a1)
