@@ -962,9 +962,11 @@ def run_matched_se(local, mode="default", c4_replicas=512, c3_replicas=512, c4_s
     Water dimers (config 3 molecules, T 0.74 K, P = 512, Q = 256, levels 4,
     reduced slices so that a series fits the run): the plain GPU path, the
     batch with its rotational sweeps made by the delayed-acceptance kernels
-    without a screen (plain Metropolis; its g is the plain path's) and with
-    the screen of the surrogate trained on the plain sampler's own rows; in
-    the "full" mode also the batch with its sweeps in the half-sweep kernel.
+    without a screen (plain Metropolis, in FP64 -- its g is the plain
+    path's -- and on the FP32 path) and, on the FP32 path, with the screen of
+    the surrogate trained on the plain sampler's own rows; in the "full" mode
+    also the screened batch in FP64 and the batch with its sweeps in the
+    half-sweep kernel.
 
     mode: "quick" (short series, for tests of the harness), "default" (the
     bench line), "full" (more sampled plain replicas, the extra dimer arm)."""
@@ -1056,11 +1058,14 @@ def run_matched_se(local, mode="default", c4_replicas=512, c3_replicas=512, c4_s
     darms = {}
     npd = 6 if quick else 32
     eq = 1 if quick else 4
-    runs = [("batched_da_exact", (None, sd)), ("batched_surrogate", (m, sd))]
+    # the unscreened and the screened batch (FP32 path); the unscreened one in
+    # FP64 too (the plain path's arithmetic, its g is the plain path's)
+    runs = [("batched_da_exact", (None, sd), False), ("batched_da_exact_fp32", (None, sd), True),
+            ("batched_surrogate_fp32", (m, sd), True)]
     if full:
-        runs.append(("batched_plain", None))
-    for name, da in runs:
-        b = G.Batch(dims)
+        runs += [("batched_surrogate", (m, sd), False), ("batched_plain", None, False)]
+    for name, da, mixed in runs:
+        b = G.Batch(dims, mixed=mixed)
         if da is None:
             b.set_rotation_mode(1)
         E, ms = batch_series(b, npd, 31, eq, da=da)

@@ -306,8 +306,10 @@ pimc_status pimc_mlp_train(pimc_mlp *m, int n, const float *x, const float *e, i
  * summed over the rotor's slices, and the second with
  * min(1, exp(-tau (dV - dV_sur))) from the exact caleng difference, so the
  * sampled distribution is the exact one; without it the plain Metropolis
- * move.  stats[4] = moves, passed the first stage, accepted, exact
- * differences evaluated. */
+ * move.  On the FP32 path (pimc_set_precision(h, 1)) the moves use the float
+ * proposal, frames, densities, features and caleng terms of that path, the
+ * differences and tests in double.  stats[4] = moves, passed the first
+ * stage, accepted, exact differences evaluated. */
 pimc_status pimc_da_samples(pimc_handle *h, float *feat, float *energy);
 pimc_status pimc_da_sweeps(pimc_handle *h, pimc_mlp *m, int nsweeps, uint64_t seed, float escale, int use_surrogate,
                            double *stats);

@@ -1375,10 +1375,6 @@ extern "C" pimc_status pimc_da_sweeps(pimc_handle *h, pimc_mlp *m, int nsweeps, 
   // same sweep count, seed, surrogate, scale and scratch come back
   auto record = [&]() -> long long {
     long long n = 1;
-    if (d.mixed) {                   // the delayed-acceptance moves read the double frames
-      launch_refresh_frames(h->ctx, h->frames, h->stream);
-      n++;
-    }
     launch_pass_begin(h->pass, h->stream);
     for (int sw = 0; sw < nsweeps; sw++)
       for (int par = 0; par < 2; par++)
@@ -2410,19 +2406,15 @@ static pimc_status batch_da_run(pimc_batch *b, pimc_mlp *m, int count, int passe
       for (int par = 0; par < 2; par++)
         for (int r = 0; r < 2; r++) {
           unsigned phase = 4u * (unsigned)sw + 2u * par + r;
-          n += launch_da_propose_b(b->d_reps, nm, b->n, r, par, phase, seed, feat, mv, h->stream);
+          n += launch_da_propose_b(b->d_reps, nm, b->n, r, par, phase, seed, feat, mv, b->mixed, h->stream);
           if (use_surrogate) n += mlp_forward_device(m, feat, (int)rows, y, h->stream);
           n += launch_da_decide_b(b->d_reps, nm, b->n, r, par, phase, seed, y, use_surrogate, escale, mv, st,
-                                  h->stream);
+                                  b->mixed, h->stream);
         }
     return n;
   };
   auto record = [&]() -> long long {
     long long n = 0;
-    if (b->mixed) {                  // the FP32 rotational moves leave the double frames to be derived
-      launch_batch_refresh(b->d_reps, b->n, 0, h->stream);
-      n++;
-    }
     if (passes) {
       // the translational moves advance the pass counters that key the sweeps' draws
       launch_batch_pass(b->d_reps, b->d_order, b->n, seed, b->d_work, b->mixed, b->warps, b->minb, nctas, h->stream,
@@ -2462,6 +2454,10 @@ static pimc_status batch_da_run(pimc_batch *b, pimc_mlp *m, int count, int passe
   for (int p = 0; p < nlaunch; p++) {
     CK(cudaGraphLaunch(b->da_exec, h->stream));
     h->launches += b->da_nodes;
+  }
+  if (b->mixed) {                    // the FP32 moves leave the double frames to be derived from the angles
+    launch_batch_refresh(b->d_reps, b->n, 0, h->stream);
+    h->launches++;
   }
   unsigned long long hs[4];
   CK(cudaMemcpyAsync(hs, st, sizeof(hs), cudaMemcpyDeviceToHost, h->stream));

@@ -40,6 +40,21 @@ __device__ __forceinline__ void dimer_features(const Frame &fa, const double ca[
   f[5] = (float)(m[2] * n[2] + m[5] * n[5] + m[8] * n[8]);
 }
 
+// the same six features from the float frames (FP32 path)
+__device__ __forceinline__ void dimer_features32(const float *m, const double ca[3], const float *nm,
+                                                 const double cb[3], float *f)
+{
+  const float R0 = (float)(cb[0] - ca[0]), R1 = (float)(cb[1] - ca[1]), R2 = (float)(cb[2] - ca[2]);
+  const float r = sqrtf(R0 * R0 + R1 * R1 + R2 * R2);
+  const float u0 = R0 / r, u1 = R1 / r, u2 = R2 / r;
+  f[0] = (r - 3.0f) * 2.0f;
+  f[1] = u0 * m[0] + u1 * m[3] + u2 * m[6];
+  f[2] = u0 * m[1] + u1 * m[4] + u2 * m[7];
+  f[3] = u0 * m[2] + u1 * m[5] + u2 * m[8];
+  f[4] = u0 * nm[2] + u1 * nm[5] + u2 * nm[8];
+  f[5] = m[2] * nm[2] + m[5] * nm[5] + m[8] * nm[8];
+}
+
 __device__ __forceinline__ void centre(const Ctx &c, int g, int it, double v[3])
 {
   size_t i = sidx(c.s, it, g);
@@ -64,7 +79,19 @@ __global__ void k_da_samples(Ctx c, const Frame *frames, float *feat, float *ene
   energy[it] = (float)caleng(f0, f1, c0[0], c0[1], c0[2], c1[0], c1[1], c1[2]);
 }
 
-// move k of the sub-phase (rotor r, slices of parity `parity`) of one system
+// the link density of two frames in the move's precision: rotden in double,
+// or rotden_rho32 from the float frames on the FP32 path
+template <bool MIX>
+__device__ __forceinline__ double da_link(const Ctx &c, const Frame &a, const Frame &b, int *bad)
+{
+  if (MIX) return (double)rotden_rho32(c.t, a.mf, b.mf, bad);
+  return rotden_rho(c.t, a, b, bad, nullptr, nullptr);
+}
+
+// move k of the sub-phase (rotor r, slices of parity `parity`) of one system.
+// FP32 path: the float uniforms and proposal increments, the float frame,
+// densities and features (as the FP32 rotational moves make them)
+template <bool MIX>
 __device__ __forceinline__ void da_propose_move(const Ctx &c, const Frame *frames, int k, int r, int parity,
                                                 unsigned phase, uint64_t seed, unsigned ps, float *feat, DaMove &d)
 {
@@ -74,29 +101,40 @@ __device__ __forceinline__ void da_propose_move(const Ctx &c, const Frame *frame
   const size_t n = (size_t)s.nrotors * Q;
   const int ri = rot_index(s, g, q);
   double u[4], prop[3];
-  rot_uniforms(seed, ps, phase, q, r, false, u);
-  rot_propose(s, false, c.st.ang[ri], c.st.ang[n + ri], c.st.ang[2 * n + ri], u, prop);
+  rot_uniforms_t<MIX>(seed, ps, phase, q, r, false, u);
+  rot_propose_t<MIX>(s, false, c.st.ang[ri], c.st.ang[n + ri], c.st.ang[2 * n + ri], u, prop);
   Frame &fn = d.fn;
-  make_frame(prop[0], prop[1], prop[2], fn);
+  if (MIX) make_frame32((float)prop[0], (float)prop[1], (float)prop[2], fn.mf, &fn.hzf);
+  else make_frame(prop[0], prop[1], prop[2], fn);
   const Frame &fo = frames[ri];
   const int im = rot_index(s, g, (q - 1 + Q) % Q);
   const Frame &fm = frames[im], &fp = frames[rot_index(s, g, (q + 1) % Q)];
-  // the old links from the link cache where it holds them (FP64 path: the
-  // cache then holds exactly rotden's value; link (q-1, q) at q-1's entry)
-  const bool links = !s.mixed && Q >= 3;
+  // the old links from the link cache where it holds them (it holds exactly
+  // what the move's precision evaluates; link (q-1, q) at q-1's entry)
+  const bool links = Q >= 3;
   int bad = 0;
-  const double l0n = rotden_rho(c.t, fm, fn, &bad, nullptr, nullptr), l1n = rotden_rho(c.t, fn, fp, &bad, nullptr, nullptr);
-  const double l0o = (links && c.st.rl_ok[im]) ? c.st.rl_cache[im] : rotden_rho(c.t, fm, fo, &bad, nullptr, nullptr);
-  const double l1o = (links && c.st.rl_ok[ri]) ? c.st.rl_cache[ri] : rotden_rho(c.t, fo, fp, &bad, nullptr, nullptr);
+  const double l0n = da_link<MIX>(c, fm, fn, &bad), l1n = da_link<MIX>(c, fn, fp, &bad);
+  const double l0o = (links && c.st.rl_ok[im]) ? c.st.rl_cache[im] : da_link<MIX>(c, fm, fo, &bad);
+  const double l1o = (links && c.st.rl_ok[ri]) ? c.st.rl_cache[ri] : da_link<MIX>(c, fo, fp, &bad);
   double rn = l0n * l1n;
   double ro = l0o * l1o;
+  if (MIX) {
+    // the float density ratio's terms as rot_decide forms them
+    rn = (double)((float)l0n * (float)l1n);
+    ro = (double)((float)l0o * (float)l1o);
+  }
   const Frame &fb = frames[rot_index(s, o, q)];
   for (int j = 0; j < R; j++) {
     double ca[3], cb[3];
     centre(c, g, q * R + j, ca);
     centre(c, o, q * R + j, cb);
-    dimer_features(fn, ca, fb, cb, feat + (2 * j) * 6);
-    dimer_features(fo, ca, fb, cb, feat + (2 * j + 1) * 6);
+    if (MIX) {
+      dimer_features32(fn.mf, ca, fb.mf, cb, feat + (2 * j) * 6);
+      dimer_features32(fo.mf, ca, fb.mf, cb, feat + (2 * j + 1) * 6);
+    } else {
+      dimer_features(fn, ca, fb, cb, feat + (2 * j) * 6);
+      dimer_features(fo, ca, fb, cb, feat + (2 * j + 1) * 6);
+    }
   }
   d.prop[0] = prop[0]; d.prop[1] = prop[1]; d.prop[2] = prop[2];
   d.rn = rn;
@@ -106,16 +144,18 @@ __device__ __forceinline__ void da_propose_move(const Ctx &c, const Frame *frame
   d.bad = bad;
 }
 
+template <bool MIX>
 __global__ void k_da_propose(Ctx c, const Frame *frames, int r, int parity, unsigned phase, uint64_t seed,
                              const unsigned *pass, float *feat, DaMove *mv)
 {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (2 * k + parity >= c.s.Q) return;
-  da_propose_move(c, frames, k, r, parity, phase, seed, *pass, feat + (size_t)k * 2 * c.s.R * 6, mv[k]);
+  da_propose_move<MIX>(c, frames, k, r, parity, phase, seed, *pass, feat + (size_t)k * 2 * c.s.R * 6, mv[k]);
 }
 
 // the same sub-phase of every replica of a batch: move j is replica j / nm's
 // move j % nm (replicas of one shape: the same Q and R)
+template <bool MIX>
 __global__ void k_da_propose_b(const BatchRep *reps, int nm, int nrep, int r, int parity, unsigned phase,
                                uint64_t seed, float *feat, DaMove *mv)
 {
@@ -123,7 +163,7 @@ __global__ void k_da_propose_b(const BatchRep *reps, int nm, int nrep, int r, in
   if (j >= nm * nrep) return;
   const int rep = j / nm, k = j - rep * nm;
   const BatchRep &b = reps[rep];
-  da_propose_move(b.c, b.frames, k, r, parity, phase, seed ^ b.seed_mix, *b.pass,
+  da_propose_move<MIX>(b.c, b.frames, k, r, parity, phase, seed ^ b.seed_mix, *b.pass,
                   feat + (size_t)j * 2 * b.c.s.R * 6, mv[j]);
 }
 
@@ -131,6 +171,7 @@ __global__ void k_da_propose_b(const BatchRep *reps, int nm, int nrep, int r, in
 // [2] accepted, [3] exact potential differences evaluated
 // returns bit 0: passed the first stage, bit 1: accepted, bit 2: exact
 // difference evaluated
+template <bool MIX>
 __device__ __forceinline__ unsigned da_decide_move(const Ctx &c, Frame *frames, int k, int r, int parity,
                                                    unsigned phase, uint64_t seed, unsigned ps, const float *y,
                                                    int use_sur, float escale, const DaMove &d)
@@ -158,11 +199,18 @@ __device__ __forceinline__ unsigned da_decide_move(const Ctx &c, Frame *frames, 
     const Frame &fo = frames[ri], &fb = frames[rot_index(s, o, q)];
     double dv = 0.0;
     for (int j = 0; j < R; j++) {
-      double ca[3], cb[3];
-      centre(c, g, q * R + j, ca);
-      centre(c, o, q * R + j, cb);
-      dv += caleng(fn, fb, ca[0], ca[1], ca[2], cb[0], cb[1], cb[2]) -
-            caleng(fo, fb, ca[0], ca[1], ca[2], cb[0], cb[1], cb[2]);
+      if (MIX) {
+        // the float pair terms from the float beads, their difference added in double
+        const float4 pa = c.st.b4[sidx(s, q * R + j, g)], pb = c.st.b4[sidx(s, q * R + j, o)];
+        dv += (double)(caleng32(fn.mf, fb.mf, pa.x, pa.y, pa.z, pb.x, pb.y, pb.z) -
+                       caleng32(fo.mf, fb.mf, pa.x, pa.y, pa.z, pb.x, pb.y, pb.z));
+      } else {
+        double ca[3], cb[3];
+        centre(c, g, q * R + j, ca);
+        centre(c, o, q * R + j, cb);
+        dv += caleng(fn, fb, ca[0], ca[1], ca[2], cb[0], cb[1], cb[2]) -
+              caleng(fo, fb, ca[0], ca[1], ca[2], cb[0], cb[1], cb[2]);
+      }
     }
     if (use_sur) acc = -s.tau * (dv - dvs) > log(u2);
     else acc = lr - s.tau * dv > log(u1);
@@ -170,12 +218,17 @@ __device__ __forceinline__ unsigned da_decide_move(const Ctx &c, Frame *frames, 
       c.st.ang[ri] = d.prop[0];
       c.st.ang[n + ri] = d.prop[1];
       c.st.ang[2 * n + ri] = d.prop[2];
-      frames[ri] = fn;
+      if (MIX) {                        // the double frame is derived from the angles later
+        for (int e = 0; e < 9; e++) frames[ri].mf[e] = fn.mf[e];
+        frames[ri].hzf = fn.hzf;
+      } else {
+        frames[ri] = fn;
+      }
     }
   }
   // the link cache after the move (its two links belong to this move alone
   // within the sub-phase)
-  if (!s.mixed && Q >= 3 && !d.bad) {
+  if (Q >= 3 && !d.bad) {
     const int im = rot_index(s, g, (q - 1 + Q) % Q);
     c.st.rl_cache[im] = acc ? d.ln[0] : d.lo[0];
     c.st.rl_cache[ri] = acc ? d.ln[1] : d.lo[1];
@@ -212,6 +265,7 @@ __device__ __forceinline__ void da_count(bool live, unsigned f, unsigned long lo
 
 // stats[0] moves, [1] passed the first stage (all, without the surrogate),
 // [2] accepted, [3] exact potential differences evaluated
+template <bool MIX>
 __global__ void k_da_decide(Ctx c, Frame *frames, int r, int parity, unsigned phase, uint64_t seed,
                             const unsigned *pass, const float *y, int use_sur, float escale, const DaMove *mv,
                             unsigned long long *stats, unsigned long long *cnt)
@@ -219,11 +273,12 @@ __global__ void k_da_decide(Ctx c, Frame *frames, int r, int parity, unsigned ph
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   const bool live = 2 * k + parity < c.s.Q;
   unsigned f = 0;
-  if (live) f = da_decide_move(c, frames, k, r, parity, phase, seed, *pass, y + (size_t)k * 2 * c.s.R, use_sur, escale,
+  if (live) f = da_decide_move<MIX>(c, frames, k, r, parity, phase, seed, *pass, y + (size_t)k * 2 * c.s.R, use_sur, escale,
                                mv[k]);
   da_count(live, f, stats, cnt + (c.s.imtype * 3 + 2) * 2);
 }
 
+template <bool MIX>
 __global__ void k_da_decide_b(const BatchRep *reps, int nm, int nrep, int r, int parity, unsigned phase,
                               uint64_t seed, const float *y, int use_sur, float escale, const DaMove *mv,
                               unsigned long long *stats)
@@ -234,7 +289,7 @@ __global__ void k_da_decide_b(const BatchRep *reps, int nm, int nrep, int r, int
   const BatchRep &b = reps[rep];
   unsigned f = 0;
   if (live)
-    f = da_decide_move(b.c, b.frames, k, r, parity, phase, seed ^ b.seed_mix, *b.pass, y + (size_t)j * 2 * b.c.s.R,
+    f = da_decide_move<MIX>(b.c, b.frames, k, r, parity, phase, seed ^ b.seed_mix, *b.pass, y + (size_t)j * 2 * b.c.s.R,
                        use_sur, escale, mv[j]);
   da_count(live, f, stats, b.cnt + (b.c.s.imtype * 3 + 2) * 2);
 }
@@ -258,7 +313,8 @@ int launch_da_propose(const Ctx &c, const Frame *f, int r, int parity, unsigned 
                       const unsigned *pass, float *feat, DaMove *mv, cudaStream_t s)
 {
   int nm = (c.s.Q + 1 - parity) / 2;
-  k_da_propose<<<(nm + 127) / 128, 128, 0, s>>>(c, f, r, parity, phase, seed, pass, feat, mv);
+  if (c.s.mixed) k_da_propose<true><<<(nm + 127) / 128, 128, 0, s>>>(c, f, r, parity, phase, seed, pass, feat, mv);
+  else k_da_propose<false><<<(nm + 127) / 128, 128, 0, s>>>(c, f, r, parity, phase, seed, pass, feat, mv);
   return 1;
 }
 
@@ -267,25 +323,35 @@ int launch_da_decide(const Ctx &c, Frame *f, int r, int parity, unsigned phase, 
                      unsigned long long *cnt, cudaStream_t s)
 {
   int nm = (c.s.Q + 1 - parity) / 2;
-  k_da_decide<<<(nm + 127) / 128, 128, 0, s>>>(c, f, r, parity, phase, seed, pass, y, use_sur, escale, mv, stats, cnt);
+  if (c.s.mixed)
+    k_da_decide<true><<<(nm + 127) / 128, 128, 0, s>>>(c, f, r, parity, phase, seed, pass, y, use_sur, escale, mv, stats,
+                                                       cnt);
+  else
+    k_da_decide<false><<<(nm + 127) / 128, 128, 0, s>>>(c, f, r, parity, phase, seed, pass, y, use_sur, escale, mv,
+                                                        stats, cnt);
   return 1;
 }
 
 int launch_da_propose_b(const BatchRep *reps, int nm, int nrep, int r, int parity, unsigned phase, uint64_t seed,
-                        float *feat, DaMove *mv, cudaStream_t s)
+                        float *feat, DaMove *mv, int mixed, cudaStream_t s)
 {
   const int n = nm * nrep;
-  k_da_propose_b<<<(n + 127) / 128, 128, 0, s>>>(reps, nm, nrep, r, parity, phase, seed, feat, mv);
+  if (mixed) k_da_propose_b<true><<<(n + 127) / 128, 128, 0, s>>>(reps, nm, nrep, r, parity, phase, seed, feat, mv);
+  else k_da_propose_b<false><<<(n + 127) / 128, 128, 0, s>>>(reps, nm, nrep, r, parity, phase, seed, feat, mv);
   return 1;
 }
 
 int launch_da_decide_b(const BatchRep *reps, int nm, int nrep, int r, int parity, unsigned phase, uint64_t seed,
                        const float *y, int use_sur, float escale, const DaMove *mv, unsigned long long *stats,
-                       cudaStream_t s)
+                       int mixed, cudaStream_t s)
 {
   const int n = nm * nrep;
-  k_da_decide_b<<<(n + 127) / 128, 128, 0, s>>>(reps, nm, nrep, r, parity, phase, seed, y, use_sur, escale, mv,
-                                                 stats);
+  if (mixed)
+    k_da_decide_b<true><<<(n + 127) / 128, 128, 0, s>>>(reps, nm, nrep, r, parity, phase, seed, y, use_sur, escale, mv,
+                                                        stats);
+  else
+    k_da_decide_b<false><<<(n + 127) / 128, 128, 0, s>>>(reps, nm, nrep, r, parity, phase, seed, y, use_sur, escale,
+                                                         mv, stats);
   return 1;
 }
 

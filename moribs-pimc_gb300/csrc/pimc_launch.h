@@ -90,9 +90,9 @@ struct BatchRep {
 
 size_t batch_smem_bytes(int warps);
 int launch_da_propose_b(const BatchRep *reps, int nm, int nrep, int r, int parity, unsigned phase, uint64_t seed,
-                        float *feat, DaMove *mv, cudaStream_t s);
+                        float *feat, DaMove *mv, int mixed, cudaStream_t s);
 int launch_da_decide_b(const BatchRep *reps, int nm, int nrep, int r, int parity, unsigned phase, uint64_t seed,
-                       const float *y, int use_sur, float escale, const DaMove *mv, unsigned long long *stats,
+                       const float *y, int use_sur, float escale, const DaMove *mv, unsigned long long *stats, int mixed,
                        cudaStream_t s);
 int launch_da_pass_b(const BatchRep *reps, int nrep, cudaStream_t s);
 int batch_max_ctas(int mixed, int warps, int minb);

@@ -25,17 +25,18 @@ def _mlp(seed=3):
     return m
 
 
+@pytest.mark.parametrize("mixed", [False, True])
 @pytest.mark.parametrize("surrogate", [False, True])
-def test_batch_da_replicas_equal_single_systems(surrogate):
+def test_batch_da_replicas_equal_single_systems(surrogate, mixed):
     ws = _dimers()
     m = _mlp() if surrogate else None
-    b = G.Batch(ws)
+    b = G.Batch(ws, mixed=mixed)
     seed = 12
     st = b.da_sweeps(6, seed, mlp=m, escale=300.0)
     assert st[0] == 6 * sum(w.nrotslices * 2 for w in ws)
     sst = np.zeros(4)
     for r, w in enumerate(ws):
-        s = G.Sampler(w)
+        s = G.Sampler(w, mixed=mixed)
         sst += s.da_sweeps(6, G.Batch.replica_seed(seed, r), mlp=m, escale=300.0)
         _, a, co, _ = s.get_state()
         _, ba, bco, _ = b.get_state(r)
@@ -67,11 +68,13 @@ def test_batch_da_passes_count_the_schedule():
     b.close()
 
 
-def test_batch_da_passes_sample_the_standard_distribution():
+@pytest.mark.parametrize("mixed", [False, True])
+def test_batch_da_passes_sample_the_standard_distribution(mixed):
     """Passes whose rotational sweeps are made by the delayed-acceptance
     kernels without a screen (plain Metropolis, the link cache of the
     tabulated densities kept by those kernels) and the batch's standard
-    passes sample the same distribution.  K identical dimers of the
+    passes sample the same distribution, in both precisions (on the FP32
+    path both arms make the FP32 path's moves).  K identical dimers of the
     statistics tests' config-3 shape (5 K, P = 64, Q = 32, bisection levels 2,
     centroid step 0.02 A), brought to equilibrium by EQ0 standard passes; each
     arm starts from those states, makes EQ passes of its own, then samples
@@ -83,13 +86,13 @@ def test_batch_da_passes_sample_the_standard_distribution():
     w = W.config3(seed=7, nslices=64, nrotslices=32, griddens=(19, 37, 37), levels=2)
     w.types[0]["mcstep"] = 0.02
     w.temperature = 5.0
-    b = G.Batch([w] * K)
+    b = G.Batch([w] * K, mixed=mixed)
     b.run_passes(EQ0, 31)
     start = [b.get_state(r) for r in range(K)]
     b.close()
     res = {}
     for arm, seed in (("standard", 1000), ("delayed", 2000)):
-        b = G.Batch([w] * K)
+        b = G.Batch([w] * K, mixed=mixed)
         for r, (c, a, _, p) in enumerate(start):
             b.set_state(r, c, a, p)
         run = b.run_passes if arm == "standard" else b.da_passes
