@@ -337,9 +337,11 @@ __device__ int warp_rot(const Ctx &c, Frame *frames, int g0, int q, const double
           for (int k = 0; k < 9; k++) frames[i1].mf[k] = w.fn.mf[k];
           frames[i1].hzf = w.fn.hzf;
         }
-        // the other rotors' potentials at slice q depend on this orientation
-        for (int rr = 0; rr < s.nrotors; rr++)
-          if (rr != r) c.st.rp_ok[rr * Q + q] = 0;
+        // the other rotors' potentials at slice q depend on this orientation:
+        // FP64 path, recomputed at their next move; FP32 path, updated below
+        if (!MIX)
+          for (int rr = 0; rr < s.nrotors; rr++)
+            if (rr != r) c.st.rp_ok[rr * Q + q] = 0;
       }
     }
     c.st.rp_cache[i1] = acc ? pot_new : pot_old;
@@ -352,6 +354,29 @@ __device__ int warp_rot(const Ctx &c, Frame *frames, int g0, int q, const double
     }
   }
   acc = __shfl_sync(0xffffffffu, acc, 0);
+  if (MIX && acc && !linear && s.nrotors > 1) {
+    // FP32 path: each other rotor's cached potential at slice q takes the
+    // change of its term with this rotor, slot by slot, instead of being
+    // recomputed over all its partners at its next move (caleng32 pairs
+    // (other rotor, slot) one per lane, summed per rotor in double)
+    const int npair = (s.nrotors - 1) * R;          // <= 15 x 16, within the warp's 256-double buffer
+    __syncwarp();
+    for (int l = lane; l < npair; l += 32) {
+      const int o = l / R, k = l - o * R, it = q * R + k;
+      const int grr = s.rot_first + (o < r ? o : o + 1);
+      const float4 pa = c.st.b4[sidx(s, it, grr)], pb = c.st.b4[sidx(s, it, g0)];
+      const float *mrr = frames[rot_index(s, grr, q)].mf;
+      buf[l] = (double)(caleng32(mrr, w.fn.mf, pa.x, pa.y, pa.z, pb.x, pb.y, pb.z) -
+                        caleng32(mrr, w.fo[1].mf, pa.x, pa.y, pa.z, pb.x, pb.y, pb.z));
+    }
+    __syncwarp();
+    if (lane < s.nrotors - 1) {
+      const int rr = lane < r ? lane : lane + 1;
+      double dsum = 0.0;
+      for (int k = 0; k < R; k++) dsum += buf[lane * R + k];
+      if (c.st.rp_ok[rr * Q + q]) c.st.rp_cache[rr * Q + q] += dsum;
+    }
+  }
   __syncwarp();
   return acc;
 }

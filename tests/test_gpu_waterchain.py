@@ -112,3 +112,43 @@ def test_flat_half_sweeps_equal_the_persistent_pass(mixed):
                 np.testing.assert_array_equal(a0, a1)
             np.testing.assert_array_equal(out[0][1][0], out[m][1][0])
             np.testing.assert_array_equal(out[0][1][1], out[m][1][1])
+
+
+def test_fp32_batch_samples_the_fp64_distribution():
+    """The FP32 path of the water-chain batch (float pair terms and densities;
+    each accepted rotor move updates the other rotors' cached potentials at
+    its slice by the change of their pair term instead of invalidating them)
+    samples the FP64 path's distribution.  K identical replicas of a small
+    chain (3 waters on the 3 A chain + 2 pH2, P = 64, Q = 16, 5 K), brought to
+    equilibrium by EQ0 FP64 passes; each precision starts from those states,
+    makes EQ passes of its own, then samples the estimators after every pass.
+    The error of a mean is the spread of the K chain means over sqrt(K).
+    Criterion: E_kin, E_pot and E_rot each within 3 combined standard errors
+    and at most one of the three beyond 2."""
+    K, EQ0, EQ, NS = 128, 200, 30, 100
+    tb = W.water_chain_tables(seed=5, grid3d=(30, 37, 19))
+    w = W.water_chain(3, 2, 64, 16, 5.0, [9, 7], tb, name="wc-stat")
+    b = G.Batch([w] * K)
+    b.set_rotation_mode(1)
+    b.run_passes(EQ0, 41)
+    start = [b.get_state(r) for r in range(K)]
+    b.close()
+    res = {}
+    for mixed, seed in ((False, 1000), (True, 2000)):
+        b = G.Batch([w] * K, mixed=mixed)
+        b.set_rotation_mode(1)
+        for r, (c, a, _, p) in enumerate(start):
+            b.set_state(r, c, a, p)
+        b.run_passes(EQ, seed)
+        acc = np.zeros((K, 3))
+        for k in range(NS):
+            b.run_passes(1, seed)
+            acc += b.estimators()[:, :3]
+        b.close()
+        means = acc / NS
+        res[mixed] = (means.mean(0), means.std(0, ddof=1) / np.sqrt(K))
+    (m0, e0), (m1, e1) = res[False], res[True]
+    z = (m1 - m0) / np.hypot(e0, e1)
+    print("E_kin, E_pot, E_rot FP64", m0, "+-", e0, "FP32 path", m1, "+-", e1, "z", z)
+    assert np.all(np.isfinite(z)) and np.all(np.abs(z) <= 3.0), z
+    assert int(np.sum(np.abs(z) > 2.0)) <= 1, z
