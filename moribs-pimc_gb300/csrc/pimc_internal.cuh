@@ -761,8 +761,9 @@ __device__ __forceinline__ float vcord32(const DevTables &t, const Frame &f, flo
   float rdoty = m[1] * Rx + m[4] * Ry + m[7] * Rz;
   float rdotz = m[2] * Rx + m[5] * Ry + m[8] * Rz;
   float rn2 = Rx * Rx + Ry * Ry + Rz * Rz;
-  float rn = sqrtf(rn2);
-  float thewff = atan2f(sqrtf(fmaxf(rdotx * rdotx + rdoty * rdoty, 0.0f)), rdotz);
+  float rn = rn2 * rsqrtf(rn2);       // a partner on the centre gives NaN, which the clamp below sends to rvmin
+  const float rho2 = rdotx * rdotx + rdoty * rdoty;
+  float thewff = atan2f(rho2 > 0.0f ? rho2 * rsqrtf(rho2) : 0.0f, rdotz);
   float chiwff = atan2f(fabsf(rdoty), fabsf(rdotx));
   float chir;
   if (rdotx >= 0.0f && rdoty >= 0.0f) chir = chiwff;
@@ -888,10 +889,14 @@ __device__ __forceinline__ float caleng32(const float *ma, const float *mb, floa
     float x = p[0] - q[0], y = p[1] - q[1], z = p[2] - q[2];
     return x * x + y * y + z * z;
   };
+  // the FP32 path's reciprocal distances and powers from the hardware
+  // reciprocal square root and reciprocal (within a few ulp of float, far
+  // inside the path's 1e-5 tolerance)
   const float roo = d2(a[0], b[0]);
-  const float roo6 = roo * roo * roo, roo12 = roo6 * roo6;
-  const float vlj = 6.e5f / roo12 - 610.0f / roo6;
-  auto inv = [&](const float *p, const float *q) { return 1.0f / sqrtf(d2(p, q)); };
+  const float iroo = __frcp_rn(roo);
+  const float iroo6 = iroo * iroo * iroo;
+  const float vlj = 6.e5f * iroo6 * iroo6 - 610.0f * iroo6;
+  auto inv = [&](const float *p, const float *q) { return rsqrtf(d2(p, q)); };
   const float vmh = qm * qh * (inv(a[1], b[2]) + inv(a[1], b[3]) + inv(b[1], a[2]) + inv(b[1], a[3]));
   const float vhh = qh * qh * (inv(a[2], b[2]) + inv(a[2], b[3]) + inv(a[3], b[2]) + inv(a[3], b[3]));
   const float vmm = qm * qm * inv(a[1], b[1]);
