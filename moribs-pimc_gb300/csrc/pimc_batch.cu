@@ -719,7 +719,7 @@ void launch_batch_pass(const BatchRep *reps, const int *order, int n, uint64_t s
 template <bool MIX, int MINB>
 __global__ void __launch_bounds__(256, MINB) k_batch_rot_flat(const BatchRep *reps, const int *sorted, const int *pre,
                                                         int nact, int blk, int j, int parity, int nbk,
-                                                        uint64_t seed)
+                                                        uint64_t seed, long long phase0)
 {
   extern __shared__ __align__(16) unsigned char smem[];
   WarpMem *wm = reinterpret_cast<WarpMem *>(smem);
@@ -742,7 +742,8 @@ __global__ void __launch_bounds__(256, MINB) k_batch_rot_flat(const BatchRep *re
   unsigned B = 0;
   for (int t = 0; t < s.ntypes; t++) B += (unsigned)((1 << s.levels[t]) * s.numb[t]);
   const int it = (int)((long long)blk * s.P / nbk) + j;
-  const unsigned phase = B + 2u * (unsigned)it + (unsigned)parity;
+  // the pass's phase of this half-sweep, or phase0 + parity where the caller keys it (the worm loop)
+  const unsigned phase = phase0 >= 0 ? (unsigned)phase0 + (unsigned)parity : B + 2u * (unsigned)it + (unsigned)parity;
   const int kk = u - pre[lo], q = parity + 2 * kk;
   const size_t nq = (size_t)s.nrotors * s.Q;
   unsigned long long tot = 0, nacc = 0;
@@ -767,12 +768,14 @@ size_t batch_flat_smem_bytes(int warps) { return (size_t)warps * sizeof(WarpMem)
 
 // minb: resident CTAs per SM the registers are bounded for (2, 3 or 4)
 void launch_batch_rot_flat(const BatchRep *reps, const int *sorted, const int *pre, int nact, int units, int blk,
-                           int j, int parity, int nbk, uint64_t seed, int mixed, int warps, int minb, cudaStream_t s)
+                           int j, int parity, int nbk, uint64_t seed, int mixed, int warps, int minb, cudaStream_t s,
+                           long long phase0)
 {
   if (units <= 0) return;
   const size_t sm = batch_flat_smem_bytes(warps);
   const int nctas = (units + warps - 1) / warps;
-#define PIMC_FLAT(M, B) k_batch_rot_flat<M, B><<<nctas, 32 * warps, sm, s>>>(reps, sorted, pre, nact, blk, j, parity, nbk, seed)
+#define PIMC_FLAT(M, B) \
+  k_batch_rot_flat<M, B><<<nctas, 32 * warps, sm, s>>>(reps, sorted, pre, nact, blk, j, parity, nbk, seed, phase0)
   if (mixed) {
     if (minb >= 4) PIMC_FLAT(true, 4);
     else if (minb == 3) PIMC_FLAT(true, 3);

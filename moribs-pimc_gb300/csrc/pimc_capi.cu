@@ -1244,7 +1244,9 @@ extern "C" pimc_status pimc_worm_move(pimc_handle *h, const double *const *strea
 // is closed, its bisection at a drawn slice (exchange for bosons) and at
 // slice 0 its exchange-cycle centroid move; the other types' PIMCPass
 // (mc_main.cc:510-522).  Uniform keys: phase 4t for the worm tries, 4t+1
-// the worm type's bisection, 4t+2 its centroid move, 4t+3 the other types.
+// the worm type's bisection, 4t+2 its centroid move, 4t+3 the other types'
+// translational moves; the rotational draws (their own key domain) phases
+// 2t and 2t+1 for the two half-sweeps at slice t.
 extern "C" pimc_status pimc_worm_run(pimc_handle *h, int npasses, uint64_t seed)
 {
   pimc_status e = ready(h);
@@ -1259,6 +1261,11 @@ extern "C" pimc_status pimc_worm_run(pimc_handle *h, int npasses, uint64_t seed)
   const int bose = d.stat[wt] == PIMC_BOSE;
   char *mscr = (char *)h->wscr + ((worm_scratch_bytes(d.na) + 255) / 256) * 256;
   ReplaySrc none{};
+  const bool flat_worm = h->sys.rotation && d.nrotors > 0 && d.Q >= 4 && d.Q % 2 == 0;
+  if (flat_worm) {
+    if ((e = upload_self_rep(h))) return e;
+    if (!batch_flat_setup(8)) return PIMC_ERR_CUDA;
+  }
   // one pass, recorded into a CUDA graph on the first call for this seed
   auto record = [&]() -> long long {
     long long n = 0;
@@ -1285,8 +1292,20 @@ extern "C" pimc_status pimc_worm_run(pimc_handle *h, int npasses, uint64_t seed)
         n += launch_bisect_slice(h->ctx, h->frames, type, t, 0, nullptr, seed, h->pass, 4u * t + 3, h->cnt,
                                  h->stream);
         if (type == d.imtype && h->sys.rotation) {
-          n += launch_rot_phase(h->ctx, h->frames, 0, 4u * t + 3, seed, h->pass, h->cnt, h->stream);
-          n += launch_rot_phase(h->ctx, h->frames, 1, 4u * t + 3, seed, h->pass, h->cnt, h->stream);
+          // the two half-sweeps draw from their own phases (slices 2p and 2p+1
+          // share the pair index p of the rotational draws' key); with an even
+          // Q a warp per slice pair (the half-sweep kernel over this handle),
+          // else a CTA per slice
+          if (flat_worm)
+            for (int parity = 0; parity < 2; parity++) {
+              launch_batch_rot_flat(h->self_rep, h->self_idx, h->self_idx + 1, 1, d.Q / 2, 0, 0, parity, 1, seed,
+                                    d.mixed, self_flat_warps(d.Q / 2), 2, h->stream, 2LL * t);
+              n++;
+            }
+          else {
+            n += launch_rot_phase(h->ctx, h->frames, 0, 2u * t, seed, h->pass, h->cnt, h->stream);
+            n += launch_rot_phase(h->ctx, h->frames, 1, 2u * t + 1, seed, h->pass, h->cnt, h->stream);
+          }
         }
       }
     }
@@ -1527,6 +1546,30 @@ static long long launch_bisection_block(pimc_handle *h, const PassPlan &pl, size
   return d.numb[t];
 }
 
+// the handle's current context for the half-sweep kernel (the recorded
+// graphs hold the device copy's address)
+static pimc_status upload_self_rep(pimc_handle *h)
+{
+  h->self_host.c = h->ctx;
+  h->self_host.frames = h->frames;
+  h->self_host.pass = h->pass;
+  h->self_host.cnt = h->cnt;
+  h->self_host.seed_mix = 0;
+  h->self_host.rotation = h->sys.rotation;
+  CK(cudaMemcpyAsync(h->self_rep, &h->self_host, sizeof(BatchRep), cudaMemcpyHostToDevice, h->stream));
+  return PIMC_OK;
+}
+
+// warps per CTA of the half-sweep kernel over this handle's Q/2 slice pairs:
+// spread over the SMs
+static int self_flat_warps(int units)
+{
+  int warps = units / 152;
+  if (warps < 1) warps = 1;
+  if (warps > 8) warps = 8;
+  return warps;
+}
+
 // several rotors whose slice moves have few rotor-partner terms (at most a
 // warp's worth, R (N - 1) <= 32, e.g. the water dimer): each half-sweep is
 // one launch of the batch's half-sweep kernel over this handle, a warp per
@@ -1546,9 +1589,7 @@ static pimc_status launch_sweeps(pimc_handle *h, const PassPlan &pl, int it0, in
   if (!h->sys.rotation || d.nrotors <= 0 || it1 <= it0) return PIMC_OK;
   if (flat_sweeps(h)) {
     const int units = d.Q / 2, nbk = (int)pl.type.size();
-    int warps = units / 152;                 // spread the slice pairs over the SMs
-    if (warps < 1) warps = 1;
-    if (warps > 8) warps = 8;
+    const int warps = self_flat_warps(units);
     for (int it = it0; it < it1; it++)
       for (int parity = 0; parity < 2; parity++) {
         launch_batch_rot_flat(h->self_rep, h->self_idx, h->self_idx + 1, 1, units, (int)group, it - it0, parity, nbk,
@@ -1624,16 +1665,7 @@ extern "C" pimc_status pimc_run_passes(pimc_handle *h, int npasses, uint64_t see
   if (npasses < 0) return PIMC_ERR_BAD_ARG;
   for (int t = 0; t < d.ntypes; t++)
     if (d.P % (1 << d.levels[t])) return PIMC_ERR_BAD_ARG;
-  if (flat_sweeps(h)) {
-    // the handle's current context for the half-sweep kernel (the graph holds its address)
-    h->self_host.c = h->ctx;
-    h->self_host.frames = h->frames;
-    h->self_host.pass = h->pass;
-    h->self_host.cnt = h->cnt;
-    h->self_host.seed_mix = 0;
-    h->self_host.rotation = h->sys.rotation;
-    CK(cudaMemcpyAsync(h->self_rep, &h->self_host, sizeof(BatchRep), cudaMemcpyHostToDevice, h->stream));
-  }
+  if (flat_sweeps(h) && (e = upload_self_rep(h))) return e;
   if (!h->pass_exec || h->pass_seed != seed) {
     if (h->pass_exec) { CK(cudaGraphExecDestroy(h->pass_exec)); h->pass_exec = nullptr; }
     if (flat_sweeps(h) && !batch_flat_setup(8)) return PIMC_ERR_CUDA;

@@ -101,7 +101,7 @@ void launch_batch_pass(const BatchRep *reps, const int *order, int n, uint64_t s
                        int blk_hi = 1 << 30);
 void launch_batch_rot_flat(const BatchRep *reps, const int *sorted, const int *pre, int nact, int units, int blk,
                            int j, int parity, int nbk, uint64_t seed, int mixed, int warps, int minb,
-                           cudaStream_t s);
+                           cudaStream_t s, long long phase0 = -1);
 int batch_flat_setup(int warps);
 void launch_batch_rot_changed(const BatchRep *reps, int n, cudaStream_t s);
 void launch_batch_est(const BatchRep *reps, int n, double *out, cudaStream_t s);
