@@ -1247,6 +1247,9 @@ extern "C" pimc_status pimc_worm_move(pimc_handle *h, const double *const *strea
 // the worm type's bisection, 4t+2 its centroid move, 4t+3 the other types'
 // translational moves; the rotational draws (their own key domain) phases
 // 2t and 2t+1 for the two half-sweeps at slice t.
+static pimc_status upload_self_rep(pimc_handle *h);
+static int self_flat_warps(int units);
+
 extern "C" pimc_status pimc_worm_run(pimc_handle *h, int npasses, uint64_t seed)
 {
   pimc_status e = ready(h);
