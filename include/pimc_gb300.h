@@ -356,7 +356,11 @@ pimc_status pimc_profile_pass(pimc_handle *h, uint64_t seed, double *ms, long lo
 pimc_status pimc_counters(pimc_handle *h, double *total, double *accep);
 pimc_status pimc_reset_counters(pimc_handle *h);
 pimc_status pimc_synchronize(pimc_handle *h);
-/* 1: table interpolation of the rotor-atom potential in FP32 with FP64 sums */
+/* 1: the FP32 path -- pair terms, table interpolation, rotational frames and
+ * link densities in float from float copies of the beads, frames and tables;
+ * sums, action differences and the Metropolis tests in FP64; the path (and
+ * the double frames, derived from the angles before anything reads them) in
+ * FP64.  0 (default): every operation in FP64 as the reference. */
 pimc_status pimc_set_precision(pimc_handle *h, int mixed);
 /* Production-schedule options (no reference counterpart; the reference has
  * one schedule).  PIMC_OPT_FUSED = 1 (default): one launch per bisection

@@ -1,6 +1,7 @@
-"""The FP32 table path (pimc_set_precision(h, 1)): pair terms in float from
-float copies of beads and tables, sums, action differences, exponentials and
-densities in FP64.  Checked move by move against the FP64 oracle on the
+"""The FP32 table path (pimc_set_precision(h, 1)): pair terms, table
+densities and rattle-and-shake log-densities in float from float copies of
+beads, frames and tables; sums, action differences and the tests in FP64.
+Checked move by move against the FP64 oracle on the
 reference-generated move sequences: action differences and acceptance
 ratios within 1e-5 of the energy terms they are built from, and the same
 accept decisions unless the uniform lies within that tolerance of the
