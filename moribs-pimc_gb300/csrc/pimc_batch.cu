@@ -108,14 +108,13 @@ __device__ int warp_bisect(const Ctx &c, const Frame *frames, int type, int atom
   __syncwarp();
   for (int level = 0; level < L; level++) {
     int seg = 1 << (L - level), half = seg >> 1, nmid = M / seg;
-    double sq = s.bis_sq[type][level], isq = s.bis_isq[type][level];
+    const double isq = s.bis_isq[type][level];
     const double *gz = w.gz + 3 * (nmid - 1);
     for (int j = lane; j < nmid; j += 32) {
       int k0 = j * seg, k1 = k0 + half, k2 = k0 + seg;
       for (int d = 0; d < 3; d++) {
         double v = 0.5 * (w.nb[d][k0] + w.nb[d][k2]);
-        if (MIX) v = fma(gz[3 * j + d], isq, v);
-        else v += gz[3 * j + d] / sq;
+        v = fma(gz[3 * j + d], isq, v);                // as bisect_move: the reciprocal, fused
         w.nb[d][k1] = v;
       }
       if (MIX) w.bf[0][k1] = make_float4((float)w.nb[0][k1], (float)w.nb[1][k1], (float)w.nb[2][k1], 0.0f);

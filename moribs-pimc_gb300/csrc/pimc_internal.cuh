@@ -79,7 +79,7 @@ struct DevSys {
   int numb[2], molecule[2], stat[2], levels[2], first[2];
   double lambda[2], mcstep[2];
   double bis_sq[2][8];         // sqrt(1 / (lambda tau 2^(L-l))): gauss()'s sqrt(alpha) at level l (mc_randg.cc:149)
-  double bis_isq[2][8];        // its inverse (FP32 path)
+  double bis_isq[2][8];        // its inverse (the bisection midpoints, both precisions)
   double tau, rot_tau, beta, temperature, rtstep;
   int ispher, rot_den_type, rot_odevn, rn_ratio;
   double rot_eoff, abc[3];

@@ -343,14 +343,17 @@ __device__ int bisect_move(const Ctx &c, const Frame *frames, int type, int atom
   // the proposed beads, level by level (mc_piqmc.cc:243-254)
   for (int level = 0; level < L; level++) {
     int seg = 1 << (L - level), half = seg >> 1, nmid = M / seg;
-    double sq = s.bis_sq[type][level], isq = s.bis_isq[type][level];
+    const double isq = s.bis_isq[type][level];
     const double *gz = sh.gz + 3 * (nmid - 1);
     for (int j = tid; j < nmid; j += blockDim.x) {
       int k0 = j * seg, k1 = k0 + half, k2 = k0 + seg;
       for (int d = 0; d < 3; d++) {
+        // mid + x / sqrt(alpha) (mc_piqmc.cc:243-254, mc_randg.cc:149) as one
+        // fused multiply-add with the reciprocal: within an ulp of the
+        // reference's division and sum, without an FP64 division chain on the
+        // few lanes that make the midpoints (both precisions)
         double v = 0.5 * (sh.nb[d][k0] + sh.nb[d][k2]);
-        if (MIX) v = fma(gz[3 * j + d], isq, v);       // FP32 path: no division chain
-        else v += gz[3 * j + d] / sq;
+        v = fma(gz[3 * j + d], isq, v);
         sh.nb[d][k1] = v;
       }
       if (MIX) sh.bf[0][k1] = make_float4((float)sh.nb[0][k1], (float)sh.nb[1][k1], (float)sh.nb[2][k1], 0.0f);
