@@ -42,7 +42,7 @@ METRIC = "bead-moves/s on 1 GB300: plain vs surrogate+batched, at matched <E> er
 # DRAM traffic per launch from ncu captures of the bench's own workload, and
 # the FP64 pipe's activity in the same capture:
 # {(kind, mixed): {"bytes": ..., "fp64_pipe": ..., "commit": ...}}, kind 2 = the rotational sweeps
-TRAFFIC_CAPTURE = {(2, False): {"bytes": 6190592 + 60160, "fp64_pipe": 0.5835, "commit": "4c8ef5c"}}
+TRAFFIC_CAPTURE = {(2, False): {"bytes": 6191872 + 62720, "fp64_pipe": 0.5853, "commit": "951d278"}}
 UNIT = "bead-moves/s"
 WORKLOAD = "config1: 1 asymmetric-top SO2 + 64 pH2, T=0.37 K, P=1024, Q=256, L=3, plain method"
 
